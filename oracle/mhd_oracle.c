@@ -1,0 +1,1035 @@
+/*
+ * CPU oracle: plain-C restatement of PLUTO 4.3's unsplit RK + CT ideal-MHD
+ * step.  TEST INFRASTRUCTURE ONLY -- see mhd_oracle.h.
+ *
+ * Each function names the reference routine it restates (file:line, paths
+ * inside the PLUTO source tree).  Expressions keep the reference's operand
+ * order so that, built with -ffp-contract=off, results match the reference
+ * binary bit for bit.
+ */
+#include "mhd_oracle.h"
+
+#include <math.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define NV OC_NVAR
+#define RHO OC_RHO
+#define VX1 OC_VX1
+#define VX2 OC_VX2
+#define VX3 OC_VX3
+#define BX1 OC_BX1
+#define BX2 OC_BX2
+#define BX3 OC_BX3
+#define PRS OC_PRS
+#define ENG OC_PRS
+#define MX1 OC_VX1
+
+/* Src/macros.h:140-151 */
+#define MAX(a, b) ((a) >= (b) ? (a) : (b))
+#define MIN(a, b) ((a) <= (b) ? (a) : (b))
+#define ABS_MIN(a, b) (fabs(a) < fabs(b) ? (a) : (b))
+#define MINMOD(a, b) ((a) * (b) > 0.0 ? (fabs(a) < fabs(b) ? (a) : (b)) : 0.0)
+
+#define SMALL_DENSITY 1.e-12  /* Src/globals.h:113 */
+#define SMALL_PRESSURE 1.e-12 /* Src/globals.h:114 */
+#define FLAG_CONS2PRIM_FAIL 64 /* Src/pluto.h:200 */
+
+struct oc_problem {
+  oc_config c;
+  int ng, nt[3], beg[3], end[3];
+  size_t ncell, nface[3];
+  double inv_dx[3];
+  double *vc[NV], *uc[NV], *u0[NV];
+  double *bs[3], *bs0[3];
+  double *sl[3], *sr[3];   /* max(0,-SL), max(0,SR) per interface, emf->S?L/R */
+  double *dv[3][3];        /* dv[d][c]: slope of velocity c along d, emf->dv?_d? */
+  double *ex, *ey, *ez;    /* edge EMFs */
+  double *cdt;             /* C_dt, update_stage.c:81 */
+  unsigned char *flag;
+  int64_t nfail;
+  double max_mach;
+};
+
+/* ------------------------------------------------------------------ */
+/* indexing                                                             */
+/* ------------------------------------------------------------------ */
+static inline size_t CI(const oc_problem *p, int k, int j, int i) {
+  return ((size_t)k * p->nt[1] + j) * p->nt[0] + i;
+}
+/* face array d, reference index with -1 origin along d
+   (Src/initialize.c:448-453) */
+static inline size_t FI(const oc_problem *p, int d, int k, int j, int i) {
+  int sx = p->nt[0] + (d == 0), sy = p->nt[1] + (d == 1);
+  return ((size_t)(k + (d == 2)) * sy + (j + (d == 1))) * sx + (i + (d == 0));
+}
+
+/* ------------------------------------------------------------------ */
+/* Physics kernels on one point                                        */
+/* ------------------------------------------------------------------ */
+
+/* Src/MHD/mappers.c:25-86 (IDEAL EOS) */
+static void prim_to_cons(const double *v, double *u, double gmm1) {
+  double kinb2;
+  u[RHO] = v[RHO];
+  u[MX1] = v[RHO] * v[VX1];
+  u[MX1 + 1] = v[RHO] * v[VX2];
+  u[MX1 + 2] = v[RHO] * v[VX3];
+  u[BX1] = v[BX1];
+  u[BX2] = v[BX2];
+  u[BX3] = v[BX3];
+  kinb2 = v[VX1] * v[VX1] + v[VX2] * v[VX2] + v[VX3] * v[VX3];
+  kinb2 = v[RHO] * kinb2 + v[BX1] * v[BX1] + v[BX2] * v[BX2] + v[BX3] * v[BX3];
+  kinb2 *= 0.5;
+  u[ENG] = kinb2 + v[PRS] / gmm1;
+}
+
+/* Src/MHD/mappers.c:88-254 (IDEAL EOS, no entropy switch).  The floors
+   modify u in place exactly as the reference does. */
+static int cons_to_prim(double *u, double *v, double gmm1, unsigned char *flag) {
+  double tau, rho, kinb2, m2, b2;
+  int ifail = 0;
+  m2 = u[MX1] * u[MX1] + u[MX1 + 1] * u[MX1 + 1] + u[MX1 + 2] * u[MX1 + 2];
+  b2 = u[BX1] * u[BX1] + u[BX2] * u[BX2] + u[BX3] * u[BX3];
+  if (u[RHO] < 0.0) {
+    u[RHO] = SMALL_DENSITY;
+    *flag |= FLAG_CONS2PRIM_FAIL;
+    ifail = 1;
+  }
+  v[RHO] = rho = u[RHO];
+  tau = 1.0 / u[RHO];
+  v[VX1] = u[MX1] * tau;
+  v[VX2] = u[MX1 + 1] * tau;
+  v[VX3] = u[MX1 + 2] * tau;
+  v[BX1] = u[BX1];
+  v[BX2] = u[BX2];
+  v[BX3] = u[BX3];
+  kinb2 = 0.5 * (m2 * tau + b2);
+  if (u[ENG] < 0.0) {
+    u[ENG] = SMALL_PRESSURE / gmm1 + kinb2;
+    *flag |= FLAG_CONS2PRIM_FAIL;
+    ifail = 1;
+  }
+  v[PRS] = gmm1 * (u[ENG] - kinb2);
+  if (v[PRS] < 0.0) {
+    v[PRS] = SMALL_PRESSURE;
+    u[ENG] = v[PRS] / gmm1 + kinb2;
+    *flag |= FLAG_CONS2PRIM_FAIL;
+    ifail = 1;
+  }
+  (void)rho;
+  return ifail;
+}
+
+/* Normal / tangent / bitangent rotation, Src/set_indexes.c:49-124 */
+typedef struct { int vn, vt, vb, bn, bt, bb; } Rot;
+static Rot rot_for(int dir) {
+  Rot r;
+  if (dir == 0) { r.vn = VX1; r.vt = VX2; r.vb = VX3; }
+  else if (dir == 1) { r.vn = VX2; r.vt = VX1; r.vb = VX3; }
+  else { r.vn = VX3; r.vt = VX1; r.vb = VX2; }
+  r.bn = r.vn + 3; r.bt = r.vt + 3; r.bb = r.vb + 3;
+  return r;
+}
+
+/* Src/MHD/fluxes.c:110-249 (ideal MHD, no background field) */
+static void flux(const double *v, const double *u, double *fx, double *ptot_out,
+                 const Rot *r) {
+  double Bmag2, ptot, vB;
+  Bmag2 = v[BX1] * v[BX1] + v[BX2] * v[BX2] + v[BX3] * v[BX3];
+  ptot = v[PRS] + 0.5 * Bmag2;
+  vB = v[VX1] * v[BX1] + v[VX2] * v[BX2] + v[VX3] * v[BX3];
+  fx[RHO] = u[r->vn];
+  fx[MX1] = v[r->vn] * u[MX1] - v[r->bn] * v[BX1];
+  fx[MX1 + 1] = v[r->vn] * u[MX1 + 1] - v[r->bn] * v[BX2];
+  fx[MX1 + 2] = v[r->vn] * u[MX1 + 2] - v[r->bn] * v[BX3];
+  fx[r->bn] = 0.0;
+  fx[r->bt] = v[r->vn] * v[r->bt] - v[r->bn] * v[r->vt];
+  fx[r->bb] = v[r->vn] * v[r->bb] - v[r->bn] * v[r->vb];
+  fx[ENG] = (u[ENG] + ptot) * v[r->vn] - v[r->bn] * vB;
+  *ptot_out = ptot;
+}
+
+/* Src/MHD/eigenv.c:35-104 (IDEAL EOS) */
+static void max_signal_speed(const double *v, double gamma, const Rot *r,
+                             double *cmin, double *cmax) {
+  double gpr, b1, b2, b3, Btmag2, Bmag2, cf;
+  gpr = gamma * v[PRS];
+  b1 = v[r->bn];
+  b2 = v[r->bt];
+  b3 = v[r->bb];
+  Btmag2 = b2 * b2 + b3 * b3;
+  Bmag2 = b1 * b1 + Btmag2;
+  cf = gpr - Bmag2;
+  cf = gpr + Bmag2 + sqrt(cf * cf + 4.0 * gpr * Btmag2);
+  cf = sqrt(0.5 * cf / v[RHO]);
+  *cmin = v[r->vn] - cf;
+  *cmax = v[r->vn] + cf;
+}
+
+/* Riemann interface record */
+typedef struct { double f[NV], press, SL, SR, cmax; } Iface;
+
+/* Src/MHD/hll_speed.c:23-108 (DAVIS_ESTIMATE) + Src/EOS/Ideal/eos.c:16-42 */
+static double hll_speed(const double *vL, const double *vR, double gamma,
+                        const Rot *r, double *SL, double *SR) {
+  double slmin, slmax, srmin, srmax, a2L, a2R, scrh;
+  max_signal_speed(vL, gamma, r, &slmin, &slmax);
+  max_signal_speed(vR, gamma, r, &srmin, &srmax);
+  *SL = MIN(slmin, srmin);
+  *SR = MAX(slmax, srmax);
+  a2L = gamma * vL[PRS] / vL[RHO];
+  a2R = gamma * vR[PRS] / vR[RHO];
+  scrh = fabs(vL[r->vn]) + fabs(vR[r->vn]);
+  scrh /= sqrt(a2L) + sqrt(a2R);
+  return scrh;
+}
+
+/* Src/MHD/hll.c:30-166 */
+static void hll_solver(const double *vL, const double *uL, const double *vR,
+                       const double *uR, double gamma, const Rot *r, Iface *o,
+                       double *mach) {
+  double fL[NV], fR[NV], ptL, ptR, SL, SR, scrh;
+  int nv;
+  flux(vL, uL, fL, &ptL, r);
+  flux(vR, uR, fR, &ptR, r);
+  *mach = hll_speed(vL, vR, gamma, r, &SL, &SR);
+  o->SL = SL;
+  o->SR = SR;
+  scrh = MAX(fabs(SL), fabs(SR));
+  o->cmax = scrh;
+  if (SL > 0.0) {
+    for (nv = 0; nv < NV; nv++) o->f[nv] = fL[nv];
+    o->press = ptL;
+  } else if (SR < 0.0) {
+    for (nv = 0; nv < NV; nv++) o->f[nv] = fR[nv];
+    o->press = ptR;
+  } else {
+    scrh = 1.0 / (SR - SL);
+    for (nv = 0; nv < NV; nv++) {
+      o->f[nv] = SL * SR * (uR[nv] - uL[nv]) + SR * fL[nv] - SL * fR[nv];
+      o->f[nv] *= scrh;
+    }
+    o->press = (SR * ptL - SL * ptR) * scrh;
+  }
+}
+
+/* Src/MHD/hlld.c:44-452 (IDEAL EOS, no background field) */
+static void hlld_solver(const double *vL, const double *uL, const double *vR,
+                        const double *uR, double gamma, const Rot *r, Iface *o,
+                        double *mach) {
+  const int MXn = r->vn, MXt = r->vt, MXb = r->vb;
+  const int VXn = r->vn, VXt = r->vt, VXb = r->vb;
+  const int BXn = r->bn, BXt = r->bt, BXb = r->bb;
+  double fL[NV], fR[NV], ptL, ptR, SL, SR, scrh, Uhll[NV];
+  double usL[NV], ussl[NV], usR[NV], ussr[NV];
+  double vsL, wsL, scrhL, S1L, sqrL, duL;
+  double vsR, wsR, scrhR, S1R, sqrR, duR;
+  double Bx, Bx1, SM, sBx, pts, vss, wss;
+  int nv, revert_to_hllc;
+
+  flux(vL, uL, fL, &ptL, r);
+  flux(vR, uR, fR, &ptR, r);
+  *mach = hll_speed(vL, vR, gamma, r, &SL, &SR);
+  o->SL = SL;
+  o->SR = SR;
+  scrh = MAX(fabs(SL), fabs(SR));
+  o->cmax = scrh;
+
+  if (SL >= 0.0) {
+    for (nv = NV; nv--;) o->f[nv] = fL[nv];
+    o->press = ptL;
+  } else if (SR <= 0.0) {
+    for (nv = NV; nv--;) o->f[nv] = fR[nv];
+    o->press = ptR;
+  } else {
+    scrh = 1.0 / (SR - SL);
+    Bx1 = Bx = (SR * vR[BXn] - SL * vL[BXn]) * scrh;
+    sBx = (Bx > 0.0 ? 1.0 : -1.0);
+    duL = SL - vL[VXn];
+    duR = SR - vR[VXn];
+    scrh = 1.0 / (duR * uR[RHO] - duL * uL[RHO]);
+    SM = (duR * uR[MXn] - duL * uL[MXn] - ptR + ptL) * scrh;
+    pts = duR * uR[RHO] * ptL - duL * uL[RHO] * ptR +
+          vL[RHO] * vR[RHO] * duR * duL * (vR[VXn] - vL[VXn]);
+    pts *= scrh;
+    usL[RHO] = uL[RHO] * duL / (SL - SM);
+    usR[RHO] = uR[RHO] * duR / (SR - SM);
+    sqrL = sqrt(usL[RHO]);
+    sqrR = sqrt(usR[RHO]);
+    S1L = SM - fabs(Bx) / sqrL;
+    S1R = SM + fabs(Bx) / sqrR;
+
+    revert_to_hllc = 0;
+    if ((S1L - SL) < 1.e-4 * (SM - SL)) revert_to_hllc = 1;
+    if ((S1R - SR) > -1.e-4 * (SR - SM)) revert_to_hllc = 1;
+
+    if (revert_to_hllc) {
+      scrh = 1.0 / (SR - SL);
+      for (nv = NV; nv--;) {
+        Uhll[nv] = SR * uR[nv] - SL * uL[nv] + fL[nv] - fR[nv];
+        Uhll[nv] *= scrh;
+      }
+      usL[BXn] = usR[BXn] = Uhll[BXn];
+      usL[BXt] = usR[BXt] = Uhll[BXt];
+      usL[BXb] = usR[BXb] = Uhll[BXb];
+      S1L = S1R = SM;
+    } else {
+      scrhL = (uL[RHO] * duL * duL - Bx * Bx) / (uL[RHO] * duL * (SL - SM) - Bx * Bx);
+      scrhR = (uR[RHO] * duR * duR - Bx * Bx) / (uR[RHO] * duR * (SR - SM) - Bx * Bx);
+      usL[BXn] = Bx1;
+      usL[BXt] = uL[BXt] * scrhL;
+      usL[BXb] = uL[BXb] * scrhL;
+      usR[BXn] = Bx1;
+      usR[BXt] = uR[BXt] * scrhR;
+      usR[BXb] = uR[BXb] * scrhR;
+    }
+
+    scrhL = Bx / (uL[RHO] * duL);
+    scrhR = Bx / (uR[RHO] * duR);
+    vsL = vL[VXt] - scrhL * (usL[BXt] - uL[BXt]);
+    vsR = vR[VXt] - scrhR * (usR[BXt] - uR[BXt]);
+    wsL = vL[VXb] - scrhL * (usL[BXb] - uL[BXb]);
+    wsR = vR[VXb] - scrhR * (usR[BXb] - uR[BXb]);
+
+    usL[MXn] = usL[RHO] * SM;
+    usR[MXn] = usR[RHO] * SM;
+    usL[MXt] = usL[RHO] * vsL;
+    usR[MXt] = usR[RHO] * vsR;
+    usL[MXb] = usL[RHO] * wsL;
+    usR[MXb] = usR[RHO] * wsR;
+
+    scrhL = vL[VXn] * Bx1 + vL[VXt] * uL[BXt] + vL[VXb] * uL[BXb];
+    scrhL -= SM * Bx1 + vsL * usL[BXt] + wsL * usL[BXb];
+    usL[ENG] = duL * uL[ENG] - ptL * vL[VXn] + pts * SM + Bx * scrhL;
+    usL[ENG] /= SL - SM;
+
+    scrhR = vR[VXn] * Bx1 + vR[VXt] * uR[BXt] + vR[VXb] * uR[BXb];
+    scrhR -= SM * Bx1 + vsR * usR[BXt] + wsR * usR[BXb];
+    usR[ENG] = duR * uR[ENG] - ptR * vR[VXn] + pts * SM + Bx * scrhR;
+    usR[ENG] /= SR - SM;
+
+    if (S1L >= 0.0) {
+      for (nv = NV; nv--;) o->f[nv] = fL[nv] + SL * (usL[nv] - uL[nv]);
+      o->press = ptL;
+    } else if (S1R <= 0.0) {
+      for (nv = NV; nv--;) o->f[nv] = fR[nv] + SR * (usR[nv] - uR[nv]);
+      o->press = ptR;
+    } else {
+      ussl[RHO] = usL[RHO];
+      ussr[RHO] = usR[RHO];
+      vss = sqrL * vsL + sqrR * vsR + (usR[BXt] - usL[BXt]) * sBx;
+      vss /= sqrL + sqrR;
+      wss = sqrL * wsL + sqrR * wsR + (usR[BXb] - usL[BXb]) * sBx;
+      wss /= sqrL + sqrR;
+      ussl[MXn] = ussl[RHO] * SM;
+      ussr[MXn] = ussr[RHO] * SM;
+      ussl[MXt] = ussl[RHO] * vss;
+      ussr[MXt] = ussr[RHO] * vss;
+      ussl[MXb] = ussl[RHO] * wss;
+      ussr[MXb] = ussr[RHO] * wss;
+      ussl[BXn] = ussr[BXn] = Bx1;
+      ussl[BXt] = sqrL * usR[BXt] + sqrR * usL[BXt] + sqrL * sqrR * (vsR - vsL) * sBx;
+      ussl[BXt] /= sqrL + sqrR;
+      ussr[BXt] = ussl[BXt];
+      ussl[BXb] = sqrL * usR[BXb] + sqrR * usL[BXb] + sqrL * sqrR * (wsR - wsL) * sBx;
+      ussl[BXb] /= sqrL + sqrR;
+      ussr[BXb] = ussl[BXb];
+
+      scrhL = SM * Bx1 + vsL * usL[BXt] + wsL * usL[BXb];
+      scrhL -= SM * Bx1 + vss * ussl[BXt] + wss * ussl[BXb];
+      scrhR = SM * Bx1 + vsR * usR[BXt] + wsR * usR[BXb];
+      scrhR -= SM * Bx1 + vss * ussr[BXt] + wss * ussr[BXb];
+      ussl[ENG] = usL[ENG] - sqrL * scrhL * sBx;
+      ussr[ENG] = usR[ENG] + sqrR * scrhR * sBx;
+
+      if (SM >= 0.0) {
+        for (nv = NV; nv--;)
+          o->f[nv] = fL[nv] + S1L * (ussl[nv] - usL[nv]) + SL * (usL[nv] - uL[nv]);
+        o->press = ptL;
+      } else {
+        for (nv = NV; nv--;)
+          o->f[nv] = fR[nv] + S1R * (ussr[nv] - usR[nv]) + SR * (usR[nv] - uR[nv]);
+        o->press = ptR;
+      }
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Reconstruction                                                       */
+/* ------------------------------------------------------------------ */
+
+/* Src/States/plm_coeffs.h:72-175 (uniform Cartesian forms) */
+static inline double limit(int lim, int nv, double dvp, double dvm) {
+  double dv;
+  if (lim == OC_DEFAULT_LIM) { /* plm_states.c:180-213 */
+    if (nv == RHO) lim = OC_MC_LIM;
+    else if (nv == PRS) lim = OC_MINMOD_LIM;
+    else lim = OC_VANLEER_LIM;
+  }
+  switch (lim) {
+    case OC_FLAT_LIM: dv = 0.0; break;
+    case OC_MINMOD_LIM: dv = (dvp * dvm > 0.0 ? ABS_MIN(dvp, dvm) : 0.0); break;
+    case OC_VANLEER_LIM: dv = (dvp * dvm > 0.0 ? 2.0 * dvp * dvm / (dvp + dvm) : 0.0); break;
+    default:
+      if (dvp * dvm > 0.0) {
+        double qc = 0.5 * (dvm + dvp), scrh = 2.0 * ABS_MIN(dvp, dvm);
+        dv = ABS_MIN(qc, scrh);
+      } else dv = 0.0;
+  }
+  return dv;
+}
+
+/* Src/States/plm_states.c:80-312: PLM on primitive variables for cells
+   beg..end of a pencil; vp/vm indexed by cell. */
+static void plm_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV],
+                       int beg, int end, int lim) {
+  int i, nv;
+  for (i = beg; i <= end; i++) {
+    for (nv = 0; nv < NV; nv++) {
+      double dvp = v[i + 1][nv] - v[i][nv];
+      double dvm = v[i][nv] - v[i - 1][nv];
+      double dv = limit(lim, nv, dvp, dvm);
+      vp[i][nv] = v[i][nv] + dv * 0.5;
+      vm[i][nv] = v[i][nv] - dv * 0.5;
+    }
+  }
+}
+
+/* Src/States/ppm_states.c:68-253 with PPM_ORDER 4, Cartesian uniform
+   coefficients (ppm_coeffs.c:478-520, Q6 hp = hm = 3 at :528-556). */
+static void ppm_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV],
+                       int beg, int end) {
+  const double w_1 = -1.0 / 12.0, w0 = 7.0 / 12.0, w1 = 7.0 / 12.0, w2 = -1.0 / 12.0;
+  const double hp = 3.0, hm = 3.0;
+  int i, nv;
+  for (i = beg - 1; i <= end; i++) {
+    for (nv = 0; nv < NV; nv++) {
+      double dv, dvp;
+      vp[i][nv] = w_1 * v[i - 1][nv] + w0 * v[i][nv] + w1 * v[i + 1][nv] + w2 * v[i + 2][nv];
+      dv = v[i + 1][nv] - v[i][nv];
+      dvp = vp[i][nv] - v[i][nv];
+      vp[i][nv] = v[i][nv] + MINMOD(dvp, dv);
+    }
+  }
+  for (i = beg; i <= end; i++)
+    for (nv = 0; nv < NV; nv++) vm[i][nv] = vp[i - 1][nv];
+  for (i = beg; i <= end; i++) {
+    double cm = (hm + 1.0) / (hp - 1.0);
+    double cp = (hp + 1.0) / (hm - 1.0);
+    for (nv = 0; nv < NV; nv++) {
+      double dvp = vp[i][nv] - v[i][nv];
+      double dvm = vm[i][nv] - v[i][nv];
+      if (dvp * dvm >= 0.0) dvp = dvm = 0.0;
+      else {
+        if (fabs(dvp) >= cm * fabs(dvm)) dvp = -cm * dvm;
+        else if (fabs(dvm) >= cp * fabs(dvp)) dvm = -cp * dvp;
+      }
+      vp[i][nv] = v[i][nv] + dvp;
+      vm[i][nv] = v[i][nv] + dvm;
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* Boundary conditions, Src/boundary.c:41-303, 439-522                 */
+/* ------------------------------------------------------------------ */
+
+static void bound_box(oc_problem *p, double *q, int face_dir, int ib, int ie,
+                      int jb, int je, int kb, int ke, int side, int type) {
+  /* q is a cell array (face_dir < 0) or face array face_dir.  Loops run
+     over the box in increasing order; the copies read interior or
+     already-assigned points only. */
+  int i, j, k;
+  int lo_i = ib < ie ? ib : ie, hi_i = ib < ie ? ie : ib;
+  int lo_j = jb < je ? jb : je, hi_j = jb < je ? je : jb;
+  int lo_k = kb < ke ? kb : ke, hi_k = kb < ke ? ke : kb;
+  int NX1 = p->c.nx[0], NX2 = p->c.nx[1], NX3 = p->c.nx[2];
+#define IDX(kk, jj, ii) (face_dir < 0 ? CI(p, kk, jj, ii) : FI(p, face_dir, kk, jj, ii))
+  /* BOX_LOOP direction follows the box's own ordering (Src/macros.h:91). */
+  int di = ib <= ie ? 1 : -1, dj = jb <= je ? 1 : -1, dk = kb <= ke ? 1 : -1;
+  (void)lo_i; (void)hi_i; (void)lo_j; (void)hi_j; (void)lo_k; (void)hi_k;
+  for (k = kb; dk * k <= dk * ke; k += dk)
+    for (j = jb; dj * j <= dj * je; j += dj)
+      for (i = ib; di * i <= di * ie; i += di) {
+        size_t dst = IDX(k, j, i), src;
+        if (type == OC_PERIODIC) {
+          if (side == 0) src = IDX(k, j, i + NX1);
+          else if (side == 1) src = IDX(k, j, i - NX1);
+          else if (side == 2) src = IDX(k, j + NX2, i);
+          else if (side == 3) src = IDX(k, j - NX2, i);
+          else if (side == 4) src = IDX(k + NX3, j, i);
+          else src = IDX(k - NX3, j, i);
+        } else {
+          if (side == 0) src = IDX(k, j, p->beg[0]);
+          else if (side == 1) src = IDX(k, j, p->end[0]);
+          else if (side == 2) src = IDX(k, p->beg[1], i);
+          else if (side == 3) src = IDX(k, p->end[1], i);
+          else if (side == 4) src = IDX(p->beg[2], j, i);
+          else src = IDX(p->end[2], j, i);
+        }
+        q[dst] = q[src];
+      }
+#undef IDX
+}
+
+static void boundary(oc_problem *p) {
+  int is, nv;
+  int dims = p->c.dims;
+  for (is = 0; is < 2 * dims; is++) {
+    int d = is / 2, type = p->c.bc[d];
+    int ib = 0, ie = p->nt[0] - 1, jb = 0, je = p->nt[1] - 1, kb = 0, ke = p->nt[2] - 1;
+    if (is == 0) { ib = p->beg[0] - 1; ie = 0; }
+    else if (is == 1) { ib = p->end[0] + 1; ie = p->nt[0] - 1; }
+    else if (is == 2) { jb = p->beg[1] - 1; je = 0; }
+    else if (is == 3) { jb = p->end[1] + 1; je = p->nt[1] - 1; }
+    else if (is == 4) { kb = p->beg[2] - 1; ke = 0; }
+    else { kb = p->end[2] + 1; ke = p->nt[2] - 1; }
+    for (nv = 0; nv < NV; nv++) bound_box(p, p->vc[nv], -1, ib, ie, jb, je, kb, ke, is, type);
+    if (p->c.ct) {
+      int fd;
+      for (fd = 0; fd < dims; fd++) {
+        int fib = ib, fie = ie, fjb = jb, fje = je, fkb = kb, fke = ke;
+        /* face boxes, Src/boundary.c:141-149 */
+        if (fd == 0) { if (ib < ie) fib = ib - 1; else fie = ie - 1; }
+        if (fd == 1) { if (jb < je) fjb = jb - 1; else fje = je - 1; }
+        if (fd == 2) { if (kb < ke) fkb = kb - 1; else fke = ke - 1; }
+        if (type == OC_PERIODIC) {
+          bound_box(p, p->bs[fd], fd, fib, fie, fjb, fje, fkb, fke, is, type);
+        } else if (fd != d) {
+          bound_box(p, p->bs[fd], fd, fib, fie, fjb, fje, fkb, fke, is, type);
+        }
+        /* outflow normal-field recovery (FillMagneticField) is not part of
+           the configurations covered here; see oc_create's check. */
+      }
+    }
+  }
+}
+
+/* ------------------------------------------------------------------ */
+/* One directional sweep of UpdateStage, Src/Time_Stepping/update_stage.c  */
+/* ------------------------------------------------------------------ */
+
+typedef struct {
+  double (*v)[NV], (*vp)[NV], (*vm)[NV], (*up)[NV], (*um)[NV], (*rhs)[NV];
+  double *bn;
+  Iface *ifc;
+} Pencil;
+
+static void pencil_alloc(Pencil *w, int n) {
+  w->v = malloc(sizeof(double[NV]) * n);
+  w->vp = malloc(sizeof(double[NV]) * n);
+  w->vm = malloc(sizeof(double[NV]) * n);
+  w->up = malloc(sizeof(double[NV]) * n);
+  w->um = malloc(sizeof(double[NV]) * n);
+  w->rhs = malloc(sizeof(double[NV]) * n);
+  w->bn = malloc(sizeof(double) * n);
+  w->ifc = malloc(sizeof(Iface) * n);
+}
+static void pencil_free(Pencil *w) {
+  free(w->v); free(w->vp); free(w->vm); free(w->up); free(w->um);
+  free(w->rhs); free(w->bn); free(w->ifc);
+}
+
+static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1d,
+                  double *mach_out) {
+  const int dims = p->c.dims;
+  const int td = dir == 0 ? 1 : 0, bd = dir == 2 ? 1 : 2; /* rbox.c:52-80 */
+  const Rot r = rot_for(dir);
+  int nbeg = p->beg[dir], nend = p->end[dir];
+  int tbeg = p->beg[td], tend = p->end[td], bbeg = p->beg[bd], bend = p->end[bd];
+  int ntot = p->nt[dir];
+  const double gmm1 = p->c.gamma - 1.0;
+  const double inv_dl = p->inv_dx[dir];
+  const double dxd = p->c.dx[dir];
+  double mach_max = 0.0, invdt1 = 0.0;
+  long npencil, ip;
+  int tn;
+
+  if (p->c.ct) { /* update_stage.c:144-148 */
+    if (dims >= 2) { tbeg--; tend++; }
+    if (dims == 3) { bbeg--; bend++; }
+  }
+  tn = tend - tbeg + 1;
+  npencil = (long)tn * (bend - bbeg + 1);
+
+#pragma omp parallel reduction(max : mach_max, invdt1)
+  {
+    Pencil w;
+    pencil_alloc(&w, ntot + 2);
+#pragma omp for schedule(static)
+    for (ip = 0; ip < npencil; ip++) {
+      int t = tbeg + (int)(ip % tn), b = bbeg + (int)(ip / tn);
+      int i, nv, ijk[3];
+      ijk[td] = t;
+      ijk[bd] = b;
+      /* gather, update_stage.c:158-164 */
+      for (i = 0; i < ntot; i++) {
+        size_t c;
+        ijk[dir] = i;
+        c = CI(p, ijk[2], ijk[1], ijk[0]);
+        for (nv = 0; nv < NV; nv++) w.v[i][nv] = p->vc[nv][c];
+        if (p->c.ct) w.bn[i] = p->bs[dir][FI(p, dir, ijk[2], ijk[1], ijk[0])];
+      }
+      /* States, update_stage.c:193 with beg = nbeg-1, end = nend+1 */
+      {
+        int beg = nbeg - 1, end = nend + 1;
+        if (p->c.recon == OC_LINEAR) plm_states(w.v, w.vp, w.vm, beg, end, p->c.limiter);
+        else ppm_states(w.v, w.vp, w.vm, beg, end);
+        if (p->c.ct) { /* plm_states.c:271-275 */
+          for (i = beg - 1; i <= end; i++) {
+            w.vp[i][r.bn] = w.bn[i];
+            w.vm[i + 1][r.bn] = w.bn[i];
+          }
+        }
+        for (i = beg; i <= end; i++) {
+          prim_to_cons(w.vp[i], w.up[i], gmm1);
+          prim_to_cons(w.vm[i], w.um[i], gmm1);
+        }
+      }
+      /* Riemann, update_stage.c:194 on interfaces nbeg-1..nend; interface
+         i lies between cell i (vp) and cell i+1 (vm). */
+      for (i = nbeg - 1; i <= nend; i++) {
+        double m;
+        if (p->c.solver == OC_HLL)
+          hll_solver(w.vp[i], w.up[i], w.vm[i + 1], w.um[i + 1], p->c.gamma, &r, &w.ifc[i], &m);
+        else
+          hlld_solver(w.vp[i], w.up[i], w.vm[i + 1], w.um[i + 1], p->c.gamma, &r, &w.ifc[i], &m);
+        mach_max = MAX(m, mach_max);
+      }
+      /* CT_StoreUpwindEMF, ct_emf.c:104-207 (UCT_HLL) + CT_StoreVelSlopes */
+      if (p->c.ct) {
+        for (i = nbeg - 1; i <= nend; i++) {
+          size_t c;
+          ijk[dir] = i;
+          c = CI(p, ijk[2], ijk[1], ijk[0]);
+          p->sl[dir][c] = MAX(0.0, -w.ifc[i].SL);
+          p->sr[dir][c] = MAX(0.0, w.ifc[i].SR);
+        }
+        for (i = nbeg - 1; i <= nend + 1; i++) {
+          size_t c;
+          int comp;
+          ijk[dir] = i;
+          c = CI(p, ijk[2], ijk[1], ijk[0]);
+          for (comp = 0; comp < dims; comp++)
+            p->dv[dir][comp][c] = w.vp[i][VX1 + comp] - w.vm[i][VX1 + comp];
+        }
+      }
+      /* RightHandSide (Src/MHD/rhs.c:193-201, Cartesian, USE_PRS_GRADIENT) */
+      for (i = nbeg; i <= nend; i++) {
+        double scrh = dt / dxd;
+        for (nv = 0; nv < NV; nv++)
+          w.rhs[i][nv] = -scrh * (w.ifc[i].f[nv] - w.ifc[i - 1].f[nv]);
+        w.rhs[i][r.vn] -= scrh * (w.ifc[i].press - w.ifc[i - 1].press);
+      }
+      /* U += rhs, update_stage.c:214-216; dt bookkeeping :229-241 */
+      for (i = nbeg; i <= nend; i++) {
+        size_t c;
+        ijk[dir] = i;
+        c = CI(p, ijk[2], ijk[1], ijk[0]);
+        for (nv = 0; nv < NV; nv++) p->uc[nv][c] += w.rhs[i][nv];
+        if (dims > 1 && stage == 1)
+          p->cdt[c] += 0.5 * (w.ifc[i - 1].cmax + w.ifc[i].cmax) * inv_dl;
+      }
+      if (dims == 1)
+        for (i = nbeg - 1; i <= nend; i++) invdt1 = MAX(invdt1, w.ifc[i].cmax * inv_dl);
+    }
+    pencil_free(&w);
+  }
+  if (*mach_out < mach_max) *mach_out = mach_max;
+  *inv_dt_1d = MAX(*inv_dt_1d, invdt1);
+}
+
+/* ------------------------------------------------------------------ */
+/* Constrained transport                                                */
+/* ------------------------------------------------------------------ */
+
+/* Src/MHD/CT/ct_stag_slopes.c:92-105 */
+static double mc_lim2(double dp, double dm) {
+  double dc, scrh;
+  if (dp * dm < 0.0) return 0.0;
+  dc = 0.5 * (dp + dm);
+  scrh = 2.0 * (fabs(dp) < fabs(dm) ? dp : dm);
+  return (fabs(dc) < fabs(scrh) ? dc : scrh);
+}
+
+/* Staggered slope of face field fd along direction a at reference index
+   (k,j,i): CT_GetStagSlopes, ct_stag_slopes.c:51-89. */
+static double bslope(const oc_problem *p, int fd, int a, int k, int j, int i) {
+  int o[3] = {0, 0, 0};
+  double b0, bp, bm;
+  o[a] = 1;
+  b0 = p->bs[fd][FI(p, fd, k, j, i)];
+  bp = p->bs[fd][FI(p, fd, k + o[2], j + o[1], i + o[0])];
+  bm = p->bs[fd][FI(p, fd, k - o[2], j - o[1], i - o[0])];
+  return mc_lim2(bp - b0, b0 - bm);
+}
+
+/* Edge EMF along axis e from the 2D HLL solver of Londrillo & Del Zanna:
+   CT_EMF_HLL_Solver, Src/MHD/CT/ct_emf_average.c:179-352.  (x,y) is the
+   ordered pair of in-plane axes: e = z -> (x,y); e = x -> (y,z);
+   e = y -> (z,x). */
+static double uct_hll_edge(const oc_problem *p, int e, int k, int j, int i) {
+  const int ax = e == 2 ? 0 : (e == 0 ? 1 : 2);
+  const int ay = e == 2 ? 1 : (e == 0 ? 2 : 0);
+  int c[3] = {i, j, k}, cx[3], cy[3], cxy[3];
+  double a_xp, a_xm, a_yp, a_ym, bS, bN, bW, bE, eSW, eSE, eNE, eNW, ez;
+  double *vxa = p->vc[VX1 + ax], *vya = p->vc[VX1 + ay];
+  size_t c00, cx0, c0y, cxy_;
+  memcpy(cx, c, sizeof c); cx[ax]++;
+  memcpy(cy, c, sizeof c); cy[ay]++;
+  memcpy(cxy, c, sizeof c); cxy[ax]++; cxy[ay]++;
+  c00 = CI(p, c[2], c[1], c[0]);
+  cx0 = CI(p, cx[2], cx[1], cx[0]);
+  c0y = CI(p, cy[2], cy[1], cy[0]);
+  cxy_ = CI(p, cxy[2], cxy[1], cxy[0]);
+
+  /* Speeds on faces normal to x (stored at cells c and c+y) and to y. */
+  a_xp = MAX(p->sr[ax][c00], p->sr[ax][c0y]);
+  a_xm = MAX(p->sl[ax][c00], p->sl[ax][c0y]);
+  a_yp = MAX(p->sr[ay][c00], p->sr[ay][cx0]);
+  a_ym = MAX(p->sl[ay][c00], p->sl[ay][cx0]);
+
+  /* bS, bN: x-face field dP/dM along y; bW, bE: y-face field along x */
+  bS = p->bs[ax][FI(p, ax, c[2], c[1], c[0])] + 0.5 * bslope(p, ax, ay, c[2], c[1], c[0]);
+  bW = p->bs[ay][FI(p, ay, c[2], c[1], c[0])] + 0.5 * bslope(p, ay, ax, c[2], c[1], c[0]);
+  bN = p->bs[ax][FI(p, ax, cy[2], cy[1], cy[0])] - 0.5 * bslope(p, ax, ay, cy[2], cy[1], cy[0]);
+  bE = p->bs[ay][FI(p, ay, cx[2], cx[1], cx[0])] - 0.5 * bslope(p, ay, ax, cx[2], cx[1], cx[0]);
+
+#define DV(comp, dir, cc) (p->dv[dir][comp][cc])
+  /* dPP, dMP, dMM, dPM macros, ct_emf_average.c:198-213 */
+  eSW = (vya[c00] + 0.5 * (DV(ay, ax, c00) + DV(ay, ay, c00))) * bS -
+        (vxa[c00] + 0.5 * (DV(ax, ax, c00) + DV(ax, ay, c00))) * bW;
+  eSE = (vya[cx0] - 0.5 * (DV(ay, ax, cx0) - DV(ay, ay, cx0))) * bS -
+        (vxa[cx0] - 0.5 * (DV(ax, ax, cx0) - DV(ax, ay, cx0))) * bE;
+  eNE = (vya[cxy_] - 0.5 * (DV(ay, ax, cxy_) + DV(ay, ay, cxy_))) * bN -
+        (vxa[cxy_] - 0.5 * (DV(ax, ax, cxy_) + DV(ax, ay, cxy_))) * bE;
+  eNW = (vya[c0y] + 0.5 * (DV(ay, ax, c0y) - DV(ay, ay, c0y))) * bN -
+        (vxa[c0y] + 0.5 * (DV(ax, ax, c0y) - DV(ax, ay, c0y))) * bW;
+#undef DV
+  ez = a_xp * a_yp * eSW + a_xm * a_yp * eSE + a_xm * a_ym * eNE + a_xp * a_ym * eNW;
+  ez /= (a_xp + a_xm) * (a_yp + a_ym);
+  ez -= a_yp * a_ym * (bN - bS) / (a_yp + a_ym);
+  ez += a_xp * a_xm * (bE - bW) / (a_xp + a_xm);
+  return ez;
+}
+
+/* CT_ComputeEMF (UCT_HLL): edges over the emf ranges set by the sweeps,
+   ct_emf.c:130-131 etc.: i in [IBEG-1, IEND], likewise j, k. */
+static void compute_emf(oc_problem *p) {
+  const int dims = p->c.dims;
+  int kb = dims == 3 ? p->beg[2] - 1 : 0, ke = dims == 3 ? p->end[2] : 0;
+  int jb = p->beg[1] - 1, je = p->end[1];
+  int ib = p->beg[0] - 1, ie = p->end[0];
+  long nj = je - jb + 1, ni = ie - ib + 1, n = (long)(ke - kb + 1) * nj * ni, q;
+#pragma omp parallel for schedule(static)
+  for (q = 0; q < n; q++) {
+    int i = ib + (int)(q % ni), j = jb + (int)((q / ni) % nj), k = kb + (int)(q / (ni * nj));
+    size_t c = CI(p, k, j, i);
+    p->ez[c] = uct_hll_edge(p, 2, k, j, i);
+    if (dims == 3) {
+      p->ex[c] = uct_hll_edge(p, 0, k, j, i);
+      p->ey[c] = uct_hll_edge(p, 1, k, j, i);
+    }
+  }
+}
+
+/* CT_Update, Src/MHD/CT/ct_update.c:29-220 (Cartesian). */
+static void ct_update(oc_problem *p, double dt) {
+  const int dims = p->c.dims;
+  const int KO = dims == 3;
+  int kb = dims == 3 ? p->beg[2] - 1 : 0, ke = dims == 3 ? p->end[2] : 0;
+  int jb = p->beg[1] - 1, je = p->end[1];
+  int ib = p->beg[0] - 1, ie = p->end[0];
+  double dx1 = p->c.dx[0], dx2 = p->c.dx[1], dx3 = p->c.dx[2];
+  int i, j, k;
+  for (k = kb + KO; k <= ke; k++)
+    for (j = jb + 1; j <= je; j++)
+      for (i = ib; i <= ie; i++) {
+        double rhs_x;
+        if (dims == 2)
+          rhs_x = 0.0 - dt / dx2 * (p->ez[CI(p, k, j, i)] - p->ez[CI(p, k, j - 1, i)]);
+        else
+          rhs_x = 0.0 - dt / dx2 * (p->ez[CI(p, k, j, i)] - p->ez[CI(p, k, j - 1, i)]) +
+                  dt / dx3 * (p->ey[CI(p, k, j, i)] - p->ey[CI(p, k - 1, j, i)]);
+        p->bs[0][FI(p, 0, k, j, i)] = p->bs[0][FI(p, 0, k, j, i)] + rhs_x;
+      }
+  for (k = kb + KO; k <= ke; k++)
+    for (j = jb; j <= je; j++)
+      for (i = ib + 1; i <= ie; i++) {
+        double rhs_y;
+        if (dims == 2)
+          rhs_y = dt / dx1 * (p->ez[CI(p, k, j, i)] - p->ez[CI(p, k, j, i - 1)]);
+        else
+          rhs_y = dt / dx1 * (p->ez[CI(p, k, j, i)] - p->ez[CI(p, k, j, i - 1)]) -
+                  dt / dx3 * (p->ex[CI(p, k, j, i)] - p->ex[CI(p, k - 1, j, i)]);
+        p->bs[1][FI(p, 1, k, j, i)] = p->bs[1][FI(p, 1, k, j, i)] + rhs_y;
+      }
+  if (dims == 3)
+    for (k = kb; k <= ke; k++)
+      for (j = jb + 1; j <= je; j++)
+        for (i = ib + 1; i <= ie; i++) {
+          double rhs_z = -dt / dx1 * (p->ey[CI(p, k, j, i)] - p->ey[CI(p, k, j, i - 1)]) +
+                         dt / dx2 * (p->ex[CI(p, k, j, i)] - p->ex[CI(p, k, j - 1, i)]);
+          p->bs[2][FI(p, 2, k, j, i)] = p->bs[2][FI(p, 2, k, j, i)] + rhs_z;
+        }
+}
+
+/* CT_AverageMagneticField, Src/MHD/CT/ct_field_average.c:13-132 (Cartesian,
+   CT_EN_CORRECTION NO): domain plus one ghost layer. */
+static void ct_average(oc_problem *p) {
+  const int dims = p->c.dims;
+  int ko = dims == 3, d, i, j, k;
+  for (k = p->beg[2] - ko; k <= p->end[2] + ko; k++)
+    for (j = p->beg[1] - 1; j <= p->end[1] + 1; j++)
+      for (i = p->beg[0] - 1; i <= p->end[0] + 1; i++) {
+        size_t c = CI(p, k, j, i);
+        for (d = 0; d < dims; d++) {
+          int o[3] = {0, 0, 0};
+          o[d] = 1;
+          p->uc[BX1 + d][c] = 0.5 * (p->bs[d][FI(p, d, k, j, i)] +
+                                     p->bs[d][FI(p, d, k - o[2], j - o[1], i - o[0])]);
+        }
+      }
+}
+
+/* ------------------------------------------------------------------ */
+/* Stage driver                                                         */
+/* ------------------------------------------------------------------ */
+
+#define DOM_LOOP(p, k, j, i)                          \
+  for (k = (p)->beg[2]; k <= (p)->end[2]; k++)         \
+    for (j = (p)->beg[1]; j <= (p)->end[1]; j++)       \
+      for (i = (p)->beg[0]; i <= (p)->end[0]; i++)
+
+static void cons_to_prim_3d(oc_problem *p) {
+  const double gmm1 = p->c.gamma - 1.0;
+  int64_t nf = 0;
+  long nk = p->end[2] - p->beg[2] + 1, nj = p->end[1] - p->beg[1] + 1;
+  long ni = p->end[0] - p->beg[0] + 1, n = nk * nj * ni, q;
+#pragma omp parallel for schedule(static) reduction(+ : nf)
+  for (q = 0; q < n; q++) {
+    int i = p->beg[0] + (int)(q % ni), j = p->beg[1] + (int)((q / ni) % nj);
+    int k = p->beg[2] + (int)(q / (ni * nj));
+    size_t c = CI(p, k, j, i);
+    double u[NV], v[NV];
+    int nv;
+    for (nv = 0; nv < NV; nv++) u[nv] = p->uc[nv][c];
+    nf += cons_to_prim(u, v, gmm1, &p->flag[c]);
+    for (nv = 0; nv < NV; nv++) { p->uc[nv][c] = u[nv]; p->vc[nv][c] = v[nv]; }
+  }
+  p->nfail += nf;
+}
+
+/* UpdateStage, update_stage.c:37-314 */
+static void update_stage(oc_problem *p, double dt, int stage, double *inv_dt,
+                         double *inv_dt_1d) {
+  int dir;
+  if (p->c.dims > 1 && stage == 1) memset(p->cdt, 0, p->ncell * sizeof(double));
+  for (dir = 0; dir < p->c.dims; dir++) sweep(p, dir, dt, stage, inv_dt_1d, &p->max_mach);
+  if (p->c.ct) {
+    compute_emf(p);
+    ct_update(p, dt);
+  }
+  if (p->c.dims > 1 && stage == 1) { /* :308-312 */
+    int i, j, k;
+    double m = *inv_dt;
+    DOM_LOOP(p, k, j, i) m = MAX(m, p->cdt[CI(p, k, j, i)]);
+    m /= (double)p->c.dims;
+    *inv_dt = m;
+  }
+}
+
+/* AdvanceStep, Src/Time_Stepping/rk_step.c:27-254 */
+int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
+               int64_t *nfail) {
+  const double gmm1 = p->c.gamma - 1.0;
+  const double w0 = p->c.stepping == OC_RK3 ? 0.75 : 0.5;
+  const double wc = p->c.stepping == OC_RK3 ? 0.25 : 0.5;
+  static const double one_third = 1.0 / 3.0;
+  double inv_dt = 0.0, inv_dt_1d = 0.0;
+  int i, j, k, nv, d;
+  size_t c;
+
+  p->nfail = 0;
+  p->max_mach = 0.0;
+  memset(p->flag, 0, p->ncell);
+  /* stage 1 */
+  boundary(p);
+  DOM_LOOP(p, k, j, i) {
+    double v[NV], u[NV];
+    c = CI(p, k, j, i);
+    for (nv = 0; nv < NV; nv++) v[nv] = p->vc[nv][c];
+    prim_to_cons(v, u, gmm1);
+    for (nv = 0; nv < NV; nv++) p->uc[nv][c] = p->u0[nv][c] = u[nv];
+  }
+  if (p->c.ct)
+    for (d = 0; d < p->c.dims; d++) memcpy(p->bs0[d], p->bs[d], p->nface[d] * sizeof(double));
+  update_stage(p, dt, 1, &inv_dt, &inv_dt_1d);
+  if (p->c.ct) ct_average(p);
+  cons_to_prim_3d(p);
+
+  /* stage 2 */
+  boundary(p);
+  update_stage(p, dt, 2, &inv_dt, &inv_dt_1d);
+  DOM_LOOP(p, k, j, i) {
+    c = CI(p, k, j, i);
+    for (nv = 0; nv < NV; nv++) p->uc[nv][c] = w0 * p->u0[nv][c] + wc * p->uc[nv][c];
+  }
+  if (p->c.ct) {
+    for (d = 0; d < p->c.dims; d++) {
+      size_t f;
+      for (f = 0; f < p->nface[d]; f++) p->bs[d][f] = w0 * p->bs0[d][f] + wc * p->bs[d][f];
+    }
+    ct_average(p);
+  }
+  cons_to_prim_3d(p);
+
+  if (p->c.stepping == OC_RK3) {
+    boundary(p);
+    update_stage(p, dt, 3, &inv_dt, &inv_dt_1d);
+    DOM_LOOP(p, k, j, i) {
+      c = CI(p, k, j, i);
+      for (nv = 0; nv < NV; nv++)
+        p->uc[nv][c] = one_third * (p->u0[nv][c] + 2.0 * p->uc[nv][c]);
+    }
+    if (p->c.ct) {
+      for (d = 0; d < p->c.dims; d++) {
+        size_t f;
+        for (f = 0; f < p->nface[d]; f++) p->bs[d][f] = (p->bs0[d][f] + 2.0 * p->bs[d][f]) / 3.0;
+      }
+      ct_average(p);
+    }
+    cons_to_prim_3d(p);
+  }
+  if (p->c.dims == 1) inv_dt = inv_dt_1d;
+  if (inv_dt_hyp) *inv_dt_hyp = inv_dt;
+  if (max_mach) *max_mach = p->max_mach;
+  if (nfail) *nfail = p->nfail;
+  return 0;
+}
+
+/* Main loop dt logic, Src/main.c:143-151, 215, 236, 389-575 */
+int oc_run(oc_problem *p, int nsteps, double first_dt, double cfl,
+           double cfl_max_var, double *dts, double *t_final) {
+  double g_dt = first_dt, g_time = 0.0;
+  int s;
+  for (s = 0; s < nsteps; s++) {
+    double inv_dt, dt_hyp, dtnext;
+    if (dts) dts[s] = g_dt;
+    oc_advance(p, g_dt, &inv_dt, NULL, NULL);
+    g_time += g_dt;
+    dt_hyp = 1.0 / inv_dt;
+    dt_hyp *= cfl;
+    dtnext = dt_hyp;
+    dtnext = MIN(dtnext, cfl_max_var * g_dt);
+    g_dt = dtnext;
+  }
+  if (t_final) *t_final = g_time;
+  return 0;
+}
+
+/* ------------------------------------------------------------------ */
+/* Allocation and state transfer                                        */
+/* ------------------------------------------------------------------ */
+
+oc_problem *oc_create(const oc_config *cfg) {
+  oc_problem *p = calloc(1, sizeof *p);
+  int d, nv;
+  p->c = *cfg;
+  if (cfg->ct && cfg->dims < 2) { free(p); return NULL; }
+  for (d = 0; d < 3; d++)
+    if (cfg->ct && d < cfg->dims && cfg->bc[d] != OC_PERIODIC) { free(p); return NULL; }
+  p->ng = cfg->recon == OC_PARABOLIC ? 3 : 2; /* Src/get_nghost.c:28-104 */
+  for (d = 0; d < 3; d++) {
+    int active = d < cfg->dims;
+    p->nt[d] = active ? cfg->nx[d] + 2 * p->ng : 1;
+    p->beg[d] = active ? p->ng : 0;
+    p->end[d] = active ? p->ng + cfg->nx[d] - 1 : 0;
+    p->inv_dx[d] = 1.0 / cfg->dx[d]; /* set_geometry.c:244 */
+    if (!active) p->c.nx[d] = 1;
+  }
+  p->ncell = (size_t)p->nt[0] * p->nt[1] * p->nt[2];
+  for (d = 0; d < 3; d++)
+    p->nface[d] = (size_t)(p->nt[0] + (d == 0)) * (p->nt[1] + (d == 1)) * (p->nt[2] + (d == 2));
+  for (nv = 0; nv < NV; nv++) {
+    p->vc[nv] = calloc(p->ncell, sizeof(double));
+    p->uc[nv] = calloc(p->ncell, sizeof(double));
+    p->u0[nv] = calloc(p->ncell, sizeof(double));
+  }
+  for (d = 0; d < 3; d++) {
+    int c;
+    p->bs[d] = calloc(p->nface[d], sizeof(double));
+    p->bs0[d] = calloc(p->nface[d], sizeof(double));
+    p->sl[d] = calloc(p->ncell, sizeof(double));
+    p->sr[d] = calloc(p->ncell, sizeof(double));
+    for (c = 0; c < 3; c++) p->dv[d][c] = calloc(p->ncell, sizeof(double));
+  }
+  p->ex = calloc(p->ncell, sizeof(double));
+  p->ey = calloc(p->ncell, sizeof(double));
+  p->ez = calloc(p->ncell, sizeof(double));
+  p->cdt = calloc(p->ncell, sizeof(double));
+  p->flag = calloc(p->ncell, 1);
+#ifdef _OPENMP
+  if (cfg->nthreads > 0) omp_set_num_threads(cfg->nthreads);
+#endif
+  return p;
+}
+
+void oc_destroy(oc_problem *p) {
+  int d, nv, c;
+  if (!p) return;
+  for (nv = 0; nv < NV; nv++) { free(p->vc[nv]); free(p->uc[nv]); free(p->u0[nv]); }
+  for (d = 0; d < 3; d++) {
+    free(p->bs[d]); free(p->bs0[d]); free(p->sl[d]); free(p->sr[d]);
+    for (c = 0; c < 3; c++) free(p->dv[d][c]);
+  }
+  free(p->ex); free(p->ey); free(p->ez); free(p->cdt); free(p->flag);
+  free(p);
+}
+
+static void xfer(oc_problem *p, double *vc, double *bs[3], int to_problem) {
+  int nx = p->c.nx[0], ny = p->c.nx[1], nz = p->c.nx[2];
+  int nv, d, i, j, k;
+  size_t q = 0;
+  for (nv = 0; nv < NV; nv++)
+    for (k = 0; k < nz; k++)
+      for (j = 0; j < ny; j++)
+        for (i = 0; i < nx; i++, q++) {
+          size_t c = CI(p, k + p->beg[2], j + p->beg[1], i + p->beg[0]);
+          if (to_problem) p->vc[nv][c] = vc[q];
+          else vc[q] = p->vc[nv][c];
+        }
+  if (!p->c.ct) return;
+  for (d = 0; d < p->c.dims; d++) {
+    int fx = nx + (d == 0), fy = ny + (d == 1), fz = nz + (d == 2);
+    q = 0;
+    if (!bs[d]) continue;
+    for (k = 0; k < fz; k++)
+      for (j = 0; j < fy; j++)
+        for (i = 0; i < fx; i++, q++) {
+          /* dump face index 0 along d is reference index beg-1 */
+          int ri = i + p->beg[0] - (d == 0), rj = j + p->beg[1] - (d == 1);
+          int rk = k + p->beg[2] - (d == 2);
+          size_t f = FI(p, d, rk, rj, ri);
+          if (to_problem) p->bs[d][f] = bs[d][q];
+          else bs[d][q] = p->bs[d][f];
+        }
+  }
+}
+
+void oc_set_state(oc_problem *p, const double *vc, const double *bs0,
+                  const double *bs1, const double *bs2) {
+  double *b[3] = {(double *)bs0, (double *)bs1, (double *)bs2};
+  xfer(p, (double *)vc, b, 1);
+}
+
+void oc_get_state(const oc_problem *p, double *vc, double *bs0, double *bs1,
+                  double *bs2) {
+  double *b[3] = {bs0, bs1, bs2};
+  xfer((oc_problem *)p, vc, b, 0);
+}

@@ -1,0 +1,64 @@
+/*
+ * CPU oracle for the unsplit ideal-MHD finite-volume step of PLUTO 4.3.
+ *
+ * TEST INFRASTRUCTURE ONLY.  This is a plain-C restatement of the reference
+ * algorithm (Src/Time_Stepping/rk_step.c, update_stage.c, the Src/States,
+ * Src/MHD and Src/MHD/CT directories), written so that every floating-point operation
+ * happens in the reference's order.  Built with -ffp-contract=off it agrees
+ * bit for bit with the reference binary on the golden problems.  Only the
+ * test suite, the smoke check and the CPU-baseline leg of the benchmark use
+ * it; the product (libpluto_gb300.so) never links or calls it.
+ *
+ * State layout (interior only, the layout of a PLUTO .dbl dump):
+ *   vc : 8 primitive variables [RHO,VX1,VX2,VX3,BX1,BX2,BX3,PRS][nz][ny][nx]
+ *        (two-component problems carry zero VX3/BX3),
+ *   bs : staggered fields, bs[d] of shape [nz+(d==2)][ny+(d==1)][nx+(d==0)],
+ *        face index 0 is the left face of the first interior cell.
+ */
+#ifndef MHD_ORACLE_H
+#define MHD_ORACLE_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+enum { OC_RHO = 0, OC_VX1, OC_VX2, OC_VX3, OC_BX1, OC_BX2, OC_BX3, OC_PRS, OC_NVAR };
+enum { OC_LINEAR = 0, OC_PARABOLIC = 1 };
+enum { OC_FLAT_LIM = 0, OC_MINMOD_LIM, OC_VANLEER_LIM, OC_MC_LIM, OC_DEFAULT_LIM };
+enum { OC_HLL = 0, OC_HLLD = 1, OC_ROE = 2 };
+enum { OC_RK2 = 2, OC_RK3 = 3 };
+enum { OC_PERIODIC = 0, OC_OUTFLOW = 1 };
+
+typedef struct {
+  int dims;            /* DIMENSIONS 1..3 */
+  int components;      /* COMPONENTS 2 or 3 */
+  int nx[3];           /* interior cells (1 for inactive dims) */
+  double dx[3];        /* uniform spacing */
+  double gamma;
+  int recon, limiter, solver, stepping;
+  int ct;              /* 1: constrained transport, UCT_HLL average */
+  int bc[3];           /* boundary type per dim (same on both sides) */
+  int nthreads;        /* OpenMP threads (0: runtime default) */
+} oc_config;
+
+typedef struct oc_problem oc_problem;
+
+oc_problem *oc_create(const oc_config *cfg);
+void oc_destroy(oc_problem *p);
+void oc_set_state(oc_problem *p, const double *vc, const double *bs0,
+                  const double *bs1, const double *bs2);
+void oc_get_state(const oc_problem *p, double *vc, double *bs0, double *bs1,
+                  double *bs2);
+/* One AdvanceStep with time step dt; returns invDt_hyp (pre-division by
+   DIMENSIONS already applied as in the reference) and the floor count. */
+int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
+               int64_t *nfail);
+/* The reference main loop for nsteps steps: dt(0) = first_dt,
+   dt(n+1) = min(cfl/invDt_hyp, cfl_max_var*dt(n)).  dts receives each dt. */
+int oc_run(oc_problem *p, int nsteps, double first_dt, double cfl,
+           double cfl_max_var, double *dts, double *t_final);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

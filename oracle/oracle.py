@@ -1,0 +1,124 @@
+"""ctypes wrapper for the CPU oracle (test infrastructure only).
+
+Used by the test suite, the smoke check and the CPU-baseline leg of the
+benchmark, never by the product path.  ``build()`` compiles ``liboracle.so``
+from ``mhd_oracle.c`` with the committed Makefile.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import subprocess
+from pathlib import Path
+
+import numpy as np
+
+HERE = Path(__file__).resolve().parent
+LIB = HERE / "liboracle.so"
+
+NVAR = 8
+RECON = {"LINEAR": 0, "PARABOLIC": 1}
+LIMITER = {"FLAT_LIM": 0, "MINMOD_LIM": 1, "VANLEER_LIM": 2, "MC_LIM": 3, "DEFAULT": 4}
+SOLVER = {"hll": 0, "hlld": 1, "roe": 2}
+STEPPING = {"RK2": 2, "RK3": 3}
+BC = {"periodic": 0, "outflow": 1}
+
+
+class OcConfig(C.Structure):
+    _fields_ = [("dims", C.c_int), ("components", C.c_int), ("nx", C.c_int * 3),
+                ("dx", C.c_double * 3), ("gamma", C.c_double), ("recon", C.c_int),
+                ("limiter", C.c_int), ("solver", C.c_int), ("stepping", C.c_int),
+                ("ct", C.c_int), ("bc", C.c_int * 3), ("nthreads", C.c_int)]
+
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    if force or not LIB.exists() or LIB.stat().st_mtime < (HERE / "mhd_oracle.c").stat().st_mtime:
+        subprocess.run(["make", "-s", "-C", str(HERE)], check=True)
+    return LIB
+
+
+def lib():
+    global _lib
+    if _lib is None:
+        build()
+        L = C.CDLL(str(LIB))
+        L.oc_create.restype = C.c_void_p
+        L.oc_create.argtypes = [C.POINTER(OcConfig)]
+        L.oc_destroy.argtypes = [C.c_void_p]
+        dp = C.POINTER(C.c_double)
+        L.oc_set_state.argtypes = [C.c_void_p, dp, dp, dp, dp]
+        L.oc_get_state.argtypes = [C.c_void_p, dp, dp, dp, dp]
+        L.oc_advance.argtypes = [C.c_void_p, C.c_double, dp, dp, C.POINTER(C.c_int64)]
+        L.oc_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, dp, dp]
+        _lib = L
+    return _lib
+
+
+def _ptr(a):
+    return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class Oracle:
+    """One problem instance held by the C oracle.
+
+    ``spec`` keys: dims, components, nx (3-tuple), dx (3-tuple), gamma,
+    recon, limiter, solver, stepping, ct, bc.
+    """
+
+    def __init__(self, spec: dict, nthreads: int = 0):
+        self.spec = dict(spec)
+        c = OcConfig()
+        c.dims = spec["dims"]
+        c.components = spec["components"]
+        for d in range(3):
+            c.nx[d] = int(spec["nx"][d]) if d < spec["dims"] else 1
+            c.dx[d] = float(spec["dx"][d])
+            c.bc[d] = BC[spec.get("bc", "periodic")]
+        c.gamma = float(spec["gamma"])
+        c.recon = RECON[spec["recon"]]
+        c.limiter = LIMITER[spec["limiter"]]
+        c.solver = SOLVER[spec["solver"]]
+        c.stepping = STEPPING[spec["stepping"]]
+        c.ct = int(bool(spec["ct"]))
+        c.nthreads = nthreads
+        self.h = lib().oc_create(C.byref(c))
+        if not self.h:
+            raise ValueError("oracle rejected the configuration")
+        self.nx = tuple(c.nx[d] for d in range(3))
+
+    def __del__(self):
+        if getattr(self, "h", None):
+            lib().oc_destroy(self.h)
+            self.h = None
+
+    def face_shape(self, d):
+        nx, ny, nz = self.nx
+        return (nz + (d == 2), ny + (d == 1), nx + (d == 0))
+
+    def set_state(self, vc: np.ndarray, bs=(None, None, None)):
+        vc = np.ascontiguousarray(vc, dtype=np.float64)
+        b = [None if x is None else np.ascontiguousarray(x, dtype=np.float64) for x in bs]
+        lib().oc_set_state(self.h, _ptr(vc), _ptr(b[0]), _ptr(b[1]), _ptr(b[2]))
+
+    def get_state(self):
+        nx, ny, nz = self.nx
+        vc = np.zeros((NVAR, nz, ny, nx))
+        bs = [np.zeros(self.face_shape(d)) if (self.spec["ct"] and d < self.spec["dims"]) else None
+              for d in range(3)]
+        lib().oc_get_state(self.h, _ptr(vc), _ptr(bs[0]), _ptr(bs[1]), _ptr(bs[2]))
+        return vc, bs
+
+    def advance(self, dt: float):
+        inv = C.c_double()
+        mach = C.c_double()
+        nf = C.c_int64()
+        lib().oc_advance(self.h, dt, C.byref(inv), C.byref(mach), C.byref(nf))
+        return inv.value, mach.value, nf.value
+
+    def run(self, nsteps: int, first_dt: float, cfl: float, cfl_max_var: float = 1.1):
+        dts = np.zeros(max(nsteps, 1))
+        t = C.c_double()
+        lib().oc_run(self.h, nsteps, first_dt, cfl, cfl_max_var, _ptr(dts), C.byref(t))
+        return dts[:nsteps], t.value

@@ -1,0 +1,87 @@
+#!/usr/bin/env python3
+"""Generate the golden fixtures by running the reference PLUTO 4.3 binary.
+
+Run in a container that has the reference tree (``PLUTO_REF``, default
+``/root/reference``) and gcc:
+
+    python tests/golden/make_golden.py
+
+Each fixture ``<name>.npz`` holds the reference's own initial dump (step 0)
+and its dump after ``steps`` steps, as written by the reference (``.dbl``,
+double precision), plus the problem description.  Variables are stored in the
+8-slot order RHO, VX1, VX2, VX3, BX1, BX2, BX3, PRS (two-component problems
+get zero VX3/BX3 slots); staggered fields as ``bs0``.. with one extra face
+along their own axis.
+"""
+from __future__ import annotations
+
+import json
+import sys
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parents[2]
+sys.path.insert(0, str(ROOT))
+from oracle import build_ref as br  # noqa: E402
+
+GOLDEN = Path(__file__).resolve().parent
+NAMES = ["rho", "vx1", "vx2", "vx3", "Bx1", "Bx2", "Bx3", "prs"]
+
+
+def to_arrays(dump: dict, s: br.Setup):
+    n = [s.n[d] if d < s.dims else 1 for d in range(3)]
+    vc = np.zeros((8, n[2], n[1], n[0]))
+    for q, nm in enumerate(NAMES):
+        if nm in dump:
+            vc[q] = dump[nm]
+    bs = {}
+    for d in range(s.dims if s.ct else 0):
+        bs[f"bs{d}"] = dump[f"Bx{d+1}s"]
+    return vc, bs
+
+
+def spec_of(s: br.Setup) -> dict:
+    n = [s.n[d] if d < s.dims else 1 for d in range(3)]
+    dx = [(s.hi[d] - s.lo[d]) / n[d] if d < s.dims else 1.0 for d in range(3)]
+    gamma = 2.0 if s.name.startswith("tube") else 5.0 / 3.0
+    return dict(name=s.name, dims=s.dims, components=s.components, nx=n, dx=dx,
+                lo=list(s.lo), hi=list(s.hi), gamma=gamma, recon=s.recon,
+                limiter=s.limiter, solver=s.solver, stepping=s.stepping, ct=s.ct,
+                bc=s.bc, cfl=s.cfl, first_dt=s.first_dt, steps=s.steps,
+                params=s.params)
+
+
+def setups():
+    out = [
+        br.ot_setup("hlld", 32, 30),
+        br.ot_setup("hll", 32, 30),
+        br.blast_setup(16, 12),
+        br.blast_setup(16, 12, pin=1000.0, name="blast_floor_16", bmag=30.0),
+        br.tube_setup(0, 256, 100),
+        br.tube_setup(1, 200, 120),
+        br.tube_setup(2, 160, 80),
+        br.cpa_setup(32, 20),
+        br.turb_setup(12, 10),
+    ]
+    for s in out:
+        s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4
+    return out
+
+
+def main():
+    for s in setups():
+        a, b = br.run(s)
+        vc0, bs0 = to_arrays(a, s)
+        vc1, bs1 = to_arrays(b, s)
+        arrs = {"vc0": vc0, "vc1": vc1}
+        arrs.update({k + "_0": v for k, v in bs0.items()})
+        arrs.update({k + "_1": v for k, v in bs1.items()})
+        meta = spec_of(s)
+        meta.update(t_final=b["t"], dt_final=b["dt"], step_final=b["step"])
+        np.savez_compressed(GOLDEN / f"{s.name}.npz", meta=json.dumps(meta), **arrs)
+        print(f"{s.name}: t={b['t']:.6e} dt={b['dt']:.6e} step={b['step']}")
+
+
+if __name__ == "__main__":
+    main()
