@@ -1,0 +1,128 @@
+/*
+ * pluto_gb300 -- C ABI of the GB300 implementation of PLUTO 4.3's unsplit
+ * finite-volume step for ideal MHD on a uniform Cartesian grid.
+ *
+ * Plain C types only; every call returns an int status (PG_OK == 0).
+ * One solver object owns the device copy of one PLUTO domain (cell-centred
+ * primitives Vc, staggered fields Vs) and one CUDA stream.  Not thread safe:
+ * like PLUTO's own globals (Src/globals.h), a solver is driven from a single
+ * host thread.
+ *
+ * Reference interfaces replaced (paths inside the PLUTO source tree):
+ *   pg_advance       int AdvanceStep(Data*, Riemann_Solver*, timeStep*, Grid*)
+ *                    Src/prototypes.h:5, Src/Time_Stepping/rk_step.c:27
+ *   pg_run           the step loop of main(), Src/main.c:133-243, with
+ *                    NextTimeStep(), Src/main.c:389-575
+ *   pg_upload /      the host arrays d->Vc, d->Vs (Src/structs.h:29-88)
+ *   pg_download      read and written by AdvanceStep
+ *   pg_config        definitions.h scheme macros (Src/pluto.h:300-445,
+ *                    Src/MHD/CT/ct.h:43-49) + pluto.ini [Grid]/[Time]
+ *                    (Src/runtime_setup.c:22) + SetSolver()
+ *                    (Src/MHD/set_solver.c:13-80)
+ */
+#ifndef PLUTO_GB300_H
+#define PLUTO_GB300_H
+#include <stdint.h>
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define PG_ABI_VERSION 1
+
+/* status codes */
+enum {
+  PG_OK = 0,
+  PG_ERR_INVALID = 1,      /* bad argument or unsupported configuration   */
+  PG_ERR_CUDA = 2,         /* CUDA runtime error (message via pg_last_error) */
+  PG_ERR_NOMEM = 3,        /* device allocation failed                    */
+  PG_ERR_NAN = 4,          /* non-finite state detected                   */
+  PG_ERR_DT_TOO_SMALL = 5, /* dt < 1e-9*first_dt, Src/main.c:534-543       */
+  PG_ERR_TIMEOUT = 6,      /* a bounded device wait ran out               */
+  PG_ERR_TOO_LARGE = 7     /* size beyond a stated maximum                */
+};
+
+/* definitions.h / pluto.ini choices */
+enum { PG_LINEAR = 0, PG_PARABOLIC = 1 };                         /* RECONSTRUCTION */
+enum { PG_FLAT_LIM = 0, PG_MINMOD_LIM = 1, PG_VANLEER_LIM = 2,
+       PG_MC_LIM = 3, PG_DEFAULT_LIM = 4 };                       /* LIMITER */
+enum { PG_HLL = 0, PG_HLLD = 1, PG_ROE = 2 };                     /* [Solver] */
+enum { PG_RK2 = 2, PG_RK3 = 3 };                                  /* TIME_STEPPING */
+enum { PG_DIVB_NONE = 0, PG_CONSTRAINED_TRANSPORT = 1 };          /* DIVB_CONTROL */
+enum { PG_UCT_HLL = 4 };                                          /* CT_EMF_AVERAGE */
+enum { PG_PERIODIC = 0, PG_OUTFLOW = 1 };                         /* [Boundary] */
+enum { PG_FP64 = 0, PG_MIXED = 1 };                               /* arithmetic */
+enum { PG_LAYOUT_INTERIOR = 0, PG_LAYOUT_PLUTO = 1 };             /* host array layout */
+
+typedef struct {
+  int dims;             /* DIMENSIONS 1..3 */
+  int components;       /* COMPONENTS 2 or 3 */
+  int nx[3];            /* interior zones per axis (1 on inactive axes) */
+  double dx[3];         /* uniform zone widths, grid->dx[d][IBEG] */
+  double gamma;         /* g_gamma */
+  int reconstruction;
+  int limiter;
+  int riemann;
+  int time_stepping;
+  int divb;
+  int emf_average;
+  int bc[3];            /* same type on both sides of an axis */
+  int precision;        /* PG_FP64: bit-compatible with the reference C path */
+  int compute_mach;     /* 1: also reduce g_maxMach (two extra sqrt per face) */
+  double small_density; /* g_smallDensity (0 -> 1e-12) */
+  double small_pressure;/* g_smallPressure (0 -> 1e-12) */
+} pg_config;
+
+typedef struct {
+  double inv_dt_hyp;    /* Dts->invDt_hyp after the step */
+  double max_mach;      /* g_maxMach (0 unless compute_mach) */
+  int64_t nfail;        /* zones floored by ConsToPrim this step */
+} pg_step_info;
+
+typedef struct pg_solver pg_solver;
+
+/* Create a solver; the device state is zero until pg_upload. */
+int pg_create(const pg_config *cfg, pg_solver **out);
+int pg_destroy(pg_solver *s);
+
+/* Host <-> device state.  vars[8] point to RHO, VX1, VX2, VX3, BX1, BX2,
+   BX3, PRS (NULL for a slot the problem does not have, e.g. VX3/BX3 with
+   COMPONENTS 2: zero on upload, skipped on download).  faces[d] point to the
+   staggered component d (NULL without CT).
+   PG_LAYOUT_INTERIOR: interior zones only, the order of a .dbl dump
+     (Src/bin_io.c:216): cells [nz][ny][nx], faces one longer along d.
+   PG_LAYOUT_PLUTO: PLUTO's in-memory arrays including ghost zones,
+     d->Vc[nv] = [NX3_TOT][NX2_TOT][NX1_TOT] and d->Vs[d] allocated as an
+     ArrayBox with index origin -1 along d (Src/initialize.c:448-453); pass
+     the pointer to element [-1] (i.e. the start of the allocation). */
+int pg_upload(pg_solver *s, const double *const vars[8], const double *const faces[3],
+              int layout);
+int pg_download(pg_solver *s, double *const vars[8], double *const faces[3], int layout);
+
+/* One AdvanceStep with time step dt (host value of g_dt).  Blocks until the
+   step is complete and fills info (may be NULL). */
+int pg_advance(pg_solver *s, double dt, pg_step_info *info);
+
+/* The reference main loop for nsteps steps without host round trips:
+   dt(0) = first_dt (or the dt carried over from a previous pg_run when
+   first_dt <= 0), dt(n+1) = min(cfl/invDt_hyp, cfl_max_var*dt(n)) computed
+   on the device.  One CUDA graph per step.  Returns the time advanced and
+   the next dt. */
+int pg_run(pg_solver *s, int nsteps, double first_dt, double cfl, double cfl_max_var,
+           double *t_out, double *next_dt_out);
+
+/* Asynchronous variant of pg_run: enqueues nsteps graph launches on the
+   solver's stream and returns; pg_sync waits for them. */
+int pg_run_async(pg_solver *s, int nsteps, double first_dt, double cfl, double cfl_max_var);
+int pg_sync(pg_solver *s);
+
+/* Diagnostics */
+int pg_get_stream(pg_solver *s, void **cuda_stream);
+int pg_get_info(pg_solver *s, pg_step_info *info, double *time, double *dt);
+int pg_kernel_launches_per_step(pg_solver *s);
+const char *pg_last_error(void);
+int pg_abi_version(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

@@ -1,0 +1,96 @@
+"""ctypes binding of libpluto_gb300.so (the C ABI in include/pluto_gb300.h).
+
+There is no fallback: if the shared library is missing or fails to load,
+``lib()`` raises.  ``build()`` compiles it in-tree with nvcc.
+"""
+from __future__ import annotations
+
+import ctypes as C
+from pathlib import Path
+
+from . import build as _build
+
+LIB_PATH = _build.LIB
+
+PG_OK = 0
+PG_LINEAR, PG_PARABOLIC = 0, 1
+PG_FLAT_LIM, PG_MINMOD_LIM, PG_VANLEER_LIM, PG_MC_LIM, PG_DEFAULT_LIM = 0, 1, 2, 3, 4
+PG_HLL, PG_HLLD, PG_ROE = 0, 1, 2
+PG_RK2, PG_RK3 = 2, 3
+PG_DIVB_NONE, PG_CONSTRAINED_TRANSPORT = 0, 1
+PG_UCT_HLL = 4
+PG_PERIODIC, PG_OUTFLOW = 0, 1
+PG_FP64, PG_MIXED = 0, 1
+PG_LAYOUT_INTERIOR, PG_LAYOUT_PLUTO = 0, 1
+
+ERRORS = {1: "PG_ERR_INVALID", 2: "PG_ERR_CUDA", 3: "PG_ERR_NOMEM", 4: "PG_ERR_NAN",
+          5: "PG_ERR_DT_TOO_SMALL", 6: "PG_ERR_TIMEOUT", 7: "PG_ERR_TOO_LARGE"}
+
+# Every symbol declared in include/pluto_gb300.h (checked by the CPU tests).
+EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
+           "pg_run_async", "pg_sync", "pg_get_stream", "pg_get_info",
+           "pg_kernel_launches_per_step", "pg_last_error", "pg_abi_version"]
+
+
+class PgConfig(C.Structure):
+    _fields_ = [("dims", C.c_int), ("components", C.c_int), ("nx", C.c_int * 3),
+                ("dx", C.c_double * 3), ("gamma", C.c_double),
+                ("reconstruction", C.c_int), ("limiter", C.c_int), ("riemann", C.c_int),
+                ("time_stepping", C.c_int), ("divb", C.c_int), ("emf_average", C.c_int),
+                ("bc", C.c_int * 3), ("precision", C.c_int), ("compute_mach", C.c_int),
+                ("small_density", C.c_double), ("small_pressure", C.c_double)]
+
+
+class PgStepInfo(C.Structure):
+    _fields_ = [("inv_dt_hyp", C.c_double), ("max_mach", C.c_double), ("nfail", C.c_int64)]
+
+
+class PgError(RuntimeError):
+    def __init__(self, code: int, where: str, msg: str):
+        super().__init__(f"{where}: {ERRORS.get(code, code)}: {msg}")
+        self.code = code
+
+
+_lib = None
+
+
+def build(force: bool = False) -> Path:
+    return _build.build(force=force)
+
+
+def load(path: Path | str | None = None):
+    """Load the library without building (raises OSError when absent)."""
+    return C.CDLL(str(path or LIB_PATH))
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not LIB_PATH.exists():
+        raise OSError(f"{LIB_PATH} is missing: run pluto_gb300.build.build() (nvcc) first")
+    L = C.CDLL(str(LIB_PATH))
+    vp, dp, ip = C.c_void_p, C.POINTER(C.c_double), C.c_int
+    L.pg_create.argtypes = [C.POINTER(PgConfig), C.POINTER(vp)]
+    L.pg_destroy.argtypes = [vp]
+    L.pg_upload.argtypes = [vp, C.POINTER(dp), C.POINTER(dp), ip]
+    L.pg_download.argtypes = [vp, C.POINTER(dp), C.POINTER(dp), ip]
+    L.pg_advance.argtypes = [vp, C.c_double, C.POINTER(PgStepInfo)]
+    L.pg_run.argtypes = [vp, ip, C.c_double, C.c_double, C.c_double, dp, dp]
+    L.pg_run_async.argtypes = [vp, ip, C.c_double, C.c_double, C.c_double]
+    L.pg_sync.argtypes = [vp]
+    L.pg_get_stream.argtypes = [vp, C.POINTER(vp)]
+    L.pg_get_info.argtypes = [vp, C.POINTER(PgStepInfo), dp, dp]
+    L.pg_kernel_launches_per_step.argtypes = [vp]
+    L.pg_last_error.restype = C.c_char_p
+    for fn in ("pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
+               "pg_run_async", "pg_sync", "pg_get_stream", "pg_get_info",
+               "pg_kernel_launches_per_step", "pg_abi_version"):
+        getattr(L, fn).restype = C.c_int
+    _lib = L
+    return L
+
+
+def check(rc: int, where: str):
+    if rc != PG_OK:
+        raise PgError(rc, where, lib().pg_last_error().decode())

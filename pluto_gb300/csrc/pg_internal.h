@@ -1,0 +1,108 @@
+// Internal solver state shared by the translation units of libpluto_gb300.
+#pragma once
+#include <cuda_runtime.h>
+#include <cstddef>
+#include <cstdint>
+
+#include "../../include/pluto_gb300.h"
+
+namespace pg {
+
+// Grid geometry as seen by the kernels: every cell array, and every face
+// array, has the same [nt2][nt1][nt0] shape.  Face array d stores the face on
+// the +1/2 side of cell (k,j,i) along d at (k,j,i), i.e. the reference index
+// of d->Vs[d][k][j][i] (Src/initialize.c:448-453) without its -1 layer.
+struct Geom {
+  int dims;
+  int nt[3];       // total cells per axis (1 on inactive axes)
+  int beg[3];      // first interior index (0 on inactive axes)
+  int end[3];      // last interior index
+  int nx[3];       // interior cells
+  long long s[3];  // strides in elements: 1, nt0, nt0*nt1
+  long long ncell;
+  double dx[3], inv_dx[3];
+};
+
+__host__ __device__ inline long long cidx(const Geom& g, int k, int j, int i) {
+  return ((long long)k * g.nt[1] + j) * g.nt[0] + i;
+}
+
+// Inclusive index box.
+struct Box {
+  int lo[3], hi[3];
+  __host__ __device__ long long count() const {
+    return (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
+  }
+  __device__ void coords(long long q, int& i, int& j, int& k) const {
+    int ni = hi[0] - lo[0] + 1, nj = hi[1] - lo[1] + 1;
+    i = lo[0] + (int)(q % ni);
+    q /= ni;
+    j = lo[1] + (int)(q % nj);
+    k = lo[2] + (int)(q / nj);
+  }
+};
+
+// Device scalars of one solver (one allocation).
+struct DevScalars {
+  double dt;             // time step used by the kernels of the current step
+  double dt_prev;        // previous step's dt (for the cfl_max_var cap)
+  double time;           // simulated time
+  unsigned long long inv_dt_bits;  // running max of invDt (non-negative double bits)
+  unsigned long long mach_bits;    // running max of the Mach estimate
+  unsigned long long nfail;        // floor events
+  int status;                      // sticky device error flags
+  int pad;
+};
+
+struct Solver;
+int fp64_alloc(Solver* S);
+void fp64_free(Solver* S);
+int fp64_enqueue_step(Solver* S);  // all stages of one step on S->stream
+
+int mixed_alloc(Solver* S);
+void mixed_free(Solver* S);
+int mixed_enqueue_step(Solver* S);
+// host <-> device copy of one FP64 array in the interior or PLUTO layout
+int xfer_f64(Solver* S, double* dev, double* host, int fd, int layout, bool to_dev);
+
+struct Solver {
+  pg_config cfg;
+  Geom g;
+  int ng;
+  cudaStream_t stream = nullptr;
+  DevScalars* sc = nullptr;        // device
+  DevScalars* sc_host = nullptr;   // pinned mirror
+  // FP64 path arrays (NV cell arrays each)
+  double* V[8] = {};
+  double* U[8] = {};
+  double* U0[8] = {};
+  double* Bs[3] = {};
+  double* Bs0[3] = {};
+  double* VP[8] = {};   // reconstructed +1/2 states (per sweep)
+  double* VM[8] = {};   // reconstructed -1/2 states
+  double* F[8] = {};    // interface fluxes
+  double* P = nullptr;  // interface total pressure
+  double* CM = nullptr; // interface cmax
+  double* SL[3] = {};   // max(0,-SL) per direction
+  double* SR[3] = {};   // max(0, SR)
+  double* DV[3][3] = {};// velocity slopes DV[dir][comp]
+  double* E[3] = {};    // edge EMFs
+  double* CDT = nullptr;
+  unsigned char* flag = nullptr;
+  // mixed path
+  void* mixed = nullptr;
+  // graph of one step
+  cudaGraphExec_t graph = nullptr;
+  bool graph_dirty = true;
+  double cfl = 0.4, cfl_max_var = 1.1;
+  bool device_dt = false;  // kernels end each step by computing the next dt
+  int steps_done = 0;
+};
+
+constexpr int kThreads = 256;
+inline unsigned grid_for(long long n, int threads = kThreads) {
+  long long b = (n + threads - 1) / threads;
+  return (unsigned)(b < 1 ? 1 : b);
+}
+
+}  // namespace pg

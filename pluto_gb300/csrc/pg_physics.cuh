@@ -1,0 +1,371 @@
+// Point-wise ideal-MHD physics on the device, templated on the arithmetic
+// type.  Every expression keeps the operand order of PLUTO 4.3 so that the
+// FP64 instantiation, compiled without multiply-add contraction, reproduces
+// the reference C code bit for bit.  References are to files in the PLUTO
+// source tree.
+#pragma once
+#include <cstdint>
+
+namespace pg {
+
+enum : int { RHO = 0, VX1 = 1, VX2 = 2, VX3 = 3, BX1 = 4, BX2 = 5, BX3 = 6, PRS = 7, NV = 8 };
+constexpr int MX1 = VX1, ENG = PRS;
+constexpr unsigned char FLAG_CONS2PRIM_FAIL = 64;  // Src/pluto.h:200
+
+template <class T> __device__ __forceinline__ T pmax(T a, T b) { return a >= b ? a : b; }  // macros.h MAX
+template <class T> __device__ __forceinline__ T pmin(T a, T b) { return a <= b ? a : b; }  // macros.h MIN
+template <class T> __device__ __forceinline__ T abs_min(T a, T b) { return fabs(a) < fabs(b) ? a : b; }
+template <class T> __device__ __forceinline__ T minmod(T a, T b) {
+  return a * b > T(0) ? (fabs(a) < fabs(b) ? a : b) : T(0);
+}
+
+// Normal/tangent/bitangent rotation, Src/set_indexes.c:49-124.
+template <int DIR> struct Rot;
+template <> struct Rot<0> { static constexpr int vn = VX1, vt = VX2, vb = VX3, bn = BX1, bt = BX2, bb = BX3; };
+template <> struct Rot<1> { static constexpr int vn = VX2, vt = VX1, vb = VX3, bn = BX2, bt = BX1, bb = BX3; };
+template <> struct Rot<2> { static constexpr int vn = VX3, vt = VX1, vb = VX2, bn = BX3, bt = BX1, bb = BX2; };
+
+// Src/MHD/mappers.c:25-86
+template <class T>
+__device__ __forceinline__ void prim_to_cons(const T* v, T* u, T gmm1) {
+  T kinb2;
+  u[RHO] = v[RHO];
+  u[MX1] = v[RHO] * v[VX1];
+  u[MX1 + 1] = v[RHO] * v[VX2];
+  u[MX1 + 2] = v[RHO] * v[VX3];
+  u[BX1] = v[BX1];
+  u[BX2] = v[BX2];
+  u[BX3] = v[BX3];
+  kinb2 = v[VX1] * v[VX1] + v[VX2] * v[VX2] + v[VX3] * v[VX3];
+  kinb2 = v[RHO] * kinb2 + v[BX1] * v[BX1] + v[BX2] * v[BX2] + v[BX3] * v[BX3];
+  kinb2 *= T(0.5);
+  u[ENG] = kinb2 + v[PRS] / gmm1;
+}
+
+// Src/MHD/mappers.c:88-254 (ideal EOS): floors modify u in place.
+template <class T>
+__device__ __forceinline__ int cons_to_prim(T* u, T* v, T gmm1, T small_rho, T small_p,
+                                            unsigned char* flag) {
+  T tau, kinb2, m2, b2;
+  int ifail = 0;
+  m2 = u[MX1] * u[MX1] + u[MX1 + 1] * u[MX1 + 1] + u[MX1 + 2] * u[MX1 + 2];
+  b2 = u[BX1] * u[BX1] + u[BX2] * u[BX2] + u[BX3] * u[BX3];
+  if (u[RHO] < T(0)) {
+    u[RHO] = small_rho;
+    *flag |= FLAG_CONS2PRIM_FAIL;
+    ifail = 1;
+  }
+  v[RHO] = u[RHO];
+  tau = T(1) / u[RHO];
+  v[VX1] = u[MX1] * tau;
+  v[VX2] = u[MX1 + 1] * tau;
+  v[VX3] = u[MX1 + 2] * tau;
+  v[BX1] = u[BX1];
+  v[BX2] = u[BX2];
+  v[BX3] = u[BX3];
+  kinb2 = T(0.5) * (m2 * tau + b2);
+  if (u[ENG] < T(0)) {
+    u[ENG] = small_p / gmm1 + kinb2;
+    *flag |= FLAG_CONS2PRIM_FAIL;
+    ifail = 1;
+  }
+  v[PRS] = gmm1 * (u[ENG] - kinb2);
+  if (v[PRS] < T(0)) {
+    v[PRS] = small_p;
+    u[ENG] = v[PRS] / gmm1 + kinb2;
+    *flag |= FLAG_CONS2PRIM_FAIL;
+    ifail = 1;
+  }
+  return ifail;
+}
+
+// Src/MHD/fluxes.c:110-249
+template <int DIR, class T>
+__device__ __forceinline__ void flux(const T* v, const T* u, T* fx, T& ptot) {
+  using R = Rot<DIR>;
+  T Bmag2 = v[BX1] * v[BX1] + v[BX2] * v[BX2] + v[BX3] * v[BX3];
+  ptot = v[PRS] + T(0.5) * Bmag2;
+  T vB = v[VX1] * v[BX1] + v[VX2] * v[BX2] + v[VX3] * v[BX3];
+  fx[RHO] = u[R::vn];
+  fx[MX1] = v[R::vn] * u[MX1] - v[R::bn] * v[BX1];
+  fx[MX1 + 1] = v[R::vn] * u[MX1 + 1] - v[R::bn] * v[BX2];
+  fx[MX1 + 2] = v[R::vn] * u[MX1 + 2] - v[R::bn] * v[BX3];
+  fx[R::bn] = T(0);
+  fx[R::bt] = v[R::vn] * v[R::bt] - v[R::bn] * v[R::vt];
+  fx[R::bb] = v[R::vn] * v[R::bb] - v[R::bn] * v[R::vb];
+  fx[ENG] = (u[ENG] + ptot) * v[R::vn] - v[R::bn] * vB;
+}
+
+// Src/MHD/eigenv.c:35-104 (ideal EOS)
+template <int DIR, class T>
+__device__ __forceinline__ void max_signal_speed(const T* v, T gamma, T& cmin, T& cmax) {
+  using R = Rot<DIR>;
+  T gpr = gamma * v[PRS];
+  T b1 = v[R::bn], b2 = v[R::bt], b3 = v[R::bb];
+  T Btmag2 = b2 * b2 + b3 * b3;
+  T Bmag2 = b1 * b1 + Btmag2;
+  T cf = gpr - Bmag2;
+  cf = gpr + Bmag2 + sqrt(cf * cf + T(4) * gpr * Btmag2);
+  cf = sqrt(T(0.5) * cf / v[RHO]);
+  cmin = v[R::vn] - cf;
+  cmax = v[R::vn] + cf;
+}
+
+template <class T> struct Iface {
+  T f[NV];
+  T press, SL, SR, cmax;
+};
+
+// Src/MHD/hll_speed.c:23-108 (DAVIS_ESTIMATE); Mach estimate only on request.
+template <int DIR, bool MACH, class T>
+__device__ __forceinline__ void hll_speed(const T* vL, const T* vR, T gamma, T& SL, T& SR, T& mach) {
+  using R = Rot<DIR>;
+  T slmin, slmax, srmin, srmax;
+  max_signal_speed<DIR>(vL, gamma, slmin, slmax);
+  max_signal_speed<DIR>(vR, gamma, srmin, srmax);
+  SL = pmin(slmin, srmin);
+  SR = pmax(slmax, srmax);
+  if (MACH) {
+    T a2L = gamma * vL[PRS] / vL[RHO];
+    T a2R = gamma * vR[PRS] / vR[RHO];
+    T scrh = fabs(vL[R::vn]) + fabs(vR[R::vn]);
+    scrh /= sqrt(a2L) + sqrt(a2R);
+    mach = scrh;
+  }
+}
+
+// Src/MHD/hll.c:30-166
+template <int DIR, bool MACH, class T>
+__device__ __forceinline__ void hll_solver(const T* vL, const T* uL, const T* vR, const T* uR, T gamma,
+                                           Iface<T>& o, T& mach) {
+  T fL[NV], fR[NV], ptL, ptR, SL, SR, scrh;
+  flux<DIR>(vL, uL, fL, ptL);
+  flux<DIR>(vR, uR, fR, ptR);
+  hll_speed<DIR, MACH>(vL, vR, gamma, SL, SR, mach);
+  o.SL = SL;
+  o.SR = SR;
+  o.cmax = pmax(fabs(SL), fabs(SR));
+  if (SL > T(0)) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) o.f[nv] = fL[nv];
+    o.press = ptL;
+  } else if (SR < T(0)) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) o.f[nv] = fR[nv];
+    o.press = ptR;
+  } else {
+    scrh = T(1) / (SR - SL);
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) {
+      o.f[nv] = SL * SR * (uR[nv] - uL[nv]) + SR * fL[nv] - SL * fR[nv];
+      o.f[nv] *= scrh;
+    }
+    o.press = (SR * ptL - SL * ptR) * scrh;
+  }
+}
+
+// Src/MHD/hlld.c:44-452 (ideal EOS, no background field)
+template <int DIR, bool MACH, class T>
+__device__ __forceinline__ void hlld_solver(const T* vL, const T* uL, const T* vR, const T* uR, T gamma,
+                                            Iface<T>& o, T& mach) {
+  using R = Rot<DIR>;
+  constexpr int MXn = R::vn, MXt = R::vt, MXb = R::vb;
+  constexpr int VXn = R::vn, VXt = R::vt, VXb = R::vb;
+  constexpr int BXn = R::bn, BXt = R::bt, BXb = R::bb;
+  T fL[NV], fR[NV], ptL, ptR, SL, SR, scrh;
+  flux<DIR>(vL, uL, fL, ptL);
+  flux<DIR>(vR, uR, fR, ptR);
+  hll_speed<DIR, MACH>(vL, vR, gamma, SL, SR, mach);
+  o.SL = SL;
+  o.SR = SR;
+  o.cmax = pmax(fabs(SL), fabs(SR));
+
+  if (SL >= T(0)) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) o.f[nv] = fL[nv];
+    o.press = ptL;
+    return;
+  }
+  if (SR <= T(0)) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) o.f[nv] = fR[nv];
+    o.press = ptR;
+    return;
+  }
+  T usL[NV], usR[NV];
+  T Bx, Bx1, sBx, duL, duR, SM, pts, sqrL, sqrR, S1L, S1R, scrhL, scrhR, vsL, vsR, wsL, wsR;
+  scrh = T(1) / (SR - SL);
+  Bx1 = Bx = (SR * vR[BXn] - SL * vL[BXn]) * scrh;
+  sBx = (Bx > T(0) ? T(1) : T(-1));
+  duL = SL - vL[VXn];
+  duR = SR - vR[VXn];
+  scrh = T(1) / (duR * uR[RHO] - duL * uL[RHO]);
+  SM = (duR * uR[MXn] - duL * uL[MXn] - ptR + ptL) * scrh;
+  pts = duR * uR[RHO] * ptL - duL * uL[RHO] * ptR + vL[RHO] * vR[RHO] * duR * duL * (vR[VXn] - vL[VXn]);
+  pts *= scrh;
+  usL[RHO] = uL[RHO] * duL / (SL - SM);
+  usR[RHO] = uR[RHO] * duR / (SR - SM);
+  sqrL = sqrt(usL[RHO]);
+  sqrR = sqrt(usR[RHO]);
+  S1L = SM - fabs(Bx) / sqrL;
+  S1R = SM + fabs(Bx) / sqrR;
+
+  bool revert_to_hllc = false;
+  if ((S1L - SL) < T(1.e-4) * (SM - SL)) revert_to_hllc = true;
+  if ((S1R - SR) > -T(1.e-4) * (SR - SM)) revert_to_hllc = true;
+
+  if (revert_to_hllc) {
+    scrh = T(1) / (SR - SL);
+    T Un = (SR * uR[BXn] - SL * uL[BXn] + fL[BXn] - fR[BXn]) * scrh;
+    T Ut = (SR * uR[BXt] - SL * uL[BXt] + fL[BXt] - fR[BXt]) * scrh;
+    T Ub = (SR * uR[BXb] - SL * uL[BXb] + fL[BXb] - fR[BXb]) * scrh;
+    usL[BXn] = usR[BXn] = Un;
+    usL[BXt] = usR[BXt] = Ut;
+    usL[BXb] = usR[BXb] = Ub;
+    S1L = S1R = SM;
+  } else {
+    scrhL = (uL[RHO] * duL * duL - Bx * Bx) / (uL[RHO] * duL * (SL - SM) - Bx * Bx);
+    scrhR = (uR[RHO] * duR * duR - Bx * Bx) / (uR[RHO] * duR * (SR - SM) - Bx * Bx);
+    usL[BXn] = Bx1;
+    usL[BXt] = uL[BXt] * scrhL;
+    usL[BXb] = uL[BXb] * scrhL;
+    usR[BXn] = Bx1;
+    usR[BXt] = uR[BXt] * scrhR;
+    usR[BXb] = uR[BXb] * scrhR;
+  }
+  scrhL = Bx / (uL[RHO] * duL);
+  scrhR = Bx / (uR[RHO] * duR);
+  vsL = vL[VXt] - scrhL * (usL[BXt] - uL[BXt]);
+  vsR = vR[VXt] - scrhR * (usR[BXt] - uR[BXt]);
+  wsL = vL[VXb] - scrhL * (usL[BXb] - uL[BXb]);
+  wsR = vR[VXb] - scrhR * (usR[BXb] - uR[BXb]);
+  usL[MXn] = usL[RHO] * SM;
+  usR[MXn] = usR[RHO] * SM;
+  usL[MXt] = usL[RHO] * vsL;
+  usR[MXt] = usR[RHO] * vsR;
+  usL[MXb] = usL[RHO] * wsL;
+  usR[MXb] = usR[RHO] * wsR;
+
+  scrhL = vL[VXn] * Bx1 + vL[VXt] * uL[BXt] + vL[VXb] * uL[BXb];
+  scrhL -= SM * Bx1 + vsL * usL[BXt] + wsL * usL[BXb];
+  usL[ENG] = duL * uL[ENG] - ptL * vL[VXn] + pts * SM + Bx * scrhL;
+  usL[ENG] /= SL - SM;
+  scrhR = vR[VXn] * Bx1 + vR[VXt] * uR[BXt] + vR[VXb] * uR[BXb];
+  scrhR -= SM * Bx1 + vsR * usR[BXt] + wsR * usR[BXb];
+  usR[ENG] = duR * uR[ENG] - ptR * vR[VXn] + pts * SM + Bx * scrhR;
+  usR[ENG] /= SR - SM;
+
+  if (S1L >= T(0)) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) o.f[nv] = fL[nv] + SL * (usL[nv] - uL[nv]);
+    o.press = ptL;
+  } else if (S1R <= T(0)) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) o.f[nv] = fR[nv] + SR * (usR[nv] - uR[nv]);
+    o.press = ptR;
+  } else {
+    T ussl[NV], ussr[NV];
+    ussl[RHO] = usL[RHO];
+    ussr[RHO] = usR[RHO];
+    T vss = sqrL * vsL + sqrR * vsR + (usR[BXt] - usL[BXt]) * sBx;
+    vss /= sqrL + sqrR;
+    T wss = sqrL * wsL + sqrR * wsR + (usR[BXb] - usL[BXb]) * sBx;
+    wss /= sqrL + sqrR;
+    ussl[MXn] = ussl[RHO] * SM;
+    ussr[MXn] = ussr[RHO] * SM;
+    ussl[MXt] = ussl[RHO] * vss;
+    ussr[MXt] = ussr[RHO] * vss;
+    ussl[MXb] = ussl[RHO] * wss;
+    ussr[MXb] = ussr[RHO] * wss;
+    ussl[BXn] = ussr[BXn] = Bx1;
+    ussl[BXt] = sqrL * usR[BXt] + sqrR * usL[BXt] + sqrL * sqrR * (vsR - vsL) * sBx;
+    ussl[BXt] /= sqrL + sqrR;
+    ussr[BXt] = ussl[BXt];
+    ussl[BXb] = sqrL * usR[BXb] + sqrR * usL[BXb] + sqrL * sqrR * (wsR - wsL) * sBx;
+    ussl[BXb] /= sqrL + sqrR;
+    ussr[BXb] = ussl[BXb];
+    scrhL = SM * Bx1 + vsL * usL[BXt] + wsL * usL[BXb];
+    scrhL -= SM * Bx1 + vss * ussl[BXt] + wss * ussl[BXb];
+    scrhR = SM * Bx1 + vsR * usR[BXt] + wsR * usR[BXb];
+    scrhR -= SM * Bx1 + vss * ussr[BXt] + wss * ussr[BXb];
+    ussl[ENG] = usL[ENG] - sqrL * scrhL * sBx;
+    ussr[ENG] = usR[ENG] + sqrR * scrhR * sBx;
+    if (SM >= T(0)) {
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) o.f[nv] = fL[nv] + S1L * (ussl[nv] - usL[nv]) + SL * (usL[nv] - uL[nv]);
+      o.press = ptL;
+    } else {
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) o.f[nv] = fR[nv] + S1R * (ussr[nv] - usR[nv]) + SR * (usR[nv] - uR[nv]);
+      o.press = ptR;
+    }
+  }
+}
+
+// Limiters, Src/States/plm_coeffs.h:72-175 (uniform Cartesian forms);
+// DEFAULT mix from Src/States/plm_states.c:180-213.
+enum : int { LIM_FLAT = 0, LIM_MINMOD = 1, LIM_VANLEER = 2, LIM_MC = 3, LIM_DEFAULT = 4 };
+
+template <class T>
+__device__ __forceinline__ T limit(int lim, int nv, T dvp, T dvm) {
+  if (lim == LIM_DEFAULT) lim = (nv == RHO) ? LIM_MC : (nv == PRS ? LIM_MINMOD : LIM_VANLEER);
+  switch (lim) {
+    case LIM_FLAT: return T(0);
+    case LIM_MINMOD: return dvp * dvm > T(0) ? abs_min(dvp, dvm) : T(0);
+    case LIM_VANLEER: return dvp * dvm > T(0) ? T(2) * dvp * dvm / (dvp + dvm) : T(0);
+    default:
+      if (dvp * dvm > T(0)) {
+        T qc = T(0.5) * (dvm + dvp), scrh = T(2) * abs_min(dvp, dvm);
+        return abs_min(qc, scrh);
+      }
+      return T(0);
+  }
+}
+
+// PPM interface value with minmod clip, ppm_states.c:131-143 (PPM_ORDER 4,
+// Cartesian coefficients ppm_coeffs.c:478-520).
+template <class T>
+__device__ __forceinline__ T ppm_iface(T vm1, T v0, T vp1, T vp2) {
+  const T w_1 = T(-1.0 / 12.0), w0 = T(7.0 / 12.0), w1 = T(7.0 / 12.0), w2 = T(-1.0 / 12.0);
+  T vp = w_1 * vm1 + w0 * v0 + w1 * vp1 + w2 * vp2;
+  T dv = vp1 - v0;
+  T dvp = vp - v0;
+  return v0 + minmod(dvp, dv);
+}
+
+// Parabolic limiter, ppm_states.c:146-207 with hp = hm = 3 (cp = cm = 2).
+template <class T>
+__device__ __forceinline__ void ppm_limit(T v, T& vp, T& vm) {
+  const T cm = (T(3) + T(1)) / (T(3) - T(1));
+  const T cp = (T(3) + T(1)) / (T(3) - T(1));
+  T dvp = vp - v, dvm = vm - v;
+  if (dvp * dvm >= T(0)) dvp = dvm = T(0);
+  else {
+    if (fabs(dvp) >= cm * fabs(dvm)) dvp = -cm * dvm;
+    else if (fabs(dvm) >= cp * fabs(dvp)) dvm = -cp * dvp;
+  }
+  vp = v + dvp;
+  vm = v + dvm;
+}
+
+// Src/MHD/CT/ct_stag_slopes.c:92-105
+template <class T>
+__device__ __forceinline__ T mc_lim2(T dp, T dm) {
+  if (dp * dm < T(0)) return T(0);
+  T dc = T(0.5) * (dp + dm);
+  T scrh = T(2) * (fabs(dp) < fabs(dm) ? dp : dm);
+  return fabs(dc) < fabs(scrh) ? dc : scrh;
+}
+
+// Combination of the 2D HLL edge formula, ct_emf_average.c:262-289.
+template <class T>
+__device__ __forceinline__ T uct_hll_combine(T a_xp, T a_xm, T a_yp, T a_ym, T eSW, T eSE, T eNE, T eNW, T bS,
+                                             T bN, T bW, T bE) {
+  T e = a_xp * a_yp * eSW + a_xm * a_yp * eSE + a_xm * a_ym * eNE + a_xp * a_ym * eNW;
+  e /= (a_xp + a_xm) * (a_yp + a_ym);
+  e -= a_yp * a_ym * (bN - bS) / (a_yp + a_ym);
+  e += a_xp * a_xm * (bE - bW) / (a_xp + a_xm);
+  return e;
+}
+
+}  // namespace pg

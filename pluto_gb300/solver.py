@@ -1,0 +1,148 @@
+"""Host-side mirror of PLUTO's AdvanceStep interface over the C ABI.
+
+A problem is described with the names PLUTO uses in ``definitions.h`` and
+``pluto.ini`` (Src/pluto.h:300-445, Src/Templates/pluto.ini):
+
+    spec = dict(dims=2, components=2, nx=(256, 256, 1), dx=(1/256, 1/256, 1.0),
+                gamma=5/3, recon="LINEAR", limiter="MC_LIM", solver="hlld",
+                stepping="RK2", ct=True, bc="periodic")
+
+``Solver.advance(dt)`` is one AdvanceStep (Src/Time_Stepping/rk_step.c:27);
+``Solver.run(n, first_dt, cfl)`` is n passes of the main loop with
+NextTimeStep (Src/main.c:133-243, 389-575) kept on the device.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib as L
+
+RECON = {"LINEAR": L.PG_LINEAR, "PARABOLIC": L.PG_PARABOLIC}
+LIMITER = {"FLAT_LIM": L.PG_FLAT_LIM, "MINMOD_LIM": L.PG_MINMOD_LIM,
+           "VANLEER_LIM": L.PG_VANLEER_LIM, "MC_LIM": L.PG_MC_LIM, "DEFAULT": L.PG_DEFAULT_LIM}
+RIEMANN = {"hll": L.PG_HLL, "hlld": L.PG_HLLD, "roe": L.PG_ROE}
+STEPPING = {"RK2": L.PG_RK2, "RK3": L.PG_RK3}
+BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW}
+PRECISION = {"fp64": L.PG_FP64, "mixed": L.PG_MIXED}
+NVAR = 8
+
+
+def make_config(spec: dict, precision: str = "fp64", compute_mach: bool = False) -> L.PgConfig:
+    c = L.PgConfig()
+    c.dims = int(spec["dims"])
+    c.components = int(spec["components"])
+    for d in range(3):
+        c.nx[d] = int(spec["nx"][d]) if d < c.dims else 1
+        c.dx[d] = float(spec["dx"][d]) if d < c.dims else 1.0
+        bc = spec.get("bc", "periodic")
+        c.bc[d] = BC[bc[d] if isinstance(bc, (list, tuple)) else bc]
+    c.gamma = float(spec["gamma"])
+    c.reconstruction = RECON[spec.get("recon", "LINEAR")]
+    c.limiter = LIMITER[spec.get("limiter", "MC_LIM")]
+    c.riemann = RIEMANN[spec.get("solver", "hlld")]
+    c.time_stepping = STEPPING[spec.get("stepping", "RK2")]
+    c.divb = L.PG_CONSTRAINED_TRANSPORT if spec.get("ct", True) else L.PG_DIVB_NONE
+    c.emf_average = L.PG_UCT_HLL
+    c.precision = PRECISION[precision]
+    c.compute_mach = int(bool(compute_mach))
+    c.small_density = 1e-12
+    c.small_pressure = 1e-12
+    return c
+
+
+def _ptrs(arrs, n):
+    P = C.POINTER(C.c_double)
+    out = (P * n)()
+    for q, a in enumerate(arrs):
+        out[q] = a.ctypes.data_as(P) if a is not None else None
+    return out
+
+
+class Solver:
+    """One PLUTO domain resident on the GPU."""
+
+    def __init__(self, spec: dict, precision: str = "fp64", compute_mach: bool = False):
+        self.spec = dict(spec)
+        self.precision = precision
+        self.cfg = make_config(spec, precision, compute_mach)
+        self.dims = self.cfg.dims
+        self.ct = self.cfg.divb == L.PG_CONSTRAINED_TRANSPORT
+        self.nx = tuple(self.cfg.nx[d] for d in range(3))
+        h = C.c_void_p()
+        L.check(L.lib().pg_create(C.byref(self.cfg), C.byref(h)), "pg_create")
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None) and self.h.value:
+            L.lib().pg_destroy(self.h)
+            self.h = C.c_void_p()
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def face_shape(self, d):
+        nx, ny, nz = self.nx
+        return (nz + (d == 2), ny + (d == 1), nx + (d == 0))
+
+    # -- state transfer (interior layout, as in a .dbl dump) --
+    def upload(self, vc: np.ndarray, bs=(None, None, None)):
+        nx, ny, nz = self.nx
+        vc = np.ascontiguousarray(vc, dtype=np.float64).reshape(NVAR, nz, ny, nx)
+        keep = [np.ascontiguousarray(vc[q]) for q in range(NVAR)]
+        faces = [None, None, None]
+        if self.ct:
+            for d in range(self.dims):
+                faces[d] = np.ascontiguousarray(bs[d], dtype=np.float64).reshape(self.face_shape(d))
+        L.check(L.lib().pg_upload(self.h, _ptrs(keep, 8), _ptrs(faces, 3), L.PG_LAYOUT_INTERIOR),
+                "pg_upload")
+
+    def download(self):
+        nx, ny, nz = self.nx
+        vc = np.zeros((NVAR, nz, ny, nx))
+        views = [vc[q] for q in range(NVAR)]
+        faces = [np.zeros(self.face_shape(d)) if (self.ct and d < self.dims) else None
+                 for d in range(3)]
+        L.check(L.lib().pg_download(self.h, _ptrs(views, 8), _ptrs(faces, 3),
+                                    L.PG_LAYOUT_INTERIOR), "pg_download")
+        return vc, faces
+
+    # -- stepping --
+    def advance(self, dt: float):
+        info = L.PgStepInfo()
+        L.check(L.lib().pg_advance(self.h, float(dt), C.byref(info)), "pg_advance")
+        return info.inv_dt_hyp, info.max_mach, info.nfail
+
+    def run(self, nsteps: int, first_dt: float, cfl: float, cfl_max_var: float = 1.1):
+        t = C.c_double()
+        dt = C.c_double()
+        L.check(L.lib().pg_run(self.h, int(nsteps), float(first_dt), float(cfl),
+                               float(cfl_max_var), C.byref(t), C.byref(dt)), "pg_run")
+        return t.value, dt.value
+
+    def run_async(self, nsteps: int, first_dt: float, cfl: float, cfl_max_var: float = 1.1):
+        L.check(L.lib().pg_run_async(self.h, int(nsteps), float(first_dt), float(cfl),
+                                     float(cfl_max_var)), "pg_run_async")
+
+    def sync(self):
+        L.check(L.lib().pg_sync(self.h), "pg_sync")
+
+    def info(self):
+        inf = L.PgStepInfo()
+        t = C.c_double()
+        dt = C.c_double()
+        L.check(L.lib().pg_get_info(self.h, C.byref(inf), C.byref(t), C.byref(dt)), "pg_get_info")
+        return dict(inv_dt_hyp=inf.inv_dt_hyp, max_mach=inf.max_mach, nfail=inf.nfail,
+                    time=t.value, dt=dt.value)
+
+    def stream(self) -> int:
+        p = C.c_void_p()
+        L.check(L.lib().pg_get_stream(self.h, C.byref(p)), "pg_get_stream")
+        return p.value or 0
+
+    def launches_per_step(self) -> int:
+        return int(L.lib().pg_kernel_launches_per_step(self.h))

@@ -1,0 +1,68 @@
+"""The C ABI library builds, loads and exports every declared entry point.
+
+No compute call is made here (no GPU on the build machine): only symbol
+presence, the ABI version and argument validation, which runs before any
+CUDA call.
+"""
+import ctypes as C
+import re
+from pathlib import Path
+
+import pytest
+
+from pluto_gb300 import _lib as L
+from pluto_gb300.solver import make_config
+
+ROOT = Path(__file__).resolve().parents[1]
+
+
+def declared_symbols():
+    names = set()
+    for h in (ROOT / "include").glob("*.h"):
+        names |= set(re.findall(r"^\s*(?:int|void|const\s+char\s*\*)\s*\**\s*(pg_\w+)\s*\(", h.read_text(), re.M))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    L.build()
+    return L.lib()
+
+
+def test_header_declares_expected_symbols():
+    assert set(L.EXPORTS) <= set(declared_symbols())
+
+
+def test_every_declared_symbol_is_exported(lib):
+    for name in declared_symbols():
+        assert hasattr(lib, name), name
+
+
+def test_abi_version(lib):
+    assert lib.pg_abi_version() == 1
+
+
+@pytest.mark.parametrize("field,value", [("dims", 4), ("components", 1), ("gamma", 1.0),
+                                         ("riemann", 7), ("time_stepping", 5), ("precision", 9)])
+def test_invalid_config_rejected_before_any_cuda_call(lib, field, value):
+    spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1.0), gamma=5 / 3)
+    cfg = make_config(spec)
+    setattr(cfg, field, value)
+    h = C.c_void_p()
+    rc = lib.pg_create(C.byref(cfg), C.byref(h))
+    assert rc == 1 and not h.value
+    assert lib.pg_last_error()
+
+
+def test_ct_requires_periodic_and_2d(lib):
+    spec = dict(dims=1, components=3, nx=(64, 1, 1), dx=(1 / 64, 1, 1), gamma=2.0, ct=True)
+    h = C.c_void_p()
+    assert lib.pg_create(C.byref(make_config(spec)), C.byref(h)) == 1
+    spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1), gamma=5 / 3, ct=True,
+                bc="outflow")
+    assert lib.pg_create(C.byref(make_config(spec)), C.byref(h)) == 1
+
+
+def test_missing_library_fails_loudly(tmp_path):
+    with pytest.raises(OSError):
+        L.load(tmp_path / "libpluto_gb300.so")

@@ -1,0 +1,155 @@
+"""FP64 CUDA path vs the reference (golden dumps) and vs the CPU oracle.
+
+Bar: relative L1 <= 1e-10 per variable after the fixed number of steps
+(the FP64 path is built without FMA contraction and is expected to agree
+bit for bit, which ``test_fp64_bitwise_on_goldens`` checks).
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_NAMES, load_golden, rel_l1
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+
+
+def _solver(meta, precision="fp64", **kw):
+    from pluto_gb300 import Solver
+    return Solver(meta, precision=precision, **kw)
+
+
+def _errors(vc, bs, vc_ref, bs_ref):
+    errs = {f"v{q}": rel_l1(vc[q], vc_ref[q]) for q in range(8)}
+    for d in range(3):
+        if bs_ref[d] is not None:
+            errs[f"b{d}"] = rel_l1(bs[d], bs_ref[d])
+    return errs
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_fp64_matches_reference_goldens(name):
+    meta, vc0, bs0, vc1, bs1 = load_golden(name)
+    s = _solver(meta)
+    s.upload(vc0, bs0)
+    t, _ = s.run(meta["steps"], meta["first_dt"], meta["cfl"])
+    vc, bs = s.download()
+    errs = _errors(vc, bs, vc1, bs1)
+    assert max(errs.values()) <= TOL, errs
+    assert abs(t - meta["t_final"]) <= 1e-6 * meta["t_final"]
+
+
+@pytest.mark.parametrize("name", ["ot_hlld_32", "blast_16", "tube_0_256", "turb_12", "blast_floor_16"])
+def test_fp64_bitwise_on_goldens(name):
+    meta, vc0, bs0, vc1, bs1 = load_golden(name)
+    s = _solver(meta)
+    s.upload(vc0, bs0)
+    s.run(meta["steps"], meta["first_dt"], meta["cfl"])
+    vc, bs = s.download()
+    assert np.array_equal(vc, vc1)
+    for d in range(3):
+        if bs1[d] is not None:
+            assert np.array_equal(bs[d], bs1[d])
+
+
+def test_advance_matches_oracle_step_by_step():
+    """pg_advance (the AdvanceStep drop-in): host dt in, invDt_hyp out."""
+    from oracle.oracle import Oracle
+    meta, vc0, bs0, _, _ = load_golden("blast_floor_16")
+    s = _solver(meta)
+    o = Oracle(meta, nthreads=4)
+    s.upload(vc0, bs0)
+    o.set_state(vc0, bs0)
+    dt = meta["first_dt"]
+    for step in range(6):
+        inv_g, _, nf_g = s.advance(dt)
+        inv_o, _, nf_o = o.advance(dt)
+        assert inv_g == inv_o, (step, inv_g, inv_o)
+        assert nf_g == nf_o
+        dt = min((1.0 / inv_o) * meta["cfl"], 1.1 * dt)
+    vc, bs = s.download()
+    vo, bo = o.get_state()
+    assert np.array_equal(vc, vo)
+
+
+def _random_blast(n, seed):
+    rng = np.random.default_rng(seed)
+    x = (np.arange(n) + 0.5) / n - 0.5
+    Z, Y, X = np.meshgrid(x, x, x, indexing="ij")
+    r = np.sqrt(X**2 + Y**2 + Z**2)
+    vc = np.zeros((8, n, n, n))
+    vc[0] = 1.0 + 0.1 * rng.random((n, n, n))
+    vc[7] = np.where(r < 0.15, 10.0, 0.1) * (1 + 0.05 * rng.random((n, n, n)))
+    vc[1:4] = 0.2 * (rng.random((3, n, n, n)) - 0.5)
+    b0 = 10.0 / np.sqrt(3.0) / np.sqrt(4 * np.pi)
+    bs = [np.full((n, n, n + 1), b0), np.full((n, n + 1, n), b0), np.full((n + 1, n, n), b0)]
+    vc[4] = 0.5 * (bs[0][:, :, 1:] + bs[0][:, :, :-1])
+    vc[5] = 0.5 * (bs[1][:, 1:, :] + bs[1][:, :-1, :])
+    vc[6] = 0.5 * (bs[2][1:, :, :] + bs[2][:-1, :, :])
+    spec = dict(dims=3, components=3, nx=(n, n, n), dx=(1 / n, 1 / n, 1 / n), gamma=5 / 3,
+                recon="LINEAR", limiter="MC_LIM", solver="hlld", stepping="RK2", ct=True,
+                bc="periodic")
+    return spec, vc, bs
+
+
+@pytest.mark.parametrize("solver,recon,stepping", [("hlld", "LINEAR", "RK2"), ("hll", "PARABOLIC", "RK3"),
+                                                   ("hlld", "PARABOLIC", "RK2")])
+def test_fp64_vs_oracle_random_3d(solver, recon, stepping):
+    from oracle.oracle import Oracle
+    spec, vc, bs = _random_blast(24, seed=7)
+    spec.update(solver=solver, recon=recon, stepping=stepping)
+    s = _solver(spec)
+    o = Oracle(spec, nthreads=4)
+    s.upload(vc, bs)
+    o.set_state(vc, bs)
+    s.run(4, 1e-3, 0.3)
+    o.run(4, 1e-3, 0.3)
+    a, ab = s.download()
+    b, bb = o.get_state()
+    errs = _errors(a, ab, b, bb)
+    assert max(errs.values()) <= TOL, errs
+
+
+def test_divergence_free_under_ct():
+    spec, vc, bs = _random_blast(24, seed=3)
+    s = _solver(spec)
+    s.upload(vc, bs)
+    s.run(8, 1e-3, 0.3)
+    _, b = s.download()
+    n = spec["nx"][0]
+    div = (b[0][:, :, 1:] - b[0][:, :, :-1] + b[1][:, 1:, :] - b[1][:, :-1, :] + b[2][1:, :, :] - b[2][:-1, :, :]) * n
+    bmag = np.abs(b[0]).max()
+    assert np.abs(div).max() * (1.0 / n) <= 1e-12 * bmag
+
+
+def test_fp64_deterministic():
+    spec, vc, bs = _random_blast(16, seed=11)
+    out = []
+    for _ in range(2):
+        s = _solver(spec)
+        s.upload(vc, bs)
+        s.run(3, 1e-3, 0.3)
+        out.append(s.download()[0])
+    assert np.array_equal(out[0], out[1])
+
+
+def test_upload_download_roundtrip():
+    spec, vc, bs = _random_blast(12, seed=5)
+    s = _solver(spec)
+    s.upload(vc, bs)
+    v2, b2 = s.download()
+    assert np.array_equal(v2, vc)
+    for d in range(3):
+        assert np.array_equal(b2[d], bs[d])
+
+
+def test_nan_state_reported_not_trapped():
+    """A corrupted state yields an error status from the step, not a fault."""
+    from pluto_gb300._lib import PgError
+    spec, vc, bs = _random_blast(12, seed=5)
+    vc[7, 3, 3, 3] = np.nan
+    s = _solver(spec)
+    s.upload(vc, bs)
+    with pytest.raises(PgError) as e:
+        s.advance(1e-3)
+    assert e.value.code == 4
