@@ -1,0 +1,405 @@
+#!/usr/bin/env python3
+"""Benchmark: MHD zone-updates/s of the unsplit ideal-MHD step on one GB300.
+
+Workload (the configuration the headline metric is quoted on): 3D MHD blast
+wave, 512^3 zones on [-0.5,0.5]^3, periodic, PLM/MC + HLLD + RK2, CFL 0.3,
+constrained transport (UCT_HLL).  A zone-update is one zone advanced by one
+full step (both RK stages).  The headline ``value`` is the mixed-precision
+path (FP32 storage and fluxes, FP64 accumulation / pressure recovery /
+face-field update / dt reduction); the plain FP64 path, the per-variable L1
+error of mixed against FP64, the roofline of the dominant kernel, the
+end-to-end rate through the C ABI with host buffers, and the CPU oracle's
+rate on the host cores are reported beside it.
+
+    python bench.py [--gpus N] [--steps K] [--warmup W] [--impl reference]
+
+Under torchrun (N>1) every rank runs an independent replica (the step has no
+data-path exchange on one GPU per box); value = N*zones*K / max over ranks.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+PEAKS = {"hbm_gbs": 6782.1}
+try:
+    PEAKS.update(json.loads((ROOT / "MEASURED_PEAKS.json").read_text()))
+    PEAK_SRC = "measured"
+except Exception:
+    PEAK_SRC = "fallback"
+
+METRIC = "MHD zone-updates/s on 1 GB300: mixed vs FP64 at L1 err <=1e-5; % of HBM peak"
+
+
+# ---------------------------------------------------------------------------
+# distributed plumbing (replicas only)
+# ---------------------------------------------------------------------------
+def dist_init():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    if ws > 1:
+        import torch
+        import torch.distributed as dist
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        local = int(os.environ.get("LOCAL_RANK", "0"))
+        torch.cuda.set_device(local)
+        os.environ["CUDA_VISIBLE_DEVICES_LOCAL"] = str(local)
+        dist.init_process_group("nccl")
+    return rank, ws
+
+
+def barrier(ws):
+    if ws > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def allmax(x, ws):
+    if ws <= 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ---------------------------------------------------------------------------
+# clocks sampled during the timed region
+# ---------------------------------------------------------------------------
+class Clocks:
+    Q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+         "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+         "clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index=0):
+        self.index = index
+        self.p = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.p = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={self.Q}",
+                                       "--format=csv,noheader,nounits", "-lms", "100"],
+                                      stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except Exception:
+            self.p = None
+        return self
+
+    def _read(self):
+        for line in self.p.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.p:
+            self.p.terminate()
+            try:
+                self.p.wait(timeout=5)
+            except Exception:
+                self.p.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], [], set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 7:
+                continue
+            try:
+                sm.append(float(f[0]))
+                mx.append(float(f[1]))
+            except ValueError:
+                continue
+            for nm, val in zip(names, f[3:7]):
+                if val.lower().startswith("active"):
+                    reasons.add(nm)
+        if not sm:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": [], "samples": 0}
+        return {"sm_mhz": statistics.median(sm), "sm_max_mhz": max(mx), "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+# algorithmic bytes of the mixed kernels (FP32 storage), per cell of the box
+# a launch covers; see DESIGN.md "Roofline accounting"
+# ---------------------------------------------------------------------------
+def kernel_bytes(name, n, stage_mix=True):
+    """Compulsory HBM bytes of one launch of kernel family ``name`` on an n^3
+    periodic grid (state words read once, results written once)."""
+    cells = n ** 3
+    ext = (n + 2) * (n + 2) * n       # transverse-extended sweep box
+    edges = (n + 1) ** 3
+    per = {
+        "mixed_sweep_x": (ext, 32 + 4 + 20 + 2 + 8 + 12),
+        "mixed_sweep_y": (ext, 32 + 4 + 40 + 4 + 8 + 12),
+        "mixed_sweep_z": (ext, 32 + 4 + 40 + 4 + 8 + 12),
+        "mixed_emf": (edges, 24 + 36 + 12 + 12 + 12),
+        "mixed_face": (edges, 12 + 12 + 6 + 12),
+        "mixed_final": (cells, 32 + 20 + 12 + 16 + 2 + 32),
+    }
+    if name not in per:
+        return None
+    units, b = per[name]
+    return units * b
+
+
+# ---------------------------------------------------------------------------
+# CPU baseline: the oracle (plain-C restatement of the reference path)
+# ---------------------------------------------------------------------------
+def cpu_rate(n=96, budget_s=12.0, threads=None):
+    from oracle.oracle import Oracle
+    from pluto_gb300 import problems
+    threads = threads or os.cpu_count() or 1
+    spec, vc, faces = problems.blast3d(n)
+    o = Oracle(spec, nthreads=threads)
+    o.set_state(vc, faces)
+    t0 = time.perf_counter()
+    o.advance(1e-4)
+    one = time.perf_counter() - t0
+    steps = max(1, min(50, int(budget_s / max(one, 1e-3))))
+    t0 = time.perf_counter()
+    dt = 1e-4
+    for _ in range(steps):
+        inv, _, _ = o.advance(dt)
+        dt = min((1.0 / inv) * spec["cfl"], 1.1 * dt)
+    el = time.perf_counter() - t0
+    return dict(value=n ** 3 * steps / el, unit="zone-updates/s", cores=threads, kind="port",
+                sample=f"oracle (C restatement of the reference path, OpenMP over pencils) on the "
+                       f"same blast scheme at {n}^3 for {steps} steps, {threads} host threads")
+
+
+def reference_arm(args, rank, ws):
+    """--impl reference: the reference algorithm on the host cores.  The
+    reference C binary cannot be built on the GPU machine (its source tree is not
+    there), so the oracle port -- bit-identical to it on the golden problems --
+    is timed, with all host threads, one bounded sample per step."""
+    if rank != 0:
+        return
+    from oracle.oracle import Oracle, build as obuild
+    from pluto_gb300 import problems
+    obuild()
+    n = args.ref_n
+    threads = os.cpu_count() or 1
+    spec, vc, faces = problems.blast3d(n)
+    o = Oracle(spec, nthreads=threads)
+    o.set_state(vc, faces)
+    dt = 1e-4
+    for _ in range(args.warmup):
+        inv, _, _ = o.advance(dt)
+        dt = min((1.0 / inv) * spec["cfl"], 1.1 * dt)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        inv, _, _ = o.advance(dt)
+        dt = min((1.0 / inv) * spec["cfl"], 1.1 * dt)
+    el = time.perf_counter() - t0
+    v = n ** 3 * args.steps / el
+    out = {"metric": METRIC, "value": v, "unit": "zone-updates/s", "impl": "reference", "n_gpus": ws,
+           "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1e3 * el / args.steps,
+           "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+           "data": "synthetic (blast IC generated in-process)",
+           "config": {"workload": f"3D MHD blast, PLM/MC + HLLD + RK2 + CT(UCT_HLL), CFL 0.3; "
+                                  f"timed sample {n}^3 per step (512^3 is the GPU arm's grid)",
+                      "grid": [n, n, n]},
+           "cpu_baseline": {"value": v, "unit": "zone-updates/s", "cores": threads, "kind": "port",
+                            "sample": f"oracle port, {n}^3, one step per bench step"},
+           "e2e": {"value": v, "unit": "zone-updates/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(out), flush=True)
+
+
+# ---------------------------------------------------------------------------
+# main GPU arm
+# ---------------------------------------------------------------------------
+def rel_l1(a, b):
+    den = np.abs(b).sum()
+    return float(np.abs(a - b).sum() / den) if den > 0 else float(np.abs(a - b).sum())
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=30)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--n", type=int, default=512)
+    ap.add_argument("--fp64-steps", type=int, default=3)
+    ap.add_argument("--l1-steps", type=int, default=100)
+    ap.add_argument("--l1-n", type=int, default=512)
+    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--ref-n", type=int, default=96)
+    ap.add_argument("--no-cpu", action="store_true")
+    args = ap.parse_args()
+    rank, ws = dist_init()
+    if args.impl == "reference":
+        reference_arm(args, rank, ws)
+        return
+    assert args.warmup >= 3, "at least 3 warm-up steps"
+
+    from pluto_gb300 import Solver, problems
+    from pluto_gb300 import build as pbuild
+    pbuild.build()
+
+    n = args.n
+    spec, vc, faces = problems.blast3d(n)
+    cfl, first_dt = spec["cfl"], spec["first_dt"]
+    cells = n ** 3
+
+    # ---- mixed precision, resident inputs (headline value) ----
+    mx = Solver(spec, precision="mixed")
+    mx.upload(vc, faces)
+    mx.run(args.warmup, first_dt, cfl)
+    launches = mx.launches_per_step()
+    barrier(ws)
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ms = mx.run_timed(args.steps, 0.0, cfl)
+    barrier(ws)
+    ms = allmax(ms, ws)
+    value = ws * cells * args.steps / (ms / 1e3)
+    clocks = clk.summary()
+
+    # ---- per-kernel profile of the mixed step (events on the solver stream) ----
+    prof = mx.profile_kernels(2, 0.0, cfl)
+    tot = sum(t for t, _ in prof.values())
+    dom_name = max(prof, key=lambda k: prof[k][0])
+    dom_ms, dom_cnt = prof[dom_name]
+    avg_ms = dom_ms / dom_cnt
+    alg = kernel_bytes(dom_name, n)
+    achieved = alg / (avg_ms / 1e3) / 1e9 if alg else None
+    traffic = None
+    tfile = ROOT / "profiles" / "traffic.json"
+    if tfile.exists():
+        try:
+            t = json.loads(tfile.read_text())
+            if t.get("kernel") == dom_name:
+                traffic = t["bytes_per_unit"] * (n + 2) * (n + 2) * n if "sweep" in dom_name else \
+                    t["bytes_per_unit"] * cells
+        except Exception:
+            traffic = None
+    mx_info = mx.info()
+    del mx
+
+    # ---- plain FP64 path on the same workload ----
+    f64 = Solver(spec, precision="fp64")
+    f64.upload(vc, faces)
+    f64.run(1, first_dt, cfl)
+    ms64 = f64.run_timed(args.fp64_steps, 0.0, cfl)
+    ms64 = allmax(ms64, ws)
+    value64 = ws * cells * args.fp64_steps / (ms64 / 1e3)
+    fp64_prof = f64.profile_kernels(1, 0.0, cfl)
+    del f64
+
+    # ---- L1 error of mixed vs FP64 after l1_steps from the same IC ----
+    l1 = None
+    if args.l1_steps > 0 and rank == 0:
+        if args.l1_n != n:
+            spec_l, vc_l, faces_l = problems.blast3d(args.l1_n)
+        else:
+            spec_l, vc_l, faces_l = spec, vc, faces
+        a = Solver(spec_l, precision="fp64")
+        a.upload(vc_l, faces_l)
+        a.run(args.l1_steps, first_dt, cfl)
+        ra, rb = a.download()
+        nf64 = a.info()["nfail"]
+        del a
+        b = Solver(spec_l, precision="mixed")
+        b.upload(vc_l, faces_l)
+        b.run(args.l1_steps, first_dt, cfl)
+        ma, mb = b.download()
+        del b
+        names = ["rho", "vx1", "vx2", "vx3", "Bx1", "Bx2", "Bx3", "prs"]
+        per = {names[q]: rel_l1(ma[q], ra[q]) for q in range(8)}
+        for d in range(3):
+            per[f"Bx{d+1}s"] = rel_l1(mb[d], rb[d])
+        l1 = {"steps": args.l1_steps, "grid": args.l1_n, "per_variable": per,
+              "max": max(per.values()), "bar": 1e-5}
+        del ra, rb, ma, mb
+
+    # ---- e2e through the C ABI with host buffers (pg_upload + pg_advance + pg_download) ----
+    e2e = None
+    if args.e2e_steps > 0:
+        try:
+            import torch
+            pin = [torch.from_numpy(np.ascontiguousarray(vc[q])).pin_memory().numpy() for q in range(8)]
+            pinf = [torch.from_numpy(np.ascontiguousarray(f)).pin_memory().numpy() for f in faces]
+        except Exception:
+            pin = [np.ascontiguousarray(vc[q]) for q in range(8)]
+            pinf = [np.ascontiguousarray(f) for f in faces]
+        host_vc = np.stack(pin)
+        e = Solver(spec, precision="mixed")
+        e.upload(host_vc, pinf)
+        e.advance(first_dt)  # warm
+        barrier(ws)
+        t0 = time.perf_counter()
+        e.upload(host_vc, pinf)
+        dt = first_dt
+        for _ in range(args.e2e_steps):
+            inv, _, _ = e.advance(dt)
+            dt = min((1.0 / inv) * cfl, 1.1 * dt)
+        out_vc, out_b = e.download()
+        el = time.perf_counter() - t0
+        el = allmax(el, ws)
+        del e
+        state_bytes = 8 * (8 * cells + sum(f.size for f in faces))
+        e2e = {"value": ws * cells * args.e2e_steps / el, "unit": "zone-updates/s",
+               "h2d_bytes_per_step": int(state_bytes / args.e2e_steps + 8),
+               "d2h_bytes_per_step": int(state_bytes / args.e2e_steps + 48),
+               "path": "pg_upload (pinned host, FP64) + pg_advance per step (host dt in, invDt out, "
+                       "synchronous) + pg_download", "steps": args.e2e_steps}
+
+    cpu = None
+    if rank == 0 and not args.no_cpu:
+        try:
+            cpu = cpu_rate()
+        except Exception as ex:  # the oracle needs gcc on the host
+            cpu = {"value": None, "unit": "zone-updates/s", "cores": 0, "kind": "port",
+                   "sample": f"unavailable: {ex}"}
+
+    if rank != 0:
+        return
+    peak = PEAKS.get("hbm_gbs", 6782.1)
+    algo_bytes_zu = 55 * 4  # 5W words of FP32, W = NVAR + DIMENSIONS = 11
+    out = {
+        "metric": METRIC, "value": value, "unit": "zone-updates/s", "n_gpus": ws, "steps": args.steps,
+        "warmup": args.warmup, "ms_per_step": ms / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f32 storage/fluxes + f64 accumulation",
+        "data": "synthetic (blast IC generated in-process, seedless)",
+        "config": {"workload": "3D MHD blast 512^3 periodic, PLM/MC + HLLD + RK2 + CT(UCT_HLL), CFL 0.3",
+                   "grid": [n, n, n], "precision": "mixed",
+                   "l2": "inputs larger than L2: ~27 GB working set vs 129 MB L2, no flush needed"},
+        "fp64": {"value": value64, "unit": "zone-updates/s", "steps": args.fp64_steps,
+                 "ms_per_step": ms64 / args.fp64_steps,
+                 "speedup_mixed_over_fp64": value / value64,
+                 "dominant_kernel": max(fp64_prof, key=lambda k: fp64_prof[k][0])},
+        "l1_mixed_vs_fp64": l1,
+        "hbm_fraction_algorithmic": value * algo_bytes_zu / (peak * 1e9),
+        "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
+                     "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
+                     "traffic": traffic, "avg_launch_ms": avg_ms, "launches": dom_cnt,
+                     "share_of_step": dom_ms / tot if tot else None, "peak_source": PEAK_SRC,
+                     "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()}},
+        "clocks": clocks,
+        "e2e": e2e,
+        "gpu_launches": launches * args.steps,
+        "floors_in_timed_run": mx_info.get("nfail"),
+        "cpu_baseline": cpu,
+    }
+    print(json.dumps(out), flush=True)
+
+
+if __name__ == "__main__":
+    main()

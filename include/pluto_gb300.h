@@ -115,6 +115,18 @@ int pg_run(pg_solver *s, int nsteps, double first_dt, double cfl, double cfl_max
 int pg_run_async(pg_solver *s, int nsteps, double first_dt, double cfl, double cfl_max_var);
 int pg_sync(pg_solver *s);
 
+/* Timing: run nsteps as in pg_run_async and return the elapsed time between
+   two CUDA events recorded on the solver's stream around the launches. */
+int pg_run_timed(pg_solver *s, int nsteps, double first_dt, double cfl, double cfl_max_var,
+                 double *elapsed_ms);
+
+/* Per-kernel profile of nsteps eagerly launched steps: CUDA events around
+   every launch, aggregated per kernel family.  names receives n_kernels
+   NUL-terminated strings of name_stride bytes each. */
+int pg_profile_kernels(pg_solver *s, int nsteps, double first_dt, double cfl, double cfl_max_var,
+                       char *names, int name_stride, double *total_ms, int *launches,
+                       int max_kernels, int *n_kernels);
+
 /* Diagnostics */
 int pg_get_stream(pg_solver *s, void **cuda_stream);
 int pg_get_info(pg_solver *s, pg_step_info *info, double *time, double *dt);

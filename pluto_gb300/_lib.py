@@ -28,8 +28,8 @@ ERRORS = {1: "PG_ERR_INVALID", 2: "PG_ERR_CUDA", 3: "PG_ERR_NOMEM", 4: "PG_ERR_N
 
 # Every symbol declared in include/pluto_gb300.h (checked by the CPU tests).
 EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
-           "pg_run_async", "pg_sync", "pg_get_stream", "pg_get_info",
-           "pg_kernel_launches_per_step", "pg_last_error", "pg_abi_version"]
+           "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
+           "pg_get_info", "pg_kernel_launches_per_step", "pg_last_error", "pg_abi_version"]
 
 
 class PgConfig(C.Structure):
@@ -79,13 +79,16 @@ def lib():
     L.pg_run.argtypes = [vp, ip, C.c_double, C.c_double, C.c_double, dp, dp]
     L.pg_run_async.argtypes = [vp, ip, C.c_double, C.c_double, C.c_double]
     L.pg_sync.argtypes = [vp]
+    L.pg_run_timed.argtypes = [vp, ip, C.c_double, C.c_double, C.c_double, dp]
+    L.pg_profile_kernels.argtypes = [vp, ip, C.c_double, C.c_double, C.c_double, C.c_char_p, ip, dp,
+                                     C.POINTER(C.c_int), ip, C.POINTER(C.c_int)]
     L.pg_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.pg_get_info.argtypes = [vp, C.POINTER(PgStepInfo), dp, dp]
     L.pg_kernel_launches_per_step.argtypes = [vp]
     L.pg_last_error.restype = C.c_char_p
     for fn in ("pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
-               "pg_run_async", "pg_sync", "pg_get_stream", "pg_get_info",
-               "pg_kernel_launches_per_step", "pg_abi_version"):
+               "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
+               "pg_get_info", "pg_kernel_launches_per_step", "pg_abi_version"):
         getattr(L, fn).restype = C.c_int
     _lib = L
     return L

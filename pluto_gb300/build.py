@@ -25,7 +25,7 @@ COMMON = ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC", "-I", str(ROO
 UNITS = {
     "pg_api.cu": [],
     "pg_fp64.cu": ["--fmad=false"],
-    "pg_mixed.cu": [],
+    "pg_mixed.cu": ["--use_fast_math"],
     "pg_batch.cu": [],
     "pg_adjoint.cu": ["--fmad=false"],
 }

@@ -381,3 +381,95 @@ extern "C" int pg_kernel_launches_per_step(pg_solver* h) {
   cudaGraphDestroy(gr);
   return kernels;
 }
+
+// -------------------------------------------------------------------------
+// timing and per-kernel profile (CUDA events on the solver's stream)
+// -------------------------------------------------------------------------
+namespace pg {
+void prof_mark(Solver* S, const char* name, bool begin) {
+  Prof* P = S->prof;
+  if (begin) P->names.push_back(name);
+  if (P->used >= P->ev.size()) {
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    P->ev.push_back(e);
+  }
+  cudaEventRecord(P->ev[P->used++], S->stream);
+}
+}  // namespace pg
+
+extern "C" int pg_run_timed(pg_solver* h, int nsteps, double first_dt, double cfl, double cfl_max_var,
+                            double* elapsed_ms) {
+  if (!h || !elapsed_ms) return fail(PG_ERR_INVALID, "null argument");
+  Solver* S = &h->S;
+  // build the graph outside the timed region
+  if (!S->device_dt || S->cfl != cfl || S->cfl_max_var != cfl_max_var || S->graph_dirty) {
+    int rc = pg_run_async(h, 0, first_dt, cfl, cfl_max_var);
+    if (rc) return rc;
+    first_dt = 0;
+  }
+  cudaEvent_t e0, e1;
+  CK(cudaEventCreate(&e0));
+  CK(cudaEventCreate(&e1));
+  CK(cudaEventRecord(e0, S->stream));
+  int rc = pg_run_async(h, nsteps, first_dt, cfl, cfl_max_var);
+  CK(cudaEventRecord(e1, S->stream));
+  CK(cudaEventSynchronize(e1));
+  float ms = 0.f;
+  cudaEventElapsedTime(&ms, e0, e1);
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  *elapsed_ms = ms;
+  if (rc) return rc;
+  return read_scalars(S);
+}
+
+extern "C" int pg_profile_kernels(pg_solver* h, int nsteps, double first_dt, double cfl, double cfl_max_var,
+                                  char* names, int name_stride, double* total_ms, int* launches, int max_kernels,
+                                  int* n_kernels) {
+  if (!h || !names || !total_ms || !launches || !n_kernels || name_stride < 8)
+    return fail(PG_ERR_INVALID, "null argument");
+  Solver* S = &h->S;
+  S->device_dt = true;
+  S->cfl = cfl;
+  S->cfl_max_var = cfl_max_var;
+  S->graph_dirty = true;
+  if (first_dt > 0) {
+    S->sc_host->dt = first_dt;
+    CK(cudaMemcpyAsync(&S->sc->dt, &S->sc_host->dt, sizeof(double), cudaMemcpyHostToDevice, S->stream));
+  }
+  Prof P;
+  S->prof = &P;
+  int rc = PG_OK;
+  for (int s = 0; s < nsteps && !rc; s++) rc = enqueue_step(S);
+  S->prof = nullptr;
+  CK(cudaStreamSynchronize(S->stream));
+  std::vector<std::string> uniq;
+  std::vector<double> tot;
+  std::vector<int> cnt;
+  for (size_t q = 0; q < P.names.size(); q++) {
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, P.ev[2 * q], P.ev[2 * q + 1]);
+    size_t u = 0;
+    while (u < uniq.size() && uniq[u] != P.names[q]) u++;
+    if (u == uniq.size()) {
+      uniq.push_back(P.names[q]);
+      tot.push_back(0.0);
+      cnt.push_back(0);
+    }
+    tot[u] += ms;
+    cnt[u] += 1;
+  }
+  for (cudaEvent_t e : P.ev) cudaEventDestroy(e);
+  int n = (int)uniq.size() < max_kernels ? (int)uniq.size() : max_kernels;
+  for (int u = 0; u < n; u++) {
+    strncpy(names + (size_t)u * name_stride, uniq[u].c_str(), name_stride - 1);
+    names[(size_t)u * name_stride + name_stride - 1] = 0;
+    total_ms[u] = tot[u];
+    launches[u] = cnt[u];
+  }
+  *n_kernels = n;
+  S->steps_done += nsteps;
+  if (rc) return rc;
+  return read_scalars(S);
+}

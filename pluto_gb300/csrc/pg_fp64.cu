@@ -546,21 +546,23 @@ static void launch_sweep(Solver* S, const F64Args& a, int stage) {
   const bool ct = a.ct;
   cudaStream_t st = S->stream;
   Box rb = sweep_box(g, DIR, -1, +1, ct);  // States on nbeg-1..nend+1
-  k_recon<DIR><<<grid_for(rb.count()), kThreads, 0, st>>>(a, rb);
+  PG_LAUNCH(S, "fp64_recon", (k_recon<DIR><<<grid_for(rb.count()), kThreads, 0, st>>>(a, rb)));
   Box ib = sweep_box(g, DIR, -1, 0, ct);   // Riemann on nbeg-1..nend
   int want1d = g.dims == 1;
   const bool mach = S->cfg.compute_mach != 0;
   unsigned gr = grid_for(ib.count(), 128);
-  if (S->cfg.riemann == PG_HLL) {
-    if (mach) k_riemann<DIR, PG_HLL, true><<<gr, 128, 0, st>>>(a, ib, want1d);
-    else k_riemann<DIR, PG_HLL, false><<<gr, 128, 0, st>>>(a, ib, want1d);
-  } else {
-    if (mach) k_riemann<DIR, PG_HLLD, true><<<gr, 128, 0, st>>>(a, ib, want1d);
-    else k_riemann<DIR, PG_HLLD, false><<<gr, 128, 0, st>>>(a, ib, want1d);
-  }
+  PG_LAUNCH(S, "fp64_riemann", {
+    if (S->cfg.riemann == PG_HLL) {
+      if (mach) k_riemann<DIR, PG_HLL, true><<<gr, 128, 0, st>>>(a, ib, want1d);
+      else k_riemann<DIR, PG_HLL, false><<<gr, 128, 0, st>>>(a, ib, want1d);
+    } else {
+      if (mach) k_riemann<DIR, PG_HLLD, true><<<gr, 128, 0, st>>>(a, ib, want1d);
+      else k_riemann<DIR, PG_HLLD, false><<<gr, 128, 0, st>>>(a, ib, want1d);
+    }
+  });
   Box ub = sweep_box(g, DIR, 0, 0, ct);    // RHS/update on nbeg..nend
   int cdt_mode = (g.dims > 1 && stage == 1) ? (DIR == 0 ? 1 : 2) : 0;
-  k_update<DIR><<<grid_for(ub.count()), kThreads, 0, st>>>(a, ub, cdt_mode);
+  PG_LAUNCH(S, "fp64_update", (k_update<DIR><<<grid_for(ub.count()), kThreads, 0, st>>>(a, ub, cdt_mode)));
 }
 
 template <int STAGE, int NSTAGE>
@@ -573,11 +575,11 @@ static void launch_stage_tail(Solver* S, const F64Args& a, const Box& dom) {
       if (ax < g.dims) { eb.lo[ax] = g.beg[ax] - 1; eb.hi[ax] = g.end[ax]; }
       else { eb.lo[ax] = eb.hi[ax] = 0; }
     }
-    k_emf<<<grid_for(eb.count(), 128), 128, 0, st>>>(a, eb);
-    k_ct_update<STAGE, NSTAGE><<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb);
+    PG_LAUNCH(S, "fp64_emf", (k_emf<<<grid_for(eb.count(), 128), 128, 0, st>>>(a, eb)));
+    PG_LAUNCH(S, "fp64_ct_update", (k_ct_update<STAGE, NSTAGE><<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb)));
   }
   int reduce = (STAGE == 1 && g.dims > 1);
-  k_finalize<STAGE, NSTAGE><<<grid_for(dom.count()), kThreads, 0, st>>>(a, dom, reduce);
+  PG_LAUNCH(S, "fp64_finalize", (k_finalize<STAGE, NSTAGE><<<grid_for(dom.count()), kThreads, 0, st>>>(a, dom, reduce)));
 }
 
 static void launch_bound(Solver* S, const F64Args& a) {
@@ -585,8 +587,8 @@ static void launch_bound(Solver* S, const F64Args& a) {
   long long n0 = g.dims > 0 ? 2LL * g.beg[0] * g.nt[1] * g.nt[2] : 0;
   long long n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
   long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
-  k_bound<<<grid_for(n0 + n1 + n2), kThreads, 0, S->stream>>>(a, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0,
-                                                               n1, n2);
+  PG_LAUNCH(S, "fp64_bound", (k_bound<<<grid_for(n0 + n1 + n2), kThreads, 0, S->stream>>>(
+                                   a, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0, n1, n2)));
 }
 
 template <int NSTAGE>
@@ -597,7 +599,7 @@ static void enqueue_rk(Solver* S, const F64Args& a) {
   cudaStream_t st = S->stream;
   // stage 1
   launch_bound(S, a);
-  k_begin_step<<<grid_for(g.ncell), kThreads, 0, st>>>(a, dom);
+  PG_LAUNCH(S, "fp64_begin_step", (k_begin_step<<<grid_for(g.ncell), kThreads, 0, st>>>(a, dom)));
   launch_sweep<0>(S, a, 1);
   if (g.dims > 1) launch_sweep<1>(S, a, 1);
   if (g.dims > 2) launch_sweep<2>(S, a, 1);
@@ -615,7 +617,7 @@ static void enqueue_rk(Solver* S, const F64Args& a) {
     if (g.dims > 2) launch_sweep<2>(S, a, 3);
     launch_stage_tail<3, NSTAGE>(S, a, dom);
   }
-  k_end_step<<<1, 1, 0, st>>>(a);
+  PG_LAUNCH(S, "fp64_end_step", (k_end_step<<<1, 1, 0, st>>>(a)));
 }
 
 int fp64_enqueue_step(Solver* S) {

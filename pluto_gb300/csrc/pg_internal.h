@@ -3,6 +3,8 @@
 #include <cuda_runtime.h>
 #include <cstddef>
 #include <cstdint>
+#include <string>
+#include <vector>
 
 #include "../../include/pluto_gb300.h"
 
@@ -54,7 +56,22 @@ struct DevScalars {
   int pad;
 };
 
+// Optional per-launch timing with CUDA events on the solver's stream.
+struct Prof {
+  std::vector<std::string> names;
+  std::vector<cudaEvent_t> ev;  // two events per launch
+  size_t used = 0;
+};
+
 struct Solver;
+void prof_mark(Solver* S, const char* name, bool begin);
+#define PG_LAUNCH(S, name, ...)                   \
+  do {                                            \
+    if ((S)->prof) prof_mark((S), (name), true);  \
+    __VA_ARGS__;                                  \
+    if ((S)->prof) prof_mark((S), (name), false); \
+  } while (0)
+
 int fp64_alloc(Solver* S);
 void fp64_free(Solver* S);
 int fp64_enqueue_step(Solver* S);  // all stages of one step on S->stream
@@ -94,6 +111,7 @@ struct Solver {
   // graph of one step
   cudaGraphExec_t graph = nullptr;
   bool graph_dirty = true;
+  Prof* prof = nullptr;
   double cfl = 0.4, cfl_max_var = 1.1;
   bool device_dt = false;  // kernels end each step by computing the next dt
   int steps_done = 0;

@@ -174,16 +174,21 @@ __global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_l
   const bool face_ok = i <= g.end[0];        // interfaces beg-1+1/2 .. end+1/2
   const long long c = cidx(g, k, j, i);
   float vL[NV], vR[NV], slope[3] = {0.f, 0.f, 0.f};
+  // Stencil reads: cell i needs i-1..i+1 (PLM) or i-2..i+2 (PPM); the right
+  // state of interface i+1/2 (cell i+1, only when face_ok) needs one more.
+  // With ng = 2 (PLM) / 3 (PPM) ghosts every read stays inside the row.
+  const bool ppm = a.recon == PG_PARABOLIC;
   if (cell_ok) {
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
       const float* V = a.Vin[nv];
-      float w2 = a.recon == PG_PARABOLIC ? ldg(V, c - 2) : 0.f;
-      float w1 = ldg(V, c - 1), v0 = ldg(V, c), e1 = ldg(V, c + 1), e2 = ldg(V, c + 2);
-      float e3 = a.recon == PG_PARABOLIC ? ldg(V, c + 3) : 0.f;
-      float vp, vm, vp1, vm1;
+      float w2 = ppm ? ldg(V, c - 2) : 0.f;
+      float w1 = ldg(V, c - 1), v0 = ldg(V, c), e1 = ldg(V, c + 1);
+      float e2 = (ppm || face_ok) ? ldg(V, c + 2) : 0.f;
+      float e3 = (ppm && face_ok) ? ldg(V, c + 3) : 0.f;
+      float vp, vm, vp1 = 0.f, vm1 = 0.f;
       recon_cell(a.recon, a.limiter, nv, w2, w1, v0, e1, e2, vp, vm);      // cell i
-      recon_cell(a.recon, a.limiter, nv, w1, v0, e1, e2, e3, vp1, vm1);    // cell i+1
+      if (face_ok) recon_cell(a.recon, a.limiter, nv, w1, v0, e1, e2, e3, vp1, vm1);  // cell i+1
       vL[nv] = vp;
       vR[nv] = vm1;
       if (nv >= VX1 && nv <= VX3) slope[nv - VX1] = vp - vm;
@@ -679,8 +684,8 @@ static void mlaunch_bound(Solver* S, const MixArgs& a) {
   long long n0 = 2LL * g.beg[0] * g.nt[1] * g.nt[2];
   long long n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
   long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
-  k_mbound<<<grid_for(n0 + n1 + n2), kThreads, 0, S->stream>>>(g, arr, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2],
-                                                                 n0, n1, n2);
+  PG_LAUNCH(S, "mixed_bound", (k_mbound<<<grid_for(n0 + n1 + n2), kThreads, 0, S->stream>>>(
+                                    g, arr, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0, n1, n2)));
 }
 
 static const int kSeg = 32;
@@ -699,8 +704,8 @@ static void mlaunch_sweeps(Solver* S, const MixArgs& a, int stage) {
     int nwx = (g.nx[0] + 2 + 30) / 31;
     long long nrows = (long long)t_n * b_n;
     long long threads = (long long)nwx * nrows * 32;
-    k_msweep_x<CT><<<grid_for(threads, 128), 128, 0, st>>>(a, solver, t_lo, t_n, b_lo, nrows, stage1,
-                                                              g.dims == 1, nwx);
+    PG_LAUNCH(S, "mixed_sweep_x", (k_msweep_x<CT><<<grid_for(threads, 128), 128, 0, st>>>(
+                                      a, solver, t_lo, t_n, b_lo, nrows, stage1, g.dims == 1, nwx)));
   }
   for (int dir = 1; dir < g.dims; dir++) {
     int i_lo = g.beg[0] - ext, i_n = g.nx[0] + 2 * ext;
@@ -709,11 +714,11 @@ static void mlaunch_sweeps(Solver* S, const MixArgs& a, int stage) {
     int nseg = (g.nx[dir] + kSeg - 1) / kSeg;
     long long threads = (long long)i_n * o_n * nseg;
     if (dir == 1)
-      k_msweep_yz<1, CT><<<grid_for(threads, 128), 128, 0, st>>>(a, solver, i_lo, i_n, o_lo, o_n, kSeg, nseg,
-                                                                   stage1, 0);
+      PG_LAUNCH(S, "mixed_sweep_y", (k_msweep_yz<1, CT><<<grid_for(threads, 128), 128, 0, st>>>(
+                                        a, solver, i_lo, i_n, o_lo, o_n, kSeg, nseg, stage1, 0)));
     else
-      k_msweep_yz<2, CT><<<grid_for(threads, 128), 128, 0, st>>>(a, solver, i_lo, i_n, o_lo, o_n, kSeg, nseg,
-                                                                   stage1, 0);
+      PG_LAUNCH(S, "mixed_sweep_z", (k_msweep_yz<2, CT><<<grid_for(threads, 128), 128, 0, st>>>(
+                                        a, solver, i_lo, i_n, o_lo, o_n, kSeg, nseg, stage1, 0)));
   }
 }
 
@@ -727,12 +732,12 @@ static void mlaunch_tail(Solver* S, const MixArgs& a, const Box& dom) {
       if (ax < g.dims) { eb.lo[ax] = g.beg[ax] - 1; eb.hi[ax] = g.end[ax]; }
       else { eb.lo[ax] = eb.hi[ax] = 0; }
     }
-    k_memf<<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb);
-    k_mface<STAGE, NSTAGE><<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb);
+    PG_LAUNCH(S, "mixed_emf", (k_memf<<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb)));
+    PG_LAUNCH(S, "mixed_face", (k_mface<STAGE, NSTAGE><<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb)));
   }
-  if (g.dims == 1) k_m1d_dt<<<grid_for(dom.count()), kThreads, 0, st>>>(a, dom);
+  if (g.dims == 1) PG_LAUNCH(S, "mixed_dt1d", (k_m1d_dt<<<grid_for(dom.count()), kThreads, 0, st>>>(a, dom)));
   int reduce = (STAGE == 1 && g.dims > 1);
-  k_mfinal<STAGE, NSTAGE><<<grid_for(dom.count()), kThreads, 0, st>>>(a, dom, reduce);
+  PG_LAUNCH(S, "mixed_final", (k_mfinal<STAGE, NSTAGE><<<grid_for(dom.count()), kThreads, 0, st>>>(a, dom, reduce)));
 }
 
 template <int NSTAGE>
@@ -745,7 +750,7 @@ static void menqueue(Solver* S) {
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
   // stage 1: A -> B
   MixArgs a1 = margs(S, A, B, A);
-  k_mbegin<<<grid_for(g.ncell), kThreads, 0, S->stream>>>(a1, g.ncell);
+  PG_LAUNCH(S, "mixed_begin", (k_mbegin<<<grid_for(g.ncell), kThreads, 0, S->stream>>>(a1, g.ncell)));
   mlaunch_bound(S, a1);
   if (ct) mlaunch_sweeps<true>(S, a1, 1); else mlaunch_sweeps<false>(S, a1, 1);
   mlaunch_tail<1, NSTAGE>(S, a1, dom);
@@ -755,7 +760,7 @@ static void menqueue(Solver* S) {
     mlaunch_bound(S, a2);
     if (ct) mlaunch_sweeps<true>(S, a2, 2); else mlaunch_sweeps<false>(S, a2, 2);
     mlaunch_tail<2, NSTAGE>(S, a2, dom);
-    k_mend_step<<<1, 1, 0, S->stream>>>(a2);
+    PG_LAUNCH(S, "mixed_end_step", (k_mend_step<<<1, 1, 0, S->stream>>>(a2)));
   } else {
     MixArgs a2 = margs(S, B, B, A);  // in place: the final kernel reads its own cell only
     mlaunch_bound(S, a2);
@@ -765,7 +770,7 @@ static void menqueue(Solver* S) {
     mlaunch_bound(S, a3);
     if (ct) mlaunch_sweeps<true>(S, a3, 3); else mlaunch_sweeps<false>(S, a3, 3);
     mlaunch_tail<3, NSTAGE>(S, a3, dom);
-    k_mend_step<<<1, 1, 0, S->stream>>>(a3);
+    PG_LAUNCH(S, "mixed_end_step", (k_mend_step<<<1, 1, 0, S->stream>>>(a3)));
   }
 }
 

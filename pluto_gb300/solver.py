@@ -128,6 +128,29 @@ class Solver:
         L.check(L.lib().pg_run_async(self.h, int(nsteps), float(first_dt), float(cfl),
                                      float(cfl_max_var)), "pg_run_async")
 
+    def run_timed(self, nsteps: int, first_dt: float, cfl: float, cfl_max_var: float = 1.1) -> float:
+        """Run nsteps; return milliseconds between CUDA events on the solver stream."""
+        ms = C.c_double()
+        L.check(L.lib().pg_run_timed(self.h, int(nsteps), float(first_dt), float(cfl),
+                                     float(cfl_max_var), C.byref(ms)), "pg_run_timed")
+        return ms.value
+
+    def profile_kernels(self, nsteps: int, first_dt: float, cfl: float, cfl_max_var: float = 1.1):
+        """Per-kernel-family device time (ms) and launch counts over nsteps eager steps."""
+        stride, cap = 64, 64
+        names = C.create_string_buffer(stride * cap)
+        tot = (C.c_double * cap)()
+        cnt = (C.c_int * cap)()
+        n = C.c_int()
+        L.check(L.lib().pg_profile_kernels(self.h, int(nsteps), float(first_dt), float(cfl),
+                                           float(cfl_max_var), names, stride, tot, cnt, cap,
+                                           C.byref(n)), "pg_profile_kernels")
+        out = {}
+        for u in range(n.value):
+            nm = names.raw[u * stride:(u + 1) * stride].split(b"\0", 1)[0].decode()
+            out[nm] = (tot[u], cnt[u])
+        return out
+
     def sync(self):
         L.check(L.lib().pg_sync(self.h), "pg_sync")
 

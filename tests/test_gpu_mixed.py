@@ -1,0 +1,79 @@
+"""Mixed-precision path (FP32 storage/fluxes, FP64 accumulation) vs FP64.
+
+Bar (the benchmark's): per-variable relative L1 <= 1e-5 against the FP64
+path on the 3D blast; looser bounds on the small golden problems, where a
+few FP32-rounded steps of strongly non-linear flows are compared with the
+reference binary directly.
+"""
+import numpy as np
+import pytest
+
+from conftest import GOLDEN_NAMES, load_golden, rel_l1
+
+pytestmark = pytest.mark.gpu
+
+
+def _s(spec, precision):
+    from pluto_gb300 import Solver
+    return Solver(spec, precision=precision)
+
+
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
+def test_mixed_close_to_reference_goldens(name):
+    meta, vc0, bs0, vc1, bs1 = load_golden(name)
+    s = _s(meta, "mixed")
+    s.upload(vc0, bs0)
+    s.run(meta["steps"], meta["first_dt"], meta["cfl"])
+    vc, bs = s.download()
+    errs = [rel_l1(vc[q], vc1[q]) for q in range(8) if np.abs(vc1[q]).sum() > 0]
+    tol = 5e-3 if "floor" in name else 2e-4
+    assert max(errs) <= tol, errs
+
+
+def test_mixed_vs_fp64_blast_l1():
+    from pluto_gb300 import problems
+    spec, vc, faces = problems.blast3d(48)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = _s(spec, prec)
+        s.upload(vc, faces)
+        s.run(40, spec["first_dt"], spec["cfl"])
+        out[prec] = s.download()
+    errs = {q: rel_l1(out["mixed"][0][q], out["fp64"][0][q]) for q in (0, 1, 2, 3, 4, 5, 6, 7)}
+    for d in range(3):
+        errs[f"b{d}"] = rel_l1(out["mixed"][1][d], out["fp64"][1][d])
+    assert max(errs.values()) <= 1e-5, errs
+
+
+def test_mixed_divergence_free_to_fp32_roundoff():
+    from pluto_gb300 import problems
+    spec, vc, faces = problems.blast3d(32)
+    s = _s(spec, "mixed")
+    s.upload(vc, faces)
+    s.run(20, spec["first_dt"], spec["cfl"])
+    _, b = s.download()
+    div = (np.diff(b[0], axis=2) + np.diff(b[1], axis=1) + np.diff(b[2], axis=0))
+    assert np.abs(div).max() <= 1e-5 * np.abs(b[0]).max()
+
+
+def test_mixed_upload_roundtrip_is_fp32_rounding():
+    from pluto_gb300 import problems
+    spec, vc, faces = problems.blast3d(16)
+    vc = vc + 1e-3 * np.random.default_rng(0).random(vc.shape)
+    s = _s(spec, "mixed")
+    s.upload(vc, faces)
+    v2, b2 = s.download()
+    assert np.array_equal(v2, vc.astype(np.float32).astype(np.float64))
+
+
+def test_mixed_rk3_ppm_turbulence_small():
+    from pluto_gb300 import problems
+    spec, vc, faces = problems.turbulence3d(24, seed=1)
+    out = {}
+    for prec in ("fp64", "mixed"):
+        s = _s(spec, prec)
+        s.upload(vc, faces)
+        s.run(10, spec["first_dt"], spec["cfl"])
+        out[prec] = s.download()[0]
+    errs = [rel_l1(out["mixed"][q], out["fp64"][q]) for q in range(8)]
+    assert max(errs) <= 1e-5, errs
