@@ -50,7 +50,11 @@ enum { PG_RK2 = 2, PG_RK3 = 3 };                                  /* TIME_STEPPI
 enum { PG_DIVB_NONE = 0, PG_CONSTRAINED_TRANSPORT = 1 };          /* DIVB_CONTROL */
 enum { PG_UCT_HLL = 4 };                                          /* CT_EMF_AVERAGE */
 enum { PG_PERIODIC = 0, PG_OUTFLOW = 1 };                         /* [Boundary] */
-enum { PG_FP64 = 0, PG_MIXED = 1 };                               /* arithmetic */
+/* arithmetic: PG_FP64 bit-compatible with the reference C path;
+   PG_MIXED FP32 storage and fluxes, FP64 accumulation / pressure recovery /
+   face update / dt reduction; PG_MIXED_DW the same with the FP64 parts done
+   as FP32 double-word pairs (48-bit significand) on the FP32 pipes. */
+enum { PG_FP64 = 0, PG_MIXED = 1, PG_MIXED_DW = 2 };
 enum { PG_LAYOUT_INTERIOR = 0, PG_LAYOUT_PLUTO = 1 };             /* host array layout */
 
 typedef struct {

@@ -20,7 +20,7 @@ PG_RK2, PG_RK3 = 2, 3
 PG_DIVB_NONE, PG_CONSTRAINED_TRANSPORT = 0, 1
 PG_UCT_HLL = 4
 PG_PERIODIC, PG_OUTFLOW = 0, 1
-PG_FP64, PG_MIXED = 0, 1
+PG_FP64, PG_MIXED, PG_MIXED_DW = 0, 1, 2
 PG_LAYOUT_INTERIOR, PG_LAYOUT_PLUTO = 0, 1
 
 ERRORS = {1: "PG_ERR_INVALID", 2: "PG_ERR_CUDA", 3: "PG_ERR_NOMEM", 4: "PG_ERR_NAN",

@@ -58,7 +58,8 @@ static int validate(const pg_config* c) {
   } else if (c->divb != PG_DIVB_NONE) {
     return fail(PG_ERR_INVALID, "unsupported divergence control");
   }
-  if (c->precision != PG_FP64 && c->precision != PG_MIXED) return fail(PG_ERR_INVALID, "unsupported precision");
+  if (c->precision != PG_FP64 && c->precision != PG_MIXED && c->precision != PG_MIXED_DW)
+    return fail(PG_ERR_INVALID, "unsupported precision");
   return PG_OK;
 }
 
@@ -201,7 +202,7 @@ extern "C" int pg_upload(pg_solver* h, const double* const vars[8], const double
   Solver* S = &h->S;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
   if (ct && !faces) return fail(PG_ERR_INVALID, "constrained transport needs staggered fields");
-  if (S->cfg.precision == PG_MIXED) return mixed_upload_host(S, vars, faces, layout);
+  if (S->cfg.precision != PG_FP64) return mixed_upload_host(S, vars, faces, layout);
   for (int nv = 0; nv < 8; nv++) {
     if (vars[nv]) {
       int rc = xfer_f64(S, S->V[nv], (double*)vars[nv], -1, layout, true);
@@ -225,7 +226,7 @@ extern "C" int pg_download(pg_solver* h, double* const vars[8], double* const fa
   if (layout != PG_LAYOUT_INTERIOR && layout != PG_LAYOUT_PLUTO) return fail(PG_ERR_INVALID, "bad layout");
   Solver* S = &h->S;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
-  if (S->cfg.precision == PG_MIXED) return mixed_download(S, vars, faces, layout);
+  if (S->cfg.precision != PG_FP64) return mixed_download(S, vars, faces, layout);
   for (int nv = 0; nv < 8; nv++)
     if (vars[nv]) {
       int rc = xfer_f64(S, S->V[nv], vars[nv], -1, layout, false);

@@ -54,6 +54,8 @@ struct DevScalars {
   unsigned long long nfail;        // floor events
   int status;                      // sticky device error flags
   int pad;
+  float dtdx[3];                   // FP32 dt/dx per axis for the mixed sweeps
+  float pad2;
 };
 
 // Optional per-launch timing with CUDA events on the solver's stream.

@@ -1,16 +1,18 @@
 // Mixed-precision path: FP32 storage and FP32 reconstruction / Riemann /
-// EMF arithmetic; FP64 for the conserved-variable accumulation, the CT
-// face-field update, the pressure recovery p = (g-1)(E - rho v^2/2 - B^2/2)
-// and the global dt reduction.
+// EMF arithmetic; the conserved-variable accumulation, the CT face-field
+// update, the pressure recovery p = (g-1)(E - rho v^2/2 - B^2/2) and the
+// global dt reduction in a wider accumulator: native FP64 (PG_MIXED) or an
+// FP32 double-word pair (PG_MIXED_DW, 48-bit significand on the FP32 pipes,
+// see pg_dw.cuh).
 //
 // One stage = seven launches:
 //   k_mbound      ghost fill (Src/boundary.c:41-303)
 //   k_msweep_x    reconstruct + Riemann + flux difference along x; one warp
 //                 covers 31 cells of a row, the left interface flux comes
 //                 from the neighbouring lane by shuffle
-//   k_msweep_yz   the same along y or z; each thread marches along the
-//                 direction with a three-cell register window, so every
-//                 cell is reconstructed once and every interface solved once
+//   k_msweep_t    the same along y or z: blocks of 32 x-lanes by 8 rows, the
+//                 left flux of a cell comes from the row below through
+//                 shared memory (7 cells per 8 interfaces along the sweep)
 //   k_memf        UCT_HLL edge EMFs (Src/MHD/CT/ct_emf_average.c:179-352)
 //   k_mface       CT face update (Src/MHD/CT/ct_update.c) + RK face combination
 //   k_mfinal      RK cell combination, face average, ConsToPrim
@@ -22,6 +24,7 @@
 
 #include "pg_internal.h"
 #include "pg_physics.cuh"
+#include "pg_dw.cuh"
 
 namespace pg {
 
@@ -52,7 +55,11 @@ struct MixArgs {
   unsigned char* flag;
   DevScalars* sc;
   float gamma;
+  float inv_dx_f[3];
   double gamma_d, small_rho, small_p, cfl, cfl_max_var;
+  double inv_gmm1_d;     // 1/(gamma-1) as a double
+  float inv_gmm1_hi, inv_gmm1_lo;  // the same as a double-word pair
+  float third_hi, third_lo;        // 1/3 as a double-word pair
   int limiter, recon, ct, nbfield, accmask, device_dt;
 };
 
@@ -73,19 +80,27 @@ __device__ __forceinline__ double warp_max_d(double v) {
   return v;
 }
 
-// PLM or PPM states of one cell from its stencil (w2, w1, v0, e1, e2).
-__device__ __forceinline__ void recon_cell(int recon, int lim, int nv, float w2, float w1, float v0, float e1,
-                                           float e2, float& vp, float& vm) {
-  if (recon == PG_LINEAR) {
-    float dv = limit(lim, nv, e1 - v0, v0 - w1);
-    vp = v0 + dv * 0.5f;
-    vm = v0 - dv * 0.5f;
-  } else {
+// Reconstruction schemes known at compile time (the reference selects them
+// with the RECONSTRUCTION / LIMITER macros of definitions.h).
+enum : int { RS_PLM_MC = 0, RS_PLM_MINMOD = 1, RS_PLM_VANLEER = 2, RS_PLM_GENERIC = 3, RS_PPM = 4 };
+
+__host__ __device__ constexpr int rs_ghost_reach(int rs) { return rs == RS_PPM ? 2 : 1; }
+
+// States (vp, vm) of one cell from its stencil w2 w1 v0 e1 e2 (v[c-2..c+2]).
+template <int RS>
+__device__ __forceinline__ void recon(int lim, int nv, float w2, float w1, float v0, float e1, float e2, float& vp,
+                                      float& vm) {
+  if (RS == RS_PPM) {
     float p = ppm_iface(w1, v0, e1, e2);
     float m = ppm_iface(w2, w1, v0, e1);
     ppm_limit(v0, p, m);
     vp = p;
     vm = m;
+  } else {
+    const int L = RS == RS_PLM_MC ? LIM_MC : RS == RS_PLM_MINMOD ? LIM_MINMOD : RS == RS_PLM_VANLEER ? LIM_VANLEER : lim;
+    float dv = limit(L, nv, e1 - v0, v0 - w1);
+    vp = v0 + dv * 0.5f;
+    vm = v0 - dv * 0.5f;
   }
 }
 
@@ -156,49 +171,50 @@ __global__ void k_mbound(Geom g, BoundArrays arr, int bcx, int bcy, int bcz, lon
 }
 
 // ---------------------------------------------------------------------------
-// x sweep: warp = 32 consecutive cells of one row, 31 of them updated
+// x sweep: a warp covers 32 consecutive cells of one row; lane l reconstructs
+// cell i = ibase + l once, gets the right state of interface i+1/2 from lane
+// l+1 and the flux of interface i-1/2 from lane l-1 (shuffles).  Lanes 1..30
+// update their cell: 30 cells per warp, 31 interfaces, 32 reconstructions.
 // ---------------------------------------------------------------------------
-template <bool CT>
-__global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_lo, int t_n, int b_lo,
-                                                  long long nrows, int stage1, int oned, int nwx) {
+template <int RS, bool CT>
+__global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_lo, int t_n, int b_lo, int nrows,
+                                                  int stage1, int oned, int nwx) {
   const Geom& g = a.g;
   const int lane = threadIdx.x & 31;
-  long long wid = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
-  const int wx = (int)(wid % nwx);
-  const long long row = wid / nwx;
-  if (row >= nrows) return;  // whole warp leaves together
-  const int j = t_lo + (int)(row % t_n);
-  const int k = b_lo + (int)(row / t_n);
-  const int i = g.beg[0] - 1 + 31 * wx + lane;
-  const bool cell_ok = i <= g.end[0] + 1;    // slopes of cells beg-1..end+1
-  const bool face_ok = i <= g.end[0];        // interfaces beg-1+1/2 .. end+1/2
-  const long long c = cidx(g, k, j, i);
-  float vL[NV], vR[NV], slope[3] = {0.f, 0.f, 0.f};
-  // Stencil reads: cell i needs i-1..i+1 (PLM) or i-2..i+2 (PPM); the right
-  // state of interface i+1/2 (cell i+1, only when face_ok) needs one more.
-  // With ng = 2 (PLM) / 3 (PPM) ghosts every read stays inside the row.
-  const bool ppm = a.recon == PG_PARABOLIC;
-  if (cell_ok) {
+  const int wid = (int)((blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+  const int wx = wid % nwx;
+  const int row = wid / nwx;
+  if (row >= nrows) return;  // the whole warp leaves together
+  const int j = t_lo + row % t_n;
+  const int k = b_lo + row / t_n;
+  const int i = g.beg[0] - 1 + 30 * wx + lane;
+  const bool cell_ok = i <= g.end[0] + 1;          // cells beg-1 .. end+1
+  const bool face_ok = i <= g.end[0] && lane < 31;  // interfaces beg-1+1/2 .. end+1/2
+  const int nt0 = g.nt[0];
+  const int c = (k * g.nt[1] + j) * nt0 + i;
+  float vp[NV], vm[NV];
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
+  for (int nv = 0; nv < NV; nv++) {
+    vp[nv] = vm[nv] = 0.f;
+    if (cell_ok) {
       const float* V = a.Vin[nv];
-      float w2 = ppm ? ldg(V, c - 2) : 0.f;
-      float w1 = ldg(V, c - 1), v0 = ldg(V, c), e1 = ldg(V, c + 1);
-      float e2 = (ppm || face_ok) ? ldg(V, c + 2) : 0.f;
-      float e3 = (ppm && face_ok) ? ldg(V, c + 3) : 0.f;
-      float vp, vm, vp1 = 0.f, vm1 = 0.f;
-      recon_cell(a.recon, a.limiter, nv, w2, w1, v0, e1, e2, vp, vm);      // cell i
-      if (face_ok) recon_cell(a.recon, a.limiter, nv, w1, v0, e1, e2, e3, vp1, vm1);  // cell i+1
-      vL[nv] = vp;
-      vR[nv] = vm1;
-      if (nv >= VX1 && nv <= VX3) slope[nv - VX1] = vp - vm;
+      float w2 = RS == RS_PPM ? __ldg(V + c - 2) : 0.f;
+      float e2 = RS == RS_PPM ? __ldg(V + c + 2) : 0.f;
+      recon<RS>(a.limiter, nv, w2, __ldg(V + c - 1), __ldg(V + c), __ldg(V + c + 1), e2, vp[nv], vm[nv]);
     }
   }
-  Iface<float> o;
+  if (CT && cell_ok)
+    for (int comp = 0; comp < g.dims; comp++) a.DV[0][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+  float vR[NV];
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) vR[nv] = __shfl_down_sync(0xffffffffu, vm[nv], 1);
   float fl[NV], pr = 0.f, cm = 0.f;
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) fl[nv] = 0.f;
   if (face_ok) {
+    Iface<float> o;
     float bn = CT ? a.Bin[0][c] : 0.f;
-    solve_iface<0, CT>(a, solver, vL, vR, bn, o);
+    solve_iface<0, CT>(a, solver, vp, vR, bn, o);
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) fl[nv] = o.f[nv];
     pr = o.press;
@@ -207,20 +223,14 @@ __global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_l
       a.S[0][0][c] = pmax(0.f, -o.SL);
       a.S[0][1][c] = pmax(0.f, o.SR);
     }
-  } else {
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) fl[nv] = 0.f;
   }
-  if (CT && cell_ok)
-    for (int comp = 0; comp < g.dims; comp++) a.DV[0][comp][c] = slope[comp];
-  // left interface (i-1/2) from the previous lane
   float flm[NV];
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) flm[nv] = __shfl_up_sync(0xffffffffu, fl[nv], 1);
-  float prm = __shfl_up_sync(0xffffffffu, pr, 1);
-  float cmm = __shfl_up_sync(0xffffffffu, cm, 1);
-  if (lane >= 1 && i >= g.beg[0] && i <= g.end[0]) {
-    const float scrh = (float)(a.sc->dt * g.inv_dx[0]);
+  const float prm = __shfl_up_sync(0xffffffffu, pr, 1);
+  const float cmm = __shfl_up_sync(0xffffffffu, cm, 1);
+  if (lane >= 1 && lane <= 30 && i >= g.beg[0] && i <= g.end[0]) {
+    const float scrh = a.sc->dtdx[0];
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
       if (!((a.accmask >> nv) & 1)) continue;
@@ -230,105 +240,88 @@ __global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_l
     }
     // 2D/3D: C_dt term of update_stage.c:233; 1D: the larger adjacent
     // cmax (the 1D reduction of update_stage.c:237-241 is a plain max).
-    if (oned) a.CDT[c] = pmax(cmm, cm) * (float)g.inv_dx[0];
-    else if (stage1) a.CDT[c] = 0.5f * (cmm + cm) * (float)g.inv_dx[0];
+    if (oned) a.CDT[c] = pmax(cmm, cm) * a.inv_dx_f[0];
+    else if (stage1) a.CDT[c] = 0.5f * (cmm + cm) * a.inv_dx_f[0];
   }
 }
 
 // ---------------------------------------------------------------------------
-// y/z sweep: lanes along x, each thread marches along DIR over a segment
+// y/z sweep: block = 32 lanes along x by kTY rows along DIR.  Row ty holds
+// cell m = m0 - 1 + ty: every row reconstructs its cell once (left states of
+// the row above go through shared memory), rows 0..kTY-2 solve interface
+// m+1/2, rows 1..kTY-2 update their cell from the fluxes of rows ty-1, ty.
 // ---------------------------------------------------------------------------
-template <int DIR, bool CT>
-__global__ void __launch_bounds__(128) k_msweep_yz(MixArgs a, int solver, int i_lo, int i_n, int o_lo, int o_n,
-                                                   int seg_len, int nseg, int stage1, int first_dir) {
+constexpr int kTY = 12;
+
+template <int RS, int DIR, bool CT>
+__global__ void __launch_bounds__(32 * kTY, 2) k_msweep_t(MixArgs a, int solver, int i_lo, int i_n, int o_lo,
+                                                          int o_n, int stage1) {
+  __shared__ float svm[NV][kTY][32];
+  __shared__ float sf[NV + 2][kTY][32];
   const Geom& g = a.g;
-  long long tid = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const int ii = (int)(tid % i_n);
-  long long r = tid / i_n;
-  const int oo = (int)(r % o_n);
-  const int sg = (int)(r / o_n);
-  if (sg >= nseg) return;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const int nbx = (i_n + 31) >> 5;
+  const int bx = blockIdx.x % nbx;
+  const int bo = blockIdx.x / nbx;
+  const int ii = 32 * bx + tx;
   const int i = i_lo + ii;
-  // the other transverse axis: z for DIR=y, y for DIR=z
-  const int other = o_lo + oo;
-  const long long s = g.s[DIR];
+  const int other = o_lo + bo;
   const int beg = g.beg[DIR], end = g.end[DIR];
-  const int d0 = beg + sg * seg_len;
-  const int d1 = min(d0 + seg_len - 1, end);  // cells updated: d0..d1
-  long long base = DIR == 1 ? cidx(g, other, 0, i) : cidx(g, 0, other, i);
-  const bool ppm = a.recon == PG_PARABOLIC;
-  const float scrh = (float)(a.sc->dt * g.inv_dx[DIR]);
-  const float invdx = (float)g.inv_dx[DIR];
-  // window: w[0]=v[m-1], w[1]=v[m], w[2]=v[m+1], w[3]=v[m+2] (PPM also w[-1])
-  float wm2[NV], w0[NV], w1[NV], w2[NV], w3[NV];
-  float vprev[NV];           // vp of cell m
-  float fprev[NV], pprev = 0.f, cprev = 0.f;
-  int m = d0 - 1;
+  const int m = beg - 1 + (kTY - 2) * (int)blockIdx.y + ty;
+  const bool col_ok = ii < i_n && bo < o_n;
+  const bool cell_ok = col_ok && m <= end + 1;               // cells beg-1 .. end+1
+  const bool face_ok = col_ok && m <= end && ty < kTY - 1;   // interfaces beg-1+1/2 .. end+1/2
+  const int s = DIR == 1 ? g.nt[0] : g.nt[0] * g.nt[1];
+  const int c = (DIR == 1 ? (other * g.nt[1]) * g.nt[0] + i : other * g.nt[0] + i) + m * s;
+  float vp[NV], vm[NV];
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
-    const float* V = a.Vin[nv];
-    wm2[nv] = ppm ? ldg(V, base + (m - 2) * s) : 0.f;
-    w0[nv] = ldg(V, base + (m - 1) * s);
-    w1[nv] = ldg(V, base + m * s);
-    w2[nv] = ldg(V, base + (m + 1) * s);
-    w3[nv] = ppm ? ldg(V, base + (m + 2) * s) : 0.f;
-    float vp, vm;
-    recon_cell(a.recon, a.limiter, nv, wm2[nv], w0[nv], w1[nv], w2[nv], w3[nv], vp, vm);
-    vprev[nv] = vp;
-    if (CT && nv >= VX1 && nv < VX1 + g.dims && m >= beg - 1) a.DV[DIR][nv - VX1][base + m * s] = vp - vm;
-    fprev[nv] = 0.f;
-  }
-  for (; m <= d1; m++) {
-    // shift window so that w0=v[m], w1=v[m+1], w2=v[m+2], w3=v[m+3]
-    float vL[NV], vR[NV];
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
+    vp[nv] = vm[nv] = 0.f;
+    if (cell_ok) {
       const float* V = a.Vin[nv];
-      float nw = ldg(V, base + (m + (ppm ? 3 : 2)) * s);
-      wm2[nv] = w0[nv];
-      w0[nv] = w1[nv];
-      w1[nv] = w2[nv];
-      if (ppm) {
-        w2[nv] = w3[nv];
-        w3[nv] = nw;
-      } else {
-        w2[nv] = nw;
-      }
-      float vp, vm;  // states of cell m+1
-      recon_cell(a.recon, a.limiter, nv, wm2[nv], w0[nv], w1[nv], w2[nv], w3[nv], vp, vm);
-      vL[nv] = vprev[nv];
-      vR[nv] = vm;
-      vprev[nv] = vp;
-      if (CT && nv >= VX1 && nv < VX1 + g.dims && m + 1 <= end + 1)
-        a.DV[DIR][nv - VX1][base + (m + 1) * s] = vp - vm;
+      float w2 = RS == RS_PPM ? __ldg(V + c - 2 * s) : 0.f;
+      float e2 = RS == RS_PPM ? __ldg(V + c + 2 * s) : 0.f;
+      recon<RS>(a.limiter, nv, w2, __ldg(V + c - s), __ldg(V + c), __ldg(V + c + s), e2, vp[nv], vm[nv]);
     }
-    const long long c = base + m * s;  // interface m+1/2 is stored at cell m
+    svm[nv][ty][tx] = vm[nv];
+  }
+  if (CT && cell_ok)
+    for (int comp = 0; comp < g.dims; comp++) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+  __syncthreads();
+  float fl[NV], pr = 0.f, cm = 0.f;
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) fl[nv] = 0.f;
+  if (face_ok) {
+    float vR[NV];
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) vR[nv] = svm[nv][ty + 1][tx];
     Iface<float> o;
     float bn = CT ? a.Bin[DIR][c] : 0.f;
-    solve_iface<DIR, CT>(a, solver, vL, vR, bn, o);
+    solve_iface<DIR, CT>(a, solver, vp, vR, bn, o);
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) fl[nv] = o.f[nv];
+    pr = o.press;
+    cm = o.cmax;
     if (CT) {
       a.S[DIR][0][c] = pmax(0.f, -o.SL);
       a.S[DIR][1][c] = pmax(0.f, o.SR);
     }
-    if (m >= d0) {  // update cell m from interfaces m-1/2 (prev) and m+1/2
+  }
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) {
-        if (!((a.accmask >> nv) & 1)) continue;
-        float rhs = -scrh * (o.f[nv] - fprev[nv]);
-        if (nv == Rot<DIR>::vn) rhs -= scrh * (o.press - pprev);
-        if (first_dir) a.dU[nv][c] = rhs;
-        else a.dU[nv][c] += rhs;
-      }
-      if (stage1) {
-        float term = 0.5f * (cprev + o.cmax) * invdx;
-        if (first_dir) a.CDT[c] = term;
-        else a.CDT[c] += term;
-      }
+  for (int nv = 0; nv < NV; nv++) sf[nv][ty][tx] = fl[nv];
+  sf[NV][ty][tx] = pr;
+  sf[NV + 1][ty][tx] = cm;
+  __syncthreads();
+  if (ty >= 1 && ty <= kTY - 2 && col_ok && m >= beg && m <= end) {
+    const float scrh = a.sc->dtdx[DIR];
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) {
+      if (!((a.accmask >> nv) & 1)) continue;
+      float rhs = -scrh * (fl[nv] - sf[nv][ty - 1][tx]);
+      if (nv == Rot<DIR>::vn) rhs -= scrh * (pr - sf[NV][ty - 1][tx]);
+      a.dU[nv][c] += rhs;
     }
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) fprev[nv] = o.f[nv];
-    pprev = o.press;
-    cprev = o.cmax;
+    if (stage1) a.CDT[c] += 0.5f * (sf[NV + 1][ty - 1][tx] + cm) * a.inv_dx_f[DIR];
   }
 }
 
@@ -387,21 +380,21 @@ __global__ void k_memf(MixArgs a, Box box) {
 }
 
 // CT face update: EMF differences in FP32, accumulation into the face field
-// in FP64, RK face combination in FP64.
-template <int STAGE, int NSTAGE>
+// and the RK face combination in the accumulator type A (double or dw).
+template <int STAGE, int NSTAGE, class A>
 __global__ void k_mface(MixArgs a, Box box) {
+  using O = Acc<A>;
   long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= box.count()) return;
   int i, j, k;
   box.coords(q, i, j, k);
   const Geom& g = a.g;
   const long long c = cidx(g, k, j, i);
-  const double dt = a.sc->dt;
   const bool d3 = g.dims == 3;
   const float* E1 = a.E[0];
   const float* E2 = a.E[1];
   const float* E3 = a.E[2];
-  const float f1 = (float)(dt * g.inv_dx[0]), f2 = (float)(dt * g.inv_dx[1]), f3 = (float)(dt * g.inv_dx[2]);
+  const float f1 = a.sc->dtdx[0], f2 = a.sc->dtdx[1], f3 = a.sc->dtdx[2];
   for (int fd = 0; fd < g.dims; fd++) {
     bool in = true;
     for (int ax = 0; ax < g.dims; ax++) {
@@ -420,92 +413,127 @@ __global__ void k_mface(MixArgs a, Box box) {
     } else {
       rhs = -f1 * (E2[c] - E2[c - 1]) + f2 * (E1[c] - E1[c - g.s[1]]);
     }
-    double bb = (double)a.Bin[fd][c] + (double)rhs;
+    typename O::T bb = O::addf(O::from(a.Bin[fd][c]), rhs);
     if (STAGE == 2) {
-      const double w0 = NSTAGE == 3 ? 0.75 : 0.5, wc = NSTAGE == 3 ? 0.25 : 0.5;
-      bb = w0 * (double)a.B0[fd][c] + wc * bb;
+      if (NSTAGE == 2) bb = O::mulf(O::addf(bb, a.B0[fd][c]), 0.5f);
+      else bb = O::add(O::mulf(O::from(a.B0[fd][c]), 0.75f), O::mulf(bb, 0.25f));
     } else if (STAGE == 3) {
-      bb = ((double)a.B0[fd][c] + 2.0 * bb) * (1.0 / 3.0);
+      typename O::T third = O::konst(1.0 / 3.0, a.third_hi, a.third_lo);
+      bb = O::mul(O::add(O::from(a.B0[fd][c]), O::mulf(bb, 2.0f)), third);
     }
-    a.Bout[fd][c] = (float)bb;
+    a.Bout[fd][c] = O::tof(bb);
   }
 }
 
-// Conservative variables in FP64 from FP32 primitives (Src/MHD/mappers.c:25-86).
-__device__ __forceinline__ void prim_to_cons_d(const float* vf, double* u, double inv_gmm1) {
-  double rho = vf[RHO];
-  double vx = vf[VX1], vy = vf[VX2], vz = vf[VX3];
-  double bx = vf[BX1], by = vf[BX2], bz = vf[BX3];
-  u[RHO] = rho;
-  u[MX1] = rho * vx;
-  u[MX1 + 1] = rho * vy;
-  u[MX1 + 2] = rho * vz;
-  u[BX1] = bx;
-  u[BX2] = by;
-  u[BX3] = bz;
-  double kin = vx * vx + vy * vy + vz * vz;
-  double kinb2 = 0.5 * (rho * kin + (bx * bx + by * by + bz * bz));
-  u[ENG] = kinb2 + (double)vf[PRS] * inv_gmm1;
+// Conserved variables of an FP32 primitive state in the accumulator type.
+template <class A>
+struct ConsA {
+  typename Acc<A>::T rho, m[3], E, b[3];
+};
+
+template <class A>
+__device__ __forceinline__ ConsA<A> cons_of(const float* v, typename Acc<A>::T inv_gmm1) {
+  using O = Acc<A>;
+  ConsA<A> u;
+  u.rho = O::from(v[RHO]);
+#pragma unroll
+  for (int q = 0; q < 3; q++) {
+    u.m[q] = O::prod(v[RHO], v[VX1 + q]);
+    u.b[q] = O::from(v[BX1 + q]);
+  }
+  typename O::T kin = O::add(O::add(O::prod(v[VX1], v[VX1]), O::prod(v[VX2], v[VX2])), O::prod(v[VX3], v[VX3]));
+  typename O::T b2 = O::add(O::add(O::prod(v[BX1], v[BX1]), O::prod(v[BX2], v[BX2])), O::prod(v[BX3], v[BX3]));
+  typename O::T kinb2 = O::mulf(O::add(O::mulf(kin, v[RHO]), b2), 0.5f);
+  u.E = O::add(kinb2, O::mulf(inv_gmm1, v[PRS]));
+  return u;
 }
 
-template <int STAGE, int NSTAGE>
+template <int STAGE, int NSTAGE, class A>
 __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
+  using O = Acc<A>;
+  using T = typename O::T;
   long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  double cd = 0.0;
+  float cd = 0.f;
   bool fails = false, bad = false;
   if (q < dom.count()) {
     int i, j, k;
     dom.coords(q, i, j, k);
     const Geom& g = a.g;
     const long long c = cidx(g, k, j, i);
-    const double gmm1 = a.gamma_d - 1.0, inv_gmm1 = 1.0 / gmm1;
+    const T inv_gmm1 = O::konst(a.inv_gmm1_d, a.inv_gmm1_hi, a.inv_gmm1_lo);
     float vin[NV];
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) vin[nv] = a.Vin[nv][c];
-    double u[NV];
-    prim_to_cons_d(vin, u, inv_gmm1);
+    ConsA<A> u = cons_of<A>(vin, inv_gmm1);
+    // U += dU (flux differences of all directions, FP32) in A
+    const int msk = a.accmask;
+    if (msk & (1 << RHO)) u.rho = O::addf(u.rho, a.dU[RHO][c]);
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++)
-      if ((a.accmask >> nv) & 1) u[nv] += (double)a.dU[nv][c];
+    for (int d = 0; d < 3; d++) {
+      if (msk & (1 << (VX1 + d))) u.m[d] = O::addf(u.m[d], a.dU[VX1 + d][c]);
+      if (msk & (1 << (BX1 + d))) u.b[d] = O::addf(u.b[d], a.dU[BX1 + d][c]);
+    }
+    if (msk & (1 << ENG)) u.E = O::addf(u.E, a.dU[ENG][c]);
     if (STAGE >= 2) {
       float v0[NV];
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) v0[nv] = a.V0[nv][c];
-      double u0[NV];
-      prim_to_cons_d(v0, u0, inv_gmm1);
-      if (STAGE == 2) {
-        const double w0 = NSTAGE == 3 ? 0.75 : 0.5, wc = NSTAGE == 3 ? 0.25 : 0.5;
+      ConsA<A> u0 = cons_of<A>(v0, inv_gmm1);
+      if (STAGE == 2 && NSTAGE == 2) {
+        u.rho = O::mulf(O::add(u0.rho, u.rho), 0.5f);
+        u.E = O::mulf(O::add(u0.E, u.E), 0.5f);
 #pragma unroll
-        for (int nv = 0; nv < NV; nv++) u[nv] = w0 * u0[nv] + wc * u[nv];
+        for (int d = 0; d < 3; d++) {
+          u.m[d] = O::mulf(O::add(u0.m[d], u.m[d]), 0.5f);
+          u.b[d] = O::mulf(O::add(u0.b[d], u.b[d]), 0.5f);
+        }
+      } else if (STAGE == 2) {
+        u.rho = O::add(O::mulf(u0.rho, 0.75f), O::mulf(u.rho, 0.25f));
+        u.E = O::add(O::mulf(u0.E, 0.75f), O::mulf(u.E, 0.25f));
+#pragma unroll
+        for (int d = 0; d < 3; d++) {
+          u.m[d] = O::add(O::mulf(u0.m[d], 0.75f), O::mulf(u.m[d], 0.25f));
+          u.b[d] = O::add(O::mulf(u0.b[d], 0.75f), O::mulf(u.b[d], 0.25f));
+        }
       } else {
+        const T third = O::konst(1.0 / 3.0, a.third_hi, a.third_lo);
+        u.rho = O::mul(O::add(u0.rho, O::mulf(u.rho, 2.0f)), third);
+        u.E = O::mul(O::add(u0.E, O::mulf(u.E, 2.0f)), third);
 #pragma unroll
-        for (int nv = 0; nv < NV; nv++) u[nv] = (u0[nv] + 2.0 * u[nv]) * (1.0 / 3.0);
+        for (int d = 0; d < 3; d++) {
+          u.m[d] = O::mul(O::add(u0.m[d], O::mulf(u.m[d], 2.0f)), third);
+          u.b[d] = O::mul(O::add(u0.b[d], O::mulf(u.b[d], 2.0f)), third);
+        }
       }
     }
+    // CT_AverageMagneticField: staggered components from the new faces
     if (a.ct)
       for (int d = 0; d < g.dims; d++)
-        u[BX1 + d] = 0.5 * ((double)a.Bout[d][c] + (double)a.Bout[d][c - g.s[d]]);
-    // ConsToPrim with FP64 pressure recovery; velocities in FP32.
+        u.b[d] = O::mulf(O::addf(O::from(a.Bout[d][c]), a.Bout[d][c - g.s[d]]), 0.5f);
+    // ConsToPrim (Src/MHD/mappers.c:88-254) with the pressure recovered in A
     unsigned char fl = 0;
-    if (u[RHO] < 0.0) {
-      u[RHO] = a.small_rho;
+    if (O::neg(u.rho)) {
+      u.rho = O::from((float)a.small_rho);
       fl = FLAG_CONS2PRIM_FAIL;
     }
-    float rho_f = (float)u[RHO];
-    float tau = 1.0f / rho_f;
-    float vx = (float)u[MX1] * tau, vy = (float)u[MX1 + 1] * tau, vz = (float)u[MX1 + 2] * tau;
-    double ke = 0.5 * (u[MX1] * (double)vx + u[MX1 + 1] * (double)vy + u[MX1 + 2] * (double)vz);
-    double kinb2 = ke + 0.5 * (u[BX1] * u[BX1] + u[BX2] * u[BX2] + u[BX3] * u[BX3]);
-    if (u[ENG] < 0.0) {
-      u[ENG] = a.small_p * inv_gmm1 + kinb2;
+    const float rho_f = O::tof(u.rho);
+    const float tau = 1.0f / rho_f;
+    float vel[3];
+#pragma unroll
+    for (int d = 0; d < 3; d++) vel[d] = O::tof(u.m[d]) * tau;
+    T m2 = O::add(O::add(O::mul(u.m[0], u.m[0]), O::mul(u.m[1], u.m[1])), O::mul(u.m[2], u.m[2]));
+    T b2 = O::add(O::add(O::mul(u.b[0], u.b[0]), O::mul(u.b[1], u.b[1])), O::mul(u.b[2], u.b[2]));
+    T kinb2 = O::mulf(O::add(O::div(m2, u.rho), b2), 0.5f);
+    if (O::neg(u.E)) {
+      u.E = O::add(O::mulf(inv_gmm1, (float)a.small_p), kinb2);
       fl = FLAG_CONS2PRIM_FAIL;
     }
-    double p = gmm1 * (u[ENG] - kinb2);
-    if (p < 0.0) {
-      p = a.small_p;
+    float p = O::tof(O::mulf(O::sub(u.E, kinb2), a.gamma - 1.0f));
+    if (p < 0.f) {
+      p = (float)a.small_p;
       fl = FLAG_CONS2PRIM_FAIL;
     }
-    float out[NV] = {rho_f, vx, vy, vz, (float)u[BX1], (float)u[BX2], (float)u[BX3], (float)p};
+    float out[NV] = {rho_f, vel[0], vel[1], vel[2], O::tof(u.b[0]), O::tof(u.b[1]), O::tof(u.b[2]), p};
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
       a.Vout[nv][c] = out[nv];
@@ -515,11 +543,14 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
       a.flag[c] = fl;
       fails = true;
     }
-    if (reduce_cdt) cd = (double)a.CDT[c];
+    if (reduce_cdt) cd = a.CDT[c];
   }
-  if (reduce_cdt) {
-    double m = warp_max_d(cd);
-    if ((threadIdx.x & 31) == 0) atomic_max_nonneg_d(&a.sc->inv_dt_bits, m);
+  if (reduce_cdt) {  // the max is exact in FP32; the global reduction runs on FP64 bits
+    for (int o = 16; o > 0; o >>= 1) {
+      float w = __shfl_down_sync(0xffffffffu, cd, o);
+      cd = (w > cd || w != w) ? w : cd;
+    }
+    if ((threadIdx.x & 31) == 0) atomic_max_nonneg_d(&a.sc->inv_dt_bits, (double)cd);
   }
   unsigned ball = __ballot_sync(0xffffffffu, fails);
   if ((threadIdx.x & 31) == 0 && ball) atomicAdd(&a.sc->nfail, (unsigned long long)__popc(ball));
@@ -537,6 +568,7 @@ __global__ void k_mbegin(MixArgs a, long long n) {
     a.sc->inv_dt_bits = 0ull;
     a.sc->mach_bits = 0ull;
     a.sc->nfail = 0ull;
+    for (int d = 0; d < 3; d++) a.sc->dtdx[d] = (float)(a.sc->dt * a.g.inv_dx[d]);
   }
 }
 
@@ -658,6 +690,12 @@ static MixArgs margs(Solver* S, int in_buf, int out_buf, int v0_buf) {
   a.sc = S->sc;
   a.gamma = (float)S->cfg.gamma;
   a.gamma_d = S->cfg.gamma;
+  for (int d = 0; d < 3; d++) a.inv_dx_f[d] = (float)S->g.inv_dx[d];
+  a.inv_gmm1_d = 1.0 / (S->cfg.gamma - 1.0);
+  a.inv_gmm1_hi = (float)a.inv_gmm1_d;
+  a.inv_gmm1_lo = (float)(a.inv_gmm1_d - (double)a.inv_gmm1_hi);
+  a.third_hi = (float)(1.0 / 3.0);
+  a.third_lo = (float)(1.0 / 3.0 - (double)a.third_hi);
   a.small_rho = S->cfg.small_density > 0 ? S->cfg.small_density : 1e-12;
   a.small_p = S->cfg.small_pressure > 0 ? S->cfg.small_pressure : 1e-12;
   a.cfl = S->cfl;
@@ -688,41 +726,57 @@ static void mlaunch_bound(Solver* S, const MixArgs& a) {
                                     g, arr, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0, n1, n2)));
 }
 
-static const int kSeg = 32;
 
-template <bool CT>
-static void mlaunch_sweeps(Solver* S, const MixArgs& a, int stage) {
+template <int RS, bool CT>
+static void mlaunch_sweeps_rs(Solver* S, const MixArgs& a, int stage) {
   const Geom& g = S->g;
   cudaStream_t st = S->stream;
   const int solver = S->cfg.riemann;
   const int ext = CT ? 1 : 0;
   const int stage1 = (stage == 1) ? 1 : 0;
-  // x sweep over rows (j,k) in the transverse-extended box
-  {
+  {  // x sweep over rows (j,k) of the transverse-extended box
     int t_lo = g.dims > 1 ? g.beg[1] - ext : 0, t_n = g.dims > 1 ? g.nx[1] + 2 * ext : 1;
     int b_lo = g.dims > 2 ? g.beg[2] - ext : 0, b_n = g.dims > 2 ? g.nx[2] + 2 * ext : 1;
-    int nwx = (g.nx[0] + 2 + 30) / 31;
-    long long nrows = (long long)t_n * b_n;
+    int nwx = (g.nx[0] + 2 + 29) / 30;  // lanes reach cell end+1
+    int nrows = t_n * b_n;
     long long threads = (long long)nwx * nrows * 32;
-    PG_LAUNCH(S, "mixed_sweep_x", (k_msweep_x<CT><<<grid_for(threads, 128), 128, 0, st>>>(
+    PG_LAUNCH(S, "mixed_sweep_x", (k_msweep_x<RS, CT><<<grid_for(threads, 128), 128, 0, st>>>(
                                       a, solver, t_lo, t_n, b_lo, nrows, stage1, g.dims == 1, nwx)));
   }
   for (int dir = 1; dir < g.dims; dir++) {
     int i_lo = g.beg[0] - ext, i_n = g.nx[0] + 2 * ext;
     int oax = dir == 1 ? 2 : 1;
     int o_lo = oax < g.dims ? g.beg[oax] - ext : 0, o_n = oax < g.dims ? g.nx[oax] + 2 * ext : 1;
-    int nseg = (g.nx[dir] + kSeg - 1) / kSeg;
-    long long threads = (long long)i_n * o_n * nseg;
+    int nbx = (i_n + 31) / 32;
+    int nblk = (g.nx[dir] + 2 + kTY - 3) / (kTY - 2);  // rows reach cell end+1
+    dim3 grid((unsigned)(nbx * o_n), (unsigned)nblk), block(32, kTY);
     if (dir == 1)
-      PG_LAUNCH(S, "mixed_sweep_y", (k_msweep_yz<1, CT><<<grid_for(threads, 128), 128, 0, st>>>(
-                                        a, solver, i_lo, i_n, o_lo, o_n, kSeg, nseg, stage1, 0)));
+      PG_LAUNCH(S, "mixed_sweep_y", (k_msweep_t<RS, 1, CT><<<grid, block, 0, st>>>(a, solver, i_lo, i_n, o_lo,
+                                                                                     o_n, stage1)));
     else
-      PG_LAUNCH(S, "mixed_sweep_z", (k_msweep_yz<2, CT><<<grid_for(threads, 128), 128, 0, st>>>(
-                                        a, solver, i_lo, i_n, o_lo, o_n, kSeg, nseg, stage1, 0)));
+      PG_LAUNCH(S, "mixed_sweep_z", (k_msweep_t<RS, 2, CT><<<grid, block, 0, st>>>(a, solver, i_lo, i_n, o_lo,
+                                                                                     o_n, stage1)));
   }
 }
 
-template <int STAGE, int NSTAGE>
+template <bool CT>
+static void mlaunch_sweeps(Solver* S, const MixArgs& a, int stage) {
+  int rs;
+  if (S->cfg.reconstruction == PG_PARABOLIC) rs = RS_PPM;
+  else if (S->cfg.limiter == PG_MC_LIM) rs = RS_PLM_MC;
+  else if (S->cfg.limiter == PG_MINMOD_LIM) rs = RS_PLM_MINMOD;
+  else if (S->cfg.limiter == PG_VANLEER_LIM) rs = RS_PLM_VANLEER;
+  else rs = RS_PLM_GENERIC;
+  switch (rs) {
+    case RS_PLM_MC: mlaunch_sweeps_rs<RS_PLM_MC, CT>(S, a, stage); break;
+    case RS_PLM_MINMOD: mlaunch_sweeps_rs<RS_PLM_MINMOD, CT>(S, a, stage); break;
+    case RS_PLM_VANLEER: mlaunch_sweeps_rs<RS_PLM_VANLEER, CT>(S, a, stage); break;
+    case RS_PPM: mlaunch_sweeps_rs<RS_PPM, CT>(S, a, stage); break;
+    default: mlaunch_sweeps_rs<RS_PLM_GENERIC, CT>(S, a, stage); break;
+  }
+}
+
+template <int STAGE, int NSTAGE, class A>
 static void mlaunch_tail(Solver* S, const MixArgs& a, const Box& dom) {
   const Geom& g = S->g;
   cudaStream_t st = S->stream;
@@ -733,50 +787,56 @@ static void mlaunch_tail(Solver* S, const MixArgs& a, const Box& dom) {
       else { eb.lo[ax] = eb.hi[ax] = 0; }
     }
     PG_LAUNCH(S, "mixed_emf", (k_memf<<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb)));
-    PG_LAUNCH(S, "mixed_face", (k_mface<STAGE, NSTAGE><<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb)));
+    PG_LAUNCH(S, "mixed_face", (k_mface<STAGE, NSTAGE, A><<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb)));
   }
   if (g.dims == 1) PG_LAUNCH(S, "mixed_dt1d", (k_m1d_dt<<<grid_for(dom.count()), kThreads, 0, st>>>(a, dom)));
   int reduce = (STAGE == 1 && g.dims > 1);
-  PG_LAUNCH(S, "mixed_final", (k_mfinal<STAGE, NSTAGE><<<grid_for(dom.count()), kThreads, 0, st>>>(a, dom, reduce)));
+  PG_LAUNCH(S, "mixed_final", (k_mfinal<STAGE, NSTAGE, A><<<grid_for(dom.count()), kThreads, 0, st>>>(a, dom, reduce)));
 }
 
-template <int NSTAGE>
+template <int NSTAGE, class A>
 static void menqueue(Solver* S) {
   MixedState* M = (MixedState*)S->mixed;
   const Geom& g = S->g;
   Box dom;
   for (int ax = 0; ax < 3; ax++) { dom.lo[ax] = g.beg[ax]; dom.hi[ax] = g.end[ax]; }
-  const int A = M->cur, B = 1 - M->cur;
+  const int bA = M->cur, bB = 1 - M->cur;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
   // stage 1: A -> B
-  MixArgs a1 = margs(S, A, B, A);
+  MixArgs a1 = margs(S, bA, bB, bA);
   PG_LAUNCH(S, "mixed_begin", (k_mbegin<<<grid_for(g.ncell), kThreads, 0, S->stream>>>(a1, g.ncell)));
   mlaunch_bound(S, a1);
   if (ct) mlaunch_sweeps<true>(S, a1, 1); else mlaunch_sweeps<false>(S, a1, 1);
-  mlaunch_tail<1, NSTAGE>(S, a1, dom);
+  mlaunch_tail<1, NSTAGE, A>(S, a1, dom);
   if (NSTAGE == 2) {
     // stage 2: B (+A) -> A
-    MixArgs a2 = margs(S, B, A, A);
+    MixArgs a2 = margs(S, bB, bA, bA);
     mlaunch_bound(S, a2);
     if (ct) mlaunch_sweeps<true>(S, a2, 2); else mlaunch_sweeps<false>(S, a2, 2);
-    mlaunch_tail<2, NSTAGE>(S, a2, dom);
+    mlaunch_tail<2, NSTAGE, A>(S, a2, dom);
     PG_LAUNCH(S, "mixed_end_step", (k_mend_step<<<1, 1, 0, S->stream>>>(a2)));
   } else {
-    MixArgs a2 = margs(S, B, B, A);  // in place: the final kernel reads its own cell only
+    MixArgs a2 = margs(S, bB, bB, bA);  // in place: the final kernel reads its own cell only
     mlaunch_bound(S, a2);
     if (ct) mlaunch_sweeps<true>(S, a2, 2); else mlaunch_sweeps<false>(S, a2, 2);
-    mlaunch_tail<2, NSTAGE>(S, a2, dom);
-    MixArgs a3 = margs(S, B, A, A);
+    mlaunch_tail<2, NSTAGE, A>(S, a2, dom);
+    MixArgs a3 = margs(S, bB, bA, bA);
     mlaunch_bound(S, a3);
     if (ct) mlaunch_sweeps<true>(S, a3, 3); else mlaunch_sweeps<false>(S, a3, 3);
-    mlaunch_tail<3, NSTAGE>(S, a3, dom);
+    mlaunch_tail<3, NSTAGE, A>(S, a3, dom);
     PG_LAUNCH(S, "mixed_end_step", (k_mend_step<<<1, 1, 0, S->stream>>>(a3)));
   }
 }
 
 int mixed_enqueue_step(Solver* S) {
-  if (S->cfg.time_stepping == PG_RK3) menqueue<3>(S);
-  else menqueue<2>(S);
+  const bool dwacc = S->cfg.precision == PG_MIXED_DW;
+  if (S->cfg.time_stepping == PG_RK3) {
+    if (dwacc) menqueue<3, dw>(S);
+    else menqueue<3, double>(S);
+  } else {
+    if (dwacc) menqueue<2, dw>(S);
+    else menqueue<2, double>(S);
+  }
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ERR_CUDA;
 }
 

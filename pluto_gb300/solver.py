@@ -25,7 +25,7 @@ LIMITER = {"FLAT_LIM": L.PG_FLAT_LIM, "MINMOD_LIM": L.PG_MINMOD_LIM,
 RIEMANN = {"hll": L.PG_HLL, "hlld": L.PG_HLLD, "roe": L.PG_ROE}
 STEPPING = {"RK2": L.PG_RK2, "RK3": L.PG_RK3}
 BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW}
-PRECISION = {"fp64": L.PG_FP64, "mixed": L.PG_MIXED}
+PRECISION = {"fp64": L.PG_FP64, "mixed": L.PG_MIXED, "mixed_dw": L.PG_MIXED_DW}
 NVAR = 8
 
 

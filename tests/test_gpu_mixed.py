@@ -18,10 +18,14 @@ def _s(spec, precision):
     return Solver(spec, precision=precision)
 
 
+MIXED = ["mixed", "mixed_dw"]
+
+
+@pytest.mark.parametrize("prec", MIXED)
 @pytest.mark.parametrize("name", GOLDEN_NAMES)
-def test_mixed_close_to_reference_goldens(name):
+def test_mixed_close_to_reference_goldens(name, prec):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
-    s = _s(meta, "mixed")
+    s = _s(meta, prec)
     s.upload(vc0, bs0)
     s.run(meta["steps"], meta["first_dt"], meta["cfl"])
     vc, bs = s.download()
@@ -30,25 +34,28 @@ def test_mixed_close_to_reference_goldens(name):
     assert max(errs) <= tol, errs
 
 
-def test_mixed_vs_fp64_blast_l1():
+@pytest.mark.parametrize("prec", MIXED)
+def test_mixed_vs_fp64_blast_l1(prec):
     from pluto_gb300 import problems
     spec, vc, faces = problems.blast3d(48)
     out = {}
-    for prec in ("fp64", "mixed"):
-        s = _s(spec, prec)
+    for p in ("fp64", prec):
+        s = _s(spec, p)
         s.upload(vc, faces)
         s.run(40, spec["first_dt"], spec["cfl"])
-        out[prec] = s.download()
-    errs = {q: rel_l1(out["mixed"][0][q], out["fp64"][0][q]) for q in (0, 1, 2, 3, 4, 5, 6, 7)}
+        out[p] = s.download()
+    m = out[prec]
+    errs = {q: rel_l1(m[0][q], out["fp64"][0][q]) for q in (0, 1, 2, 3, 4, 5, 6, 7)}
     for d in range(3):
-        errs[f"b{d}"] = rel_l1(out["mixed"][1][d], out["fp64"][1][d])
+        errs[f"b{d}"] = rel_l1(m[1][d], out["fp64"][1][d])
     assert max(errs.values()) <= 1e-5, errs
 
 
-def test_mixed_divergence_free_to_fp32_roundoff():
+@pytest.mark.parametrize("prec", MIXED)
+def test_mixed_divergence_free_to_fp32_roundoff(prec):
     from pluto_gb300 import problems
     spec, vc, faces = problems.blast3d(32)
-    s = _s(spec, "mixed")
+    s = _s(spec, prec)
     s.upload(vc, faces)
     s.run(20, spec["first_dt"], spec["cfl"])
     _, b = s.download()
@@ -66,14 +73,15 @@ def test_mixed_upload_roundtrip_is_fp32_rounding():
     assert np.array_equal(v2, vc.astype(np.float32).astype(np.float64))
 
 
-def test_mixed_rk3_ppm_turbulence_small():
+@pytest.mark.parametrize("prec", MIXED)
+def test_mixed_rk3_ppm_turbulence_small(prec):
     from pluto_gb300 import problems
     spec, vc, faces = problems.turbulence3d(24, seed=1)
     out = {}
-    for prec in ("fp64", "mixed"):
-        s = _s(spec, prec)
+    for p in ("fp64", prec):
+        s = _s(spec, p)
         s.upload(vc, faces)
         s.run(10, spec["first_dt"], spec["cfl"])
-        out[prec] = s.download()[0]
-    errs = [rel_l1(out["mixed"][q], out["fp64"][q]) for q in range(8)]
+        out[p] = s.download()[0]
+    errs = [rel_l1(out[prec][q], out["fp64"][q]) for q in range(8)]
     assert max(errs) <= 1e-5, errs
