@@ -1,0 +1,179 @@
+/* ///////////////////////////////////////////////////////////////////// */
+/*!
+  \file
+  \brief GB300 replacement for PLUTO's unsplit RK AdvanceStep().
+
+  Link this object instead of rk_step.o and update_stage.o (the objects the
+  setup tool lists for an unsplit RK scheme) and add -lpluto_gb300 -lcudart.
+  It defines the same symbol PLUTO's Integrate() calls,
+
+      int AdvanceStep (Data *d, Riemann_Solver *Riemann,
+                       timeStep *Dts, Grid *grid)      (Src/prototypes.h:5)
+
+  and forwards the step to libpluto_gb300 through its C ABI
+  (include/pluto_gb300.h).  The scheme is read from the same definitions.h
+  macros the reference uses, the Riemann solver from the function pointer
+  SetSolver() returned (Src/MHD/set_solver.c:40-47).
+
+  Device residency: the state lives on the GPU between steps.  It is
+  uploaded on the first call and whenever the environment variable
+  PLUTO_GPU_UPLOAD_EVERY says so (e.g. after a restart or when init code
+  changed d->Vc), and downloaded into d->Vc / d->Vs every
+  PLUTO_GPU_SYNC_EVERY steps (default 1: the host arrays are always
+  current, as output, analysis and restart in Src/main.c expect).
+
+  Errors: a non-zero status from the library is fatal, as the reference's
+  own fatal conditions are (QUIT_PLUTO).
+*/
+/* ///////////////////////////////////////////////////////////////////// */
+#include <stdlib.h>
+#include <string.h>
+
+#include "pluto.h"
+#include "pluto_gb300.h"
+
+static pg_solver *s_gpu = NULL;
+static long s_calls = 0;
+
+static int gpu_riemann(Riemann_Solver *R)
+{
+  if (R == HLL_Solver)  return PG_HLL;
+  if (R == HLLD_Solver) return PG_HLLD;
+  if (R == Roe_Solver)  return PG_ROE;
+  return -1;
+}
+
+static int gpu_bc(int t)
+{
+  if (t == PERIODIC) return PG_PERIODIC;
+  if (t == OUTFLOW)  return PG_OUTFLOW;
+  return -1;
+}
+
+static void gpu_config(pg_config *c, Riemann_Solver *Riemann, Grid *grid)
+{
+  int d;
+  const char *prec = getenv("PLUTO_GPU_PRECISION");
+
+  memset(c, 0, sizeof *c);
+  c->dims       = DIMENSIONS;
+  c->components = COMPONENTS;
+  for (d = 0; d < 3; d++) {
+    c->nx[d] = d < DIMENSIONS ? grid->np_int[d] : 1;
+    c->dx[d] = d < DIMENSIONS ? grid->dx[d][grid->nghost[d]] : 1.0;
+    c->bc[d] = d < DIMENSIONS ? gpu_bc(grid->lbound[d]) : PG_PERIODIC;
+    if (d < DIMENSIONS && grid->lbound[d] != grid->rbound[d]) c->bc[d] = -1;
+  }
+  c->gamma = g_gamma;
+#if RECONSTRUCTION == PARABOLIC
+  c->reconstruction = PG_PARABOLIC;
+#else
+  c->reconstruction = PG_LINEAR;
+#endif
+#if LIMITER == MC_LIM
+  c->limiter = PG_MC_LIM;
+#elif LIMITER == MINMOD_LIM
+  c->limiter = PG_MINMOD_LIM;
+#elif LIMITER == VANLEER_LIM
+  c->limiter = PG_VANLEER_LIM;
+#elif LIMITER == FLAT_LIM
+  c->limiter = PG_FLAT_LIM;
+#else
+  c->limiter = PG_DEFAULT_LIM;
+#endif
+  c->riemann = gpu_riemann(Riemann);
+#if TIME_STEPPING == RK3
+  c->time_stepping = PG_RK3;
+#else
+  c->time_stepping = PG_RK2;
+#endif
+#ifdef STAGGERED_MHD
+  c->divb = PG_CONSTRAINED_TRANSPORT;
+  c->emf_average = PG_UCT_HLL;
+#else
+  c->divb = PG_DIVB_NONE;
+#endif
+  c->precision = PG_FP64;
+  if (prec && !strcmp(prec, "mixed"))    c->precision = PG_MIXED;
+  if (prec && !strcmp(prec, "mixed_dw")) c->precision = PG_MIXED_DW;
+  c->compute_mach = 1;
+  c->small_density  = g_smallDensity;
+  c->small_pressure = g_smallPressure;
+}
+
+/* Pointers to PLUTO's host arrays in the 8-slot order of the C ABI. */
+static void gpu_host_arrays(Data *d, double *vars[8], double *faces[3])
+{
+  int q;
+  for (q = 0; q < 8; q++) vars[q] = NULL;
+  faces[0] = faces[1] = faces[2] = NULL;
+  vars[0] = d->Vc[RHO][0][0];
+  EXPAND(vars[1] = d->Vc[VX1][0][0];  ,
+         vars[2] = d->Vc[VX2][0][0];  ,
+         vars[3] = d->Vc[VX3][0][0];)
+  EXPAND(vars[4] = d->Vc[BX1][0][0];  ,
+         vars[5] = d->Vc[BX2][0][0];  ,
+         vars[6] = d->Vc[BX3][0][0];)
+  vars[7] = d->Vc[PRS][0][0];
+#ifdef STAGGERED_MHD
+  /* ArrayBox storage is contiguous; pass the first element (index -1
+     along the staggered axis), Src/initialize.c:448-453. */
+  D_EXPAND(faces[0] = &d->Vs[BX1s][0][0][-1];  ,
+           faces[1] = &d->Vs[BX2s][0][-1][0];  ,
+           faces[2] = &d->Vs[BX3s][-1][0][0];)
+#endif
+}
+
+static void gpu_check(int rc, const char *where)
+{
+  if (rc != PG_OK) {
+    print ("! AdvanceStep (GPU): %s failed (%d): %s\n", where, rc, pg_last_error());
+    QUIT_PLUTO(1);
+  }
+}
+
+/* ********************************************************************* */
+int AdvanceStep (Data *d, Riemann_Solver *Riemann, timeStep *Dts, Grid *grid)
+/*!
+ * Advance the solution by one unsplit RK step on the GPU.
+ *
+ * \param [in,out]      d  pointer to Data structure
+ * \param [in]    Riemann  pointer to a Riemann solver function
+ * \param [in,out]    Dts  pointer to time step structure
+ * \param [in]       grid  pointer to Grid structure
+ *********************************************************************** */
+{
+  double *vars[8], *faces[3];
+  pg_step_info info;
+  const char *env;
+  long up_every = 0, sync_every = 1;
+
+  if ((env = getenv("PLUTO_GPU_UPLOAD_EVERY")) != NULL) up_every = atol(env);
+  if ((env = getenv("PLUTO_GPU_SYNC_EVERY")) != NULL)   sync_every = atol(env);
+  if (sync_every < 1) sync_every = 1;
+
+  gpu_host_arrays(d, vars, faces);
+  if (s_gpu == NULL) {
+    pg_config cfg;
+    gpu_config(&cfg, Riemann, grid);
+    gpu_check(pg_create(&cfg, &s_gpu), "pg_create");
+    gpu_check(pg_upload(s_gpu, (const double *const *)vars, (const double *const *)faces,
+                        PG_LAYOUT_PLUTO), "pg_upload");
+  } else if (up_every > 0 && s_calls % up_every == 0) {
+    gpu_check(pg_upload(s_gpu, (const double *const *)vars, (const double *const *)faces,
+                        PG_LAYOUT_PLUTO), "pg_upload");
+  }
+
+  gpu_check(pg_advance(s_gpu, g_dt, &info), "pg_advance");
+  s_calls++;
+
+/* -- the quantities NextTimeStep() and the log read (Src/main.c:389-575) -- */
+
+  Dts->invDt_hyp = MAX(Dts->invDt_hyp, info.inv_dt_hyp);
+  g_maxMach      = MAX(g_maxMach, info.max_mach);
+
+  if (s_calls % sync_every == 0) {
+    gpu_check(pg_download(s_gpu, vars, faces, PG_LAYOUT_PLUTO), "pg_download");
+  }
+  return 0;
+}

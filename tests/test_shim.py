@@ -1,0 +1,51 @@
+"""The PLUTO-side shim compiles against the reference's headers and links a
+complete PLUTO executable with libpluto_gb300 in place of the RK objects.
+
+Needs the reference source tree (skipped where it is absent, e.g. on the GPU
+machine); no GPU is used: the binary is built, not run.
+"""
+import os
+import subprocess
+from pathlib import Path
+
+import pytest
+
+ROOT = Path(__file__).resolve().parents[1]
+REF = Path(os.environ.get("PLUTO_REF", "/root/reference"))
+
+pytestmark = pytest.mark.skipif(not (REF / "Src" / "main.c").exists(), reason="reference tree absent")
+
+
+def _link(setup_fn, tmp_path):
+    from oracle import build_ref as br
+    from pluto_gb300 import build as pb
+    lib = pb.build()
+    s = setup_fn()
+    run = br.build(s)  # reference objects for this scheme
+    objs = [p for p in (run / "obj").glob("*.o") if p.stem not in ("rk_step", "update_stage")]
+    inc = ["-I", str(run)] + sum((["-I", str(REF / d)] for d in br.INC_DIRS), []) + ["-I", str(ROOT / "include")]
+    shim_o = tmp_path / "gpu_step.o"
+    subprocess.run(["gcc", "-c", "-O2", "-Wall", "-Wno-unused-variable", *inc,
+                    str(ROOT / "pluto_gb300" / "shim" / "gpu_step.c"), "-o", str(shim_o)],
+                   check=True, capture_output=True, text=True)
+    exe = tmp_path / "pluto_gpu"
+    r = subprocess.run(["g++", *map(str, objs), str(shim_o), f"-L{lib.parent}", "-lpluto_gb300",
+                        f"-Wl,-rpath,{lib.parent}", "-L/usr/local/cuda/lib64", "-lcudart", "-lm",
+                        "-o", str(exe)], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    return exe
+
+
+def test_shim_links_ot_ct(tmp_path):
+    from oracle import build_ref as br
+    assert _link(lambda: br.ot_setup("hlld", 32, 30), tmp_path).exists()
+
+
+def test_shim_links_1d_no_ct(tmp_path):
+    from oracle import build_ref as br
+    assert _link(lambda: br.tube_setup(0, 64, 10), tmp_path).exists()
+
+
+def test_shim_links_3d_ppm_rk3(tmp_path):
+    from oracle import build_ref as br
+    assert _link(lambda: br.turb_setup(12, 10), tmp_path).exists()
