@@ -29,7 +29,9 @@ ERRORS = {1: "PG_ERR_INVALID", 2: "PG_ERR_CUDA", 3: "PG_ERR_NOMEM", 4: "PG_ERR_N
 # Every symbol declared in include/pluto_gb300.h (checked by the CPU tests).
 EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
            "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
-           "pg_get_info", "pg_kernel_launches_per_step", "pg_last_error", "pg_abi_version"]
+           "pg_get_info", "pg_kernel_launches_per_step", "pg_last_error", "pg_abi_version",
+           "pg_tube_step_static"]
+PG_STATIC_MAX_ZONES = 32768
 
 
 class PgConfig(C.Structure):
@@ -85,10 +87,11 @@ def lib():
     L.pg_get_stream.argtypes = [vp, C.POINTER(vp)]
     L.pg_get_info.argtypes = [vp, C.POINTER(PgStepInfo), dp, dp]
     L.pg_kernel_launches_per_step.argtypes = [vp]
+    L.pg_tube_step_static.argtypes = [C.POINTER(PgConfig), vp, vp, C.c_double, vp, C.POINTER(PgStepInfo)]
     L.pg_last_error.restype = C.c_char_p
     for fn in ("pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
                "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
-               "pg_get_info", "pg_kernel_launches_per_step", "pg_abi_version"):
+               "pg_get_info", "pg_kernel_launches_per_step", "pg_abi_version", "pg_tube_step_static"):
         getattr(L, fn).restype = C.c_int
     _lib = L
     return L

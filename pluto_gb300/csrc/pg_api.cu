@@ -31,7 +31,8 @@ static int cuda_fail(cudaError_t e, const char* where) {
 extern "C" const char* pg_last_error(void) { return g_last_error.c_str(); }
 extern "C" int pg_abi_version(void) { return PG_ABI_VERSION; }
 
-static int validate(const pg_config* c) {
+namespace pg {
+int validate_config(const pg_config* c) {
   if (!c) return fail(PG_ERR_INVALID, "null config");
   if (c->dims < 1 || c->dims > 3) return fail(PG_ERR_INVALID, "dims must be 1..3");
   if (c->components != 2 && c->components != 3) return fail(PG_ERR_INVALID, "components must be 2 or 3");
@@ -63,27 +64,8 @@ static int validate(const pg_config* c) {
   return PG_OK;
 }
 
-static void free_all(Solver* S) {
-  if (S->graph) cudaGraphExecDestroy(S->graph);
-  S->graph = nullptr;
-  fp64_free(S);
-  mixed_free(S);
-  if (S->sc) cudaFree(S->sc);
-  if (S->sc_host) cudaFreeHost(S->sc_host);
-  if (S->stream) cudaStreamDestroy(S->stream);
-  S->sc = nullptr;
-  S->sc_host = nullptr;
-  S->stream = nullptr;
-}
-
-extern "C" int pg_create(const pg_config* cfg, pg_solver** out) {
-  if (!out) return fail(PG_ERR_INVALID, "null output pointer");
-  *out = nullptr;
-  int rc = validate(cfg);
-  if (rc) return rc;
-  pg_solver* h = new pg_solver();
-  Solver* S = &h->S;
-  S->cfg = *cfg;
+void init_geom(Solver* S) {
+  const pg_config* cfg = &S->cfg;
   S->ng = cfg->reconstruction == PG_PARABOLIC ? 3 : 2;  // Src/get_nghost.c:28-104
   Geom& g = S->g;
   g.dims = cfg->dims;
@@ -100,6 +82,33 @@ extern "C" int pg_create(const pg_config* cfg, pg_solver** out) {
   g.s[1] = g.nt[0];
   g.s[2] = (long long)g.nt[0] * g.nt[1];
   g.ncell = (long long)g.nt[0] * g.nt[1] * g.nt[2];
+}
+
+void set_last_error(const char* msg) { g_last_error = msg; }
+}  // namespace pg
+
+static void free_all(Solver* S) {
+  if (S->graph) cudaGraphExecDestroy(S->graph);
+  S->graph = nullptr;
+  fp64_free(S);
+  mixed_free(S);
+  if (S->sc) cudaFree(S->sc);
+  if (S->sc_host) cudaFreeHost(S->sc_host);
+  if (S->stream) cudaStreamDestroy(S->stream);
+  S->sc = nullptr;
+  S->sc_host = nullptr;
+  S->stream = nullptr;
+}
+
+extern "C" int pg_create(const pg_config* cfg, pg_solver** out) {
+  if (!out) return fail(PG_ERR_INVALID, "null output pointer");
+  *out = nullptr;
+  int rc = validate_config(cfg);
+  if (rc) return rc;
+  pg_solver* h = new pg_solver();
+  Solver* S = &h->S;
+  S->cfg = *cfg;
+  init_geom(S);
   cudaError_t e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {
     delete h;

@@ -628,3 +628,156 @@ int fp64_enqueue_step(Solver* S) {
 }
 
 }  // namespace pg
+
+// ===========================================================================
+// Allocation-free entry point: pg_tube_step_static
+//
+// For callers that cannot call cudaMalloc while they run: code executing
+// under CUDA stream capture (allocation is illegal inside a capture), a host
+// application that has handed all device memory to its own pool allocator,
+// or a real-time loop that must not hit the implicit device synchronisation
+// of cudaMalloc/cudaFree.  One plain-FP64 AdvanceStep of a 1D problem without
+// constrained transport (the Riemann-tube family: HLL/HLLD, PLM/PPM,
+// RK2/RK3, periodic or outflow) runs with every work array carved out of the
+// file-scope device array below, the same kernels as pg_advance.
+//
+// The array is sized for PG_STATIC_MAX_ZONES interior zones (plus ghosts):
+// 51 double arrays + flags + scalars, about 13.4 MB, held by every GPU that
+// loads this library until the process exits.  Larger problems are
+// rejected with PG_ERR_TOO_LARGE.  All calls share the array and it keeps
+// the last call's contents; everything a step reads is written earlier in
+// the same step, and the scalars are cleared on entry.  Calls that overlap
+// on the GPU (two streams, two host threads) race on the array: serialise
+// them.  The first call on a device looks up the array's device address
+// (cudaGetSymbolAddress) and caches it; make that first call before any
+// stream capture begins.
+// ===========================================================================
+namespace pg {
+
+constexpr long long kStaticZones = PG_STATIC_MAX_ZONES + 6;  // + up to 3 ghosts per side
+constexpr int kStaticArrays = 6 * 8 + 3;                     // V U U0 VP VM F, P CM CDT
+constexpr size_t kStaticDoubles = (size_t)kStaticArrays * kStaticZones;
+constexpr size_t kStaticBytes =
+    kStaticDoubles * sizeof(double) + ((kStaticZones + 255) / 256) * 256 + sizeof(DevScalars);
+
+static __device__ __align__(256) unsigned char g_pg_static_scratch[kStaticBytes];
+
+static void* s_static_base[64];  // device address of the array, per device
+
+__global__ void k_static_setup(DevScalars* sc, double dt) {
+  sc->dt = dt;
+  sc->dt_prev = 0.0;
+  sc->time = 0.0;
+  sc->inv_dt_bits = 0ull;
+  sc->mach_bits = 0ull;
+  sc->nfail = 0ull;
+  sc->status = 0;
+}
+
+// The pointer table travels by value as a kernel argument.
+struct StaticVTab {
+  double* V[8];
+};
+
+// Caller's [8][nx] interior state <-> the ghosted arrays of the step.
+__global__ void k_static_copy(StaticVTab t, const double* src, double* dst, int nx, int beg, int to_state) {
+  int q = blockIdx.x * blockDim.x + threadIdx.x;
+  if (q >= NV * nx) return;
+  int nv = q / nx, i = q - nv * nx;
+  if (to_state) t.V[nv][beg + i] = src[q];
+  else dst[q] = t.V[nv][beg + i];
+}
+
+}  // namespace pg
+
+extern "C" int pg_tube_step_static(const pg_config* cfg, const double* v_in, double* v_out, double dt,
+                                   void* cuda_stream, pg_step_info* info) {
+  using namespace pg;
+  if (!cfg || !v_in || !v_out) {
+    set_last_error("pg_tube_step_static: null argument");
+    return PG_ERR_INVALID;
+  }
+  int rc = validate_config(cfg);
+  if (rc) return rc;
+  if (cfg->dims != 1 || cfg->divb != PG_DIVB_NONE || cfg->precision != PG_FP64) {
+    set_last_error("pg_tube_step_static: only 1D FP64 problems without constrained transport");
+    return PG_ERR_INVALID;
+  }
+  if (cfg->nx[0] > PG_STATIC_MAX_ZONES) {
+    set_last_error("pg_tube_step_static: nx exceeds PG_STATIC_MAX_ZONES (32768 zones)");
+    return PG_ERR_TOO_LARGE;
+  }
+  if (!(dt > 0)) {
+    set_last_error("pg_tube_step_static: dt must be positive");
+    return PG_ERR_INVALID;
+  }
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess || dev < 0 || dev >= 64) {
+    set_last_error("pg_tube_step_static: no current CUDA device");
+    return PG_ERR_CUDA;
+  }
+  if (!s_static_base[dev]) {  // once per device, with that device current
+    void* p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress(&p, g_pg_static_scratch);
+    if (e != cudaSuccess || !p) {
+      set_last_error("pg_tube_step_static: cudaGetSymbolAddress failed");
+      return PG_ERR_CUDA;
+    }
+    s_static_base[dev] = p;
+  }
+  // A solver description on the host stack; every device pointer is a slice
+  // of the static array.
+  Solver S;
+  S.cfg = *cfg;
+  init_geom(&S);
+  S.stream = (cudaStream_t)cuda_stream;
+  S.device_dt = false;
+  const long long n = S.g.ncell;  // <= kStaticZones
+  double* d = (double*)s_static_base[dev];
+  int a = 0;
+  for (int nv = 0; nv < 8; nv++) {
+    S.V[nv] = d + (size_t)(a++) * kStaticZones;
+    S.U[nv] = d + (size_t)(a++) * kStaticZones;
+    S.U0[nv] = d + (size_t)(a++) * kStaticZones;
+    S.VP[nv] = d + (size_t)(a++) * kStaticZones;
+    S.VM[nv] = d + (size_t)(a++) * kStaticZones;
+    S.F[nv] = d + (size_t)(a++) * kStaticZones;
+  }
+  S.P = d + (size_t)(a++) * kStaticZones;
+  S.CM = d + (size_t)(a++) * kStaticZones;
+  S.CDT = d + (size_t)(a++) * kStaticZones;
+  unsigned char* tail = (unsigned char*)(d + kStaticDoubles);
+  S.flag = tail;
+  S.sc = (DevScalars*)(tail + ((kStaticZones + 255) / 256) * 256);
+  (void)n;
+  StaticVTab vt;
+  for (int nv = 0; nv < 8; nv++) vt.V[nv] = S.V[nv];
+  k_static_setup<<<1, 1, 0, S.stream>>>(S.sc, dt);
+  const int nx = S.g.nx[0], beg = S.g.beg[0];
+  k_static_copy<<<(8 * nx + 255) / 256, 256, 0, S.stream>>>(vt, v_in, nullptr, nx, beg, 1);
+  rc = fp64_enqueue_step(&S);
+  if (rc) {
+    set_last_error("pg_tube_step_static: kernel launch failed");
+    return PG_ERR_CUDA;
+  }
+  k_static_copy<<<(8 * nx + 255) / 256, 256, 0, S.stream>>>(vt, nullptr, v_out, nx, beg, 0);
+  DevScalars hs;
+  if (cudaMemcpyAsync(&hs, S.sc, sizeof hs, cudaMemcpyDeviceToHost, S.stream) != cudaSuccess ||
+      cudaStreamSynchronize(S.stream) != cudaSuccess) {
+    set_last_error("pg_tube_step_static: CUDA error during the step");
+    return PG_ERR_CUDA;
+  }
+  if (info) {
+    double inv, mach;
+    memcpy(&inv, &hs.inv_dt_bits, sizeof inv);
+    memcpy(&mach, &hs.mach_bits, sizeof mach);
+    info->inv_dt_hyp = inv;
+    info->max_mach = mach;
+    info->nfail = (int64_t)hs.nfail;
+  }
+  if (hs.status) {
+    set_last_error("pg_tube_step_static: non-finite state");
+    return PG_ERR_NAN;
+  }
+  return PG_OK;
+}

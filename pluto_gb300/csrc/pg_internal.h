@@ -81,6 +81,9 @@ int fp64_enqueue_step(Solver* S);  // all stages of one step on S->stream
 int mixed_alloc(Solver* S);
 void mixed_free(Solver* S);
 int mixed_enqueue_step(Solver* S);
+int validate_config(const pg_config* c);
+void init_geom(Solver* S);
+void set_last_error(const char* msg);
 // host <-> device copy of one FP64 array in the interior or PLUTO layout
 int xfer_f64(Solver* S, double* dev, double* host, int fd, int layout, bool to_dev);
 
