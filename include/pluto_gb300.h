@@ -53,8 +53,10 @@ enum { PG_PERIODIC = 0, PG_OUTFLOW = 1 };                         /* [Boundary] 
 /* arithmetic: PG_FP64 bit-compatible with the reference C path;
    PG_MIXED FP32 storage and fluxes, FP64 accumulation / pressure recovery /
    face update / dt reduction; PG_MIXED_DW the same with the FP64 parts done
-   as FP32 double-word pairs (48-bit significand) on the FP32 pipes. */
-enum { PG_FP64 = 0, PG_MIXED = 1, PG_MIXED_DW = 2 };
+   as FP32 double-word pairs (48-bit significand) on the FP32 pipes.
+   PG_FP64_TANGENT: the FP64 step together with its tangent-linear model
+   (each value carries one directional derivative; see pg_tangent_upload). */
+enum { PG_FP64 = 0, PG_MIXED = 1, PG_MIXED_DW = 2, PG_FP64_TANGENT = 3 };
 enum { PG_LAYOUT_INTERIOR = 0, PG_LAYOUT_PLUTO = 1 };             /* host array layout */
 
 typedef struct {
@@ -130,6 +132,63 @@ int pg_run_timed(pg_solver *s, int nsteps, double first_dt, double cfl, double c
 int pg_profile_kernels(pg_solver *s, int nsteps, double first_dt, double cfl, double cfl_max_var,
                        char *names, int name_stride, double *total_ms, int *launches,
                        int max_kernels, int *n_kernels);
+
+/* ---------------------------------------------------------------------
+   Differentiation (no reference counterpart: PLUTO has no adjoint).
+   The step is differentiated for a given, frozen dt; the derivative follows
+   the limiter, Riemann-solver and floor branches the forward step takes.
+   --------------------------------------------------------------------- */
+/* PG_FP64_TANGENT solvers: pg_upload sets the state with a zero tangent;
+   these set / read the tangent (direction) of the same arrays, same layouts.
+   pg_advance then moves state and tangent together. */
+int pg_tangent_upload(pg_solver *s, const double *const vars[8], const double *const faces[3],
+                      int layout);
+int pg_tangent_download(pg_solver *s, double *const vars[8], double *const faces[3], int layout);
+
+/* PG_FP64 solvers with RK2: adjoint of one step.  pg_adjoint_set loads the
+   adjoint (gradient of a scalar with respect to the state after the step)
+   into device buffers; pg_adjoint_step(dt) replaces it, on the device, with
+   the gradient with respect to the state before a step of length dt taken
+   from the solver's current state (which it leaves unchanged);
+   pg_adjoint_get reads it back.  Adjoint values on ghost zones are ignored
+   on set and zero on get. */
+int pg_adjoint_set(pg_solver *s, const double *const vars[8], const double *const faces[3],
+                   int layout);
+int pg_adjoint_step(pg_solver *s, double dt);
+int pg_adjoint_get(pg_solver *s, double *const vars[8], double *const faces[3], int layout);
+
+/* Device-resident state checkpoints (PG_FP64 / PG_FP64_TANGENT): copy the
+   whole state into slot (0..PG_MAX_CHECKPOINTS-1, allocated on first use)
+   or back. */
+#define PG_MAX_CHECKPOINTS 256
+int pg_checkpoint_save(pg_solver *s, int slot);
+int pg_checkpoint_load(pg_solver *s, int slot);
+
+/* ---------------------------------------------------------------------
+   Batched independent 1D problems ("tubes"), each an independent PLUTO run
+   (Src/main.c step loop with its own NextTimeStep dt), all advanced by one
+   persistent, CUDA-graph-captured launch.  cfg supplies the scheme (dims 1,
+   no constrained transport; PLM minmod/MC or PPM; HLL/HLLD; RK2/RK3;
+   PG_FP64 / PG_MIXED / PG_MIXED_DW; nx/dx are taken per tube).
+   --------------------------------------------------------------------- */
+typedef struct pg_batch pg_batch;
+int pg_batch_create(const pg_config *cfg, int ntubes, const int *nx, const double *dx,
+                    pg_batch **out);
+int pg_batch_destroy(pg_batch *b);
+/* vars: the tubes one after the other, each [8][nx_t] interior zones. */
+int pg_batch_upload(pg_batch *b, const double *vars);
+int pg_batch_download(pg_batch *b, double *vars);
+/* nsteps steps of every tube; first_dt > 0 restarts each tube at t = 0;
+   cfl <= 0 keeps every tube's dt fixed (no NextTimeStep update). */
+int pg_batch_run(pg_batch *b, int nsteps, double first_dt, double cfl, double cfl_max_var,
+                 double *elapsed_ms);
+int pg_batch_get(pg_batch *b, double *time, double *dt, int64_t *nfail);
+/* Schedule autotuner: times trial_steps for each (threads per CTA, CTAs per
+   SM, queue order) candidate from the same state, keeps the fastest and
+   restores the state. */
+int pg_batch_autotune(pg_batch *b, int trial_steps, double first_dt, double cfl, double cfl_max_var,
+                      int *best_threads, int *best_blocks_per_sm, int *best_order, double *best_ms);
+int pg_batch_set_schedule(pg_batch *b, int threads, int blocks_per_sm, int largest_first);
 
 /* Allocation-free variant of one 1D AdvanceStep (no reference counterpart;
    an addition of this library).  For callers that may not allocate device

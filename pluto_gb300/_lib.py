@@ -20,7 +20,7 @@ PG_RK2, PG_RK3 = 2, 3
 PG_DIVB_NONE, PG_CONSTRAINED_TRANSPORT = 0, 1
 PG_UCT_HLL = 4
 PG_PERIODIC, PG_OUTFLOW = 0, 1
-PG_FP64, PG_MIXED, PG_MIXED_DW = 0, 1, 2
+PG_FP64, PG_MIXED, PG_MIXED_DW, PG_FP64_TANGENT = 0, 1, 2, 3
 PG_LAYOUT_INTERIOR, PG_LAYOUT_PLUTO = 0, 1
 
 ERRORS = {1: "PG_ERR_INVALID", 2: "PG_ERR_CUDA", 3: "PG_ERR_NOMEM", 4: "PG_ERR_NAN",
@@ -30,8 +30,12 @@ ERRORS = {1: "PG_ERR_INVALID", 2: "PG_ERR_CUDA", 3: "PG_ERR_NOMEM", 4: "PG_ERR_N
 EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
            "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
            "pg_get_info", "pg_kernel_launches_per_step", "pg_last_error", "pg_abi_version",
-           "pg_tube_step_static"]
+           "pg_tube_step_static", "pg_batch_create", "pg_batch_destroy", "pg_batch_upload",
+           "pg_batch_download", "pg_batch_run", "pg_batch_get", "pg_batch_autotune",
+           "pg_batch_set_schedule", "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set",
+           "pg_adjoint_step", "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load"]
 PG_STATIC_MAX_ZONES = 32768
+PG_MAX_CHECKPOINTS = 256
 
 
 class PgConfig(C.Structure):
@@ -88,10 +92,28 @@ def lib():
     L.pg_get_info.argtypes = [vp, C.POINTER(PgStepInfo), dp, dp]
     L.pg_kernel_launches_per_step.argtypes = [vp]
     L.pg_tube_step_static.argtypes = [C.POINTER(PgConfig), vp, vp, C.c_double, vp, C.POINTER(PgStepInfo)]
+    IP = C.POINTER(C.c_int)
+    L.pg_batch_create.argtypes = [C.POINTER(PgConfig), ip, IP, dp, C.POINTER(vp)]
+    L.pg_batch_destroy.argtypes = [vp]
+    L.pg_batch_upload.argtypes = [vp, dp]
+    L.pg_batch_download.argtypes = [vp, dp]
+    L.pg_batch_run.argtypes = [vp, ip, C.c_double, C.c_double, C.c_double, dp]
+    L.pg_batch_get.argtypes = [vp, dp, dp, C.POINTER(C.c_int64)]
+    L.pg_batch_autotune.argtypes = [vp, ip, C.c_double, C.c_double, C.c_double, IP, IP, IP, dp]
+    L.pg_batch_set_schedule.argtypes = [vp, ip, ip, ip]
+    for fn in ("pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set", "pg_adjoint_get"):
+        getattr(L, fn).argtypes = [vp, C.POINTER(dp), C.POINTER(dp), ip]
+    L.pg_adjoint_step.argtypes = [vp, C.c_double]
+    L.pg_checkpoint_save.argtypes = [vp, ip]
+    L.pg_checkpoint_load.argtypes = [vp, ip]
     L.pg_last_error.restype = C.c_char_p
     for fn in ("pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
                "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
-               "pg_get_info", "pg_kernel_launches_per_step", "pg_abi_version", "pg_tube_step_static"):
+               "pg_get_info", "pg_kernel_launches_per_step", "pg_abi_version", "pg_tube_step_static",
+               "pg_batch_create", "pg_batch_destroy", "pg_batch_upload", "pg_batch_download",
+               "pg_batch_run", "pg_batch_get", "pg_batch_autotune", "pg_batch_set_schedule",
+               "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set", "pg_adjoint_step",
+               "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load"):
         getattr(L, fn).restype = C.c_int
     _lib = L
     return L

@@ -1,0 +1,143 @@
+"""Differentiable multi-step rollout over the C ABI.
+
+``Rollout`` advances a PLUTO domain through a fixed (frozen) sequence of time
+steps on the GPU.  ``rollout(runner, vc, *faces)`` is a
+``torch.autograd.Function``: its forward runs the steps and stores a
+device-resident checkpoint every ``every`` steps (``pg_checkpoint_save``);
+its backward walks the segments from last to first, recomputes the states
+inside a segment from its checkpoint, and applies the hand-written adjoint of
+each step (``pg_adjoint_step``) in reverse order.  The dt sequence is frozen:
+the derivative is that of the state map for the given dts, which is what
+PLUTO's own step computes for a given g_dt (Src/Time_Stepping/rk_step.c:27).
+
+``tangent_linear`` runs the FP64 tangent-linear model (precision
+"fp64_tangent") for the same dts: the directional derivative of the final
+state along a direction of the initial state.
+
+Tensors are CPU float64, as the C ABI takes host arrays (interior layout:
+cells [8][nz][ny][nx], face d one longer along axis d).
+"""
+from __future__ import annotations
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from .solver import Solver
+
+
+class Rollout:
+    """One FP64 solver and a frozen dt sequence."""
+
+    def __init__(self, spec: dict, dts, every: int = 16):
+        self.spec = dict(spec)
+        self.dts = [float(x) for x in dts]
+        self.every = int(every)
+        nseg = -(-len(self.dts) // self.every)
+        if nseg + self.every > L.PG_MAX_CHECKPOINTS:
+            raise ValueError("too many checkpoint slots for this many steps")
+        self.solver = Solver(spec, "fp64")
+        self.dims = self.solver.dims
+        self.ct = self.solver.ct
+
+    @property
+    def nsteps(self) -> int:
+        return len(self.dts)
+
+    def face_list(self, faces):
+        return [faces[d] if (self.ct and d < self.dims) else None for d in range(3)]
+
+    def run(self, vc, faces, checkpoint: bool = False):
+        s = self.solver
+        s.upload(vc, self.face_list(faces))
+        for q, dt in enumerate(self.dts):
+            if checkpoint and q % self.every == 0:
+                s.checkpoint_save(q // self.every)
+            s.advance(dt)
+        return s.download()
+
+    def gradient(self, lvc, lfaces):
+        """Adjoint of the whole rollout (after ``run(..., checkpoint=True)``)."""
+        s = self.solver
+        s.adjoint_set(lvc, self.face_list(lfaces))
+        n, e = self.nsteps, self.every
+        nseg = -(-n // e)
+        base = nseg  # slots of the states inside one segment
+        for seg in range(nseg - 1, -1, -1):
+            q0, q1 = seg * e, min(n, seg * e + e)
+            s.checkpoint_load(seg)
+            for q in range(q0, q1 - 1):  # states q0+1 .. q1-1 from the checkpoint
+                s.checkpoint_save(base + q - q0)
+                s.advance(self.dts[q])
+            s.checkpoint_save(base + q1 - 1 - q0)
+            for q in range(q1 - 1, q0 - 1, -1):
+                s.checkpoint_load(base + q - q0)
+                s.adjoint_step(self.dts[q])
+        return s.adjoint_get()
+
+
+class _RolloutFn(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, runner: Rollout, vc: torch.Tensor, *faces: torch.Tensor):
+        ctx.runner = runner
+        fin = [f.detach().numpy() if f is not None else None for f in faces]
+        vT, fT = runner.run(vc.detach().numpy(), fin + [None] * (3 - len(fin)), checkpoint=True)
+        outs = [torch.from_numpy(vT)]
+        for d in range(len(faces)):
+            outs.append(torch.from_numpy(fT[d]) if fT[d] is not None else None)
+        ctx.nfaces = len(faces)
+        return tuple(outs)
+
+    @staticmethod
+    def backward(ctx, gvc, *gfaces):
+        runner = ctx.runner
+        lvc = gvc.detach().numpy() if gvc is not None else np.zeros((8,) + tuple(reversed(runner.solver.nx)))
+        lf = []
+        for d in range(ctx.nfaces):
+            g = gfaces[d] if d < len(gfaces) else None
+            lf.append(g.detach().numpy() if g is not None else
+                      (np.zeros(runner.solver.face_shape(d)) if (runner.ct and d < runner.dims) else None))
+        gv, gf = runner.gradient(lvc, lf + [None] * (3 - len(lf)))
+        grads = [torch.from_numpy(gv)]
+        for d in range(ctx.nfaces):
+            grads.append(torch.from_numpy(gf[d]) if gf[d] is not None else None)
+        return (None, *grads)
+
+
+def rollout(runner: Rollout, vc: torch.Tensor, *faces: torch.Tensor):
+    """Differentiable rollout: returns (vc_T, *faces_T)."""
+    return _RolloutFn.apply(runner, vc, *faces)
+
+
+def tangent_linear(spec: dict, dts, vc, faces, dvc, dfaces):
+    """FP64 tangent-linear model: (final state, its derivative along (dvc, dfaces))."""
+    s = Solver(spec, "fp64_tangent")
+    try:
+        fl = [faces[d] if (s.ct and d < s.dims) else None for d in range(3)]
+        dl = [dfaces[d] if (s.ct and d < s.dims) else None for d in range(3)]
+        s.upload(vc, fl)
+        s.tangent_upload(dvc, dl)
+        for dt in dts:
+            s.advance(float(dt))
+        state = s.download()
+        tangent = s.tangent_download()
+    finally:
+        s.close()
+    return state, tangent
+
+
+def cfl_dt_sequence(spec: dict, vc, faces, nsteps: int, first_dt: float, cfl: float,
+                    cfl_max_var: float = 1.1):
+    """The dt sequence PLUTO's main loop takes from this state (NextTimeStep,
+    Src/main.c:459-532), recorded with single FP64 steps; returned frozen."""
+    s = Solver(spec, "fp64")
+    try:
+        s.upload(vc, [faces[d] if (s.ct and d < s.dims) else None for d in range(3)])
+        dts, dt = [], float(first_dt)
+        for _ in range(nsteps):
+            dts.append(dt)
+            inv, _, _ = s.advance(dt)  # invDt_hyp, already divided by DIMENSIONS
+            dt = min(cfl / inv, cfl_max_var * dt)
+    finally:
+        s.close()
+    return dts

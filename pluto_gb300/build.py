@@ -26,7 +26,8 @@ UNITS = {
     "pg_api.cu": [],
     "pg_fp64.cu": ["--fmad=false"],
     "pg_mixed.cu": ["--use_fast_math"],
-    "pg_batch.cu": [],
+    "pg_batch.cu": ["--fmad=false"],
+    "pg_batch_mixed.cu": ["--use_fast_math"],
     "pg_adjoint.cu": ["--fmad=false"],
 }
 

@@ -1,0 +1,1010 @@
+// Differentiated FP64 path: tangent-linear model, adjoint of one RK2 step,
+// device-resident checkpoints.
+//
+// Tangent-linear: the FP64 step kernels of pg_fp64_kernels.cuh instantiated
+// with T = Dual<1>; value parts are the plain FP64 step, derivative parts its
+// directional derivative through the branches taken (precision
+// PG_FP64_TANGENT).
+//
+// Adjoint: pg_adjoint_step maps lambda(n+1) -> lambda(n) for one RK2 step of
+// a given (frozen) dt.  The step is recomputed from the solver's state, then
+// each forward operation is undone in reverse order by a hand-written kernel:
+//   k_adj_c2p      ConsToPrim                  (Src/MHD/mappers.c:88-254)
+//   k_adj_avg      CT_AverageMagneticField     (Src/MHD/CT/ct_field_average.c:13)
+//   k_adj_rk_*     RK2 combination             (Src/Time_Stepping/rk_step.c:93-160)
+//   k_adj_ct       CT_Update                   (Src/MHD/CT/ct_update.c:29-220)
+//   k_adj_emf      CT_EMF_HLL_Solver           (Src/MHD/CT/ct_emf_average.c:179-352)
+//   k_adj_flux     RightHandSide, U += rhs     (Src/MHD/rhs.c:193-201)
+//   k_adj_riemann  HLL / HLLD flux with the face-field override
+//                  (Src/MHD/hll.c, Src/MHD/hlld.c, Src/States/plm_states.c:271)
+//   k_adj_recon    States (PLM / PPM) and CT_StoreVelSlopes
+//   k_adj_bound    Boundary (periodic / outflow copies), transposed
+//   k_adj_p2c      PrimToCons3D                (Src/mappers3D.c:74)
+// The local derivatives inside those kernels (limiter, reconstruction,
+// Riemann solver, edge EMF, prim<->cons maps) come from evaluating the same
+// templated point functions as the forward kernels with Dual<1> inputs, one
+// seeded input at a time, so they belong to exactly the branch the forward
+// evaluation takes, floors included.
+#include <cstring>
+#include <string>
+#include <utility>
+#include <vector>
+
+#include "pg_fp64_kernels.cuh"
+
+namespace pg {
+
+using D1 = Dual<1>;
+
+int tl_enqueue_step(Solver* S) { return fp64_enqueue_step_t<D1>(S); }
+
+// ---------------------------------------------------------------------------
+// tangent-solver transfers: FP64 staging array <-> value / tangent parts
+// ---------------------------------------------------------------------------
+__global__ void k_tl_put(D1* dst, const double* src, long long n, int part) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  if (part == 0) {
+    dst[q].v = src[q];
+    dst[q].d[0] = 0.0;
+  } else {
+    dst[q].d[0] = src[q];
+  }
+}
+__global__ void k_tl_get(double* dst, const D1* src, long long n, int part) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q < n) dst[q] = part == 0 ? src[q].v : src[q].d[0];
+}
+
+static int ensure_stage(Solver* S) {
+  if (S->stage) return PG_OK;
+  if (cudaMalloc(&S->stage, S->g.ncell * sizeof(double)) != cudaSuccess) {
+    S->stage = nullptr;
+    set_last_error("staging allocation failed");
+    return PG_ERR_NOMEM;
+  }
+  return PG_OK;
+}
+
+int tl_xfer(Solver* S, double* const vars[8], double* const faces[3], int layout, bool to_dev, int part) {
+  if (layout != PG_LAYOUT_INTERIOR && layout != PG_LAYOUT_PLUTO) {
+    set_last_error("bad layout");
+    return PG_ERR_INVALID;
+  }
+  int rc = ensure_stage(S);
+  if (rc) return rc;
+  const Geom& g = S->g;
+  const long long n = g.ncell;
+  cudaStream_t st = S->stream;
+  const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
+  if (to_dev && ct && !faces) {
+    set_last_error("constrained transport needs staggered fields");
+    return PG_ERR_INVALID;
+  }
+  auto one = [&](double* dev_arr, double* host, int fd) -> int {
+    D1* arr = (D1*)dev_arr;
+    if (to_dev) {
+      cudaMemsetAsync(S->stage, 0, n * sizeof(double), st);
+      if (host) {
+        int r = xfer_f64(S, S->stage, host, fd, layout, true);
+        if (r) return r;
+      }
+      k_tl_put<<<grid_for(n), kThreads, 0, st>>>(arr, S->stage, n, part);
+    } else if (host) {
+      k_tl_get<<<grid_for(n), kThreads, 0, st>>>(S->stage, arr, n, part);
+      int r = xfer_f64(S, S->stage, host, fd, layout, false);
+      if (r) return r;
+    }
+    return PG_OK;
+  };
+  for (int nv = 0; nv < 8; nv++)
+    if ((rc = one(S->V[nv], vars ? vars[nv] : nullptr, -1))) return rc;
+  if (ct && faces)
+    for (int d = 0; d < g.dims; d++) {
+      if (to_dev && !faces[d]) {
+        set_last_error("missing staggered component");
+        return PG_ERR_INVALID;
+      }
+      if ((rc = one(S->Bs[d], faces[d], d))) return rc;
+    }
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    set_last_error(cudaGetErrorString(e));
+    return PG_ERR_CUDA;
+  }
+  return PG_OK;
+}
+
+// ---------------------------------------------------------------------------
+// point functions evaluated by the adjoint kernels (the arithmetic of the
+// forward kernels, written over a small input vector)
+// ---------------------------------------------------------------------------
+
+// States of one zone from w[0..4] = v[c-2..c+2] (as k_recon).
+template <class T>
+__device__ __forceinline__ void recon_pt(int recon, int lim, int nv, const T* w, T& vp, T& vm) {
+  if (recon == PG_LINEAR) {
+    T v0 = w[2];
+    T dvp = w[3] - v0;
+    T dvm = v0 - w[1];
+    T dv = limit(lim, nv, dvp, dvm);
+    vp = v0 + dv * 0.5;
+    vm = v0 - dv * 0.5;
+  } else {
+    T v0 = w[2];
+    T p = ppm_iface(w[1], v0, w[3], w[4]);
+    T m = ppm_iface(w[0], w[1], v0, w[3]);
+    ppm_limit(v0, p, m);
+    vp = p;
+    vm = m;
+  }
+}
+
+// Riemann outputs at one interface (as k_riemann):
+// out[0..7] flux, out[8] total pressure, out[9] max(0,-SL), out[10] max(0,SR).
+template <class T, int DIR>
+__device__ __forceinline__ void riemann_pt(int solver, double gamma, const T* vL, const T* vR, T* out) {
+  T uL[NV], uR[NV], mach = T(0.0);
+  const T gmm1 = T(gamma - 1.0);
+  prim_to_cons(vL, uL, gmm1);
+  prim_to_cons(vR, uR, gmm1);
+  Iface<T> o;
+  if (solver == PG_HLL) hll_solver<DIR, false>(vL, uL, vR, uR, T(gamma), o, mach);
+  else hlld_solver<DIR, false>(vL, uL, vR, uR, T(gamma), o, mach);
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) out[nv] = o.f[nv];
+  out[NV] = o.press;
+  out[NV + 1] = pmax(T(0.0), -o.SL);
+  out[NV + 2] = pmax(T(0.0), o.SR);
+}
+
+// Edge EMF from its 40 inputs (as uct_edge):
+//  in[0..7]   SR_x(c00) SR_x(c0y) SL_x(c00) SL_x(c0y) SR_y(c00) SR_y(cx0) SL_y(c00) SL_y(cx0)
+//  in[8..11]  x-face field at c00-sy, c00, c0y, c0y+sy
+//  in[12..15] y-face field at c00-sx, c00, cx0, cx0+sx
+//  in[16..39] per zone q of (c00, cx0, c0y, cxy): vy, vx, dvy_dx, dvy_dy, dvx_dx, dvx_dy
+constexpr int kEdgeIn = 40;
+template <class T>
+__device__ __forceinline__ T emf_pt(const T* in) {
+  T a_xp = pmax(in[0], in[1]);
+  T a_xm = pmax(in[2], in[3]);
+  T a_yp = pmax(in[4], in[5]);
+  T a_ym = pmax(in[6], in[7]);
+  T sbS = mc_lim2(in[10] - in[9], in[9] - in[8]);
+  T sbN = mc_lim2(in[11] - in[10], in[10] - in[9]);
+  T sbW = mc_lim2(in[14] - in[13], in[13] - in[12]);
+  T sbE = mc_lim2(in[15] - in[14], in[14] - in[13]);
+  T bS = in[9] + 0.5 * sbS;
+  T bW = in[13] + 0.5 * sbW;
+  T bN = in[10] - 0.5 * sbN;
+  T bE = in[14] - 0.5 * sbE;
+  const T* q0 = in + 16;  // c00
+  const T* q1 = in + 22;  // cx0
+  const T* q2 = in + 28;  // c0y
+  const T* q3 = in + 34;  // cxy
+  T eSW = (q0[0] + 0.5 * (q0[2] + q0[3])) * bS - (q0[1] + 0.5 * (q0[4] + q0[5])) * bW;
+  T eSE = (q1[0] - 0.5 * (q1[2] - q1[3])) * bS - (q1[1] - 0.5 * (q1[4] - q1[5])) * bE;
+  T eNE = (q3[0] - 0.5 * (q3[2] + q3[3])) * bN - (q3[1] - 0.5 * (q3[4] + q3[5])) * bE;
+  T eNW = (q2[0] + 0.5 * (q2[2] - q2[3])) * bN - (q2[1] + 0.5 * (q2[4] - q2[5])) * bW;
+  return uct_hll_combine(a_xp, a_xm, a_yp, a_ym, eSW, eSE, eNE, eNW, bS, bN, bW, bE);
+}
+
+// ---------------------------------------------------------------------------
+// adjoint buffers
+// ---------------------------------------------------------------------------
+struct AdjBufs {
+  // adjoint variables (full ghosted arrays)
+  double* lV[8];    // on the primitive state after the part being undone
+  double* lB[3];    // on the face field likewise
+  double* lVin[8];  // on the stage-input primitives
+  double* lBin[3];  // on the stage-input faces
+  double* lU[8];    // on the conserved variables inside a stage
+  double* lU0[8];   // on U0 = PrimToCons(V^n)
+  double* lUx[8];   // on U1 through the base of stage 2
+  double* lB0[3];   // on B^n through the RK2 face combination
+  double* lVP[8];
+  double* lVM[8];
+  double* lF[8];
+  double* lP;
+  double* lS[3][2];  // on max(0,-SL) and max(0,SR) per direction
+  double* lDV[3][3];
+  double* lE[3];
+  // forward states saved by the recomputation
+  double* Vn[8];
+  double* Bn[3];
+  double* V1[8];
+  double* B1[3];
+  double* U1[8];
+  double* U2[8];
+};
+
+struct AdjArgs {
+  F64A<double> f;  // forward arrays (the solver's own)
+  AdjBufs b;
+  double dt;
+};
+
+struct Tab8 {
+  double* p[8];
+};
+
+__device__ __forceinline__ bool in_dom(const Geom& g, int i, int j, int k) {
+  return i >= g.beg[0] && i <= g.end[0] && j >= g.beg[1] && j <= g.end[1] && k >= g.beg[2] && k <= g.end[2];
+}
+__device__ __forceinline__ void cell_ijk(const Geom& g, long long c, int& i, int& j, int& k) {
+  i = (int)(c % g.nt[0]);
+  j = (int)((c / g.nt[0]) % g.nt[1]);
+  k = (int)(c / ((long long)g.nt[0] * g.nt[1]));
+}
+// faces written by CT_Update for component fd (ct_update.c:79-81,132-134,188-190)
+__device__ __forceinline__ bool ct_face(const Geom& g, int fd, int i, int j, int k) {
+  const int x[3] = {i, j, k};
+  for (int ax = 0; ax < g.dims; ax++) {
+    const int lo = g.beg[ax] - (ax == fd ? 1 : 0), hi = g.end[ax];
+    if (x[ax] < lo || x[ax] > hi) return false;
+  }
+  return g.dims == 3 || k == 0;
+}
+
+#define ADJ_CELL_PROLOGUE                                         \
+  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x; \
+  const Geom& g = A.f.g;                                          \
+  if (c >= g.ncell) return;                                       \
+  int i, j, k;                                                    \
+  cell_ijk(g, c, i, j, k);
+
+// lU = J_C(U)^T lambda_V (+ lUx), zero off the domain.
+__global__ void k_adj_c2p(AdjArgs A, Tab8 Ust, Tab8 L, int add_ux) {
+  ADJ_CELL_PROLOGUE
+  if (!in_dom(g, i, j, k)) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) A.b.lU[nv][c] = 0.0;
+    return;
+  }
+  double lv[NV], u0[NV];
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    lv[nv] = L.p[nv][c];
+    u0[nv] = Ust.p[nv][c];
+  }
+  for (int kk = 0; kk < NV; kk++) {
+    D1 u[NV], v[NV];
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) u[nv] = D1(u0[nv]);
+    u[kk].d[0] = 1.0;
+    unsigned char fl = 0;
+    cons_to_prim(u, v, D1(A.f.gamma - 1.0), D1(A.f.small_rho), D1(A.f.small_p), &fl);
+    double s = 0.0;
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) s += lv[nv] * v[nv].d[0];
+    A.b.lU[kk][c] = s + (add_ux ? A.b.lUx[kk][c] : 0.0);
+  }
+}
+
+// lVin[dom] += J_P(V^n)^T lU0.
+__global__ void k_adj_p2c(AdjArgs A) {
+  ADJ_CELL_PROLOGUE
+  if (!in_dom(g, i, j, k)) return;
+  double lu[NV], v0[NV];
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    lu[nv] = A.b.lU0[nv][c];
+    v0[nv] = A.b.Vn[nv][c];
+  }
+  for (int kk = 0; kk < NV; kk++) {
+    D1 v[NV], u[NV];
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) v[nv] = D1(v0[nv]);
+    v[kk].d[0] = 1.0;
+    prim_to_cons(v, u, D1(A.f.gamma - 1.0));
+    double s = 0.0;
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) s += lu[nv] * u[nv].d[0];
+    A.b.lVin[kk][c] += s;
+  }
+}
+
+// Face average U[BX] = (B[f] + B[f-s]) / 2 on the domain, transposed.
+__global__ void k_adj_avg(AdjArgs A, Tab8 lBdst) {
+  ADJ_CELL_PROLOGUE
+  for (int d = 0; d < g.dims; d++) {
+    int o[3] = {0, 0, 0};
+    o[d] = 1;
+    double s = 0.0;
+    if (in_dom(g, i, j, k)) s += 0.5 * A.b.lU[BX1 + d][c];
+    if (in_dom(g, i + o[0], j + o[1], k + o[2])) s += 0.5 * A.b.lU[BX1 + d][c + g.s[d]];
+    if (s != 0.0) lBdst.p[d][c] += s;
+  }
+}
+// The averaged components replaced the conserved ones: clear their adjoint.
+__global__ void k_adj_zero_bx(AdjArgs A) {
+  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= A.f.g.ncell) return;
+  for (int d = 0; d < A.f.g.dims; d++) A.b.lU[BX1 + d][c] = 0.0;
+}
+
+// Stage-2 RK2 combination transposed, cell part:
+// U2 = w0 U0 + wc U  =>  lU0 = w0 lU, lU <- wc lU, lUx = lU (adjoint on U1).
+__global__ void k_adj_rk_cells(AdjArgs A, double w0, double wc) {
+  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= A.f.g.ncell) return;
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    const double l = A.b.lU[nv][c];
+    A.b.lU0[nv][c] = w0 * l;
+    A.b.lU[nv][c] = wc * l;
+    A.b.lUx[nv][c] = wc * l;
+  }
+}
+// Face part on the CT faces: B2 = w0 B0 + wc (B + dt curl E)
+// => lB0 = w0 lB, lB <- wc lB (the curl part is then taken from the scaled lB).
+__global__ void k_adj_rk_faces(AdjArgs A, double w0, double wc) {
+  ADJ_CELL_PROLOGUE
+  for (int d = 0; d < g.dims; d++) {
+    const double l = A.b.lB[d][c];
+    const bool on = ct_face(g, d, i, j, k);
+    A.b.lB0[d][c] = on ? w0 * l : 0.0;
+    A.b.lB[d][c] = on ? wc * l : l;
+  }
+}
+// Stage-1: U before the sweeps equals U0 (both PrimToCons(V^n)).
+__global__ void k_adj_add_u0(AdjArgs A) {
+  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= A.f.g.ncell) return;
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) A.b.lU0[nv][c] += A.b.lU[nv][c];
+}
+__global__ void k_add(double* y, const double* x, long long n) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q < n) y[q] += x[q];
+}
+
+// CT_Update transposed: lBin += lB on the CT faces (identity part) and
+// lE = curl^T lB.
+__global__ void k_adj_ct(AdjArgs A, Tab8 lBc) {
+  ADJ_CELL_PROLOGUE
+  auto lb = [&](int fd, int ii, int jj, int kk) -> double {
+    if (ii >= g.nt[0] || jj >= g.nt[1] || kk >= g.nt[2]) return 0.0;
+    if (!ct_face(g, fd, ii, jj, kk)) return 0.0;
+    return lBc.p[fd][cidx(g, kk, jj, ii)];
+  };
+  for (int fd = 0; fd < g.dims; fd++)
+    if (ct_face(g, fd, i, j, k)) A.b.lBin[fd][c] += lBc.p[fd][c];
+  const double dt = A.dt;
+  const double c1 = dt / g.dx[0], c2 = dt / g.dx[1], c3 = g.dims == 3 ? dt / g.dx[2] : 0.0;
+  // Bx[f] += -c2 (Ez[f] - Ez[f-sy]) + c3 (Ey[f] - Ey[f-sz])
+  // By[f] +=  c1 (Ez[f] - Ez[f-sx]) - c3 (Ex[f] - Ex[f-sz])
+  // Bz[f] += -c1 (Ey[f] - Ey[f-sx]) + c2 (Ex[f] - Ex[f-sy])
+  A.b.lE[2][c] = -c2 * (lb(0, i, j, k) - lb(0, i, j + 1, k)) + c1 * (lb(1, i, j, k) - lb(1, i + 1, j, k));
+  if (g.dims == 3) {
+    A.b.lE[1][c] = c3 * (lb(0, i, j, k) - lb(0, i, j, k + 1)) - c1 * (lb(2, i, j, k) - lb(2, i + 1, j, k));
+    A.b.lE[0][c] = -c3 * (lb(1, i, j, k) - lb(1, i, j, k + 1)) + c2 * (lb(2, i, j, k) - lb(2, i, j + 1, k));
+  }
+}
+
+// One edge EMF component transposed: gathers its 40 inputs, forms the
+// gradient by 40 seeded evaluations and scatters it.
+template <int E>
+__device__ __forceinline__ void adj_edge(const AdjArgs& A, long long c, double lam) {
+  if (lam == 0.0) return;
+  constexpr int AX = E == 2 ? 0 : (E == 0 ? 1 : 2);
+  constexpr int AY = E == 2 ? 1 : (E == 0 ? 2 : 0);
+  const Geom& g = A.f.g;
+  const F64A<double>& f = A.f;
+  const AdjBufs& b = A.b;
+  const long long sx = g.s[AX], sy = g.s[AY];
+  const long long c00 = c, cx0 = c + sx, c0y = c + sy, cxy = c + sx + sy;
+  const long long cells[4] = {c00, cx0, c0y, cxy};
+  double in[kEdgeIn];
+  double* dst[kEdgeIn];
+  in[0] = f.SR[AX][c00]; dst[0] = &b.lS[AX][1][c00];
+  in[1] = f.SR[AX][c0y]; dst[1] = &b.lS[AX][1][c0y];
+  in[2] = f.SL[AX][c00]; dst[2] = &b.lS[AX][0][c00];
+  in[3] = f.SL[AX][c0y]; dst[3] = &b.lS[AX][0][c0y];
+  in[4] = f.SR[AY][c00]; dst[4] = &b.lS[AY][1][c00];
+  in[5] = f.SR[AY][cx0]; dst[5] = &b.lS[AY][1][cx0];
+  in[6] = f.SL[AY][c00]; dst[6] = &b.lS[AY][0][c00];
+  in[7] = f.SL[AY][cx0]; dst[7] = &b.lS[AY][0][cx0];
+  const long long bxi[4] = {c00 - sy, c00, c0y, c0y + sy};
+  const long long byi[4] = {c00 - sx, c00, cx0, cx0 + sx};
+  for (int t = 0; t < 4; t++) {
+    in[8 + t] = f.Bs[AX][bxi[t]];
+    dst[8 + t] = &b.lBin[AX][bxi[t]];
+    in[12 + t] = f.Bs[AY][byi[t]];
+    dst[12 + t] = &b.lBin[AY][byi[t]];
+  }
+  for (int q = 0; q < 4; q++) {
+    const long long cc = cells[q];
+    double** d6 = dst + 16 + 6 * q;
+    double* i6 = in + 16 + 6 * q;
+    i6[0] = f.V[VX1 + AY][cc]; d6[0] = &b.lVin[VX1 + AY][cc];
+    i6[1] = f.V[VX1 + AX][cc]; d6[1] = &b.lVin[VX1 + AX][cc];
+    i6[2] = f.DV[AX][AY][cc];  d6[2] = &b.lDV[AX][AY][cc];
+    i6[3] = f.DV[AY][AY][cc];  d6[3] = &b.lDV[AY][AY][cc];
+    i6[4] = f.DV[AX][AX][cc];  d6[4] = &b.lDV[AX][AX][cc];
+    i6[5] = f.DV[AY][AX][cc];  d6[5] = &b.lDV[AY][AX][cc];
+  }
+  for (int kk = 0; kk < kEdgeIn; kk++) {
+    D1 x[kEdgeIn];
+#pragma unroll
+    for (int q = 0; q < kEdgeIn; q++) x[q] = D1(in[q]);
+    x[kk].d[0] = 1.0;
+    const double gk = lam * emf_pt(x).d[0];
+    if (gk != 0.0) atomicAdd(dst[kk], gk);
+  }
+}
+
+__global__ void k_adj_emf(AdjArgs A, Box box) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= box.count()) return;
+  int i, j, k;
+  box.coords(q, i, j, k);
+  const long long c = cidx(A.f.g, k, j, i);
+  adj_edge<2>(A, c, A.b.lE[2][c]);
+  if (A.f.g.dims == 3) {
+    adj_edge<0>(A, c, A.b.lE[0][c]);
+    adj_edge<1>(A, c, A.b.lE[1][c]);
+  }
+}
+
+// U[c] += -dt/dx (F[c] - F[c-s]) (and the pressure term on the normal
+// momentum) transposed: adjoint on the interface fluxes at c+1/2.
+template <int DIR>
+__global__ void k_adj_flux(AdjArgs A, Box box) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= box.count()) return;
+  int i, j, k;
+  box.coords(q, i, j, k);
+  const Geom& g = A.f.g;
+  const long long c = cidx(g, k, j, i), s = g.s[DIR];
+  const double scrh = A.dt / g.dx[DIR];
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) A.b.lF[nv][c] = -scrh * (A.b.lU[nv][c] - A.b.lU[nv][c + s]);
+  A.b.lP[c] = -scrh * (A.b.lU[Rot<DIR>::vn][c] - A.b.lU[Rot<DIR>::vn][c + s]);
+}
+
+// Riemann problem at interface c+1/2 transposed: adjoint on VP[c], VM[c+s]
+// (and on the face field that replaces their normal component under CT).
+template <int DIR>
+__global__ void k_adj_riemann(AdjArgs A, Box box, int solver) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= box.count()) return;
+  int i, j, k;
+  box.coords(q, i, j, k);
+  const Geom& g = A.f.g;
+  const long long c = cidx(g, k, j, i), s = g.s[DIR];
+  const bool ct = A.f.ct;
+  constexpr int NO = NV + 3;
+  double lam[NO];
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) lam[nv] = A.b.lF[nv][c];
+  lam[NV] = A.b.lP[c];
+  lam[NV + 1] = ct ? A.b.lS[DIR][0][c] : 0.0;
+  lam[NV + 2] = ct ? A.b.lS[DIR][1][c] : 0.0;
+  bool any = false;
+#pragma unroll
+  for (int o = 0; o < NO; o++) any |= lam[o] != 0.0;
+  constexpr int BN = Rot<DIR>::bn;
+  double vL[NV], vR[NV];
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    vL[nv] = A.f.VP[nv][c];
+    vR[nv] = A.f.VM[nv][c + s];
+  }
+  if (ct) {
+    const double bn = A.f.Bs[DIR][c];
+    vL[BN] = bn;
+    vR[BN] = bn;
+  }
+  double gL[NV], gR[NV];
+  for (int kk = 0; kk < 2 * NV; kk++) {
+    double gk = 0.0;
+    if (any) {
+      D1 xL[NV], xR[NV], out[NO];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        xL[nv] = D1(vL[nv]);
+        xR[nv] = D1(vR[nv]);
+      }
+      if (kk < NV) xL[kk].d[0] = 1.0;
+      else xR[kk - NV].d[0] = 1.0;
+      riemann_pt<D1, DIR>(solver, A.f.gamma, xL, xR, out);
+#pragma unroll
+      for (int o = 0; o < NO; o++) gk += lam[o] * out[o].d[0];
+    }
+    if (kk < NV) gL[kk] = gk;
+    else gR[kk - NV] = gk;
+  }
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    A.b.lVP[nv][c] = (ct && nv == BN) ? 0.0 : gL[nv];
+    A.b.lVM[nv][c + s] = (ct && nv == BN) ? 0.0 : gR[nv];
+  }
+  if (ct) A.b.lBin[DIR][c] += gL[BN] + gR[BN];
+}
+
+// States of zone c (and its velocity slopes DV = vp - vm) transposed:
+// scatter into the adjoint on the stage-input primitives of its stencil.
+template <int DIR>
+__global__ void k_adj_recon(AdjArgs A, Box box) {
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= box.count()) return;
+  int i, j, k;
+  box.coords(q, i, j, k);
+  const Geom& g = A.f.g;
+  const long long c = cidx(g, k, j, i), s = g.s[DIR];
+  const int recon = A.f.recon;
+  const int t0 = recon == PG_LINEAR ? 1 : 0, t1 = recon == PG_LINEAR ? 3 : 4;
+  for (int nv = 0; nv < NV; nv++) {
+    double lp = A.b.lVP[nv][c], lm = A.b.lVM[nv][c];
+    if (A.f.ct && nv >= VX1 && nv < VX1 + g.dims) {
+      const double ld = A.b.lDV[DIR][nv - VX1][c];
+      lp += ld;
+      lm -= ld;
+    }
+    if (lp == 0.0 && lm == 0.0) continue;
+    double w[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
+    for (int t = t0; t <= t1; t++) w[t] = A.f.V[nv][c + (t - 2) * s];
+    for (int t = t0; t <= t1; t++) {
+      D1 x[5], vp, vm;
+      for (int u = 0; u < 5; u++) x[u] = D1(w[u]);
+      x[t].d[0] = 1.0;
+      recon_pt(recon, A.f.limiter, nv, x, vp, vm);
+      const double gk = lp * vp.d[0] + lm * vm.d[0];
+      if (gk != 0.0) atomicAdd(&A.b.lVin[nv][c + (t - 2) * s], gk);
+    }
+  }
+}
+
+// Boundary transposed: the adjoint on every ghost zone goes to the zone it
+// was copied from (the single-pass map of k_bound), and the ghost is cleared.
+struct BoundTab {
+  double* p[12];
+};
+__global__ void k_adj_bound(Geom g, BoundTab t, int narr, int bcx, int bcy, int bcz) {
+  long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (c >= g.ncell) return;
+  int i, j, k;
+  cell_ijk(g, c, i, j, k);
+  if (in_dom(g, i, j, k)) return;
+  const int si = bmap(i, g.beg[0], g.end[0], g.nx[0], bcx);
+  const int sj = g.dims > 1 ? bmap(j, g.beg[1], g.end[1], g.nx[1], bcy) : j;
+  const int sk = g.dims > 2 ? bmap(k, g.beg[2], g.end[2], g.nx[2], bcz) : k;
+  const long long src = cidx(g, sk, sj, si);
+  for (int a = 0; a < narr; a++) {
+    const double v = t.p[a][c];
+    if (v != 0.0) {
+      atomicAdd(&t.p[a][src], v);
+      t.p[a][c] = 0.0;
+    }
+  }
+}
+
+// Adjoint input: the cell adjoint on ghosts and the face adjoint off the
+// faces the step writes are cleared (those values are refilled, not evolved).
+__global__ void k_adj_clean(AdjArgs A, int ct) {
+  ADJ_CELL_PROLOGUE
+  if (!in_dom(g, i, j, k))
+    for (int nv = 0; nv < NV; nv++) A.b.lV[nv][c] = 0.0;
+  if (ct)
+    for (int d = 0; d < g.dims; d++)
+      if (!ct_face(g, d, i, j, k)) A.b.lB[d][c] = 0.0;
+}
+
+// ---------------------------------------------------------------------------
+// host side
+// ---------------------------------------------------------------------------
+struct Checkpoints {
+  std::vector<std::vector<void*>> slots;  // per slot: 8 cell arrays + the face arrays
+};
+
+static int adjoint_alloc(Solver* S, AdjBufs** out) {
+  if (S->adj) {
+    *out = (AdjBufs*)S->adj;
+    return PG_OK;
+  }
+  AdjBufs* B = new AdjBufs();
+  memset(B, 0, sizeof *B);
+  S->adj = B;
+  *out = B;
+  const size_t bytes = sizeof(double) * S->g.ncell;
+  double** p = (double**)B;
+  for (size_t q = 0; q < sizeof(AdjBufs) / sizeof(double*); q++) {
+    if (cudaMalloc(&p[q], bytes) != cudaSuccess) {
+      p[q] = nullptr;
+      return PG_ERR_NOMEM;
+    }
+    if (cudaMemset(p[q], 0, bytes) != cudaSuccess) return PG_ERR_CUDA;
+  }
+  return PG_OK;
+}
+
+void adjoint_free(Solver* S) {
+  if (S->adj) {
+    AdjBufs* B = (AdjBufs*)S->adj;
+    double** p = (double**)B;
+    for (size_t q = 0; q < sizeof(AdjBufs) / sizeof(double*); q++)
+      if (p[q]) cudaFree(p[q]);
+    delete B;
+    S->adj = nullptr;
+  }
+  if (S->ckpt) {
+    Checkpoints* C = (Checkpoints*)S->ckpt;
+    for (auto& sl : C->slots)
+      for (void* q : sl)
+        if (q) cudaFree(q);
+    delete C;
+    S->ckpt = nullptr;
+  }
+  if (S->stage) {
+    cudaFree(S->stage);
+    S->stage = nullptr;
+  }
+}
+
+}  // namespace pg
+
+using namespace pg;
+
+namespace {
+
+constexpr int kT = kThreads;
+
+void dcopy(double* dst, const double* src, long long n, cudaStream_t st) {
+  cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+}
+
+Box dir_box(const Geom& g, int dir, int lo_off, int hi_off, bool ct) {
+  Box b;
+  for (int ax = 0; ax < 3; ax++) {
+    if (ax >= g.dims) {
+      b.lo[ax] = b.hi[ax] = 0;
+    } else if (ax == dir) {
+      b.lo[ax] = g.beg[ax] + lo_off;
+      b.hi[ax] = g.end[ax] + hi_off;
+    } else {
+      const int e = ct ? 1 : 0;
+      b.lo[ax] = g.beg[ax] - e;
+      b.hi[ax] = g.end[ax] + e;
+    }
+  }
+  return b;
+}
+
+// Recompute the states and Riemann outputs along DIR from the solver's V/Bs.
+template <int DIR>
+void fwd_dir(Solver* S, const F64A<double>& f) {
+  const Geom& g = S->g;
+  cudaStream_t st = S->stream;
+  Box rb = dir_box(g, DIR, -1, 1, f.ct), ib = dir_box(g, DIR, -1, 0, f.ct);
+  k_recon<double, DIR><<<grid_for(rb.count()), kT, 0, st>>>(f, rb);
+  if (S->cfg.riemann == PG_HLL)
+    k_riemann<double, DIR, PG_HLL, false><<<grid_for(ib.count(), 128), 128, 0, st>>>(f, ib, 0);
+  else
+    k_riemann<double, DIR, PG_HLLD, false><<<grid_for(ib.count(), 128), 128, 0, st>>>(f, ib, 0);
+}
+
+template <int DIR>
+void rev_dir(Solver* S, const AdjArgs& A) {
+  const Geom& g = S->g;
+  cudaStream_t st = S->stream;
+  const long long n = g.ncell;
+  Box rb = dir_box(g, DIR, -1, 1, A.f.ct), ib = dir_box(g, DIR, -1, 0, A.f.ct);
+  fwd_dir<DIR>(S, A.f);  // states of this direction
+  for (int nv = 0; nv < NV; nv++) {
+    cudaMemsetAsync(A.b.lVP[nv], 0, n * sizeof(double), st);
+    cudaMemsetAsync(A.b.lVM[nv], 0, n * sizeof(double), st);
+  }
+  k_adj_flux<DIR><<<grid_for(ib.count()), kT, 0, st>>>(A, ib);
+  k_adj_riemann<DIR><<<grid_for(ib.count(), 64), 64, 0, st>>>(A, ib, S->cfg.riemann);
+  k_adj_recon<DIR><<<grid_for(rb.count(), 128), 128, 0, st>>>(A, rb);
+}
+
+void fwd_bound(Solver* S, const F64A<double>& f) {
+  const Geom& g = S->g;
+  const long long n0 = g.dims > 0 ? 2LL * g.beg[0] * g.nt[1] * g.nt[2] : 0;
+  const long long n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
+  const long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
+  k_bound<double><<<grid_for(n0 + n1 + n2), kT, 0, S->stream>>>(f, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0,
+                                                                n1, n2);
+}
+
+Tab8 tab(double* const* p, int n) {
+  Tab8 t;
+  for (int q = 0; q < 8; q++) t.p[q] = q < n ? p[q] : nullptr;
+  return t;
+}
+
+// One stage reversed.  On entry lU holds the adjoint on the stage's
+// conserved result (after the face-average part was undone) and lB the
+// adjoint on the faces after CT_Update; the solver's V/Bs hold the stage
+// input.  On exit lVin/lBin hold the adjoint on the stage input before its
+// boundary fill.  add_b0: stage 1 of RK2, where Bs0 copies Bs after the fill.
+void rev_stage(Solver* S, const AdjArgs& A, bool add_b0) {
+  const Geom& g = S->g;
+  cudaStream_t st = S->stream;
+  const long long n = g.ncell;
+  const bool ct = A.f.ct;
+  const AdjBufs& b = A.b;
+  for (int nv = 0; nv < NV; nv++) cudaMemsetAsync(b.lVin[nv], 0, n * sizeof(double), st);
+  for (int d = 0; d < 3; d++) {
+    cudaMemsetAsync(b.lBin[d], 0, n * sizeof(double), st);
+    if (ct) {
+      cudaMemsetAsync(b.lS[d][0], 0, n * sizeof(double), st);
+      cudaMemsetAsync(b.lS[d][1], 0, n * sizeof(double), st);
+      cudaMemsetAsync(b.lE[d], 0, n * sizeof(double), st);
+      for (int q = 0; q < 3; q++) cudaMemsetAsync(b.lDV[d][q], 0, n * sizeof(double), st);
+    }
+  }
+  fwd_bound(S, A.f);
+  if (ct) {
+    // wave speeds and velocity slopes of every direction, inputs of the EMF
+    fwd_dir<0>(S, A.f);
+    if (g.dims > 1) fwd_dir<1>(S, A.f);
+    if (g.dims > 2) fwd_dir<2>(S, A.f);
+    k_adj_ct<<<grid_for(n), kT, 0, st>>>(A, tab(b.lB, 3));
+    Box eb;
+    for (int ax = 0; ax < 3; ax++) {
+      if (ax < g.dims) {
+        eb.lo[ax] = g.beg[ax] - 1;
+        eb.hi[ax] = g.end[ax];
+      } else {
+        eb.lo[ax] = eb.hi[ax] = 0;
+      }
+    }
+    k_adj_emf<<<grid_for(eb.count(), 64), 64, 0, st>>>(A, eb);
+  }
+  if (g.dims > 2) rev_dir<2>(S, A);
+  if (g.dims > 1) rev_dir<1>(S, A);
+  rev_dir<0>(S, A);
+  if (add_b0)
+    for (int d = 0; d < g.dims; d++) k_add<<<grid_for(n), kT, 0, st>>>(b.lBin[d], b.lB0[d], n);
+  BoundTab t;
+  int na = 0;
+  for (int nv = 0; nv < NV; nv++) t.p[na++] = b.lVin[nv];
+  if (ct)
+    for (int d = 0; d < g.dims; d++) t.p[na++] = b.lBin[d];
+  k_adj_bound<<<grid_for(n), kT, 0, st>>>(g, t, na, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2]);
+}
+
+int check_fp64(pg_solver* h, const char* who, bool tangent_ok) {
+  if (!h) {
+    set_last_error("null solver");
+    return PG_ERR_INVALID;
+  }
+  const int p = h->S.cfg.precision;
+  if (p == PG_FP64 || (tangent_ok && p == PG_FP64_TANGENT)) return PG_OK;
+  std::string m = std::string(who) + ": needs a PG_FP64" + (tangent_ok ? " or PG_FP64_TANGENT" : "") + " solver";
+  set_last_error(m.c_str());
+  return PG_ERR_INVALID;
+}
+
+int sync_status(Solver* S) {
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess) e = cudaStreamSynchronize(S->stream);
+  if (e != cudaSuccess) {
+    set_last_error(cudaGetErrorString(e));
+    return PG_ERR_CUDA;
+  }
+  return PG_OK;
+}
+
+}  // namespace
+
+extern "C" int pg_tangent_upload(pg_solver* h, const double* const vars[8], const double* const faces[3],
+                                 int layout) {
+  if (!h || !vars) {
+    set_last_error("null argument");
+    return PG_ERR_INVALID;
+  }
+  if (h->S.cfg.precision != PG_FP64_TANGENT) {
+    set_last_error("pg_tangent_upload: needs a PG_FP64_TANGENT solver");
+    return PG_ERR_INVALID;
+  }
+  return tl_xfer(&h->S, (double* const*)vars, (double* const*)faces, layout, true, 1);
+}
+
+extern "C" int pg_tangent_download(pg_solver* h, double* const vars[8], double* const faces[3], int layout) {
+  if (!h || !vars) {
+    set_last_error("null argument");
+    return PG_ERR_INVALID;
+  }
+  if (h->S.cfg.precision != PG_FP64_TANGENT) {
+    set_last_error("pg_tangent_download: needs a PG_FP64_TANGENT solver");
+    return PG_ERR_INVALID;
+  }
+  return tl_xfer(&h->S, vars, faces, layout, false, 1);
+}
+
+extern "C" int pg_adjoint_set(pg_solver* h, const double* const vars[8], const double* const faces[3], int layout) {
+  int rc = check_fp64(h, "pg_adjoint_set", false);
+  if (rc) return rc;
+  Solver* S = &h->S;
+  if (!vars) {
+    set_last_error("pg_adjoint_set: null vars");
+    return PG_ERR_INVALID;
+  }
+  if (layout != PG_LAYOUT_INTERIOR && layout != PG_LAYOUT_PLUTO) {
+    set_last_error("bad layout");
+    return PG_ERR_INVALID;
+  }
+  if (S->cfg.time_stepping != PG_RK2) {
+    set_last_error("pg_adjoint_set: the adjoint covers RK2 time stepping");
+    return PG_ERR_INVALID;
+  }
+  AdjBufs* B = nullptr;
+  if ((rc = adjoint_alloc(S, &B))) {
+    adjoint_free(S);
+    set_last_error("pg_adjoint_set: allocation failed");
+    return rc;
+  }
+  const long long n = S->g.ncell;
+  cudaStream_t st = S->stream;
+  const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
+  for (int nv = 0; nv < NV; nv++) {
+    cudaMemsetAsync(B->lV[nv], 0, n * sizeof(double), st);
+    if (vars[nv] && (rc = xfer_f64(S, B->lV[nv], (double*)vars[nv], -1, layout, true))) return rc;
+  }
+  for (int d = 0; d < 3; d++) cudaMemsetAsync(B->lB[d], 0, n * sizeof(double), st);
+  if (ct && faces)
+    for (int d = 0; d < S->g.dims; d++)
+      if (faces[d] && (rc = xfer_f64(S, B->lB[d], (double*)faces[d], d, layout, true))) return rc;
+  AdjArgs A;
+  memset(&A, 0, sizeof A);
+  A.f = make_args<double>(S);
+  A.b = *B;
+  k_adj_clean<<<grid_for(n), kT, 0, st>>>(A, ct);
+  return sync_status(S);
+}
+
+extern "C" int pg_adjoint_get(pg_solver* h, double* const vars[8], double* const faces[3], int layout) {
+  int rc = check_fp64(h, "pg_adjoint_get", false);
+  if (rc) return rc;
+  Solver* S = &h->S;
+  if (!S->adj || !vars) {
+    set_last_error("pg_adjoint_get: no adjoint set, or null vars");
+    return PG_ERR_INVALID;
+  }
+  if (layout != PG_LAYOUT_INTERIOR && layout != PG_LAYOUT_PLUTO) {
+    set_last_error("bad layout");
+    return PG_ERR_INVALID;
+  }
+  AdjBufs* B = (AdjBufs*)S->adj;
+  for (int nv = 0; nv < NV; nv++)
+    if (vars[nv] && (rc = xfer_f64(S, B->lV[nv], vars[nv], -1, layout, false))) return rc;
+  if (S->cfg.divb == PG_CONSTRAINED_TRANSPORT && faces)
+    for (int d = 0; d < S->g.dims; d++)
+      if (faces[d] && (rc = xfer_f64(S, B->lB[d], faces[d], d, layout, false))) return rc;
+  return sync_status(S);
+}
+
+extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
+  int rc = check_fp64(h, "pg_adjoint_step", false);
+  if (rc) return rc;
+  Solver* S = &h->S;
+  if (!S->adj) {
+    set_last_error("pg_adjoint_step: call pg_adjoint_set first");
+    return PG_ERR_INVALID;
+  }
+  if (!(dt > 0)) {
+    set_last_error("pg_adjoint_step: dt must be positive");
+    return PG_ERR_INVALID;
+  }
+  AdjBufs* B = (AdjBufs*)S->adj;
+  const Geom& g = S->g;
+  const long long n = g.ncell;
+  const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
+  const int nb = ct ? g.dims : 0;
+  cudaStream_t st = S->stream;
+  if (S->device_dt) {
+    S->device_dt = false;
+    S->graph_dirty = true;
+  }
+  // ---- forward recomputation of the step, saving what the reverse needs ----
+  S->sc_host->dt = dt;
+  cudaMemcpyAsync(&S->sc->dt, &S->sc_host->dt, sizeof(double), cudaMemcpyHostToDevice, st);
+  for (int nv = 0; nv < NV; nv++) dcopy(B->Vn[nv], S->V[nv], n, st);
+  for (int d = 0; d < nb; d++) dcopy(B->Bn[d], S->Bs[d], n, st);
+  Box dom;
+  for (int ax = 0; ax < 3; ax++) {
+    dom.lo[ax] = g.beg[ax];
+    dom.hi[ax] = g.end[ax];
+  }
+  const F64A<double> f = make_args<double>(S);
+  launch_bound<double>(S, f);
+  k_begin_step<double><<<grid_for(n), kT, 0, st>>>(f, dom);
+  launch_sweep<double, 0>(S, f, 1);
+  if (g.dims > 1) launch_sweep<double, 1>(S, f, 1);
+  if (g.dims > 2) launch_sweep<double, 2>(S, f, 1);
+  launch_stage_tail<double, 1, 2>(S, f, dom);
+  for (int nv = 0; nv < NV; nv++) {
+    dcopy(B->V1[nv], S->V[nv], n, st);
+    dcopy(B->U1[nv], S->U[nv], n, st);
+  }
+  for (int d = 0; d < nb; d++) dcopy(B->B1[d], S->Bs[d], n, st);
+  launch_bound<double>(S, f);
+  launch_sweep<double, 0>(S, f, 2);
+  if (g.dims > 1) launch_sweep<double, 1>(S, f, 2);
+  if (g.dims > 2) launch_sweep<double, 2>(S, f, 2);
+  launch_stage_tail<double, 2, 2>(S, f, dom);
+  for (int nv = 0; nv < NV; nv++) dcopy(B->U2[nv], S->U[nv], n, st);
+
+  AdjArgs A;
+  memset(&A, 0, sizeof A);
+  A.f = f;
+  A.dt = dt;
+  const double w0 = 0.5, wc = 0.5;  // RK2 weights
+  // ---- stage 2 reversed ----
+  A.b = *B;
+  k_adj_c2p<<<grid_for(n), kT, 0, st>>>(A, tab(B->U2, 8), tab(B->lV, 8), 0);
+  if (ct) {
+    k_adj_avg<<<grid_for(n), kT, 0, st>>>(A, tab(B->lB, 3));
+    k_adj_zero_bx<<<grid_for(n), kT, 0, st>>>(A);
+    k_adj_rk_faces<<<grid_for(n), kT, 0, st>>>(A, w0, wc);
+  }
+  k_adj_rk_cells<<<grid_for(n), kT, 0, st>>>(A, w0, wc);
+  for (int nv = 0; nv < NV; nv++) dcopy(S->V[nv], B->V1[nv], n, st);
+  for (int d = 0; d < nb; d++) dcopy(S->Bs[d], B->B1[d], n, st);
+  rev_stage(S, A, false);
+  // lVin / lBin hold the adjoint on V1 / B1: they become lV / lB
+  for (int nv = 0; nv < NV; nv++) std::swap(B->lV[nv], B->lVin[nv]);
+  for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
+  // ---- stage 1 reversed ----
+  A.b = *B;
+  k_adj_c2p<<<grid_for(n), kT, 0, st>>>(A, tab(B->U1, 8), tab(B->lV, 8), 1);
+  if (ct) {
+    k_adj_avg<<<grid_for(n), kT, 0, st>>>(A, tab(B->lB, 3));
+    k_adj_zero_bx<<<grid_for(n), kT, 0, st>>>(A);
+  }
+  k_adj_add_u0<<<grid_for(n), kT, 0, st>>>(A);
+  for (int nv = 0; nv < NV; nv++) dcopy(S->V[nv], B->Vn[nv], n, st);
+  for (int d = 0; d < nb; d++) dcopy(S->Bs[d], B->Bn[d], n, st);
+  rev_stage(S, A, ct);
+  k_adj_p2c<<<grid_for(n), kT, 0, st>>>(A);
+  for (int nv = 0; nv < NV; nv++) std::swap(B->lV[nv], B->lVin[nv]);
+  for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
+  // the solver's state is the step's start again
+  for (int nv = 0; nv < NV; nv++) dcopy(S->V[nv], B->Vn[nv], n, st);
+  for (int d = 0; d < nb; d++) dcopy(S->Bs[d], B->Bn[d], n, st);
+  return sync_status(S);
+}
+
+static int ckpt_xfer(pg_solver* h, int slot, bool save) {
+  int rc = check_fp64(h, save ? "pg_checkpoint_save" : "pg_checkpoint_load", true);
+  if (rc) return rc;
+  Solver* S = &h->S;
+  if (slot < 0 || slot >= PG_MAX_CHECKPOINTS) {
+    set_last_error("checkpoint slot out of range");
+    return PG_ERR_INVALID;
+  }
+  if (!S->ckpt) S->ckpt = new Checkpoints();
+  Checkpoints* C = (Checkpoints*)S->ckpt;
+  if ((int)C->slots.size() <= slot) C->slots.resize(slot + 1);
+  std::vector<void*>& sl = C->slots[slot];
+  const size_t bytes = S->elem_bytes * S->g.ncell;
+  const int nb = S->cfg.divb == PG_CONSTRAINED_TRANSPORT ? S->g.dims : 0;
+  if (sl.empty()) {
+    if (!save) {
+      set_last_error("pg_checkpoint_load: empty slot");
+      return PG_ERR_INVALID;
+    }
+    sl.assign(NV + nb, nullptr);
+    for (auto& q : sl)
+      if (cudaMalloc(&q, bytes) != cudaSuccess) {
+        for (auto& r : sl)
+          if (r) cudaFree(r);
+        sl.clear();
+        set_last_error("checkpoint allocation failed");
+        return PG_ERR_NOMEM;
+      }
+  }
+  for (int a = 0; a < NV + nb; a++) {
+    void* arr = a < NV ? (void*)S->V[a] : (void*)S->Bs[a - NV];
+    if (save) cudaMemcpyAsync(sl[a], arr, bytes, cudaMemcpyDeviceToDevice, S->stream);
+    else cudaMemcpyAsync(arr, sl[a], bytes, cudaMemcpyDeviceToDevice, S->stream);
+  }
+  return sync_status(S);
+}
+
+extern "C" int pg_checkpoint_save(pg_solver* h, int slot) { return ckpt_xfer(h, slot, true); }
+extern "C" int pg_checkpoint_load(pg_solver* h, int slot) { return ckpt_xfer(h, slot, false); }

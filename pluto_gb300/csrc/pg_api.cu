@@ -8,10 +8,6 @@
 
 using namespace pg;
 
-struct pg_solver {
-  Solver S;
-};
-
 static thread_local std::string g_last_error = "";
 
 static int fail(int code, const char* msg) {
@@ -59,7 +55,8 @@ int validate_config(const pg_config* c) {
   } else if (c->divb != PG_DIVB_NONE) {
     return fail(PG_ERR_INVALID, "unsupported divergence control");
   }
-  if (c->precision != PG_FP64 && c->precision != PG_MIXED && c->precision != PG_MIXED_DW)
+  if (c->precision != PG_FP64 && c->precision != PG_MIXED && c->precision != PG_MIXED_DW &&
+      c->precision != PG_FP64_TANGENT)
     return fail(PG_ERR_INVALID, "unsupported precision");
   return PG_OK;
 }
@@ -90,6 +87,7 @@ void set_last_error(const char* msg) { g_last_error = msg; }
 static void free_all(Solver* S) {
   if (S->graph) cudaGraphExecDestroy(S->graph);
   S->graph = nullptr;
+  adjoint_free(S);
   fp64_free(S);
   mixed_free(S);
   if (S->sc) cudaFree(S->sc);
@@ -122,7 +120,9 @@ extern "C" int pg_create(const pg_config* cfg, pg_solver** out) {
   }
   cudaMemset(S->sc, 0, sizeof(DevScalars));
   memset(S->sc_host, 0, sizeof(DevScalars));
-  rc = cfg->precision == PG_FP64 ? fp64_alloc(S) : mixed_alloc(S);
+  const bool f64 = cfg->precision == PG_FP64 || cfg->precision == PG_FP64_TANGENT;
+  if (cfg->precision == PG_FP64_TANGENT) S->elem_bytes = 2 * sizeof(double);  // value + tangent
+  rc = f64 ? fp64_alloc(S) : mixed_alloc(S);
   if (rc) {
     free_all(S);
     delete h;
@@ -211,6 +211,7 @@ extern "C" int pg_upload(pg_solver* h, const double* const vars[8], const double
   Solver* S = &h->S;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
   if (ct && !faces) return fail(PG_ERR_INVALID, "constrained transport needs staggered fields");
+  if (S->cfg.precision == PG_FP64_TANGENT) return tl_xfer(S, (double* const*)vars, (double* const*)faces, layout, true, 0);
   if (S->cfg.precision != PG_FP64) return mixed_upload_host(S, vars, faces, layout);
   for (int nv = 0; nv < 8; nv++) {
     if (vars[nv]) {
@@ -235,6 +236,7 @@ extern "C" int pg_download(pg_solver* h, double* const vars[8], double* const fa
   if (layout != PG_LAYOUT_INTERIOR && layout != PG_LAYOUT_PLUTO) return fail(PG_ERR_INVALID, "bad layout");
   Solver* S = &h->S;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
+  if (S->cfg.precision == PG_FP64_TANGENT) return tl_xfer(S, vars, faces, layout, false, 0);
   if (S->cfg.precision != PG_FP64) return mixed_download(S, vars, faces, layout);
   for (int nv = 0; nv < 8; nv++)
     if (vars[nv]) {
@@ -256,7 +258,9 @@ extern "C" int pg_download(pg_solver* h, double* const vars[8], double* const fa
 // -------------------------------------------------------------------------
 
 static int enqueue_step(Solver* S) {
-  return S->cfg.precision == PG_FP64 ? fp64_enqueue_step(S) : mixed_enqueue_step(S);
+  if (S->cfg.precision == PG_FP64) return fp64_enqueue_step(S);
+  if (S->cfg.precision == PG_FP64_TANGENT) return tl_enqueue_step(S);
+  return mixed_enqueue_step(S);
 }
 
 static int read_scalars(Solver* S) {

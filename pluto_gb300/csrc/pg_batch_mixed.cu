@@ -1,0 +1,41 @@
+// Mixed-precision instantiations of the batched 1D kernel (FP32 storage and
+// fluxes; conserved accumulation in FP64 or FP32 double-word pairs).
+#include "pg_batch.cuh"
+
+namespace pg {
+
+template <class A>
+static cudaError_t launch_mixed_a(const BatchArgs<float>& b, int rs, int solver, int nstage, int nsteps, int grid,
+                                  int threads, cudaStream_t st) {
+  const size_t smem = batch_smem_bytes<float>(threads);
+#define PG_BATCH_CASE(RS_, SOLV_, NST_)                                                               \
+  if (rs == RS_ && solver == SOLV_ && nstage == NST_) {                                               \
+    auto k = k_batch<float, A, RS_, SOLV_, NST_>;                                                     \
+    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
+    if (e != cudaSuccess) return e;                                                                   \
+    k<<<grid, threads, smem, st>>>(b, nsteps);                                                        \
+    return cudaGetLastError();                                                                        \
+  }
+  PG_BATCH_CASE(1, PG_HLLD, 2)
+  PG_BATCH_CASE(1, PG_HLLD, 3)
+  PG_BATCH_CASE(1, PG_HLL, 2)
+  PG_BATCH_CASE(1, PG_HLL, 3)
+  PG_BATCH_CASE(0, PG_HLLD, 2)
+  PG_BATCH_CASE(0, PG_HLLD, 3)
+  PG_BATCH_CASE(0, PG_HLL, 2)
+  PG_BATCH_CASE(0, PG_HLL, 3)
+  PG_BATCH_CASE(4, PG_HLLD, 2)
+  PG_BATCH_CASE(4, PG_HLLD, 3)
+  PG_BATCH_CASE(4, PG_HLL, 2)
+  PG_BATCH_CASE(4, PG_HLL, 3)
+#undef PG_BATCH_CASE
+  return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_batch_mixed(const BatchArgs<float>& b, bool use_dw, int rs, int solver, int nstage, int nsteps,
+                               int grid, int threads, cudaStream_t st) {
+  if (use_dw) return launch_mixed_a<pg::dw>(b, rs, solver, nstage, nsteps, grid, threads, st);
+  return launch_mixed_a<double>(b, rs, solver, nstage, nsteps, grid, threads, st);
+}
+
+}  // namespace pg

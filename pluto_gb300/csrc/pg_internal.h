@@ -78,6 +78,10 @@ int fp64_alloc(Solver* S);
 void fp64_free(Solver* S);
 int fp64_enqueue_step(Solver* S);  // all stages of one step on S->stream
 
+int tl_enqueue_step(Solver* S);  // PG_FP64_TANGENT: state and tangent
+int tl_xfer(Solver* S, double* const vars[8], double* const faces[3], int layout, bool to_dev, int part);
+void adjoint_free(Solver* S);      // adjoint buffers, checkpoints, staging
+
 int mixed_alloc(Solver* S);
 void mixed_free(Solver* S);
 int mixed_enqueue_step(Solver* S);
@@ -117,6 +121,10 @@ struct Solver {
   cudaGraphExec_t graph = nullptr;
   bool graph_dirty = true;
   Prof* prof = nullptr;
+  size_t elem_bytes = sizeof(double);  // FP64-path array element size (16 with tangents)
+  void* adj = nullptr;     // adjoint buffers (pg_adjoint.cu)
+  void* ckpt = nullptr;    // checkpoint slots
+  double* stage = nullptr; // FP64 staging array for tangent-solver transfers
   double cfl = 0.4, cfl_max_var = 1.1;
   bool device_dt = false;  // kernels end each step by computing the next dt
   int steps_done = 0;
@@ -129,3 +137,8 @@ inline unsigned grid_for(long long n, int threads = kThreads) {
 }
 
 }  // namespace pg
+
+// The opaque handle of the C ABI.
+struct pg_solver {
+  pg::Solver S;
+};

@@ -25,7 +25,8 @@ LIMITER = {"FLAT_LIM": L.PG_FLAT_LIM, "MINMOD_LIM": L.PG_MINMOD_LIM,
 RIEMANN = {"hll": L.PG_HLL, "hlld": L.PG_HLLD, "roe": L.PG_ROE}
 STEPPING = {"RK2": L.PG_RK2, "RK3": L.PG_RK3}
 BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW}
-PRECISION = {"fp64": L.PG_FP64, "mixed": L.PG_MIXED, "mixed_dw": L.PG_MIXED_DW}
+PRECISION = {"fp64": L.PG_FP64, "mixed": L.PG_MIXED, "mixed_dw": L.PG_MIXED_DW,
+             "fp64_tangent": L.PG_FP64_TANGENT}
 NVAR = 8
 
 
@@ -90,7 +91,7 @@ class Solver:
         return (nz + (d == 2), ny + (d == 1), nx + (d == 0))
 
     # -- state transfer (interior layout, as in a .dbl dump) --
-    def upload(self, vc: np.ndarray, bs=(None, None, None)):
+    def _put(self, fn: str, vc: np.ndarray, bs=(None, None, None)):
         nx, ny, nz = self.nx
         vc = np.ascontiguousarray(vc, dtype=np.float64).reshape(NVAR, nz, ny, nx)
         keep = [np.ascontiguousarray(vc[q]) for q in range(NVAR)]
@@ -98,18 +99,47 @@ class Solver:
         if self.ct:
             for d in range(self.dims):
                 faces[d] = np.ascontiguousarray(bs[d], dtype=np.float64).reshape(self.face_shape(d))
-        L.check(L.lib().pg_upload(self.h, _ptrs(keep, 8), _ptrs(faces, 3), L.PG_LAYOUT_INTERIOR),
-                "pg_upload")
+        L.check(getattr(L.lib(), fn)(self.h, _ptrs(keep, 8), _ptrs(faces, 3), L.PG_LAYOUT_INTERIOR), fn)
 
-    def download(self):
+    def _get(self, fn: str):
         nx, ny, nz = self.nx
         vc = np.zeros((NVAR, nz, ny, nx))
         views = [vc[q] for q in range(NVAR)]
         faces = [np.zeros(self.face_shape(d)) if (self.ct and d < self.dims) else None
                  for d in range(3)]
-        L.check(L.lib().pg_download(self.h, _ptrs(views, 8), _ptrs(faces, 3),
-                                    L.PG_LAYOUT_INTERIOR), "pg_download")
+        L.check(getattr(L.lib(), fn)(self.h, _ptrs(views, 8), _ptrs(faces, 3), L.PG_LAYOUT_INTERIOR), fn)
         return vc, faces
+
+    def upload(self, vc: np.ndarray, bs=(None, None, None)):
+        self._put("pg_upload", vc, bs)
+
+    def download(self):
+        return self._get("pg_download")
+
+    # -- differentiation (frozen dt) --
+    def tangent_upload(self, dvc: np.ndarray, dbs=(None, None, None)):
+        """Direction of the tangent-linear model (precision "fp64_tangent")."""
+        self._put("pg_tangent_upload", dvc, dbs)
+
+    def tangent_download(self):
+        return self._get("pg_tangent_download")
+
+    def adjoint_set(self, lvc: np.ndarray, lbs=(None, None, None)):
+        """Adjoint (gradient) on the state after the step to be reversed."""
+        self._put("pg_adjoint_set", lvc, lbs)
+
+    def adjoint_step(self, dt: float):
+        """Adjoint through one RK2 step of length dt from the current state."""
+        L.check(L.lib().pg_adjoint_step(self.h, float(dt)), "pg_adjoint_step")
+
+    def adjoint_get(self):
+        return self._get("pg_adjoint_get")
+
+    def checkpoint_save(self, slot: int):
+        L.check(L.lib().pg_checkpoint_save(self.h, int(slot)), "pg_checkpoint_save")
+
+    def checkpoint_load(self, slot: int):
+        L.check(L.lib().pg_checkpoint_load(self.h, int(slot)), "pg_checkpoint_load")
 
     # -- stepping --
     def advance(self, dt: float):
