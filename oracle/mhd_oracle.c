@@ -52,6 +52,7 @@ struct oc_problem {
   unsigned char *flag;
   int64_t nfail;
   double max_mach;
+  int roe_bad;           /* Roe: negative a^2 met (the reference stops there) */
 };
 
 /* ------------------------------------------------------------------ */
@@ -215,6 +216,231 @@ static void hll_solver(const double *vL, const double *uL, const double *vR,
     }
     o->press = (SR * ptL - SL * ptR) * scrh;
   }
+}
+
+/* Src/MHD/roe.c:53-799: linearised solver of Cargo & Gallice (1997), ideal
+   EOS, no background field, HLL hybridisation off, entropy fix with
+   delta = 1e-6.  Waves in the order of the KWAVES enumeration
+   (Src/MHD/mod_defs.h:54-72): fast-, fast+, entropy, div.B, slow-, slow+
+   and, with three components, Alfven-, Alfven+.  Returns 1 when the Roe
+   sound speed squared is negative (the reference stops there). */
+static int roe_solver(const double *vL, const double *uL, const double *vR,
+                      const double *uR, double gamma, int c3, const Rot *r,
+                      Iface *o, double *mach) {
+  const int vn = r->vn, vt = r->vt, vb = r->vb, bn = r->bn, bt = r->bt, bb = r->bb;
+  const double delta = 1.e-6, g1 = gamma - 1.0;
+  double fL[NV], fR[NV], ptL, ptR, dV[NV], dU[NV];
+  double srL, srR, sl, sr, rho, sqrt_rho, u, v, w, Bx, By, Bz, sBx, bx, by, bz;
+  double bt2, b2, Btmag, X, vdm, BdB, vel2, HL, HR, H, Hgas, a2, scrh, ca2, cf2, cs2;
+  double cf, cs, ca, a, af, as, beta_y, beta_z, beta_dv, beta_dB, beta_v;
+  double lam[8], eta[8], al[8], c[8];
+  double Rf[8], Rs[8], Ra[8], Rfp[8], Rsp[8], Rap[8], Re[8];
+  int bad = 0, nv, k;
+  flux(vL, uL, fL, &ptL, r);
+  flux(vR, uR, fR, &ptR, r);
+  for (nv = 0; nv < NV; nv++) {
+    dV[nv] = vR[nv] - vL[nv];
+    dU[nv] = uR[nv] - uL[nv];
+  }
+  /* Roe averages */
+  srL = sqrt(vL[RHO]);
+  srR = sqrt(vR[RHO]);
+  sl = srL / (srL + srR);
+  sr = srR / (srL + srR);
+  rho = sr * vL[RHO] + sl * vR[RHO];
+  sqrt_rho = sqrt(rho);
+  u = sl * vL[vn] + sr * vR[vn];
+  v = sl * vL[vt] + sr * vR[vt];
+  w = sl * vL[vb] + sr * vR[vb];
+  Bx = sr * vL[bn] + sl * vR[bn];
+  By = sr * vL[bt] + sl * vR[bt];
+  Bz = sr * vL[bb] + sl * vR[bb];
+  sBx = (Bx >= 0.0 ? 1.0 : -1.0);
+  bx = Bx / sqrt_rho;
+  by = By / sqrt_rho;
+  bz = Bz / sqrt_rho;
+  bt2 = 0.0 + by * by + bz * bz;
+  b2 = bx * bx + bt2;
+  Btmag = sqrt(bt2 * rho);
+  X = dV[bn] * dV[bn] + dV[bt] * dV[bt] + dV[bb] * dV[bb];
+  X /= (srL + srR) * (srL + srR) * 2.0;
+  vdm = u * dU[vn] + v * dU[vt] + w * dU[vb];
+  BdB = Bx * dU[bn] + By * dU[bt] + Bz * dU[bb];
+  /* enthalpy and sound speed */
+  vel2 = u * u + v * v + w * w;
+  dV[PRS] = g1 * ((0.5 * vel2 - X) * dV[RHO] - vdm + dU[ENG] - BdB);
+  HL = (uL[ENG] + ptL) / vL[RHO];
+  HR = (uR[ENG] + ptR) / vR[RHO];
+  H = sl * HL + sr * HR;
+  Hgas = H - b2;
+  a2 = (2.0 - gamma) * X + g1 * (Hgas - 0.5 * vel2);
+  if (a2 < 0.0) {
+    bad = 1;
+    a2 = sqrt(gamma * (vL[PRS] + vR[PRS]) / (vL[RHO] + vR[RHO]));
+  }
+  /* fast and slow speeds */
+  scrh = a2 - b2;
+  ca2 = bx * bx;
+  scrh = scrh * scrh + 4.0 * bt2 * a2;
+  scrh = sqrt(scrh);
+  cf2 = 0.5 * (a2 + b2 + scrh);
+  cs2 = a2 * ca2 / cf2;
+  cf = sqrt(cf2);
+  cs = sqrt(cs2);
+  ca = sqrt(ca2);
+  a = sqrt(a2);
+  if (cf == cs) {
+    af = 1.0;
+    as = 0.0;
+  } else if (a <= cs) {
+    af = 0.0;
+    as = 1.0;
+  } else if (cf <= a) {
+    af = 1.0;
+    as = 0.0;
+  } else {
+    scrh = 1.0 / (cf2 - cs2);
+    af = (a2 - cs2) * scrh;
+    as = (cf2 - a2) * scrh;
+    af = MAX(0.0, af);
+    as = MAX(0.0, as);
+    af = sqrt(af);
+    as = sqrt(as);
+  }
+  if (Btmag > 1.e-9) {
+    if (c3) {
+      beta_y = By / Btmag;
+      beta_z = Bz / Btmag;
+    } else {
+      beta_y = (By >= 0.0 ? 1.0 : -1.0);
+      beta_z = 0.0;
+    }
+  } else {
+    beta_y = c3 ? 0.70710678118654752440 : 1.0;
+    beta_z = c3 ? 0.70710678118654752440 : 0.0;
+  }
+  beta_dv = 0.0 + beta_y * dV[vt] + beta_z * dV[vb];
+  beta_dB = 0.0 + beta_y * dV[bt] + beta_z * dV[bb];
+  beta_v = 0.0 + beta_y * v + beta_z * w;
+
+  /* eigenvector entries by row role: 0 rho, 1 m_n, 2 m_t, 3 m_b, 4 B_t,
+     5 B_b, 6 energy (the B_n row is zero for every wave) */
+  /* fast waves */
+  scrh = as * cs * sBx;
+  lam[0] = u - cf;
+  Rf[0] = af;
+  Rf[1] = af * lam[0];
+  Rf[2] = af * v + scrh * beta_y;
+  Rf[3] = af * w + scrh * beta_z;
+  Rf[4] = as * a * beta_y / sqrt_rho;
+  Rf[5] = as * a * beta_z / sqrt_rho;
+  Rf[6] = af * (Hgas - u * cf) + scrh * beta_v + as * a * Btmag / sqrt_rho;
+  eta[0] = af * (X * dV[RHO] + dV[PRS]) + rho * scrh * beta_dv - rho * af * cf * dV[vn] +
+           sqrt_rho * as * a * beta_dB;
+  eta[0] *= 0.5 / a2;
+  lam[1] = u + cf;
+  Rfp[0] = af;
+  Rfp[1] = af * lam[1];
+  Rfp[2] = af * v - scrh * beta_y;
+  Rfp[3] = af * w - scrh * beta_z;
+  Rfp[4] = Rf[4];
+  Rfp[5] = Rf[5];
+  Rfp[6] = af * (Hgas + u * cf) - scrh * beta_v + as * a * Btmag / sqrt_rho;
+  eta[1] = af * (X * dV[RHO] + dV[PRS]) - rho * scrh * beta_dv + rho * af * cf * dV[vn] +
+           sqrt_rho * as * a * beta_dB;
+  eta[1] *= 0.5 / a2;
+  /* entropy wave */
+  lam[2] = u;
+  Re[0] = 1.0;
+  Re[1] = u;
+  Re[2] = v;
+  Re[3] = w;
+  Re[6] = 0.5 * vel2 + (gamma - 2.0) / g1 * X;
+  eta[2] = ((a2 - X) * dV[RHO] - dV[PRS]) / a2;
+  /* div.B wave: zero jump */
+  lam[3] = u;
+  eta[3] = 0.0;
+  /* slow waves */
+  scrh = af * cf * sBx;
+  lam[4] = u - cs;
+  Rs[0] = as;
+  Rs[1] = as * lam[4];
+  Rs[2] = as * v - scrh * beta_y;
+  Rs[3] = as * w - scrh * beta_z;
+  Rs[4] = -af * a * beta_y / sqrt_rho;
+  Rs[5] = -af * a * beta_z / sqrt_rho;
+  Rs[6] = as * (Hgas - u * cs) - scrh * beta_v - af * a * Btmag / sqrt_rho;
+  eta[4] = as * (X * dV[RHO] + dV[PRS]) - rho * scrh * beta_dv - rho * as * cs * dV[vn] -
+           sqrt_rho * af * a * beta_dB;
+  eta[4] *= 0.5 / a2;
+  lam[5] = u + cs;
+  Rsp[0] = as;
+  Rsp[1] = as * lam[5];
+  Rsp[2] = as * v + scrh * beta_y;
+  Rsp[3] = as * w + scrh * beta_z;
+  Rsp[4] = Rs[4];
+  Rsp[5] = Rs[5];
+  Rsp[6] = as * (Hgas + u * cs) + scrh * beta_v - af * a * Btmag / sqrt_rho;
+  eta[5] = as * (X * dV[RHO] + dV[PRS]) + rho * scrh * beta_dv + rho * as * cs * dV[vn] -
+           sqrt_rho * af * a * beta_dB;
+  eta[5] *= 0.5 / a2;
+  /* Alfven waves (three components only) */
+  lam[6] = u - ca;
+  lam[7] = u + ca;
+  Ra[2] = -rho * beta_z;
+  Ra[3] = +rho * beta_y;
+  Ra[4] = -sBx * sqrt_rho * beta_z;
+  Ra[5] = sBx * sqrt_rho * beta_y;
+  Ra[6] = -rho * (v * beta_z - w * beta_y);
+  Rap[2] = -Ra[2];
+  Rap[3] = -Ra[3];
+  Rap[4] = Ra[4];
+  Rap[5] = Ra[5];
+  Rap[6] = -Ra[6];
+  eta[6] = +beta_y * dV[vb] - beta_z * dV[vt] + sBx / sqrt_rho * (beta_y * dV[bb] - beta_z * dV[bt]);
+  eta[6] *= 0.5;
+  eta[7] = -beta_y * dV[vb] + beta_z * dV[vt] + sBx / sqrt_rho * (beta_y * dV[bb] - beta_z * dV[bt]);
+  eta[7] *= 0.5;
+
+  o->cmax = fabs(u) + cf;
+  *mach = fabs(u / a);
+  for (k = 0; k < 8; k++) al[k] = fabs(lam[k]);
+  /* entropy fix */
+  if (al[0] < 0.5 * delta) al[0] = lam[0] * lam[0] / delta + 0.25 * delta;
+  if (al[1] < 0.5 * delta) al[1] = lam[1] * lam[1] / delta + 0.25 * delta;
+  if (al[4] < 0.5 * delta) al[4] = lam[4] * lam[4] / delta + 0.25 * delta;
+  if (al[5] < 0.5 * delta) al[5] = lam[5] * lam[5] / delta + 0.25 * delta;
+  for (k = 0; k < 8; k++) c[k] = al[k] * eta[k];
+  /* upwind sum over the waves in enumeration order (zero entries skipped) */
+  {
+    double s_rho, s_mn, s_mt, s_mb, s_bt, s_bb, s_en;
+    s_rho = 0.0 + c[0] * Rf[0] + c[1] * Rfp[0] + c[2] * Re[0] + c[4] * Rs[0] + c[5] * Rsp[0];
+    s_mn = 0.0 + c[0] * Rf[1] + c[1] * Rfp[1] + c[2] * Re[1] + c[4] * Rs[1] + c[5] * Rsp[1];
+    s_mt = 0.0 + c[0] * Rf[2] + c[1] * Rfp[2] + c[2] * Re[2] + c[4] * Rs[2] + c[5] * Rsp[2];
+    s_mb = 0.0 + c[0] * Rf[3] + c[1] * Rfp[3] + c[2] * Re[3] + c[4] * Rs[3] + c[5] * Rsp[3];
+    s_bt = 0.0 + c[0] * Rf[4] + c[1] * Rfp[4] + c[4] * Rs[4] + c[5] * Rsp[4];
+    s_bb = 0.0 + c[0] * Rf[5] + c[1] * Rfp[5] + c[4] * Rs[5] + c[5] * Rsp[5];
+    s_en = 0.0 + c[0] * Rf[6] + c[1] * Rfp[6] + c[2] * Re[6] + c[4] * Rs[6] + c[5] * Rsp[6];
+    if (c3) {
+      s_mt = s_mt + c[6] * Ra[2] + c[7] * Rap[2];
+      s_mb = s_mb + c[6] * Ra[3] + c[7] * Rap[3];
+      s_bt = s_bt + c[6] * Ra[4] + c[7] * Rap[4];
+      s_bb = s_bb + c[6] * Ra[5] + c[7] * Rap[5];
+      s_en = s_en + c[6] * Ra[6] + c[7] * Rap[6];
+    }
+    o->f[RHO] = 0.5 * (fL[RHO] + fR[RHO] - s_rho);
+    o->f[vn] = 0.5 * (fL[vn] + fR[vn] - s_mn);
+    o->f[vt] = 0.5 * (fL[vt] + fR[vt] - s_mt);
+    o->f[vb] = 0.5 * (fL[vb] + fR[vb] - s_mb);
+    o->f[bn] = 0.5 * (fL[bn] + fR[bn] - 0.0);
+    o->f[bt] = 0.5 * (fL[bt] + fR[bt] - s_bt);
+    o->f[bb] = 0.5 * (fL[bb] + fR[bb] - s_bb);
+    o->f[ENG] = 0.5 * (fL[ENG] + fR[ENG] - s_en);
+  }
+  o->press = 0.5 * (ptL + ptR);
+  o->SL = lam[0];
+  o->SR = lam[1];
+  return bad;
 }
 
 /* Src/MHD/hlld.c:44-452 (IDEAL EOS, no background field) */
@@ -548,7 +774,7 @@ static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1
   const double dxd = p->c.dx[dir];
   double mach_max = 0.0, invdt1 = 0.0;
   long npencil, ip;
-  int tn;
+  int tn, roe_bad = 0;
 
   if (p->c.ct) { /* update_stage.c:144-148 */
     if (dims >= 2) { tbeg--; tend++; }
@@ -557,7 +783,7 @@ static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1
   tn = tend - tbeg + 1;
   npencil = (long)tn * (bend - bbeg + 1);
 
-#pragma omp parallel reduction(max : mach_max, invdt1)
+#pragma omp parallel reduction(max : mach_max, invdt1) reduction(| : roe_bad)
   {
     Pencil w;
     pencil_alloc(&w, ntot + 2);
@@ -597,6 +823,9 @@ static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1
         double m;
         if (p->c.solver == OC_HLL)
           hll_solver(w.vp[i], w.up[i], w.vm[i + 1], w.um[i + 1], p->c.gamma, &r, &w.ifc[i], &m);
+        else if (p->c.solver == OC_ROE)
+          roe_bad |= roe_solver(w.vp[i], w.up[i], w.vm[i + 1], w.um[i + 1], p->c.gamma,
+                                p->c.components == 3, &r, &w.ifc[i], &m);
         else
           hlld_solver(w.vp[i], w.up[i], w.vm[i + 1], w.um[i + 1], p->c.gamma, &r, &w.ifc[i], &m);
         mach_max = MAX(m, mach_max);
@@ -641,6 +870,7 @@ static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1
     pencil_free(&w);
   }
   if (*mach_out < mach_max) *mach_out = mach_max;
+  if (roe_bad) p->roe_bad = 1;
   *inv_dt_1d = MAX(*inv_dt_1d, invdt1);
 }
 
@@ -857,6 +1087,7 @@ int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
 
   p->nfail = 0;
   p->max_mach = 0.0;
+  p->roe_bad = 0;
   memset(p->flag, 0, p->ncell);
   /* stage 1 */
   boundary(p);
@@ -910,7 +1141,7 @@ int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
   if (inv_dt_hyp) *inv_dt_hyp = inv_dt;
   if (max_mach) *max_mach = p->max_mach;
   if (nfail) *nfail = p->nfail;
-  return 0;
+  return p->roe_bad ? 1 : 0;
 }
 
 /* Main loop dt logic, Src/main.c:143-151, 215, 236, 389-575 */
@@ -921,7 +1152,7 @@ int oc_run(oc_problem *p, int nsteps, double first_dt, double cfl,
   for (s = 0; s < nsteps; s++) {
     double inv_dt, dt_hyp, dtnext;
     if (dts) dts[s] = g_dt;
-    oc_advance(p, g_dt, &inv_dt, NULL, NULL);
+    if (oc_advance(p, g_dt, &inv_dt, NULL, NULL)) return 1;
     g_time += g_dt;
     dt_hyp = 1.0 / inv_dt;
     dt_hyp *= cfl;

@@ -49,7 +49,8 @@ void oc_set_state(oc_problem *p, const double *vc, const double *bs0,
                   const double *bs1, const double *bs2);
 void oc_get_state(const oc_problem *p, double *vc, double *bs0, double *bs1,
                   double *bs2);
-/* One AdvanceStep with time step dt; returns invDt_hyp (pre-division by
+/* One AdvanceStep with time step dt (returns 0; 1 when the Roe solver met a
+   negative sound speed squared, where the reference stops); gives invDt_hyp (pre-division by
    DIMENSIONS already applied as in the reference) and the floor count. */
 int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
                int64_t *nfail);

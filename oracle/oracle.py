@@ -114,11 +114,13 @@ class Oracle:
         inv = C.c_double()
         mach = C.c_double()
         nf = C.c_int64()
-        lib().oc_advance(self.h, dt, C.byref(inv), C.byref(mach), C.byref(nf))
+        if lib().oc_advance(self.h, dt, C.byref(inv), C.byref(mach), C.byref(nf)):
+            raise RuntimeError("oracle: Roe solver met a negative sound speed squared")
         return inv.value, mach.value, nf.value
 
     def run(self, nsteps: int, first_dt: float, cfl: float, cfl_max_var: float = 1.1):
         dts = np.zeros(max(nsteps, 1))
         t = C.c_double()
-        lib().oc_run(self.h, nsteps, first_dt, cfl, cfl_max_var, _ptr(dts), C.byref(t))
+        if lib().oc_run(self.h, nsteps, first_dt, cfl, cfl_max_var, _ptr(dts), C.byref(t)):
+            raise RuntimeError("oracle: Roe solver met a negative sound speed squared")
         return dts[:nsteps], t.value

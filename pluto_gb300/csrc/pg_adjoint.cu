@@ -15,8 +15,8 @@
 //   k_adj_ct       CT_Update                   (Src/MHD/CT/ct_update.c:29-220)
 //   k_adj_emf      CT_EMF_HLL_Solver           (Src/MHD/CT/ct_emf_average.c:179-352)
 //   k_adj_flux     RightHandSide, U += rhs     (Src/MHD/rhs.c:193-201)
-//   k_adj_riemann  HLL / HLLD flux with the face-field override
-//                  (Src/MHD/hll.c, Src/MHD/hlld.c, Src/States/plm_states.c:271)
+//   k_adj_riemann  HLL / HLLD / Roe flux with the face-field override
+//                  (Src/MHD/hll.c, hlld.c, roe.c, Src/States/plm_states.c:271)
 //   k_adj_recon    States (PLM / PPM) and CT_StoreVelSlopes
 //   k_adj_bound    Boundary (periodic / outflow copies), transposed
 //   k_adj_p2c      PrimToCons3D                (Src/mappers3D.c:74)
@@ -143,14 +143,20 @@ __device__ __forceinline__ void recon_pt(int recon, int lim, int nv, const T* w,
 // Riemann outputs at one interface (as k_riemann):
 // out[0..7] flux, out[8] total pressure, out[9] max(0,-SL), out[10] max(0,SR).
 template <class T, int DIR>
-__device__ __forceinline__ void riemann_pt(int solver, double gamma, const T* vL, const T* vR, T* out) {
+__device__ __forceinline__ void riemann_pt(int solver, double gamma, bool c3, const T* vL, const T* vR, T* out) {
   T uL[NV], uR[NV], mach = T(0.0);
   const T gmm1 = T(gamma - 1.0);
   prim_to_cons(vL, uL, gmm1);
   prim_to_cons(vR, uR, gmm1);
   Iface<T> o;
-  if (solver == PG_HLL) hll_solver<DIR, false>(vL, uL, vR, uR, T(gamma), o, mach);
-  else hlld_solver<DIR, false>(vL, uL, vR, uR, T(gamma), o, mach);
+  if (solver == PG_HLL) {
+    hll_solver<DIR, false>(vL, uL, vR, uR, T(gamma), o, mach);
+  } else if (solver == PG_ROE) {
+    int bad = 0;
+    roe_solver<DIR, false>(vL, uL, vR, uR, T(gamma), c3, o, mach, bad);
+  } else {
+    hlld_solver<DIR, false>(vL, uL, vR, uR, T(gamma), o, mach);
+  }
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) out[nv] = o.f[nv];
   out[NV] = o.press;
@@ -508,7 +514,7 @@ __global__ void k_adj_riemann(AdjArgs A, Box box, int solver) {
       }
       if (kk < NV) xL[kk].d[0] = 1.0;
       else xR[kk - NV].d[0] = 1.0;
-      riemann_pt<D1, DIR>(solver, A.f.gamma, xL, xR, out);
+      riemann_pt<D1, DIR>(solver, A.f.gamma, A.f.ncomp == 3, xL, xR, out);
 #pragma unroll
       for (int o = 0; o < NO; o++) gk += lam[o] * out[o].d[0];
     }
@@ -680,6 +686,8 @@ void fwd_dir(Solver* S, const F64A<double>& f) {
   k_recon<double, DIR><<<grid_for(rb.count()), kT, 0, st>>>(f, rb);
   if (S->cfg.riemann == PG_HLL)
     k_riemann<double, DIR, PG_HLL, false><<<grid_for(ib.count(), 128), 128, 0, st>>>(f, ib, 0);
+  else if (S->cfg.riemann == PG_ROE)
+    k_riemann<double, DIR, PG_ROE, false><<<grid_for(ib.count(), 128), 128, 0, st>>>(f, ib, 0);
   else
     k_riemann<double, DIR, PG_HLLD, false><<<grid_for(ib.count(), 128), 128, 0, st>>>(f, ib, 0);
 }

@@ -42,7 +42,7 @@ int validate_config(const pg_config* c) {
   if (c->reconstruction != PG_LINEAR && c->reconstruction != PG_PARABOLIC)
     return fail(PG_ERR_INVALID, "unsupported reconstruction");
   if (c->limiter < PG_FLAT_LIM || c->limiter > PG_DEFAULT_LIM) return fail(PG_ERR_INVALID, "unsupported limiter");
-  if (c->riemann != PG_HLL && c->riemann != PG_HLLD)
+  if (c->riemann != PG_HLL && c->riemann != PG_HLLD && c->riemann != PG_ROE)
     return fail(PG_ERR_INVALID, "unsupported Riemann solver");
   if (c->time_stepping != PG_RK2 && c->time_stepping != PG_RK3)
     return fail(PG_ERR_INVALID, "unsupported time stepping");
@@ -266,6 +266,8 @@ static int enqueue_step(Solver* S) {
 static int read_scalars(Solver* S) {
   CK(cudaMemcpyAsync(S->sc_host, S->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, S->stream));
   CK(cudaStreamSynchronize(S->stream));
+  if (S->sc_host->status & 2)
+    return fail(PG_ERR_NAN, "Roe solver: negative sound speed squared (Src/MHD/roe.c stops the run here)");
   if (S->sc_host->status) return fail(PG_ERR_NAN, "non-finite inverse time step (NaN or Inf in the state)");
   return PG_OK;
 }

@@ -37,6 +37,12 @@ static cudaError_t launch_batch_t(const BatchArgs<T>& b, int rs, int solver, int
   PG_BATCH_CASE(4, PG_HLLD, 3)
   PG_BATCH_CASE(4, PG_HLL, 2)
   PG_BATCH_CASE(4, PG_HLL, 3)
+  PG_BATCH_CASE(1, PG_ROE, 2)
+  PG_BATCH_CASE(1, PG_ROE, 3)
+  PG_BATCH_CASE(0, PG_ROE, 2)
+  PG_BATCH_CASE(0, PG_ROE, 3)
+  PG_BATCH_CASE(4, PG_ROE, 2)
+  PG_BATCH_CASE(4, PG_ROE, 3)
 #undef PG_BATCH_CASE
   return cudaErrorInvalidValue;
 }
@@ -122,6 +128,7 @@ BatchArgs<T> bargs(pg_batch* B) {
   a.bc = B->cfg.bc[0];
   a.limiter = B->cfg.limiter;
   a.solver = B->cfg.riemann;
+  a.ncomp = B->cfg.components;
   return a;
 }
 
@@ -348,6 +355,7 @@ extern "C" int pg_batch_run(pg_batch* B, int nsteps, double first_dt, double cfl
   if (elapsed_ms) *elapsed_ms = ms;
   int st = 0;
   BCK(cudaMemcpy(&st, B->d_status, sizeof(int), cudaMemcpyDeviceToHost));
+  if (st & 2) return bfail(PG_ERR_NAN, "pg_batch_run: Roe solver met a negative sound speed squared");
   if (st) return bfail(PG_ERR_NAN, "pg_batch_run: non-finite dt in a tube");
   return PG_OK;
 }

@@ -37,7 +37,7 @@ struct BatchArgs {
   int* status;               // sticky error flags
   unsigned int* counter;     // work queue head
   double gamma, cfl, cfl_max_var, small_rho, small_p;
-  int ng, bc, limiter, solver;
+  int ng, bc, limiter, solver, ncomp;
 };
 
 template <class T> struct Batch;
@@ -242,8 +242,15 @@ __device__ double batch_stage(const BatchArgs<T>& b, int tube, T* const* Vin, T*
       prim_to_cons(vL, uL, gmm1);
       prim_to_cons(vR, uR, gmm1);
       Iface<T> o;
-      if (SOLVER == PG_HLL) hll_solver<0, false>(vL, uL, vR, uR, (T)gam, o, mach);
-      else hlld_solver<0, false>(vL, uL, vR, uR, (T)gam, o, mach);
+      if (SOLVER == PG_HLL) {
+        hll_solver<0, false>(vL, uL, vR, uR, (T)gam, o, mach);
+      } else if (SOLVER == PG_ROE) {
+        int bad = 0;
+        roe_solver<0, false>(vL, uL, vR, uR, (T)gam, b.ncomp == 3, o, mach, bad);
+        if (bad) atomicOr(b.status, 2);
+      } else {
+        hlld_solver<0, false>(vL, uL, vR, uR, (T)gam, o, mach);
+      }
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) sf[nv * (B + 1) + s] = o.f[nv];
       sf[NV * (B + 1) + s] = o.press;

@@ -28,6 +28,12 @@ static cudaError_t launch_mixed_a(const BatchArgs<float>& b, int rs, int solver,
   PG_BATCH_CASE(4, PG_HLLD, 3)
   PG_BATCH_CASE(4, PG_HLL, 2)
   PG_BATCH_CASE(4, PG_HLL, 3)
+  PG_BATCH_CASE(1, PG_ROE, 2)
+  PG_BATCH_CASE(1, PG_ROE, 3)
+  PG_BATCH_CASE(0, PG_ROE, 2)
+  PG_BATCH_CASE(0, PG_ROE, 3)
+  PG_BATCH_CASE(4, PG_ROE, 2)
+  PG_BATCH_CASE(4, PG_ROE, 3)
 #undef PG_BATCH_CASE
   return cudaErrorInvalidValue;
 }

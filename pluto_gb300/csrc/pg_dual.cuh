@@ -62,6 +62,11 @@ __host__ __device__ __forceinline__ Dual<N> operator-(const Dual<N>& a) {
   return r;
 }
 
+template <int N>
+__host__ __device__ __forceinline__ Dual<N> operator+(const Dual<N>& a) {
+  return a;
+}
+
 // mixed Dual/double operands (a double is a constant)
 template <int N> __host__ __device__ __forceinline__ Dual<N> operator+(const Dual<N>& a, double b) { return a + Dual<N>(b); }
 template <int N> __host__ __device__ __forceinline__ Dual<N> operator+(double a, const Dual<N>& b) { return Dual<N>(a) + b; }

@@ -33,7 +33,7 @@ struct F64A {
   unsigned char* flag;
   DevScalars* sc;
   double gamma, small_rho, small_p, cfl, cfl_max_var;
-  int limiter, recon, ct, nbfield;
+  int limiter, recon, ct, nbfield, ncomp;
   int device_dt;
 };
 
@@ -210,8 +210,15 @@ __global__ void k_riemann(F64A<T> a, Box box, int want_invdt_1d) {
     prim_to_cons(vL, uL, gmm1);
     prim_to_cons(vR, uR, gmm1);
     Iface<T> o;
-    if (SOLVER == PG_HLL) hll_solver<DIR, MACH>(vL, uL, vR, uR, T(a.gamma), o, machT);
-    else hlld_solver<DIR, MACH>(vL, uL, vR, uR, T(a.gamma), o, machT);
+    if (SOLVER == PG_HLL) {
+      hll_solver<DIR, MACH>(vL, uL, vR, uR, T(a.gamma), o, machT);
+    } else if (SOLVER == PG_ROE) {
+      int bad = 0;
+      roe_solver<DIR, MACH>(vL, uL, vR, uR, T(a.gamma), a.ncomp == 3, o, machT, bad);
+      if (bad) atomicOr(&a.sc->status, 2);
+    } else {
+      hlld_solver<DIR, MACH>(vL, uL, vR, uR, T(a.gamma), o, machT);
+    }
     mach = value_of(machT);
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) a.F[nv][c] = o.f[nv];
@@ -464,6 +471,7 @@ static F64A<T> make_args(Solver* S) {
   a.recon = S->cfg.reconstruction;
   a.ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
   a.nbfield = a.ct ? S->g.dims : 0;
+  a.ncomp = S->cfg.components;
   a.device_dt = S->device_dt;
   return a;
 }
@@ -499,6 +507,9 @@ static void launch_sweep(Solver* S, const F64A<T>& a, int stage) {
     if (S->cfg.riemann == PG_HLL) {
       if (mach) k_riemann<T, DIR, PG_HLL, true><<<gr, 128, 0, st>>>(a, ib, want1d);
       else k_riemann<T, DIR, PG_HLL, false><<<gr, 128, 0, st>>>(a, ib, want1d);
+    } else if (S->cfg.riemann == PG_ROE) {
+      if (mach) k_riemann<T, DIR, PG_ROE, true><<<gr, 128, 0, st>>>(a, ib, want1d);
+      else k_riemann<T, DIR, PG_ROE, false><<<gr, 128, 0, st>>>(a, ib, want1d);
     } else {
       if (mach) k_riemann<T, DIR, PG_HLLD, true><<<gr, 128, 0, st>>>(a, ib, want1d);
       else k_riemann<T, DIR, PG_HLLD, false><<<gr, 128, 0, st>>>(a, ib, want1d);

@@ -60,7 +60,7 @@ struct MixArgs {
   double inv_gmm1_d;     // 1/(gamma-1) as a double
   float inv_gmm1_hi, inv_gmm1_lo;  // the same as a double-word pair
   float third_hi, third_lo;        // 1/3 as a double-word pair
-  int limiter, recon, ct, nbfield, accmask, device_dt;
+  int limiter, recon, ct, nbfield, accmask, device_dt, ncomp;
 };
 
 // ---------------------------------------------------------------------------
@@ -115,8 +115,15 @@ __device__ __forceinline__ void solve_iface(const MixArgs& a, int solver, float*
   float uL[NV], uR[NV], mach;
   prim_to_cons(vL, uL, gmm1);
   prim_to_cons(vR, uR, gmm1);
-  if (solver == PG_HLL) hll_solver<DIR, false>(vL, uL, vR, uR, a.gamma, o, mach);
-  else hlld_solver<DIR, false>(vL, uL, vR, uR, a.gamma, o, mach);
+  if (solver == PG_HLL) {
+    hll_solver<DIR, false>(vL, uL, vR, uR, a.gamma, o, mach);
+  } else if (solver == PG_ROE) {
+    int bad = 0;
+    roe_solver<DIR, false>(vL, uL, vR, uR, a.gamma, a.ncomp == 3, o, mach, bad);
+    if (bad) atomicOr(&a.sc->status, 2);
+  } else {
+    hlld_solver<DIR, false>(vL, uL, vR, uR, a.gamma, o, mach);
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -704,6 +711,7 @@ static MixArgs margs(Solver* S, int in_buf, int out_buf, int v0_buf) {
   a.recon = S->cfg.reconstruction;
   a.ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
   a.nbfield = a.ct ? S->g.dims : 0;
+  a.ncomp = S->cfg.components;
   // Variables whose flux difference is accumulated: all of them except the
   // cell-centred field components that CT rebuilds from the faces.
   a.accmask = 0xff;

@@ -164,6 +164,182 @@ __device__ __forceinline__ void hll_solver(const T* vL, const T* uL, const T* vR
   }
 }
 
+// Src/MHD/roe.c:53-799: linearised solver of Cargo & Gallice (1997), ideal
+// EOS, no background field, HLL hybridisation off, entropy fix delta = 1e-6.
+// Waves in the order of the KWAVES enumeration (Src/MHD/mod_defs.h:54-72):
+// fast-, fast+, entropy, div.B (zero jump), slow-, slow+ and, with three
+// components, Alfven-, Alfven+.  The upwind sum skips the structurally zero
+// eigenvector entries (adding them changes no bit).  bad = 1 when the Roe
+// sound speed squared is negative (the reference stops the run there).
+template <int DIR, bool MACH, class T>
+__device__ __forceinline__ void roe_solver(const T* vL, const T* uL, const T* vR, const T* uR, T gamma, bool c3,
+                                           Iface<T>& o, T& mach, int& bad) {
+  using R = Rot<DIR>;
+  constexpr int vn = R::vn, vt = R::vt, vb = R::vb, bn = R::bn, bt = R::bt, bb = R::bb;
+  const T delta = T(1.e-6), g1 = gamma - T(1);
+  T fL[NV], fR[NV], ptL, ptR, dV[NV], dU[NV];
+  flux<DIR>(vL, uL, fL, ptL);
+  flux<DIR>(vR, uR, fR, ptR);
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    dV[nv] = vR[nv] - vL[nv];
+    dU[nv] = uR[nv] - uL[nv];
+  }
+  // Roe averages
+  const T srL = sqrt(vL[RHO]), srR = sqrt(vR[RHO]);
+  const T sl = srL / (srL + srR), sr = srR / (srL + srR);
+  const T rho = sr * vL[RHO] + sl * vR[RHO];
+  const T sqrt_rho = sqrt(rho);
+  const T u = sl * vL[vn] + sr * vR[vn];
+  const T v = sl * vL[vt] + sr * vR[vt];
+  const T w = sl * vL[vb] + sr * vR[vb];
+  const T Bx = sr * vL[bn] + sl * vR[bn];
+  const T By = sr * vL[bt] + sl * vR[bt];
+  const T Bz = sr * vL[bb] + sl * vR[bb];
+  const T sBx = Bx >= T(0) ? T(1) : T(-1);
+  const T bx = Bx / sqrt_rho, by = By / sqrt_rho, bz = Bz / sqrt_rho;
+  const T bt2 = T(0) + by * by + bz * bz;
+  const T b2 = bx * bx + bt2;
+  const T Btmag = sqrt(bt2 * rho);
+  T X = dV[bn] * dV[bn] + dV[bt] * dV[bt] + dV[bb] * dV[bb];
+  X /= (srL + srR) * (srL + srR) * T(2);
+  const T vdm = u * dU[vn] + v * dU[vt] + w * dU[vb];
+  const T BdB = Bx * dU[bn] + By * dU[bt] + Bz * dU[bb];
+  // enthalpy and sound speed
+  const T vel2 = u * u + v * v + w * w;
+  dV[PRS] = g1 * ((T(0.5) * vel2 - X) * dV[RHO] - vdm + dU[ENG] - BdB);
+  const T HL = (uL[ENG] + ptL) / vL[RHO];
+  const T HR = (uR[ENG] + ptR) / vR[RHO];
+  const T H = sl * HL + sr * HR;
+  const T Hgas = H - b2;
+  T a2 = (T(2) - gamma) * X + g1 * (Hgas - T(0.5) * vel2);
+  if (a2 < T(0)) {
+    bad = 1;
+    a2 = sqrt(gamma * (vL[PRS] + vR[PRS]) / (vL[RHO] + vR[RHO]));
+  }
+  // fast and slow speeds
+  T scrh = a2 - b2;
+  const T ca2 = bx * bx;
+  scrh = scrh * scrh + T(4) * bt2 * a2;
+  scrh = sqrt(scrh);
+  const T cf2 = T(0.5) * (a2 + b2 + scrh);
+  const T cs2 = a2 * ca2 / cf2;
+  const T cf = sqrt(cf2), cs = sqrt(cs2), ca = sqrt(ca2), a = sqrt(a2);
+  T af, as;
+  if (cf == cs) {
+    af = T(1);
+    as = T(0);
+  } else if (a <= cs) {
+    af = T(0);
+    as = T(1);
+  } else if (cf <= a) {
+    af = T(1);
+    as = T(0);
+  } else {
+    scrh = T(1) / (cf2 - cs2);
+    af = (a2 - cs2) * scrh;
+    as = (cf2 - a2) * scrh;
+    af = pmax(T(0), af);
+    as = pmax(T(0), as);
+    af = sqrt(af);
+    as = sqrt(as);
+  }
+  T beta_y, beta_z;
+  if (Btmag > T(1.e-9)) {
+    if (c3) {
+      beta_y = By / Btmag;
+      beta_z = Bz / Btmag;
+    } else {
+      beta_y = By >= T(0) ? T(1) : T(-1);
+      beta_z = T(0);
+    }
+  } else {
+    beta_y = c3 ? T(0.70710678118654752440) : T(1);
+    beta_z = c3 ? T(0.70710678118654752440) : T(0);
+  }
+  const T beta_dv = T(0) + beta_y * dV[vt] + beta_z * dV[vb];
+  const T beta_dB = T(0) + beta_y * dV[bt] + beta_z * dV[bb];
+  const T beta_v = T(0) + beta_y * v + beta_z * w;
+  const T h2 = T(0.5) / a2;
+
+  // fast waves (eigenvector rows: rho, m_n, m_t, m_b, B_t, B_b, energy)
+  scrh = as * cs * sBx;
+  const T l0 = u - cf, l1 = u + cf;
+  const T f_mt0 = af * v + scrh * beta_y, f_mb0 = af * w + scrh * beta_z;
+  const T f_mt1 = af * v - scrh * beta_y, f_mb1 = af * w - scrh * beta_z;
+  const T f_bt = as * a * beta_y / sqrt_rho, f_bb = as * a * beta_z / sqrt_rho;
+  const T f_e0 = af * (Hgas - u * cf) + scrh * beta_v + as * a * Btmag / sqrt_rho;
+  const T f_e1 = af * (Hgas + u * cf) - scrh * beta_v + as * a * Btmag / sqrt_rho;
+  T eta0 = af * (X * dV[RHO] + dV[PRS]) + rho * scrh * beta_dv - rho * af * cf * dV[vn] +
+           sqrt_rho * as * a * beta_dB;
+  eta0 *= h2;
+  T eta1 = af * (X * dV[RHO] + dV[PRS]) - rho * scrh * beta_dv + rho * af * cf * dV[vn] +
+           sqrt_rho * as * a * beta_dB;
+  eta1 *= h2;
+  // entropy wave
+  const T e_en = T(0.5) * vel2 + (gamma - T(2)) / g1 * X;
+  const T eta2 = ((a2 - X) * dV[RHO] - dV[PRS]) / a2;
+  // slow waves
+  scrh = af * cf * sBx;
+  const T l4 = u - cs, l5 = u + cs;
+  const T s_mt4 = as * v - scrh * beta_y, s_mb4 = as * w - scrh * beta_z;
+  const T s_mt5 = as * v + scrh * beta_y, s_mb5 = as * w + scrh * beta_z;
+  const T s_bt = -af * a * beta_y / sqrt_rho, s_bb = -af * a * beta_z / sqrt_rho;
+  const T s_e4 = as * (Hgas - u * cs) - scrh * beta_v - af * a * Btmag / sqrt_rho;
+  const T s_e5 = as * (Hgas + u * cs) + scrh * beta_v - af * a * Btmag / sqrt_rho;
+  T eta4 = as * (X * dV[RHO] + dV[PRS]) - rho * scrh * beta_dv - rho * as * cs * dV[vn] -
+           sqrt_rho * af * a * beta_dB;
+  eta4 *= h2;
+  T eta5 = as * (X * dV[RHO] + dV[PRS]) + rho * scrh * beta_dv + rho * as * cs * dV[vn] -
+           sqrt_rho * af * a * beta_dB;
+  eta5 *= h2;
+
+  o.cmax = fabs(u) + cf;
+  if (MACH) mach = fabs(u / a);
+  // |lambda| with the entropy fix on the fast and slow waves
+  auto fix = [&](T l) -> T {
+    T al = fabs(l);
+    if (al < T(0.5) * delta) al = l * l / delta + T(0.25) * delta;
+    return al;
+  };
+  const T c0 = fix(l0) * eta0, c1 = fix(l1) * eta1, c2 = fabs(u) * eta2;
+  const T c4 = fix(l4) * eta4, c5 = fix(l5) * eta5;
+  T s_rho = T(0) + c0 * af + c1 * af + c2 * T(1) + c4 * as + c5 * as;
+  T s_mn = T(0) + c0 * (af * l0) + c1 * (af * l1) + c2 * u + c4 * (as * l4) + c5 * (as * l5);
+  T s_mt = T(0) + c0 * f_mt0 + c1 * f_mt1 + c2 * v + c4 * s_mt4 + c5 * s_mt5;
+  T s_mb = T(0) + c0 * f_mb0 + c1 * f_mb1 + c2 * w + c4 * s_mb4 + c5 * s_mb5;
+  T s_bt2 = T(0) + c0 * f_bt + c1 * f_bt + c4 * s_bt + c5 * s_bt;
+  T s_bb2 = T(0) + c0 * f_bb + c1 * f_bb + c4 * s_bb + c5 * s_bb;
+  T s_en = T(0) + c0 * f_e0 + c1 * f_e1 + c2 * e_en + c4 * s_e4 + c5 * s_e5;
+  if (c3) {  // Alfven waves
+    const T l6 = u - ca, l7 = u + ca;
+    const T a_mt = -rho * beta_z, a_mb = +rho * beta_y;
+    const T a_bt = -sBx * sqrt_rho * beta_z, a_bb = sBx * sqrt_rho * beta_y;
+    const T a_en = -rho * (v * beta_z - w * beta_y);
+    T eta6 = +beta_y * dV[vb] - beta_z * dV[vt] + sBx / sqrt_rho * (beta_y * dV[bb] - beta_z * dV[bt]);
+    eta6 *= T(0.5);
+    T eta7 = -beta_y * dV[vb] + beta_z * dV[vt] + sBx / sqrt_rho * (beta_y * dV[bb] - beta_z * dV[bt]);
+    eta7 *= T(0.5);
+    const T c6 = fabs(l6) * eta6, c7 = fabs(l7) * eta7;
+    s_mt = s_mt + c6 * a_mt + c7 * (-a_mt);
+    s_mb = s_mb + c6 * a_mb + c7 * (-a_mb);
+    s_bt2 = s_bt2 + c6 * a_bt + c7 * a_bt;
+    s_bb2 = s_bb2 + c6 * a_bb + c7 * a_bb;
+    s_en = s_en + c6 * a_en + c7 * (-a_en);
+  }
+  o.f[RHO] = T(0.5) * (fL[RHO] + fR[RHO] - s_rho);
+  o.f[vn] = T(0.5) * (fL[vn] + fR[vn] - s_mn);
+  o.f[vt] = T(0.5) * (fL[vt] + fR[vt] - s_mt);
+  o.f[vb] = T(0.5) * (fL[vb] + fR[vb] - s_mb);
+  o.f[bn] = T(0.5) * (fL[bn] + fR[bn] - T(0));
+  o.f[bt] = T(0.5) * (fL[bt] + fR[bt] - s_bt2);
+  o.f[bb] = T(0.5) * (fL[bb] + fR[bb] - s_bb2);
+  o.f[ENG] = T(0.5) * (fL[ENG] + fR[ENG] - s_en);
+  o.press = T(0.5) * (ptL + ptR);
+  o.SL = l0;
+  o.SR = l1;
+}
+
 // Src/MHD/hlld.c:44-452 (ideal EOS, no background field)
 template <int DIR, bool MACH, class T>
 __device__ __forceinline__ void hlld_solver(const T* vL, const T* uL, const T* vR, const T* uR, T gamma,

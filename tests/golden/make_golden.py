@@ -17,6 +17,7 @@ from __future__ import annotations
 
 import json
 import sys
+from dataclasses import replace
 from pathlib import Path
 
 import numpy as np
@@ -63,6 +64,10 @@ def setups():
         br.tube_setup(2, 160, 80),
         br.cpa_setup(32, 20),
         br.turb_setup(12, 10),
+        br.ot_setup("roe", 32, 30),
+        replace(br.cpa_setup(32, 20), solver="roe", name="cpa_roe_32"),
+        replace(br.blast_setup(16, 12), solver="roe", name="blast_roe_16"),
+        replace(br.tube_setup(0, 256, 100), solver="roe", name="tube_roe_0_256"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

@@ -42,7 +42,7 @@ def test_batch_fp64_matches_oracle_per_tube(recon, stepping):
 
 def test_batch_fp64_matches_golden_tubes():
     from pluto_gb300.batch import Batch
-    names = ["tube_0_256", "tube_1_200", "tube_2_160"]
+    names = ["tube_0_256", "tube_1_200", "tube_2_160", "tube_roe_0_256"]
     metas, st0, st1 = [], [], []
     for nm in names:
         meta, vc0, _, vc1, _ = load_golden(nm)

@@ -39,7 +39,8 @@ def test_fp64_matches_reference_goldens(name):
     assert abs(t - meta["t_final"]) <= 1e-6 * meta["t_final"]
 
 
-@pytest.mark.parametrize("name", ["ot_hlld_32", "blast_16", "tube_0_256", "turb_12", "blast_floor_16"])
+@pytest.mark.parametrize("name", ["ot_hlld_32", "blast_16", "tube_0_256", "turb_12", "blast_floor_16",
+                                  "ot_roe_32", "cpa_roe_32", "blast_roe_16", "tube_roe_0_256"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
@@ -93,7 +94,7 @@ def _random_blast(n, seed):
 
 
 @pytest.mark.parametrize("solver,recon,stepping", [("hlld", "LINEAR", "RK2"), ("hll", "PARABOLIC", "RK3"),
-                                                   ("hlld", "PARABOLIC", "RK2")])
+                                                   ("hlld", "PARABOLIC", "RK2"), ("roe", "PARABOLIC", "RK3")])
 def test_fp64_vs_oracle_random_3d(solver, recon, stepping):
     from oracle.oracle import Oracle
     spec, vc, bs = _random_blast(24, seed=7)
