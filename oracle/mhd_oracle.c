@@ -703,6 +703,81 @@ static void bound_box(oc_problem *p, double *q, int face_dir, int ib, int ie,
 #undef IDX
 }
 
+/* Face areas of a uniform Cartesian grid, Src/set_geometry.c:139-210:
+   A1 = 1*dx2(*dx3), A2 = dx1*1(*dx3), A3 = dx1*dx2*1 (D_EXPAND over DIMENSIONS). */
+static void face_areas(const oc_problem *p, double A[3]) {
+  const double *dx = p->c.dx;
+  if (p->c.dims == 2) {
+    A[0] = 1.0 * dx[1];
+    A[1] = dx[0] * 1.0;
+    A[2] = 0.0;
+  } else {
+    A[0] = 1.0 * dx[1] * dx[2];
+    A[1] = dx[0] * 1.0 * dx[2];
+    A[2] = dx[0] * dx[1] * 1.0;
+  }
+}
+
+/* FillMagneticField, Src/MHD/CT/ct_fill_mag_field.c:38-180 (Cartesian): the
+   staggered component normal to an outflow side is recovered in the ghost
+   faces from div B = 0, marching away from the boundary face. */
+static void fill_magnetic_field(oc_problem *p, int side) {
+  const int dims = p->c.dims;
+  int ibeg = 0, iend = p->nt[0] - 1, di = 1;
+  int jbeg = 0, jend = p->nt[1] - 1, dj = 1;
+  int kbeg = 0, kend = p->nt[2] - 1, dk = 1;
+  int i, j, k;
+  double A[3];
+  double *bx = p->bs[0], *by = p->bs[1], *bz = dims == 3 ? p->bs[2] : NULL;
+  face_areas(p, A);
+  if (dims < 3) { kbeg = kend = 0; dk = 1; }
+  if (side == 0) { ibeg = p->beg[0] - 1; iend = 0; di = -1; }
+  if (side == 1) ibeg = p->end[0] + 1;
+  if (side == 2) { jbeg = p->beg[1] - 1; jend = 0; dj = -1; }
+  if (side == 3) jbeg = p->end[1] + 1;
+  if (side == 4) { kbeg = p->beg[2] - 1; kend = 0; dk = -1; }
+  if (side == 5) kbeg = p->end[2] + 1;
+  for (k = kbeg; dk * k <= dk * kend; k += dk)
+    for (j = jbeg; dj * j <= dj * jend; j += dj)
+      for (i = ibeg; di * i <= di * iend; i += di) {
+        double bxp = bx[FI(p, 0, k, j, i)], bxm = bx[FI(p, 0, k, j, i - 1)];
+        double byp = by[FI(p, 1, k, j, i)], bym = by[FI(p, 1, k, j - 1, i)];
+        double bzp = 0.0, bzm = 0.0;
+        double dBx = 0.0, dBy = 0.0, dBz = 0.0;
+        if (dims == 3) {
+          bzp = bz[FI(p, 2, k, j, i)];
+          bzm = bz[FI(p, 2, k - 1, j, i)];
+        }
+        dBx = (A[0] * bxp - A[0] * bxm);
+        dBy = (A[1] * byp - A[1] * bym);
+        if (dims == 3) dBz = (A[2] * bzp - A[2] * bzm);
+        if (side == 0) bx[FI(p, 0, k, j, i - 1)] = (A[0] * bxp + dBy + dBz) / A[0];
+        else if (side == 1) bx[FI(p, 0, k, j, i)] = (A[0] * bxm - (dBy + dBz)) / A[0];
+        else if (side == 2) by[FI(p, 1, k, j - 1, i)] = (A[1] * byp + dBx + dBz) / A[1];
+        else if (side == 3) by[FI(p, 1, k, j, i)] = (A[1] * bym - (dBx + dBz)) / A[1];
+        else if (side == 4) bz[FI(p, 2, k - 1, j, i)] = (A[2] * bzp + dBx + dBy) / A[2];
+        else bz[FI(p, 2, k, j, i)] = (A[2] * bzm - (dBx + dBy)) / A[2];
+      }
+}
+
+/* CT_AverageNormalMagField, Src/MHD/CT/ct_field_average.c:134-275
+   (Cartesian): normal cell-centred field in the ghost zones of one side. */
+static void ct_average_normal(oc_problem *p, int side) {
+  const int d = side / 2;
+  int i, j, k;
+  int lo[3] = {0, 0, 0}, hi[3] = {p->nt[0] - 1, p->nt[1] - 1, p->nt[2] - 1};
+  double *B = p->vc[BX1 + d], *b = p->bs[d];
+  if (side % 2 == 0) { lo[d] = 0; hi[d] = p->beg[d] - 1; }
+  else { lo[d] = p->end[d] + 1; hi[d] = p->nt[d] - 1; }
+  for (k = lo[2]; k <= hi[2]; k++)
+    for (j = lo[1]; j <= hi[1]; j++)
+      for (i = lo[0]; i <= hi[0]; i++) {
+        int o[3] = {0, 0, 0};
+        o[d] = 1;
+        B[CI(p, k, j, i)] = 0.5 * (b[FI(p, d, k, j, i)] + b[FI(p, d, k - o[2], j - o[1], i - o[0])]);
+      }
+}
+
 static void boundary(oc_problem *p) {
   int is, nv;
   int dims = p->c.dims;
@@ -729,8 +804,12 @@ static void boundary(oc_problem *p) {
         } else if (fd != d) {
           bound_box(p, p->bs[fd], fd, fib, fie, fjb, fje, fkb, fke, is, type);
         }
-        /* outflow normal-field recovery (FillMagneticField) is not part of
-           the configurations covered here; see oc_create's check. */
+      }
+      /* outflow: the normal staggered component from div B = 0, then its
+         cell average (Src/boundary.c:171-190) */
+      if (type == OC_OUTFLOW) {
+        fill_magnetic_field(p, is);
+        ct_average_normal(p, is);
       }
     }
   }
@@ -1174,7 +1253,7 @@ oc_problem *oc_create(const oc_config *cfg) {
   p->c = *cfg;
   if (cfg->ct && cfg->dims < 2) { free(p); return NULL; }
   for (d = 0; d < 3; d++)
-    if (cfg->ct && d < cfg->dims && cfg->bc[d] != OC_PERIODIC) { free(p); return NULL; }
+    if (cfg->bc[d] != OC_PERIODIC && cfg->bc[d] != OC_OUTFLOW) { free(p); return NULL; }
   p->ng = cfg->recon == OC_PARABOLIC ? 3 : 2; /* Src/get_nghost.c:28-104 */
   for (d = 0; d < 3; d++) {
     int active = d < cfg->dims;

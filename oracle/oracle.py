@@ -75,7 +75,8 @@ class Oracle:
         for d in range(3):
             c.nx[d] = int(spec["nx"][d]) if d < spec["dims"] else 1
             c.dx[d] = float(spec["dx"][d])
-            c.bc[d] = BC[spec.get("bc", "periodic")]
+            bc = spec.get("bc", "periodic")
+            c.bc[d] = BC[bc[d] if isinstance(bc, (list, tuple)) else bc]
         c.gamma = float(spec["gamma"])
         c.recon = RECON[spec["recon"]]
         c.limiter = LIMITER[spec["limiter"]]

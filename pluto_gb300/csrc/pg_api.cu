@@ -49,9 +49,7 @@ int validate_config(const pg_config* c) {
   if (c->divb == PG_CONSTRAINED_TRANSPORT) {
     if (c->dims < 2) return fail(PG_ERR_INVALID, "constrained transport needs dims >= 2");
     if (c->emf_average != PG_UCT_HLL) return fail(PG_ERR_INVALID, "only the UCT_HLL emf average is supported");
-    for (int d = 0; d < c->dims; d++)
-      if (c->bc[d] != PG_PERIODIC)
-        return fail(PG_ERR_INVALID, "constrained transport supports periodic boundaries only");
+
   } else if (c->divb != PG_DIVB_NONE) {
     return fail(PG_ERR_INVALID, "unsupported divergence control");
   }

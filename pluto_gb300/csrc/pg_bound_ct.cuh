@@ -1,0 +1,182 @@
+// Boundary fill under constrained transport when an axis has outflow sides:
+// the reference's side-by-side sequence (Src/boundary.c:137-300), one axis
+// after the other.  Per axis, k_bound_axis copies the cells and the
+// transverse face components (zero gradient or periodic image; the normal
+// component too on a periodic axis), including the faces' -1 layers (index -1
+// along their own axis, Src/initialize.c:448-453), which live in Bm1 because
+// the face arrays do not store them; then, on an outflow axis,
+// k_fill_normal recovers the normal face component in the ghost faces from
+// div B = 0 (FillMagneticField, Src/MHD/CT/ct_fill_mag_field.c:38-180) and
+// averages it to the cell centres (CT_AverageNormalMagField,
+// Src/MHD/CT/ct_field_average.c:134-275).  T is the storage type, C the
+// arithmetic type (double for the FP32-storage mixed path).
+#pragma once
+#include "pg_internal.h"
+#include "pg_physics.cuh"
+
+namespace pg {
+
+template <class T>
+struct BoundCT {
+  Geom g;
+  T* V[8];
+  T* Bs[3];
+  T* Bm1[3];  // -1 layers: Bm1[0][k][j], Bm1[1][k][i], Bm1[2][j][i]
+  int nbfield;
+  double area[3];
+};
+
+// Cartesian face areas, Src/set_geometry.c:139-210 (D_EXPAND over DIMENSIONS).
+inline void face_areas(const Geom& g, double A[3]) {
+  const double* dx = g.dx;
+  if (g.dims == 2) {
+    A[0] = 1.0 * dx[1];
+    A[1] = dx[0] * 1.0;
+    A[2] = 0.0;
+  } else {
+    A[0] = 1.0 * dx[1] * dx[2];
+    A[1] = dx[0] * 1.0 * dx[2];
+    A[2] = dx[0] * dx[1] * 1.0;
+  }
+}
+
+template <class T>
+__device__ __forceinline__ T* bct_face(const BoundCT<T>& a, int fd, int k, int j, int i) {
+  const Geom& g = a.g;
+  const int x = fd == 0 ? i : (fd == 1 ? j : k);
+  if (x < 0) {
+    if (fd == 0) return a.Bm1[0] + (long long)k * g.nt[1] + j;
+    if (fd == 1) return a.Bm1[1] + (long long)k * g.nt[0] + i;
+    return a.Bm1[2] + (long long)j * g.nt[0] + i;
+  }
+  return a.Bs[fd] + cidx(g, k, j, i);
+}
+
+// Ghost layers of axis AX over the full extent of the other axes (the
+// reference's CENTER / X*FACE boxes).  Sources are interior along AX, so the
+// threads are independent.
+template <class T, int AX>
+__global__ void k_bound_axis(BoundCT<T> a, int type, long long nghost) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= nghost) return;
+  const Geom& g = a.g;
+  constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
+  const int ng = g.beg[AX], n = g.nx[AX];
+  const int l = (int)(q % (2 * ng));
+  const long long t = q / (2 * ng);
+  int c[3], s[3];
+  c[B1] = (int)(t % g.nt[B1]);
+  c[B2] = (int)(t / g.nt[B1]);
+  const bool lo = l < ng;
+  c[AX] = lo ? l : g.end[AX] + 1 + (l - ng);
+  s[B1] = c[B1];
+  s[B2] = c[B2];
+  s[AX] = type == PG_PERIODIC ? (lo ? c[AX] + n : c[AX] - n) : (lo ? g.beg[AX] : g.end[AX]);
+  const long long dst = cidx(g, c[2], c[1], c[0]), src = cidx(g, s[2], s[1], s[0]);
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) a.V[nv][dst] = a.V[nv][src];
+  for (int fd = 0; fd < a.nbfield; fd++) {
+    if (fd != AX) {
+      a.Bs[fd][dst] = a.Bs[fd][src];
+      if (c[fd] == 0) {  // the -1 layer of this transverse component
+        int cm[3] = {c[0], c[1], c[2]}, sm[3] = {s[0], s[1], s[2]};
+        cm[fd] = -1;
+        sm[fd] = -1;
+        *bct_face(a, fd, cm[2], cm[1], cm[0]) = *bct_face(a, fd, sm[2], sm[1], sm[0]);
+      }
+    } else if (type == PG_PERIODIC) {
+      // normal component: faces beg-1 .. -1 from their images; on the end
+      // side the face at end keeps its value (its image beg-1 is set equal
+      // to it by the begin side)
+      if (lo || c[AX] != g.end[AX]) a.Bs[fd][dst] = a.Bs[fd][src];
+      if (lo && c[AX] == 0) {
+        int cm[3] = {c[0], c[1], c[2]}, sm[3] = {s[0], s[1], s[2]};
+        cm[AX] = -1;
+        sm[AX] = n - 1;
+        *bct_face(a, fd, cm[2], cm[1], cm[0]) = *bct_face(a, fd, sm[2], sm[1], sm[0]);
+      }
+    }
+  }
+}
+
+// One thread per transverse position and side: the normal component marched
+// away from the boundary face, then its cell average.
+template <class T, class C, int AX>
+__global__ void k_fill_normal(BoundCT<T> a, long long ntrans) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= 2 * ntrans) return;
+  const Geom& g = a.g;
+  constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
+  const bool lo = (q & 1) == 0;
+  const long long t = q >> 1;
+  int c[3];
+  c[B1] = (int)(t % g.nt[B1]);
+  c[B2] = (int)(t / g.nt[B1]);
+  const bool d3 = g.dims == 3;
+  auto face = [&](int fd, int k, int j, int i) -> C { return C(*bct_face(a, fd, k, j, i)); };
+  // A_d b_d(+) - A_d b_d(-) of component fd at cell c
+  auto dB = [&](int fd) -> C {
+    int m[3] = {c[0], c[1], c[2]};
+    m[fd] -= 1;
+    return a.area[fd] * face(fd, c[2], c[1], c[0]) - a.area[fd] * face(fd, m[2], m[1], m[0]);
+  };
+  // the other two terms in x, y, z order (zero for z in 2D)
+  auto others = [&]() -> C {
+    if (AX == 0) return dB(1) + (d3 ? dB(2) : C(0.0));
+    if (AX == 1) return dB(0) + (d3 ? dB(2) : C(0.0));
+    return dB(0) + dB(1);
+  };
+  const double An = a.area[AX];
+  auto average = [&](int x) {
+    c[AX] = x;
+    int m[3] = {c[0], c[1], c[2]};
+    m[AX] = x - 1;
+    const C avg = 0.5 * (face(AX, c[2], c[1], c[0]) + face(AX, m[2], m[1], m[0]));
+    a.V[BX1 + AX][cidx(g, c[2], c[1], c[0])] = T(avg);
+  };
+  if (lo) {
+    for (int x = g.beg[AX] - 1; x >= 0; x--) {
+      c[AX] = x;
+      const C bp = face(AX, c[2], c[1], c[0]);
+      C r;
+      if (AX == 0) r = (An * bp + dB(1) + (d3 ? dB(2) : C(0.0))) / An;
+      else if (AX == 1) r = (An * bp + dB(0) + (d3 ? dB(2) : C(0.0))) / An;
+      else r = (An * bp + dB(0) + dB(1)) / An;
+      int m[3] = {c[0], c[1], c[2]};
+      m[AX] = x - 1;
+      *bct_face(a, AX, m[2], m[1], m[0]) = T(r);
+    }
+    for (int x = 0; x < g.beg[AX]; x++) average(x);
+  } else {
+    for (int x = g.end[AX] + 1; x < g.nt[AX]; x++) {
+      c[AX] = x;
+      int m[3] = {c[0], c[1], c[2]};
+      m[AX] = x - 1;
+      const C bm = face(AX, m[2], m[1], m[0]);
+      *bct_face(a, AX, c[2], c[1], c[0]) = T((An * bm - others()) / An);
+    }
+    for (int x = g.end[AX] + 1; x < g.nt[AX]; x++) average(x);
+  }
+}
+
+template <class T, class C, int AX>
+static void launch_bound_ct_axis(Solver* S, const BoundCT<T>& b, const char* copy_name, const char* fill_name) {
+  const Geom& g = b.g;
+  constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
+  const long long ntrans = (long long)g.nt[B1] * g.nt[B2];
+  const long long nghost = 2LL * g.beg[AX] * ntrans;
+  PG_LAUNCH(S, copy_name, (k_bound_axis<T, AX><<<grid_for(nghost), kThreads, 0, S->stream>>>(
+                              b, S->cfg.bc[AX], nghost)));
+  if (S->cfg.bc[AX] == PG_OUTFLOW)
+    PG_LAUNCH(S, fill_name, (k_fill_normal<T, C, AX><<<grid_for(2 * ntrans, 128), 128, 0, S->stream>>>(
+                                b, ntrans)));
+}
+
+template <class T, class C>
+static void launch_bound_ct(Solver* S, const BoundCT<T>& b, const char* copy_name, const char* fill_name) {
+  launch_bound_ct_axis<T, C, 0>(S, b, copy_name, fill_name);
+  if (b.g.dims > 1) launch_bound_ct_axis<T, C, 1>(S, b, copy_name, fill_name);
+  if (b.g.dims > 2) launch_bound_ct_axis<T, C, 2>(S, b, copy_name, fill_name);
+}
+
+}  // namespace pg

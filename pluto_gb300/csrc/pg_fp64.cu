@@ -52,6 +52,17 @@ int fp64_alloc(Solver* S) {
     }
     if (alloc(&S->E[2])) return PG_ERR_NOMEM;
     if (S->g.dims == 3 && (alloc(&S->E[0]) || alloc(&S->E[1]))) return PG_ERR_NOMEM;
+    bool outflow = false;
+    for (int d = 0; d < S->g.dims; d++) outflow |= S->cfg.bc[d] == PG_OUTFLOW;
+    if (outflow) {
+      const Geom& g = S->g;
+      const long long m[3] = {(long long)g.nt[1] * g.nt[2], (long long)g.nt[0] * g.nt[2],
+                              (long long)g.nt[0] * g.nt[1]};
+      for (int d = 0; d < g.dims; d++) {
+        if (cudaMalloc(&S->Bm1[d], m[d] * es) != cudaSuccess) return PG_ERR_NOMEM;
+        cudaMemset(S->Bm1[d], 0, m[d] * es);
+      }
+    }
   }
   if (cudaMalloc(&S->flag, n) != cudaSuccess) return PG_ERR_NOMEM;
   cudaMemset(S->flag, 0, n);
@@ -70,8 +81,8 @@ void fp64_free(Solver* S) {
   S->P = S->CM = S->CDT = nullptr;
   S->flag = nullptr;
   for (int d = 0; d < 3; d++) {
-    f(S->Bs[d]); f(S->Bs0[d]); f(S->SL[d]); f(S->SR[d]); f(S->E[d]);
-    S->Bs[d] = S->Bs0[d] = S->SL[d] = S->SR[d] = S->E[d] = nullptr;
+    f(S->Bs[d]); f(S->Bs0[d]); f(S->SL[d]); f(S->SR[d]); f(S->E[d]); f(S->Bm1[d]);
+    S->Bs[d] = S->Bs0[d] = S->SL[d] = S->SR[d] = S->E[d] = S->Bm1[d] = nullptr;
     for (int c = 0; c < 3; c++) { f(S->DV[d][c]); S->DV[d][c] = nullptr; }
   }
 }

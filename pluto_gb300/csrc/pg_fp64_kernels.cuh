@@ -9,6 +9,7 @@
 #include "pg_internal.h"
 #include "pg_physics.cuh"
 #include "pg_dual.cuh"
+#include "pg_bound_ct.cuh"
 
 namespace pg {
 
@@ -29,12 +30,15 @@ struct F64A {
   T* SR[3];
   T* DV[3][3];
   T* E[3];
+  T* Bm1[3];  // face -1 layers: Bm1[0][k][j], Bm1[1][k][i], Bm1[2][j][i]
   T* CDT;
   unsigned char* flag;
   DevScalars* sc;
   double gamma, small_rho, small_p, cfl, cfl_max_var;
   int limiter, recon, ct, nbfield, ncomp;
   int device_dt;
+  int bc[3];
+  int ct_outflow;   // constrained transport with an outflow axis: per-axis boundary passes
 };
 
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
@@ -472,6 +476,14 @@ static F64A<T> make_args(Solver* S) {
   a.ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
   a.nbfield = a.ct ? S->g.dims : 0;
   a.ncomp = S->cfg.components;
+  for (int d = 0; d < 3; d++) {
+    a.Bm1[d] = (T*)S->Bm1[d];
+    a.bc[d] = S->cfg.bc[d];
+  }
+  a.ct_outflow = 0;
+  if (a.ct)
+    for (int d = 0; d < S->g.dims; d++) a.ct_outflow |= S->cfg.bc[d] == PG_OUTFLOW;
+
   a.device_dt = S->device_dt;
   return a;
 }
@@ -540,6 +552,19 @@ static void launch_stage_tail(Solver* S, const F64A<T>& a, const Box& dom) {
 template <class T>
 static void launch_bound(Solver* S, const F64A<T>& a) {
   const Geom& g = S->g;
+  if (a.ct_outflow) {
+    BoundCT<T> b;
+    b.g = a.g;
+    for (int nv = 0; nv < 8; nv++) b.V[nv] = a.V[nv];
+    for (int d = 0; d < 3; d++) {
+      b.Bs[d] = a.Bs[d];
+      b.Bm1[d] = a.Bm1[d];
+    }
+    b.nbfield = a.nbfield;
+    face_areas(g, b.area);
+    launch_bound_ct<T, T>(S, b, "fp64_bound", "fp64_fill_normal");
+    return;
+  }
   long long n0 = g.dims > 0 ? 2LL * g.beg[0] * g.nt[1] * g.nt[2] : 0;
   long long n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
   long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;

@@ -113,6 +113,7 @@ struct Solver {
   double* SR[3] = {};   // max(0, SR)
   double* DV[3][3] = {};// velocity slopes DV[dir][comp]
   double* E[3] = {};    // edge EMFs
+  double* Bm1[3] = {};  // face -1 layers (boundary scratch for outflow sides under CT)
   double* CDT = nullptr;
   unsigned char* flag = nullptr;
   // mixed path

@@ -25,6 +25,7 @@
 #include "pg_internal.h"
 #include "pg_physics.cuh"
 #include "pg_dw.cuh"
+#include "pg_bound_ct.cuh"
 
 namespace pg {
 
@@ -37,6 +38,7 @@ struct MixBufs {
   float* E[3];
   float* CDT;
   unsigned char* flag;
+  float* Bm1[3];  // face -1 layers (outflow sides under CT)
 };
 
 struct MixArgs {
@@ -644,6 +646,17 @@ int mixed_alloc(Solver* S) {
     }
     if (al(&M->b.E[2])) return PG_ERR_NOMEM;
     if (S->g.dims == 3 && (al(&M->b.E[0]) || al(&M->b.E[1]))) return PG_ERR_NOMEM;
+    const Geom& g = S->g;
+    const long long m[3] = {(long long)g.nt[1] * g.nt[2], (long long)g.nt[0] * g.nt[2],
+                            (long long)g.nt[0] * g.nt[1]};
+    for (int d = 0; d < g.dims; d++)
+      if (S->cfg.bc[d] == PG_OUTFLOW) {
+        for (int e = 0; e < g.dims; e++) {
+          if (cudaMalloc(&M->b.Bm1[e], m[e] * sizeof(float)) != cudaSuccess) return PG_ERR_NOMEM;
+          cudaMemset(M->b.Bm1[e], 0, m[e] * sizeof(float));
+        }
+        break;
+      }
   }
   if (cudaMalloc(&M->b.flag, n) != cudaSuccess) return PG_ERR_NOMEM;
   cudaMemset(M->b.flag, 0, n);
@@ -666,6 +679,7 @@ void mixed_free(Solver* S) {
     f(M->b.S[d][0]);
     f(M->b.S[d][1]);
     f(M->b.E[d]);
+    f(M->b.Bm1[d]);
     for (int c = 0; c < 3; c++) f(M->b.DV[d][c]);
   }
   delete M;
@@ -723,6 +737,20 @@ static MixArgs margs(Solver* S, int in_buf, int out_buf, int v0_buf) {
 
 static void mlaunch_bound(Solver* S, const MixArgs& a) {
   const Geom& g = S->g;
+  MixedState* M = (MixedState*)S->mixed;
+  if (a.ct && M->b.Bm1[0]) {  // outflow axis under CT: per-axis passes, FP64 face recovery
+    BoundCT<float> b;
+    b.g = g;
+    for (int nv = 0; nv < NV; nv++) b.V[nv] = (float*)a.Vin[nv];
+    for (int d = 0; d < 3; d++) {
+      b.Bs[d] = (float*)a.Bin[d];
+      b.Bm1[d] = M->b.Bm1[d];
+    }
+    b.nbfield = a.nbfield;
+    face_areas(g, b.area);
+    launch_bound_ct<float, double>(S, b, "mixed_bound", "mixed_fill_normal");
+    return;
+  }
   BoundArrays arr;
   arr.n = 0;
   for (int nv = 0; nv < NV; nv++) arr.q[arr.n++] = (float*)a.Vin[nv];

@@ -68,6 +68,8 @@ def setups():
         replace(br.cpa_setup(32, 20), solver="roe", name="cpa_roe_32"),
         replace(br.blast_setup(16, 12), solver="roe", name="blast_roe_16"),
         replace(br.tube_setup(0, 256, 100), solver="roe", name="tube_roe_0_256"),
+        replace(br.ot_setup("hlld", 32, 30), bc="outflow", name="ot_outflow_32"),
+        replace(br.turb_setup(12, 10), bc="outflow", name="turb_outflow_12"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

@@ -40,7 +40,8 @@ def test_fp64_matches_reference_goldens(name):
 
 
 @pytest.mark.parametrize("name", ["ot_hlld_32", "blast_16", "tube_0_256", "turb_12", "blast_floor_16",
-                                  "ot_roe_32", "cpa_roe_32", "blast_roe_16", "tube_roe_0_256"])
+                                  "ot_roe_32", "cpa_roe_32", "blast_roe_16", "tube_roe_0_256",
+                                  "ot_outflow_32", "turb_outflow_12"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
@@ -109,6 +110,27 @@ def test_fp64_vs_oracle_random_3d(solver, recon, stepping):
     b, bb = o.get_state()
     errs = _errors(a, ab, b, bb)
     assert max(errs.values()) <= TOL, errs
+
+
+@pytest.mark.parametrize("bc", [("outflow", "outflow", "outflow"), ("outflow", "periodic", "outflow"),
+                                ("periodic", "outflow", "periodic")])
+def test_fp64_vs_oracle_outflow_ct_3d(bc):
+    """Outflow sides under CT (FillMagneticField + normal averaging), mixed
+    with periodic axes, on a random 3D state against the oracle."""
+    from oracle.oracle import Oracle
+    spec, vc, bs = _random_blast(20, seed=5)
+    spec.update(bc=list(bc), solver="roe", recon="PARABOLIC", stepping="RK3")
+    s = _solver(spec)
+    o = Oracle(spec, nthreads=4)
+    s.upload(vc, bs)
+    o.set_state(vc, bs)
+    s.run(4, 1e-3, 0.3)
+    o.run(4, 1e-3, 0.3)
+    a, ab = s.download()
+    b, bb = o.get_state()
+    assert np.array_equal(a, b), _errors(a, ab, b, bb)
+    for d in range(3):
+        assert np.array_equal(ab[d], bb[d])
 
 
 def test_divergence_free_under_ct():
