@@ -61,7 +61,7 @@ def test_ct_requires_2d_and_accepts_outflow(lib):
     # outflow sides under CT pass validation (without a GPU the create then
     # stops at the first CUDA call, not at PG_ERR_INVALID)
     spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1), gamma=5 / 3, ct=True,
-                bc=("outflow", "periodic"))
+                bc=("outflow", "periodic", "periodic"))
     rc = lib.pg_create(C.byref(make_config(spec)), C.byref(h))
     assert rc != 1
     if rc == 0:
