@@ -49,7 +49,7 @@ math_interp math_lu_decomp math_qr_decomp math_misc math_ode math_quadrature
 math_random math_root_finders math_table2D
 bckgrnd_field eigenv fluxes get_current hll hllc hlld hll_speed mappers
 prim_eqn rhs roe set_solver source tvdlf rhs_source eos
-rk_step update_stage vec_pot_diff vec_pot_update""".split()
+vec_pot_diff vec_pot_update""".split()
 CT_SRC = "ct_field_average ct_emf ct_emf_average emf_userdef ct_update ct_fill_mag_field ct_stag_slopes".split()
 SRC_DIRS = ["Src", "Src/Time_Stepping", "Src/States", "Src/Math_Tools",
             "Src/MHD", "Src/MHD/CT", "Src/EOS/Ideal"]
@@ -211,6 +211,8 @@ def build(s: Setup, jobs: int = 8) -> Path:
     (run / "init.c").write_text(INIT_TEMPLATE % s.init_body)
     names = list(BASE_SRC)
     names += ["plm_states"] if s.recon == "LINEAR" else ["ppm_states", "ppm_coeffs"]
+    # time stepping: RK (rk_step + update_stage) or CTU (ctu_step + hancock)
+    names += ["ctu_step", "hancock"] if s.stepping == "HANCOCK" else ["rk_step", "update_stage"]
     if s.ct:
         names += CT_SRC
     srcs = [run / "init.c"]

@@ -53,6 +53,12 @@ struct oc_problem {
   int64_t nfail;
   double max_mach;
   int roe_bad;           /* Roe: negative a^2 met (the reference stops there) */
+  /* CTU (TIME_STEPPING HANCOCK) work arrays, ctu_step.c:195-221 */
+  double *up_s[3][NV], *um_s[3][NV], *rhs_s[3][NV], *uh[NV];
+  double *eface[6];        /* face EMFs: ezi, ezj, eyi, eyk, exj, exk (ct_emf.c:29-100) */
+  signed char *sv[3];      /* sign of the mass flux at each face (UCT_CONTACT) */
+  double *ecc[3];          /* cell-centred EMF (CT_ComputeCenterEMF) */
+  int emf_lo[3], emf_hi[3];/* emf->ibeg.. set by CT_StoreUpwindEMF */
 };
 
 /* ------------------------------------------------------------------ */
@@ -1153,6 +1159,472 @@ static void update_stage(oc_problem *p, double dt, int stage, double *inv_dt,
   }
 }
 
+
+/* ------------------------------------------------------------------ */
+/* Corner Transport Upwind (TIME_STEPPING HANCOCK), ctu_step.c:140-727  */
+/* ------------------------------------------------------------------ */
+
+/* PrimRHS, Src/MHD/prim_eqn.c:29-112 (ideal EOS, no 8-wave / GLM terms) */
+static void prim_rhs(const double *v, const double *dv, double gamma, const Rot *r, int c3,
+                     double *Adv) {
+  const int vn = r->vn, vt = r->vt, vb = r->vb, bn = r->bn, bt = r->bt, bb = r->bb;
+  double tau = 1.0 / v[RHO], scrh;
+  int nv;
+  for (nv = 0; nv < NV; nv++) Adv[nv] = 0.0;
+  Adv[RHO] = v[vn] * dv[RHO] + v[RHO] * dv[vn];
+  scrh = c3 ? 0.0 + v[bt] * dv[bt] + v[bb] * dv[bb] : 0.0 + v[bt] * dv[bt];
+  Adv[vn] = v[vn] * dv[vn] + tau * (dv[PRS] + scrh);
+  Adv[vt] = v[vn] * dv[vt] - tau * v[bn] * dv[bt];
+  if (c3) Adv[vb] = v[vn] * dv[vb] - tau * v[bn] * dv[bb];
+  Adv[bn] = 0.0;
+  Adv[bt] = v[bt] * dv[vn] - v[bn] * dv[vt] + v[vn] * dv[bt];
+  if (c3) Adv[bb] = v[bb] * dv[vn] - v[bn] * dv[vb] + v[vn] * dv[bb];
+  Adv[PRS] = gamma * v[PRS] * dv[vn] + v[vn] * dv[PRS];
+}
+
+/* face-EMF slot of (dir, component): ezi, ezj, eyi, eyk, exj, exk */
+enum { EZI = 0, EZJ, EYI, EYK, EXJ, EXK };
+
+/* One CTU sweep.  stage 1: normal predictors (PLM + primitive Hancock,
+   hancock.c:36-172, CheckPrimStates check_states.c:18-70), Riemann
+   problems, rhs with dt/2 and CTU_CT_Source (ctu_step.c:731-816), stored in
+   up_s/um_s/rhs_s (ctu_step.c:286-450).  stage 2: corner-coupled states
+   U +- + sum of the other directions' rhs, face normal field, ConsToPrim,
+   Riemann problems and U += rhs with dt (ctu_step.c:533-645). */
+static void ctu_sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt) {
+  const int dims = p->c.dims, ct = p->c.ct, c3 = p->c.components == 3;
+  const int td = dir == 0 ? 1 : 0, bd = dir == 2 ? 1 : 2;
+  const Rot r = rot_for(dir);
+  int nbeg = p->beg[dir], nend = p->end[dir];
+  int tbeg = p->beg[td], tend = p->end[td], bbeg = p->beg[bd], bend = p->end[bd];
+  const int ntot = p->nt[dir];
+  const double gmm1 = p->c.gamma - 1.0, inv_dl = p->inv_dx[dir], dxd = p->c.dx[dir];
+  const double dt2 = 0.5 * dt;
+  double invdt = *inv_dt;
+  long npencil, ip;
+  int tn;
+  if (stage == 1) {
+    if (dims >= 2) { tbeg--; tend++; }
+    if (dims == 3) { bbeg--; bend++; }
+    if (ct) {
+      nbeg--; nend++;
+      if (dims >= 2) { tbeg--; tend++; }
+      if (dims == 3) { bbeg--; bend++; }
+    }
+  } else if (ct) {
+    if (dims >= 2) { tbeg--; tend++; }
+    if (dims == 3) { bbeg--; bend++; }
+  }
+  if (ct) { p->emf_lo[dir] = nbeg - 1; p->emf_hi[dir] = nend; }
+  tn = tend - tbeg + 1;
+  npencil = (long)tn * (bend - bbeg + 1);
+
+#pragma omp parallel reduction(max : invdt)
+  {
+    Pencil w;
+    double (*vn)[NV] = malloc(sizeof(double[NV]) * (ntot + 2));
+    pencil_alloc(&w, ntot + 2);
+#pragma omp for schedule(static)
+    for (ip = 0; ip < npencil; ip++) {
+      int t = tbeg + (int)(ip % tn), b = bbeg + (int)(ip / tn);
+      int i, nv, ijk[3];
+      ijk[td] = t;
+      ijk[bd] = b;
+      for (i = 0; i < ntot; i++) {
+        size_t c;
+        ijk[dir] = i;
+        c = CI(p, ijk[2], ijk[1], ijk[0]);
+        for (nv = 0; nv < NV; nv++) w.v[i][nv] = vn[i][nv] = p->vc[nv][c];
+        if (ct) w.bn[i] = p->bs[dir][FI(p, dir, ijk[2], ijk[1], ijk[0])];
+      }
+      if (stage == 1) {
+        plm_states(w.v, w.vp, w.vm, nbeg - 1, nend + 1, p->c.limiter);
+        if (ct)
+          for (i = nbeg - 2; i <= nend + 1; i++) {
+            w.vp[i][r.bn] = w.bn[i];
+            w.vm[i + 1][r.bn] = w.bn[i];
+          }
+        for (i = nbeg - 1; i <= nend + 1; i++) { /* primitive Hancock step */
+          double dv[NV], Adv[NV];
+          for (nv = 0; nv < NV; nv++) dv[nv] = w.vp[i][nv] - w.vm[i][nv];
+          prim_rhs(w.v[i], dv, p->c.gamma, &r, c3, Adv);
+          for (nv = NV - 1; nv >= 0; nv--) {
+            double scrh = dt2 * (inv_dl * Adv[nv] - 0.0);
+            w.vp[i][nv] -= scrh;
+            w.vm[i][nv] -= scrh;
+          }
+        }
+        for (i = nbeg - 1; i <= nend + 1; i++) { /* CheckPrimStates */
+          int sw = (w.vp[i][PRS] < 0.0) || (w.vm[i][PRS] < 0.0);
+          sw = sw || (w.vp[i][RHO] < 0.0) || (w.vm[i][RHO] < 0.0);
+          if (sw) {
+            double sp = w.vp[i][r.bn], sm = w.vm[i][r.bn];
+            for (nv = 0; nv < NV; nv++) w.vm[i][nv] = w.vp[i][nv] = w.v[i][nv];
+            if (ct) { w.vp[i][r.bn] = sp; w.vm[i][r.bn] = sm; }
+          }
+        }
+        for (i = nbeg - 1; i <= nend + 1; i++) {
+          prim_to_cons(w.vp[i], w.up[i], gmm1);
+          prim_to_cons(w.vm[i], w.um[i], gmm1);
+        }
+      } else {
+        for (i = nbeg - 1; i <= nend + 1; i++) {
+          size_t c;
+          ijk[dir] = i;
+          c = CI(p, ijk[2], ijk[1], ijk[0]);
+          for (nv = 0; nv < NV; nv++) {
+            double dU;
+            if (dir == 0) dU = dims == 1 ? 0.0 : (dims == 2 ? 0.0 + p->rhs_s[1][nv][c]
+                                                            : 0.0 + p->rhs_s[1][nv][c] + p->rhs_s[2][nv][c]);
+            else if (dir == 1) dU = dims == 2 ? p->rhs_s[0][nv][c] + 0.0
+                                              : p->rhs_s[0][nv][c] + 0.0 + p->rhs_s[2][nv][c];
+            else dU = p->rhs_s[0][nv][c] + p->rhs_s[1][nv][c];
+            w.up[i][nv] = p->up_s[dir][nv][c] + dU;
+            w.um[i][nv] = p->um_s[dir][nv][c] + dU;
+          }
+        }
+        if (ct)
+          for (i = nbeg - 2; i <= nend + 1; i++) {
+            if (i >= nbeg - 1) w.up[i][r.bn] = w.bn[i];
+            if (i + 1 <= nend + 1) w.um[i + 1][r.bn] = w.bn[i];
+          }
+        for (i = nbeg - 1; i <= nend + 1; i++) {
+          unsigned char fm = 0, fp = 0;
+          cons_to_prim(w.um[i], w.vm[i], gmm1, &fm);
+          cons_to_prim(w.up[i], w.vp[i], gmm1, &fp);
+        }
+      }
+      /* Riemann problems on interfaces nbeg-1 .. nend */
+      for (i = nbeg - 1; i <= nend; i++) {
+        double m;
+        if (p->c.solver == OC_HLL)
+          hll_solver(w.vp[i], w.up[i], w.vm[i + 1], w.um[i + 1], p->c.gamma, &r, &w.ifc[i], &m);
+        else if (p->c.solver == OC_ROE)
+          roe_solver(w.vp[i], w.up[i], w.vm[i + 1], w.um[i + 1], p->c.gamma, c3, &r, &w.ifc[i], &m);
+        else
+          hlld_solver(w.vp[i], w.up[i], w.vm[i + 1], w.um[i + 1], p->c.gamma, &r, &w.ifc[i], &m);
+      }
+      /* CT_StoreUpwindEMF, ct_emf.c:104-207 */
+      if (ct)
+        for (i = nbeg - 1; i <= nend; i++) {
+          size_t c;
+          const double *F = w.ifc[i].f;
+          ijk[dir] = i;
+          c = CI(p, ijk[2], ijk[1], ijk[0]);
+          if (dir == 0) {
+            p->eface[EZI][c] = -F[BX2];
+            if (dims == 3) p->eface[EYI][c] = F[BX3];
+          } else if (dir == 1) {
+            p->eface[EZJ][c] = F[BX1];
+            if (dims == 3) p->eface[EXJ][c] = -F[BX3];
+          } else {
+            p->eface[EYK][c] = -F[BX1];
+            p->eface[EXK][c] = F[BX2];
+          }
+          p->sv[dir][c] = F[RHO] > 1.e-6 ? 1 : (F[RHO] < -1.e-6 ? -1 : 0);
+        }
+      /* RightHandSide with dt/2 (predictor) or dt (corrector) */
+      for (i = nbeg; i <= nend; i++) {
+        double scrh = (stage == 1 ? dt2 : dt) / dxd;
+        for (nv = 0; nv < NV; nv++) w.rhs[i][nv] = -scrh * (w.ifc[i].f[nv] - w.ifc[i - 1].f[nv]);
+        w.rhs[i][r.vn] -= scrh * (w.ifc[i].press - w.ifc[i - 1].press);
+      }
+      if (stage == 1) {
+        if (ct) { /* CTU_CT_Source */
+          const double dt2_dx = dt2 / dxd;
+          for (i = nbeg - 1; i <= nend + 1; i++) {
+            double db = dt2_dx * (w.up[i][r.bn] - w.um[i][r.bn]), scrh;
+            w.up[i][MX1] += vn[i][BX1] * db;
+            w.um[i][MX1] += vn[i][BX1] * db;
+            w.up[i][MX1 + 1] += vn[i][BX2] * db;
+            w.um[i][MX1 + 1] += vn[i][BX2] * db;
+            if (c3) {
+              w.up[i][MX1 + 2] += vn[i][BX3] * db;
+              w.um[i][MX1 + 2] += vn[i][BX3] * db;
+            }
+            w.up[i][r.bt] += vn[i][r.vt] * db;
+            w.um[i][r.bt] += vn[i][r.vt] * db;
+            if (c3) {
+              w.up[i][r.bb] += vn[i][r.vb] * db;
+              w.um[i][r.bb] += vn[i][r.vb] * db;
+            }
+            scrh = c3 ? vn[i][VX1] * vn[i][BX1] + vn[i][VX2] * vn[i][BX2] + vn[i][VX3] * vn[i][BX3]
+                      : vn[i][VX1] * vn[i][BX1] + vn[i][VX2] * vn[i][BX2];
+            w.up[i][ENG] += scrh * db;
+            w.um[i][ENG] += scrh * db;
+          }
+        }
+        for (i = nbeg - 1; i <= nend + 1; i++) {
+          size_t c;
+          ijk[dir] = i;
+          c = CI(p, ijk[2], ijk[1], ijk[0]);
+          for (nv = 0; nv < NV; nv++) {
+            p->up_s[dir][nv][c] = w.up[i][nv];
+            p->um_s[dir][nv][c] = w.um[i][nv];
+            if (i >= nbeg && i <= nend) p->rhs_s[dir][nv][c] = w.rhs[i][nv];
+          }
+        }
+      } else {
+        for (i = nbeg; i <= nend; i++) {
+          size_t c;
+          ijk[dir] = i;
+          c = CI(p, ijk[2], ijk[1], ijk[0]);
+          for (nv = 0; nv < NV; nv++) p->uc[nv][c] += w.rhs[i][nv];
+        }
+      }
+      for (i = nbeg; i <= nend; i++) invdt = MAX(invdt, w.ifc[i].cmax * inv_dl);
+    }
+    pencil_free(&w);
+    free(vn);
+  }
+  *inv_dt = invdt;
+}
+
+/* CT_ComputeEMF for ARITHMETIC and UCT_CONTACT (ct_emf.c:210-291,
+   ct_emf_average.c:13-164); CT_ComputeCenterEMF (ct_emf.c:348-388). */
+static void ctu_compute_emf(oc_problem *p, int stage) {
+  const int dims = p->c.dims, uct = p->c.emf == OC_UCT_CONTACT;
+  const double w = uct ? 1.0 : 0.25;
+  const int ib = p->emf_lo[0], ie = p->emf_hi[0], jb = p->emf_lo[1], je = p->emf_hi[1];
+  const int kb = dims == 3 ? p->emf_lo[2] : 0, ke = dims == 3 ? p->emf_hi[2] : 0;
+  const int KO = dims == 3;
+  double *ezi = p->eface[EZI], *ezj = p->eface[EZJ], *eyi = p->eface[EYI], *eyk = p->eface[EYK];
+  double *exj = p->eface[EXJ], *exk = p->eface[EXK];
+  double *Ex1 = p->ecc[0], *Ex2 = p->ecc[1], *Ex3 = p->ecc[2];
+  int i, j, k;
+  if (uct) {
+    size_t c;
+    for (c = 0; c < p->ncell; c++) {
+      double vx1 = p->vc[VX1][c], vx2 = p->vc[VX2][c], vx3 = p->vc[VX3][c];
+      double Bx1 = p->vc[BX1][c], Bx2 = p->vc[BX2][c], Bx3 = p->vc[BX3][c];
+      Ex1[c] = (vx3 * Bx2 - vx2 * Bx3);
+      Ex2[c] = (vx1 * Bx3 - vx3 * Bx1);
+      Ex3[c] = (vx2 * Bx1 - vx1 * Bx2);
+    }
+  }
+#define E3(a, kk, jj, ii) (a[CI(p, kk, jj, ii)])
+  for (k = kb; k <= ke; k++)
+    for (j = jb; j <= je; j++)
+      for (i = ib; i <= ie; i++) {
+        if (dims == 3) {
+          E3(p->ex, k, j, i) = w * (E3(exk, k, j, i) + E3(exk, k, j + 1, i) + E3(exj, k, j, i) + E3(exj, k + 1, j, i));
+          E3(p->ey, k, j, i) = w * (E3(eyi, k, j, i) + E3(eyi, k + 1, j, i) + E3(eyk, k, j, i) + E3(eyk, k, j, i + 1));
+        }
+        E3(p->ez, k, j, i) = w * (E3(ezi, k, j, i) + E3(ezi, k, j + 1, i) + E3(ezj, k, j, i) + E3(ezj, k, j, i + 1));
+      }
+  if (uct && stage == 2) { /* CT_EMF_IntegrateToCorner */
+#define DEX_DYP(kk, jj, ii) (E3(exj, kk, jj, ii) - E3(Ex1, kk, jj, ii))
+#define DEX_DZP(kk, jj, ii) (E3(exk, kk, jj, ii) - E3(Ex1, kk, jj, ii))
+#define DEY_DXP(kk, jj, ii) (E3(eyi, kk, jj, ii) - E3(Ex2, kk, jj, ii))
+#define DEY_DZP(kk, jj, ii) (E3(eyk, kk, jj, ii) - E3(Ex2, kk, jj, ii))
+#define DEZ_DXP(kk, jj, ii) (E3(ezi, kk, jj, ii) - E3(Ex3, kk, jj, ii))
+#define DEZ_DYP(kk, jj, ii) (E3(ezj, kk, jj, ii) - E3(Ex3, kk, jj, ii))
+#define DEX_DYM(kk, jj, ii) (E3(Ex1, kk, jj, ii) - E3(exj, kk, jj - 1, ii))
+#define DEX_DZM(kk, jj, ii) (E3(Ex1, kk, jj, ii) - E3(exk, kk - 1, jj, ii))
+#define DEY_DXM(kk, jj, ii) (E3(Ex2, kk, jj, ii) - E3(eyi, kk, jj, ii - 1))
+#define DEY_DZM(kk, jj, ii) (E3(Ex2, kk, jj, ii) - E3(eyk, kk - 1, jj, ii))
+#define DEZ_DXM(kk, jj, ii) (E3(Ex3, kk, jj, ii) - E3(ezi, kk, jj, ii - 1))
+#define DEZ_DYM(kk, jj, ii) (E3(Ex3, kk, jj, ii) - E3(ezj, kk, jj - 1, ii))
+    for (k = kb; k <= ke + KO; k++)
+      for (j = jb; j <= je + 1; j++)
+        for (i = ib; i <= ie + 1; i++) {
+          int sx = p->sv[0][CI(p, k, j, i)], sy = p->sv[1][CI(p, k, j, i)];
+          int sz = dims == 3 ? p->sv[2][CI(p, k, j, i)] : 0;
+          int iu = sx > 0 ? i : i + 1, ju = sy > 0 ? j : j + 1, ku = sz > 0 ? k : k + 1;
+          if (sx == 0) {
+            E3(p->ez, k, j, i) += 0.5 * (DEZ_DYP(k, j, i) + DEZ_DYP(k, j, i + 1));
+            E3(p->ez, k, j - 1, i) -= 0.5 * (DEZ_DYM(k, j, i) + DEZ_DYM(k, j, i + 1));
+            if (dims == 3) {
+              E3(p->ey, k, j, i) += 0.5 * (DEY_DZP(k, j, i) + DEY_DZP(k, j, i + 1));
+              E3(p->ey, k - 1, j, i) -= 0.5 * (DEY_DZM(k, j, i) + DEY_DZM(k, j, i + 1));
+            }
+          } else {
+            E3(p->ez, k, j, i) += DEZ_DYP(k, j, iu);
+            E3(p->ez, k, j - 1, i) -= DEZ_DYM(k, j, iu);
+            if (dims == 3) {
+              E3(p->ey, k, j, i) += DEY_DZP(k, j, iu);
+              E3(p->ey, k - 1, j, i) -= DEY_DZM(k, j, iu);
+            }
+          }
+          if (sy == 0) {
+            E3(p->ez, k, j, i) += 0.5 * (DEZ_DXP(k, j, i) + DEZ_DXP(k, j + 1, i));
+            E3(p->ez, k, j, i - 1) -= 0.5 * (DEZ_DXM(k, j, i) + DEZ_DXM(k, j + 1, i));
+            if (dims == 3) {
+              E3(p->ex, k, j, i) += 0.5 * (DEX_DZP(k, j, i) + DEX_DZP(k, j + 1, i));
+              E3(p->ex, k - 1, j, i) -= 0.5 * (DEX_DZM(k, j, i) + DEX_DZM(k, j + 1, i));
+            }
+          } else {
+            E3(p->ez, k, j, i) += DEZ_DXP(k, ju, i);
+            E3(p->ez, k, j, i - 1) -= DEZ_DXM(k, ju, i);
+            if (dims == 3) {
+              E3(p->ex, k, j, i) += DEX_DZP(k, ju, i);
+              E3(p->ex, k - 1, j, i) -= DEX_DZM(k, ju, i);
+            }
+          }
+          if (dims == 3) {
+            if (sz == 0) {
+              E3(p->ex, k, j, i) += 0.5 * (DEX_DYP(k, j, i) + DEX_DYP(k + 1, j, i));
+              E3(p->ex, k, j - 1, i) -= 0.5 * (DEX_DYM(k, j, i) + DEX_DYM(k + 1, j, i));
+              E3(p->ey, k, j, i) += 0.5 * (DEY_DXP(k, j, i) + DEY_DXP(k + 1, j, i));
+              E3(p->ey, k, j, i - 1) -= 0.5 * (DEY_DXM(k, j, i) + DEY_DXM(k + 1, j, i));
+            } else {
+              E3(p->ex, k, j, i) += DEX_DYP(ku, j, i);
+              E3(p->ex, k, j - 1, i) -= DEX_DYM(ku, j, i);
+              E3(p->ey, k, j, i) += DEY_DXP(ku, j, i);
+              E3(p->ey, k, j, i - 1) -= DEY_DXM(ku, j, i);
+            }
+          }
+        }
+#undef DEX_DYP
+#undef DEX_DZP
+#undef DEY_DXP
+#undef DEY_DZP
+#undef DEZ_DXP
+#undef DEZ_DYP
+#undef DEX_DYM
+#undef DEX_DZM
+#undef DEY_DXM
+#undef DEY_DZM
+#undef DEZ_DXM
+#undef DEZ_DYM
+  }
+  if (uct)
+    for (k = kb; k <= ke; k++)
+      for (j = jb; j <= je; j++)
+        for (i = ib; i <= ie; i++) {
+          if (dims == 3) {
+            E3(p->ex, k, j, i) *= 0.25;
+            E3(p->ey, k, j, i) *= 0.25;
+          }
+          E3(p->ez, k, j, i) *= 0.25;
+        }
+#undef E3
+}
+
+/* CT_Update over the emf ranges (ct_update.c:29-220): Vs = base + dt curl E */
+static void ct_update_ranges(oc_problem *p, double *const base[3], double dt) {
+  const int dims = p->c.dims;
+  const int KO = dims == 3;
+  const int kb = dims == 3 ? p->emf_lo[2] : 0, ke = dims == 3 ? p->emf_hi[2] : 0;
+  const int jb = p->emf_lo[1], je = p->emf_hi[1], ib = p->emf_lo[0], ie = p->emf_hi[0];
+  const double dx1 = p->c.dx[0], dx2 = p->c.dx[1], dx3 = p->c.dx[2];
+  int i, j, k;
+  for (k = kb + KO; k <= ke; k++)
+    for (j = jb + 1; j <= je; j++)
+      for (i = ib; i <= ie; i++) {
+        double rhs_x;
+        if (dims == 2)
+          rhs_x = 0.0 - dt / dx2 * (p->ez[CI(p, k, j, i)] - p->ez[CI(p, k, j - 1, i)]);
+        else
+          rhs_x = 0.0 - dt / dx2 * (p->ez[CI(p, k, j, i)] - p->ez[CI(p, k, j - 1, i)]) +
+                  dt / dx3 * (p->ey[CI(p, k, j, i)] - p->ey[CI(p, k - 1, j, i)]);
+        p->bs[0][FI(p, 0, k, j, i)] = base[0][FI(p, 0, k, j, i)] + rhs_x;
+      }
+  for (k = kb + KO; k <= ke; k++)
+    for (j = jb; j <= je; j++)
+      for (i = ib + 1; i <= ie; i++) {
+        double rhs_y;
+        if (dims == 2)
+          rhs_y = dt / dx1 * (p->ez[CI(p, k, j, i)] - p->ez[CI(p, k, j, i - 1)]);
+        else
+          rhs_y = dt / dx1 * (p->ez[CI(p, k, j, i)] - p->ez[CI(p, k, j, i - 1)]) -
+                  dt / dx3 * (p->ex[CI(p, k, j, i)] - p->ex[CI(p, k - 1, j, i)]);
+        p->bs[1][FI(p, 1, k, j, i)] = base[1][FI(p, 1, k, j, i)] + rhs_y;
+      }
+  if (dims == 3)
+    for (k = kb; k <= ke; k++)
+      for (j = jb + 1; j <= je; j++)
+        for (i = ib + 1; i <= ie; i++) {
+          double rhs_z = -dt / dx1 * (p->ey[CI(p, k, j, i)] - p->ey[CI(p, k, j, i - 1)]) +
+                         dt / dx2 * (p->ex[CI(p, k, j, i)] - p->ex[CI(p, k, j - 1, i)]);
+          p->bs[2][FI(p, 2, k, j, i)] = base[2][FI(p, 2, k, j, i)] + rhs_z;
+        }
+}
+
+/* CT_AverageMagneticField into an arbitrary conserved array (domain + 1) */
+static void ct_average_into(oc_problem *p, double *const U[NV]) {
+  const int dims = p->c.dims;
+  int ko = dims == 3, d, i, j, k;
+  for (k = p->beg[2] - ko; k <= p->end[2] + ko; k++)
+    for (j = p->beg[1] - 1; j <= p->end[1] + 1; j++)
+      for (i = p->beg[0] - 1; i <= p->end[0] + 1; i++) {
+        size_t c = CI(p, k, j, i);
+        for (d = 0; d < dims; d++) {
+          int o[3] = {0, 0, 0};
+          o[d] = 1;
+          U[BX1 + d][c] = 0.5 * (p->bs[d][FI(p, d, k, j, i)] + p->bs[d][FI(p, d, k - o[2], j - o[1], i - o[0])]);
+        }
+      }
+}
+
+/* AdvanceStep for CTU, ctu_step.c:140-727 (no parabolic terms) */
+static int oc_advance_ctu(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
+                          int64_t *nfail) {
+  const double gmm1 = p->c.gamma - 1.0;
+  const int dims = p->c.dims, ct = p->c.ct;
+  double inv_dt = 0.0;
+  int i, j, k, nv, d, lo[3], hi[3];
+  size_t c;
+
+  p->nfail = 0;
+  p->max_mach = 0.0;
+  p->roe_bad = 0;
+  memset(p->flag, 0, p->ncell);
+  boundary(p);
+  if (ct)
+    for (d = 0; d < dims; d++) memcpy(p->bs0[d], p->bs[d], p->nface[d] * sizeof(double));
+  for (c = 0; c < p->ncell; c++) { /* PrimToCons3D over the whole grid */
+    double v[NV], u[NV];
+    for (nv = 0; nv < NV; nv++) v[nv] = p->vc[nv][c];
+    prim_to_cons(v, u, gmm1);
+    for (nv = 0; nv < NV; nv++) p->uc[nv][c] = u[nv];
+  }
+  /* predictor */
+  for (d = 0; d < dims; d++) ctu_sweep(p, d, dt, 1, &inv_dt);
+  for (d = 0; d < 3; d++) {
+    int e = (ct && d < dims) ? 1 : 0;
+    lo[d] = p->beg[d] - e;
+    hi[d] = p->end[d] + e;
+  }
+  for (k = lo[2]; k <= hi[2]; k++)
+    for (j = lo[1]; j <= hi[1]; j++)
+      for (i = lo[0]; i <= hi[0]; i++) {
+        c = CI(p, k, j, i);
+        for (nv = 0; nv < NV; nv++) {
+          double dU = dims == 1 ? p->rhs_s[0][nv][c]
+                    : (dims == 2 ? p->rhs_s[0][nv][c] + p->rhs_s[1][nv][c]
+                                 : p->rhs_s[0][nv][c] + p->rhs_s[1][nv][c] + p->rhs_s[2][nv][c]);
+          p->uh[nv][c] = p->uc[nv][c] + dU;
+        }
+      }
+  if (ct) {
+    ctu_compute_emf(p, 1);
+    ct_update_ranges(p, p->bs, 0.5 * dt);
+    ct_average_into(p, p->uh);
+  }
+  for (k = lo[2]; k <= hi[2]; k++)
+    for (j = lo[1]; j <= hi[1]; j++)
+      for (i = lo[0]; i <= hi[0]; i++) {
+        double u[NV], v[NV];
+        c = CI(p, k, j, i);
+        for (nv = 0; nv < NV; nv++) u[nv] = p->uh[nv][c];
+        cons_to_prim(u, v, gmm1, &p->flag[c]);
+        for (nv = 0; nv < NV; nv++) { p->uh[nv][c] = u[nv]; p->vc[nv][c] = v[nv]; }
+      }
+  /* corrector */
+  for (d = 0; d < dims; d++) ctu_sweep(p, d, dt, 2, &inv_dt);
+  if (ct) {
+    ctu_compute_emf(p, 2);
+    ct_update_ranges(p, p->bs0, dt);
+    ct_average(p);
+  }
+  cons_to_prim_3d(p);
+  if (inv_dt_hyp) *inv_dt_hyp = inv_dt;
+  if (max_mach) *max_mach = p->max_mach;
+  if (nfail) *nfail = p->nfail;
+  return p->roe_bad ? 1 : 0;
+}
+
 /* AdvanceStep, Src/Time_Stepping/rk_step.c:27-254 */
 int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
                int64_t *nfail) {
@@ -1163,6 +1635,8 @@ int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
   double inv_dt = 0.0, inv_dt_1d = 0.0;
   int i, j, k, nv, d;
   size_t c;
+
+  if (p->c.stepping == OC_HANCOCK) return oc_advance_ctu(p, dt, inv_dt_hyp, max_mach, nfail);
 
   p->nfail = 0;
   p->max_mach = 0.0;
@@ -1255,6 +1729,11 @@ oc_problem *oc_create(const oc_config *cfg) {
   for (d = 0; d < 3; d++)
     if (cfg->bc[d] != OC_PERIODIC && cfg->bc[d] != OC_OUTFLOW) { free(p); return NULL; }
   p->ng = cfg->recon == OC_PARABOLIC ? 3 : 2; /* Src/get_nghost.c:28-104 */
+  if (cfg->stepping == OC_HANCOCK) {
+    if (cfg->recon != OC_LINEAR) { free(p); return NULL; } /* hancock.c:64-67 */
+    if (cfg->ct && cfg->emf != OC_ARITHMETIC && cfg->emf != OC_UCT_CONTACT) { free(p); return NULL; }
+    if (cfg->ct) p->ng++;                                    /* get_nghost.c:84-90 */
+  }
   for (d = 0; d < 3; d++) {
     int active = d < cfg->dims;
     p->nt[d] = active ? cfg->nx[d] + 2 * p->ng : 1;
@@ -1284,6 +1763,20 @@ oc_problem *oc_create(const oc_config *cfg) {
   p->ez = calloc(p->ncell, sizeof(double));
   p->cdt = calloc(p->ncell, sizeof(double));
   p->flag = calloc(p->ncell, 1);
+  if (cfg->stepping == OC_HANCOCK) {
+    for (d = 0; d < 3; d++)
+      for (nv = 0; nv < NV; nv++) {
+        p->up_s[d][nv] = calloc(p->ncell, sizeof(double));
+        p->um_s[d][nv] = calloc(p->ncell, sizeof(double));
+        p->rhs_s[d][nv] = calloc(p->ncell, sizeof(double));
+      }
+    for (nv = 0; nv < NV; nv++) p->uh[nv] = calloc(p->ncell, sizeof(double));
+    for (d = 0; d < 6; d++) p->eface[d] = calloc(p->ncell, sizeof(double));
+    for (d = 0; d < 3; d++) {
+      p->sv[d] = calloc(p->ncell, 1);
+      p->ecc[d] = calloc(p->ncell, sizeof(double));
+    }
+  }
 #ifdef _OPENMP
   if (cfg->nthreads > 0) omp_set_num_threads(cfg->nthreads);
 #endif
@@ -1294,6 +1787,11 @@ void oc_destroy(oc_problem *p) {
   int d, nv, c;
   if (!p) return;
   for (nv = 0; nv < NV; nv++) { free(p->vc[nv]); free(p->uc[nv]); free(p->u0[nv]); }
+  for (d = 0; d < 3; d++)
+    for (nv = 0; nv < NV; nv++) { free(p->up_s[d][nv]); free(p->um_s[d][nv]); free(p->rhs_s[d][nv]); }
+  for (nv = 0; nv < NV; nv++) free(p->uh[nv]);
+  for (d = 0; d < 6; d++) free(p->eface[d]);
+  for (d = 0; d < 3; d++) { free(p->sv[d]); free(p->ecc[d]); }
   for (d = 0; d < 3; d++) {
     free(p->bs[d]); free(p->bs0[d]); free(p->sl[d]); free(p->sr[d]);
     for (c = 0; c < 3; c++) free(p->dv[d][c]);

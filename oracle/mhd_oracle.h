@@ -26,7 +26,8 @@ enum { OC_RHO = 0, OC_VX1, OC_VX2, OC_VX3, OC_BX1, OC_BX2, OC_BX3, OC_PRS, OC_NV
 enum { OC_LINEAR = 0, OC_PARABOLIC = 1 };
 enum { OC_FLAT_LIM = 0, OC_MINMOD_LIM, OC_VANLEER_LIM, OC_MC_LIM, OC_DEFAULT_LIM };
 enum { OC_HLL = 0, OC_HLLD = 1, OC_ROE = 2 };
-enum { OC_RK2 = 2, OC_RK3 = 3 };
+enum { OC_RK2 = 2, OC_RK3 = 3, OC_HANCOCK = 4 }; /* HANCOCK: CTU with the primitive Hancock predictor */
+enum { OC_ARITHMETIC = 1, OC_UCT_CONTACT = 3, OC_UCT_HLL = 4 }; /* CT_EMF_AVERAGE */
 enum { OC_PERIODIC = 0, OC_OUTFLOW = 1 };
 
 typedef struct {
@@ -36,9 +37,10 @@ typedef struct {
   double dx[3];        /* uniform spacing */
   double gamma;
   int recon, limiter, solver, stepping;
-  int ct;              /* 1: constrained transport, UCT_HLL average */
+  int ct;              /* 1: constrained transport (EMF average in emf) */
   int bc[3];           /* boundary type per dim (same on both sides) */
   int nthreads;        /* OpenMP threads (0: runtime default) */
+  int emf;             /* CT_EMF_AVERAGE (0 = UCT_HLL) */
 } oc_config;
 
 typedef struct oc_problem oc_problem;

@@ -19,15 +19,16 @@ NVAR = 8
 RECON = {"LINEAR": 0, "PARABOLIC": 1}
 LIMITER = {"FLAT_LIM": 0, "MINMOD_LIM": 1, "VANLEER_LIM": 2, "MC_LIM": 3, "DEFAULT": 4}
 SOLVER = {"hll": 0, "hlld": 1, "roe": 2}
-STEPPING = {"RK2": 2, "RK3": 3}
+STEPPING = {"RK2": 2, "RK3": 3, "HANCOCK": 4}
 BC = {"periodic": 0, "outflow": 1}
+EMF = {"ARITHMETIC": 1, "UCT_CONTACT": 3, "UCT_HLL": 4}
 
 
 class OcConfig(C.Structure):
     _fields_ = [("dims", C.c_int), ("components", C.c_int), ("nx", C.c_int * 3),
                 ("dx", C.c_double * 3), ("gamma", C.c_double), ("recon", C.c_int),
                 ("limiter", C.c_int), ("solver", C.c_int), ("stepping", C.c_int),
-                ("ct", C.c_int), ("bc", C.c_int * 3), ("nthreads", C.c_int)]
+                ("ct", C.c_int), ("bc", C.c_int * 3), ("nthreads", C.c_int), ("emf", C.c_int)]
 
 
 _lib = None
@@ -84,6 +85,7 @@ class Oracle:
         c.stepping = STEPPING[spec["stepping"]]
         c.ct = int(bool(spec["ct"]))
         c.nthreads = nthreads
+        c.emf = EMF[spec.get("emf", "UCT_HLL")]
         self.h = lib().oc_create(C.byref(c))
         if not self.h:
             raise ValueError("oracle rejected the configuration")

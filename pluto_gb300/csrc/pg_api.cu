@@ -44,11 +44,22 @@ int validate_config(const pg_config* c) {
   if (c->limiter < PG_FLAT_LIM || c->limiter > PG_DEFAULT_LIM) return fail(PG_ERR_INVALID, "unsupported limiter");
   if (c->riemann != PG_HLL && c->riemann != PG_HLLD && c->riemann != PG_ROE)
     return fail(PG_ERR_INVALID, "unsupported Riemann solver");
-  if (c->time_stepping != PG_RK2 && c->time_stepping != PG_RK3)
+  if (c->time_stepping != PG_RK2 && c->time_stepping != PG_RK3 && c->time_stepping != PG_HANCOCK)
     return fail(PG_ERR_INVALID, "unsupported time stepping");
+  if (c->time_stepping == PG_HANCOCK) {
+    if (c->reconstruction != PG_LINEAR)  // Src/States/hancock.c:64-67
+      return fail(PG_ERR_INVALID, "the MUSCL-Hancock predictor needs linear reconstruction");
+    if (c->precision != PG_FP64 && c->precision != PG_FP64_TANGENT)
+      return fail(PG_ERR_INVALID, "CTU runs on the FP64 path");
+  }
   if (c->divb == PG_CONSTRAINED_TRANSPORT) {
     if (c->dims < 2) return fail(PG_ERR_INVALID, "constrained transport needs dims >= 2");
-    if (c->emf_average != PG_UCT_HLL) return fail(PG_ERR_INVALID, "only the UCT_HLL emf average is supported");
+    if (c->time_stepping == PG_HANCOCK) {  // Src/MHD/CT/ct_emf.c:196-199
+      if (c->emf_average != PG_ARITHMETIC && c->emf_average != PG_UCT_CONTACT)
+        return fail(PG_ERR_INVALID, "CTU takes the ARITHMETIC or UCT_CONTACT emf average");
+    } else if (c->emf_average != PG_UCT_HLL) {
+      return fail(PG_ERR_INVALID, "RK time stepping takes the UCT_HLL emf average");
+    }
 
   } else if (c->divb != PG_DIVB_NONE) {
     return fail(PG_ERR_INVALID, "unsupported divergence control");
@@ -62,6 +73,8 @@ int validate_config(const pg_config* c) {
 void init_geom(Solver* S) {
   const pg_config* cfg = &S->cfg;
   S->ng = cfg->reconstruction == PG_PARABOLIC ? 3 : 2;  // Src/get_nghost.c:28-104
+  // CTU with constrained transport keeps one more ghost layer (get_nghost.c:84-90)
+  if (cfg->time_stepping == PG_HANCOCK && cfg->divb == PG_CONSTRAINED_TRANSPORT) S->ng++;
   Geom& g = S->g;
   g.dims = cfg->dims;
   for (int d = 0; d < 3; d++) {

@@ -64,6 +64,21 @@ int fp64_alloc(Solver* S) {
       }
     }
   }
+  if (S->cfg.time_stepping == PG_HANCOCK) {
+    for (int d = 0; d < S->g.dims; d++)
+      for (int nv = 0; nv < 8; nv++)
+        if (alloc(&S->Upd[d][nv]) || alloc(&S->Umd[d][nv]) || alloc(&S->Rhd[d][nv])) return PG_ERR_NOMEM;
+    for (int nv = 0; nv < 8; nv++)
+      if (alloc(&S->Uh[nv])) return PG_ERR_NOMEM;
+    if (ct) {
+      for (int q = 0; q < 6; q++)
+        if (alloc(&S->EF[q])) return PG_ERR_NOMEM;
+      for (int d = 0; d < S->g.dims; d++) {
+        if (cudaMalloc(&S->SV[d], n) != cudaSuccess) return PG_ERR_NOMEM;
+        cudaMemset(S->SV[d], 0, n);
+      }
+    }
+  }
   if (cudaMalloc(&S->flag, n) != cudaSuccess) return PG_ERR_NOMEM;
   cudaMemset(S->flag, 0, n);
   return PG_OK;
@@ -84,7 +99,15 @@ void fp64_free(Solver* S) {
     f(S->Bs[d]); f(S->Bs0[d]); f(S->SL[d]); f(S->SR[d]); f(S->E[d]); f(S->Bm1[d]);
     S->Bs[d] = S->Bs0[d] = S->SL[d] = S->SR[d] = S->E[d] = S->Bm1[d] = nullptr;
     for (int c = 0; c < 3; c++) { f(S->DV[d][c]); S->DV[d][c] = nullptr; }
+    for (int nv = 0; nv < 8; nv++) {
+      f(S->Upd[d][nv]); f(S->Umd[d][nv]); f(S->Rhd[d][nv]);
+      S->Upd[d][nv] = S->Umd[d][nv] = S->Rhd[d][nv] = nullptr;
+    }
+    f(S->SV[d]);
+    S->SV[d] = nullptr;
   }
+  for (int nv = 0; nv < 8; nv++) { f(S->Uh[nv]); S->Uh[nv] = nullptr; }
+  for (int q = 0; q < 6; q++) { f(S->EF[q]); S->EF[q] = nullptr; }
 }
 
 int fp64_enqueue_step(Solver* S) { return fp64_enqueue_step_t<double>(S); }

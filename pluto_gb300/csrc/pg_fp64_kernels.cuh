@@ -31,6 +31,12 @@ struct F64A {
   T* DV[3][3];
   T* E[3];
   T* Bm1[3];  // face -1 layers: Bm1[0][k][j], Bm1[1][k][i], Bm1[2][j][i]
+  T* Upd[3][8];
+  T* Umd[3][8];
+  T* Rhd[3][8];
+  T* Uh[8];
+  T* EF[6];
+  signed char* SV[3];
   T* CDT;
   unsigned char* flag;
   DevScalars* sc;
@@ -39,6 +45,8 @@ struct F64A {
   int device_dt;
   int bc[3];
   int ct_outflow;   // constrained transport with an outflow axis: per-axis boundary passes
+  int div_dims;     // RK: invDt_hyp /= DIMENSIONS (update_stage.c:311); CTU: no
+  int emf_avg, c3;
 };
 
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
@@ -421,7 +429,7 @@ template <class T>
 __global__ void k_end_step(F64A<T> a) {
   DevScalars* sc = a.sc;
   double inv = __longlong_as_double((long long)sc->inv_dt_bits);
-  if (a.g.dims > 1) inv /= (double)a.g.dims;  // update_stage.c:311
+  if (a.div_dims && a.g.dims > 1) inv /= (double)a.g.dims;  // update_stage.c:311
   sc->inv_dt_bits = (unsigned long long)__double_as_longlong(inv);
   if (!(inv == inv) || inv > 1e300) sc->status |= 1;  // NaN / inf guard
   if (a.device_dt) {
@@ -480,6 +488,18 @@ static F64A<T> make_args(Solver* S) {
     a.Bm1[d] = (T*)S->Bm1[d];
     a.bc[d] = S->cfg.bc[d];
   }
+  for (int d = 0; d < 3; d++)
+    for (int nv = 0; nv < 8; nv++) {
+      a.Upd[d][nv] = (T*)S->Upd[d][nv];
+      a.Umd[d][nv] = (T*)S->Umd[d][nv];
+      a.Rhd[d][nv] = (T*)S->Rhd[d][nv];
+    }
+  for (int nv = 0; nv < 8; nv++) a.Uh[nv] = (T*)S->Uh[nv];
+  for (int q = 0; q < 6; q++) a.EF[q] = (T*)S->EF[q];
+  for (int d = 0; d < 3; d++) a.SV[d] = S->SV[d];
+  a.div_dims = S->cfg.time_stepping != PG_HANCOCK;
+  a.emf_avg = S->cfg.emf_average;
+  a.c3 = S->cfg.components == 3;
   a.ct_outflow = 0;
   if (a.ct)
     for (int d = 0; d < S->g.dims; d++) a.ct_outflow |= S->cfg.bc[d] == PG_OUTFLOW;
@@ -602,10 +622,17 @@ static void enqueue_rk(Solver* S, const F64A<T>& a) {
 }
 
 
+}  // namespace pg
+
+#include "pg_ctu.cuh"
+
+namespace pg {
+
 template <class T>
 int fp64_enqueue_step_t(Solver* S) {
   F64A<T> a = make_args<T>(S);
-  if (S->cfg.time_stepping == PG_RK3) enqueue_rk<T, 3>(S, a);
+  if (S->cfg.time_stepping == PG_HANCOCK) enqueue_ctu<T>(S, a);
+  else if (S->cfg.time_stepping == PG_RK3) enqueue_rk<T, 3>(S, a);
   else enqueue_rk<T, 2>(S, a);
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ERR_CUDA;
 }

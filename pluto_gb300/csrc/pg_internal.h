@@ -114,6 +114,13 @@ struct Solver {
   double* DV[3][3] = {};// velocity slopes DV[dir][comp]
   double* E[3] = {};    // edge EMFs
   double* Bm1[3] = {};  // face -1 layers (boundary scratch for outflow sides under CT)
+  // CTU work arrays (TIME_STEPPING HANCOCK)
+  double* Upd[3][8] = {};  // predicted conservative +/- states per direction
+  double* Umd[3][8] = {};
+  double* Rhd[3][8] = {};  // predictor right-hand sides per direction (dt/2)
+  double* Uh[8] = {};      // conservative state at the half step
+  double* EF[6] = {};      // face EMFs from the fluxes: ezi, ezj, eyi, eyk, exj, exk
+  signed char* SV[3] = {}; // sign of the mass flux per face (UCT_CONTACT)
   double* CDT = nullptr;
   unsigned char* flag = nullptr;
   // mixed path

@@ -23,7 +23,8 @@ RECON = {"LINEAR": L.PG_LINEAR, "PARABOLIC": L.PG_PARABOLIC}
 LIMITER = {"FLAT_LIM": L.PG_FLAT_LIM, "MINMOD_LIM": L.PG_MINMOD_LIM,
            "VANLEER_LIM": L.PG_VANLEER_LIM, "MC_LIM": L.PG_MC_LIM, "DEFAULT": L.PG_DEFAULT_LIM}
 RIEMANN = {"hll": L.PG_HLL, "hlld": L.PG_HLLD, "roe": L.PG_ROE}
-STEPPING = {"RK2": L.PG_RK2, "RK3": L.PG_RK3}
+STEPPING = {"RK2": L.PG_RK2, "RK3": L.PG_RK3, "HANCOCK": L.PG_HANCOCK}
+EMF = {"ARITHMETIC": L.PG_ARITHMETIC, "UCT_CONTACT": L.PG_UCT_CONTACT, "UCT_HLL": L.PG_UCT_HLL}
 BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW}
 PRECISION = {"fp64": L.PG_FP64, "mixed": L.PG_MIXED, "mixed_dw": L.PG_MIXED_DW,
              "fp64_tangent": L.PG_FP64_TANGENT}
@@ -45,7 +46,7 @@ def make_config(spec: dict, precision: str = "fp64", compute_mach: bool = False)
     c.riemann = RIEMANN[spec.get("solver", "hlld")]
     c.time_stepping = STEPPING[spec.get("stepping", "RK2")]
     c.divb = L.PG_CONSTRAINED_TRANSPORT if spec.get("ct", True) else L.PG_DIVB_NONE
-    c.emf_average = L.PG_UCT_HLL
+    c.emf_average = EMF[spec.get("emf", "UCT_HLL")]
     c.precision = PRECISION[precision]
     c.compute_mach = int(bool(compute_mach))
     c.small_density = 1e-12

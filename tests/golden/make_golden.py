@@ -48,7 +48,7 @@ def spec_of(s: br.Setup) -> dict:
     gamma = 2.0 if s.name.startswith("tube") else 5.0 / 3.0
     return dict(name=s.name, dims=s.dims, components=s.components, nx=n, dx=dx,
                 lo=list(s.lo), hi=list(s.hi), gamma=gamma, recon=s.recon,
-                limiter=s.limiter, solver=s.solver, stepping=s.stepping, ct=s.ct,
+                limiter=s.limiter, solver=s.solver, stepping=s.stepping, ct=s.ct, emf=s.emf,
                 bc=s.bc, cfl=s.cfl, first_dt=s.first_dt, steps=s.steps,
                 params=s.params)
 
@@ -70,6 +70,13 @@ def setups():
         replace(br.tube_setup(0, 256, 100), solver="roe", name="tube_roe_0_256"),
         replace(br.ot_setup("hlld", 32, 30), bc="outflow", name="ot_outflow_32"),
         replace(br.turb_setup(12, 10), bc="outflow", name="turb_outflow_12"),
+        replace(br.ot_setup("hlld", 32, 30), stepping="HANCOCK", emf="UCT_CONTACT", name="ot_ctu_uctc_32"),
+        replace(br.ot_setup("roe", 32, 30), stepping="HANCOCK", emf="ARITHMETIC", name="ot_ctu_arith_roe_32"),
+        replace(br.turb_setup(12, 10), recon="LINEAR", stepping="HANCOCK", emf="UCT_CONTACT",
+                name="turb_ctu_uctc_12"),
+        replace(br.tube_setup(1, 200, 120), stepping="HANCOCK", name="tube_ctu_1_200"),
+        replace(br.cpa_setup(32, 20), stepping="HANCOCK", emf="UCT_CONTACT", bc="outflow",
+                name="cpa_ctu_outflow_32"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

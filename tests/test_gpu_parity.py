@@ -41,7 +41,9 @@ def test_fp64_matches_reference_goldens(name):
 
 @pytest.mark.parametrize("name", ["ot_hlld_32", "blast_16", "tube_0_256", "turb_12", "blast_floor_16",
                                   "ot_roe_32", "cpa_roe_32", "blast_roe_16", "tube_roe_0_256",
-                                  "ot_outflow_32", "turb_outflow_12"])
+                                  "ot_outflow_32", "turb_outflow_12", "ot_ctu_uctc_32",
+                                  "ot_ctu_arith_roe_32", "turb_ctu_uctc_12", "tube_ctu_1_200",
+                                  "cpa_ctu_outflow_32"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
@@ -176,3 +178,43 @@ def test_nan_state_reported_not_trapped():
     with pytest.raises(PgError) as e:
         s.advance(1e-3)
     assert e.value.code == 4
+
+
+@pytest.mark.parametrize("emf,solver,bc", [("UCT_CONTACT", "hlld", "periodic"), ("ARITHMETIC", "hll", "outflow"),
+                                           ("UCT_CONTACT", "roe", "outflow")])
+def test_ctu_vs_oracle_random_3d(emf, solver, bc):
+    """CTU (primitive Hancock predictor, corner-coupled corrector) with CT on a
+    random 3D state against the oracle, bit for bit."""
+    from oracle.oracle import Oracle
+    spec, vc, bs = _random_blast(16, seed=9)
+    spec.update(stepping="HANCOCK", emf=emf, solver=solver, bc=bc, limiter="MC_LIM")
+    s = _solver(spec)
+    o = Oracle(spec, nthreads=4)
+    s.upload(vc, bs)
+    o.set_state(vc, bs)
+    s.run(4, 1e-3, 0.3)
+    o.run(4, 1e-3, 0.3)
+    a, ab = s.download()
+    b, bb = o.get_state()
+    assert np.array_equal(a, b), _errors(a, ab, b, bb)
+    for d in range(3):
+        assert np.array_equal(ab[d], bb[d])
+
+
+def test_ctu_tangent_value_part_is_the_fp64_step():
+    from pluto_gb300 import Solver
+    from pluto_gb300.adjoint import tangent_linear
+    spec, vc, bs = _random_blast(12, seed=4)
+    spec.update(stepping="HANCOCK", emf="UCT_CONTACT")
+    s = _solver(spec)
+    s.upload(vc, bs)
+    dts = [1e-3] * 3
+    for dt in dts:
+        s.advance(dt)
+    want, wb = s.download()
+    rng = np.random.default_rng(3)
+    (got, gb), _ = tangent_linear(spec, dts, vc, bs, rng.normal(size=vc.shape),
+                                  [rng.normal(size=f.shape) for f in bs])
+    assert np.array_equal(got, want)
+    for d in range(3):
+        assert np.array_equal(gb[d], wb[d])
