@@ -201,6 +201,9 @@ __global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_l
   const bool face_ok = i <= g.end[0] && lane < 31;  // interfaces beg-1+1/2 .. end+1/2
   const int nt0 = g.nt[0];
   const int c = (k * g.nt[1] + j) * nt0 + i;
+  // loaded up front so that their latency overlaps the reconstruction
+  const float bn = (CT && face_ok) ? a.Bin[0][c] : 0.f;
+  const float scrh = a.sc->dtdx[0];
   float vp[NV], vm[NV];
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
@@ -222,7 +225,6 @@ __global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_l
   for (int nv = 0; nv < NV; nv++) fl[nv] = 0.f;
   if (face_ok) {
     Iface<float> o;
-    float bn = CT ? a.Bin[0][c] : 0.f;
     solve_iface<0, CT>(a, solver, vp, vR, bn, o);
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) fl[nv] = o.f[nv];
@@ -239,7 +241,6 @@ __global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_l
   const float prm = __shfl_up_sync(0xffffffffu, pr, 1);
   const float cmm = __shfl_up_sync(0xffffffffu, cm, 1);
   if (lane >= 1 && lane <= 30 && i >= g.beg[0] && i <= g.end[0]) {
-    const float scrh = a.sc->dtdx[0];
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
       if (!((a.accmask >> nv) & 1)) continue;
@@ -282,6 +283,15 @@ __global__ void __launch_bounds__(32 * kTY, 2) k_msweep_t(MixArgs a, int solver,
   const bool face_ok = col_ok && m <= end && ty < kTY - 1;   // interfaces beg-1+1/2 .. end+1/2
   const int s = DIR == 1 ? g.nt[0] : g.nt[0] * g.nt[1];
   const int c = (DIR == 1 ? (other * g.nt[1]) * g.nt[0] + i : other * g.nt[0] + i) + m * s;
+  // the accumulated update of this zone, loaded now so that its latency
+  // overlaps the reconstruction and the Riemann problem
+  const bool upd = ty >= 1 && ty <= kTY - 2 && col_ok && m >= beg && m <= end;
+  float du[NV], cdt = 0.f;
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) du[nv] = (upd && ((a.accmask >> nv) & 1)) ? a.dU[nv][c] : 0.f;
+  if (upd && stage1) cdt = a.CDT[c];
+  const float bn = (CT && face_ok) ? a.Bin[DIR][c] : 0.f;
+  const float scrh = a.sc->dtdx[DIR];
   float vp[NV], vm[NV];
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
@@ -305,7 +315,6 @@ __global__ void __launch_bounds__(32 * kTY, 2) k_msweep_t(MixArgs a, int solver,
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) vR[nv] = svm[nv][ty + 1][tx];
     Iface<float> o;
-    float bn = CT ? a.Bin[DIR][c] : 0.f;
     solve_iface<DIR, CT>(a, solver, vp, vR, bn, o);
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) fl[nv] = o.f[nv];
@@ -321,16 +330,15 @@ __global__ void __launch_bounds__(32 * kTY, 2) k_msweep_t(MixArgs a, int solver,
   sf[NV][ty][tx] = pr;
   sf[NV + 1][ty][tx] = cm;
   __syncthreads();
-  if (ty >= 1 && ty <= kTY - 2 && col_ok && m >= beg && m <= end) {
-    const float scrh = a.sc->dtdx[DIR];
+  if (upd) {
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
       if (!((a.accmask >> nv) & 1)) continue;
       float rhs = -scrh * (fl[nv] - sf[nv][ty - 1][tx]);
       if (nv == Rot<DIR>::vn) rhs -= scrh * (pr - sf[NV][ty - 1][tx]);
-      a.dU[nv][c] += rhs;
+      a.dU[nv][c] = du[nv] + rhs;
     }
-    if (stage1) a.CDT[c] += 0.5f * (sf[NV + 1][ty - 1][tx] + cm) * a.inv_dx_f[DIR];
+    if (stage1) a.CDT[c] = cdt + 0.5f * (sf[NV + 1][ty - 1][tx] + cm) * a.inv_dx_f[DIR];
   }
 }
 
