@@ -1,10 +1,11 @@
 /* ///////////////////////////////////////////////////////////////////// */
 /*!
   \file
-  \brief GB300 replacement for PLUTO's unsplit RK AdvanceStep().
+  \brief GB300 replacement for PLUTO's unsplit AdvanceStep() (RK and CTU).
 
   Link this object instead of rk_step.o and update_stage.o (the objects the
-  setup tool lists for an unsplit RK scheme) and add -lpluto_gb300 -lcudart.
+  setup tool lists for an unsplit RK scheme; ctu_step.o for CTU) and add
+  -lpluto_gb300 -lcudart.
   It defines the same symbol PLUTO's Integrate() calls,
 
       int AdvanceStep (Data *d, Riemann_Solver *Riemann,
@@ -84,12 +85,20 @@ static void gpu_config(pg_config *c, Riemann_Solver *Riemann, Grid *grid)
   c->riemann = gpu_riemann(Riemann);
 #if TIME_STEPPING == RK3
   c->time_stepping = PG_RK3;
+#elif TIME_STEPPING == HANCOCK
+  c->time_stepping = PG_HANCOCK;
 #else
   c->time_stepping = PG_RK2;
 #endif
 #ifdef STAGGERED_MHD
   c->divb = PG_CONSTRAINED_TRANSPORT;
+  #if CT_EMF_AVERAGE == ARITHMETIC
+  c->emf_average = PG_ARITHMETIC;
+  #elif CT_EMF_AVERAGE == UCT_CONTACT
+  c->emf_average = PG_UCT_CONTACT;
+  #else
   c->emf_average = PG_UCT_HLL;
+  #endif
 #else
   c->divb = PG_DIVB_NONE;
 #endif
