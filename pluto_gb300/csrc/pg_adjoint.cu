@@ -259,55 +259,51 @@ __device__ __forceinline__ bool ct_face(const Geom& g, int fd, int i, int j, int
   int i, j, k;                                                    \
   cell_ijk(g, c, i, j, k);
 
-// lU = J_C(U)^T lambda_V (+ lUx), zero off the domain.
+// lU = J_C(U)^T lambda_V (+ lUx), zero off the domain.  One thread per
+// (zone, seeded conserved component).
 __global__ void k_adj_c2p(AdjArgs A, Tab8 Ust, Tab8 L, int add_ux) {
-  ADJ_CELL_PROLOGUE
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const Geom& g = A.f.g;
+  if (q >= g.ncell * NV) return;
+  const long long c = q / NV;
+  const int kk = (int)(q % NV);
+  int i, j, k;
+  cell_ijk(g, c, i, j, k);
   if (!in_dom(g, i, j, k)) {
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) A.b.lU[nv][c] = 0.0;
+    A.b.lU[kk][c] = 0.0;
     return;
   }
-  double lv[NV], u0[NV];
+  D1 u[NV], v[NV];
 #pragma unroll
-  for (int nv = 0; nv < NV; nv++) {
-    lv[nv] = L.p[nv][c];
-    u0[nv] = Ust.p[nv][c];
-  }
-  for (int kk = 0; kk < NV; kk++) {
-    D1 u[NV], v[NV];
+  for (int nv = 0; nv < NV; nv++) u[nv] = D1(Ust.p[nv][c]);
+  u[kk].d[0] = 1.0;
+  unsigned char fl = 0;
+  cons_to_prim(u, v, D1(A.f.gamma - 1.0), D1(A.f.small_rho), D1(A.f.small_p), &fl);
+  double s = 0.0;
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++) u[nv] = D1(u0[nv]);
-    u[kk].d[0] = 1.0;
-    unsigned char fl = 0;
-    cons_to_prim(u, v, D1(A.f.gamma - 1.0), D1(A.f.small_rho), D1(A.f.small_p), &fl);
-    double s = 0.0;
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) s += lv[nv] * v[nv].d[0];
-    A.b.lU[kk][c] = s + (add_ux ? A.b.lUx[kk][c] : 0.0);
-  }
+  for (int nv = 0; nv < NV; nv++) s += L.p[nv][c] * v[nv].d[0];
+  A.b.lU[kk][c] = s + (add_ux ? A.b.lUx[kk][c] : 0.0);
 }
 
-// lVin[dom] += J_P(V^n)^T lU0.
+// lVin[dom] += J_P(V^n)^T lU0.  One thread per (zone, seeded primitive).
 __global__ void k_adj_p2c(AdjArgs A) {
-  ADJ_CELL_PROLOGUE
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const Geom& g = A.f.g;
+  if (q >= g.ncell * NV) return;
+  const long long c = q / NV;
+  const int kk = (int)(q % NV);
+  int i, j, k;
+  cell_ijk(g, c, i, j, k);
   if (!in_dom(g, i, j, k)) return;
-  double lu[NV], v0[NV];
+  D1 v[NV], u[NV];
 #pragma unroll
-  for (int nv = 0; nv < NV; nv++) {
-    lu[nv] = A.b.lU0[nv][c];
-    v0[nv] = A.b.Vn[nv][c];
-  }
-  for (int kk = 0; kk < NV; kk++) {
-    D1 v[NV], u[NV];
+  for (int nv = 0; nv < NV; nv++) v[nv] = D1(A.b.Vn[nv][c]);
+  v[kk].d[0] = 1.0;
+  prim_to_cons(v, u, D1(A.f.gamma - 1.0));
+  double s = 0.0;
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++) v[nv] = D1(v0[nv]);
-    v[kk].d[0] = 1.0;
-    prim_to_cons(v, u, D1(A.f.gamma - 1.0));
-    double s = 0.0;
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) s += lu[nv] * u[nv].d[0];
-    A.b.lVin[kk][c] += s;
-  }
+  for (int nv = 0; nv < NV; nv++) s += A.b.lU0[nv][c] * u[nv].d[0];
+  A.b.lVin[kk][c] += s;
 }
 
 // Face average U[BX] = (B[f] + B[f-s]) / 2 on the domain, transposed.
@@ -388,10 +384,11 @@ __global__ void k_adj_ct(AdjArgs A, Tab8 lBc) {
   }
 }
 
-// One edge EMF component transposed: gathers its 40 inputs, forms the
-// gradient by 40 seeded evaluations and scatters it.
+// One edge EMF component transposed for one seeded input kk: gathers the 40
+// inputs, evaluates the derivative of the edge value along input kk and
+// scatters it.
 template <int E>
-__device__ __forceinline__ void adj_edge(const AdjArgs& A, long long c, double lam) {
+__device__ __forceinline__ void adj_edge(const AdjArgs& A, long long c, double lam, int kk) {
   if (lam == 0.0) return;
   constexpr int AX = E == 2 ? 0 : (E == 0 ? 1 : 2);
   constexpr int AY = E == 2 ? 1 : (E == 0 ? 2 : 0);
@@ -430,27 +427,27 @@ __device__ __forceinline__ void adj_edge(const AdjArgs& A, long long c, double l
     i6[4] = f.DV[AX][AX][cc];  d6[4] = &b.lDV[AX][AX][cc];
     i6[5] = f.DV[AY][AX][cc];  d6[5] = &b.lDV[AY][AX][cc];
   }
-  for (int kk = 0; kk < kEdgeIn; kk++) {
-    D1 x[kEdgeIn];
+  D1 x[kEdgeIn];
 #pragma unroll
-    for (int q = 0; q < kEdgeIn; q++) x[q] = D1(in[q]);
-    x[kk].d[0] = 1.0;
-    const double gk = lam * emf_pt(x).d[0];
-    if (gk != 0.0) atomicAdd(dst[kk], gk);
-  }
+  for (int q = 0; q < kEdgeIn; q++) x[q] = D1(in[q]);
+  x[kk].d[0] = 1.0;
+  const double gk = lam * emf_pt(x).d[0];
+  if (gk != 0.0) atomicAdd(dst[kk], gk);
 }
 
 __global__ void k_adj_emf(AdjArgs A, Box box) {
-  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= box.count()) return;
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  const int ncomp = A.f.g.dims == 3 ? 3 : 1;
+  if (q >= box.count() * kEdgeIn * ncomp) return;
+  const int kk = (int)(q % kEdgeIn);
+  const long long r = q / kEdgeIn;
+  const int e = (int)(r % ncomp);
   int i, j, k;
-  box.coords(q, i, j, k);
+  box.coords(r / ncomp, i, j, k);
   const long long c = cidx(A.f.g, k, j, i);
-  adj_edge<2>(A, c, A.b.lE[2][c]);
-  if (A.f.g.dims == 3) {
-    adj_edge<0>(A, c, A.b.lE[0][c]);
-    adj_edge<1>(A, c, A.b.lE[1][c]);
-  }
+  if (ncomp == 1 || e == 2) adj_edge<2>(A, c, A.b.lE[2][c], kk);
+  else if (e == 0) adj_edge<0>(A, c, A.b.lE[0][c], kk);
+  else adj_edge<1>(A, c, A.b.lE[1][c], kk);
 }
 
 // U[c] += -dt/dx (F[c] - F[c-s]) (and the pressure term on the normal
@@ -471,12 +468,15 @@ __global__ void k_adj_flux(AdjArgs A, Box box) {
 
 // Riemann problem at interface c+1/2 transposed: adjoint on VP[c], VM[c+s]
 // (and on the face field that replaces their normal component under CT).
+// One thread per (interface, seeded input of the 16 states); lVP / lVM are
+// zero on entry.
 template <int DIR>
 __global__ void k_adj_riemann(AdjArgs A, Box box, int solver) {
-  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= box.count()) return;
+  const long long qq = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (qq >= box.count() * 2 * NV) return;
+  const int kk = (int)(qq % (2 * NV));
   int i, j, k;
-  box.coords(q, i, j, k);
+  box.coords(qq / (2 * NV), i, j, k);
   const Geom& g = A.f.g;
   const long long c = cidx(g, k, j, i), s = g.s[DIR];
   const bool ct = A.f.ct;
@@ -502,53 +502,50 @@ __global__ void k_adj_riemann(AdjArgs A, Box box, int solver) {
     vL[BN] = bn;
     vR[BN] = bn;
   }
-  double gL[NV], gR[NV];
-  for (int kk = 0; kk < 2 * NV; kk++) {
-    double gk = 0.0;
-    if (any) {
-      D1 xL[NV], xR[NV], out[NO];
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) {
-        xL[nv] = D1(vL[nv]);
-        xR[nv] = D1(vR[nv]);
-      }
-      if (kk < NV) xL[kk].d[0] = 1.0;
-      else xR[kk - NV].d[0] = 1.0;
-      riemann_pt<D1, DIR>(solver, A.f.gamma, A.f.ncomp == 3, xL, xR, out);
-#pragma unroll
-      for (int o = 0; o < NO; o++) gk += lam[o] * out[o].d[0];
-    }
-    if (kk < NV) gL[kk] = gk;
-    else gR[kk - NV] = gk;
-  }
+  if (!any) return;
+  D1 xL[NV], xR[NV], out[NO];
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
-    A.b.lVP[nv][c] = (ct && nv == BN) ? 0.0 : gL[nv];
-    A.b.lVM[nv][c + s] = (ct && nv == BN) ? 0.0 : gR[nv];
+    xL[nv] = D1(vL[nv]);
+    xR[nv] = D1(vR[nv]);
   }
-  if (ct) A.b.lBin[DIR][c] += gL[BN] + gR[BN];
+  if (kk < NV) xL[kk].d[0] = 1.0;
+  else xR[kk - NV].d[0] = 1.0;
+  riemann_pt<D1, DIR>(solver, A.f.gamma, A.f.ncomp == 3, xL, xR, out);
+  double gk = 0.0;
+#pragma unroll
+  for (int o = 0; o < NO; o++) gk += lam[o] * out[o].d[0];
+  const int nv = kk < NV ? kk : kk - NV;
+  if (ct && nv == BN) {
+    if (gk != 0.0) atomicAdd(&A.b.lBin[DIR][c], gk);
+  } else if (kk < NV) {
+    A.b.lVP[nv][c] = gk;
+  } else {
+    A.b.lVM[nv][c + s] = gk;
+  }
 }
 
 // States of zone c (and its velocity slopes DV = vp - vm) transposed:
 // scatter into the adjoint on the stage-input primitives of its stencil.
 template <int DIR>
 __global__ void k_adj_recon(AdjArgs A, Box box) {
-  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= box.count()) return;
+  const long long qq = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (qq >= box.count() * NV) return;
   int i, j, k;
-  box.coords(q, i, j, k);
+  box.coords(qq / NV, i, j, k);
   const Geom& g = A.f.g;
   const long long c = cidx(g, k, j, i), s = g.s[DIR];
   const int recon = A.f.recon;
   const int t0 = recon == PG_LINEAR ? 1 : 0, t1 = recon == PG_LINEAR ? 3 : 4;
-  for (int nv = 0; nv < NV; nv++) {
+  {
+    const int nv = (int)(qq % NV);
     double lp = A.b.lVP[nv][c], lm = A.b.lVM[nv][c];
     if (A.f.ct && nv >= VX1 && nv < VX1 + g.dims) {
       const double ld = A.b.lDV[DIR][nv - VX1][c];
       lp += ld;
       lm -= ld;
     }
-    if (lp == 0.0 && lm == 0.0) continue;
+    if (lp == 0.0 && lm == 0.0) return;
     double w[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     for (int t = t0; t <= t1; t++) w[t] = A.f.V[nv][c + (t - 2) * s];
     for (int t = t0; t <= t1; t++) {
@@ -704,8 +701,8 @@ void rev_dir(Solver* S, const AdjArgs& A) {
     cudaMemsetAsync(A.b.lVM[nv], 0, n * sizeof(double), st);
   }
   k_adj_flux<DIR><<<grid_for(ib.count()), kT, 0, st>>>(A, ib);
-  k_adj_riemann<DIR><<<grid_for(ib.count(), 64), 64, 0, st>>>(A, ib, S->cfg.riemann);
-  k_adj_recon<DIR><<<grid_for(rb.count(), 128), 128, 0, st>>>(A, rb);
+  k_adj_riemann<DIR><<<grid_for(ib.count() * 2 * NV, 64), 64, 0, st>>>(A, ib, S->cfg.riemann);
+  k_adj_recon<DIR><<<grid_for(rb.count() * NV, 128), 128, 0, st>>>(A, rb);
 }
 
 void fwd_bound(Solver* S, const F64A<double>& f) {
@@ -760,7 +757,7 @@ void rev_stage(Solver* S, const AdjArgs& A, bool add_b0) {
         eb.lo[ax] = eb.hi[ax] = 0;
       }
     }
-    k_adj_emf<<<grid_for(eb.count(), 64), 64, 0, st>>>(A, eb);
+    k_adj_emf<<<grid_for(eb.count() * kEdgeIn * (g.dims == 3 ? 3 : 1), 64), 64, 0, st>>>(A, eb);
   }
   if (g.dims > 2) rev_dir<2>(S, A);
   if (g.dims > 1) rev_dir<1>(S, A);
@@ -950,7 +947,7 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
   const double w0 = 0.5, wc = 0.5;  // RK2 weights
   // ---- stage 2 reversed ----
   A.b = *B;
-  k_adj_c2p<<<grid_for(n), kT, 0, st>>>(A, tab(B->U2, 8), tab(B->lV, 8), 0);
+  k_adj_c2p<<<grid_for(n * NV), kT, 0, st>>>(A, tab(B->U2, 8), tab(B->lV, 8), 0);
   if (ct) {
     k_adj_avg<<<grid_for(n), kT, 0, st>>>(A, tab(B->lB, 3));
     k_adj_zero_bx<<<grid_for(n), kT, 0, st>>>(A);
@@ -965,7 +962,7 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
   for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
   // ---- stage 1 reversed ----
   A.b = *B;
-  k_adj_c2p<<<grid_for(n), kT, 0, st>>>(A, tab(B->U1, 8), tab(B->lV, 8), 1);
+  k_adj_c2p<<<grid_for(n * NV), kT, 0, st>>>(A, tab(B->U1, 8), tab(B->lV, 8), 1);
   if (ct) {
     k_adj_avg<<<grid_for(n), kT, 0, st>>>(A, tab(B->lB, 3));
     k_adj_zero_bx<<<grid_for(n), kT, 0, st>>>(A);
@@ -974,7 +971,7 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
   for (int nv = 0; nv < NV; nv++) dcopy(S->V[nv], B->Vn[nv], n, st);
   for (int d = 0; d < nb; d++) dcopy(S->Bs[d], B->Bn[d], n, st);
   rev_stage(S, A, ct);
-  k_adj_p2c<<<grid_for(n), kT, 0, st>>>(A);
+  k_adj_p2c<<<grid_for(n * NV), kT, 0, st>>>(A);
   for (int nv = 0; nv < NV; nv++) std::swap(B->lV[nv], B->lVin[nv]);
   for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
   // the solver's state is the step's start again
