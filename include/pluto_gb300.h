@@ -50,7 +50,8 @@ enum { PG_RK2 = 2, PG_RK3 = 3,                                    /* TIME_STEPPI
        PG_HANCOCK = 4 };  /* CTU (ctu_step.c) with the primitive MUSCL-Hancock predictor */
 enum { PG_DIVB_NONE = 0, PG_CONSTRAINED_TRANSPORT = 1 };          /* DIVB_CONTROL */
 enum { PG_ARITHMETIC = 1, PG_UCT_CONTACT = 3, PG_UCT_HLL = 4 };   /* CT_EMF_AVERAGE */
-enum { PG_PERIODIC = 0, PG_OUTFLOW = 1 };                         /* [Boundary] */
+enum { PG_PERIODIC = 0, PG_OUTFLOW = 1, PG_REFLECTIVE = 2,
+       PG_EQTSYMMETRIC = 3 };                                     /* [Boundary] */
 /* arithmetic: PG_FP64 bit-compatible with the reference C path;
    PG_MIXED FP32 storage and fluxes, FP64 accumulation / pressure recovery /
    face update / dt reduction; PG_MIXED_DW the same with the FP64 parts done

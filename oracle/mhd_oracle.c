@@ -671,8 +671,21 @@ static void ppm_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV],
 /* Boundary conditions, Src/boundary.c:41-303, 439-522                 */
 /* ------------------------------------------------------------------ */
 
+/* FlipSign, Src/boundary.c:318-437 (REFLECTIVE and EQTSYMMETRIC): sign of
+   variable nv (or of face component BX1+fd) mirrored across a side of axis d */
+static int flip_sign(int d, int type, int nv, int components) {
+  const int vn = VX1 + d, bn = BX1 + d;
+  if (nv == vn) return -1;
+  if (type == OC_EQTSYMMETRIC) {
+    if (nv == bn) return 1;
+    if (nv >= BX1 && nv <= BX3 && nv - BX1 < components) return -1; /* EXPAND(Bn, Bp, Bt) */
+    return 1;
+  }
+  return nv == bn ? -1 : 1;
+}
+
 static void bound_box(oc_problem *p, double *q, int face_dir, int ib, int ie,
-                      int jb, int je, int kb, int ke, int side, int type) {
+                      int jb, int je, int kb, int ke, int side, int type, int sgn) {
   /* q is a cell array (face_dir < 0) or face array face_dir.  Loops run
      over the box in increasing order; the copies read interior or
      already-assigned points only. */
@@ -689,7 +702,16 @@ static void bound_box(oc_problem *p, double *q, int face_dir, int ib, int ie,
     for (j = jb; dj * j <= dj * je; j += dj)
       for (i = ib; di * i <= di * ie; i += di) {
         size_t dst = IDX(k, j, i), src;
-        if (type == OC_PERIODIC) {
+        if (type == OC_REFLECTIVE || type == OC_EQTSYMMETRIC) { /* ReflectiveBound, boundary.c:523-560 */
+          if (side == 0) src = IDX(k, j, 2 * p->beg[0] - i - 1);
+          else if (side == 1) src = IDX(k, j, 2 * p->end[0] - i + 1);
+          else if (side == 2) src = IDX(k, 2 * p->beg[1] - j - 1, i);
+          else if (side == 3) src = IDX(k, 2 * p->end[1] - j + 1, i);
+          else if (side == 4) src = IDX(2 * p->beg[2] - k - 1, j, i);
+          else src = IDX(2 * p->end[2] - k + 1, j, i);
+          q[dst] = sgn * q[src];
+          continue;
+        } else if (type == OC_PERIODIC) {
           if (side == 0) src = IDX(k, j, i + NX1);
           else if (side == 1) src = IDX(k, j, i - NX1);
           else if (side == 2) src = IDX(k, j + NX2, i);
@@ -796,7 +818,8 @@ static void boundary(oc_problem *p) {
     else if (is == 3) { jb = p->end[1] + 1; je = p->nt[1] - 1; }
     else if (is == 4) { kb = p->beg[2] - 1; ke = 0; }
     else { kb = p->end[2] + 1; ke = p->nt[2] - 1; }
-    for (nv = 0; nv < NV; nv++) bound_box(p, p->vc[nv], -1, ib, ie, jb, je, kb, ke, is, type);
+    for (nv = 0; nv < NV; nv++)
+      bound_box(p, p->vc[nv], -1, ib, ie, jb, je, kb, ke, is, type, flip_sign(d, type, nv, p->c.components));
     if (p->c.ct) {
       int fd;
       for (fd = 0; fd < dims; fd++) {
@@ -806,9 +829,10 @@ static void boundary(oc_problem *p) {
         if (fd == 1) { if (jb < je) fjb = jb - 1; else fje = je - 1; }
         if (fd == 2) { if (kb < ke) fkb = kb - 1; else fke = ke - 1; }
         if (type == OC_PERIODIC) {
-          bound_box(p, p->bs[fd], fd, fib, fie, fjb, fje, fkb, fke, is, type);
+          bound_box(p, p->bs[fd], fd, fib, fie, fjb, fje, fkb, fke, is, type, 1);
         } else if (fd != d) {
-          bound_box(p, p->bs[fd], fd, fib, fie, fjb, fje, fkb, fke, is, type);
+          bound_box(p, p->bs[fd], fd, fib, fie, fjb, fje, fkb, fke, is, type,
+                    flip_sign(d, type, BX1 + fd, p->c.components));
         }
       }
       /* outflow: the normal staggered component from div B = 0, then its
@@ -816,6 +840,8 @@ static void boundary(oc_problem *p) {
       if (type == OC_OUTFLOW) {
         fill_magnetic_field(p, is);
         ct_average_normal(p, is);
+      } else if (type == OC_REFLECTIVE || type == OC_EQTSYMMETRIC) {
+        fill_magnetic_field(p, is); /* no normal averaging here (boundary.c:192-207) */
       }
     }
   }
@@ -1727,7 +1753,7 @@ oc_problem *oc_create(const oc_config *cfg) {
   p->c = *cfg;
   if (cfg->ct && cfg->dims < 2) { free(p); return NULL; }
   for (d = 0; d < 3; d++)
-    if (cfg->bc[d] != OC_PERIODIC && cfg->bc[d] != OC_OUTFLOW) { free(p); return NULL; }
+    if (cfg->bc[d] < OC_PERIODIC || cfg->bc[d] > OC_EQTSYMMETRIC) { free(p); return NULL; }
   p->ng = cfg->recon == OC_PARABOLIC ? 3 : 2; /* Src/get_nghost.c:28-104 */
   if (cfg->stepping == OC_HANCOCK) {
     if (cfg->recon != OC_LINEAR) { free(p); return NULL; } /* hancock.c:64-67 */

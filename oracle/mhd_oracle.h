@@ -28,7 +28,7 @@ enum { OC_FLAT_LIM = 0, OC_MINMOD_LIM, OC_VANLEER_LIM, OC_MC_LIM, OC_DEFAULT_LIM
 enum { OC_HLL = 0, OC_HLLD = 1, OC_ROE = 2 };
 enum { OC_RK2 = 2, OC_RK3 = 3, OC_HANCOCK = 4 }; /* HANCOCK: CTU with the primitive Hancock predictor */
 enum { OC_ARITHMETIC = 1, OC_UCT_CONTACT = 3, OC_UCT_HLL = 4 }; /* CT_EMF_AVERAGE */
-enum { OC_PERIODIC = 0, OC_OUTFLOW = 1 };
+enum { OC_PERIODIC = 0, OC_OUTFLOW = 1, OC_REFLECTIVE = 2, OC_EQTSYMMETRIC = 3 };
 
 typedef struct {
   int dims;            /* DIMENSIONS 1..3 */

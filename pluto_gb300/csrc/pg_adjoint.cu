@@ -564,7 +564,7 @@ __global__ void k_adj_recon(AdjArgs A, Box box) {
 struct BoundTab {
   double* p[12];
 };
-__global__ void k_adj_bound(Geom g, BoundTab t, int narr, int bcx, int bcy, int bcz) {
+__global__ void k_adj_bound(Geom g, BoundTab t, int narr, int bcx, int bcy, int bcz, int ncomp) {
   long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (c >= g.ncell) return;
   int i, j, k;
@@ -574,10 +574,17 @@ __global__ void k_adj_bound(Geom g, BoundTab t, int narr, int bcx, int bcy, int 
   const int sj = g.dims > 1 ? bmap(j, g.beg[1], g.end[1], g.nx[1], bcy) : j;
   const int sk = g.dims > 2 ? bmap(k, g.beg[2], g.end[2], g.nx[2], bcz) : k;
   const long long src = cidx(g, sk, sj, si);
+  const int bt[3] = {bcx, bcy, bcz};
+  const int x[3] = {i, j, k};
+  int flips = 0;  // mirror signs of the cell variables (the first NV arrays)
+  for (int d = 0; d < g.dims; d++)
+    if (x[d] < g.beg[d] || x[d] > g.end[d])
+      for (int nv = 0; nv < NV; nv++)
+        if (bc_flip(d, bt[d], nv, ncomp) < 0) flips ^= 1 << nv;
   for (int a = 0; a < narr; a++) {
     const double v = t.p[a][c];
     if (v != 0.0) {
-      atomicAdd(&t.p[a][src], v);
+      atomicAdd(&t.p[a][src], (a < NV && ((flips >> a) & 1)) ? -v : v);
       t.p[a][c] = 0.0;
     }
   }
@@ -769,7 +776,8 @@ void rev_stage(Solver* S, const AdjArgs& A, bool add_b0) {
   for (int nv = 0; nv < NV; nv++) t.p[na++] = b.lVin[nv];
   if (ct)
     for (int d = 0; d < g.dims; d++) t.p[na++] = b.lBin[d];
-  k_adj_bound<<<grid_for(n), kT, 0, st>>>(g, t, na, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2]);
+  k_adj_bound<<<grid_for(n), kT, 0, st>>>(g, t, na, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2],
+                                          S->cfg.components);
 }
 
 int check_fp64(pg_solver* h, const char* who, bool tangent_ok) {
@@ -839,8 +847,8 @@ extern "C" int pg_adjoint_set(pg_solver* h, const double* const vars[8], const d
   }
   if (S->cfg.divb == PG_CONSTRAINED_TRANSPORT)
     for (int d = 0; d < S->g.dims; d++)
-      if (S->cfg.bc[d] == PG_OUTFLOW) {
-        set_last_error("pg_adjoint_set: outflow boundaries under constrained transport are not covered");
+      if (S->cfg.bc[d] != PG_PERIODIC) {
+        set_last_error("pg_adjoint_set: non-periodic boundaries under constrained transport are not covered");
         return PG_ERR_INVALID;
       }
   AdjBufs* B = nullptr;

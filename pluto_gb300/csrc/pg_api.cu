@@ -36,7 +36,7 @@ int validate_config(const pg_config* c) {
   for (int d = 0; d < c->dims; d++) {
     if (c->nx[d] < 4) return fail(PG_ERR_INVALID, "nx must be >= 4 on active axes");
     if (!(c->dx[d] > 0)) return fail(PG_ERR_INVALID, "dx must be positive");
-    if (c->bc[d] != PG_PERIODIC && c->bc[d] != PG_OUTFLOW) return fail(PG_ERR_INVALID, "unsupported boundary");
+    if (c->bc[d] < PG_PERIODIC || c->bc[d] > PG_EQTSYMMETRIC) return fail(PG_ERR_INVALID, "unsupported boundary");
   }
   if (!(c->gamma > 1.0)) return fail(PG_ERR_INVALID, "gamma must be > 1");
   if (c->reconstruction != PG_LINEAR && c->reconstruction != PG_PARABOLIC)

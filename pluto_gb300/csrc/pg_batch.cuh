@@ -205,12 +205,14 @@ __device__ double batch_stage(const BatchArgs<T>& b, int tube, T* const* Vin, T*
   const int B = blockDim.x, tid = threadIdx.x;
   const T inv_dx = (T)b.inv_dx[tube];
   const T dtdx = (T)(dt / b.dxv[tube]);
-  // ghost fill of the stage input (outflow: copy edge zone; periodic: wrap)
+  // ghost fill of the stage input (outflow: copy edge zone; periodic: wrap;
+  // reflective / equatorial-symmetric: mirror with the FlipSign signs)
   for (int q = tid; q < 2 * ng * NV; q += B) {
     int nv = q / (2 * ng), gi = q % (2 * ng);
     int i = gi < ng ? gi : end + 1 + (gi - ng);
-    int src = gi < ng ? (b.bc == PG_PERIODIC ? i + n : beg) : (b.bc == PG_PERIODIC ? i - n : end);
-    Vin[nv][base + i] = Vin[nv][base + src];
+    int src = bc_src(i, beg, end, n, b.bc);
+    const T v = Vin[nv][base + src];
+    Vin[nv][base + i] = bc_flip(0, b.bc, nv, b.ncomp) < 0 ? -v : v;
   }
   __syncthreads();
   T cm_max = T(0);

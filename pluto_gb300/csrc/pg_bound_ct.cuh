@@ -1,13 +1,14 @@
-// Boundary fill under constrained transport when an axis has outflow sides:
+// Boundary fill under constrained transport when an axis is not periodic:
 // the reference's side-by-side sequence (Src/boundary.c:137-300), one axis
 // after the other.  Per axis, k_bound_axis copies the cells and the
-// transverse face components (zero gradient or periodic image; the normal
-// component too on a periodic axis), including the faces' -1 layers (index -1
-// along their own axis, Src/initialize.c:448-453), which live in Bm1 because
-// the face arrays do not store them; then, on an outflow axis,
-// k_fill_normal recovers the normal face component in the ghost faces from
-// div B = 0 (FillMagneticField, Src/MHD/CT/ct_fill_mag_field.c:38-180) and
-// averages it to the cell centres (CT_AverageNormalMagField,
+// transverse face components (zero gradient, periodic image, or mirror image
+// with the FlipSign signs; the normal component too on a periodic axis),
+// including the faces' -1 layers (index -1 along their own axis,
+// Src/initialize.c:448-453), which live in Bm1 because the face arrays do not
+// store them; then, on a non-periodic axis, k_fill_normal recovers the normal
+// face component in the ghost faces from div B = 0 (FillMagneticField,
+// Src/MHD/CT/ct_fill_mag_field.c:38-180) and, on outflow sides, averages it
+// to the cell centres (CT_AverageNormalMagField,
 // Src/MHD/CT/ct_field_average.c:134-275).  T is the storage type, C the
 // arithmetic type (double for the FP32-storage mixed path).
 #pragma once
@@ -22,7 +23,7 @@ struct BoundCT {
   T* V[8];
   T* Bs[3];
   T* Bm1[3];  // -1 layers: Bm1[0][k][j], Bm1[1][k][i], Bm1[2][j][i]
-  int nbfield;
+  int nbfield, ncomp;
   double area[3];
 };
 
@@ -71,18 +72,24 @@ __global__ void k_bound_axis(BoundCT<T> a, int type, long long nghost) {
   c[AX] = lo ? l : g.end[AX] + 1 + (l - ng);
   s[B1] = c[B1];
   s[B2] = c[B2];
-  s[AX] = type == PG_PERIODIC ? (lo ? c[AX] + n : c[AX] - n) : (lo ? g.beg[AX] : g.end[AX]);
+  s[AX] = bc_src(c[AX], g.beg[AX], g.end[AX], n, type);
   const long long dst = cidx(g, c[2], c[1], c[0]), src = cidx(g, s[2], s[1], s[0]);
 #pragma unroll
-  for (int nv = 0; nv < NV; nv++) a.V[nv][dst] = a.V[nv][src];
+  for (int nv = 0; nv < NV; nv++) {
+    const T v = a.V[nv][src];
+    a.V[nv][dst] = bc_flip(AX, type, nv, a.ncomp) < 0 ? -v : v;
+  }
   for (int fd = 0; fd < a.nbfield; fd++) {
     if (fd != AX) {
-      a.Bs[fd][dst] = a.Bs[fd][src];
+      const bool neg = bc_flip(AX, type, BX1 + fd, a.ncomp) < 0;
+      const T v = a.Bs[fd][src];
+      a.Bs[fd][dst] = neg ? -v : v;
       if (c[fd] == 0) {  // the -1 layer of this transverse component
         int cm[3] = {c[0], c[1], c[2]}, sm[3] = {s[0], s[1], s[2]};
         cm[fd] = -1;
         sm[fd] = -1;
-        *bct_face(a, fd, cm[2], cm[1], cm[0]) = *bct_face(a, fd, sm[2], sm[1], sm[0]);
+        const T w = *bct_face(a, fd, sm[2], sm[1], sm[0]);
+        *bct_face(a, fd, cm[2], cm[1], cm[0]) = neg ? -w : w;
       }
     } else if (type == PG_PERIODIC) {
       // normal component: faces beg-1 .. -1 from their images; on the end
@@ -102,7 +109,7 @@ __global__ void k_bound_axis(BoundCT<T> a, int type, long long nghost) {
 // One thread per transverse position and side: the normal component marched
 // away from the boundary face, then its cell average.
 template <class T, class C, int AX>
-__global__ void k_fill_normal(BoundCT<T> a, long long ntrans) {
+__global__ void k_fill_normal(BoundCT<T> a, long long ntrans, int average) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= 2 * ntrans) return;
   const Geom& g = a.g;
@@ -127,7 +134,7 @@ __global__ void k_fill_normal(BoundCT<T> a, long long ntrans) {
     return dB(0) + dB(1);
   };
   const double An = a.area[AX];
-  auto average = [&](int x) {
+  auto cell_average = [&](int x) {
     c[AX] = x;
     int m[3] = {c[0], c[1], c[2]};
     m[AX] = x - 1;
@@ -146,7 +153,8 @@ __global__ void k_fill_normal(BoundCT<T> a, long long ntrans) {
       m[AX] = x - 1;
       *bct_face(a, AX, m[2], m[1], m[0]) = T(r);
     }
-    for (int x = 0; x < g.beg[AX]; x++) average(x);
+    if (average)
+      for (int x = 0; x < g.beg[AX]; x++) cell_average(x);
   } else {
     for (int x = g.end[AX] + 1; x < g.nt[AX]; x++) {
       c[AX] = x;
@@ -155,7 +163,8 @@ __global__ void k_fill_normal(BoundCT<T> a, long long ntrans) {
       const C bm = face(AX, m[2], m[1], m[0]);
       *bct_face(a, AX, c[2], c[1], c[0]) = T((An * bm - others()) / An);
     }
-    for (int x = g.end[AX] + 1; x < g.nt[AX]; x++) average(x);
+    if (average)
+      for (int x = g.end[AX] + 1; x < g.nt[AX]; x++) cell_average(x);
   }
 }
 
@@ -167,9 +176,11 @@ static void launch_bound_ct_axis(Solver* S, const BoundCT<T>& b, const char* cop
   const long long nghost = 2LL * g.beg[AX] * ntrans;
   PG_LAUNCH(S, copy_name, (k_bound_axis<T, AX><<<grid_for(nghost), kThreads, 0, S->stream>>>(
                               b, S->cfg.bc[AX], nghost)));
-  if (S->cfg.bc[AX] == PG_OUTFLOW)
+  // outflow: FillMagneticField + CT_AverageNormalMagField; reflective and
+  // equatorial-symmetric: FillMagneticField only (Src/boundary.c:171-207)
+  if (S->cfg.bc[AX] != PG_PERIODIC)
     PG_LAUNCH(S, fill_name, (k_fill_normal<T, C, AX><<<grid_for(2 * ntrans, 128), 128, 0, S->stream>>>(
-                                b, ntrans)));
+                                b, ntrans, S->cfg.bc[AX] == PG_OUTFLOW ? 1 : 0)));
 }
 
 template <class T, class C>

@@ -53,7 +53,7 @@ int fp64_alloc(Solver* S) {
     if (alloc(&S->E[2])) return PG_ERR_NOMEM;
     if (S->g.dims == 3 && (alloc(&S->E[0]) || alloc(&S->E[1]))) return PG_ERR_NOMEM;
     bool outflow = false;
-    for (int d = 0; d < S->g.dims; d++) outflow |= S->cfg.bc[d] == PG_OUTFLOW;
+    for (int d = 0; d < S->g.dims; d++) outflow |= S->cfg.bc[d] != PG_PERIODIC;
     if (outflow) {
       const Geom& g = S->g;
       const long long m[3] = {(long long)g.nt[1] * g.nt[2], (long long)g.nt[0] * g.nt[2],

@@ -44,7 +44,7 @@ struct F64A {
   int limiter, recon, ct, nbfield, ncomp;
   int device_dt;
   int bc[3];
-  int ct_outflow;   // constrained transport with an outflow axis: per-axis boundary passes
+  int ct_outflow;   // constrained transport with a non-periodic axis: per-axis boundary passes
   int div_dims;     // RK: invDt_hyp /= DIMENSIONS (update_stage.c:311); CTU: no
   int emf_avg, c3;
 };
@@ -78,9 +78,7 @@ __device__ __forceinline__ double block_max(double v) {
 // Src/boundary.c:482-522 applied to the X1FACE box).
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int bmap(int x, int beg, int end, int n, int type) {
-  if (x < beg) return type == PG_PERIODIC ? x + n : beg;
-  if (x > end) return type == PG_PERIODIC ? x - n : end;
-  return x;
+  return bc_src(x, beg, end, n, type);
 }
 
 template <class T>
@@ -119,8 +117,20 @@ __global__ void k_bound(F64A<T> a, int bcx, int bcy, int bcz, long long nslab0, 
   int sj = g.dims > 1 ? bmap(j, g.beg[1], g.end[1], g.nx[1], bcy) : j;
   int sk = g.dims > 2 ? bmap(k, g.beg[2], g.end[2], g.nx[2], bcz) : k;
   long long dst = cidx(g, k, j, i), src = cidx(g, sk, sj, si);
+  // reflective / equatorial-symmetric axes mirror with the FlipSign signs,
+  // one factor per axis whose ghost region holds this zone
+  const int bt[3] = {bcx, bcy, bcz};
+  const int x[3] = {i, j, k};
+  int flips = 0;  // bit nv set: variable nv changes sign
+  for (int d = 0; d < g.dims; d++)
+    if (x[d] < g.beg[d] || x[d] > g.end[d])
+      for (int nv = 0; nv < NV; nv++)
+        if (bc_flip(d, bt[d], nv, a.ncomp) < 0) flips ^= 1 << nv;
 #pragma unroll
-  for (int nv = 0; nv < NV; nv++) a.V[nv][dst] = a.V[nv][src];
+  for (int nv = 0; nv < NV; nv++) {
+    const T v = a.V[nv][src];
+    a.V[nv][dst] = ((flips >> nv) & 1) ? -v : v;
+  }
   for (int d = 0; d < a.nbfield; d++) a.Bs[d][dst] = a.Bs[d][src];
 }
 
@@ -502,7 +512,7 @@ static F64A<T> make_args(Solver* S) {
   a.c3 = S->cfg.components == 3;
   a.ct_outflow = 0;
   if (a.ct)
-    for (int d = 0; d < S->g.dims; d++) a.ct_outflow |= S->cfg.bc[d] == PG_OUTFLOW;
+    for (int d = 0; d < S->g.dims; d++) a.ct_outflow |= S->cfg.bc[d] != PG_PERIODIC;
 
   a.device_dt = S->device_dt;
   return a;
@@ -581,6 +591,7 @@ static void launch_bound(Solver* S, const F64A<T>& a) {
       b.Bm1[d] = a.Bm1[d];
     }
     b.nbfield = a.nbfield;
+    b.ncomp = a.ncomp;
     face_areas(g, b.area);
     launch_bound_ct<T, T>(S, b, "fp64_bound", "fp64_fill_normal");
     return;

@@ -132,14 +132,12 @@ __device__ __forceinline__ void solve_iface(const MixArgs& a, int solver, float*
 // boundary (same maps as the FP64 path)
 // ---------------------------------------------------------------------------
 __device__ __forceinline__ int mbmap(int x, int beg, int end, int n, int type) {
-  if (x < beg) return type == PG_PERIODIC ? x + n : beg;
-  if (x > end) return type == PG_PERIODIC ? x - n : end;
-  return x;
+  return bc_src(x, beg, end, n, type);
 }
 
 struct BoundArrays {
   float* q[11];
-  int n;
+  int n, ncomp;
 };
 
 __global__ void k_mbound(Geom g, BoundArrays arr, int bcx, int bcy, int bcz, long long n0, long long n1,
@@ -176,7 +174,18 @@ __global__ void k_mbound(Geom g, BoundArrays arr, int bcx, int bcy, int bcz, lon
   int sj = g.dims > 1 ? mbmap(j, g.beg[1], g.end[1], g.nx[1], bcy) : j;
   int sk = g.dims > 2 ? mbmap(k, g.beg[2], g.end[2], g.nx[2], bcz) : k;
   long long dst = cidx(g, k, j, i), src = cidx(g, sk, sj, si);
-  for (int a = 0; a < arr.n; a++) arr.q[a][dst] = arr.q[a][src];
+  // mirror signs (FlipSign) of the first NV arrays, the cell variables
+  const int bt[3] = {bcx, bcy, bcz};
+  const int x[3] = {i, j, k};
+  int flips = 0;
+  for (int d = 0; d < g.dims; d++)
+    if (x[d] < g.beg[d] || x[d] > g.end[d])
+      for (int nv = 0; nv < NV; nv++)
+        if (bc_flip(d, bt[d], nv, arr.ncomp) < 0) flips ^= 1 << nv;
+  for (int a = 0; a < arr.n; a++) {
+    const float v = arr.q[a][src];
+    arr.q[a][dst] = (a < NV && ((flips >> a) & 1)) ? -v : v;
+  }
 }
 
 // ---------------------------------------------------------------------------
@@ -658,7 +667,7 @@ int mixed_alloc(Solver* S) {
     const long long m[3] = {(long long)g.nt[1] * g.nt[2], (long long)g.nt[0] * g.nt[2],
                             (long long)g.nt[0] * g.nt[1]};
     for (int d = 0; d < g.dims; d++)
-      if (S->cfg.bc[d] == PG_OUTFLOW) {
+      if (S->cfg.bc[d] != PG_PERIODIC) {
         for (int e = 0; e < g.dims; e++) {
           if (cudaMalloc(&M->b.Bm1[e], m[e] * sizeof(float)) != cudaSuccess) return PG_ERR_NOMEM;
           cudaMemset(M->b.Bm1[e], 0, m[e] * sizeof(float));
@@ -755,12 +764,14 @@ static void mlaunch_bound(Solver* S, const MixArgs& a) {
       b.Bm1[d] = M->b.Bm1[d];
     }
     b.nbfield = a.nbfield;
+    b.ncomp = S->cfg.components;
     face_areas(g, b.area);
     launch_bound_ct<float, double>(S, b, "mixed_bound", "mixed_fill_normal");
     return;
   }
   BoundArrays arr;
   arr.n = 0;
+  arr.ncomp = S->cfg.components;
   for (int nv = 0; nv < NV; nv++) arr.q[arr.n++] = (float*)a.Vin[nv];
   for (int d = 0; d < a.nbfield; d++) arr.q[arr.n++] = (float*)a.Bin[d];
   long long n0 = 2LL * g.beg[0] * g.nt[1] * g.nt[2];

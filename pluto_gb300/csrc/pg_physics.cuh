@@ -12,6 +12,24 @@ enum : int { RHO = 0, VX1 = 1, VX2 = 2, VX3 = 3, BX1 = 4, BX2 = 5, BX3 = 6, PRS 
 constexpr int MX1 = VX1, ENG = PRS;
 constexpr unsigned char FLAG_CONS2PRIM_FAIL = 64;  // Src/pluto.h:200
 
+// FlipSign, Src/boundary.c:318-437: +1 or -1 for variable nv (BX1+d for a
+// face component) mirrored across a REFLECTIVE / EQTSYMMETRIC side of axis d.
+__host__ __device__ __forceinline__ int bc_flip(int d, int type, int nv, int components) {
+  if (type != 2 && type != 3) return 1;  // PG_REFLECTIVE, PG_EQTSYMMETRIC
+  if (nv == 1 + d) return -1;            // normal velocity
+  if (type == 3) {
+    if (nv == 4 + d) return 1;
+    return (nv >= 4 && nv <= 6 && nv - 4 < components) ? -1 : 1;
+  }
+  return nv == 4 + d ? -1 : 1;           // normal field
+}
+// mirror / image / edge zone that ghost x copies from (Src/boundary.c:439-560)
+__host__ __device__ __forceinline__ int bc_src(int x, int beg, int end, int n, int type) {
+  if (x < beg) return type == 0 ? x + n : (type == 1 ? beg : 2 * beg - x - 1);
+  if (x > end) return type == 0 ? x - n : (type == 1 ? end : 2 * end - x + 1);
+  return x;
+}
+
 template <class T> __device__ __forceinline__ T pmax(T a, T b) { return a >= b ? a : b; }  // macros.h MAX
 template <class T> __device__ __forceinline__ T pmin(T a, T b) { return a <= b ? a : b; }  // macros.h MIN
 template <class T> __device__ __forceinline__ T abs_min(T a, T b) { return fabs(a) < fabs(b) ? a : b; }

@@ -48,6 +48,8 @@ static int gpu_bc(int t)
 {
   if (t == PERIODIC) return PG_PERIODIC;
   if (t == OUTFLOW)  return PG_OUTFLOW;
+  if (t == REFLECTIVE)   return PG_REFLECTIVE;
+  if (t == EQTSYMMETRIC) return PG_EQTSYMMETRIC;
   return -1;
 }
 

@@ -25,7 +25,8 @@ LIMITER = {"FLAT_LIM": L.PG_FLAT_LIM, "MINMOD_LIM": L.PG_MINMOD_LIM,
 RIEMANN = {"hll": L.PG_HLL, "hlld": L.PG_HLLD, "roe": L.PG_ROE}
 STEPPING = {"RK2": L.PG_RK2, "RK3": L.PG_RK3, "HANCOCK": L.PG_HANCOCK}
 EMF = {"ARITHMETIC": L.PG_ARITHMETIC, "UCT_CONTACT": L.PG_UCT_CONTACT, "UCT_HLL": L.PG_UCT_HLL}
-BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW}
+BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW, "reflective": L.PG_REFLECTIVE,
+      "eqtsymmetric": L.PG_EQTSYMMETRIC}
 PRECISION = {"fp64": L.PG_FP64, "mixed": L.PG_MIXED, "mixed_dw": L.PG_MIXED_DW,
              "fp64_tangent": L.PG_FP64_TANGENT}
 NVAR = 8

@@ -77,6 +77,12 @@ def setups():
         replace(br.tube_setup(1, 200, 120), stepping="HANCOCK", name="tube_ctu_1_200"),
         replace(br.cpa_setup(32, 20), stepping="HANCOCK", emf="UCT_CONTACT", bc="outflow",
                 name="cpa_ctu_outflow_32"),
+        replace(br.blast_setup(16, 12), bc="reflective", name="blast_reflective_16"),
+        replace(br.ot_setup("hlld", 32, 30), bc="reflective", name="ot_reflective_32"),
+        replace(br.cpa_setup(32, 20), bc="eqtsymmetric", name="cpa_eqtsym_32"),
+        replace(br.tube_setup(0, 256, 100), bc="reflective", name="tube_reflective_0_256"),
+        replace(br.ot_setup("hlld", 32, 30), stepping="HANCOCK", emf="UCT_CONTACT", bc="reflective",
+                name="ot_ctu_reflective_32"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

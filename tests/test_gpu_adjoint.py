@@ -53,11 +53,17 @@ def _case(name):
     if name == "tube1d_ppm_outflow":
         spec, vc, f = P.riemann_tube(48, 2)
         return dict(spec, recon="PARABOLIC", limiter="MC_LIM"), vc, f, [1e-3] * 6
+    if name == "tube1d_reflective":
+        spec, vc, f = P.riemann_tube(48, 1)
+        return dict(spec, bc="reflective"), vc, f, [1e-3] * 5
+    if name == "ot2d_mirror_noct":
+        spec, vc, f = P.orszag_tang(16)
+        return dict(spec, ct=False, bc=["reflective", "eqtsymmetric", "periodic"]), vc, f, [1e-3] * 3
     raise KeyError(name)
 
 
 CASES = ["cpa2d_plm_hlld", "ot2d_plm_hll", "turb3d_ppm_hlld", "turb3d_plm_minmod_hll",
-         "tube1d_outflow", "tube1d_ppm_outflow", "cpa2d_plm_roe"]
+         "tube1d_outflow", "tube1d_ppm_outflow", "cpa2d_plm_roe", "tube1d_reflective", "ot2d_mirror_noct"]
 
 
 def _smooth(vc):

@@ -24,11 +24,13 @@ def _oracle_run(spec, n, dx, state, nsteps, first_dt):
     return o.get_state()[0].reshape(8, int(n)), t
 
 
-@pytest.mark.parametrize("recon,stepping", [("LINEAR", "RK2"), ("PARABOLIC", "RK3")])
-def test_batch_fp64_matches_oracle_per_tube(recon, stepping):
+@pytest.mark.parametrize("recon,stepping,bc", [("LINEAR", "RK2", "outflow"), ("PARABOLIC", "RK3", "outflow"),
+                                               ("LINEAR", "RK2", "reflective"),
+                                               ("PARABOLIC", "RK2", "eqtsymmetric")])
+def test_batch_fp64_matches_oracle_per_tube(recon, stepping, bc):
     from pluto_gb300.batch import Batch
     spec, ns, dxs, states = _family(24, 7, 16, 300)
-    spec = dict(spec, recon=recon, stepping=stepping)
+    spec = dict(spec, recon=recon, stepping=stepping, bc=bc)
     b = Batch(spec, ns, dxs, "fp64")
     b.upload(states)
     b.run(60, 1e-4, spec["cfl"])
@@ -42,7 +44,7 @@ def test_batch_fp64_matches_oracle_per_tube(recon, stepping):
 
 def test_batch_fp64_matches_golden_tubes():
     from pluto_gb300.batch import Batch
-    names = ["tube_0_256", "tube_1_200", "tube_2_160", "tube_roe_0_256"]
+    names = ["tube_0_256", "tube_1_200", "tube_2_160", "tube_roe_0_256", "tube_reflective_0_256"]
     metas, st0, st1 = [], [], []
     for nm in names:
         meta, vc0, _, vc1, _ = load_golden(nm)

@@ -43,7 +43,8 @@ def test_fp64_matches_reference_goldens(name):
                                   "ot_roe_32", "cpa_roe_32", "blast_roe_16", "tube_roe_0_256",
                                   "ot_outflow_32", "turb_outflow_12", "ot_ctu_uctc_32",
                                   "ot_ctu_arith_roe_32", "turb_ctu_uctc_12", "tube_ctu_1_200",
-                                  "cpa_ctu_outflow_32"])
+                                  "cpa_ctu_outflow_32", "blast_reflective_16", "ot_reflective_32",
+                                  "cpa_eqtsym_32", "tube_reflective_0_256", "ot_ctu_reflective_32"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
@@ -115,10 +116,13 @@ def test_fp64_vs_oracle_random_3d(solver, recon, stepping):
 
 
 @pytest.mark.parametrize("bc", [("outflow", "outflow", "outflow"), ("outflow", "periodic", "outflow"),
-                                ("periodic", "outflow", "periodic")])
+                                ("periodic", "outflow", "periodic"), ("reflective", "eqtsymmetric", "reflective"),
+                                ("eqtsymmetric", "periodic", "outflow")])
 def test_fp64_vs_oracle_outflow_ct_3d(bc):
-    """Outflow sides under CT (FillMagneticField + normal averaging), mixed
-    with periodic axes, on a random 3D state against the oracle."""
+    """Outflow, reflective and equatorial-symmetric sides under CT
+    (FillMagneticField, normal averaging on outflow sides, FlipSign mirror
+    signs), mixed with periodic axes, on a random 3D state against the
+    oracle."""
     from oracle.oracle import Oracle
     spec, vc, bs = _random_blast(20, seed=5)
     spec.update(bc=list(bc), solver="roe", recon="PARABOLIC", stepping="RK3")
@@ -181,7 +185,8 @@ def test_nan_state_reported_not_trapped():
 
 
 @pytest.mark.parametrize("emf,solver,bc", [("UCT_CONTACT", "hlld", "periodic"), ("ARITHMETIC", "hll", "outflow"),
-                                           ("UCT_CONTACT", "roe", "outflow")])
+                                           ("UCT_CONTACT", "roe", "outflow"),
+                                           ("UCT_CONTACT", "hlld", ["reflective", "periodic", "eqtsymmetric"])])
 def test_ctu_vs_oracle_random_3d(emf, solver, bc):
     """CTU (primitive Hancock predictor, corner-coupled corrector) with CT on a
     random 3D state against the oracle, bit for bit."""
