@@ -668,7 +668,7 @@ static void ppm_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV],
 }
 
 /* ------------------------------------------------------------------ */
-/* Boundary conditions, Src/boundary.c:41-303, 439-522                 */
+/* Boundary conditions, Src/boundary.c:41-303, 318-565                 */
 /* ------------------------------------------------------------------ */
 
 /* FlipSign, Src/boundary.c:318-437 (REFLECTIVE and EQTSYMMETRIC): sign of

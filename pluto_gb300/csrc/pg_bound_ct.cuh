@@ -177,7 +177,7 @@ static void launch_bound_ct_axis(Solver* S, const BoundCT<T>& b, const char* cop
   PG_LAUNCH(S, copy_name, (k_bound_axis<T, AX><<<grid_for(nghost), kThreads, 0, S->stream>>>(
                               b, S->cfg.bc[AX], nghost)));
   // outflow: FillMagneticField + CT_AverageNormalMagField; reflective and
-  // equatorial-symmetric: FillMagneticField only (Src/boundary.c:171-207)
+  // equatorial-symmetric: FillMagneticField only (Src/boundary.c:188-206)
   if (S->cfg.bc[AX] != PG_PERIODIC)
     PG_LAUNCH(S, fill_name, (k_fill_normal<T, C, AX><<<grid_for(2 * ntrans, 128), 128, 0, S->stream>>>(
                                 b, ntrans, S->cfg.bc[AX] == PG_OUTFLOW ? 1 : 0)));

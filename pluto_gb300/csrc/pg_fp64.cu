@@ -6,7 +6,7 @@
 // (states, fluxes) and computes each interface exactly once.
 //
 // Kernel <-> reference map (files inside the PLUTO source tree):
-//   k_bound        Boundary(), Src/boundary.c:41-303 (periodic/outflow)
+//   k_bound        Boundary(), Src/boundary.c:41-303 (periodic/outflow/reflective/eqtsymmetric)
 //   k_begin_step   PrimToCons3D + U0/Bs0 save, Src/Time_Stepping/rk_step.c:93-100
 //   k_recon<D>     States(), Src/States/plm_states.c:80-312, ppm_states.c:68-253,
 //                  plus CT_StoreVelSlopes, Src/MHD/CT/ct_stag_slopes.c:5-49
