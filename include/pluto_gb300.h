@@ -216,6 +216,15 @@ int pg_kernel_launches_per_step(pg_solver *s);
 const char *pg_last_error(void);
 int pg_abi_version(void);
 
+/* Self-test of the integer float<->double conversions the mixed path uses
+   in place of the hardware ones (no reference counterpart): counts[0] =
+   float bit patterns whose widening differs from the hardware conversion
+   (all 2^32 checked), counts[1] = doubles whose round-to-nearest-even
+   narrowing differs (5 * 2^32 near-float and 2^32 wide-exponent patterns,
+   ties included).  NaN matches any NaN.  Both are 0 on a correct build.
+   Runs on the current device, about a second. */
+int pg_selftest_conversions(unsigned long long counts[2]);
+
 #ifdef __cplusplus
 }
 #endif

@@ -33,7 +33,8 @@ EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", 
            "pg_tube_step_static", "pg_batch_create", "pg_batch_destroy", "pg_batch_upload",
            "pg_batch_download", "pg_batch_run", "pg_batch_get", "pg_batch_autotune",
            "pg_batch_set_schedule", "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set",
-           "pg_adjoint_step", "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load"]
+           "pg_adjoint_step", "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load",
+           "pg_selftest_conversions"]
 PG_STATIC_MAX_ZONES = 32768
 PG_MAX_CHECKPOINTS = 256
 
@@ -106,6 +107,7 @@ def lib():
     L.pg_adjoint_step.argtypes = [vp, C.c_double]
     L.pg_checkpoint_save.argtypes = [vp, ip]
     L.pg_checkpoint_load.argtypes = [vp, ip]
+    L.pg_selftest_conversions.argtypes = [C.POINTER(C.c_ulonglong)]
     L.pg_last_error.restype = C.c_char_p
     for fn in ("pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
                "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
@@ -113,7 +115,7 @@ def lib():
                "pg_batch_create", "pg_batch_destroy", "pg_batch_upload", "pg_batch_download",
                "pg_batch_run", "pg_batch_get", "pg_batch_autotune", "pg_batch_set_schedule",
                "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set", "pg_adjoint_step",
-               "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load"):
+               "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load", "pg_selftest_conversions"):
         getattr(L, fn).restype = C.c_int
     _lib = L
     return L

@@ -5,6 +5,7 @@
 #include <string>
 
 #include "pg_internal.h"
+#include "pg_xfer.cuh"
 
 using namespace pg;
 
@@ -26,6 +27,10 @@ static int cuda_fail(cudaError_t e, const char* where) {
 
 extern "C" const char* pg_last_error(void) { return g_last_error.c_str(); }
 extern "C" int pg_abi_version(void) { return PG_ABI_VERSION; }
+extern "C" int pg_selftest_conversions(unsigned long long counts[2]) {
+  if (!counts) return fail(PG_ERR_INVALID, "pg_selftest_conversions: null counts");
+  return pg::mixed_selftest_conversions(counts);
+}
 
 namespace pg {
 int validate_config(const pg_config* c) {
@@ -162,6 +167,11 @@ namespace pg {
 int xfer_f64(Solver* S, double* dev, double* host, int fd, int layout, bool to_dev) {
   const Geom& g = S->g;
   cudaStream_t st = S->stream;
+  if (double* alias = host_alias(host)) {
+    launch_host_xfer<double>(st, alias, dev, g, fd, layout, to_dev);
+    CK(cudaGetLastError());
+    return PG_OK;
+  }
   const size_t e = sizeof(double);
   cudaMemcpyKind kind = to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
   if (layout == PG_LAYOUT_PLUTO) {

@@ -84,27 +84,58 @@ __device__ __forceinline__ dw dw_div(dw x, dw y) {  // DWDivDW2 (Alg. 17)
 
 __device__ __forceinline__ float dw_to_float(dw x) { return __fadd_rn(x.hi, x.lo); }
 
+// Exact float -> double from the IEEE-754 fields with integer operations:
+// sign kept, exponent rebiased (127 -> 1023), the 23 fraction bits shifted to
+// the top of the 52.  GB300 issues the hardware conversion on its FP64 pipe
+// (about as costly as a DADD there); this form issues on the integer pipes.
+// Subnormal inputs take the hardware conversion.  NaN payloads are kept.
+__device__ __forceinline__ double widen(float f) {
+  const unsigned u = __float_as_uint(f);
+  const unsigned e = (u >> 23) & 0xffu, frac = u & 0x7fffffu;
+  if (e == 0u && frac != 0u) return (double)f;
+  const unsigned ex = e == 0u ? 0u : (e == 0xffu ? 0x7ffu : e + 896u);
+  const unsigned hi = (u & 0x80000000u) | (ex << 20) | (frac >> 3);
+  return __hiloint2double((int)hi, (int)(u << 29));
+}
+
+// double -> float with round-to-nearest-even, from the fields: for results
+// whose exponent lies in the normal float range the top 23 fraction bits are
+// kept and the 29 dropped bits decide the rounding (above half, or exactly
+// half with an odd last bit, adds one ulp; the carry may step the exponent,
+// up to infinity).  Zero, subnormal, out-of-range and non-finite values take
+// the hardware conversion.
+__device__ __forceinline__ float narrow(double d) {
+  const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned e = (hi >> 20) & 0x7ffu;
+  if (e - 897u > 253u) return (float)d;
+  unsigned r = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+  const unsigned rest = lo & 0x1fffffffu;
+  r += (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) ? 1u : 0u;
+  return __uint_as_float(r);
+}
+
 // Accumulator traits: the mixed path is instantiated with native double or
 // with dw; both expose the same handful of operations.
 template <class A> struct Acc;
 
 template <> struct Acc<double> {
   using T = double;
-  static __device__ __forceinline__ T from(float a) { return (double)a; }
-  static __device__ __forceinline__ T prod(float a, float b) { return (double)a * (double)b; }
+  // conversions through widen / narrow (same values as the hardware ones)
+  static __device__ __forceinline__ T from(float a) { return widen(a); }
+  static __device__ __forceinline__ T prod(float a, float b) { return widen(a) * widen(b); }
   static __device__ __forceinline__ T add(T a, T b) { return a + b; }
-  static __device__ __forceinline__ T addf(T a, float b) { return a + (double)b; }
+  static __device__ __forceinline__ T addf(T a, float b) { return a + widen(b); }
   static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
-  static __device__ __forceinline__ T mulf(T a, float b) { return a * (double)b; }
+  static __device__ __forceinline__ T mulf(T a, float b) { return a * widen(b); }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
   // a/b through an FP32 reciprocal refined by one Newton step in FP64
   // (relative error ~1e-14), three FP64 operations instead of a full division.
   static __device__ __forceinline__ T div(T a, T b) {
-    double r = (double)__frcp_rn((float)b);
+    double r = widen(__frcp_rn(narrow(b)));
     r = fma(r, fma(-b, r, 1.0), r);
     return a * r;
   }
-  static __device__ __forceinline__ float tof(T a) { return (float)a; }
+  static __device__ __forceinline__ float tof(T a) { return narrow(a); }
   static __device__ __forceinline__ bool neg(T a) { return a < 0.0; }
   static __device__ __forceinline__ T konst(double hi, float, float) { return hi; }
 };

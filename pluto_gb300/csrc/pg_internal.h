@@ -85,6 +85,7 @@ void adjoint_free(Solver* S);      // adjoint buffers, checkpoints, staging
 int mixed_alloc(Solver* S);
 void mixed_free(Solver* S);
 int mixed_enqueue_step(Solver* S);
+int mixed_selftest_conversions(unsigned long long counts[2]);
 int validate_config(const pg_config* c);
 void init_geom(Solver* S);
 void set_last_error(const char* msg);

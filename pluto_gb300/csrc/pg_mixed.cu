@@ -26,6 +26,7 @@
 #include "pg_physics.cuh"
 #include "pg_dw.cuh"
 #include "pg_bound_ct.cuh"
+#include "pg_xfer.cuh"
 
 namespace pg {
 
@@ -914,11 +915,15 @@ static int mixed_xfer(Solver* S, const double* const vars[8], double* const outv
   MixedState* M = (MixedState*)S->mixed;
   const Geom& g = S->g;
   const long long n = g.ncell;
-  double* tmp = nullptr;
-  if (cudaMalloc(&tmp, n * sizeof(double)) != cudaSuccess) return PG_ERR_NOMEM;
+  double* tmp = nullptr;  // FP64 staging array, only for host memory the device cannot reach
   int rc = PG_OK;
   const int cur = M->cur;
   auto one = [&](float* dev, const double* hin, double* hout, int fd) -> int {
+    if (double* alias = host_alias(to_dev ? hin : hout)) {
+      launch_host_xfer<float>(S->stream, alias, dev, g, fd, layout, to_dev);
+      return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ERR_CUDA;
+    }
+    if (!tmp && cudaMalloc(&tmp, n * sizeof(double)) != cudaSuccess) return PG_ERR_NOMEM;
     if (to_dev) {
       cudaMemsetAsync(tmp, 0, n * sizeof(double), S->stream);
       int r = xfer_f64(S, tmp, (double*)hin, fd, layout, true);
@@ -936,16 +941,16 @@ static int mixed_xfer(Solver* S, const double* const vars[8], double* const outv
     } else if (outv[nv]) {
       rc = one(M->b.V[cur][nv], nullptr, outv[nv], -1);
     }
-    cudaStreamSynchronize(S->stream);
+    if (tmp) cudaStreamSynchronize(S->stream);  // the staging array is reused
   }
   if (S->cfg.divb == PG_CONSTRAINED_TRANSPORT)
     for (int d = 0; d < g.dims && !rc; d++) {
       if (to_dev && faces && faces[d]) rc = one(M->b.Bs[cur][d], faces[d], nullptr, d);
       if (!to_dev && outf && outf[d]) rc = one(M->b.Bs[cur][d], nullptr, outf[d], d);
-      cudaStreamSynchronize(S->stream);
+      if (tmp) cudaStreamSynchronize(S->stream);
     }
   if (cudaStreamSynchronize(S->stream) != cudaSuccess && !rc) rc = PG_ERR_CUDA;
-  cudaFree(tmp);
+  if (tmp) cudaFree(tmp);
   return rc;
 }
 
@@ -955,3 +960,67 @@ int mixed_upload_host(Solver* S, const double* const vars[8], const double* cons
 int mixed_download(Solver* S, double* const vars[8], double* const faces[3], int layout) {
   return mixed_xfer(S, nullptr, vars, nullptr, faces, layout, false);
 }
+
+namespace pg {
+
+__device__ __forceinline__ bool same_bits_d(double a, double b) {
+  return __double_as_longlong(a) == __double_as_longlong(b) || (a != a && b != b);
+}
+__device__ __forceinline__ bool same_bits_f(float a, float b) {
+  return __float_as_uint(a) == __float_as_uint(b) || (a != a && b != b);
+}
+
+// widen over every float bit pattern; narrow over doubles built from each
+// float pattern with five choices of the 29 bits below float precision
+// (zero, exactly half, half - 1, half + 1, a hash) and over doubles with the
+// exponent taken from a hash (underflow, overflow, subnormal results).
+__global__ void k_selftest_conv(unsigned long long* bad) {
+  unsigned long long nw = 0, nn = 0;
+  const unsigned long long stride = (unsigned long long)gridDim.x * blockDim.x;
+  for (unsigned long long q = blockIdx.x * (unsigned long long)blockDim.x + threadIdx.x; q < (1ull << 32);
+       q += stride) {
+    const unsigned u = (unsigned)q;
+    const float f = __uint_as_float(u);
+    const double h = (double)f;
+    nw += same_bits_d(widen(f), h) ? 0 : 1;
+    const unsigned hash = (u * 2654435761u) ^ (u >> 13);
+    const unsigned long long top = (unsigned long long)__double_as_longlong(h) & ~0x1fffffffull;
+    const unsigned pats[5] = {0u, 0x10000000u, 0x0fffffffu, 0x10000001u, hash & 0x1fffffffu};
+#pragma unroll
+    for (int p = 0; p < 5; p++) {
+      const double d = __longlong_as_double((long long)(top | pats[p]));
+      nn += same_bits_f(narrow(d), (float)d) ? 0 : 1;
+    }
+    const unsigned long long e2 = (unsigned long long)((hash >> 7) & 0x7ffu);
+    const unsigned long long wide = (top & 0x800fffffffffffffull) | (e2 << 52) | (hash & 0x1fffffffu);
+    const double d2 = __longlong_as_double((long long)wide);
+    nn += same_bits_f(narrow(d2), (float)d2) ? 0 : 1;
+  }
+  if (nw) atomicAdd(&bad[0], nw);
+  if (nn) atomicAdd(&bad[1], nn);
+}
+
+int mixed_selftest_conversions(unsigned long long counts[2]) {
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, 2 * sizeof(unsigned long long)) != cudaSuccess) {
+    set_last_error("pg_selftest_conversions: cudaMalloc failed");
+    return PG_ERR_NOMEM;
+  }
+  cudaError_t e = cudaMemset(d, 0, 2 * sizeof(unsigned long long));
+  int nsm = 152;
+  int dev = 0;
+  if (cudaGetDevice(&dev) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) {
+    k_selftest_conv<<<nsm * 8, 256>>>(d);
+    e = cudaGetLastError();
+  }
+  if (e == cudaSuccess) e = cudaMemcpy(counts, d, 2 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  if (e != cudaSuccess) {
+    set_last_error((std::string("pg_selftest_conversions: ") + cudaGetErrorString(e)).c_str());
+    return PG_ERR_CUDA;
+  }
+  return PG_OK;
+}
+
+}  // namespace pg

@@ -103,20 +103,37 @@ class Solver:
                 faces[d] = np.ascontiguousarray(bs[d], dtype=np.float64).reshape(self.face_shape(d))
         L.check(getattr(L.lib(), fn)(self.h, _ptrs(keep, 8), _ptrs(faces, 3), L.PG_LAYOUT_INTERIOR), fn)
 
-    def _get(self, fn: str):
+    def _get(self, fn: str, out=None):
         nx, ny, nz = self.nx
-        vc = np.zeros((NVAR, nz, ny, nx))
+        if out is None:
+            vc = np.zeros((NVAR, nz, ny, nx))
+            faces = [np.zeros(self.face_shape(d)) if (self.ct and d < self.dims) else None
+                     for d in range(3)]
+        else:
+            vc, faces = out[0], list(out[1]) + [None] * (3 - len(out[1]))
+            if vc.shape != (NVAR, nz, ny, nx) or vc.dtype != np.float64 or not vc.flags.c_contiguous:
+                raise ValueError("out[0] must be a C-contiguous float64 array of shape %s" % ((NVAR, nz, ny, nx),))
+            for d in range(3):
+                want = self.ct and d < self.dims
+                f = faces[d]
+                if want and (f is None or f.shape != self.face_shape(d) or f.dtype != np.float64
+                             or not f.flags.c_contiguous):
+                    raise ValueError("out[1][%d] must be a C-contiguous float64 array of shape %s"
+                                     % (d, self.face_shape(d)))
+                if not want:
+                    faces[d] = None
         views = [vc[q] for q in range(NVAR)]
-        faces = [np.zeros(self.face_shape(d)) if (self.ct and d < self.dims) else None
-                 for d in range(3)]
         L.check(getattr(L.lib(), fn)(self.h, _ptrs(views, 8), _ptrs(faces, 3), L.PG_LAYOUT_INTERIOR), fn)
         return vc, faces
 
     def upload(self, vc: np.ndarray, bs=(None, None, None)):
         self._put("pg_upload", vc, bs)
 
-    def download(self):
-        return self._get("pg_download")
+    def download(self, out=None):
+        """State as (vc [8,nz,ny,nx], faces).  out=(vc, faces) writes into
+        preallocated arrays instead (e.g. pinned host memory, which the
+        device writes in place)."""
+        return self._get("pg_download", out)
 
     # -- differentiation (frozen dt) --
     def tangent_upload(self, dvc: np.ndarray, dbs=(None, None, None)):

@@ -21,6 +21,17 @@ def _s(spec, precision):
 MIXED = ["mixed", "mixed_dw"]
 
 
+def test_integer_conversions_match_hardware():
+    """The mixed path's integer float<->double conversions (they keep the
+    FP64 pipe free for the accumulation) give the hardware conversions'
+    bits: all 2^32 floats widened, 6 * 2^32 doubles narrowed (ties incl.)."""
+    import ctypes as C
+    from pluto_gb300 import _lib as L
+    counts = (C.c_ulonglong * 2)()
+    L.check(L.lib().pg_selftest_conversions(counts), "pg_selftest_conversions")
+    assert list(counts) == [0, 0]
+
+
 # the CTU step (TIME_STEPPING HANCOCK) runs on the FP64 path only
 RK_GOLDENS = [n for n in GOLDEN_NAMES if "_ctu" not in n]
 
