@@ -218,9 +218,9 @@ int pg_abi_version(void);
 
 /* Self-test of the integer float<->double conversions the mixed path uses
    in place of the hardware ones (no reference counterpart): counts[0] =
-   float bit patterns whose widening differs from the hardware conversion
-   (all 2^32 checked), counts[1] = doubles whose round-to-nearest-even
-   narrowing differs (5 * 2^32 near-float and 2^32 wide-exponent patterns,
+   float bit patterns whose widening differs from the IEEE conversion
+   (PTX cvt.f64.f32 without flush-to-zero; all 2^32 checked), counts[1] =
+   doubles whose round-to-nearest-even narrowing differs from cvt.rn.f32.f64 (5 * 2^32 near-float and 2^32 wide-exponent patterns,
    ties included).  NaN matches any NaN.  Both are 0 on a correct build.
    Runs on the current device, about a second. */
 int pg_selftest_conversions(unsigned long long counts[2]);

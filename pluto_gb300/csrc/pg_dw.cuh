@@ -84,34 +84,72 @@ __device__ __forceinline__ dw dw_div(dw x, dw y) {  // DWDivDW2 (Alg. 17)
 
 __device__ __forceinline__ float dw_to_float(dw x) { return __fadd_rn(x.hi, x.lo); }
 
-// Exact float -> double from the IEEE-754 fields with integer operations:
-// sign kept, exponent rebiased (127 -> 1023), the 23 fraction bits shifted to
-// the top of the 52.  GB300 issues the hardware conversion on its FP64 pipe
-// (about as costly as a DADD there); this form issues on the integer pipes.
-// Subnormal inputs take the hardware conversion.  NaN payloads are kept.
+// Exact float -> double from the IEEE-754 fields with integer operations
+// only: sign kept; a normal number has its exponent rebiased (127 -> 1023)
+// and its 23 fraction bits moved to the top of the 52; a subnormal one,
+// frac * 2^-149 with its leading one at bit p, becomes the normal double
+// 2^(p-149) * 1.f (exponent field p + 874, the bits below p shifted up to
+// the top of the fraction); zero stays zero; Inf/NaN keep the all-ones
+// exponent and the fraction bits.  GB300 issues the hardware conversion on
+// its FP64 pipe (about as costly as a DADD there); every case here is
+// integer work and the compiler turns the cases into selects.
 __device__ __forceinline__ double widen(float f) {
   const unsigned u = __float_as_uint(f);
+  const unsigned sign = u & 0x80000000u;
   const unsigned e = (u >> 23) & 0xffu, frac = u & 0x7fffffu;
-  if (e == 0u && frac != 0u) return (double)f;
-  const unsigned ex = e == 0u ? 0u : (e == 0xffu ? 0x7ffu : e + 896u);
-  const unsigned hi = (u & 0x80000000u) | (ex << 20) | (frac >> 3);
-  return __hiloint2double((int)hi, (int)(u << 29));
+  unsigned hi, lo;
+  if (e - 1u < 254u) {  // normal
+    hi = sign | ((e + 896u) << 20) | (frac >> 3);
+    lo = frac << 29;
+  } else if (e == 0xffu) {  // Inf / NaN
+    hi = sign | 0x7ff00000u | (frac >> 3);
+    lo = frac << 29;
+  } else if (frac == 0u) {  // zero
+    hi = sign;
+    lo = 0u;
+  } else {  // subnormal
+    const unsigned p = 31u - (unsigned)__clz((int)frac);
+    const unsigned long long m = (unsigned long long)(frac ^ (1u << p)) << (52u - p);
+    hi = sign | ((p + 874u) << 20) | (unsigned)(m >> 32);
+    lo = (unsigned)m;
+  }
+  return __hiloint2double((int)hi, (int)lo);
 }
 
-// double -> float with round-to-nearest-even, from the fields: for results
-// whose exponent lies in the normal float range the top 23 fraction bits are
-// kept and the 29 dropped bits decide the rounding (above half, or exactly
-// half with an odd last bit, adds one ulp; the carry may step the exponent,
-// up to infinity).  Zero, subnormal, out-of-range and non-finite values take
-// the hardware conversion.
+// double -> float with round-to-nearest-even from the fields, integer
+// operations only.  Normal results (double exponent 897..1150): the top 23
+// fraction bits are kept and the 29 dropped bits round (above half, or
+// exactly half with an odd last bit, adds one ulp; the carry may step the
+// exponent, up to infinity).  Smaller magnitudes: the 53-bit significand
+// shifted to units of 2^-149 and rounded the same way gives the subnormal
+// (or zero, or smallest normal) encoding directly.  Exponents above the float
+// range give infinity; Inf stays Inf and NaN gives a quiet NaN.
 __device__ __forceinline__ float narrow(double d) {
   const unsigned hi = (unsigned)__double2hiint(d), lo = (unsigned)__double2loint(d);
+  const unsigned sign = hi & 0x80000000u;
   const unsigned e = (hi >> 20) & 0x7ffu;
-  if (e - 897u > 253u) return (float)d;
-  unsigned r = (hi & 0x80000000u) | ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
-  const unsigned rest = lo & 0x1fffffffu;
-  r += (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) ? 1u : 0u;
-  return __uint_as_float(r);
+  unsigned r;
+  if (e - 897u <= 253u) {  // normal float result
+    r = ((e - 896u) << 23) | ((hi & 0xfffffu) << 3) | (lo >> 29);
+    const unsigned rest = lo & 0x1fffffffu;
+    r += (rest > 0x10000000u || (rest == 0x10000000u && (r & 1u))) ? 1u : 0u;
+  } else if (e == 0x7ffu) {  // Inf / NaN
+    r = ((hi & 0xfffffu) | lo) ? 0x7fc00000u : 0x7f800000u;
+  } else if (e > 1150u) {  // overflow
+    r = 0x7f800000u;
+  } else if (e == 0u) {  // zero or double subnormal: far below half the smallest float
+    r = 0u;
+  } else {  // subnormal float result (or a round-up to the smallest normal)
+    const unsigned long long s = (1ull << 52) | ((unsigned long long)(hi & 0xfffffu) << 32) | lo;
+    const unsigned sh = 926u - e;  // >= 30
+    if (sh > 63u) {
+      r = 0u;
+    } else {
+      const unsigned long long q = s >> sh, rem = s & ((1ull << sh) - 1ull), half = 1ull << (sh - 1u);
+      r = (unsigned)q + ((rem > half || (rem == half && (q & 1ull))) ? 1u : 0u);
+    }
+  }
+  return __uint_as_float(sign | r);
 }
 
 // Accumulator traits: the mixed path is instantiated with native double or

@@ -970,6 +970,20 @@ __device__ __forceinline__ bool same_bits_f(float a, float b) {
   return __float_as_uint(a) == __float_as_uint(b) || (a != a && b != b);
 }
 
+// IEEE conversions without flush-to-zero (this unit is compiled with
+// --use_fast_math, under which the compiler's own conversions flush
+// subnormals): the reference the integer forms are checked against.
+__device__ __forceinline__ double cvt_f64_f32(float f) {
+  double d;
+  asm("cvt.f64.f32 %0, %1;" : "=d"(d) : "f"(f));
+  return d;
+}
+__device__ __forceinline__ float cvt_rn_f32_f64(double d) {
+  float f;
+  asm("cvt.rn.f32.f64 %0, %1;" : "=f"(f) : "d"(d));
+  return f;
+}
+
 // widen over every float bit pattern; narrow over doubles built from each
 // float pattern with five choices of the 29 bits below float precision
 // (zero, exactly half, half - 1, half + 1, a hash) and over doubles with the
@@ -981,7 +995,7 @@ __global__ void k_selftest_conv(unsigned long long* bad) {
        q += stride) {
     const unsigned u = (unsigned)q;
     const float f = __uint_as_float(u);
-    const double h = (double)f;
+    const double h = cvt_f64_f32(f);
     nw += same_bits_d(widen(f), h) ? 0 : 1;
     const unsigned hash = (u * 2654435761u) ^ (u >> 13);
     const unsigned long long top = (unsigned long long)__double_as_longlong(h) & ~0x1fffffffull;
@@ -989,12 +1003,12 @@ __global__ void k_selftest_conv(unsigned long long* bad) {
 #pragma unroll
     for (int p = 0; p < 5; p++) {
       const double d = __longlong_as_double((long long)(top | pats[p]));
-      nn += same_bits_f(narrow(d), (float)d) ? 0 : 1;
+      nn += same_bits_f(narrow(d), cvt_rn_f32_f64(d)) ? 0 : 1;
     }
     const unsigned long long e2 = (unsigned long long)((hash >> 7) & 0x7ffu);
     const unsigned long long wide = (top & 0x800fffffffffffffull) | (e2 << 52) | (hash & 0x1fffffffu);
     const double d2 = __longlong_as_double((long long)wide);
-    nn += same_bits_f(narrow(d2), (float)d2) ? 0 : 1;
+    nn += same_bits_f(narrow(d2), cvt_rn_f32_f64(d2)) ? 0 : 1;
   }
   if (nw) atomicAdd(&bad[0], nw);
   if (nn) atomicAdd(&bad[1], nn);

@@ -23,8 +23,9 @@ MIXED = ["mixed", "mixed_dw"]
 
 def test_integer_conversions_match_hardware():
     """The mixed path's integer float<->double conversions (they keep the
-    FP64 pipe free for the accumulation) give the hardware conversions'
-    bits: all 2^32 floats widened, 6 * 2^32 doubles narrowed (ties incl.)."""
+    FP64 pipe free for the accumulation) give the IEEE conversions' bits
+    (subnormals included): all 2^32 floats widened, 6 * 2^32 doubles
+    narrowed (ties included)."""
     import ctypes as C
     from pluto_gb300 import _lib as L
     counts = (C.c_ulonglong * 2)()
