@@ -149,6 +149,8 @@ def kernel_bytes(name, n, stage_mix=True):
         "mixed_sweep_x": (ext, 32 + 4 + 20 + 2 + 8 + 12),
         "mixed_sweep_y": (ext, 32 + 4 + 40 + 4 + 8 + 12),
         "mixed_sweep_z": (ext, 32 + 4 + 40 + 4 + 8 + 12),
+        "mixed_sweep_y_tma": (ext, 32 + 4 + 40 + 4 + 8 + 12),
+        "mixed_sweep_z_tma": (ext, 32 + 4 + 40 + 4 + 8 + 12),
         "mixed_emf": (edges, 24 + 36 + 12 + 12 + 12),
         "mixed_face": (edges, 12 + 12 + 6 + 12),
         "mixed_final": (cells, 32 + 20 + 12 + 16 + 2 + 32),

@@ -287,6 +287,8 @@ static int enqueue_step(Solver* S) {
 static int read_scalars(Solver* S) {
   CK(cudaMemcpyAsync(S->sc_host, S->sc, sizeof(DevScalars), cudaMemcpyDeviceToHost, S->stream));
   CK(cudaStreamSynchronize(S->stream));
+  if (S->sc_host->status & 8)
+    return fail(PG_ERR_TIMEOUT, "a sweep's wait for its TMA-staged tile ran out (the step's results are invalid)");
   if (S->sc_host->status & 2)
     return fail(PG_ERR_NAN, "Roe solver: negative sound speed squared (Src/MHD/roe.c stops the run here)");
   if (S->sc_host->status) return fail(PG_ERR_NAN, "non-finite inverse time step (NaN or Inf in the state)");

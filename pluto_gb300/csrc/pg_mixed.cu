@@ -27,6 +27,7 @@
 #include "pg_dw.cuh"
 #include "pg_bound_ct.cuh"
 #include "pg_xfer.cuh"
+#include "pg_tma.cuh"
 
 namespace pg {
 
@@ -352,6 +353,159 @@ __global__ void __launch_bounds__(32 * kTY, 2) k_msweep_t(MixArgs a, int solver,
   }
 }
 
+
+// ---------------------------------------------------------------------------
+// y/z sweep with TMA staging (used when the row pitch is a multiple of 16
+// bytes): the tile and arithmetic of k_msweep_t, run by persistent blocks
+// over all tiles.  One thread issues the bulk tensor loads of the block's
+// next tile -- the stencil rows of the 8 variables (one 4D box), the
+// accumulated update and C_dt of the updated rows, the normal face field of
+// the interface rows -- into the other half of a double buffer, completed on
+// an mbarrier, so they land while the block solves the current tile.
+// ---------------------------------------------------------------------------
+struct SweepMaps {
+  CUtensorMap V, dU, CDT, B;
+};
+
+template <int RS>
+struct SweepTile {
+  static constexpr int REACH = rs_ghost_reach(RS);
+  static constexpr int R = kTY + 2 * REACH;  // stencil rows
+  static constexpr int NU = kTY - 2;         // updated rows
+  static constexpr int NF = kTY - 1;         // interface rows
+  static constexpr int BUF = (8 * R + 8 * NU + NU + NF) * 32;  // floats per buffer
+  static constexpr int SMEM = (2 * BUF + (NV + NV + 2) * kTY * 32) * 4 + 16;
+};
+
+template <int RS, int DIR, bool CT>
+__global__ void __launch_bounds__(32 * kTY, 2)
+    k_msweep_tma(const __grid_constant__ SweepMaps maps, MixArgs a, int solver, int xa, int i_lo, int i_n, int o_lo,
+                 int nbx, int ncols, int ntiles, int stage1) {
+  using TL = SweepTile<RS>;
+  constexpr int REACH = TL::REACH, R = TL::R, NU = TL::NU, NF = TL::NF, BUF = TL::BUF;
+  extern __shared__ __align__(128) float smem[];
+  float* svm = smem + 2 * BUF;        // [NV][kTY][32]
+  float* sf = svm + NV * kTY * 32;    // [NV + 2][kTY][32]
+  uint64_t* bar = (uint64_t*)(sf + (NV + 2) * kTY * 32);
+  const Geom& g = a.g;
+  const int tx = threadIdx.x, ty = threadIdx.y;
+  const bool leader = tx == 0 && ty == 0;
+  const int beg = g.beg[DIR], end = g.end[DIR];
+  const int s = DIR == 1 ? g.nt[0] : g.nt[0] * g.nt[1];
+  const float scrh = a.sc->dtdx[DIR];
+  const uint32_t tx_bytes = (uint32_t)((8 * R + 8 * NU + (stage1 ? NU : 0) + (CT ? NF : 0)) * 32 * 4);
+  if (leader) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto issue = [&](int t, int b) {
+    const int col = t % ncols, rb = t / ncols;
+    const int x0 = xa + 32 * (col % nbx), other = o_lo + col / nbx;
+    const int m0 = beg + NU * rb;
+    float* base = smem + b * BUF;
+    mbar_arrive_expect_tx(&bar[b], tx_bytes);
+    if (DIR == 1) {
+      tma_load_4d(base, &maps.V, x0, m0 - 1 - REACH, other, 0, &bar[b]);
+      tma_load_4d(base + 8 * R * 32, &maps.dU, x0, m0, other, 0, &bar[b]);
+      if (stage1) tma_load_3d(base + (8 * R + 8 * NU) * 32, &maps.CDT, x0, m0, other, &bar[b]);
+      if (CT) tma_load_3d(base + (8 * R + 9 * NU) * 32, &maps.B, x0, m0 - 1, other, &bar[b]);
+    } else {
+      tma_load_4d(base, &maps.V, x0, other, m0 - 1 - REACH, 0, &bar[b]);
+      tma_load_4d(base + 8 * R * 32, &maps.dU, x0, other, m0, 0, &bar[b]);
+      if (stage1) tma_load_3d(base + (8 * R + 8 * NU) * 32, &maps.CDT, x0, other, m0, &bar[b]);
+      if (CT) tma_load_3d(base + (8 * R + 9 * NU) * 32, &maps.B, x0, other, m0 - 1, &bar[b]);
+    }
+  };
+  int it = 0;
+  if (leader && (int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
+    const int b = it & 1;
+    const int tn = t + gridDim.x;
+    if (leader && tn < ntiles) {
+      fence_proxy_async_smem();  // buffer b^1 was read by the block in the previous iteration
+      issue(tn, b ^ 1);
+    }
+    const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1));
+    if (__syncthreads_or(!ok)) {
+      // a load did not complete in time: report, let the copies in flight
+      // land (bounded), leave
+      if (leader) {
+        atomicOr(&a.sc->status, 8);
+        mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1));
+        if (tn < ntiles) mbar_wait_bounded(&bar[b ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+      }
+      __syncthreads();
+      return;
+    }
+    const int col = t % ncols, rb = t / ncols;
+    const int i = xa + 32 * (col % nbx) + tx;
+    const int other = o_lo + col / nbx;
+    const int m = beg + NU * rb - 1 + ty;
+    const bool col_ok = i >= i_lo && i < i_lo + i_n;
+    const bool cell_ok = col_ok && m <= end + 1;
+    const bool face_ok = col_ok && m <= end && ty < kTY - 1;
+    const bool upd = ty >= 1 && ty <= kTY - 2 && col_ok && m >= beg && m <= end;
+    const int c = (DIR == 1 ? (other * g.nt[1]) * g.nt[0] + i : other * g.nt[0] + i) + m * s;
+    const float* sV = smem + b * BUF;
+    const float* sDU = sV + 8 * R * 32;
+    const float* sCDT = sDU + 8 * NU * 32;
+    const float* sB = sCDT + NU * 32;
+    float vp[NV], vm[NV];
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) {
+      vp[nv] = vm[nv] = 0.f;
+      if (cell_ok) {
+        const float* q = sV + (nv * R + ty + REACH) * 32 + tx;
+        const float w2 = RS == RS_PPM ? q[-64] : 0.f;
+        const float e2 = RS == RS_PPM ? q[64] : 0.f;
+        recon<RS>(a.limiter, nv, w2, q[-32], q[0], q[32], e2, vp[nv], vm[nv]);
+      }
+      svm[(nv * kTY + ty) * 32 + tx] = vm[nv];
+    }
+    if (CT && cell_ok)
+      for (int comp = 0; comp < g.dims; comp++) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+    __syncthreads();
+    float fl[NV], pr = 0.f, cm = 0.f;
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) fl[nv] = 0.f;
+    if (face_ok) {
+      float vR[NV];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) vR[nv] = svm[(nv * kTY + ty + 1) * 32 + tx];
+      const float bn = CT ? sB[ty * 32 + tx] : 0.f;
+      Iface<float> o;
+      solve_iface<DIR, CT>(a, solver, vp, vR, bn, o);
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) fl[nv] = o.f[nv];
+      pr = o.press;
+      cm = o.cmax;
+      if (CT) {
+        a.S[DIR][0][c] = pmax(0.f, -o.SL);
+        a.S[DIR][1][c] = pmax(0.f, o.SR);
+      }
+    }
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) sf[(nv * kTY + ty) * 32 + tx] = fl[nv];
+    sf[(NV * kTY + ty) * 32 + tx] = pr;
+    sf[((NV + 1) * kTY + ty) * 32 + tx] = cm;
+    __syncthreads();
+    if (upd) {
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        if (!((a.accmask >> nv) & 1)) continue;
+        float rhs = -scrh * (fl[nv] - sf[(nv * kTY + ty - 1) * 32 + tx]);
+        if (nv == Rot<DIR>::vn) rhs -= scrh * (pr - sf[(NV * kTY + ty - 1) * 32 + tx]);
+        a.dU[nv][c] = sDU[(nv * NU + ty - 1) * 32 + tx] + rhs;
+      }
+      if (stage1)
+        a.CDT[c] = sCDT[(ty - 1) * 32 + tx] + 0.5f * (sf[((NV + 1) * kTY + ty - 1) * 32 + tx] + cm) * a.inv_dx_f[DIR];
+    }
+    __syncthreads();  // the buffer and the exchange arrays are free again
+  }
+}
+
 // ---------------------------------------------------------------------------
 // edge EMFs (FP32)
 // ---------------------------------------------------------------------------
@@ -635,7 +789,71 @@ __global__ void k_m1d_dt(MixArgs a, Box dom) {
 struct MixedState {
   MixBufs b;
   int cur = 0;  // buffer holding the state at the start of the next step
+  // TMA tensor maps of the y/z sweeps (tma: maps encoded, kernels configured)
+  bool tma = false;
+  SweepMaps ymaps[2], zmaps[2];  // per state buffer (V, face field); dU, CDT shared
 };
+
+// Tensor maps and shared-memory opt-in of the TMA sweeps; false leaves the
+// solver on k_msweep_t.  Needs a row pitch that is a multiple of 16 bytes,
+// V and dU each one block of 8 arrays, and PLUTO_GB300_SWEEP_TMA not "0".
+template <int RS, bool CT>
+static bool mixed_prepare_tma_rs(Solver* S, MixedState* M) {
+  const Geom& g = S->g;
+  using TL = SweepTile<RS>;
+  if (cudaFuncSetAttribute(k_msweep_tma<RS, 1, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, TL::SMEM) !=
+          cudaSuccess ||
+      (g.dims > 2 &&
+       cudaFuncSetAttribute(k_msweep_tma<RS, 2, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, TL::SMEM) !=
+           cudaSuccess)) {
+    cudaGetLastError();
+    return false;
+  }
+  const uint64_t d4[4] = {(uint64_t)g.nt[0], (uint64_t)g.nt[1], (uint64_t)g.nt[2], 8};
+  const uint64_t s4[3] = {(uint64_t)g.nt[0] * 4, (uint64_t)g.nt[0] * g.nt[1] * 4, (uint64_t)g.ncell * 4};
+  for (int dir = 1; dir < g.dims; dir++) {
+    auto box = [&](int rows, int r) {  // box of `rows` along dir
+      return dir == 1 ? (r == 1 ? (uint32_t)rows : 1u) : (r == 2 ? (uint32_t)rows : 1u);
+    };
+    for (int sb = 0; sb < 2; sb++) {
+      SweepMaps& m = dir == 1 ? M->ymaps[sb] : M->zmaps[sb];
+      const uint32_t bv[4] = {32, box(TL::R, 1), box(TL::R, 2), 8};
+      const uint32_t bu[4] = {32, box(TL::NU, 1), box(TL::NU, 2), 8};
+      const uint32_t bc[3] = {32, box(TL::NU, 1), box(TL::NU, 2)};
+      const uint32_t bf[3] = {32, box(TL::NF, 1), box(TL::NF, 2)};
+      if (!encode_f32_map(&m.V, M->b.V[sb][0], 4, d4, s4, bv)) return false;
+      if (!encode_f32_map(&m.dU, M->b.dU[0], 4, d4, s4, bu)) return false;
+      if (!encode_f32_map(&m.CDT, M->b.CDT, 3, d4, s4, bc)) return false;
+      if (CT && !encode_f32_map(&m.B, M->b.Bs[sb][dir], 3, d4, s4, bf)) return false;
+      if (!CT) m.B = m.CDT;  // unused
+    }
+  }
+  return true;
+}
+
+static bool mixed_prepare_tma(Solver* S, MixedState* M) {
+  const char* env = getenv("PLUTO_GB300_SWEEP_TMA");
+  if (env && env[0] == '0') return false;
+  const Geom& g = S->g;
+  if (g.dims < 2 || (g.nt[0] % 4) != 0) return false;
+  const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
+  int rs;
+  if (S->cfg.reconstruction == PG_PARABOLIC) rs = RS_PPM;
+  else if (S->cfg.limiter == PG_MC_LIM) rs = RS_PLM_MC;
+  else if (S->cfg.limiter == PG_MINMOD_LIM) rs = RS_PLM_MINMOD;
+  else if (S->cfg.limiter == PG_VANLEER_LIM) rs = RS_PLM_VANLEER;
+  else rs = RS_PLM_GENERIC;
+  switch (rs) {
+    case RS_PLM_MC: return ct ? mixed_prepare_tma_rs<RS_PLM_MC, true>(S, M) : mixed_prepare_tma_rs<RS_PLM_MC, false>(S, M);
+    case RS_PLM_MINMOD:
+      return ct ? mixed_prepare_tma_rs<RS_PLM_MINMOD, true>(S, M) : mixed_prepare_tma_rs<RS_PLM_MINMOD, false>(S, M);
+    case RS_PLM_VANLEER:
+      return ct ? mixed_prepare_tma_rs<RS_PLM_VANLEER, true>(S, M) : mixed_prepare_tma_rs<RS_PLM_VANLEER, false>(S, M);
+    case RS_PPM: return ct ? mixed_prepare_tma_rs<RS_PPM, true>(S, M) : mixed_prepare_tma_rs<RS_PPM, false>(S, M);
+    default:
+      return ct ? mixed_prepare_tma_rs<RS_PLM_GENERIC, true>(S, M) : mixed_prepare_tma_rs<RS_PLM_GENERIC, false>(S, M);
+  }
+}
 
 int mixed_alloc(Solver* S) {
   MixedState* M = new MixedState();
@@ -648,11 +866,18 @@ int mixed_alloc(Solver* S) {
     return PG_OK;
   };
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
+  // V of each state buffer and dU: one block of 8 arrays each (the TMA
+  // sweeps read all 8 through one 4D tensor map)
+  auto al8 = [&](float** p) -> int {
+    float* base = nullptr;
+    if (cudaMalloc(&base, 8 * n * sizeof(float)) != cudaSuccess) return PG_ERR_NOMEM;
+    cudaMemset(base, 0, 8 * n * sizeof(float));
+    for (int nv = 0; nv < 8; nv++) p[nv] = base + nv * n;
+    return PG_OK;
+  };
   for (int s = 0; s < 2; s++)
-    for (int nv = 0; nv < 8; nv++)
-      if (al(&M->b.V[s][nv])) return PG_ERR_NOMEM;
-  for (int nv = 0; nv < 8; nv++)
-    if (al(&M->b.dU[nv])) return PG_ERR_NOMEM;
+    if (al8(M->b.V[s])) return PG_ERR_NOMEM;
+  if (al8(M->b.dU)) return PG_ERR_NOMEM;
   if (al(&M->b.CDT)) return PG_ERR_NOMEM;
   if (ct) {
     for (int d = 0; d < S->g.dims; d++) {
@@ -678,6 +903,7 @@ int mixed_alloc(Solver* S) {
   }
   if (cudaMalloc(&M->b.flag, n) != cudaSuccess) return PG_ERR_NOMEM;
   cudaMemset(M->b.flag, 0, n);
+  M->tma = mixed_prepare_tma(S, M);
   return PG_OK;
 }
 
@@ -687,9 +913,8 @@ void mixed_free(Solver* S) {
   auto f = [](void* p) {
     if (p) cudaFree(p);
   };
-  for (int s = 0; s < 2; s++)
-    for (int nv = 0; nv < 8; nv++) f(M->b.V[s][nv]);
-  for (int nv = 0; nv < 8; nv++) f(M->b.dU[nv]);
+  for (int s = 0; s < 2; s++) f(M->b.V[s][0]);  // blocks of 8 arrays
+  f(M->b.dU[0]);
   f(M->b.CDT);
   f(M->b.flag);
   for (int d = 0; d < 3; d++) {
@@ -799,10 +1024,31 @@ static void mlaunch_sweeps_rs(Solver* S, const MixArgs& a, int stage) {
     PG_LAUNCH(S, "mixed_sweep_x", (k_msweep_x<RS, CT><<<grid_for(threads, 128), 128, 0, st>>>(
                                       a, solver, t_lo, t_n, b_lo, nrows, stage1, g.dims == 1, nwx)));
   }
+  MixedState* M = (MixedState*)S->mixed;
   for (int dir = 1; dir < g.dims; dir++) {
     int i_lo = g.beg[0] - ext, i_n = g.nx[0] + 2 * ext;
     int oax = dir == 1 ? 2 : 1;
     int o_lo = oax < g.dims ? g.beg[oax] - ext : 0, o_n = oax < g.dims ? g.nx[oax] + 2 * ext : 1;
+    if (M->tma) {
+      using TL = SweepTile<RS>;
+      const int sb = a.Vin[0] == M->b.V[0][0] ? 0 : 1;
+      const SweepMaps& maps = dir == 1 ? M->ymaps[sb] : M->zmaps[sb];
+      const int xa = i_lo & ~3;  // tiles start on 16-byte boundaries
+      const int nbt = (i_n + (i_lo - xa) + 31) / 32;
+      const int nrb = (g.nx[dir] + 2 + TL::NU - 1) / TL::NU;  // rows reach cell end+1
+      const int ncols = nbt * o_n, ntiles = ncols * nrb;
+      int nsm = 152, dv = 0;
+      if (cudaGetDevice(&dv) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dv);
+      const int grid = ntiles < 2 * nsm ? ntiles : 2 * nsm;
+      dim3 block(32, kTY);
+      if (dir == 1)
+        PG_LAUNCH(S, "mixed_sweep_y_tma", (k_msweep_tma<RS, 1, CT><<<grid, block, TL::SMEM, st>>>(
+                                          maps, a, solver, xa, i_lo, i_n, o_lo, nbt, ncols, ntiles, stage1)));
+      else
+        PG_LAUNCH(S, "mixed_sweep_z_tma", (k_msweep_tma<RS, 2, CT><<<grid, block, TL::SMEM, st>>>(
+                                          maps, a, solver, xa, i_lo, i_n, o_lo, nbt, ncols, ntiles, stage1)));
+      continue;
+    }
     int nbx = (i_n + 31) / 32;
     int nblk = (g.nx[dir] + 2 + kTY - 3) / (kTY - 2);  // rows reach cell end+1
     dim3 grid((unsigned)(nbx * o_n), (unsigned)nblk), block(32, kTY);

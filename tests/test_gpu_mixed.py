@@ -33,6 +33,43 @@ def test_integer_conversions_match_hardware():
     assert list(counts) == [0, 0]
 
 
+def _tma_cases():
+    from pluto_gb300 import problems as P
+    out = {}
+    spec, vc, f = P.blast3d(32)                                 # PLM/MC + HLLD + CT, pitch 36
+    out["blast3d_plm_ct"] = (spec, vc, f)
+    spec, vc, f = P.turbulence3d(26)                             # PPM + RK3 + CT, pitch 32
+    out["turb3d_ppm_rk3"] = (spec, vc, f)
+    spec, vc, f = P.orszag_tang(36)                              # 2D, y sweep only
+    out["ot2d_roe_minmod"] = (dict(spec, solver="roe", limiter="MINMOD_LIM"), vc, f)
+    spec, vc, f = P.blast3d(28)
+    out["blast3d_noct_hll_outflow"] = (dict(spec, ct=False, solver="hll", bc="outflow"), vc, f)
+    return out
+
+
+@pytest.mark.parametrize("prec", MIXED)
+@pytest.mark.parametrize("case", ["blast3d_plm_ct", "turb3d_ppm_rk3", "ot2d_roe_minmod",
+                                  "blast3d_noct_hll_outflow"])
+def test_tma_sweeps_bitwise_equal_to_plain_sweeps(case, prec, monkeypatch):
+    """The TMA-staged persistent y/z sweeps compute exactly what the
+    directly-loading sweeps compute (same tile, same arithmetic)."""
+    spec, vc, f = _tma_cases()[case]
+    out, names = {}, {}
+    for tma in ("1", "0"):
+        monkeypatch.setenv("PLUTO_GB300_SWEEP_TMA", tma)
+        s = _s(spec, prec)
+        s.upload(vc, f)
+        names[tma] = set(s.profile_kernels(1, spec["first_dt"], spec["cfl"]))
+        s.upload(vc, f)
+        s.run(6, spec["first_dt"], spec["cfl"])
+        out[tma] = s.download()
+    assert "mixed_sweep_y_tma" in names["1"] and "mixed_sweep_y_tma" not in names["0"], names
+    assert np.array_equal(out["1"][0], out["0"][0])
+    for d in range(3):
+        if out["0"][1][d] is not None:
+            assert np.array_equal(out["1"][1][d], out["0"][1][d])
+
+
 # the CTU step (TIME_STEPPING HANCOCK) runs on the FP64 path only
 RK_GOLDENS = [n for n in GOLDEN_NAMES if "_ctu" not in n]
 
