@@ -176,6 +176,9 @@ template <> struct Acc<double> {
   static __device__ __forceinline__ float tof(T a) { return narrow(a); }
   static __device__ __forceinline__ bool neg(T a) { return a < 0.0; }
   static __device__ __forceinline__ T konst(double hi, float, float) { return hi; }
+  // element q of a resident accumulator array
+  static __device__ __forceinline__ T ld(const void* p, long long q) { return ((const double*)p)[q]; }
+  static __device__ __forceinline__ void st(void* p, long long q, T v) { ((double*)p)[q] = v; }
 };
 
 template <> struct Acc<dw> {
@@ -191,6 +194,11 @@ template <> struct Acc<dw> {
   static __device__ __forceinline__ float tof(T a) { return dw_to_float(a); }
   static __device__ __forceinline__ bool neg(T a) { return a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f); }
   static __device__ __forceinline__ T konst(double, float hi, float lo) { return {hi, lo}; }
+  static __device__ __forceinline__ T ld(const void* p, long long q) {
+    const float2 f = ((const float2*)p)[q];
+    return {f.x, f.y};
+  }
+  static __device__ __forceinline__ void st(void* p, long long q, T v) { ((float2*)p)[q] = make_float2(v.hi, v.lo); }
 };
 
 }  // namespace pg

@@ -41,6 +41,10 @@ struct MixBufs {
   float* CDT;
   unsigned char* flag;
   float* Bm1[3];  // face -1 layers (outflow sides under CT)
+  // Resident conserved accumulators in the accumulator type (FP64, or FP32
+  // pairs for PG_MIXED_DW), 8 arrays each: U[0] the state at the start of the
+  // step, U[1] the stage result (PLUTO keeps the same pair, d->Uc and U0).
+  void* U[2];
 };
 
 struct MixArgs {
@@ -57,6 +61,8 @@ struct MixArgs {
   float* E[3];
   float* CDT;
   unsigned char* flag;
+  void* U0;  // conserved state at the start of the step (accumulator type)
+  void* Us;  // conserved stage result
   DevScalars* sc;
   float gamma;
   float inv_dx_f[3];
@@ -642,12 +648,20 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
     const Geom& g = a.g;
     const long long c = cidx(g, k, j, i);
     const T inv_gmm1 = O::konst(a.inv_gmm1_d, a.inv_gmm1_hi, a.inv_gmm1_lo);
-    float vin[NV];
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) vin[nv] = a.Vin[nv][c];
-    ConsA<A> u = cons_of<A>(vin, inv_gmm1);
-    // U += dU (flux differences of all directions, FP32) in A
+    const long long n = g.ncell;
     const int msk = a.accmask;
+    // the resident accumulators: U of the previous stage (stage 1: of the
+    // step start); the cell field under CT comes from the faces below
+    const void* Uin = STAGE == 1 ? a.U0 : a.Us;
+    ConsA<A> u;
+    u.rho = O::ld(Uin, RHO * n + c);
+    u.E = O::ld(Uin, ENG * n + c);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      u.m[d] = O::ld(Uin, (VX1 + d) * n + c);
+      u.b[d] = (msk & (1 << (BX1 + d))) ? O::ld(Uin, (BX1 + d) * n + c) : O::from(0.f);
+    }
+    // U += dU (flux differences of all directions, FP32) in A
     if (msk & (1 << RHO)) u.rho = O::addf(u.rho, a.dU[RHO][c]);
 #pragma unroll
     for (int d = 0; d < 3; d++) {
@@ -656,10 +670,14 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
     }
     if (msk & (1 << ENG)) u.E = O::addf(u.E, a.dU[ENG][c]);
     if (STAGE >= 2) {
-      float v0[NV];
+      ConsA<A> u0;
+      u0.rho = O::ld(a.U0, RHO * n + c);
+      u0.E = O::ld(a.U0, ENG * n + c);
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) v0[nv] = a.V0[nv][c];
-      ConsA<A> u0 = cons_of<A>(v0, inv_gmm1);
+      for (int d = 0; d < 3; d++) {
+        u0.m[d] = O::ld(a.U0, (VX1 + d) * n + c);
+        u0.b[d] = (msk & (1 << (BX1 + d))) ? O::ld(a.U0, (BX1 + d) * n + c) : O::from(0.f);
+      }
       if (STAGE == 2 && NSTAGE == 2) {
         u.rho = O::mulf(O::add(u0.rho, u.rho), 0.5f);
         u.E = O::mulf(O::add(u0.E, u.E), 0.5f);
@@ -710,9 +728,19 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
       fl = FLAG_CONS2PRIM_FAIL;
     }
     float p = O::tof(O::mulf(O::sub(u.E, kinb2), a.gamma - 1.0f));
-    if (p < 0.f) {
+    if (p < 0.f) {  // floor and recompute the energy (Src/MHD/mappers.c:190-200)
       p = (float)a.small_p;
+      u.E = O::add(O::mulf(inv_gmm1, (float)a.small_p), kinb2);
       fl = FLAG_CONS2PRIM_FAIL;
+    }
+    // the accumulators of the next stage (the last stage: of the next step)
+    void* Uout = STAGE == NSTAGE ? a.U0 : a.Us;
+    O::st(Uout, RHO * n + c, u.rho);
+    O::st(Uout, ENG * n + c, u.E);
+#pragma unroll
+    for (int d = 0; d < 3; d++) {
+      O::st(Uout, (VX1 + d) * n + c, u.m[d]);
+      if (msk & (1 << (BX1 + d))) O::st(Uout, (BX1 + d) * n + c, u.b[d]);
     }
     float out[NV] = {rho_f, vel[0], vel[1], vel[2], O::tof(u.b[0]), O::tof(u.b[1]), O::tof(u.b[2]), p};
 #pragma unroll
@@ -736,6 +764,30 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
   unsigned ball = __ballot_sync(0xffffffffu, fails);
   if ((threadIdx.x & 31) == 0 && ball) atomicAdd(&a.sc->nfail, (unsigned long long)__popc(ball));
   if (__any_sync(0xffffffffu, bad) && (threadIdx.x & 31) == 0) atomicOr(&a.sc->status, 1);
+}
+
+// U0 from the primitive state (PrimToCons in the accumulator type), after
+// the host set the state.
+template <class A>
+__global__ void k_mcons_init(MixArgs a, Box dom) {
+  using O = Acc<A>;
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= dom.count()) return;
+  int i, j, k;
+  dom.coords(q, i, j, k);
+  const Geom& g = a.g;
+  const long long c = cidx(g, k, j, i), n = g.ncell;
+  float v[NV];
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) v[nv] = a.Vin[nv][c];
+  const ConsA<A> u = cons_of<A>(v, O::konst(a.inv_gmm1_d, a.inv_gmm1_hi, a.inv_gmm1_lo));
+  O::st(a.U0, RHO * n + c, u.rho);
+  O::st(a.U0, ENG * n + c, u.E);
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    O::st(a.U0, (VX1 + d) * n + c, u.m[d]);
+    O::st(a.U0, (BX1 + d) * n + c, u.b[d]);
+  }
 }
 
 // 1D time step: max over interfaces of cmax/dx, every stage
@@ -903,6 +955,10 @@ int mixed_alloc(Solver* S) {
   }
   if (cudaMalloc(&M->b.flag, n) != cudaSuccess) return PG_ERR_NOMEM;
   cudaMemset(M->b.flag, 0, n);
+  for (int u = 0; u < 2; u++) {  // 8 bytes per element for double and for FP32 pairs
+    if (cudaMalloc(&M->b.U[u], 8 * n * 8) != cudaSuccess) return PG_ERR_NOMEM;
+    cudaMemset(M->b.U[u], 0, 8 * n * 8);
+  }
   M->tma = mixed_prepare_tma(S, M);
   return PG_OK;
 }
@@ -917,6 +973,8 @@ void mixed_free(Solver* S) {
   f(M->b.dU[0]);
   f(M->b.CDT);
   f(M->b.flag);
+  f(M->b.U[0]);
+  f(M->b.U[1]);
   for (int d = 0; d < 3; d++) {
     for (int s = 0; s < 2; s++) f(M->b.Bs[s][d]);
     f(M->b.S[d][0]);
@@ -951,6 +1009,8 @@ static MixArgs margs(Solver* S, int in_buf, int out_buf, int v0_buf) {
   }
   a.CDT = M->b.CDT;
   a.flag = M->b.flag;
+  a.U0 = M->b.U[0];
+  a.Us = M->b.U[1];
   a.sc = S->sc;
   a.gamma = (float)S->cfg.gamma;
   a.gamma_d = S->cfg.gamma;
@@ -1201,7 +1261,21 @@ static int mixed_xfer(Solver* S, const double* const vars[8], double* const outv
 }
 
 int mixed_upload_host(Solver* S, const double* const vars[8], const double* const faces[3], int layout) {
-  return mixed_xfer(S, vars, nullptr, faces, nullptr, layout, true);
+  int rc = mixed_xfer(S, vars, nullptr, faces, nullptr, layout, true);
+  if (rc) return rc;
+  MixedState* M = (MixedState*)S->mixed;
+  const MixArgs a = margs(S, M->cur, M->cur, M->cur);
+  Box dom;
+  for (int ax = 0; ax < 3; ax++) {
+    dom.lo[ax] = S->g.beg[ax];
+    dom.hi[ax] = S->g.end[ax];
+  }
+  if (S->cfg.precision == PG_MIXED_DW)
+    k_mcons_init<dw><<<grid_for(dom.count()), kThreads, 0, S->stream>>>(a, dom);
+  else
+    k_mcons_init<double><<<grid_for(dom.count()), kThreads, 0, S->stream>>>(a, dom);
+  if (cudaGetLastError() != cudaSuccess || cudaStreamSynchronize(S->stream) != cudaSuccess) return PG_ERR_CUDA;
+  return PG_OK;
 }
 int mixed_download(Solver* S, double* const vars[8], double* const faces[3], int layout) {
   return mixed_xfer(S, nullptr, vars, nullptr, faces, layout, false);
