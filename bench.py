@@ -149,6 +149,7 @@ def kernel_bytes(name, n, stage_mix=True):
         "mixed_sweep_x": (ext, 32 + 4 + 20 + 2 + 8 + 12),
         "mixed_sweep_y": (ext, 32 + 4 + 40 + 4 + 8 + 12),
         "mixed_sweep_z": (ext, 32 + 4 + 40 + 4 + 8 + 12),
+        "mixed_sweep_x_tma": (ext, 32 + 4 + 20 + 2 + 8 + 12),
         "mixed_sweep_y_tma": (ext, 32 + 4 + 40 + 4 + 8 + 12),
         "mixed_sweep_z_tma": (ext, 32 + 4 + 40 + 4 + 8 + 12),
         "mixed_emf": (edges, 24 + 36 + 12 + 12 + 12),

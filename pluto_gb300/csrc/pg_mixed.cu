@@ -273,6 +273,139 @@ __global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_l
 }
 
 // ---------------------------------------------------------------------------
+// x sweep with TMA staging: tiles of kXR rows (consecutive j at one k) by
+// kXC chunks of 30 cells; warp r walks row r chunk by chunk with the lane
+// arithmetic of k_msweep_x (32 reconstructions, 31 interfaces, 30 updated
+// cells per chunk).  The rows' stencil (8 variables, one 4D box kXW floats
+// wide, starting on a 16-byte boundary) and normal face field of the next
+// tile are loaded by TMA into the other half of a double buffer.
+// ---------------------------------------------------------------------------
+constexpr int kXR = 8, kXC = 4, kXW = 136;
+
+struct XSweepMaps {
+  CUtensorMap V, B;
+};
+
+constexpr int kXBUF = (8 + 1) * kXR * kXW;                  // floats per buffer
+constexpr int kXSMEM = 2 * kXBUF * 4 + 16;
+
+template <int RS, bool CT>
+__global__ void __launch_bounds__(32 * kXR, 2)
+    k_msweep_x_tma(const __grid_constant__ XSweepMaps maps, MixArgs a, int solver, int t_lo, int t_n, int b_lo,
+                   int nxt, int njt, int ntiles, int stage1) {
+  constexpr int REACH = rs_ghost_reach(RS);
+  extern __shared__ __align__(128) float smem[];
+  uint64_t* bar = (uint64_t*)(smem + 2 * kXBUF);
+  const Geom& g = a.g;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const bool leader = threadIdx.x == 0;
+  const float scrh = a.sc->dtdx[0];
+  const int nt0 = g.nt[0];
+  const uint32_t tx_bytes = (uint32_t)((8 + (CT ? 1 : 0)) * kXR * kXW * 4);
+  if (leader) {
+    mbar_init(&bar[0], 1);
+    mbar_init(&bar[1], 1);
+    fence_mbar_init();
+  }
+  __syncthreads();
+  auto tile_of = [&](int t, int& cs, int& xs, int& j0, int& k) {
+    const int xt = t % nxt, rest = t / nxt;
+    cs = g.beg[0] - 1 + 30 * kXC * xt;  // first cell of the tile
+    xs = (cs - REACH) & ~3;
+    j0 = t_lo + kXR * (rest % njt);
+    k = b_lo + rest / njt;
+  };
+  auto issue = [&](int t, int b) {
+    int cs, xs, j0, k;
+    tile_of(t, cs, xs, j0, k);
+    float* base = smem + b * kXBUF;
+    mbar_arrive_expect_tx(&bar[b], tx_bytes);
+    tma_load_4d(base, &maps.V, xs, j0, k, 0, &bar[b]);
+    if (CT) tma_load_3d(base + 8 * kXR * kXW, &maps.B, xs, j0, k, &bar[b]);
+  };
+  int it = 0;
+  if (leader && (int)blockIdx.x < ntiles) issue(blockIdx.x, 0);
+  for (int t = blockIdx.x; t < ntiles; t += gridDim.x, it++) {
+    const int b = it & 1;
+    const int tn = t + gridDim.x;
+    if (leader && tn < ntiles) {
+      fence_proxy_async_smem();
+      issue(tn, b ^ 1);
+    }
+    const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1));
+    if (__syncthreads_or(!ok)) {
+      if (leader) {
+        atomicOr(&a.sc->status, 8);
+        mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1));
+        if (tn < ntiles) mbar_wait_bounded(&bar[b ^ 1], (uint32_t)(((it + 1) >> 1) & 1));
+      }
+      __syncthreads();
+      return;
+    }
+    int cs, xs, j0, k;
+    tile_of(t, cs, xs, j0, k);
+    const int j = j0 + w;
+    const bool row_ok = j < t_lo + t_n;
+    const float* sV = smem + b * kXBUF + w * kXW;   // row w of variable 0
+    const float* sB = smem + b * kXBUF + 8 * kXR * kXW + w * kXW;
+    for (int q = 0; q < kXC; q++) {
+      const int i = cs + 30 * q + lane;
+      const bool cell_ok = row_ok && i <= g.end[0] + 1;
+      const bool face_ok = row_ok && i <= g.end[0] && lane < 31;
+      const int c = (k * g.nt[1] + j) * nt0 + i;
+      const int x = i - xs;  // column in the staged rows
+      float vp[NV], vm[NV];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        vp[nv] = vm[nv] = 0.f;
+        if (cell_ok) {
+          const float* p = sV + nv * kXR * kXW + x;
+          const float w2 = RS == RS_PPM ? p[-2] : 0.f;
+          const float e2 = RS == RS_PPM ? p[2] : 0.f;
+          recon<RS>(a.limiter, nv, w2, p[-1], p[0], p[1], e2, vp[nv], vm[nv]);
+        }
+      }
+      if (CT && cell_ok)
+        for (int comp = 0; comp < g.dims; comp++) a.DV[0][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+      float vR[NV];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) vR[nv] = __shfl_down_sync(0xffffffffu, vm[nv], 1);
+      float fl[NV], pr = 0.f, cm = 0.f;
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) fl[nv] = 0.f;
+      if (face_ok) {
+        Iface<float> o;
+        solve_iface<0, CT>(a, solver, vp, vR, CT ? sB[x] : 0.f, o);
+#pragma unroll
+        for (int nv = 0; nv < NV; nv++) fl[nv] = o.f[nv];
+        pr = o.press;
+        cm = o.cmax;
+        if (CT) {
+          a.S[0][0][c] = pmax(0.f, -o.SL);
+          a.S[0][1][c] = pmax(0.f, o.SR);
+        }
+      }
+      float flm[NV];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) flm[nv] = __shfl_up_sync(0xffffffffu, fl[nv], 1);
+      const float prm = __shfl_up_sync(0xffffffffu, pr, 1);
+      const float cmm = __shfl_up_sync(0xffffffffu, cm, 1);
+      if (row_ok && lane >= 1 && lane <= 30 && i >= g.beg[0] && i <= g.end[0]) {
+#pragma unroll
+        for (int nv = 0; nv < NV; nv++) {
+          if (!((a.accmask >> nv) & 1)) continue;
+          float rhs = -scrh * (fl[nv] - flm[nv]);
+          if (nv == VX1) rhs -= scrh * (pr - prm);
+          a.dU[nv][c] = rhs;
+        }
+        if (stage1) a.CDT[c] = 0.5f * (cmm + cm) * a.inv_dx_f[0];
+      }
+    }
+    __syncthreads();  // the buffer is free again
+  }
+}
+
+// ---------------------------------------------------------------------------
 // y/z sweep: block = 32 lanes along x by kTY rows along DIR.  Row ty holds
 // cell m = m0 - 1 + ty: every row reconstructs its cell once (left states of
 // the row above go through shared memory), rows 0..kTY-2 solve interface
@@ -844,6 +977,7 @@ struct MixedState {
   // TMA tensor maps of the y/z sweeps (tma: maps encoded, kernels configured)
   bool tma = false;
   SweepMaps ymaps[2], zmaps[2];  // per state buffer (V, face field); dU, CDT shared
+  XSweepMaps xmaps[2];
 };
 
 // Tensor maps and shared-memory opt-in of the TMA sweeps; false leaves the
@@ -861,8 +995,20 @@ static bool mixed_prepare_tma_rs(Solver* S, MixedState* M) {
     cudaGetLastError();
     return false;
   }
+  if (cudaFuncSetAttribute(k_msweep_x_tma<RS, CT>, cudaFuncAttributeMaxDynamicSharedMemorySize, kXSMEM) !=
+      cudaSuccess) {
+    cudaGetLastError();
+    return false;
+  }
   const uint64_t d4[4] = {(uint64_t)g.nt[0], (uint64_t)g.nt[1], (uint64_t)g.nt[2], 8};
   const uint64_t s4[3] = {(uint64_t)g.nt[0] * 4, (uint64_t)g.nt[0] * g.nt[1] * 4, (uint64_t)g.ncell * 4};
+  for (int sb = 0; sb < 2; sb++) {
+    const uint32_t bv[4] = {kXW, kXR, 1, 8};
+    const uint32_t bf[3] = {kXW, kXR, 1};
+    if (!encode_f32_map(&M->xmaps[sb].V, M->b.V[sb][0], 4, d4, s4, bv)) return false;
+    if (CT && !encode_f32_map(&M->xmaps[sb].B, M->b.Bs[sb][0], 3, d4, s4, bf)) return false;
+    if (!CT) M->xmaps[sb].B = M->xmaps[sb].V;  // unused
+  }
   for (int dir = 1; dir < g.dims; dir++) {
     auto box = [&](int rows, int r) {  // box of `rows` along dir
       return dir == 1 ? (r == 1 ? (uint32_t)rows : 1u) : (r == 2 ? (uint32_t)rows : 1u);
@@ -1075,7 +1221,20 @@ static void mlaunch_sweeps_rs(Solver* S, const MixArgs& a, int stage) {
   const int solver = S->cfg.riemann;
   const int ext = CT ? 1 : 0;
   const int stage1 = (stage == 1) ? 1 : 0;
-  {  // x sweep over rows (j,k) of the transverse-extended box
+  MixedState* M = (MixedState*)S->mixed;
+  if (M->tma) {  // x sweep, TMA-staged tiles of kXR rows by kXC chunks
+    const int t_lo = g.beg[1] - ext, t_n = g.nx[1] + 2 * ext;
+    const int b_lo = g.dims > 2 ? g.beg[2] - ext : 0, b_n = g.dims > 2 ? g.nx[2] + 2 * ext : 1;
+    const int nxt = (g.nx[0] + 2 + 30 * kXC - 1) / (30 * kXC);  // chunks reach cell end+1
+    const int njt = (t_n + kXR - 1) / kXR;
+    const int ntiles = nxt * njt * b_n;
+    int nsm = 152, dv = 0;
+    if (cudaGetDevice(&dv) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dv);
+    const int grid = ntiles < 2 * nsm ? ntiles : 2 * nsm;
+    const int sb = a.Vin[0] == M->b.V[0][0] ? 0 : 1;
+    PG_LAUNCH(S, "mixed_sweep_x_tma", (k_msweep_x_tma<RS, CT><<<grid, 32 * kXR, kXSMEM, st>>>(
+                                          M->xmaps[sb], a, solver, t_lo, t_n, b_lo, nxt, njt, ntiles, stage1)));
+  } else {  // x sweep over rows (j,k) of the transverse-extended box
     int t_lo = g.dims > 1 ? g.beg[1] - ext : 0, t_n = g.dims > 1 ? g.nx[1] + 2 * ext : 1;
     int b_lo = g.dims > 2 ? g.beg[2] - ext : 0, b_n = g.dims > 2 ? g.nx[2] + 2 * ext : 1;
     int nwx = (g.nx[0] + 2 + 29) / 30;  // lanes reach cell end+1
@@ -1084,7 +1243,6 @@ static void mlaunch_sweeps_rs(Solver* S, const MixArgs& a, int stage) {
     PG_LAUNCH(S, "mixed_sweep_x", (k_msweep_x<RS, CT><<<grid_for(threads, 128), 128, 0, st>>>(
                                       a, solver, t_lo, t_n, b_lo, nrows, stage1, g.dims == 1, nwx)));
   }
-  MixedState* M = (MixedState*)S->mixed;
   for (int dir = 1; dir < g.dims; dir++) {
     int i_lo = g.beg[0] - ext, i_n = g.nx[0] + 2 * ext;
     int oax = dir == 1 ? 2 : 1;

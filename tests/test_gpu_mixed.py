@@ -50,24 +50,30 @@ def _tma_cases():
 @pytest.mark.parametrize("prec", MIXED)
 @pytest.mark.parametrize("case", ["blast3d_plm_ct", "turb3d_ppm_rk3", "ot2d_roe_minmod",
                                   "blast3d_noct_hll_outflow"])
-def test_tma_sweeps_bitwise_equal_to_plain_sweeps(case, prec, monkeypatch):
-    """The TMA-staged persistent y/z sweeps compute exactly what the
-    directly-loading sweeps compute (same tile, same arithmetic)."""
+def test_tma_sweeps_match_plain_sweeps(case, prec, monkeypatch):
+    """The TMA-staged persistent sweeps are deterministic and compute what the
+    directly-loading sweeps compute: same tiles and arithmetic, equal to FP32
+    round-off (the compiler may contract a multiply-add differently in the
+    two kernels, so single ulps can differ and then spread)."""
     spec, vc, f = _tma_cases()[case]
     out, names = {}, {}
-    for tma in ("1", "0"):
-        monkeypatch.setenv("PLUTO_GB300_SWEEP_TMA", tma)
+    for tma in ("1", "1b", "0"):
+        monkeypatch.setenv("PLUTO_GB300_SWEEP_TMA", tma[0])
         s = _s(spec, prec)
         s.upload(vc, f)
         names[tma] = set(s.profile_kernels(1, spec["first_dt"], spec["cfl"]))
         s.upload(vc, f)
         s.run(6, spec["first_dt"], spec["cfl"])
         out[tma] = s.download()
-    assert "mixed_sweep_y_tma" in names["1"] and "mixed_sweep_y_tma" not in names["0"], names
-    assert np.array_equal(out["1"][0], out["0"][0])
+    for k in ("mixed_sweep_x_tma", "mixed_sweep_y_tma"):
+        assert k in names["1"] and k not in names["0"], names
+    assert np.array_equal(out["1"][0], out["1b"][0])
+    errs = {q: rel_l1(out["1"][0][q], out["0"][0][q]) for q in range(8) if np.abs(out["0"][0][q]).sum() > 0}
     for d in range(3):
         if out["0"][1][d] is not None:
-            assert np.array_equal(out["1"][1][d], out["0"][1][d])
+            assert np.array_equal(out["1"][1][d], out["1b"][1][d])
+            errs[f"b{d}"] = rel_l1(out["1"][1][d], out["0"][1][d])
+    assert max(errs.values()) <= 1e-6, errs
 
 
 # the CTU step (TIME_STEPPING HANCOCK) runs on the FP64 path only
