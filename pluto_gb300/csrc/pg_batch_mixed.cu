@@ -41,7 +41,7 @@ static cudaError_t launch_mixed_a(const BatchArgs<float>& b, int rs, int solver,
 cudaError_t launch_batch_mixed(const BatchArgs<float>& b, bool use_dw, int rs, int solver, int nstage, int nsteps,
                                int grid, int threads, cudaStream_t st) {
   if (use_dw) return launch_mixed_a<pg::dw>(b, rs, solver, nstage, nsteps, grid, threads, st);
-  return launch_mixed_a<double>(b, rs, solver, nstage, nsteps, grid, threads, st);
+  return launch_mixed_a<pg::f64hw>(b, rs, solver, nstage, nsteps, grid, threads, st);
 }
 
 }  // namespace pg

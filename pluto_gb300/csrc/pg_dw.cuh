@@ -181,6 +181,23 @@ template <> struct Acc<double> {
   static __device__ __forceinline__ void st(void* p, long long q, T v) { ((double*)p)[q] = v; }
 };
 
+// FP64 accumulators with the hardware conversions, for kernels that are not
+// bound by the FP64 pipe (the batched tubes): there the integer forms only
+// add issue slots and registers.
+struct f64hw {};
+template <> struct Acc<f64hw> : Acc<double> {
+  static __device__ __forceinline__ T from(float a) { return (double)a; }
+  static __device__ __forceinline__ T prod(float a, float b) { return (double)a * (double)b; }
+  static __device__ __forceinline__ T addf(T a, float b) { return a + (double)b; }
+  static __device__ __forceinline__ T mulf(T a, float b) { return a * (double)b; }
+  static __device__ __forceinline__ T div(T a, T b) {
+    double r = (double)__frcp_rn((float)b);
+    r = fma(r, fma(-b, r, 1.0), r);
+    return a * r;
+  }
+  static __device__ __forceinline__ float tof(T a) { return (float)a; }
+};
+
 template <> struct Acc<dw> {
   using T = dw;
   static __device__ __forceinline__ T from(float a) { return {a, 0.f}; }
