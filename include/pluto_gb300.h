@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PG_ABI_VERSION 1
+#define PG_ABI_VERSION 2  /* 2: pg_config gained bc_hi / bc_sides */
 
 /* status codes */
 enum {
@@ -73,11 +73,15 @@ typedef struct {
   int time_stepping;
   int divb;
   int emf_average;
-  int bc[3];            /* same type on both sides of an axis */
+  int bc[3];            /* boundary type per axis (the beginning side, X*_BEG,
+                           and the end side too unless bc_sides is 1) */
   int precision;        /* PG_FP64: bit-compatible with the reference C path */
   int compute_mach;     /* 1: also reduce g_maxMach (two extra sqrt per face) */
   double small_density; /* g_smallDensity (0 -> 1e-12) */
   double small_pressure;/* g_smallPressure (0 -> 1e-12) */
+  int bc_hi[3];         /* type of the end side (X*_END) when bc_sides is 1 */
+  int bc_sides;         /* 0: bc[d] on both sides; 1: bc[d] / bc_hi[d] per side
+                           (PERIODIC must then be on both sides of an axis) */
 } pg_config;
 
 typedef struct {

@@ -72,7 +72,7 @@ class Setup:
     n: tuple = (32, 32, 1)
     lo: tuple = (0.0, 0.0, 0.0)
     hi: tuple = (1.0, 1.0, 1.0)
-    bc: str = "periodic"
+    bc: object = "periodic"       # one type, or a (beg, end) pair per axis
     cfl: float = 0.4
     first_dt: float = 1e-4
     steps: int = 20
@@ -119,8 +119,13 @@ def pluto_ini(s: Setup) -> str:
         g.append(f"X{d+1}-grid    1    {_fmt(lo)}    {n}    u    {_fmt(hi)}")
     bcs = []
     for d in range(3):
-        t = s.bc if d < s.dims else "outflow"
-        bcs.append(f"X{d+1}-beg        {t}\nX{d+1}-end        {t}")
+        if d >= s.dims:
+            lo = hi = "outflow"
+        elif isinstance(s.bc, (list, tuple)):
+            lo, hi = s.bc[d]
+        else:
+            lo = hi = s.bc
+        bcs.append(f"X{d+1}-beg        {lo}\nX{d+1}-end        {hi}")
     par = "\n".join(f"{k}    {_fmt(v)}" for k, v in s.params.items())
     return f"""[Grid]
 

@@ -810,7 +810,7 @@ static void boundary(oc_problem *p) {
   int is, nv;
   int dims = p->c.dims;
   for (is = 0; is < 2 * dims; is++) {
-    int d = is / 2, type = p->c.bc[d];
+    int d = is / 2, type = (is & 1) ? p->c.bc_hi[d] : p->c.bc[d]; /* X*_BEG, X*_END */
     int ib = 0, ie = p->nt[0] - 1, jb = 0, je = p->nt[1] - 1, kb = 0, ke = p->nt[2] - 1;
     if (is == 0) { ib = p->beg[0] - 1; ie = 0; }
     else if (is == 1) { ib = p->end[0] + 1; ie = p->nt[0] - 1; }
@@ -1752,8 +1752,11 @@ oc_problem *oc_create(const oc_config *cfg) {
   int d, nv;
   p->c = *cfg;
   if (cfg->ct && cfg->dims < 2) { free(p); return NULL; }
-  for (d = 0; d < 3; d++)
+  for (d = 0; d < 3; d++) {
     if (cfg->bc[d] < OC_PERIODIC || cfg->bc[d] > OC_EQTSYMMETRIC) { free(p); return NULL; }
+    if (cfg->bc_hi[d] < OC_PERIODIC || cfg->bc_hi[d] > OC_EQTSYMMETRIC) { free(p); return NULL; }
+    if ((cfg->bc[d] == OC_PERIODIC) != (cfg->bc_hi[d] == OC_PERIODIC)) { free(p); return NULL; }
+  }
   p->ng = cfg->recon == OC_PARABOLIC ? 3 : 2; /* Src/get_nghost.c:28-104 */
   if (cfg->stepping == OC_HANCOCK) {
     if (cfg->recon != OC_LINEAR) { free(p); return NULL; } /* hancock.c:64-67 */

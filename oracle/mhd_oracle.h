@@ -38,9 +38,10 @@ typedef struct {
   double gamma;
   int recon, limiter, solver, stepping;
   int ct;              /* 1: constrained transport (EMF average in emf) */
-  int bc[3];           /* boundary type per dim (same on both sides) */
+  int bc[3];           /* boundary type per dim, beginning side (X*-beg) */
   int nthreads;        /* OpenMP threads (0: runtime default) */
   int emf;             /* CT_EMF_AVERAGE (0 = UCT_HLL) */
+  int bc_hi[3];        /* end side (X*-end) */
 } oc_config;
 
 typedef struct oc_problem oc_problem;

@@ -28,7 +28,8 @@ class OcConfig(C.Structure):
     _fields_ = [("dims", C.c_int), ("components", C.c_int), ("nx", C.c_int * 3),
                 ("dx", C.c_double * 3), ("gamma", C.c_double), ("recon", C.c_int),
                 ("limiter", C.c_int), ("solver", C.c_int), ("stepping", C.c_int),
-                ("ct", C.c_int), ("bc", C.c_int * 3), ("nthreads", C.c_int), ("emf", C.c_int)]
+                ("ct", C.c_int), ("bc", C.c_int * 3), ("nthreads", C.c_int), ("emf", C.c_int),
+                ("bc_hi", C.c_int * 3)]
 
 
 _lib = None
@@ -76,8 +77,12 @@ class Oracle:
         for d in range(3):
             c.nx[d] = int(spec["nx"][d]) if d < spec["dims"] else 1
             c.dx[d] = float(spec["dx"][d])
+            # one type for every side, one per axis, or a (beg, end) pair per axis
             bc = spec.get("bc", "periodic")
-            c.bc[d] = BC[bc[d] if isinstance(bc, (list, tuple)) else bc]
+            t = bc[d] if isinstance(bc, (list, tuple)) else bc
+            lo, hi = (t[0], t[1]) if isinstance(t, (list, tuple)) else (t, t)
+            c.bc[d] = BC[lo]
+            c.bc_hi[d] = BC[hi]
         c.gamma = float(spec["gamma"])
         c.recon = RECON[spec["recon"]]
         c.limiter = LIMITER[spec["limiter"]]

@@ -35,6 +35,7 @@ EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", 
            "pg_batch_set_schedule", "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set",
            "pg_adjoint_step", "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load",
            "pg_selftest_conversions"]
+PG_ABI_VERSION = 2  # the pg_config layout these bindings describe
 PG_STATIC_MAX_ZONES = 32768
 PG_MAX_CHECKPOINTS = 256
 
@@ -45,7 +46,8 @@ class PgConfig(C.Structure):
                 ("reconstruction", C.c_int), ("limiter", C.c_int), ("riemann", C.c_int),
                 ("time_stepping", C.c_int), ("divb", C.c_int), ("emf_average", C.c_int),
                 ("bc", C.c_int * 3), ("precision", C.c_int), ("compute_mach", C.c_int),
-                ("small_density", C.c_double), ("small_pressure", C.c_double)]
+                ("small_density", C.c_double), ("small_pressure", C.c_double),
+                ("bc_hi", C.c_int * 3), ("bc_sides", C.c_int)]
 
 
 class PgStepInfo(C.Structure):
@@ -117,6 +119,9 @@ def lib():
                "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set", "pg_adjoint_step",
                "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load", "pg_selftest_conversions"):
         getattr(L, fn).restype = C.c_int
+    if L.pg_abi_version() != PG_ABI_VERSION:
+        raise OSError(f"libpluto_gb300 has ABI version {L.pg_abi_version()}, these bindings expect "
+                      f"{PG_ABI_VERSION}: rebuild the library")
     _lib = L
     return L
 

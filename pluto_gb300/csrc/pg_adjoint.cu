@@ -580,7 +580,7 @@ __global__ void k_adj_bound(Geom g, BoundTab t, int narr, int bcx, int bcy, int 
   for (int d = 0; d < g.dims; d++)
     if (x[d] < g.beg[d] || x[d] > g.end[d])
       for (int nv = 0; nv < NV; nv++)
-        if (bc_flip(d, bt[d], nv, ncomp) < 0) flips ^= 1 << nv;
+        if (bc_flip(d, bc_side(bt[d], x[d] > g.end[d]), nv, ncomp) < 0) flips ^= 1 << nv;
   for (int a = 0; a < narr; a++) {
     const double v = t.p[a][c];
     if (v != 0.0) {

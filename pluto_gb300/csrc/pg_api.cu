@@ -33,6 +33,13 @@ extern "C" int pg_selftest_conversions(unsigned long long counts[2]) {
 }
 
 namespace pg {
+// The library's private copy of a validated config keeps both sides' types
+// in bc[d] = beginning | end << 4 (as bc_pack in pg_physics.cuh); PERIODIC on
+// both sides stays 0.
+void pack_bc(pg_config* c) {
+  for (int d = 0; d < 3; d++) c->bc[d] = c->bc[d] | ((c->bc_sides ? c->bc_hi[d] : c->bc[d]) << 4);
+}
+
 int validate_config(const pg_config* c) {
   if (!c) return fail(PG_ERR_INVALID, "null config");
   if (c->dims < 1 || c->dims > 3) return fail(PG_ERR_INVALID, "dims must be 1..3");
@@ -42,6 +49,13 @@ int validate_config(const pg_config* c) {
     if (c->nx[d] < 4) return fail(PG_ERR_INVALID, "nx must be >= 4 on active axes");
     if (!(c->dx[d] > 0)) return fail(PG_ERR_INVALID, "dx must be positive");
     if (c->bc[d] < PG_PERIODIC || c->bc[d] > PG_EQTSYMMETRIC) return fail(PG_ERR_INVALID, "unsupported boundary");
+    if (c->bc_sides != 0 && c->bc_sides != 1) return fail(PG_ERR_INVALID, "bc_sides must be 0 or 1");
+    if (c->bc_sides) {
+      if (c->bc_hi[d] < PG_PERIODIC || c->bc_hi[d] > PG_EQTSYMMETRIC)
+        return fail(PG_ERR_INVALID, "unsupported boundary (end side)");
+      if ((c->bc[d] == PG_PERIODIC) != (c->bc_hi[d] == PG_PERIODIC))
+        return fail(PG_ERR_INVALID, "a periodic axis is periodic on both sides");
+    }
   }
   if (!(c->gamma > 1.0)) return fail(PG_ERR_INVALID, "gamma must be > 1");
   if (c->reconstruction != PG_LINEAR && c->reconstruction != PG_PARABOLIC)
@@ -122,6 +136,7 @@ extern "C" int pg_create(const pg_config* cfg, pg_solver** out) {
   pg_solver* h = new pg_solver();
   Solver* S = &h->S;
   S->cfg = *cfg;
+  pack_bc(&S->cfg);
   init_geom(S);
   cudaError_t e = cudaStreamCreateWithFlags(&S->stream, cudaStreamNonBlocking);
   if (e != cudaSuccess) {

@@ -183,6 +183,7 @@ extern "C" int pg_batch_create(const pg_config* cfg, int ntubes, const int* nx, 
   else if (c.limiter == PG_MINMOD_LIM) rs = 1;
   else if (c.limiter == PG_MC_LIM) rs = 0;
   else return bfail(PG_ERR_INVALID, "pg_batch_create: batch supports PLM minmod/MC and PPM");
+  pack_bc(&c);
   pg_batch* B = new pg_batch();
   B->cfg = c;
   B->rs = rs;

@@ -212,7 +212,7 @@ __device__ double batch_stage(const BatchArgs<T>& b, int tube, T* const* Vin, T*
     int i = gi < ng ? gi : end + 1 + (gi - ng);
     int src = bc_src(i, beg, end, n, b.bc);
     const T v = Vin[nv][base + src];
-    Vin[nv][base + i] = bc_flip(0, b.bc, nv, b.ncomp) < 0 ? -v : v;
+    Vin[nv][base + i] = bc_flip(0, bc_side(b.bc, i > end), nv, b.ncomp) < 0 ? -v : v;
   }
   __syncthreads();
   T cm_max = T(0);

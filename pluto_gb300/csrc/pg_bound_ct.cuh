@@ -73,15 +73,16 @@ __global__ void k_bound_axis(BoundCT<T> a, int type, long long nghost) {
   s[B1] = c[B1];
   s[B2] = c[B2];
   s[AX] = bc_src(c[AX], g.beg[AX], g.end[AX], n, type);
+  const int side = bc_side(type, !lo);  // this ghost's side of the axis
   const long long dst = cidx(g, c[2], c[1], c[0]), src = cidx(g, s[2], s[1], s[0]);
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
     const T v = a.V[nv][src];
-    a.V[nv][dst] = bc_flip(AX, type, nv, a.ncomp) < 0 ? -v : v;
+    a.V[nv][dst] = bc_flip(AX, side, nv, a.ncomp) < 0 ? -v : v;
   }
   for (int fd = 0; fd < a.nbfield; fd++) {
     if (fd != AX) {
-      const bool neg = bc_flip(AX, type, BX1 + fd, a.ncomp) < 0;
+      const bool neg = bc_flip(AX, side, BX1 + fd, a.ncomp) < 0;
       const T v = a.Bs[fd][src];
       a.Bs[fd][dst] = neg ? -v : v;
       if (c[fd] == 0) {  // the -1 layer of this transverse component
@@ -107,14 +108,16 @@ __global__ void k_bound_axis(BoundCT<T> a, int type, long long nghost) {
 }
 
 // One thread per transverse position and side: the normal component marched
-// away from the boundary face, then its cell average.
+// away from the boundary face, then (outflow sides) its cell average.  type:
+// the axis's packed side types.
 template <class T, class C, int AX>
-__global__ void k_fill_normal(BoundCT<T> a, long long ntrans, int average) {
+__global__ void k_fill_normal(BoundCT<T> a, long long ntrans, int type) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= 2 * ntrans) return;
   const Geom& g = a.g;
   constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
   const bool lo = (q & 1) == 0;
+  const bool average = bc_side(type, !lo) == PG_OUTFLOW;
   const long long t = q >> 1;
   int c[3];
   c[B1] = (int)(t % g.nt[B1]);
@@ -176,11 +179,12 @@ static void launch_bound_ct_axis(Solver* S, const BoundCT<T>& b, const char* cop
   const long long nghost = 2LL * g.beg[AX] * ntrans;
   PG_LAUNCH(S, copy_name, (k_bound_axis<T, AX><<<grid_for(nghost), kThreads, 0, S->stream>>>(
                               b, S->cfg.bc[AX], nghost)));
-  // outflow: FillMagneticField + CT_AverageNormalMagField; reflective and
-  // equatorial-symmetric: FillMagneticField only (Src/boundary.c:188-206)
+  // per side, outflow: FillMagneticField + CT_AverageNormalMagField;
+  // reflective and equatorial-symmetric: FillMagneticField only
+  // (Src/boundary.c:188-206)
   if (S->cfg.bc[AX] != PG_PERIODIC)
     PG_LAUNCH(S, fill_name, (k_fill_normal<T, C, AX><<<grid_for(2 * ntrans, 128), 128, 0, S->stream>>>(
-                                b, ntrans, S->cfg.bc[AX] == PG_OUTFLOW ? 1 : 0)));
+                                b, ntrans, S->cfg.bc[AX])));
 }
 
 template <class T, class C>

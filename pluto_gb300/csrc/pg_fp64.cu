@@ -214,6 +214,7 @@ extern "C" int pg_tube_step_static(const pg_config* cfg, const double* v_in, dou
   // of the static array.
   Solver S;
   S.cfg = *cfg;
+  pack_bc(&S.cfg);
   init_geom(&S);
   S.stream = (cudaStream_t)cuda_stream;
   S.device_dt = false;

@@ -125,7 +125,7 @@ __global__ void k_bound(F64A<T> a, int bcx, int bcy, int bcz, long long nslab0, 
   for (int d = 0; d < g.dims; d++)
     if (x[d] < g.beg[d] || x[d] > g.end[d])
       for (int nv = 0; nv < NV; nv++)
-        if (bc_flip(d, bt[d], nv, a.ncomp) < 0) flips ^= 1 << nv;
+        if (bc_flip(d, bc_side(bt[d], x[d] > g.end[d]), nv, a.ncomp) < 0) flips ^= 1 << nv;
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
     const T v = a.V[nv][src];

@@ -87,6 +87,7 @@ void mixed_free(Solver* S);
 int mixed_enqueue_step(Solver* S);
 int mixed_selftest_conversions(unsigned long long counts[2]);
 int validate_config(const pg_config* c);
+void pack_bc(pg_config* c);
 void init_geom(Solver* S);
 void set_last_error(const char* msg);
 // host <-> device copy of one FP64 array in the interior or PLUTO layout

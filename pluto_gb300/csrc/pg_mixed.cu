@@ -189,7 +189,7 @@ __global__ void k_mbound(Geom g, BoundArrays arr, int bcx, int bcy, int bcz, lon
   for (int d = 0; d < g.dims; d++)
     if (x[d] < g.beg[d] || x[d] > g.end[d])
       for (int nv = 0; nv < NV; nv++)
-        if (bc_flip(d, bt[d], nv, arr.ncomp) < 0) flips ^= 1 << nv;
+        if (bc_flip(d, bc_side(bt[d], x[d] > g.end[d]), nv, arr.ncomp) < 0) flips ^= 1 << nv;
   for (int a = 0; a < arr.n; a++) {
     const float v = arr.q[a][src];
     arr.q[a][dst] = (a < NV && ((flips >> a) & 1)) ? -v : v;

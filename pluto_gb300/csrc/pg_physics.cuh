@@ -23,10 +23,23 @@ __host__ __device__ __forceinline__ int bc_flip(int d, int type, int nv, int com
   }
   return nv == 4 + d ? -1 : 1;           // normal field
 }
+// An axis's boundary types packed as beginning | end << 4 (the reference sets
+// them per side, pluto.ini X*-beg / X*-end; PERIODIC on both sides is 0), and
+// the type of one side.
+__host__ __device__ __forceinline__ int bc_pack(int lo, int hi) { return lo | (hi << 4); }
+__host__ __device__ __forceinline__ int bc_side(int packed, bool end_side) {
+  return end_side ? (packed >> 4) & 15 : packed & 15;
+}
 // mirror / image / edge zone that ghost x copies from (Src/boundary.c:439-560)
-__host__ __device__ __forceinline__ int bc_src(int x, int beg, int end, int n, int type) {
-  if (x < beg) return type == 0 ? x + n : (type == 1 ? beg : 2 * beg - x - 1);
-  if (x > end) return type == 0 ? x - n : (type == 1 ? end : 2 * end - x + 1);
+__host__ __device__ __forceinline__ int bc_src(int x, int beg, int end, int n, int packed) {
+  if (x < beg) {
+    const int type = packed & 15;
+    return type == 0 ? x + n : (type == 1 ? beg : 2 * beg - x - 1);
+  }
+  if (x > end) {
+    const int type = (packed >> 4) & 15;
+    return type == 0 ? x - n : (type == 1 ? end : 2 * end - x + 1);
+  }
   return x;
 }
 

@@ -64,8 +64,9 @@ static void gpu_config(pg_config *c, Riemann_Solver *Riemann, Grid *grid)
   for (d = 0; d < 3; d++) {
     c->nx[d] = d < DIMENSIONS ? grid->np_int[d] : 1;
     c->dx[d] = d < DIMENSIONS ? grid->dx[d][grid->nghost[d]] : 1.0;
-    c->bc[d] = d < DIMENSIONS ? gpu_bc(grid->lbound[d]) : PG_PERIODIC;
-    if (d < DIMENSIONS && grid->lbound[d] != grid->rbound[d]) c->bc[d] = -1;
+    c->bc[d]    = d < DIMENSIONS ? gpu_bc(grid->lbound[d]) : PG_PERIODIC;
+    c->bc_hi[d] = d < DIMENSIONS ? gpu_bc(grid->rbound[d]) : PG_PERIODIC;
+    if (c->bc_hi[d] != c->bc[d]) c->bc_sides = 1;
   }
   c->gamma = g_gamma;
 #if RECONSTRUCTION == PARABOLIC

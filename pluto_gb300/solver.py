@@ -39,8 +39,14 @@ def make_config(spec: dict, precision: str = "fp64", compute_mach: bool = False)
     for d in range(3):
         c.nx[d] = int(spec["nx"][d]) if d < c.dims else 1
         c.dx[d] = float(spec["dx"][d]) if d < c.dims else 1.0
+        # "bc": one type for every side, one per axis, or a (beg, end) pair per axis
         bc = spec.get("bc", "periodic")
-        c.bc[d] = BC[bc[d] if isinstance(bc, (list, tuple)) else bc]
+        t = bc[d] if isinstance(bc, (list, tuple)) else bc
+        lo, hi = (t[0], t[1]) if isinstance(t, (list, tuple)) else (t, t)
+        c.bc[d] = BC[lo]
+        c.bc_hi[d] = BC[hi]
+        if lo != hi:
+            c.bc_sides = 1
     c.gamma = float(spec["gamma"])
     c.reconstruction = RECON[spec.get("recon", "LINEAR")]
     c.limiter = LIMITER[spec.get("limiter", "MC_LIM")]

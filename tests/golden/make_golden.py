@@ -4,7 +4,7 @@
 Run in a container that has the reference tree (``PLUTO_REF``, default
 ``/root/reference``) and gcc:
 
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py [name ...]
 
 Each fixture ``<name>.npz`` holds the reference's own initial dump (step 0)
 and its dump after ``steps`` steps, as written by the reference (``.dbl``,
@@ -83,6 +83,15 @@ def setups():
         replace(br.tube_setup(0, 256, 100), bc="reflective", name="tube_reflective_0_256"),
         replace(br.ot_setup("hlld", 32, 30), stepping="HANCOCK", emf="UCT_CONTACT", bc="reflective",
                 name="ot_ctu_reflective_32"),
+        # a different type on each side of an axis (pluto.ini X*-beg / X*-end)
+        replace(br.blast_setup(16, 12), name="blast_sides_16",
+                bc=(("reflective", "outflow"), ("outflow", "eqtsymmetric"), ("periodic", "periodic"))),
+        replace(br.ot_setup("hlld", 32, 30), name="ot_sides_32",
+                bc=(("reflective", "outflow"), ("eqtsymmetric", "reflective"), ("outflow", "outflow"))),
+        replace(br.ot_setup("hlld", 32, 30), stepping="HANCOCK", emf="UCT_CONTACT", name="ot_ctu_sides_32",
+                bc=(("outflow", "reflective"), ("reflective", "outflow"), ("outflow", "outflow"))),
+        replace(br.tube_setup(0, 256, 100), name="tube_sides_0_256",
+                bc=(("reflective", "outflow"), ("outflow", "outflow"), ("outflow", "outflow"))),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4
@@ -90,7 +99,10 @@ def setups():
 
 
 def main():
+    only = set(sys.argv[1:])  # fixture names to (re)make; all when empty
     for s in setups():
+        if only and s.name not in only:
+            continue
         a, b = br.run(s)
         vc0, bs0 = to_arrays(a, s)
         vc1, bs1 = to_arrays(b, s)

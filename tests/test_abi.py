@@ -39,7 +39,8 @@ def test_every_declared_symbol_is_exported(lib):
 
 
 def test_abi_version(lib):
-    assert lib.pg_abi_version() == 1
+    from pluto_gb300 import _lib as L
+    assert lib.pg_abi_version() == L.PG_ABI_VERSION == 2
 
 
 @pytest.mark.parametrize("field,value", [("dims", 4), ("components", 1), ("gamma", 1.0),
@@ -64,6 +65,44 @@ def test_ct_requires_2d_and_accepts_outflow(lib):
                 bc=("outflow", "periodic", "periodic"))
     rc = lib.pg_create(C.byref(make_config(spec)), C.byref(h))
     assert rc != 1
+    if rc == 0:
+        lib.pg_destroy(h)
+
+
+def test_config_layout_matches_header(tmp_path):
+    """The ctypes pg_config matches the C header field by field (offsets and
+    size, from a program compiled against include/pluto_gb300.h)."""
+    import shutil
+    import subprocess
+    from pluto_gb300 import _lib as L
+    cc = shutil.which("gcc") or shutil.which("cc")
+    if not cc:
+        pytest.skip("no C compiler")
+    names = [f[0] for f in L.PgConfig._fields_]
+    src = tmp_path / "layout.c"
+    src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"pluto_gb300.h\"\nint main(void){\n"
+                   + "".join(f'printf("%zu\\n", offsetof(pg_config, {n}));\n' for n in names)
+                   + 'printf("%zu\\n", sizeof(pg_config)); return 0; }\n')
+    exe = tmp_path / "layout"
+    subprocess.run([cc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    want = [getattr(L.PgConfig, n).offset for n in names] + [C.sizeof(L.PgConfig)]
+    assert got == want, dict(zip(names + ["sizeof"], zip(got, want)))
+
+
+@pytest.mark.parametrize("bc,ok", [((("reflective", "outflow"), "periodic", "periodic"), True),
+                                   ((("outflow", "eqtsymmetric"), ("reflective", "outflow"), "periodic"), True),
+                                   ((("periodic", "outflow"), "periodic", "periodic"), False),
+                                   (("periodic", ("reflective", "periodic"), "periodic"), False)])
+def test_boundary_types_per_side(lib, bc, ok):
+    """A different type on each side of an axis is accepted, except that a
+    periodic axis is periodic on both sides (as pluto.ini requires)."""
+    spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1), gamma=5 / 3, ct=True, bc=bc)
+    c = make_config(spec)
+    assert c.bc_sides == 1
+    h = C.c_void_p()
+    rc = lib.pg_create(C.byref(c), C.byref(h))
+    assert (rc != 1) == ok
     if rc == 0:
         lib.pg_destroy(h)
 

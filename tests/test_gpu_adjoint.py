@@ -56,6 +56,9 @@ def _case(name):
     if name == "tube1d_reflective":
         spec, vc, f = P.riemann_tube(48, 1)
         return dict(spec, bc="reflective"), vc, f, [1e-3] * 5
+    if name == "tube1d_sides":
+        spec, vc, f = P.riemann_tube(48, 0)
+        return dict(spec, bc=[("reflective", "outflow"), "outflow", "outflow"]), vc, f, [1e-3] * 5
     if name == "ot2d_mirror_noct":
         spec, vc, f = P.orszag_tang(16)
         return dict(spec, ct=False, bc=["reflective", "eqtsymmetric", "periodic"]), vc, f, [1e-3] * 3
@@ -63,7 +66,8 @@ def _case(name):
 
 
 CASES = ["cpa2d_plm_hlld", "ot2d_plm_hll", "turb3d_ppm_hlld", "turb3d_plm_minmod_hll",
-         "tube1d_outflow", "tube1d_ppm_outflow", "cpa2d_plm_roe", "tube1d_reflective", "ot2d_mirror_noct"]
+         "tube1d_outflow", "tube1d_ppm_outflow", "cpa2d_plm_roe", "tube1d_reflective", "ot2d_mirror_noct",
+         "tube1d_sides"]
 
 
 def _smooth(vc):

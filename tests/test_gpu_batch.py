@@ -26,7 +26,8 @@ def _oracle_run(spec, n, dx, state, nsteps, first_dt):
 
 @pytest.mark.parametrize("recon,stepping,bc", [("LINEAR", "RK2", "outflow"), ("PARABOLIC", "RK3", "outflow"),
                                                ("LINEAR", "RK2", "reflective"),
-                                               ("PARABOLIC", "RK2", "eqtsymmetric")])
+                                               ("PARABOLIC", "RK2", "eqtsymmetric"),
+                                               ("LINEAR", "RK3", [("reflective", "outflow"), "outflow", "outflow"])])
 def test_batch_fp64_matches_oracle_per_tube(recon, stepping, bc):
     from pluto_gb300.batch import Batch
     spec, ns, dxs, states = _family(24, 7, 16, 300)
@@ -44,7 +45,8 @@ def test_batch_fp64_matches_oracle_per_tube(recon, stepping, bc):
 
 def test_batch_fp64_matches_golden_tubes():
     from pluto_gb300.batch import Batch
-    names = ["tube_0_256", "tube_1_200", "tube_2_160", "tube_roe_0_256", "tube_reflective_0_256"]
+    names = ["tube_0_256", "tube_1_200", "tube_2_160", "tube_roe_0_256", "tube_reflective_0_256",
+             "tube_sides_0_256"]
     metas, st0, st1 = [], [], []
     for nm in names:
         meta, vc0, _, vc1, _ = load_golden(nm)

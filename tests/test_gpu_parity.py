@@ -44,7 +44,8 @@ def test_fp64_matches_reference_goldens(name):
                                   "ot_outflow_32", "turb_outflow_12", "ot_ctu_uctc_32",
                                   "ot_ctu_arith_roe_32", "turb_ctu_uctc_12", "tube_ctu_1_200",
                                   "cpa_ctu_outflow_32", "blast_reflective_16", "ot_reflective_32",
-                                  "cpa_eqtsym_32", "tube_reflective_0_256", "ot_ctu_reflective_32"])
+                                  "cpa_eqtsym_32", "tube_reflective_0_256", "ot_ctu_reflective_32",
+                                  "blast_sides_16", "ot_sides_32", "ot_ctu_sides_32", "tube_sides_0_256"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
@@ -117,7 +118,8 @@ def test_fp64_vs_oracle_random_3d(solver, recon, stepping):
 
 @pytest.mark.parametrize("bc", [("outflow", "outflow", "outflow"), ("outflow", "periodic", "outflow"),
                                 ("periodic", "outflow", "periodic"), ("reflective", "eqtsymmetric", "reflective"),
-                                ("eqtsymmetric", "periodic", "outflow")])
+                                ("eqtsymmetric", "periodic", "outflow"),
+                                (("reflective", "outflow"), ("outflow", "eqtsymmetric"), ("eqtsymmetric", "reflective"))])
 def test_fp64_vs_oracle_outflow_ct_3d(bc):
     """Outflow, reflective and equatorial-symmetric sides under CT
     (FillMagneticField, normal averaging on outflow sides, FlipSign mirror
@@ -186,7 +188,9 @@ def test_nan_state_reported_not_trapped():
 
 @pytest.mark.parametrize("emf,solver,bc", [("UCT_CONTACT", "hlld", "periodic"), ("ARITHMETIC", "hll", "outflow"),
                                            ("UCT_CONTACT", "roe", "outflow"),
-                                           ("UCT_CONTACT", "hlld", ["reflective", "periodic", "eqtsymmetric"])])
+                                           ("UCT_CONTACT", "hlld", ["reflective", "periodic", "eqtsymmetric"]),
+                                           ("ARITHMETIC", "roe", [("outflow", "reflective"), "periodic",
+                                                                  ("eqtsymmetric", "outflow")])])
 def test_ctu_vs_oracle_random_3d(emf, solver, bc):
     """CTU (primitive Hancock predictor, corner-coupled corrector) with CT on a
     random 3D state against the oracle, bit for bit."""
