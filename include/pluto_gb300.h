@@ -51,7 +51,7 @@ enum { PG_RK2 = 2, PG_RK3 = 3,                                    /* TIME_STEPPI
 enum { PG_DIVB_NONE = 0, PG_CONSTRAINED_TRANSPORT = 1 };          /* DIVB_CONTROL */
 enum { PG_ARITHMETIC = 1, PG_UCT_CONTACT = 3, PG_UCT_HLL = 4 };   /* CT_EMF_AVERAGE */
 enum { PG_PERIODIC = 0, PG_OUTFLOW = 1, PG_REFLECTIVE = 2,
-       PG_EQTSYMMETRIC = 3 };                                     /* [Boundary] */
+       PG_EQTSYMMETRIC = 3, PG_USERDEF = 4 };                     /* [Boundary] */
 /* arithmetic: PG_FP64 bit-compatible with the reference C path;
    PG_MIXED FP32 storage and fluxes, FP64 accumulation / pressure recovery /
    face update / dt reduction; PG_MIXED_DW the same with the FP64 parts done
@@ -91,6 +91,13 @@ typedef struct {
 } pg_step_info;
 
 typedef struct pg_solver pg_solver;
+
+/* PG_USERDEF sides (PLUTO's UserDefBoundary).  side: 0..5 = X1_BEG, X1_END,
+   X2_BEG, X2_END, X3_BEG, X3_END; vpos: 0 the cell box (CENTER), 1..3 the
+   box of staggered component 1..3 (X1FACE..X3FACE); stage: 1-based index of
+   the boundary fill within the step (g_intStage).  Called on a CUDA host
+   thread, in stream order inside the step: it must not call CUDA. */
+typedef void (*pg_userdef_fn)(void *user, int side, int vpos, int stage);
 
 /* Create a solver; the device state is zero until pg_upload. */
 int pg_create(const pg_config *cfg, pg_solver **out);
@@ -212,6 +219,19 @@ int pg_batch_set_schedule(pg_batch *b, int threads, int blocks_per_sm, int large
 #define PG_STATIC_MAX_ZONES 32768
 int pg_tube_step_static(const pg_config *cfg, const double *v_in, double *v_out, double dt,
                         void *cuda_stream, pg_step_info *info);
+
+/* USERDEF sides: fn is called for every such side at every boundary fill,
+   in the reference's order (Src/boundary.c:258-288: the cell box, then each
+   staggered box; FillMagneticField follows under CT).  vars[8] / faces[3]
+   are the caller's host arrays in PG_LAYOUT_PLUTO (null slots skipped).
+   Before the calls for a side the library writes into them the side's slab
+   -- its ghost layers and as many interior layers, over the whole transverse
+   extent (faces with their -1 layer) -- and after the calls it reads back
+   the boxes the reference hands to UserDefBoundary for that side.  The
+   arrays must stay valid for the solver's life; arrays the device cannot
+   reach are pinned here (cudaHostRegister) and unpinned by pg_destroy.  Not
+   for PG_FP64_TANGENT solvers, batches or the adjoint. */
+int pg_set_userdef(pg_solver *s, pg_userdef_fn fn, void *user, double *const vars[8], double *const faces[3]);
 
 /* Diagnostics */
 int pg_get_stream(pg_solver *s, void **cuda_stream);

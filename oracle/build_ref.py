@@ -78,6 +78,7 @@ class Setup:
     steps: int = 20
     params: dict = field(default_factory=dict)
     init_body: str = ""
+    userdef_body: str = ""          # body of UserDefBoundary (USERDEF sides)
 
 
 def _fmt(x: float) -> str:
@@ -200,7 +201,10 @@ void Analysis (const Data *d, Grid *grid) {}
 void BackgroundField (double x1, double x2, double x3, double *B0)
 { B0[0] = B0[1] = B0[2] = 0.0; }
 #endif
-void UserDefBoundary (const Data *d, RBox *box, int side, Grid *grid) {}
+void UserDefBoundary (const Data *d, RBox *box, int side, Grid *grid)
+{
+%s
+}
 """
 
 
@@ -213,7 +217,7 @@ def build(s: Setup, jobs: int = 8) -> Path:
     obj.mkdir(parents=True, exist_ok=True)
     (run / "definitions.h").write_text(definitions_h(s))
     (run / "pluto.ini").write_text(pluto_ini(s))
-    (run / "init.c").write_text(INIT_TEMPLATE % s.init_body)
+    (run / "init.c").write_text(INIT_TEMPLATE % (s.init_body, s.userdef_body))
     names = list(BASE_SRC)
     names += ["plm_states"] if s.recon == "LINEAR" else ["ppm_states", "ppm_coeffs"]
     # time stepping: RK (rk_step + update_stage) or CTU (ctu_step + hancock)

@@ -40,6 +40,9 @@
 
 struct oc_problem {
   oc_config c;
+  oc_userdef_fn ud_fn;     /* USERDEF sides */
+  void *ud_user;
+  int bstage;              /* boundary fills so far in the step */
   int ng, nt[3], beg[3], end[3];
   size_t ncell, nface[3];
   double inv_dx[3];
@@ -806,6 +809,26 @@ static void ct_average_normal(oc_problem *p, int side) {
       }
 }
 
+/* CT_AverageTransverseMagField, Src/MHD/CT/ct_field_average.c:275-440
+   (Cartesian): the transverse cell-centred field in the ghost zones of side
+   is from the staggered components. */
+static void ct_average_transverse(oc_problem *p, int is) {
+  int d = is / 2, i, j, k, fd;
+  int lo[3] = {0, 0, 0}, hi[3] = {p->nt[0] - 1, p->nt[1] - 1, p->nt[2] - 1};
+  if (is & 1) lo[d] = p->end[d] + 1;
+  else hi[d] = p->beg[d] - 1;
+  for (k = lo[2]; k <= hi[2]; k++)
+    for (j = lo[1]; j <= hi[1]; j++)
+      for (i = lo[0]; i <= hi[0]; i++)
+        for (fd = 0; fd < p->c.dims; fd++) {
+          int o[3] = {0, 0, 0};
+          if (fd == d) continue;
+          o[fd] = 1;
+          p->vc[BX1 + fd][CI(p, k, j, i)] =
+              0.5 * (p->bs[fd][FI(p, fd, k, j, i)] + p->bs[fd][FI(p, fd, k - o[2], j - o[1], i - o[0])]);
+        }
+}
+
 static void boundary(oc_problem *p) {
   int is, nv;
   int dims = p->c.dims;
@@ -818,6 +841,20 @@ static void boundary(oc_problem *p) {
     else if (is == 3) { jb = p->end[1] + 1; je = p->nt[1] - 1; }
     else if (is == 4) { kb = p->beg[2] - 1; ke = 0; }
     else { kb = p->end[2] + 1; ke = p->nt[2] - 1; }
+    if (type == OC_USERDEF) { /* Src/boundary.c:258-288 */
+      int fd;
+      if (p->ud_fn) {
+        p->ud_fn(p->ud_user, is, 0, p->bstage + 1);
+        if (p->c.ct)
+          for (fd = 0; fd < dims; fd++) p->ud_fn(p->ud_user, is, 1 + fd, p->bstage + 1);
+      }
+      if (p->c.ct) { /* Src/boundary.c:287-289 */
+        fill_magnetic_field(p, is);
+        ct_average_normal(p, is);
+        ct_average_transverse(p, is);
+      }
+      continue;
+    }
     for (nv = 0; nv < NV; nv++)
       bound_box(p, p->vc[nv], -1, ib, ie, jb, je, kb, ke, is, type, flip_sign(d, type, nv, p->c.components));
     if (p->c.ct) {
@@ -845,6 +882,7 @@ static void boundary(oc_problem *p) {
       }
     }
   }
+  p->bstage++;
 }
 
 /* ------------------------------------------------------------------ */
@@ -1662,6 +1700,7 @@ int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
   int i, j, k, nv, d;
   size_t c;
 
+  p->bstage = 0;
   if (p->c.stepping == OC_HANCOCK) return oc_advance_ctu(p, dt, inv_dt_hyp, max_mach, nfail);
 
   p->nfail = 0;
@@ -1753,8 +1792,8 @@ oc_problem *oc_create(const oc_config *cfg) {
   p->c = *cfg;
   if (cfg->ct && cfg->dims < 2) { free(p); return NULL; }
   for (d = 0; d < 3; d++) {
-    if (cfg->bc[d] < OC_PERIODIC || cfg->bc[d] > OC_EQTSYMMETRIC) { free(p); return NULL; }
-    if (cfg->bc_hi[d] < OC_PERIODIC || cfg->bc_hi[d] > OC_EQTSYMMETRIC) { free(p); return NULL; }
+    if (cfg->bc[d] < OC_PERIODIC || cfg->bc[d] > OC_USERDEF) { free(p); return NULL; }
+    if (cfg->bc_hi[d] < OC_PERIODIC || cfg->bc_hi[d] > OC_USERDEF) { free(p); return NULL; }
     if ((cfg->bc[d] == OC_PERIODIC) != (cfg->bc_hi[d] == OC_PERIODIC)) { free(p); return NULL; }
   }
   p->ng = cfg->recon == OC_PARABOLIC ? 3 : 2; /* Src/get_nghost.c:28-104 */
@@ -1857,6 +1896,17 @@ static void xfer(oc_problem *p, double *vc, double *bs[3], int to_problem) {
           else bs[d][q] = p->bs[d][f];
         }
   }
+}
+
+void oc_set_userdef(oc_problem *p, oc_userdef_fn fn, void *user) {
+  p->ud_fn = fn;
+  p->ud_user = user;
+}
+
+void oc_arrays(oc_problem *p, double **vc, double **bs) {
+  int q;
+  for (q = 0; q < NV; q++) vc[q] = p->vc[q];
+  for (q = 0; q < 3; q++) bs[q] = p->bs[q];
 }
 
 void oc_set_state(oc_problem *p, const double *vc, const double *bs0,

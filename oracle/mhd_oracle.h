@@ -28,7 +28,12 @@ enum { OC_FLAT_LIM = 0, OC_MINMOD_LIM, OC_VANLEER_LIM, OC_MC_LIM, OC_DEFAULT_LIM
 enum { OC_HLL = 0, OC_HLLD = 1, OC_ROE = 2 };
 enum { OC_RK2 = 2, OC_RK3 = 3, OC_HANCOCK = 4 }; /* HANCOCK: CTU with the primitive Hancock predictor */
 enum { OC_ARITHMETIC = 1, OC_UCT_CONTACT = 3, OC_UCT_HLL = 4 }; /* CT_EMF_AVERAGE */
-enum { OC_PERIODIC = 0, OC_OUTFLOW = 1, OC_REFLECTIVE = 2, OC_EQTSYMMETRIC = 3 };
+enum { OC_PERIODIC = 0, OC_OUTFLOW = 1, OC_REFLECTIVE = 2, OC_EQTSYMMETRIC = 3, OC_USERDEF = 4 };
+
+/* USERDEF sides: called in Boundary's order with side 0..5 (X1_BEG..X3_END),
+   vpos 0 (cell box) then 1..3 (staggered boxes, under CT), stage = index of
+   the boundary fill within the step; writes the problem's own arrays. */
+typedef void (*oc_userdef_fn)(void *user, int side, int vpos, int stage);
 
 typedef struct {
   int dims;            /* DIMENSIONS 1..3 */
@@ -47,6 +52,10 @@ typedef struct {
 typedef struct oc_problem oc_problem;
 
 oc_problem *oc_create(const oc_config *cfg);
+void oc_set_userdef(oc_problem *p, oc_userdef_fn fn, void *user);
+/* the problem's own arrays in PLUTO's layout: vc[8] ghosted cell arrays,
+   bs[3] face arrays (one longer along their axis, -1 layer first) */
+void oc_arrays(oc_problem *p, double **vc, double **bs);
 void oc_destroy(oc_problem *p);
 void oc_set_state(oc_problem *p, const double *vc, const double *bs0,
                   const double *bs1, const double *bs2);

@@ -20,7 +20,7 @@ RECON = {"LINEAR": 0, "PARABOLIC": 1}
 LIMITER = {"FLAT_LIM": 0, "MINMOD_LIM": 1, "VANLEER_LIM": 2, "MC_LIM": 3, "DEFAULT": 4}
 SOLVER = {"hll": 0, "hlld": 1, "roe": 2}
 STEPPING = {"RK2": 2, "RK3": 3, "HANCOCK": 4}
-BC = {"periodic": 0, "outflow": 1, "reflective": 2, "eqtsymmetric": 3}
+BC = {"periodic": 0, "outflow": 1, "reflective": 2, "eqtsymmetric": 3, "userdef": 4}
 EMF = {"ARITHMETIC": 1, "UCT_CONTACT": 3, "UCT_HLL": 4}
 
 
@@ -41,6 +41,9 @@ def build(force: bool = False) -> Path:
     return LIB
 
 
+USERDEF_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int)
+
+
 def lib():
     global _lib
     if _lib is None:
@@ -54,12 +57,25 @@ def lib():
         L.oc_get_state.argtypes = [C.c_void_p, dp, dp, dp, dp]
         L.oc_advance.argtypes = [C.c_void_p, C.c_double, dp, dp, C.POINTER(C.c_int64)]
         L.oc_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, dp, dp]
+        L.oc_set_userdef.argtypes = [C.c_void_p, USERDEF_FN, C.c_void_p]
+        L.oc_arrays.argtypes = [C.c_void_p, C.POINTER(dp), C.POINTER(dp)]
         _lib = L
     return _lib
 
 
 def _ptr(a):
     return None if a is None else a.ctypes.data_as(C.POINTER(C.c_double))
+
+
+class _VarStack:
+    """vc[q] -> the view of variable q (the oracle's cell arrays are separate
+    allocations, so they cannot form one numpy array without a copy)."""
+
+    def __init__(self, views):
+        self.views = views
+
+    def __getitem__(self, q):
+        return self.views[q]
 
 
 class Oracle:
@@ -104,6 +120,28 @@ class Oracle:
     def face_shape(self, d):
         nx, ny, nz = self.nx
         return (nz + (d == 2), ny + (d == 1), nx + (d == 0))
+
+    def set_userdef(self, fn):
+        """USERDEF sides: fn(side, vpos, stage, vc, faces) on numpy views of
+        the oracle's own PLUTO-layout arrays (vc [8, nt2, nt1, nt0], faces[d]
+        one longer along d with the -1 layer first)."""
+        ng = 3 if self.spec["recon"] == "PARABOLIC" else 2
+        if self.spec["stepping"] == "HANCOCK" and self.spec["ct"]:
+            ng += 1
+        nt = [self.nx[d] + 2 * ng if d < self.spec["dims"] else 1 for d in range(3)]
+        dp = C.POINTER(C.c_double)
+        vp, bp = (dp * NVAR)(), (dp * 3)()
+        lib().oc_arrays(self.h, vp, bp)
+        vviews = [np.ctypeslib.as_array(vp[q], shape=(nt[2], nt[1], nt[0])) for q in range(NVAR)]
+        faces = [np.ctypeslib.as_array(bp[d], shape=(nt[2] + (d == 2), nt[1] + (d == 1), nt[0] + (d == 0)))
+                 if (self.spec["ct"] and d < self.spec["dims"]) else None for d in range(3)]
+        self._ud_views = (_VarStack(vviews), faces)
+
+        def cb(user, side, vpos, stage):
+            fn(side, vpos, stage, self._ud_views[0], self._ud_views[1])
+
+        self._ud_cb = USERDEF_FN(cb)
+        lib().oc_set_userdef(self.h, self._ud_cb, None)
 
     def set_state(self, vc: np.ndarray, bs=(None, None, None)):
         vc = np.ascontiguousarray(vc, dtype=np.float64)

@@ -19,7 +19,7 @@ PG_HLL, PG_HLLD, PG_ROE = 0, 1, 2
 PG_RK2, PG_RK3, PG_HANCOCK = 2, 3, 4
 PG_DIVB_NONE, PG_CONSTRAINED_TRANSPORT = 0, 1
 PG_ARITHMETIC, PG_UCT_CONTACT, PG_UCT_HLL = 1, 3, 4
-PG_PERIODIC, PG_OUTFLOW, PG_REFLECTIVE, PG_EQTSYMMETRIC = 0, 1, 2, 3
+PG_PERIODIC, PG_OUTFLOW, PG_REFLECTIVE, PG_EQTSYMMETRIC, PG_USERDEF = 0, 1, 2, 3, 4
 PG_FP64, PG_MIXED, PG_MIXED_DW, PG_FP64_TANGENT = 0, 1, 2, 3
 PG_LAYOUT_INTERIOR, PG_LAYOUT_PLUTO = 0, 1
 
@@ -34,8 +34,10 @@ EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", 
            "pg_batch_download", "pg_batch_run", "pg_batch_get", "pg_batch_autotune",
            "pg_batch_set_schedule", "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set",
            "pg_adjoint_step", "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load",
-           "pg_selftest_conversions"]
+           "pg_selftest_conversions", "pg_set_userdef"]
 PG_ABI_VERSION = 2  # the pg_config layout these bindings describe
+# pg_userdef_fn: (user, side 0..5, vpos 0 cells / 1..3 faces, stage)
+USERDEF_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int)
 PG_STATIC_MAX_ZONES = 32768
 PG_MAX_CHECKPOINTS = 256
 
@@ -110,6 +112,7 @@ def lib():
     L.pg_checkpoint_save.argtypes = [vp, ip]
     L.pg_checkpoint_load.argtypes = [vp, ip]
     L.pg_selftest_conversions.argtypes = [C.POINTER(C.c_ulonglong)]
+    L.pg_set_userdef.argtypes = [vp, USERDEF_FN, vp, C.POINTER(dp), C.POINTER(dp)]
     L.pg_last_error.restype = C.c_char_p
     for fn in ("pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
                "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
@@ -117,7 +120,8 @@ def lib():
                "pg_batch_create", "pg_batch_destroy", "pg_batch_upload", "pg_batch_download",
                "pg_batch_run", "pg_batch_get", "pg_batch_autotune", "pg_batch_set_schedule",
                "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set", "pg_adjoint_step",
-               "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load", "pg_selftest_conversions"):
+               "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load", "pg_selftest_conversions",
+               "pg_set_userdef"):
         getattr(L, fn).restype = C.c_int
     if L.pg_abi_version() != PG_ABI_VERSION:
         raise OSError(f"libpluto_gb300 has ABI version {L.pg_abi_version()}, these bindings expect "

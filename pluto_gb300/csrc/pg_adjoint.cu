@@ -851,6 +851,11 @@ extern "C" int pg_adjoint_set(pg_solver* h, const double* const vars[8], const d
         set_last_error("pg_adjoint_set: non-periodic boundaries under constrained transport are not covered");
         return PG_ERR_INVALID;
       }
+  for (int d = 0; d < S->g.dims; d++)
+    if (bc_side(S->cfg.bc[d], false) == PG_USERDEF || bc_side(S->cfg.bc[d], true) == PG_USERDEF) {
+      set_last_error("pg_adjoint_set: user-defined boundaries have no adjoint");
+      return PG_ERR_INVALID;
+    }
   AdjBufs* B = nullptr;
   if ((rc = adjoint_alloc(S, &B))) {
     adjoint_free(S);

@@ -5,6 +5,7 @@
 #include <string>
 
 #include "pg_internal.h"
+#include "pg_userdef.cuh"
 #include "pg_xfer.cuh"
 
 using namespace pg;
@@ -48,10 +49,10 @@ int validate_config(const pg_config* c) {
   for (int d = 0; d < c->dims; d++) {
     if (c->nx[d] < 4) return fail(PG_ERR_INVALID, "nx must be >= 4 on active axes");
     if (!(c->dx[d] > 0)) return fail(PG_ERR_INVALID, "dx must be positive");
-    if (c->bc[d] < PG_PERIODIC || c->bc[d] > PG_EQTSYMMETRIC) return fail(PG_ERR_INVALID, "unsupported boundary");
+    if (c->bc[d] < PG_PERIODIC || c->bc[d] > PG_USERDEF) return fail(PG_ERR_INVALID, "unsupported boundary");
     if (c->bc_sides != 0 && c->bc_sides != 1) return fail(PG_ERR_INVALID, "bc_sides must be 0 or 1");
     if (c->bc_sides) {
-      if (c->bc_hi[d] < PG_PERIODIC || c->bc_hi[d] > PG_EQTSYMMETRIC)
+      if (c->bc_hi[d] < PG_PERIODIC || c->bc_hi[d] > PG_USERDEF)
         return fail(PG_ERR_INVALID, "unsupported boundary (end side)");
       if ((c->bc[d] == PG_PERIODIC) != (c->bc_hi[d] == PG_PERIODIC))
         return fail(PG_ERR_INVALID, "a periodic axis is periodic on both sides");
@@ -86,6 +87,10 @@ int validate_config(const pg_config* c) {
   if (c->precision != PG_FP64 && c->precision != PG_MIXED && c->precision != PG_MIXED_DW &&
       c->precision != PG_FP64_TANGENT)
     return fail(PG_ERR_INVALID, "unsupported precision");
+  if (c->precision == PG_FP64_TANGENT)
+    for (int d = 0; d < c->dims; d++)
+      if (c->bc[d] == PG_USERDEF || (c->bc_sides && c->bc_hi[d] == PG_USERDEF))
+        return fail(PG_ERR_INVALID, "user-defined boundaries have no tangent-linear model");
   return PG_OK;
 }
 
@@ -117,6 +122,12 @@ void set_last_error(const char* msg) { g_last_error = msg; }
 static void free_all(Solver* S) {
   if (S->graph) cudaGraphExecDestroy(S->graph);
   S->graph = nullptr;
+  if (S->stream) cudaStreamSynchronize(S->stream);
+  for (int q = 0; q < 11; q++)
+    if (S->ud_pinned[q]) {
+      cudaHostUnregister(S->ud_pinned[q]);
+      S->ud_pinned[q] = nullptr;
+    }
   adjoint_free(S);
   fp64_free(S);
   mixed_free(S);
@@ -161,6 +172,51 @@ extern "C" int pg_create(const pg_config* cfg, pg_solver** out) {
   }
   CK(cudaDeviceSynchronize());
   *out = h;
+  return PG_OK;
+}
+
+extern "C" int pg_set_userdef(pg_solver* h, pg_userdef_fn fn, void* user, double* const vars[8],
+                              double* const faces[3]) {
+  if (!h || !fn || !vars) return fail(PG_ERR_INVALID, "pg_set_userdef: null argument");
+  Solver* S = &h->S;
+  const Geom& g = S->g;
+  const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
+  if (ct && !faces) return fail(PG_ERR_INVALID, "pg_set_userdef: constrained transport needs the face arrays");
+  CK(cudaStreamSynchronize(S->stream));
+  for (int q = 0; q < 11; q++)
+    if (S->ud_pinned[q]) {
+      cudaHostUnregister(S->ud_pinned[q]);
+      S->ud_pinned[q] = nullptr;
+    }
+  auto reach = [&](double* p, size_t n, int q) -> double* {
+    if (!p) return nullptr;
+    if (double* a = host_alias(p)) return a;
+    if (cudaHostRegister(p, n * sizeof(double), cudaHostRegisterMapped) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    S->ud_pinned[q] = p;
+    void* d = nullptr;
+    if (cudaHostGetDevicePointer(&d, p, 0) != cudaSuccess) {
+      cudaGetLastError();
+      return nullptr;
+    }
+    return (double*)d;
+  };
+  for (int nv = 0; nv < 8; nv++) {
+    S->ud_dev_v[nv] = reach(vars[nv], (size_t)g.ncell, nv);
+    if (vars[nv] && !S->ud_dev_v[nv]) return fail(PG_ERR_CUDA, "pg_set_userdef: host array not reachable");
+  }
+  for (int d = 0; d < 3; d++) {
+    S->ud_dev_f[d] = nullptr;
+    if (!ct || d >= g.dims) continue;
+    const size_t n = (size_t)(g.nt[0] + (d == 0)) * (g.nt[1] + (d == 1)) * (g.nt[2] + (d == 2));
+    S->ud_dev_f[d] = reach(faces[d], n, 8 + d);
+    if (faces[d] && !S->ud_dev_f[d]) return fail(PG_ERR_CUDA, "pg_set_userdef: host face array not reachable");
+  }
+  S->ud_fn = fn;
+  S->ud_user = user;
+  S->graph_dirty = true;
   return PG_OK;
 }
 
@@ -294,6 +350,9 @@ extern "C" int pg_download(pg_solver* h, double* const vars[8], double* const fa
 // -------------------------------------------------------------------------
 
 static int enqueue_step(Solver* S) {
+  if (has_userdef(S) && !S->ud_fn)
+    return fail(PG_ERR_INVALID, "a user-defined boundary side needs pg_set_userdef before the first step");
+  S->ud_stage = 0;
   if (S->cfg.precision == PG_FP64) return fp64_enqueue_step(S);
   if (S->cfg.precision == PG_FP64_TANGENT) return tl_enqueue_step(S);
   return mixed_enqueue_step(S);

@@ -1,4 +1,5 @@
-// Boundary fill under constrained transport when an axis is not periodic:
+// Boundary fill under constrained transport when an axis is not periodic,
+// and whenever a side is user-defined (then also without CT, nbfield 0):
 // the reference's side-by-side sequence (Src/boundary.c:137-300), one axis
 // after the other.  Per axis, k_bound_axis copies the cells and the
 // transverse face components (zero gradient, periodic image, or mirror image
@@ -14,6 +15,7 @@
 #pragma once
 #include "pg_internal.h"
 #include "pg_physics.cuh"
+#include "pg_userdef.cuh"
 
 namespace pg {
 
@@ -74,6 +76,7 @@ __global__ void k_bound_axis(BoundCT<T> a, int type, long long nghost) {
   s[B2] = c[B2];
   s[AX] = bc_src(c[AX], g.beg[AX], g.end[AX], n, type);
   const int side = bc_side(type, !lo);  // this ghost's side of the axis
+  if (side == PG_USERDEF) return;       // the host callback fills it
   const long long dst = cidx(g, c[2], c[1], c[0]), src = cidx(g, s[2], s[1], s[0]);
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
@@ -117,7 +120,8 @@ __global__ void k_fill_normal(BoundCT<T> a, long long ntrans, int type) {
   const Geom& g = a.g;
   constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
   const bool lo = (q & 1) == 0;
-  const bool average = bc_side(type, !lo) == PG_OUTFLOW;
+  const int st = bc_side(type, !lo);
+  const bool average = st == PG_OUTFLOW || st == PG_USERDEF;
   const long long t = q >> 1;
   int c[3];
   c[B1] = (int)(t % g.nt[B1]);
@@ -171,6 +175,35 @@ __global__ void k_fill_normal(BoundCT<T> a, long long ntrans, int type) {
   }
 }
 
+// CT_AverageTransverseMagField (Src/MHD/CT/ct_field_average.c:275-440,
+// Cartesian) on the user-defined sides of axis AX: the transverse
+// cell-centred components in the ghost zones from the staggered field
+// (0.5 (b + b(-1)) along the component's axis, its -1 layer from Bm1).  The
+// same thread layout as k_bound_axis.
+template <class T, class C, int AX>
+__global__ void k_avg_transverse(BoundCT<T> a, int type, long long nghost) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= nghost) return;
+  const Geom& g = a.g;
+  constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
+  const int ng = g.beg[AX];
+  const int l = (int)(q % (2 * ng));
+  const long long t = q / (2 * ng);
+  int c[3];
+  c[B1] = (int)(t % g.nt[B1]);
+  c[B2] = (int)(t / g.nt[B1]);
+  const bool lo = l < ng;
+  if (bc_side(type, !lo) != PG_USERDEF) return;
+  c[AX] = lo ? l : g.end[AX] + 1 + (l - ng);
+  for (int fd = 0; fd < a.nbfield; fd++) {
+    if (fd == AX) continue;
+    int m[3] = {c[0], c[1], c[2]};
+    m[fd] -= 1;
+    const C avg = 0.5 * (C(*bct_face(a, fd, c[2], c[1], c[0])) + C(*bct_face(a, fd, m[2], m[1], m[0])));
+    a.V[BX1 + fd][cidx(g, c[2], c[1], c[0])] = T(avg);
+  }
+}
+
 template <class T, class C, int AX>
 static void launch_bound_ct_axis(Solver* S, const BoundCT<T>& b, const char* copy_name, const char* fill_name) {
   const Geom& g = b.g;
@@ -179,12 +212,20 @@ static void launch_bound_ct_axis(Solver* S, const BoundCT<T>& b, const char* cop
   const long long nghost = 2LL * g.beg[AX] * ntrans;
   PG_LAUNCH(S, copy_name, (k_bound_axis<T, AX><<<grid_for(nghost), kThreads, 0, S->stream>>>(
                               b, S->cfg.bc[AX], nghost)));
-  // per side, outflow: FillMagneticField + CT_AverageNormalMagField;
-  // reflective and equatorial-symmetric: FillMagneticField only
-  // (Src/boundary.c:188-206)
-  if (S->cfg.bc[AX] != PG_PERIODIC)
+  if (bc_side(S->cfg.bc[AX], false) == PG_USERDEF || bc_side(S->cfg.bc[AX], true) == PG_USERDEF)
+    launch_userdef_axis<T>(S, b.V, b.Bs, b.Bm1, b.nbfield, AX);
+  // per side, outflow and user-defined: FillMagneticField +
+  // CT_AverageNormalMagField; reflective and equatorial-symmetric:
+  // FillMagneticField only (Src/boundary.c:188-206, 285-288)
+  if (S->cfg.bc[AX] != PG_PERIODIC && b.nbfield > 0)
     PG_LAUNCH(S, fill_name, (k_fill_normal<T, C, AX><<<grid_for(2 * ntrans, 128), 128, 0, S->stream>>>(
                                 b, ntrans, S->cfg.bc[AX])));
+  // user-defined sides under CT: CT_AverageTransverseMagField too
+  // (Src/boundary.c:287-289)
+  if (b.nbfield > 0 &&
+      (bc_side(S->cfg.bc[AX], false) == PG_USERDEF || bc_side(S->cfg.bc[AX], true) == PG_USERDEF))
+    PG_LAUNCH(S, fill_name, (k_avg_transverse<T, C, AX><<<grid_for(nghost), kThreads, 0, S->stream>>>(
+                                b, S->cfg.bc[AX], nghost)));
 }
 
 template <class T, class C>
@@ -192,6 +233,7 @@ static void launch_bound_ct(Solver* S, const BoundCT<T>& b, const char* copy_nam
   launch_bound_ct_axis<T, C, 0>(S, b, copy_name, fill_name);
   if (b.g.dims > 1) launch_bound_ct_axis<T, C, 1>(S, b, copy_name, fill_name);
   if (b.g.dims > 2) launch_bound_ct_axis<T, C, 2>(S, b, copy_name, fill_name);
+  S->ud_stage++;
 }
 
 }  // namespace pg

@@ -582,7 +582,7 @@ static void launch_stage_tail(Solver* S, const F64A<T>& a, const Box& dom) {
 template <class T>
 static void launch_bound(Solver* S, const F64A<T>& a) {
   const Geom& g = S->g;
-  if (a.ct_outflow) {
+  if (a.ct_outflow || has_userdef(S)) {
     BoundCT<T> b;
     b.g = a.g;
     for (int nv = 0; nv < 8; nv++) b.V[nv] = a.V[nv];

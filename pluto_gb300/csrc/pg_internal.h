@@ -93,6 +93,13 @@ void set_last_error(const char* msg);
 // host <-> device copy of one FP64 array in the interior or PLUTO layout
 int xfer_f64(Solver* S, double* dev, double* host, int fd, int layout, bool to_dev);
 
+// arguments of one USERDEF host call (captured into the step graph)
+struct UdCall {
+  const Solver* S;
+  int side, stage, nbfield;
+};
+constexpr int kUdStages = 4;  // boundary fills per step: RK3 has 3, CTU 1
+
 struct Solver {
   pg_config cfg;
   Geom g;
@@ -138,6 +145,14 @@ struct Solver {
   double cfl = 0.4, cfl_max_var = 1.1;
   bool device_dt = false;  // kernels end each step by computing the next dt
   int steps_done = 0;
+  // USERDEF sides (pg_set_userdef)
+  pg_userdef_fn ud_fn = nullptr;
+  void* ud_user = nullptr;
+  double* ud_dev_v[8] = {};   // device-usable addresses of the caller's host arrays
+  double* ud_dev_f[3] = {};
+  void* ud_pinned[11] = {};   // host arrays this library pinned (unpinned by pg_destroy)
+  int ud_stage = 0;           // boundary fills enqueued so far in the step
+  UdCall ud_calls[kUdStages][6] = {};
 };
 
 constexpr int kThreads = 256;

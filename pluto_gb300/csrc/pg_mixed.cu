@@ -1187,7 +1187,7 @@ static MixArgs margs(Solver* S, int in_buf, int out_buf, int v0_buf) {
 static void mlaunch_bound(Solver* S, const MixArgs& a) {
   const Geom& g = S->g;
   MixedState* M = (MixedState*)S->mixed;
-  if (a.ct && M->b.Bm1[0]) {  // outflow axis under CT: per-axis passes, FP64 face recovery
+  if ((a.ct && M->b.Bm1[0]) || has_userdef(S)) {  // non-periodic axis under CT, or a user-defined side: per-axis passes
     BoundCT<float> b;
     b.g = g;
     for (int nv = 0; nv < NV; nv++) b.V[nv] = (float*)a.Vin[nv];

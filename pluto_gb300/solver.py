@@ -26,7 +26,7 @@ RIEMANN = {"hll": L.PG_HLL, "hlld": L.PG_HLLD, "roe": L.PG_ROE}
 STEPPING = {"RK2": L.PG_RK2, "RK3": L.PG_RK3, "HANCOCK": L.PG_HANCOCK}
 EMF = {"ARITHMETIC": L.PG_ARITHMETIC, "UCT_CONTACT": L.PG_UCT_CONTACT, "UCT_HLL": L.PG_UCT_HLL}
 BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW, "reflective": L.PG_REFLECTIVE,
-      "eqtsymmetric": L.PG_EQTSYMMETRIC}
+      "eqtsymmetric": L.PG_EQTSYMMETRIC, "userdef": L.PG_USERDEF}
 PRECISION = {"fp64": L.PG_FP64, "mixed": L.PG_MIXED, "mixed_dw": L.PG_MIXED_DW,
              "fp64_tangent": L.PG_FP64_TANGENT}
 NVAR = 8
@@ -131,6 +131,35 @@ class Solver:
         views = [vc[q] for q in range(NVAR)]
         L.check(getattr(L.lib(), fn)(self.h, _ptrs(views, 8), _ptrs(faces, 3), L.PG_LAYOUT_INTERIOR), fn)
         return vc, faces
+
+    def ghost_shape(self):
+        """(nt2, nt1, nt0): the ghosted cell-array shape (PLUTO layout)."""
+        s = self.spec
+        ng = 3 if s.get("recon", "LINEAR") == "PARABOLIC" else 2
+        if s.get("stepping", "RK2") == "HANCOCK" and self.ct:
+            ng += 1
+        return tuple(int(s["nx"][d]) + 2 * ng if d < self.dims else 1 for d in (2, 1, 0))
+
+    def set_userdef(self, fn):
+        """User-defined boundary sides (PLUTO's UserDefBoundary).  fn(side,
+        vpos, stage, vc, faces) is called at every boundary fill for every
+        "userdef" side (side 0..5 = X1_BEG..X3_END; vpos 0 the cell box, 1..3
+        the box of face component 1..3); vc [8, nt2, nt1, nt0] and faces[d]
+        (one longer along d, -1 layer first) are PLUTO-layout host arrays that
+        hold the current state near the side; fn writes the side's ghost
+        boxes.  It runs on a CUDA host thread while the step waits for it."""
+        nz, ny, nx = self.ghost_shape()
+        self._ud_vc = np.zeros((NVAR, nz, ny, nx))
+        self._ud_f = [np.zeros((nz + (d == 2), ny + (d == 1), nx + (d == 0)))
+                      if (self.ct and d < self.dims) else None for d in range(3)]
+
+        def cb(user, side, vpos, stage):
+            fn(side, vpos, stage, self._ud_vc, self._ud_f)
+
+        self._ud_cb = L.USERDEF_FN(cb)
+        views = [self._ud_vc[q] for q in range(NVAR)]
+        L.check(L.lib().pg_set_userdef(self.h, self._ud_cb, None, _ptrs(views, 8), _ptrs(self._ud_f, 3)),
+                "pg_set_userdef")
 
     def upload(self, vc: np.ndarray, bs=(None, None, None)):
         self._put("pg_upload", vc, bs)

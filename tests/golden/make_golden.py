@@ -53,6 +53,75 @@ def spec_of(s: br.Setup) -> dict:
                 params=s.params)
 
 
+# UserDefBoundary of the USERDEF fixtures (the same rules, in numpy, are in
+# tests/userdef_cases.py): an X1_BEG nozzle -- a fixed inflow state on the
+# middle half of the rows, a mirror wall (vx, Bx negated) elsewhere; the
+# staggered By and Bz of the side's x2face / x3face boxes likewise -- and an
+# X3_END side copied from the last interior plane (cells with vz = 0 and
+# p = 0.1, the staggered Bx and By of its boxes).  Every transverse staggered
+# component of a side's boxes is set, so nothing depends on ghost values that
+# only the initial condition wrote.
+USERDEF_C = r"""
+  int i, j, k, nv;
+  if (side == X1_BEG) {
+    if (box->vpos == CENTER) {
+      BOX_LOOP(box, k, j, i) {
+        if (j >= JBEG + NX2/4 && j < JBEG + (3*NX2)/4) {
+          d->Vc[RHO][k][j][i] = 2.0;
+          d->Vc[VX1][k][j][i] = 0.5;
+          d->Vc[VX2][k][j][i] = 0.0;
+          d->Vc[PRS][k][j][i] = 0.3;
+          d->Vc[BX1][k][j][i] = 0.2;
+          d->Vc[BX2][k][j][i] = 0.1;
+#if COMPONENTS == 3
+          d->Vc[VX3][k][j][i] = 0.0;
+          d->Vc[BX3][k][j][i] = 0.0;
+#endif
+        } else {
+          NVAR_LOOP(nv) d->Vc[nv][k][j][i] = d->Vc[nv][k][j][2*IBEG - 1 - i];
+          d->Vc[VX1][k][j][i] = -d->Vc[VX1][k][j][i];
+          d->Vc[BX1][k][j][i] = -d->Vc[BX1][k][j][i];
+        }
+      }
+    }
+#ifdef STAGGERED_MHD
+    else if (box->vpos == X2FACE) {
+      BOX_LOOP(box, k, j, i) {
+        if (j >= JBEG + NX2/4 && j < JBEG + (3*NX2)/4) d->Vs[BX2s][k][j][i] = 0.1;
+        else d->Vs[BX2s][k][j][i] = d->Vs[BX2s][k][j][2*IBEG - 1 - i];
+      }
+    }
+  #if DIMENSIONS == 3
+    else if (box->vpos == X3FACE) {
+      BOX_LOOP(box, k, j, i) {
+        if (j >= JBEG + NX2/4 && j < JBEG + (3*NX2)/4) d->Vs[BX3s][k][j][i] = 0.0;
+        else d->Vs[BX3s][k][j][i] = d->Vs[BX3s][k][j][2*IBEG - 1 - i];
+      }
+    }
+  #endif
+#endif
+  }
+#if DIMENSIONS == 3
+  if (side == X3_END) {
+    if (box->vpos == CENTER) {
+      BOX_LOOP(box, k, j, i) {
+        NVAR_LOOP(nv) d->Vc[nv][k][j][i] = d->Vc[nv][KEND][j][i];
+        d->Vc[VX3][k][j][i] = 0.0;
+        d->Vc[PRS][k][j][i] = 0.1;
+      }
+    }
+  #ifdef STAGGERED_MHD
+    else if (box->vpos == X1FACE) {
+      BOX_LOOP(box, k, j, i) d->Vs[BX1s][k][j][i] = d->Vs[BX1s][KEND][j][i];
+    } else if (box->vpos == X2FACE) {
+      BOX_LOOP(box, k, j, i) d->Vs[BX2s][k][j][i] = d->Vs[BX2s][KEND][j][i];
+    }
+  #endif
+  }
+#endif
+"""
+
+
 def setups():
     out = [
         br.ot_setup("hlld", 32, 30),
@@ -92,6 +161,13 @@ def setups():
                 bc=(("outflow", "reflective"), ("reflective", "outflow"), ("outflow", "outflow"))),
         replace(br.tube_setup(0, 256, 100), name="tube_sides_0_256",
                 bc=(("reflective", "outflow"), ("outflow", "outflow"), ("outflow", "outflow"))),
+        # user-defined sides (UserDefBoundary above)
+        replace(br.ot_setup("hlld", 32, 30), name="ot_userdef_32", userdef_body=USERDEF_C,
+                bc=(("userdef", "outflow"), ("periodic", "periodic"), ("outflow", "outflow"))),
+        replace(br.blast_setup(16, 12), name="blast_userdef_16", userdef_body=USERDEF_C, ct=False,
+                bc=(("periodic", "periodic"), ("outflow", "outflow"), ("reflective", "userdef"))),
+        replace(br.blast_setup(16, 12), name="blast_userdef_ct_16", userdef_body=USERDEF_C,
+                bc=(("userdef", "outflow"), ("periodic", "periodic"), ("reflective", "userdef"))),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

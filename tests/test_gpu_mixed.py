@@ -8,6 +8,7 @@ reference binary directly.
 import numpy as np
 import pytest
 
+import userdef_cases
 from conftest import GOLDEN_NAMES, load_golden, rel_l1
 
 pytestmark = pytest.mark.gpu
@@ -15,7 +16,10 @@ pytestmark = pytest.mark.gpu
 
 def _s(spec, precision):
     from pluto_gb300 import Solver
-    return Solver(spec, precision=precision)
+    s = Solver(spec, precision=precision)
+    if userdef_cases.has_userdef(spec):
+        s.set_userdef(userdef_cases.make(spec))
+    return s
 
 
 MIXED = ["mixed", "mixed_dw"]

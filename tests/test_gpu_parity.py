@@ -7,6 +7,7 @@ bit for bit, which ``test_fp64_bitwise_on_goldens`` checks).
 import numpy as np
 import pytest
 
+import userdef_cases
 from conftest import GOLDEN_NAMES, load_golden, rel_l1
 
 pytestmark = pytest.mark.gpu
@@ -16,7 +17,10 @@ TOL = 1e-10
 
 def _solver(meta, precision="fp64", **kw):
     from pluto_gb300 import Solver
-    return Solver(meta, precision=precision, **kw)
+    s = Solver(meta, precision=precision, **kw)
+    if userdef_cases.has_userdef(meta):
+        s.set_userdef(userdef_cases.make(meta))
+    return s
 
 
 def _errors(vc, bs, vc_ref, bs_ref):
@@ -45,7 +49,8 @@ def test_fp64_matches_reference_goldens(name):
                                   "ot_ctu_arith_roe_32", "turb_ctu_uctc_12", "tube_ctu_1_200",
                                   "cpa_ctu_outflow_32", "blast_reflective_16", "ot_reflective_32",
                                   "cpa_eqtsym_32", "tube_reflective_0_256", "ot_ctu_reflective_32",
-                                  "blast_sides_16", "ot_sides_32", "ot_ctu_sides_32", "tube_sides_0_256"])
+                                  "blast_sides_16", "ot_sides_32", "ot_ctu_sides_32", "tube_sides_0_256",
+                                  "ot_userdef_32", "blast_userdef_16", "blast_userdef_ct_16"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
@@ -119,7 +124,8 @@ def test_fp64_vs_oracle_random_3d(solver, recon, stepping):
 @pytest.mark.parametrize("bc", [("outflow", "outflow", "outflow"), ("outflow", "periodic", "outflow"),
                                 ("periodic", "outflow", "periodic"), ("reflective", "eqtsymmetric", "reflective"),
                                 ("eqtsymmetric", "periodic", "outflow"),
-                                (("reflective", "outflow"), ("outflow", "eqtsymmetric"), ("eqtsymmetric", "reflective"))])
+                                (("reflective", "outflow"), ("outflow", "eqtsymmetric"), ("eqtsymmetric", "reflective")),
+                                (("userdef", "outflow"), "periodic", ("reflective", "userdef"))])
 def test_fp64_vs_oracle_outflow_ct_3d(bc):
     """Outflow, reflective and equatorial-symmetric sides under CT
     (FillMagneticField, normal averaging on outflow sides, FlipSign mirror
@@ -130,6 +136,8 @@ def test_fp64_vs_oracle_outflow_ct_3d(bc):
     spec.update(bc=list(bc), solver="roe", recon="PARABOLIC", stepping="RK3")
     s = _solver(spec)
     o = Oracle(spec, nthreads=4)
+    if userdef_cases.has_userdef(spec):
+        o.set_userdef(userdef_cases.make(spec))
     s.upload(vc, bs)
     o.set_state(vc, bs)
     s.run(4, 1e-3, 0.3)
@@ -190,7 +198,9 @@ def test_nan_state_reported_not_trapped():
                                            ("UCT_CONTACT", "roe", "outflow"),
                                            ("UCT_CONTACT", "hlld", ["reflective", "periodic", "eqtsymmetric"]),
                                            ("ARITHMETIC", "roe", [("outflow", "reflective"), "periodic",
-                                                                  ("eqtsymmetric", "outflow")])])
+                                                                  ("eqtsymmetric", "outflow")]),
+                                           ("UCT_CONTACT", "hlld", [("userdef", "outflow"), "periodic",
+                                                                    ("outflow", "userdef")])])
 def test_ctu_vs_oracle_random_3d(emf, solver, bc):
     """CTU (primitive Hancock predictor, corner-coupled corrector) with CT on a
     random 3D state against the oracle, bit for bit."""
@@ -199,6 +209,8 @@ def test_ctu_vs_oracle_random_3d(emf, solver, bc):
     spec.update(stepping="HANCOCK", emf=emf, solver=solver, bc=bc, limiter="MC_LIM")
     s = _solver(spec)
     o = Oracle(spec, nthreads=4)
+    if userdef_cases.has_userdef(spec):
+        o.set_userdef(userdef_cases.make(spec))
     s.upload(vc, bs)
     o.set_state(vc, bs)
     s.run(4, 1e-3, 0.3)

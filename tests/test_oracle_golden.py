@@ -7,6 +7,7 @@ oracle restates the same algorithm and must match every double exactly.
 import numpy as np
 import pytest
 
+import userdef_cases
 from conftest import GOLDEN_NAMES, load_golden, rel_l1
 from oracle.oracle import Oracle
 
@@ -15,6 +16,8 @@ from oracle.oracle import Oracle
 def test_oracle_matches_reference_bitwise(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     o = Oracle(meta, nthreads=2)
+    if userdef_cases.has_userdef(meta):
+        o.set_userdef(userdef_cases.make(meta))
     o.set_state(vc0, bs0)
     dts, t = o.run(meta["steps"], meta["first_dt"], meta["cfl"])
     vc, bs = o.get_state()
