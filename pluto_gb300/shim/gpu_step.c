@@ -35,6 +35,8 @@
 
 static pg_solver *s_gpu = NULL;
 static long s_calls = 0;
+static Data *s_data = NULL;   /* for UserDefBoundary on USERDEF sides */
+static Grid *s_grid = NULL;
 
 static int gpu_riemann(Riemann_Solver *R)
 {
@@ -50,6 +52,7 @@ static int gpu_bc(int t)
   if (t == OUTFLOW)  return PG_OUTFLOW;
   if (t == REFLECTIVE)   return PG_REFLECTIVE;
   if (t == EQTSYMMETRIC) return PG_EQTSYMMETRIC;
+  if (t == USERDEF)      return PG_USERDEF;
   return -1;
 }
 
@@ -136,6 +139,38 @@ static void gpu_host_arrays(Data *d, double *vars[8], double *faces[3])
 #endif
 }
 
+/* USERDEF sides: the library calls this, in stream order inside the step,
+   for every such side at every boundary fill, after writing the side's slab
+   into d->Vc / d->Vs; it hands UserDefBoundary the box the reference builds
+   for that side and variable position (Src/boundary.c:144-164, 279-283). */
+static void gpu_userdef(void *user, int side, int vpos, int stage)
+{
+  static const int sides[6] = {X1_BEG, X1_END, X2_BEG, X2_END, X3_BEG, X3_END};
+  int ib = 0, ie = NX1_TOT - 1, jb = 0, je = NX2_TOT - 1, kb = 0, ke = NX3_TOT - 1;
+  RBox box;
+
+  (void)user;
+  if      (side == 0) {ib = IBEG - 1; ie = 0;}
+  else if (side == 1) {ib = IEND + 1; ie = NX1_TOT - 1;}
+  else if (side == 2) {jb = JBEG - 1; je = 0;}
+  else if (side == 3) {jb = JEND + 1; je = NX2_TOT - 1;}
+  else if (side == 4) {kb = KBEG - 1; ke = 0;}
+  else                {kb = KEND + 1; ke = NX3_TOT - 1;}
+  if (vpos == 0) RBoxDefine (ib, ie, jb, je, kb, ke, CENTER, &box);
+  else if (vpos == 1) {
+    if (ib < ie) RBoxDefine (ib-1, ie, jb, je, kb, ke, X1FACE, &box);
+    else         RBoxDefine (ib, ie-1, jb, je, kb, ke, X1FACE, &box);
+  } else if (vpos == 2) {
+    if (jb < je) RBoxDefine (ib, ie, jb-1, je, kb, ke, X2FACE, &box);
+    else         RBoxDefine (ib, ie, jb, je-1, kb, ke, X2FACE, &box);
+  } else {
+    if (kb < ke) RBoxDefine (ib, ie, jb, je, kb-1, ke, X3FACE, &box);
+    else         RBoxDefine (ib, ie, jb, je, kb, ke-1, X3FACE, &box);
+  }
+  g_intStage = stage;
+  UserDefBoundary (s_data, &box, sides[side], s_grid);
+}
+
 static void gpu_check(int rc, const char *where)
 {
   if (rc != PG_OK) {
@@ -165,10 +200,16 @@ int AdvanceStep (Data *d, Riemann_Solver *Riemann, timeStep *Dts, Grid *grid)
   if (sync_every < 1) sync_every = 1;
 
   gpu_host_arrays(d, vars, faces);
+  s_data = d;
+  s_grid = grid;
   if (s_gpu == NULL) {
     pg_config cfg;
+    int dd, ud = 0;
     gpu_config(&cfg, Riemann, grid);
     gpu_check(pg_create(&cfg, &s_gpu), "pg_create");
+    for (dd = 0; dd < DIMENSIONS; dd++)
+      ud |= grid->lbound[dd] == USERDEF || grid->rbound[dd] == USERDEF;
+    if (ud) gpu_check(pg_set_userdef(s_gpu, gpu_userdef, NULL, vars, faces), "pg_set_userdef");
     gpu_check(pg_upload(s_gpu, (const double *const *)vars, (const double *const *)faces,
                         PG_LAYOUT_PLUTO), "pg_upload");
   } else if (up_every > 0 && s_calls % up_every == 0) {
