@@ -152,6 +152,14 @@ __device__ __forceinline__ float narrow(double d) {
   return __uint_as_float(sign | r);
 }
 
+// widen(f) / 2 exactly: a double made from a float is zero or normal with an
+// exponent far above 1, so halving is one step down of the exponent field.
+__device__ __forceinline__ double widen_half(float f) {
+  const double w = widen(f);
+  const long long b = __double_as_longlong(w);
+  return (b & 0x7fffffffffffffffll) == 0 ? w : __longlong_as_double(b - (1ll << 52));
+}
+
 // Accumulator traits: the mixed path is instantiated with native double or
 // with dw; both expose the same handful of operations.
 template <class A> struct Acc;
@@ -176,6 +184,11 @@ template <> struct Acc<double> {
   static __device__ __forceinline__ float tof(T a) { return narrow(a); }
   static __device__ __forceinline__ bool neg(T a) { return a < 0.0; }
   static __device__ __forceinline__ T konst(double hi, float, float) { return hi; }
+  // (x + y) / 2 of two floats: one FMA, the same value as 0.5 * (x + y)
+  // (halving commutes with rounding)
+  static __device__ __forceinline__ T avg2(float x, float y) { return fma(0.5, widen(x), widen_half(y)); }
+  // RK2 corrector (u0 + u + d) / 2 with one FMA after the sum
+  static __device__ __forceinline__ T half_sum3(T u0, T u, float d) { return fma(0.5, u0 + u, widen_half(d)); }
   // element q of a resident accumulator array
   static __device__ __forceinline__ T ld(const void* p, long long q) { return ((const double*)p)[q]; }
   static __device__ __forceinline__ void st(void* p, long long q, T v) { ((double*)p)[q] = v; }
@@ -211,6 +224,8 @@ template <> struct Acc<dw> {
   static __device__ __forceinline__ float tof(T a) { return dw_to_float(a); }
   static __device__ __forceinline__ bool neg(T a) { return a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f); }
   static __device__ __forceinline__ T konst(double, float hi, float lo) { return {hi, lo}; }
+  static __device__ __forceinline__ T avg2(float x, float y) { return (dw{x, 0.f} + y) * 0.5f; }
+  static __device__ __forceinline__ T half_sum3(T u0, T u, float d) { return ((u + d) + u0) * 0.5f; }
   static __device__ __forceinline__ T ld(const void* p, long long q) {
     const float2 f = ((const float2*)p)[q];
     return {f.x, f.y};

@@ -733,10 +733,14 @@ __global__ void k_mface(MixArgs a, Box box) {
     } else {
       rhs = -f1 * (E2[c] - E2[c - 1]) + f2 * (E1[c] - E1[c - g.s[1]]);
     }
-    typename O::T bb = O::addf(O::from(a.Bin[fd][c]), rhs);
+    typename O::T bb;
+    if (STAGE == 2 && NSTAGE == 2) {  // (B0 + B + rhs) / 2
+      bb = O::half_sum3(O::from(a.B0[fd][c]), O::from(a.Bin[fd][c]), rhs);
+    } else {
+      bb = O::addf(O::from(a.Bin[fd][c]), rhs);
+    }
     if (STAGE == 2) {
-      if (NSTAGE == 2) bb = O::mulf(O::addf(bb, a.B0[fd][c]), 0.5f);
-      else bb = O::add(O::mulf(O::from(a.B0[fd][c]), 0.75f), O::mulf(bb, 0.25f));
+      if (NSTAGE == 3) bb = O::add(O::mulf(O::from(a.B0[fd][c]), 0.75f), O::mulf(bb, 0.25f));
     } else if (STAGE == 3) {
       typename O::T third = O::konst(1.0 / 3.0, a.third_hi, a.third_lo);
       bb = O::mul(O::add(O::from(a.B0[fd][c]), O::mulf(bb, 2.0f)), third);
@@ -794,15 +798,30 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
       u.m[d] = O::ld(Uin, (VX1 + d) * n + c);
       u.b[d] = (msk & (1 << (BX1 + d))) ? O::ld(Uin, (BX1 + d) * n + c) : O::from(0.f);
     }
-    // U += dU (flux differences of all directions, FP32) in A
-    if (msk & (1 << RHO)) u.rho = O::addf(u.rho, a.dU[RHO][c]);
+    // U += dU (flux differences of all directions, FP32) in A; only the
+    // accumulated variables (the cell field under CT comes from the faces)
+    float du[NV];
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      if (msk & (1 << (VX1 + d))) u.m[d] = O::addf(u.m[d], a.dU[VX1 + d][c]);
-      if (msk & (1 << (BX1 + d))) u.b[d] = O::addf(u.b[d], a.dU[BX1 + d][c]);
+    for (int nv = 0; nv < NV; nv++) du[nv] = (msk & (1 << nv)) ? a.dU[nv][c] : 0.f;
+    if (STAGE == 2 && NSTAGE == 2) {  // (U0 + U1 + dU) / 2
+      const T u0rho = O::ld(a.U0, RHO * n + c), u0E = O::ld(a.U0, ENG * n + c);
+      u.rho = O::half_sum3(u0rho, u.rho, du[RHO]);
+      u.E = O::half_sum3(u0E, u.E, du[ENG]);
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        u.m[d] = O::half_sum3(O::ld(a.U0, (VX1 + d) * n + c), u.m[d], du[VX1 + d]);
+        if (msk & (1 << (BX1 + d))) u.b[d] = O::half_sum3(O::ld(a.U0, (BX1 + d) * n + c), u.b[d], du[BX1 + d]);
+      }
+    } else {
+      if (msk & (1 << RHO)) u.rho = O::addf(u.rho, du[RHO]);
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        if (msk & (1 << (VX1 + d))) u.m[d] = O::addf(u.m[d], du[VX1 + d]);
+        if (msk & (1 << (BX1 + d))) u.b[d] = O::addf(u.b[d], du[BX1 + d]);
+      }
+      if (msk & (1 << ENG)) u.E = O::addf(u.E, du[ENG]);
     }
-    if (msk & (1 << ENG)) u.E = O::addf(u.E, a.dU[ENG][c]);
-    if (STAGE >= 2) {
+    if (STAGE >= 2 && NSTAGE == 3) {
       ConsA<A> u0;
       u0.rho = O::ld(a.U0, RHO * n + c);
       u0.E = O::ld(a.U0, ENG * n + c);
@@ -811,15 +830,7 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
         u0.m[d] = O::ld(a.U0, (VX1 + d) * n + c);
         u0.b[d] = (msk & (1 << (BX1 + d))) ? O::ld(a.U0, (BX1 + d) * n + c) : O::from(0.f);
       }
-      if (STAGE == 2 && NSTAGE == 2) {
-        u.rho = O::mulf(O::add(u0.rho, u.rho), 0.5f);
-        u.E = O::mulf(O::add(u0.E, u.E), 0.5f);
-#pragma unroll
-        for (int d = 0; d < 3; d++) {
-          u.m[d] = O::mulf(O::add(u0.m[d], u.m[d]), 0.5f);
-          u.b[d] = O::mulf(O::add(u0.b[d], u.b[d]), 0.5f);
-        }
-      } else if (STAGE == 2) {
+      if (STAGE == 2) {
         u.rho = O::add(O::mulf(u0.rho, 0.75f), O::mulf(u.rho, 0.25f));
         u.E = O::add(O::mulf(u0.E, 0.75f), O::mulf(u.E, 0.25f));
 #pragma unroll
@@ -841,7 +852,7 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
     // CT_AverageMagneticField: staggered components from the new faces
     if (a.ct)
       for (int d = 0; d < g.dims; d++)
-        u.b[d] = O::mulf(O::addf(O::from(a.Bout[d][c]), a.Bout[d][c - g.s[d]]), 0.5f);
+        u.b[d] = O::avg2(a.Bout[d][c], a.Bout[d][c - g.s[d]]);
     // ConsToPrim (Src/MHD/mappers.c:88-254) with the pressure recovered in A
     unsigned char fl = 0;
     if (O::neg(u.rho)) {
