@@ -1721,6 +1721,7 @@ int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
   update_stage(p, dt, 1, &inv_dt, &inv_dt_1d);
   if (p->c.ct) ct_average(p);
   cons_to_prim_3d(p);
+  if (p->c.stepping == OC_EULER) goto done; /* the predictor alone, rk_step.c:145 */
 
   /* stage 2 */
   boundary(p);
@@ -1755,6 +1756,7 @@ int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
     }
     cons_to_prim_3d(p);
   }
+done:
   if (p->c.dims == 1) inv_dt = inv_dt_1d;
   if (inv_dt_hyp) *inv_dt_hyp = inv_dt;
   if (max_mach) *max_mach = p->max_mach;

@@ -19,7 +19,7 @@ NVAR = 8
 RECON = {"LINEAR": 0, "PARABOLIC": 1}
 LIMITER = {"FLAT_LIM": 0, "MINMOD_LIM": 1, "VANLEER_LIM": 2, "MC_LIM": 3, "DEFAULT": 4}
 SOLVER = {"hll": 0, "hlld": 1, "roe": 2}
-STEPPING = {"RK2": 2, "RK3": 3, "HANCOCK": 4}
+STEPPING = {"EULER": 1, "RK2": 2, "RK3": 3, "HANCOCK": 4}
 BC = {"periodic": 0, "outflow": 1, "reflective": 2, "eqtsymmetric": 3, "userdef": 4}
 EMF = {"ARITHMETIC": 1, "UCT_CONTACT": 3, "UCT_HLL": 4}
 

@@ -20,6 +20,7 @@ PG_RK2, PG_RK3, PG_HANCOCK = 2, 3, 4
 PG_DIVB_NONE, PG_CONSTRAINED_TRANSPORT = 0, 1
 PG_ARITHMETIC, PG_UCT_CONTACT, PG_UCT_HLL = 1, 3, 4
 PG_PERIODIC, PG_OUTFLOW, PG_REFLECTIVE, PG_EQTSYMMETRIC, PG_USERDEF = 0, 1, 2, 3, 4
+PG_EULER = 1
 PG_FP64, PG_MIXED, PG_MIXED_DW, PG_FP64_TANGENT = 0, 1, 2, 3
 PG_LAYOUT_INTERIOR, PG_LAYOUT_PLUTO = 0, 1
 

@@ -64,7 +64,8 @@ int validate_config(const pg_config* c) {
   if (c->limiter < PG_FLAT_LIM || c->limiter > PG_DEFAULT_LIM) return fail(PG_ERR_INVALID, "unsupported limiter");
   if (c->riemann != PG_HLL && c->riemann != PG_HLLD && c->riemann != PG_ROE)
     return fail(PG_ERR_INVALID, "unsupported Riemann solver");
-  if (c->time_stepping != PG_RK2 && c->time_stepping != PG_RK3 && c->time_stepping != PG_HANCOCK)
+  if (c->time_stepping != PG_EULER && c->time_stepping != PG_RK2 && c->time_stepping != PG_RK3 &&
+      c->time_stepping != PG_HANCOCK)
     return fail(PG_ERR_INVALID, "unsupported time stepping");
   if (c->time_stepping == PG_HANCOCK) {
     if (c->reconstruction != PG_LINEAR)  // Src/States/hancock.c:64-67

@@ -616,12 +616,14 @@ static void enqueue_rk(Solver* S, const F64A<T>& a) {
   if (g.dims > 1) launch_sweep<T, 1>(S, a, 1);
   if (g.dims > 2) launch_sweep<T, 2>(S, a, 1);
   launch_stage_tail<T, 1, NSTAGE>(S, a, dom);
-  // stage 2
-  launch_bound(S, a);
-  launch_sweep<T, 0>(S, a, 2);
-  if (g.dims > 1) launch_sweep<T, 1>(S, a, 2);
-  if (g.dims > 2) launch_sweep<T, 2>(S, a, 2);
-  launch_stage_tail<T, 2, NSTAGE>(S, a, dom);
+  // stage 2 (EULER: the predictor alone, rk_step.c:145)
+  if (NSTAGE >= 2) {
+    launch_bound(S, a);
+    launch_sweep<T, 0>(S, a, 2);
+    if (g.dims > 1) launch_sweep<T, 1>(S, a, 2);
+    if (g.dims > 2) launch_sweep<T, 2>(S, a, 2);
+    launch_stage_tail<T, 2, NSTAGE>(S, a, dom);
+  }
   if (NSTAGE == 3) {
     launch_bound(S, a);
     launch_sweep<T, 0>(S, a, 3);
@@ -644,6 +646,7 @@ int fp64_enqueue_step_t(Solver* S) {
   F64A<T> a = make_args<T>(S);
   if (S->cfg.time_stepping == PG_HANCOCK) enqueue_ctu<T>(S, a);
   else if (S->cfg.time_stepping == PG_RK3) enqueue_rk<T, 3>(S, a);
+  else if (S->cfg.time_stepping == PG_EULER) enqueue_rk<T, 1>(S, a);
   else enqueue_rk<T, 2>(S, a);
   return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ERR_CUDA;
 }

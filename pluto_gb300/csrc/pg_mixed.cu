@@ -1333,13 +1333,16 @@ static void menqueue(Solver* S) {
   for (int ax = 0; ax < 3; ax++) { dom.lo[ax] = g.beg[ax]; dom.hi[ax] = g.end[ax]; }
   const int bA = M->cur, bB = 1 - M->cur;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
-  // stage 1: A -> B
-  MixArgs a1 = margs(S, bA, bB, bA);
+  // stage 1: A -> B (EULER: in place, A -> A; the final kernel reads no
+  // primitive state)
+  MixArgs a1 = NSTAGE == 1 ? margs(S, bA, bA, bA) : margs(S, bA, bB, bA);
   PG_LAUNCH(S, "mixed_begin", (k_mbegin<<<grid_for(g.ncell), kThreads, 0, S->stream>>>(a1, g.ncell)));
   mlaunch_bound(S, a1);
   if (ct) mlaunch_sweeps<true>(S, a1, 1); else mlaunch_sweeps<false>(S, a1, 1);
   mlaunch_tail<1, NSTAGE, A>(S, a1, dom);
-  if (NSTAGE == 2) {
+  if (NSTAGE == 1) {
+    PG_LAUNCH(S, "mixed_end_step", (k_mend_step<<<1, 1, 0, S->stream>>>(a1)));
+  } else if (NSTAGE == 2) {
     // stage 2: B (+A) -> A
     MixArgs a2 = margs(S, bB, bA, bA);
     mlaunch_bound(S, a2);
@@ -1364,6 +1367,9 @@ int mixed_enqueue_step(Solver* S) {
   if (S->cfg.time_stepping == PG_RK3) {
     if (dwacc) menqueue<3, dw>(S);
     else menqueue<3, double>(S);
+  } else if (S->cfg.time_stepping == PG_EULER) {
+    if (dwacc) menqueue<1, dw>(S);
+    else menqueue<1, double>(S);
   } else {
     if (dwacc) menqueue<2, dw>(S);
     else menqueue<2, double>(S);

@@ -91,6 +91,8 @@ static void gpu_config(pg_config *c, Riemann_Solver *Riemann, Grid *grid)
   c->riemann = gpu_riemann(Riemann);
 #if TIME_STEPPING == RK3
   c->time_stepping = PG_RK3;
+#elif TIME_STEPPING == EULER
+  c->time_stepping = PG_EULER;
 #elif TIME_STEPPING == HANCOCK
   c->time_stepping = PG_HANCOCK;
 #else

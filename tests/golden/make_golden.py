@@ -168,6 +168,9 @@ def setups():
                 bc=(("periodic", "periodic"), ("outflow", "outflow"), ("reflective", "userdef"))),
         replace(br.blast_setup(16, 12), name="blast_userdef_ct_16", userdef_body=USERDEF_C,
                 bc=(("userdef", "outflow"), ("periodic", "periodic"), ("reflective", "userdef"))),
+        # TIME_STEPPING EULER (the RK predictor alone)
+        replace(br.ot_setup("hlld", 32, 10), stepping="EULER", cfl=0.2, name="ot_euler_32"),
+        replace(br.tube_setup(0, 256, 60), stepping="EULER", name="tube_euler_0_256"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

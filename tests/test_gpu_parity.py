@@ -50,7 +50,8 @@ def test_fp64_matches_reference_goldens(name):
                                   "cpa_ctu_outflow_32", "blast_reflective_16", "ot_reflective_32",
                                   "cpa_eqtsym_32", "tube_reflective_0_256", "ot_ctu_reflective_32",
                                   "blast_sides_16", "ot_sides_32", "ot_ctu_sides_32", "tube_sides_0_256",
-                                  "ot_userdef_32", "blast_userdef_16", "blast_userdef_ct_16"])
+                                  "ot_userdef_32", "blast_userdef_16", "blast_userdef_ct_16",
+                                  "ot_euler_32", "tube_euler_0_256"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
