@@ -49,3 +49,23 @@ def test_shim_links_1d_no_ct(tmp_path):
 def test_shim_links_3d_ppm_rk3(tmp_path):
     from oracle import build_ref as br
     assert _link(lambda: br.turb_setup(12, 10), tmp_path).exists()
+
+
+def test_enable_script_edits_the_template_makefile(tmp_path):
+    """The build switch inserts the shim include after the template's
+    object-file block, once, and removes it again."""
+    import importlib.util
+    spec = importlib.util.spec_from_file_location("pg_enable", ROOT / "pluto_gb300" / "shim" / "enable.py")
+    en = importlib.util.module_from_spec(spec)
+    spec.loader.exec_module(en)
+    mk = tmp_path / "makefile"
+    orig = (REF / "Src" / "Templates" / "makefile").read_text()
+    mk.write_text(orig)
+    assert en.main([str(tmp_path)]) == 0
+    once = mk.read_text()
+    assert once.count("include $(PG_ROOT)/pluto_gb300/shim/Makefile.gpu") == 1
+    assert once.index("Additional_object_files_here") < once.index(en.BEGIN) < once.index("PLUTO target rule")
+    en.main([str(mk)])
+    assert mk.read_text() == once
+    en.main([str(mk), "--disable"])
+    assert mk.read_text() == orig
