@@ -234,6 +234,20 @@ int pg_tube_step_static(const pg_config *cfg, const double *v_in, double *v_out,
    for PG_FP64_TANGENT solvers, batches or the adjoint. */
 int pg_set_userdef(pg_solver *s, pg_userdef_fn fn, void *user, double *const vars[8], double *const faces[3]);
 
+/* INTERNAL_BOUNDARY YES (Src/boundary.c:90-92): at the start of every
+   boundary fill the callback of pg_set_userdef is called with side
+   PG_SIDE_INTERNAL (UserDefBoundary with a null box) after the library wrote
+   the whole state into its host arrays and the zone flags into flags[]
+   (PG_LAYOUT_PLUTO, one byte per zone, cleared at the start of each step as
+   Src/main.c:329 does); afterwards it reads the whole state and the flags
+   back.  Zones flagged PG_FLAG_INTERNAL_BOUNDARY get a zero right-hand side
+   (Src/int_bound_reset.c).  Each fill moves the whole state across the host
+   link.  PG_FP64 solvers with EULER/RK2/RK3 time stepping; call
+   pg_set_userdef first. */
+#define PG_SIDE_INTERNAL 6
+#define PG_FLAG_INTERNAL_BOUNDARY 32  /* Src/pluto.h:197 */
+int pg_set_internal_boundary(pg_solver *s, unsigned char *flags);
+
 /* Diagnostics */
 int pg_get_stream(pg_solver *s, void **cuda_stream);
 int pg_get_info(pg_solver *s, pg_step_info *info, double *time, double *dt);

@@ -79,6 +79,7 @@ class Setup:
     params: dict = field(default_factory=dict)
     init_body: str = ""
     userdef_body: str = ""          # body of UserDefBoundary (USERDEF sides)
+    internal_boundary: bool = False  # INTERNAL_BOUNDARY YES
 
 
 def _fmt(x: float) -> str:
@@ -99,6 +100,8 @@ def definitions_h(s: Setup) -> str:
         ("THERMAL_CONDUCTION", "NO"), ("VISCOSITY", "NO"),
         ("ROTATING_FRAME", "NO"),
     ]
+    if s.internal_boundary:
+        lines.append(("INTERNAL_BOUNDARY", "YES"))
     out = [f"#define  {k:<30} {v}" for k, v in lines]
     for idx, key in enumerate(s.params):
         out.append(f"#define  {key:<30} {idx}")

@@ -37,11 +37,13 @@
 #define SMALL_DENSITY 1.e-12  /* Src/globals.h:113 */
 #define SMALL_PRESSURE 1.e-12 /* Src/globals.h:114 */
 #define FLAG_CONS2PRIM_FAIL 64 /* Src/pluto.h:200 */
+#define FLAG_INTERNAL_BOUNDARY 32 /* Src/pluto.h:197 */
 
 struct oc_problem {
   oc_config c;
   oc_userdef_fn ud_fn;     /* USERDEF sides */
   void *ud_user;
+  int internal;            /* INTERNAL_BOUNDARY */
   int bstage;              /* boundary fills so far in the step */
   int ng, nt[3], beg[3], end[3];
   size_t ncell, nface[3];
@@ -832,6 +834,8 @@ static void ct_average_transverse(oc_problem *p, int is) {
 static void boundary(oc_problem *p) {
   int is, nv;
   int dims = p->c.dims;
+  /* INTERNAL_BOUNDARY: UserDefBoundary (d, NULL, 0, grid), Src/boundary.c:90-92 */
+  if (p->internal && p->ud_fn) p->ud_fn(p->ud_user, 6, 0, p->bstage + 1);
   for (is = 0; is < 2 * dims; is++) {
     int d = is / 2, type = (is & 1) ? p->c.bc_hi[d] : p->c.bc[d]; /* X*_BEG, X*_END */
     int ib = 0, ie = p->nt[0] - 1, jb = 0, je = p->nt[1] - 1, kb = 0, ke = p->nt[2] - 1;
@@ -1009,6 +1013,9 @@ static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1
         size_t c;
         ijk[dir] = i;
         c = CI(p, ijk[2], ijk[1], ijk[0]);
+        /* InternalBoundaryReset, Src/int_bound_reset.c:33-37 */
+        if (p->internal && (p->flag[c] & FLAG_INTERNAL_BOUNDARY))
+          for (nv = 0; nv < NV; nv++) w.rhs[i][nv] = 0.0;
         for (nv = 0; nv < NV; nv++) p->uc[nv][c] += w.rhs[i][nv];
         if (dims > 1 && stage == 1)
           p->cdt[c] += 0.5 * (w.ifc[i - 1].cmax + w.ifc[i].cmax) * inv_dl;
@@ -1904,6 +1911,9 @@ void oc_set_userdef(oc_problem *p, oc_userdef_fn fn, void *user) {
   p->ud_fn = fn;
   p->ud_user = user;
 }
+
+void oc_set_internal(oc_problem *p, int on) { p->internal = on; }
+unsigned char *oc_flags(oc_problem *p) { return p->flag; }
 
 void oc_arrays(oc_problem *p, double **vc, double **bs) {
   int q;

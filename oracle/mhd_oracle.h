@@ -56,6 +56,11 @@ void oc_set_userdef(oc_problem *p, oc_userdef_fn fn, void *user);
 /* the problem's own arrays in PLUTO's layout: vc[8] ghosted cell arrays,
    bs[3] face arrays (one longer along their axis, -1 layer first) */
 void oc_arrays(oc_problem *p, double **vc, double **bs);
+/* INTERNAL_BOUNDARY: the userdef callback also runs with side 6 at the start
+   of every boundary fill; zones flagged FLAG_INTERNAL_BOUNDARY (32) in the
+   flag array (oc_flags, PLUTO layout, cleared every step) are not updated. */
+void oc_set_internal(oc_problem *p, int on);
+unsigned char *oc_flags(oc_problem *p);
 void oc_destroy(oc_problem *p);
 void oc_set_state(oc_problem *p, const double *vc, const double *bs0,
                   const double *bs1, const double *bs2);

@@ -59,6 +59,9 @@ def lib():
         L.oc_run.argtypes = [C.c_void_p, C.c_int, C.c_double, C.c_double, C.c_double, dp, dp]
         L.oc_set_userdef.argtypes = [C.c_void_p, USERDEF_FN, C.c_void_p]
         L.oc_arrays.argtypes = [C.c_void_p, C.POINTER(dp), C.POINTER(dp)]
+        L.oc_set_internal.argtypes = [C.c_void_p, C.c_int]
+        L.oc_flags.argtypes = [C.c_void_p]
+        L.oc_flags.restype = C.POINTER(C.c_ubyte)
         _lib = L
     return _lib
 
@@ -135,13 +138,19 @@ class Oracle:
         vviews = [np.ctypeslib.as_array(vp[q], shape=(nt[2], nt[1], nt[0])) for q in range(NVAR)]
         faces = [np.ctypeslib.as_array(bp[d], shape=(nt[2] + (d == 2), nt[1] + (d == 1), nt[0] + (d == 0)))
                  if (self.spec["ct"] and d < self.spec["dims"]) else None for d in range(3)]
-        self._ud_views = (_VarStack(vviews), faces)
+        flags = np.ctypeslib.as_array(lib().oc_flags(self.h), shape=(nt[2], nt[1], nt[0]))
+        self._ud_views = (_VarStack(vviews), faces, flags)
 
         def cb(user, side, vpos, stage):
-            fn(side, vpos, stage, self._ud_views[0], self._ud_views[1])
+            fn(side, vpos, stage, self._ud_views[0], self._ud_views[1], self._ud_views[2])
 
         self._ud_cb = USERDEF_FN(cb)
         lib().oc_set_userdef(self.h, self._ud_cb, None)
+
+    def set_internal_boundary(self):
+        """INTERNAL_BOUNDARY YES: the userdef callback also runs with side 6
+        before every boundary fill and sees the zone flags (set_userdef first)."""
+        lib().oc_set_internal(self.h, 1)
 
     def set_state(self, vc: np.ndarray, bs=(None, None, None)):
         vc = np.ascontiguousarray(vc, dtype=np.float64)

@@ -35,7 +35,7 @@ EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", 
            "pg_batch_download", "pg_batch_run", "pg_batch_get", "pg_batch_autotune",
            "pg_batch_set_schedule", "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set",
            "pg_adjoint_step", "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load",
-           "pg_selftest_conversions", "pg_set_userdef"]
+           "pg_selftest_conversions", "pg_set_userdef", "pg_set_internal_boundary"]
 PG_ABI_VERSION = 2  # the pg_config layout these bindings describe
 # pg_userdef_fn: (user, side 0..5, vpos 0 cells / 1..3 faces, stage)
 USERDEF_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int)
@@ -114,6 +114,7 @@ def lib():
     L.pg_checkpoint_load.argtypes = [vp, ip]
     L.pg_selftest_conversions.argtypes = [C.POINTER(C.c_ulonglong)]
     L.pg_set_userdef.argtypes = [vp, USERDEF_FN, vp, C.POINTER(dp), C.POINTER(dp)]
+    L.pg_set_internal_boundary.argtypes = [vp, C.POINTER(C.c_ubyte)]
     L.pg_last_error.restype = C.c_char_p
     for fn in ("pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
                "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
@@ -122,7 +123,7 @@ def lib():
                "pg_batch_run", "pg_batch_get", "pg_batch_autotune", "pg_batch_set_schedule",
                "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set", "pg_adjoint_step",
                "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load", "pg_selftest_conversions",
-               "pg_set_userdef"):
+               "pg_set_userdef", "pg_set_internal_boundary"):
         getattr(L, fn).restype = C.c_int
     if L.pg_abi_version() != PG_ABI_VERSION:
         raise OSError(f"libpluto_gb300 has ABI version {L.pg_abi_version()}, these bindings expect "

@@ -129,6 +129,10 @@ static void free_all(Solver* S) {
       cudaHostUnregister(S->ud_pinned[q]);
       S->ud_pinned[q] = nullptr;
     }
+  if (S->ud_pinned_flag) {
+    cudaHostUnregister(S->ud_pinned_flag);
+    S->ud_pinned_flag = nullptr;
+  }
   adjoint_free(S);
   fp64_free(S);
   mixed_free(S);
@@ -217,6 +221,44 @@ extern "C" int pg_set_userdef(pg_solver* h, pg_userdef_fn fn, void* user, double
   }
   S->ud_fn = fn;
   S->ud_user = user;
+  S->graph_dirty = true;
+  return PG_OK;
+}
+
+extern "C" int pg_set_internal_boundary(pg_solver* h, unsigned char* flags) {
+  if (!h || !flags) return fail(PG_ERR_INVALID, "pg_set_internal_boundary: null argument");
+  Solver* S = &h->S;
+  if (!S->ud_fn) return fail(PG_ERR_INVALID, "pg_set_internal_boundary: call pg_set_userdef first");
+  if (S->cfg.precision != PG_FP64 || S->cfg.time_stepping == PG_HANCOCK)
+    return fail(PG_ERR_INVALID, "pg_set_internal_boundary: PG_FP64 solvers with EULER/RK2/RK3 time stepping");
+  CK(cudaStreamSynchronize(S->stream));
+  if (S->ud_pinned_flag) {
+    cudaHostUnregister(S->ud_pinned_flag);
+    S->ud_pinned_flag = nullptr;
+  }
+  unsigned char* d = nullptr;
+  cudaPointerAttributes at;
+  if (cudaPointerGetAttributes(&at, flags) == cudaSuccess && at.type == cudaMemoryTypeHost && at.devicePointer) {
+    d = (unsigned char*)at.devicePointer;
+  } else {
+    cudaGetLastError();
+    int dev = 0, ats = 0;
+    if (cudaGetDevice(&dev) == cudaSuccess &&
+        cudaDeviceGetAttribute(&ats, cudaDevAttrPageableMemoryAccessUsesHostPageTables, dev) == cudaSuccess &&
+        ats == 1) {
+      d = flags;
+    } else {
+      cudaGetLastError();
+      if (cudaHostRegister(flags, (size_t)S->g.ncell, cudaHostRegisterMapped) != cudaSuccess ||
+          cudaHostGetDevicePointer((void**)&d, flags, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return fail(PG_ERR_CUDA, "pg_set_internal_boundary: flag array not reachable");
+      }
+      S->ud_pinned_flag = flags;
+    }
+  }
+  S->ud_dev_flag = d;
+  S->ud_internal = true;
   S->graph_dirty = true;
   return PG_OK;
 }

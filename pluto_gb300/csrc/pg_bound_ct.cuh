@@ -8,8 +8,8 @@
 // Src/initialize.c:448-453), which live in Bm1 because the face arrays do not
 // store them; then, on a non-periodic axis, k_fill_normal recovers the normal
 // face component in the ghost faces from div B = 0 (FillMagneticField,
-// Src/MHD/CT/ct_fill_mag_field.c:38-180) and, on outflow sides, averages it
-// to the cell centres (CT_AverageNormalMagField,
+// Src/MHD/CT/ct_fill_mag_field.c:38-180) and, on outflow and user-defined
+// sides, averages it to the cell centres (CT_AverageNormalMagField,
 // Src/MHD/CT/ct_field_average.c:134-275).  T is the storage type, C the
 // arithmetic type (double for the FP32-storage mixed path).
 #pragma once
@@ -233,7 +233,6 @@ static void launch_bound_ct(Solver* S, const BoundCT<T>& b, const char* copy_nam
   launch_bound_ct_axis<T, C, 0>(S, b, copy_name, fill_name);
   if (b.g.dims > 1) launch_bound_ct_axis<T, C, 1>(S, b, copy_name, fill_name);
   if (b.g.dims > 2) launch_bound_ct_axis<T, C, 2>(S, b, copy_name, fill_name);
-  S->ud_stage++;
 }
 
 }  // namespace pg

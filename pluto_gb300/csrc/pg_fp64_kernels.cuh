@@ -45,6 +45,7 @@ struct F64A {
   int device_dt;
   int bc[3];
   int ct_outflow;   // constrained transport with a non-periodic axis: per-axis boundary passes
+  int intb;         // INTERNAL_BOUNDARY: flagged zones are not updated
   int div_dims;     // RK: invDt_hyp /= DIMENSIONS (update_stage.c:311); CTU: no
   int emf_avg, c3;
 };
@@ -141,7 +142,7 @@ __global__ void k_begin_step(F64A<T> a, Box dom) {
   long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const Geom& g = a.g;
   if (q < g.ncell) {
-    a.flag[q] = 0;
+    if (!a.intb) a.flag[q] = 0;  // with internal boundaries: cleared before the first fill
     for (int d = 0; d < a.nbfield; d++) a.Bs0[d][q] = a.Bs[d][q];
   }
   if (q == 0) {
@@ -274,10 +275,14 @@ __global__ void k_update(F64A<T> a, Box box, int cdt_mode) {
   const long long c = cidx(g, k, j, i), s = g.s[DIR];
   const double dt = a.sc->dt;
   const double scrh = dt / g.dx[DIR];
+  // InternalBoundaryReset (Src/int_bound_reset.c:33-37): no update in
+  // zones of an internal boundary
+  const bool frozen = a.intb && (a.flag[c] & PG_FLAG_INTERNAL_BOUNDARY);
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
     T rhs = -scrh * (a.F[nv][c] - a.F[nv][c - s]);
     if (nv == Rot<DIR>::vn) rhs -= scrh * (a.P[c] - a.P[c - s]);
+    if (frozen) rhs = 0.0;
     a.U[nv][c] += rhs;
   }
   if (cdt_mode) {
@@ -510,6 +515,7 @@ static F64A<T> make_args(Solver* S) {
   a.div_dims = S->cfg.time_stepping != PG_HANCOCK;
   a.emf_avg = S->cfg.emf_average;
   a.c3 = S->cfg.components == 3;
+  a.intb = S->ud_internal ? 1 : 0;
   a.ct_outflow = 0;
   if (a.ct)
     for (int d = 0; d < S->g.dims; d++) a.ct_outflow |= S->cfg.bc[d] != PG_PERIODIC;
@@ -582,6 +588,7 @@ static void launch_stage_tail(Solver* S, const F64A<T>& a, const Box& dom) {
 template <class T>
 static void launch_bound(Solver* S, const F64A<T>& a) {
   const Geom& g = S->g;
+  if (S->ud_internal) launch_internal_boundary<T>(S, a.V, a.Bs, a.Bm1, a.nbfield, a.flag);
   if (a.ct_outflow || has_userdef(S)) {
     BoundCT<T> b;
     b.g = a.g;
@@ -594,13 +601,14 @@ static void launch_bound(Solver* S, const F64A<T>& a) {
     b.ncomp = a.ncomp;
     face_areas(g, b.area);
     launch_bound_ct<T, T>(S, b, "fp64_bound", "fp64_fill_normal");
-    return;
+  } else {
+    long long n0 = g.dims > 0 ? 2LL * g.beg[0] * g.nt[1] * g.nt[2] : 0;
+    long long n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
+    long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
+    PG_LAUNCH(S, "fp64_bound", (k_bound<T><<<grid_for(n0 + n1 + n2), kThreads, 0, S->stream>>>(
+                                     a, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0, n1, n2)));
   }
-  long long n0 = g.dims > 0 ? 2LL * g.beg[0] * g.nt[1] * g.nt[2] : 0;
-  long long n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
-  long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
-  PG_LAUNCH(S, "fp64_bound", (k_bound<T><<<grid_for(n0 + n1 + n2), kThreads, 0, S->stream>>>(
-                                   a, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0, n1, n2)));
+  S->ud_stage++;  // boundary fills so far in the step (the callbacks' stage index)
 }
 
 template <class T, int NSTAGE>

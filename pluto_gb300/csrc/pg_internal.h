@@ -152,7 +152,10 @@ struct Solver {
   double* ud_dev_f[3] = {};
   void* ud_pinned[11] = {};   // host arrays this library pinned (unpinned by pg_destroy)
   int ud_stage = 0;           // boundary fills enqueued so far in the step
-  UdCall ud_calls[kUdStages][6] = {};
+  UdCall ud_calls[kUdStages][7] = {};  // sides 0..5, PG_SIDE_INTERNAL
+  bool ud_internal = false;   // INTERNAL_BOUNDARY: a callback with the whole state per fill
+  unsigned char* ud_dev_flag = nullptr;  // device-usable address of the caller's flag array
+  void* ud_pinned_flag = nullptr;
 };
 
 constexpr int kThreads = 256;

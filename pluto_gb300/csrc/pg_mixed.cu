@@ -1210,6 +1210,7 @@ static void mlaunch_bound(Solver* S, const MixArgs& a) {
     b.ncomp = S->cfg.components;
     face_areas(g, b.area);
     launch_bound_ct<float, double>(S, b, "mixed_bound", "mixed_fill_normal");
+    S->ud_stage++;
     return;
   }
   BoundArrays arr;
@@ -1222,6 +1223,7 @@ static void mlaunch_bound(Solver* S, const MixArgs& a) {
   long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
   PG_LAUNCH(S, "mixed_bound", (k_mbound<<<grid_for(n0 + n1 + n2), kThreads, 0, S->stream>>>(
                                     g, arr, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0, n1, n2)));
+  S->ud_stage++;
 }
 
 

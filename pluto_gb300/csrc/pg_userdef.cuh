@@ -114,6 +114,51 @@ inline void CUDART_CB ud_host_call(void* p) {
   for (int fd = 0; fd < c->nbfield; fd++) S->ud_fn(S->ud_user, c->side, 1 + fd, c->stage);  // X*FACE
 }
 
+__global__ inline void k_flag_xfer(unsigned char* host, unsigned char* dev, long long n, int to_dev) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= n) return;
+  if (to_dev) dev[q] = host[q];
+  else host[q] = dev[q];
+}
+
+// INTERNAL_BOUNDARY (Src/boundary.c:90-92): before the fill, the callback
+// with side PG_SIDE_INTERNAL on the whole state and the zone flags; the flags
+// are cleared before the step's first fill (Src/main.c:329).
+template <class T>
+inline void launch_internal_boundary(Solver* S, T* const V[8], T* const Bs[3], T* const Bm1[3], int nbfield,
+                                     unsigned char* dflag) {
+  const Geom& g = S->g;
+  cudaStream_t st = S->stream;
+  const int stage = S->ud_stage < kUdStages ? S->ud_stage : kUdStages - 1;
+  if (S->ud_stage == 0) cudaMemsetAsync(dflag, 0, (size_t)g.ncell, st);
+  IBox cb;
+  for (int d = 0; d < 3; d++) {
+    cb.lo[d] = 0;
+    cb.hi[d] = g.nt[d] - 1;
+  }
+  for (int dir = 0; dir < 2; dir++) {
+    const int up = dir;
+    if (up) {
+      UdCall* c = &S->ud_calls[stage][PG_SIDE_INTERNAL];
+      c->S = S;
+      c->side = PG_SIDE_INTERNAL;
+      c->stage = S->ud_stage + 1;
+      c->nbfield = 0;  // one call, UserDefBoundary (d, NULL, 0, grid)
+      cudaLaunchHostFunc(st, ud_host_call, c);
+    }
+    for (int nv = 0; nv < NV; nv++)
+      if (S->ud_dev_v[nv])
+        k_box_xfer<T><<<grid_for(cb.count()), kThreads, 0, st>>>(S->ud_dev_v[nv], V[nv], (T*)nullptr, g, -1, cb, up);
+    for (int fd = 0; fd < nbfield; fd++) {
+      if (!S->ud_dev_f[fd]) continue;
+      IBox fb = cb;
+      fb.lo[fd] = -1;
+      k_box_xfer<T><<<grid_for(fb.count()), kThreads, 0, st>>>(S->ud_dev_f[fd], Bs[fd], Bm1[fd], g, fd, fb, up);
+    }
+    k_flag_xfer<<<grid_for(g.ncell), kThreads, 0, st>>>(S->ud_dev_flag, dflag, g.ncell, up);
+  }
+}
+
 // the USERDEF sides of axis ax, after the other sides of the axis were filled
 template <class T>
 inline void launch_userdef_axis(Solver* S, T* const V[8], T* const Bs[3], T* const Bm1[3], int nbfield, int ax) {

@@ -152,6 +152,11 @@ static void gpu_userdef(void *user, int side, int vpos, int stage)
   RBox box;
 
   (void)user;
+  g_intStage = stage;
+  if (side == PG_SIDE_INTERNAL) {  /* INTERNAL_BOUNDARY, Src/boundary.c:90-92 */
+    UserDefBoundary (s_data, NULL, 0, s_grid);
+    return;
+  }
   if      (side == 0) {ib = IBEG - 1; ie = 0;}
   else if (side == 1) {ib = IEND + 1; ie = NX1_TOT - 1;}
   else if (side == 2) {jb = JBEG - 1; je = 0;}
@@ -211,7 +216,13 @@ int AdvanceStep (Data *d, Riemann_Solver *Riemann, timeStep *Dts, Grid *grid)
     gpu_check(pg_create(&cfg, &s_gpu), "pg_create");
     for (dd = 0; dd < DIMENSIONS; dd++)
       ud |= grid->lbound[dd] == USERDEF || grid->rbound[dd] == USERDEF;
+  #if INTERNAL_BOUNDARY == YES
+    ud = 1;
+  #endif
     if (ud) gpu_check(pg_set_userdef(s_gpu, gpu_userdef, NULL, vars, faces), "pg_set_userdef");
+  #if INTERNAL_BOUNDARY == YES
+    gpu_check(pg_set_internal_boundary(s_gpu, d->flag[0][0]), "pg_set_internal_boundary");
+  #endif
     gpu_check(pg_upload(s_gpu, (const double *const *)vars, (const double *const *)faces,
                         PG_LAYOUT_PLUTO), "pg_upload");
   } else if (up_every > 0 && s_calls % up_every == 0) {

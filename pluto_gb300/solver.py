@@ -147,19 +147,30 @@ class Solver:
         the box of face component 1..3); vc [8, nt2, nt1, nt0] and faces[d]
         (one longer along d, -1 layer first) are PLUTO-layout host arrays that
         hold the current state near the side; fn writes the side's ghost
-        boxes.  It runs on a CUDA host thread while the step waits for it."""
+        boxes.  It runs on a CUDA host thread while the step waits for it.
+        A sixth argument, flags, is the zone-flag array (internal boundaries)."""
         nz, ny, nx = self.ghost_shape()
         self._ud_vc = np.zeros((NVAR, nz, ny, nx))
         self._ud_f = [np.zeros((nz + (d == 2), ny + (d == 1), nx + (d == 0)))
                       if (self.ct and d < self.dims) else None for d in range(3)]
 
+        self._ud_flags = np.zeros((nz, ny, nx), dtype=np.uint8)
+
         def cb(user, side, vpos, stage):
-            fn(side, vpos, stage, self._ud_vc, self._ud_f)
+            fn(side, vpos, stage, self._ud_vc, self._ud_f, self._ud_flags)
 
         self._ud_cb = L.USERDEF_FN(cb)
         views = [self._ud_vc[q] for q in range(NVAR)]
         L.check(L.lib().pg_set_userdef(self.h, self._ud_cb, None, _ptrs(views, 8), _ptrs(self._ud_f, 3)),
                 "pg_set_userdef")
+
+    def set_internal_boundary(self):
+        """INTERNAL_BOUNDARY YES: the set_userdef function is also called with
+        side 6 (PG_SIDE_INTERNAL) before every boundary fill, with the whole
+        state and the zone flags (flags, uint8, PLUTO layout); zones flagged 32
+        are not updated.  FP64 solvers with EULER/RK2/RK3 time stepping."""
+        ptr = self._ud_flags.ctypes.data_as(C.POINTER(C.c_ubyte))
+        L.check(L.lib().pg_set_internal_boundary(self.h, ptr), "pg_set_internal_boundary")
 
     def upload(self, vc: np.ndarray, bs=(None, None, None)):
         self._put("pg_upload", vc, bs)

@@ -50,6 +50,7 @@ def spec_of(s: br.Setup) -> dict:
                 lo=list(s.lo), hi=list(s.hi), gamma=gamma, recon=s.recon,
                 limiter=s.limiter, solver=s.solver, stepping=s.stepping, ct=s.ct, emf=s.emf,
                 bc=s.bc, cfl=s.cfl, first_dt=s.first_dt, steps=s.steps,
+                internal_boundary=s.internal_boundary,
                 params=s.params)
 
 
@@ -101,6 +102,19 @@ USERDEF_C = r"""
   #endif
 #endif
   }
+#if INTERNAL_BOUNDARY == YES
+  if (side == 0) {  /* internal boundary: a dense block that is not updated */
+    TOT_LOOP(k, j, i) {
+      if (i >= IBEG + NX1/4 && i < IBEG + NX1/4 + 3 && j >= JBEG + NX2/2 - 2 && j < JBEG + NX2/2 + 2) {
+        d->Vc[RHO][k][j][i] = 10.0;
+        d->Vc[VX1][k][j][i] = 0.0;
+        d->Vc[VX2][k][j][i] = 0.0;
+        d->Vc[PRS][k][j][i] = 1.0;
+        d->flag[k][j][i] |= FLAG_INTERNAL_BOUNDARY;
+      }
+    }
+  }
+#endif
 #if DIMENSIONS == 3
   if (side == X3_END) {
     if (box->vpos == CENTER) {
@@ -168,6 +182,9 @@ def setups():
                 bc=(("periodic", "periodic"), ("outflow", "outflow"), ("reflective", "userdef"))),
         replace(br.blast_setup(16, 12), name="blast_userdef_ct_16", userdef_body=USERDEF_C,
                 bc=(("userdef", "outflow"), ("periodic", "periodic"), ("reflective", "userdef"))),
+        # INTERNAL_BOUNDARY (UserDefBoundary with side 0 before every fill)
+        replace(br.ot_setup("hlld", 32, 30), name="ot_internal_32", userdef_body=USERDEF_C,
+                internal_boundary=True),
         # TIME_STEPPING EULER (the RK predictor alone)
         replace(br.ot_setup("hlld", 32, 10), stepping="EULER", cfl=0.2, name="ot_euler_32"),
         replace(br.tube_setup(0, 256, 60), stepping="EULER", name="tube_euler_0_256"),

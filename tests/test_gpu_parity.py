@@ -20,6 +20,8 @@ def _solver(meta, precision="fp64", **kw):
     s = Solver(meta, precision=precision, **kw)
     if userdef_cases.has_userdef(meta):
         s.set_userdef(userdef_cases.make(meta))
+        if meta.get("internal_boundary"):
+            s.set_internal_boundary()
     return s
 
 
@@ -51,7 +53,7 @@ def test_fp64_matches_reference_goldens(name):
                                   "cpa_eqtsym_32", "tube_reflective_0_256", "ot_ctu_reflective_32",
                                   "blast_sides_16", "ot_sides_32", "ot_ctu_sides_32", "tube_sides_0_256",
                                   "ot_userdef_32", "blast_userdef_16", "blast_userdef_ct_16",
-                                  "ot_euler_32", "tube_euler_0_256"])
+                                  "ot_euler_32", "tube_euler_0_256", "ot_internal_32"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)

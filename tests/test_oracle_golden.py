@@ -18,6 +18,8 @@ def test_oracle_matches_reference_bitwise(name):
     o = Oracle(meta, nthreads=2)
     if userdef_cases.has_userdef(meta):
         o.set_userdef(userdef_cases.make(meta))
+        if meta.get("internal_boundary"):
+            o.set_internal_boundary()
     o.set_state(vc0, bs0)
     dts, t = o.run(meta["steps"], meta["first_dt"], meta["cfl"])
     vc, bs = o.get_state()

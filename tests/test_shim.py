@@ -69,3 +69,12 @@ def test_enable_script_edits_the_template_makefile(tmp_path):
     assert mk.read_text() == once
     en.main([str(mk), "--disable"])
     assert mk.read_text() == orig
+
+
+def test_shim_links_internal_boundary(tmp_path):
+    """INTERNAL_BOUNDARY YES: the shim registers the flag array and calls
+    UserDefBoundary with a null box."""
+    from dataclasses import replace
+    from oracle import build_ref as br
+    s = replace(br.ot_setup("hlld", 32, 30), name="ot_shim_internal", internal_boundary=True)
+    assert _link(lambda: s, tmp_path).exists()

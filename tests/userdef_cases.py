@@ -6,6 +6,8 @@ state on the middle half of the rows, a mirror wall (vx, Bx negated)
 elsewhere, and the staggered By and Bz of the side's x2face / x3face boxes
 likewise -- and an X3_END side copied from the last interior plane (cells with
 vz = 0 and p = 0.1, the staggered Bx and By of its boxes).
+With INTERNAL_BOUNDARY, a dense block (rho 10, v 0, p 1) a quarter of the
+way along x is set before every fill and flagged so it is not updated.
 Only assignments and negations, so results match the C version bit for bit.
 
 The callback signature is the one of Solver.set_userdef / Oracle.set_userdef:
@@ -19,7 +21,7 @@ RHO, VX1, VX2, VX3, BX1, BX2, BX3, PRS = range(8)
 
 def has_userdef(spec) -> bool:
     bc = spec.get("bc", "periodic")
-    return "userdef" in repr(bc)
+    return "userdef" in repr(bc) or bool(spec.get("internal_boundary"))
 
 
 def nghost(spec) -> int:
@@ -37,8 +39,16 @@ def make(spec):
     lo, hi = jbeg + nx2 // 4, jbeg + (3 * nx2) // 4
     inflow = ((RHO, 2.0), (VX1, 0.5), (VX2, 0.0), (PRS, 0.3), (BX1, 0.2), (BX2, 0.1), (VX3, 0.0), (BX3, 0.0))
 
-    def fn(side, vpos, stage, vc, faces):
-        if side == 0:  # X1_BEG
+    nx1 = int(spec["nx"][0])
+    i0, j0 = ng + nx1 // 4, jbeg + nx2 // 2 - 2
+
+    def fn(side, vpos, stage, vc, faces, flags=None):
+        if side == 6:  # internal boundary: a dense block that is not updated
+            if flags is not None:
+                for q, val in ((RHO, 10.0), (VX1, 0.0), (VX2, 0.0), (PRS, 1.0)):
+                    vc[q][:, j0:j0 + 4, i0:i0 + 3] = val
+                flags[:, j0:j0 + 4, i0:i0 + 3] |= 32
+        elif side == 0:  # X1_BEG
             if vpos == 0:  # CENTER
                 j = np.arange(vc[0].shape[1])
                 noz = (j >= lo) & (j < hi)
