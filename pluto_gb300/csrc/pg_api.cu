@@ -229,8 +229,8 @@ extern "C" int pg_set_internal_boundary(pg_solver* h, unsigned char* flags) {
   if (!h || !flags) return fail(PG_ERR_INVALID, "pg_set_internal_boundary: null argument");
   Solver* S = &h->S;
   if (!S->ud_fn) return fail(PG_ERR_INVALID, "pg_set_internal_boundary: call pg_set_userdef first");
-  if (S->cfg.precision != PG_FP64 || S->cfg.time_stepping == PG_HANCOCK)
-    return fail(PG_ERR_INVALID, "pg_set_internal_boundary: PG_FP64 solvers with EULER/RK2/RK3 time stepping");
+  if (S->cfg.precision == PG_FP64_TANGENT || S->cfg.time_stepping == PG_HANCOCK)
+    return fail(PG_ERR_INVALID, "pg_set_internal_boundary: EULER/RK2/RK3 time stepping, FP64 or mixed");
   CK(cudaStreamSynchronize(S->stream));
   if (S->ud_pinned_flag) {
     cudaHostUnregister(S->ud_pinned_flag);

@@ -436,7 +436,7 @@ __global__ void k_ctu_c2p_half(F64A<T> a, Box box) {
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) u[nv] = a.Uh[nv][c];
   unsigned char fl = a.flag[c];
-  if (cons_to_prim(u, v, T(a.gamma - 1.0), T(a.small_rho), T(a.small_p), &fl)) a.flag[c] = fl;
+  if (cons_to_prim(u, v, T(a.gamma - 1.0), T(a.small_rho), T(a.small_p), &fl)) a.flag[c] |= fl;
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
     a.Uh[nv][c] = u[nv];

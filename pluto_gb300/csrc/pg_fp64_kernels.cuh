@@ -420,7 +420,7 @@ __global__ void k_finalize(F64A<T> a, Box dom, int reduce_cdt) {
       for (int d = 0; d < g.dims; d++) u[BX1 + d] = 0.5 * (a.Bs[d][c] + a.Bs[d][c - g.s[d]]);
     unsigned char fl = a.flag[c];
     fails = cons_to_prim(u, v, T(a.gamma - 1.0), T(a.small_rho), T(a.small_p), &fl);
-    if (fails) a.flag[c] = fl;
+    if (fails) a.flag[c] |= fl;  // flag[i] |= FLAG_CONS2PRIM_FAIL (mappers.c)
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
       a.U[nv][c] = u[nv];

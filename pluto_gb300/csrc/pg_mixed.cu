@@ -71,6 +71,7 @@ struct MixArgs {
   float inv_gmm1_hi, inv_gmm1_lo;  // the same as a double-word pair
   float third_hi, third_lo;        // 1/3 as a double-word pair
   int limiter, recon, ct, nbfield, accmask, device_dt, ncomp;
+  int intb;  // INTERNAL_BOUNDARY: flagged zones are not updated
 };
 
 // ---------------------------------------------------------------------------
@@ -803,6 +804,9 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
     float du[NV];
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) du[nv] = (msk & (1 << nv)) ? a.dU[nv][c] : 0.f;
+    if (a.intb && (a.flag[c] & PG_FLAG_INTERNAL_BOUNDARY))  // Src/int_bound_reset.c:33-37
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) du[nv] = 0.f;
     if (STAGE == 2 && NSTAGE == 2) {  // (U0 + U1 + dU) / 2
       const T u0rho = O::ld(a.U0, RHO * n + c), u0E = O::ld(a.U0, ENG * n + c);
       u.rho = O::half_sum3(u0rho, u.rho, du[RHO]);
@@ -893,7 +897,7 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
       bad |= ((__float_as_uint(out[nv]) >> 23) & 0xff) == 0xff;
     }
     if (fl) {
-      a.flag[c] = fl;
+      a.flag[c] |= fl;
       fails = true;
     }
     if (reduce_cdt) cd = a.CDT[c];
@@ -924,6 +928,41 @@ __global__ void k_mcons_init(MixArgs a, Box dom) {
   float v[NV];
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) v[nv] = a.Vin[nv][c];
+  const ConsA<A> u = cons_of<A>(v, O::konst(a.inv_gmm1_d, a.inv_gmm1_hi, a.inv_gmm1_lo));
+  O::st(a.U0, RHO * n + c, u.rho);
+  O::st(a.U0, ENG * n + c, u.E);
+#pragma unroll
+  for (int d = 0; d < 3; d++) {
+    O::st(a.U0, (VX1 + d) * n + c, u.m[d]);
+    O::st(a.U0, (BX1 + d) * n + c, u.b[d]);
+  }
+}
+
+// INTERNAL_BOUNDARY, stage 1: the reference builds U0 from the primitives
+// after the callback (rk_step.c:93-96); here U0 is resident, so it is rebuilt
+// in the zones whose primitives the callback changed (prev: the state before
+// the callback; narrowing a widened float gives it back, so unchanged zones
+// compare equal).
+struct V8 {
+  const float* p[8];
+};
+template <class A>
+__global__ void k_mrefresh(MixArgs a, V8 prev, Box dom) {
+  using O = Acc<A>;
+  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= dom.count()) return;
+  int i, j, k;
+  dom.coords(q, i, j, k);
+  const Geom& g = a.g;
+  const long long c = cidx(g, k, j, i), n = g.ncell;
+  float v[NV];
+  bool changed = false;
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    v[nv] = a.Vin[nv][c];
+    changed |= __float_as_uint(v[nv]) != __float_as_uint(prev.p[nv][c]);
+  }
+  if (!changed) return;
   const ConsA<A> u = cons_of<A>(v, O::konst(a.inv_gmm1_d, a.inv_gmm1_hi, a.inv_gmm1_lo));
   O::st(a.U0, RHO * n + c, u.rho);
   O::st(a.U0, ENG * n + c, u.E);
@@ -1192,12 +1231,38 @@ static MixArgs margs(Solver* S, int in_buf, int out_buf, int v0_buf) {
   if (a.ct)
     for (int d = 0; d < S->g.dims; d++) a.accmask &= ~(1 << (BX1 + d));
   a.device_dt = S->device_dt;
+  a.intb = S->ud_internal ? 1 : 0;
   return a;
 }
 
 static void mlaunch_bound(Solver* S, const MixArgs& a) {
   const Geom& g = S->g;
   MixedState* M = (MixedState*)S->mixed;
+  if (S->ud_internal) {  // INTERNAL_BOUNDARY: the callback on the whole state first
+    const bool first = S->ud_stage == 0;
+    const int other = a.Vin[0] == M->b.V[0][0] ? 1 : 0;  // free during stage 1's fill
+    if (first)
+      cudaMemcpyAsync(M->b.V[other][0], a.Vin[0], 8 * (size_t)g.ncell * sizeof(float), cudaMemcpyDeviceToDevice,
+                      S->stream);
+    float* vin[8];
+    float* bin[3];
+    for (int nv = 0; nv < NV; nv++) vin[nv] = (float*)a.Vin[nv];
+    for (int d = 0; d < 3; d++) bin[d] = (float*)a.Bin[d];
+    launch_internal_boundary<float>(S, vin, bin, M->b.Bm1, a.nbfield, M->b.flag);
+    if (first) {
+      Box dom;
+      for (int ax = 0; ax < 3; ax++) {
+        dom.lo[ax] = g.beg[ax];
+        dom.hi[ax] = g.end[ax];
+      }
+      V8 prev;
+      for (int nv = 0; nv < NV; nv++) prev.p[nv] = M->b.V[other][nv];
+      if (S->cfg.precision == PG_MIXED_DW)
+        k_mrefresh<dw><<<grid_for(dom.count()), kThreads, 0, S->stream>>>(a, prev, dom);
+      else
+        k_mrefresh<double><<<grid_for(dom.count()), kThreads, 0, S->stream>>>(a, prev, dom);
+    }
+  }
   if ((a.ct && M->b.Bm1[0]) || has_userdef(S)) {  // non-periodic axis under CT, or a user-defined side: per-axis passes
     BoundCT<float> b;
     b.g = g;

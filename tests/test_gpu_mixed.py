@@ -19,6 +19,8 @@ def _s(spec, precision):
     s = Solver(spec, precision=precision)
     if userdef_cases.has_userdef(spec):
         s.set_userdef(userdef_cases.make(spec))
+        if spec.get("internal_boundary"):
+            s.set_internal_boundary()
     return s
 
 
@@ -81,7 +83,7 @@ def test_tma_sweeps_match_plain_sweeps(case, prec, monkeypatch):
 
 
 # the CTU step (TIME_STEPPING HANCOCK) runs on the FP64 path only
-RK_GOLDENS = [n for n in GOLDEN_NAMES if "_ctu" not in n and "_internal" not in n]
+RK_GOLDENS = [n for n in GOLDEN_NAMES if "_ctu" not in n]
 
 
 @pytest.mark.parametrize("prec", MIXED)
