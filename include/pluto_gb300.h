@@ -242,7 +242,7 @@ int pg_set_userdef(pg_solver *s, pg_userdef_fn fn, void *user, double *const var
    Src/main.c:329 does); afterwards it reads the whole state and the flags
    back.  Zones flagged PG_FLAG_INTERNAL_BOUNDARY get a zero right-hand side
    (Src/int_bound_reset.c).  Each fill moves the whole state across the host
-   link.  PG_FP64 solvers with EULER/RK2/RK3 time stepping; call
+   link.  EULER/RK2/RK3 time stepping on the FP64 and mixed paths; call
    pg_set_userdef first. */
 #define PG_SIDE_INTERNAL 6
 #define PG_FLAG_INTERNAL_BOUNDARY 32  /* Src/pluto.h:197 */

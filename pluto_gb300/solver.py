@@ -168,7 +168,7 @@ class Solver:
         """INTERNAL_BOUNDARY YES: the set_userdef function is also called with
         side 6 (PG_SIDE_INTERNAL) before every boundary fill, with the whole
         state and the zone flags (flags, uint8, PLUTO layout); zones flagged 32
-        are not updated.  FP64 solvers with EULER/RK2/RK3 time stepping."""
+        are not updated.  EULER/RK2/RK3 time stepping, FP64 or mixed."""
         ptr = self._ud_flags.ctypes.data_as(C.POINTER(C.c_ubyte))
         L.check(L.lib().pg_set_internal_boundary(self.h, ptr), "pg_set_internal_boundary")
 
