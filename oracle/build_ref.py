@@ -223,8 +223,14 @@ def build(s: Setup, jobs: int = 8) -> Path:
     (run / "init.c").write_text(INIT_TEMPLATE % (s.init_body, s.userdef_body))
     names = list(BASE_SRC)
     names += ["plm_states"] if s.recon == "LINEAR" else ["ppm_states", "ppm_coeffs"]
-    # time stepping: RK (rk_step + update_stage) or CTU (ctu_step + hancock)
-    names += ["ctu_step", "hancock"] if s.stepping == "HANCOCK" else ["rk_step", "update_stage"]
+    # time stepping: RK (rk_step + update_stage) or CTU (ctu_step + hancock,
+    # or char_tracing for CHARACTERISTIC_TRACING)
+    if s.stepping == "HANCOCK":
+        names += ["ctu_step", "hancock"]
+    elif s.stepping == "CHARACTERISTIC_TRACING":
+        names += ["ctu_step", "char_tracing"]
+    else:
+        names += ["rk_step", "update_stage"]
     if s.ct:
         names += CT_SRC
     srcs = [run / "init.c"]

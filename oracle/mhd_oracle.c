@@ -1253,6 +1253,242 @@ static void prim_rhs(const double *v, const double *dv, double gamma, const Rot 
   Adv[PRS] = gamma * v[PRS] * dv[vn] + v[vn] * dv[PRS];
 }
 
+
+/* PrimEigenvectors, Src/MHD/eigenv.c:190-688: primitive eigenvalues and
+   eigenvectors of ideal MHD along the sweep (no 8-wave / GLM terms: the div-B
+   wave has lambda 0 and no vectors).  Waves in the order of
+   Src/MHD/mod_defs.h:54-71; L[wave][slot], R[slot][wave] over this file's 8
+   variable slots; entries not set stay zero.  dims: DIMENSIONS (the 2D
+   Alfven hot fix, eigenv.c:528-531). */
+enum { WFM = 0, WFP, WEN, WDB, WSM, WSP, WAM, WAP };
+static void prim_eigen(const double *q, double a2, const Rot *r, int c3, int dims, double L[8][8],
+                       double R[8][8], double *lambda) {
+  const int vn = r->vn, vt = r->vt, vb = r->vb, bn = r->bn, bt = r->bt, bb = r->bb;
+  const double sqrt_1_2 = 0.70710678118654752440;
+  double u, tau, sqrt_rho, scrh0, scrh1, scrh2, scrh3, scrh4, b2, ca2, A2, At2, cf2, cs2, cf, cs, ca, a;
+  double alpha_f, alpha_s, beta_y, beta_z = 0.0, S;
+  int k;
+  memset(L, 0, sizeof(double[8][8]));
+  memset(R, 0, sizeof(double[8][8]));
+  u = q[vn];
+  tau = 1.0 / q[RHO];
+  sqrt_rho = sqrt(q[RHO]);
+  scrh2 = q[bn] * q[bn];
+  scrh3 = c3 ? 0.0 + q[bt] * q[bt] + q[bb] * q[bb] : 0.0 + q[bt] * q[bt];
+  b2 = scrh2 + scrh3;
+  ca2 = scrh2 * tau;
+  A2 = b2 * tau;
+  At2 = scrh3 * tau;
+  scrh1 = a2 - A2;
+  scrh0 = sqrt(scrh1 * scrh1 + 4.0 * a2 * At2);
+  cf2 = 0.5 * (a2 + A2 + scrh0);
+  cs2 = a2 * ca2 / cf2;
+  cf = sqrt(cf2);
+  cs = sqrt(cs2);
+  ca = sqrt(ca2);
+  a = sqrt(a2);
+  if (cf == cs) {
+    alpha_f = 1.0;
+    alpha_s = 0.0;
+  } else {
+    scrh0 = 1.0 / scrh0;
+    alpha_f = (a2 - cs2) * scrh0;
+    alpha_s = (cf2 - a2) * scrh0;
+    alpha_f = MAX(0.0, alpha_f);
+    alpha_s = MAX(0.0, alpha_s);
+    alpha_f = sqrt(alpha_f);
+    alpha_s = sqrt(alpha_s);
+  }
+  scrh0 = sqrt(scrh3);
+  if (scrh0 > 1.e-9) {
+    if (c3) {
+      beta_y = q[bt] / scrh0;
+      beta_z = q[bb] / scrh0;
+    } else {
+      beta_y = (q[bt] >= 0.0 ? 1.0 : -1.0);
+    }
+  } else {
+    if (c3) beta_z = beta_y = sqrt_1_2;
+    else beta_y = 1.0;
+  }
+  S = (q[bn] >= 0.0 ? 1.0 : -1.0);
+
+  k = WFM; /* fast wave, u - c_f */
+  lambda[k] = u - cf;
+  scrh0 = alpha_s * cs * S;
+  scrh1 = alpha_s * sqrt_rho * a;
+  scrh2 = 0.5 / a2;
+  scrh3 = scrh2 * tau;
+  R[RHO][k] = q[RHO] * alpha_f;
+  R[vn][k] = -cf * alpha_f;
+  R[vt][k] = scrh0 * beta_y;
+  if (c3) R[vb][k] = scrh0 * beta_z;
+  R[bt][k] = scrh1 * beta_y;
+  if (c3) R[bb][k] = scrh1 * beta_z;
+  scrh4 = alpha_f * a2 * q[RHO];
+  R[PRS][k] = scrh4;
+  L[k][vn] = R[vn][k] * scrh2;
+  L[k][vt] = R[vt][k] * scrh2;
+  if (c3) L[k][vb] = R[vb][k] * scrh2;
+  L[k][bt] = R[bt][k] * scrh3;
+  if (c3) L[k][bb] = R[bb][k] * scrh3;
+  L[k][PRS] = alpha_f * scrh3;
+
+  k = WFP; /* fast wave, u + c_f */
+  lambda[k] = u + cf;
+  R[RHO][k] = R[RHO][WFM];
+  R[vn][k] = -R[vn][WFM];
+  R[vt][k] = -R[vt][WFM];
+  if (c3) R[vb][k] = -R[vb][WFM];
+  R[bt][k] = R[bt][WFM];
+  if (c3) R[bb][k] = R[bb][WFM];
+  R[PRS][k] = R[PRS][WFM];
+  L[k][vn] = -L[WFM][vn];
+  L[k][vt] = -L[WFM][vt];
+  if (c3) L[k][vb] = -L[WFM][vb];
+  L[k][bt] = L[WFM][bt];
+  if (c3) L[k][bb] = L[WFM][bb];
+  L[k][PRS] = L[WFM][PRS];
+
+  k = WEN; /* entropy wave, u */
+  lambda[k] = u;
+  R[RHO][k] = 1.0;
+  L[k][RHO] = 1.0;
+  L[k][PRS] = -1.0 / a2;
+
+  lambda[WDB] = 0.0; /* div-B wave (no 8-wave control) */
+
+  k = WSM; /* slow wave, u - c_s */
+  lambda[k] = u - cs;
+  scrh0 = alpha_f * cf * S;
+  scrh1 = alpha_f * sqrt_rho * a;
+  R[RHO][k] = q[RHO] * alpha_s;
+  R[vn][k] = -cs * alpha_s;
+  R[vt][k] = -scrh0 * beta_y;
+  if (c3) R[vb][k] = -scrh0 * beta_z;
+  R[bt][k] = -scrh1 * beta_y;
+  if (c3) R[bb][k] = -scrh1 * beta_z;
+  scrh4 = alpha_s * a2 * q[RHO];
+  R[PRS][k] = scrh4;
+  L[k][vn] = R[vn][k] * scrh2;
+  L[k][vt] = R[vt][k] * scrh2;
+  if (c3) L[k][vb] = R[vb][k] * scrh2;
+  L[k][bt] = R[bt][k] * scrh3;
+  if (c3) L[k][bb] = R[bb][k] * scrh3;
+  L[k][PRS] = alpha_s * scrh3;
+
+  k = WSP; /* slow wave, u + c_s */
+  lambda[k] = u + cs;
+  R[RHO][k] = R[RHO][WSM];
+  R[vn][k] = -R[vn][WSM];
+  R[vt][k] = -R[vt][WSM];
+  if (c3) R[vb][k] = -R[vb][WSM];
+  R[bt][k] = R[bt][WSM];
+  if (c3) R[bb][k] = R[bb][WSM];
+  R[PRS][k] = scrh4;
+  L[k][vn] = -L[WSM][vn];
+  L[k][vt] = -L[WSM][vt];
+  if (c3) L[k][vb] = -L[WSM][vb];
+  L[k][bt] = L[WSM][bt];
+  if (c3) L[k][bb] = L[WSM][bb];
+  L[k][PRS] = L[WSM][PRS];
+
+  if (c3) {
+    k = WAM; /* Alfven wave, u - c_a */
+    lambda[k] = u - ca;
+    scrh2 = beta_y * sqrt_1_2;
+    scrh3 = beta_z * sqrt_1_2;
+    R[vt][k] = -scrh3;
+    R[vb][k] = scrh2;
+    R[bt][k] = -scrh3 * sqrt_rho * S;
+    R[bb][k] = scrh2 * sqrt_rho * S;
+    L[k][vt] = R[vt][k];
+    L[k][vb] = R[vb][k];
+    L[k][bt] = R[bt][k] * tau;
+    L[k][bb] = R[bb][k] * tau;
+
+    k = WAP; /* Alfven wave, u + c_a */
+    lambda[k] = u + ca;
+    R[vt][k] = R[vt][WAM];
+    R[vb][k] = R[vb][WAM];
+    R[bt][k] = -R[bt][WAM];
+    R[bb][k] = -R[bb][WAM];
+    L[k][vt] = L[WAM][vt];
+    L[k][vb] = L[WAM][vb];
+    L[k][bt] = -L[WAM][bt];
+    L[k][bb] = -L[WAM][bb];
+    if (dims <= 2 && q[bn] == 0 && q[bt] == 0.0)
+      for (k = 0; k < 8; k++) R[bt][k] = 0.0;
+  }
+}
+
+/* PrimToChar, Src/MHD/eigenv.c:1310-1380: w = L . v from the nonzero entries */
+static void prim_to_char(double L[8][8], const double *v, const Rot *r, int c3, double *w) {
+  const int vn = r->vn, vt = r->vt, vb = r->vb, bt = r->bt, bb = r->bb;
+  const double *l = L[WFM];
+  double wv, wB;
+  wv = c3 ? l[vn] * v[vn] + l[vt] * v[vt] + l[vb] * v[vb] : l[vn] * v[vn] + l[vt] * v[vt];
+  wB = c3 ? l[PRS] * v[PRS] + l[bt] * v[bt] + l[bb] * v[bb] : l[PRS] * v[PRS] + l[bt] * v[bt];
+  w[WFM] = wv + wB;
+  w[WFP] = -wv + wB;
+  l = L[WEN];
+  w[WEN] = l[RHO] * v[RHO] + l[PRS] * v[PRS];
+  w[WDB] = 0.0;
+  l = L[WSM];
+  wv = c3 ? l[vn] * v[vn] + l[vt] * v[vt] + l[vb] * v[vb] : l[vn] * v[vn] + l[vt] * v[vt];
+  wB = c3 ? l[PRS] * v[PRS] + l[bt] * v[bt] + l[bb] * v[bb] : l[PRS] * v[PRS] + l[bt] * v[bt];
+  w[WSM] = wv + wB;
+  w[WSP] = -wv + wB;
+  if (c3) {
+    l = L[WAM];
+    wv = l[vt] * v[vt] + l[vb] * v[vb];
+    wB = l[bt] * v[bt] + l[bb] * v[bb];
+    w[WAM] = wv + wB;
+    w[WAP] = wv - wB;
+  }
+}
+
+/* CharTracingStep, Src/States/char_tracing.c:280-573 (LINEAR reconstruction,
+   CHTR_REF_STATE 3, Cartesian, no passive scalars; PrimSource is zero for
+   ideal Cartesian MHD without body forces, prim_eqn.c:202, and is still
+   added as +0).  vc: cell-centre state; vp, vm: its PLM states, updated in
+   place.  Variables of COMPONENTS 2 problems skip the third component slots. */
+static void char_tracing(const double *vc, double *vp, double *vm, double gamma, double dtdx, double dt,
+                         const Rot *r, int c3, int dims) {
+  double L[8][8], R[8][8], lambda[8], nu[8], dv[NV], dw[8], nu_max, nu_min;
+  const int nflx = c3 ? 8 : 6;
+  const double a2 = gamma * vc[PRS] / vc[RHO]; /* SoundSpeed2, Src/EOS/Ideal/eos.c:22 */
+  const double src = 0.0;
+  int k, nv;
+  prim_eigen(vc, a2, r, c3, dims, L, R, lambda);
+  for (k = 0; k < nflx; k++) nu[k] = dtdx * lambda[k];
+  nu_max = MAX(nu[1], 0.0);
+  nu_min = MIN(nu[0], 0.0);
+  for (nv = NV; nv--;) dv[nv] = vp[nv] - vm[nv];
+  prim_to_char(L, dv, r, c3, dw);
+  for (nv = NV; nv--;) {
+    if (!c3 && (nv == VX3 || nv == BX3)) continue;
+    vp[nv] = vc[nv] + 0.5 * dv[nv] * (1.0 - nu_max);
+    vm[nv] = vc[nv] - 0.5 * dv[nv] * (1.0 + nu_min);
+  }
+  for (k = 0; k < nflx; k++) {
+    if (nu[k] >= 0.0) {
+      dw[k] *= 0.5 * (nu_max - nu[k]);
+      for (nv = 0; nv < NV; nv++)
+        if (c3 || (nv != VX3 && nv != BX3)) vp[nv] += dw[k] * R[nv][k];
+    } else {
+      dw[k] *= 0.5 * (nu_min - nu[k]);
+      for (nv = 0; nv < NV; nv++)
+        if (c3 || (nv != VX3 && nv != BX3)) vm[nv] += dw[k] * R[nv][k];
+    }
+  }
+  for (nv = NV; nv--;) {
+    if (!c3 && (nv == VX3 || nv == BX3)) continue;
+    vp[nv] += 0.5 * dt * src;
+    vm[nv] += 0.5 * dt * src;
+  }
+}
+
 /* face-EMF slot of (dir, component): ezi, ezj, eyi, eyk, exj, exk */
 enum { EZI = 0, EZJ, EYI, EYK, EXJ, EXK };
 
@@ -1315,14 +1551,24 @@ static void ctu_sweep(oc_problem *p, int dir, double dt, int stage, double *inv_
             w.vp[i][r.bn] = w.bn[i];
             w.vm[i + 1][r.bn] = w.bn[i];
           }
-        for (i = nbeg - 1; i <= nend + 1; i++) { /* primitive Hancock step */
-          double dv[NV], Adv[NV];
-          for (nv = 0; nv < NV; nv++) dv[nv] = w.vp[i][nv] - w.vm[i][nv];
-          prim_rhs(w.v[i], dv, p->c.gamma, &r, c3, Adv);
-          for (nv = NV - 1; nv >= 0; nv--) {
-            double scrh = dt2 * (inv_dl * Adv[nv] - 0.0);
-            w.vp[i][nv] -= scrh;
-            w.vm[i][nv] -= scrh;
+        if (p->c.stepping == OC_CHARTR) { /* CharTracingStep, then its face field */
+          for (i = nbeg - 1; i <= nend + 1; i++)
+            char_tracing(w.v[i], w.vp[i], w.vm[i], p->c.gamma, dt / dxd, dt, &r, c3, dims);
+          if (ct)
+            for (i = nbeg - 2; i <= nend + 1; i++) {
+              w.vp[i][r.bn] = w.bn[i];
+              w.vm[i + 1][r.bn] = w.bn[i];
+            }
+        } else {
+          for (i = nbeg - 1; i <= nend + 1; i++) { /* primitive Hancock step */
+            double dv[NV], Adv[NV];
+            for (nv = 0; nv < NV; nv++) dv[nv] = w.vp[i][nv] - w.vm[i][nv];
+            prim_rhs(w.v[i], dv, p->c.gamma, &r, c3, Adv);
+            for (nv = NV - 1; nv >= 0; nv--) {
+              double scrh = dt2 * (inv_dl * Adv[nv] - 0.0);
+              w.vp[i][nv] -= scrh;
+              w.vm[i][nv] -= scrh;
+            }
           }
         }
         for (i = nbeg - 1; i <= nend + 1; i++) { /* CheckPrimStates */
@@ -1708,7 +1954,7 @@ int oc_advance(oc_problem *p, double dt, double *inv_dt_hyp, double *max_mach,
   size_t c;
 
   p->bstage = 0;
-  if (p->c.stepping == OC_HANCOCK) return oc_advance_ctu(p, dt, inv_dt_hyp, max_mach, nfail);
+  if (IS_CTU(p->c.stepping)) return oc_advance_ctu(p, dt, inv_dt_hyp, max_mach, nfail);
 
   p->nfail = 0;
   p->max_mach = 0.0;
@@ -1806,7 +2052,7 @@ oc_problem *oc_create(const oc_config *cfg) {
     if ((cfg->bc[d] == OC_PERIODIC) != (cfg->bc_hi[d] == OC_PERIODIC)) { free(p); return NULL; }
   }
   p->ng = cfg->recon == OC_PARABOLIC ? 3 : 2; /* Src/get_nghost.c:28-104 */
-  if (cfg->stepping == OC_HANCOCK) {
+  if (IS_CTU(cfg->stepping)) {
     if (cfg->recon != OC_LINEAR) { free(p); return NULL; } /* hancock.c:64-67 */
     if (cfg->ct && cfg->emf != OC_ARITHMETIC && cfg->emf != OC_UCT_CONTACT) { free(p); return NULL; }
     if (cfg->ct) p->ng++;                                    /* get_nghost.c:84-90 */
@@ -1840,7 +2086,7 @@ oc_problem *oc_create(const oc_config *cfg) {
   p->ez = calloc(p->ncell, sizeof(double));
   p->cdt = calloc(p->ncell, sizeof(double));
   p->flag = calloc(p->ncell, 1);
-  if (cfg->stepping == OC_HANCOCK) {
+  if (IS_CTU(cfg->stepping)) {
     for (d = 0; d < 3; d++)
       for (nv = 0; nv < NV; nv++) {
         p->up_s[d][nv] = calloc(p->ncell, sizeof(double));

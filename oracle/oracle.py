@@ -19,7 +19,8 @@ NVAR = 8
 RECON = {"LINEAR": 0, "PARABOLIC": 1}
 LIMITER = {"FLAT_LIM": 0, "MINMOD_LIM": 1, "VANLEER_LIM": 2, "MC_LIM": 3, "DEFAULT": 4}
 SOLVER = {"hll": 0, "hlld": 1, "roe": 2}
-STEPPING = {"EULER": 1, "RK2": 2, "RK3": 3, "HANCOCK": 4}
+STEPPING = {"EULER": 1, "RK2": 2, "RK3": 3, "HANCOCK": 4, "CHARACTERISTIC_TRACING": 5}
+CTU_STEPPING = ("HANCOCK", "CHARACTERISTIC_TRACING")
 BC = {"periodic": 0, "outflow": 1, "reflective": 2, "eqtsymmetric": 3, "userdef": 4}
 EMF = {"ARITHMETIC": 1, "UCT_CONTACT": 3, "UCT_HLL": 4}
 
@@ -129,7 +130,7 @@ class Oracle:
         the oracle's own PLUTO-layout arrays (vc [8, nt2, nt1, nt0], faces[d]
         one longer along d with the -1 layer first)."""
         ng = 3 if self.spec["recon"] == "PARABOLIC" else 2
-        if self.spec["stepping"] == "HANCOCK" and self.spec["ct"]:
+        if self.spec["stepping"] in CTU_STEPPING and self.spec["ct"]:
             ng += 1
         nt = [self.nx[d] + 2 * ng if d < self.spec["dims"] else 1 for d in range(3)]
         dp = C.POINTER(C.c_double)

@@ -65,17 +65,21 @@ int validate_config(const pg_config* c) {
   if (c->riemann != PG_HLL && c->riemann != PG_HLLD && c->riemann != PG_ROE)
     return fail(PG_ERR_INVALID, "unsupported Riemann solver");
   if (c->time_stepping != PG_EULER && c->time_stepping != PG_RK2 && c->time_stepping != PG_RK3 &&
-      c->time_stepping != PG_HANCOCK)
+      !is_ctu(c->time_stepping))
     return fail(PG_ERR_INVALID, "unsupported time stepping");
-  if (c->time_stepping == PG_HANCOCK) {
-    if (c->reconstruction != PG_LINEAR)  // Src/States/hancock.c:64-67
-      return fail(PG_ERR_INVALID, "the MUSCL-Hancock predictor needs linear reconstruction");
+  if (is_ctu(c->time_stepping)) {
+    // Src/States/hancock.c:64-67; char_tracing.c traces linear states only
+    // (the PARABOLIC form is not restated)
+    if (c->reconstruction != PG_LINEAR)
+      return fail(PG_ERR_INVALID, "the CTU predictors need linear reconstruction");
     if (c->precision != PG_FP64 && c->precision != PG_FP64_TANGENT)
       return fail(PG_ERR_INVALID, "CTU runs on the FP64 path");
+    if (c->time_stepping == PG_CHAR_TRACING && c->precision != PG_FP64)
+      return fail(PG_ERR_INVALID, "characteristic tracing runs on the plain FP64 path (no tangent-linear model)");
   }
   if (c->divb == PG_CONSTRAINED_TRANSPORT) {
     if (c->dims < 2) return fail(PG_ERR_INVALID, "constrained transport needs dims >= 2");
-    if (c->time_stepping == PG_HANCOCK) {  // Src/MHD/CT/ct_emf.c:196-199
+    if (is_ctu(c->time_stepping)) {  // Src/MHD/CT/ct_emf.c:196-199
       if (c->emf_average != PG_ARITHMETIC && c->emf_average != PG_UCT_CONTACT)
         return fail(PG_ERR_INVALID, "CTU takes the ARITHMETIC or UCT_CONTACT emf average");
     } else if (c->emf_average != PG_UCT_HLL) {
@@ -99,7 +103,7 @@ void init_geom(Solver* S) {
   const pg_config* cfg = &S->cfg;
   S->ng = cfg->reconstruction == PG_PARABOLIC ? 3 : 2;  // Src/get_nghost.c:28-104
   // CTU with constrained transport keeps one more ghost layer (get_nghost.c:84-90)
-  if (cfg->time_stepping == PG_HANCOCK && cfg->divb == PG_CONSTRAINED_TRANSPORT) S->ng++;
+  if (is_ctu(cfg->time_stepping) && cfg->divb == PG_CONSTRAINED_TRANSPORT) S->ng++;
   Geom& g = S->g;
   g.dims = cfg->dims;
   for (int d = 0; d < 3; d++) {
@@ -229,7 +233,7 @@ extern "C" int pg_set_internal_boundary(pg_solver* h, unsigned char* flags) {
   if (!h || !flags) return fail(PG_ERR_INVALID, "pg_set_internal_boundary: null argument");
   Solver* S = &h->S;
   if (!S->ud_fn) return fail(PG_ERR_INVALID, "pg_set_internal_boundary: call pg_set_userdef first");
-  if (S->cfg.precision == PG_FP64_TANGENT || S->cfg.time_stepping == PG_HANCOCK)
+  if (S->cfg.precision == PG_FP64_TANGENT || is_ctu(S->cfg.time_stepping))
     return fail(PG_ERR_INVALID, "pg_set_internal_boundary: EULER/RK2/RK3 time stepping, FP64 or mixed");
   CK(cudaStreamSynchronize(S->stream));
   if (S->ud_pinned_flag) {

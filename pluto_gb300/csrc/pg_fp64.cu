@@ -64,7 +64,7 @@ int fp64_alloc(Solver* S) {
       }
     }
   }
-  if (S->cfg.time_stepping == PG_HANCOCK) {
+  if (is_ctu(S->cfg.time_stepping)) {
     for (int d = 0; d < S->g.dims; d++)
       for (int nv = 0; nv < 8; nv++)
         if (alloc(&S->Upd[d][nv]) || alloc(&S->Umd[d][nv]) || alloc(&S->Rhd[d][nv])) return PG_ERR_NOMEM;

@@ -48,6 +48,7 @@ struct F64A {
   int intb;         // INTERNAL_BOUNDARY: flagged zones are not updated
   int div_dims;     // RK: invDt_hyp /= DIMENSIONS (update_stage.c:311); CTU: no
   int emf_avg, c3;
+  int chtr;         // CTU predictor: characteristic tracing (else primitive Hancock)
 };
 
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
@@ -512,7 +513,8 @@ static F64A<T> make_args(Solver* S) {
   for (int nv = 0; nv < 8; nv++) a.Uh[nv] = (T*)S->Uh[nv];
   for (int q = 0; q < 6; q++) a.EF[q] = (T*)S->EF[q];
   for (int d = 0; d < 3; d++) a.SV[d] = S->SV[d];
-  a.div_dims = S->cfg.time_stepping != PG_HANCOCK;
+  a.div_dims = !is_ctu(S->cfg.time_stepping);
+  a.chtr = S->cfg.time_stepping == PG_CHAR_TRACING;
   a.emf_avg = S->cfg.emf_average;
   a.c3 = S->cfg.components == 3;
   a.intb = S->ud_internal ? 1 : 0;
@@ -652,7 +654,7 @@ namespace pg {
 template <class T>
 int fp64_enqueue_step_t(Solver* S) {
   F64A<T> a = make_args<T>(S);
-  if (S->cfg.time_stepping == PG_HANCOCK) enqueue_ctu<T>(S, a);
+  if (is_ctu(S->cfg.time_stepping)) enqueue_ctu<T>(S, a);
   else if (S->cfg.time_stepping == PG_RK3) enqueue_rk<T, 3>(S, a);
   else if (S->cfg.time_stepping == PG_EULER) enqueue_rk<T, 1>(S, a);
   else enqueue_rk<T, 2>(S, a);

@@ -159,6 +159,9 @@ struct Solver {
 };
 
 constexpr int kThreads = 256;
+// TIME_STEPPING of the CTU family (ctu_step.c): HANCOCK or CHARACTERISTIC_TRACING
+inline bool is_ctu(int time_stepping) { return time_stepping == PG_HANCOCK || time_stepping == PG_CHAR_TRACING; }
+
 inline unsigned grid_for(long long n, int threads = kThreads) {
   long long b = (n + threads - 1) / threads;
   return (unsigned)(b < 1 ? 1 : b);

@@ -95,6 +95,8 @@ static void gpu_config(pg_config *c, Riemann_Solver *Riemann, Grid *grid)
   c->time_stepping = PG_EULER;
 #elif TIME_STEPPING == HANCOCK
   c->time_stepping = PG_HANCOCK;
+#elif TIME_STEPPING == CHARACTERISTIC_TRACING
+  c->time_stepping = PG_CHAR_TRACING;
 #else
   c->time_stepping = PG_RK2;
 #endif

@@ -23,7 +23,9 @@ RECON = {"LINEAR": L.PG_LINEAR, "PARABOLIC": L.PG_PARABOLIC}
 LIMITER = {"FLAT_LIM": L.PG_FLAT_LIM, "MINMOD_LIM": L.PG_MINMOD_LIM,
            "VANLEER_LIM": L.PG_VANLEER_LIM, "MC_LIM": L.PG_MC_LIM, "DEFAULT": L.PG_DEFAULT_LIM}
 RIEMANN = {"hll": L.PG_HLL, "hlld": L.PG_HLLD, "roe": L.PG_ROE}
-STEPPING = {"EULER": L.PG_EULER, "RK2": L.PG_RK2, "RK3": L.PG_RK3, "HANCOCK": L.PG_HANCOCK}
+STEPPING = {"EULER": L.PG_EULER, "RK2": L.PG_RK2, "RK3": L.PG_RK3, "HANCOCK": L.PG_HANCOCK,
+            "CHARACTERISTIC_TRACING": L.PG_CHAR_TRACING}
+CTU_STEPPING = ("HANCOCK", "CHARACTERISTIC_TRACING")
 EMF = {"ARITHMETIC": L.PG_ARITHMETIC, "UCT_CONTACT": L.PG_UCT_CONTACT, "UCT_HLL": L.PG_UCT_HLL}
 BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW, "reflective": L.PG_REFLECTIVE,
       "eqtsymmetric": L.PG_EQTSYMMETRIC, "userdef": L.PG_USERDEF}
@@ -136,7 +138,7 @@ class Solver:
         """(nt2, nt1, nt0): the ghosted cell-array shape (PLUTO layout)."""
         s = self.spec
         ng = 3 if s.get("recon", "LINEAR") == "PARABOLIC" else 2
-        if s.get("stepping", "RK2") == "HANCOCK" and self.ct:
+        if s.get("stepping", "RK2") in CTU_STEPPING and self.ct:
             ng += 1
         return tuple(int(s["nx"][d]) + 2 * ng if d < self.dims else 1 for d in (2, 1, 0))
 

@@ -188,6 +188,20 @@ def setups():
         # TIME_STEPPING EULER (the RK predictor alone)
         replace(br.ot_setup("hlld", 32, 10), stepping="EULER", cfl=0.2, name="ot_euler_32"),
         replace(br.tube_setup(0, 256, 60), stepping="EULER", name="tube_euler_0_256"),
+        # TIME_STEPPING CHARACTERISTIC_TRACING (CTU with CharTracingStep)
+        replace(br.ot_setup("hlld", 32, 30), stepping="CHARACTERISTIC_TRACING", emf="UCT_CONTACT",
+                name="ot_chtr_uctc_32"),
+        replace(br.ot_setup("roe", 32, 30), stepping="CHARACTERISTIC_TRACING", emf="ARITHMETIC",
+                name="ot_chtr_arith_roe_32"),
+        replace(br.cpa_setup(32, 20), stepping="CHARACTERISTIC_TRACING", emf="UCT_CONTACT",
+                name="cpa_chtr_32"),
+        replace(br.turb_setup(12, 10), recon="LINEAR", stepping="CHARACTERISTIC_TRACING",
+                emf="UCT_CONTACT", name="turb_chtr_12"),
+        replace(br.tube_setup(1, 200, 120), stepping="CHARACTERISTIC_TRACING", name="tube_chtr_1_200"),
+        replace(br.blast_setup(16, 12), stepping="CHARACTERISTIC_TRACING", emf="UCT_CONTACT",
+                bc="outflow", name="blast_chtr_outflow_16"),
+        replace(br.blast_setup(16, 12), stepping="CHARACTERISTIC_TRACING", ct=False, name="blast_chtr_noct_16"),
+        replace(br.blast_setup(16, 12), stepping="HANCOCK", ct=False, name="blast_ctu_noct_16"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

@@ -44,7 +44,7 @@ def test_abi_version(lib):
 
 
 @pytest.mark.parametrize("field,value", [("dims", 4), ("components", 1), ("gamma", 1.0),
-                                         ("riemann", 7), ("time_stepping", 5), ("precision", 9)])
+                                         ("riemann", 7), ("time_stepping", 6), ("precision", 9)])
 def test_invalid_config_rejected_before_any_cuda_call(lib, field, value):
     spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1.0), gamma=5 / 3)
     cfg = make_config(spec)
@@ -65,6 +65,26 @@ def test_ct_requires_2d_and_accepts_outflow(lib):
                 bc=("outflow", "periodic", "periodic"))
     rc = lib.pg_create(C.byref(make_config(spec)), C.byref(h))
     assert rc != 1
+    if rc == 0:
+        lib.pg_destroy(h)
+
+
+@pytest.mark.parametrize("extra,ok", [({}, True), ({"recon": "PARABOLIC"}, False),
+                                      ({"precision": "mixed"}, False), ({"precision": "fp64_tangent"}, False),
+                                      ({"ct": True, "emf": "UCT_HLL"}, False),
+                                      ({"ct": True, "emf": "UCT_CONTACT"}, True),
+                                      ({"ct": True, "emf": "ARITHMETIC"}, True)])
+def test_char_tracing_validation(lib, extra, ok):
+    """TIME_STEPPING CHARACTERISTIC_TRACING: linear reconstruction, the plain
+    FP64 path, and under CT the ARITHMETIC or UCT_CONTACT emf average."""
+    extra = dict(extra)
+    precision = extra.pop("precision", "fp64")
+    spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1), gamma=5 / 3, ct=False,
+                stepping="CHARACTERISTIC_TRACING")
+    spec.update(extra)
+    h = C.c_void_p()
+    rc = lib.pg_create(C.byref(make_config(spec, precision)), C.byref(h))
+    assert (rc != 1) == ok, lib.pg_last_error()
     if rc == 0:
         lib.pg_destroy(h)
 

@@ -53,7 +53,10 @@ def test_fp64_matches_reference_goldens(name):
                                   "cpa_eqtsym_32", "tube_reflective_0_256", "ot_ctu_reflective_32",
                                   "blast_sides_16", "ot_sides_32", "ot_ctu_sides_32", "tube_sides_0_256",
                                   "ot_userdef_32", "blast_userdef_16", "blast_userdef_ct_16",
-                                  "ot_euler_32", "tube_euler_0_256", "ot_internal_32"])
+                                  "ot_euler_32", "tube_euler_0_256", "ot_internal_32",
+                                  "ot_chtr_uctc_32", "ot_chtr_arith_roe_32", "cpa_chtr_32", "turb_chtr_12",
+                                  "tube_chtr_1_200", "blast_chtr_outflow_16", "blast_chtr_noct_16",
+                                  "blast_ctu_noct_16"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
@@ -223,6 +226,48 @@ def test_ctu_vs_oracle_random_3d(emf, solver, bc):
     assert np.array_equal(a, b), _errors(a, ab, b, bb)
     for d in range(3):
         assert np.array_equal(ab[d], bb[d])
+
+
+@pytest.mark.parametrize("emf,solver,bc", [("UCT_CONTACT", "hlld", "periodic"), ("ARITHMETIC", "roe", "outflow"),
+                                           ("UCT_CONTACT", "hll", [("reflective", "outflow"), "periodic",
+                                                                   ("eqtsymmetric", "outflow")]),
+                                           ("UCT_CONTACT", "hlld", [("userdef", "outflow"), "periodic",
+                                                                    ("outflow", "userdef")])])
+def test_char_tracing_vs_oracle_random_3d(emf, solver, bc):
+    """CTU with the characteristic tracing predictor on a random 3D state
+    against the oracle, bit for bit."""
+    from oracle.oracle import Oracle
+    spec, vc, bs = _random_blast(16, seed=12)
+    spec.update(stepping="CHARACTERISTIC_TRACING", emf=emf, solver=solver, bc=bc, limiter="MC_LIM")
+    s = _solver(spec)
+    o = Oracle(spec, nthreads=4)
+    if userdef_cases.has_userdef(spec):
+        o.set_userdef(userdef_cases.make(spec))
+    s.upload(vc, bs)
+    o.set_state(vc, bs)
+    s.run(4, 1e-3, 0.3)
+    o.run(4, 1e-3, 0.3)
+    a, ab = s.download()
+    b, bb = o.get_state()
+    assert np.array_equal(a, b), _errors(a, ab, b, bb)
+    for d in range(3):
+        assert np.array_equal(ab[d], bb[d])
+
+
+def test_char_tracing_without_ct_vs_oracle_3d():
+    """Characteristic tracing with cell-centred fields only (no CT)."""
+    from oracle.oracle import Oracle
+    spec, vc, bs = _random_blast(16, seed=13)
+    spec.update(stepping="CHARACTERISTIC_TRACING", ct=False, solver="hlld", limiter="MINMOD_LIM")
+    s = _solver(spec)
+    o = Oracle(spec, nthreads=4)
+    s.upload(vc, bs)
+    o.set_state(vc, bs)
+    s.run(4, 1e-3, 0.3)
+    o.run(4, 1e-3, 0.3)
+    a, _ = s.download()
+    b, _ = o.get_state()
+    assert np.array_equal(a, b)
 
 
 def test_ctu_tangent_value_part_is_the_fp64_step():
