@@ -315,6 +315,76 @@ def adjoint_timing():
             "timing": "host clock around synchronous C-ABI calls (one pg_advance per step)"}
 
 
+def output_timing(n=256, outputs=4, steps_between=50):
+    """The device output path (pg_write_output, .dbl single file) against
+    download-then-write through the C ABI, on the mixed 3D blast at n^3:
+    per output, the time it adds to a run of steps (outputs every
+    steps_between steps, a cadence at which the file writes keep up) over the
+    same run without outputs.  Two untimed outputs first allocate the
+    staging slots (device + pinned host, one output each)."""
+    import shutil
+    import tempfile
+
+    import torch
+    from pluto_gb300 import Solver, problems
+    spec, vc, faces = problems.blast3d(n)
+    cfl, first_dt = spec["cfl"], spec["first_dt"]
+    s = Solver(spec, precision="mixed")
+    s.upload(vc, faces)
+    s.run(3, first_dt, cfl)
+    bytes_out = 8 * (8 * n ** 3 + sum(f.size for f in faces))
+    tmp = tempfile.mkdtemp(prefix="pg_out_")
+    try:
+        if shutil.disk_usage(tmp).free < 4 * bytes_out:
+            return {"skipped": "not enough free space for the files under " + tempfile.gettempdir()}
+        steps = outputs * steps_between
+        for k in range(2):
+            s.write_output(tmp, "dbl", 0, write_record=False)
+        s.output_wait()
+        ms_run = s.run_timed(steps, 0.0, cfl)
+        # async device writer
+        s.sync()
+        t0 = time.perf_counter()
+        for k in range(outputs):
+            s.write_output(tmp, "dbl", k, time=float(k), dt=first_dt, step=k)
+            s.run_async(steps_between, 0.0, cfl)
+        s.sync()
+        t_async = time.perf_counter() - t0
+        s.output_wait()
+        t_drain = time.perf_counter() - t0
+        # the packing alone (what the compute stream waits for)
+        t0 = time.perf_counter()
+        s.write_output(tmp, "dbl", outputs, write_record=False)
+        s.sync()
+        t_pack = time.perf_counter() - t0
+        s.output_wait()
+        # download the whole state into pinned host arrays, then write the file
+        def pinned(shape):
+            return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+        hv = pinned(vc.shape)
+        hf = [pinned(f.shape) for f in faces]
+        t0 = time.perf_counter()
+        for k in range(outputs):
+            s.download(out=(hv, hf))
+            with open(os.path.join(tmp, f"host.{k:04d}.dbl"), "wb") as f:
+                for q in range(8):
+                    hv[q].tofile(f)
+                for a in hf:
+                    a.tofile(f)
+            s.run_async(steps_between, 0.0, cfl)
+        s.sync()
+        t_sync = time.perf_counter() - t0
+    finally:
+        shutil.rmtree(tmp, ignore_errors=True)
+    base = ms_run / 1e3
+    return {"workload": f"mixed 3D blast {n}^3, .dbl single file ({bytes_out / 1e9:.2f} GB) every "
+                        f"{steps_between} steps, {outputs} outputs",
+            "bytes_per_output": bytes_out, "ms_per_step": ms_run / steps,
+            "device_writer": {"added_ms_per_output": (t_async - base) / outputs * 1e3,
+                              "pack_ms": t_pack * 1e3, "all_files_written_s": t_drain},
+            "download_then_write": {"added_ms_per_output": (t_sync - base) / outputs * 1e3}}
+
+
 def rel_l1(a, b):
     den = np.abs(b).sum()
     return float(np.abs(a - b).sum() / den) if den > 0 else float(np.abs(a - b).sum())
@@ -339,6 +409,7 @@ def main():
     ap.add_argument("--tube-trial-steps", type=int, default=20)
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
+    ap.add_argument("--no-output", action="store_true")
     args = ap.parse_args()
     rank, ws = dist_init()
     if args.impl == "reference":
@@ -496,6 +567,13 @@ def main():
                "steps": args.e2e_steps,
                "upload_gbs": state_bytes / (tb - ta) / 1e9, "download_gbs": state_bytes / (tc - tb) / 1e9}
 
+    outp = None
+    if rank == 0 and not args.no_output:
+        try:
+            outp = output_timing()
+        except Exception as ex:
+            outp = {"skipped": f"{type(ex).__name__}: {ex}"}
+
     cpu = None
     if rank == 0 and not args.no_cpu:
         try:
@@ -545,6 +623,7 @@ def main():
         "cpu_baseline": cpu,
         "batched_tubes": batch,
         "adjoint": adj,
+        "output": outp,
     }
     print(json.dumps(out), flush=True)
 

@@ -251,6 +251,51 @@ int pg_set_userdef(pg_solver *s, pg_userdef_fn fn, void *user, double *const var
 #define PG_FLAG_INTERNAL_BOUNDARY 32  /* Src/pluto.h:197 */
 int pg_set_internal_boundary(pg_solver *s, unsigned char *flags);
 
+/* ---- Output files written from the device ----
+   Replaces the .dbl / .flt / .vtk branches of WriteData (Src/write_data.c:29-330;
+   FileWriteData Src/bin_io.c:216-259, Convert_dbl2flt Src/bin_io.c:51-83,
+   WriteVTK_Header / WriteVTK_Vector / WriteVTK_Scalar Src/write_vtk.c) and its
+   ".out" record (Src/write_data.c:360-385): the same file names and bytes as a
+   serial reference run writes, for the state pg_download returns.
+   pg_write_output packs the dumped variables on the device in file order
+   (doubles; single precision rounded to nearest; big-endian single precision
+   for VTK), copies them to pinned host memory on a separate stream and writes
+   the files on a background thread; it returns once the packing is enqueued,
+   so the next steps overlap the copy and the file writes.  Outputs complete
+   in call order.  pg_output_wait blocks until every pending output is on
+   disk and returns the first error met (PG_ERR_INVALID for an I/O error, the
+   message via pg_last_error).  pg_destroy waits too.  FP64 and mixed
+   precisions; the tangent-linear solver returns PG_ERR_INVALID. */
+enum { PG_OUT_DBL = 0, PG_OUT_FLT = 1, PG_OUT_VTK = 2 };
+#define PG_OUT_MAX_VARS 16
+#define PG_OUT_FACE(d) (8 + (d))   /* var id of the staggered component d (Bx1s..) */
+#define PG_OUT_VECTOR 5            /* dump value VTK_VECTOR (Src/pluto.h:97)       */
+typedef struct {
+  int format;                         /* PG_OUT_DBL / PG_OUT_FLT / PG_OUT_VTK          */
+  int single_file;                    /* output->mode "single_file" (else one per var) */
+  int nfile;                          /* file number NNNN (after WriteData's ++)       */
+  int nvar;                           /* entries below, in output->var order           */
+  int var[PG_OUT_MAX_VARS];           /* 0..7: cell slot RHO..PRS; PG_OUT_FACE(d)      */
+  int dump[PG_OUT_MAX_VARS];          /* output->dump_var: 0, 1 or PG_OUT_VECTOR       */
+  const char *name[PG_OUT_MAX_VARS];  /* output->var_name                              */
+  double unit[PG_OUT_MAX_VARS];       /* multiplier for .flt/.vtk (1, or c.g.s units)  */
+  const char *dir;                    /* output->dir                                   */
+  const double *xnode[3];             /* VTK: grid->xl_glob[d] + BEG, nx+1 entries on
+                                         an active axis, 1 otherwise                   */
+  double time, dt;                    /* g_time, g_dt for the .out record              */
+  long step;                          /* g_stepNumber                                  */
+  int write_record;                   /* 1: update dir/<ext>.out                       */
+} pg_output;
+int pg_write_output(pg_solver *s, const pg_output *out);
+int pg_output_wait(pg_solver *s);
+/* Restart from a .dbl written as above (RestartFromFile's data part,
+   Src/restart.c:17-150): reads the files named by out (format PG_OUT_DBL;
+   dump, var, single_file, nfile, dir; native little-endian doubles) and
+   uploads their interior like pg_upload with PG_LAYOUT_INTERIOR: cell slots
+   not in the list are set to zero, and under constrained transport every
+   staggered component must be listed. */
+int pg_read_output(pg_solver *s, const pg_output *out);
+
 /* Diagnostics */
 int pg_get_stream(pg_solver *s, void **cuda_stream);
 int pg_get_info(pg_solver *s, pg_step_info *info, double *time, double *dt);

@@ -80,6 +80,9 @@ class Setup:
     init_body: str = ""
     userdef_body: str = ""          # body of UserDefBoundary (USERDEF sides)
     internal_boundary: bool = False  # INTERNAL_BOUNDARY YES
+    dbl_mode: str = "single_file"    # [Static Grid Output] dbl mode
+    out_modes: tuple = ()            # extra outputs written at the dbl cadence: ((fmt, mode), ...)
+    vtk_vector: bool = False         # VTK_VECTOR_DUMP YES
 
 
 def _fmt(x: float) -> str:
@@ -102,6 +105,8 @@ def definitions_h(s: Setup) -> str:
     ]
     if s.internal_boundary:
         lines.append(("INTERNAL_BOUNDARY", "YES"))
+    if s.vtk_vector:
+        lines.append(("VTK_VECTOR_DUMP", "YES"))
     out = [f"#define  {k:<30} {v}" for k, v in lines]
     for idx, key in enumerate(s.params):
         out.append(f"#define  {key:<30} {idx}")
@@ -131,6 +136,7 @@ def pluto_ini(s: Setup) -> str:
             lo = hi = s.bc
         bcs.append(f"X{d+1}-beg        {lo}\nX{d+1}-end        {hi}")
     par = "\n".join(f"{k}    {_fmt(v)}" for k, v in s.params.items())
+    extra = {fmt: (str(s.steps), mode) for fmt, mode in s.out_modes}
     return f"""[Grid]
 
 {chr(10).join(g)}
@@ -164,9 +170,9 @@ Solver         {s.solver}
 [Static Grid Output]
 
 uservar    0
-dbl       -1.0  {s.steps}   single_file
-flt       -1.0  -1   single_file
-vtk       -1.0  -1   single_file
+dbl       -1.0  {s.steps}   {s.dbl_mode}
+flt       -1.0  {extra.get("flt", ("-1", "single_file"))[0]}   {extra.get("flt", ("-1", "single_file"))[1]}
+vtk       -1.0  {extra.get("vtk", ("-1", "single_file"))[0]}   {extra.get("vtk", ("-1", "single_file"))[1]}
 dbl.h5    -1.0  -1
 flt.h5    -1.0  -1
 tab       -1.0  -1

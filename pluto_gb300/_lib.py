@@ -35,7 +35,8 @@ EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", 
            "pg_batch_download", "pg_batch_run", "pg_batch_get", "pg_batch_autotune",
            "pg_batch_set_schedule", "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set",
            "pg_adjoint_step", "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load",
-           "pg_selftest_conversions", "pg_set_userdef", "pg_set_internal_boundary"]
+           "pg_selftest_conversions", "pg_set_userdef", "pg_set_internal_boundary",
+           "pg_write_output", "pg_output_wait", "pg_read_output"]
 PG_ABI_VERSION = 2  # the pg_config layout these bindings describe
 # pg_userdef_fn: (user, side 0..5, vpos 0 cells / 1..3 faces, stage)
 USERDEF_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int)
@@ -51,6 +52,19 @@ class PgConfig(C.Structure):
                 ("bc", C.c_int * 3), ("precision", C.c_int), ("compute_mach", C.c_int),
                 ("small_density", C.c_double), ("small_pressure", C.c_double),
                 ("bc_hi", C.c_int * 3), ("bc_sides", C.c_int)]
+
+
+PG_OUT_DBL, PG_OUT_FLT, PG_OUT_VTK = 0, 1, 2
+PG_OUT_MAX_VARS = 16
+PG_OUT_VECTOR = 5
+
+
+class PgOutput(C.Structure):
+    _fields_ = [("format", C.c_int), ("single_file", C.c_int), ("nfile", C.c_int), ("nvar", C.c_int),
+                ("var", C.c_int * PG_OUT_MAX_VARS), ("dump", C.c_int * PG_OUT_MAX_VARS),
+                ("name", C.c_char_p * PG_OUT_MAX_VARS), ("unit", C.c_double * PG_OUT_MAX_VARS),
+                ("dir", C.c_char_p), ("xnode", C.POINTER(C.c_double) * 3),
+                ("time", C.c_double), ("dt", C.c_double), ("step", C.c_long), ("write_record", C.c_int)]
 
 
 class PgStepInfo(C.Structure):
@@ -115,6 +129,9 @@ def lib():
     L.pg_selftest_conversions.argtypes = [C.POINTER(C.c_ulonglong)]
     L.pg_set_userdef.argtypes = [vp, USERDEF_FN, vp, C.POINTER(dp), C.POINTER(dp)]
     L.pg_set_internal_boundary.argtypes = [vp, C.POINTER(C.c_ubyte)]
+    L.pg_write_output.argtypes = [vp, C.POINTER(PgOutput)]
+    L.pg_output_wait.argtypes = [vp]
+    L.pg_read_output.argtypes = [vp, C.POINTER(PgOutput)]
     L.pg_last_error.restype = C.c_char_p
     for fn in ("pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
                "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
@@ -123,7 +140,8 @@ def lib():
                "pg_batch_run", "pg_batch_get", "pg_batch_autotune", "pg_batch_set_schedule",
                "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set", "pg_adjoint_step",
                "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load", "pg_selftest_conversions",
-               "pg_set_userdef", "pg_set_internal_boundary"):
+               "pg_set_userdef", "pg_set_internal_boundary", "pg_write_output", "pg_output_wait",
+               "pg_read_output"):
         getattr(L, fn).restype = C.c_int
     if L.pg_abi_version() != PG_ABI_VERSION:
         raise OSError(f"libpluto_gb300 has ABI version {L.pg_abi_version()}, these bindings expect "

@@ -125,6 +125,7 @@ void set_last_error(const char* msg) { g_last_error = msg; }
 }  // namespace pg
 
 static void free_all(Solver* S) {
+  output_free(S);
   if (S->graph) cudaGraphExecDestroy(S->graph);
   S->graph = nullptr;
   if (S->stream) cudaStreamSynchronize(S->stream);

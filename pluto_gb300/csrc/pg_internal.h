@@ -156,7 +156,10 @@ struct Solver {
   bool ud_internal = false;   // INTERNAL_BOUNDARY: a callback with the whole state per fill
   unsigned char* ud_dev_flag = nullptr;  // device-usable address of the caller's flag array
   void* ud_pinned_flag = nullptr;
+  void* out = nullptr;        // output staging, copy stream and writer thread (pg_output.cu)
 };
+
+void output_free(Solver* S);  // waits for pending outputs, then releases their resources
 
 constexpr int kThreads = 256;
 // TIME_STEPPING of the CTU family (ctu_step.c): HANCOCK or CHARACTERISTIC_TRACING

@@ -1522,6 +1522,15 @@ int mixed_upload_host(Solver* S, const double* const vars[8], const double* cons
 int mixed_download(Solver* S, double* const vars[8], double* const faces[3], int layout) {
   return mixed_xfer(S, nullptr, vars, nullptr, faces, layout, false);
 }
+// the current FP32 state arrays (what mixed_download widens), for the output packer
+float* mixed_cell_array(Solver* S, int nv) {
+  MixedState* M = (MixedState*)S->mixed;
+  return M ? M->b.V[M->cur][nv] : nullptr;
+}
+float* mixed_face_array(Solver* S, int d) {
+  MixedState* M = (MixedState*)S->mixed;
+  return (M && S->cfg.divb == PG_CONSTRAINED_TRANSPORT && d < S->g.dims) ? M->b.Bs[M->cur][d] : nullptr;
+}
 
 namespace pg {
 

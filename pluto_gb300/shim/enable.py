@@ -8,8 +8,11 @@ block for extra objects.  This script adds after that block
     PG_ROOT = <this repository>
     include $(PG_ROOT)/pluto_gb300/shim/Makefile.gpu
 
-(which swaps rk_step.o / update_stage.o / ctu_step.o for gpu_step.o and links
-libpluto_gb300), or removes it again with --disable.  Running it twice is
+(which swaps rk_step.o / update_stage.o / ctu_step.o for gpu_step.o, links
+libpluto_gb300 and compiles write_data.o / init.o with WriteData / Analysis
+renamed, since gpu_step.o wraps both), or removes it again with --disable.
+Either way the problem directory's write_data.o and init.o are deleted so
+that make rebuilds them with the matching names.  Running it twice is
 harmless; re-run it after the setup tool regenerates the makefile.
 
     python pluto_gb300/shim/enable.py <problem dir or makefile> [--disable]
@@ -69,6 +72,8 @@ def main(argv=None) -> int:
     new = strip(text) if args.disable else enable(text)
     if new != text:
         mk.write_text(new)
+    for stale in ("write_data.o", "init.o"):  # built with the other WriteData / Analysis names
+        (mk.parent / stale).unlink(missing_ok=True)
     print(f"{mk}: GPU AdvanceStep {'disabled' if args.disable else 'enabled'}")
     return 0
 

@@ -19,9 +19,20 @@
   Device residency: the state lives on the GPU between steps.  It is
   uploaded on the first call and whenever the environment variable
   PLUTO_GPU_UPLOAD_EVERY says so (e.g. after a restart or when init code
-  changed d->Vc), and downloaded into d->Vc / d->Vs every
-  PLUTO_GPU_SYNC_EVERY steps (default 1: the host arrays are always
-  current, as output, analysis and restart in Src/main.c expect).
+  changed d->Vc).  The host copy d->Vc / d->Vs is refreshed on demand by the
+  two readers of it between steps in Src/main.c, both defined here:
+    WriteData   (Src/write_data.c:29): .dbl, .flt and .vtk files are written
+                from the device by pg_write_output (asynchronously: the next
+                steps overlap the copy and the file writes); every other
+                format, user-defined output variables and anything the
+                device writer does not take download the state first and
+                call the reference's writer, compiled as pg_host_WriteData;
+    Analysis    (the problem's init.c, compiled as pg_user_Analysis):
+                downloads the state first.
+  Makefile.gpu renames the two reference definitions (-DWriteData=... on
+  write_data.o, -DAnalysis=... on init.o).  PLUTO_GPU_SYNC_EVERY=n > 0
+  also downloads after every n-th step (the former behaviour).
+  Pending output files are complete when the program exits (atexit).
 
   Errors: a non-zero status from the library is fatal, as the reference's
   own fatal conditions are (QUIT_PLUTO).
@@ -33,8 +44,13 @@
 #include "pluto.h"
 #include "pluto_gb300.h"
 
+/* the reference definitions these wrap (renamed by Makefile.gpu) */
+void pg_host_WriteData (const Data *, Output *, Grid *);
+void pg_user_Analysis (const Data *, Grid *);
+
 static pg_solver *s_gpu = NULL;
 static long s_calls = 0;
+static int s_host_stale = 0;  /* d->Vc / d->Vs older than the device state */
 static Data *s_data = NULL;   /* for UserDefBoundary on USERDEF sides */
 static Grid *s_grid = NULL;
 
@@ -188,6 +204,101 @@ static void gpu_check(int rc, const char *where)
   }
 }
 
+/* Refresh d->Vc / d->Vs from the device when a step made them stale. */
+static void gpu_sync_host(const Data *d)
+{
+  double *vars[8], *faces[3];
+  if (s_gpu == NULL || !s_host_stale) return;
+  gpu_host_arrays((Data *)d, vars, faces);
+  gpu_check(pg_download(s_gpu, vars, faces, PG_LAYOUT_PLUTO), "pg_download");
+  s_host_stale = 0;
+}
+
+static void gpu_atexit(void)
+{
+  if (s_gpu == NULL) return;
+  if (pg_output_wait(s_gpu) != PG_OK)
+    print ("! WriteData (GPU): %s\n", pg_last_error());
+  pg_destroy(s_gpu);
+  s_gpu = NULL;
+}
+
+/* The output request for pg_write_output, or 0 when the device writer does
+   not take this output (the reference's writer then runs on host data). */
+static int gpu_output_spec(const Data *d, Output *output, Grid *grid, pg_output *o)
+{
+  int nv, q, slot[NVAR];
+  static double units[MAX_OUTPUT_VARS];
+
+  if (output->type != DBL_OUTPUT && output->type != FLT_OUTPUT && output->type != VTK_OUTPUT) return 0;
+  if (d->Vuser != NULL || output->nvar > PG_OUT_MAX_VARS) return 0;
+  for (q = 0; q < NVAR; q++) slot[q] = -1;
+  slot[RHO] = 0;
+  EXPAND(slot[VX1] = 1;  , slot[VX2] = 2;  , slot[VX3] = 3;)
+  EXPAND(slot[BX1] = 4;  , slot[BX2] = 5;  , slot[BX3] = 6;)
+  slot[PRS] = 7;
+  memset(o, 0, sizeof *o);
+  o->format = output->type == DBL_OUTPUT ? PG_OUT_DBL : (output->type == FLT_OUTPUT ? PG_OUT_FLT : PG_OUT_VTK);
+  o->single_file = strcmp(output->mode, "single_file") == 0;
+  o->nvar = output->nvar;
+  for (nv = 0; nv < MAX_OUTPUT_VARS; nv++) units[nv] = 1.0;
+  if (output->cgs) GetCGSUnits(units);
+  for (nv = 0; nv < output->nvar; nv++) {
+    int id = -1;
+    for (q = 0; q < NVAR; q++)
+      if (output->V[nv] == d->Vc[q]) id = slot[q];
+  #ifdef STAGGERED_MHD
+    for (q = 0; q < DIMENSIONS; q++)
+      if (output->V[nv] == d->Vs[q]) id = 8 + q;
+  #endif
+    o->dump[nv] = output->dump_var[nv];
+    o->var[nv]  = id < 0 ? 0 : id;
+    o->name[nv] = output->var_name[nv];
+    o->unit[nv] = units[nv];
+    if (o->dump[nv] && (id < 0 || (id >= 8 && output->type != DBL_OUTPUT))) return 0;
+  }
+  o->dir = output->dir;
+  o->xnode[0] = grid->xl_glob[IDIR] + IBEG;
+  o->xnode[1] = grid->xl_glob[JDIR] + JBEG;
+  o->xnode[2] = grid->xl_glob[KDIR] + KBEG;
+  o->time = g_time;
+  o->dt   = g_dt;
+  o->step = g_stepNumber;
+  o->write_record = (prank == 0);
+  return 1;
+}
+
+/* ********************************************************************* */
+void WriteData (const Data *d, Output *output, Grid *grid)
+/*!
+ * WriteData (Src/write_data.c:29) with the .dbl, .flt and .vtk files
+ * written from the device copy of the state.
+ *********************************************************************** */
+{
+  pg_output o;
+  if (s_gpu != NULL && gpu_output_spec(d, output, grid, &o)) {
+    output->nfile++;
+    print ("> Writing file #%d (%s) to disk...", output->nfile, output->ext);
+    o.nfile = output->nfile;
+    gpu_check(pg_write_output(s_gpu, &o), "pg_write_output");
+    print ("\n");
+    return;
+  }
+  gpu_sync_host(d);
+  pg_host_WriteData(d, output, grid);
+}
+
+/* ********************************************************************* */
+void Analysis (const Data *d, Grid *grid)
+/*!
+ * The problem's Analysis() (compiled as pg_user_Analysis) on current host
+ * data.
+ *********************************************************************** */
+{
+  gpu_sync_host(d);
+  pg_user_Analysis(d, grid);
+}
+
 /* ********************************************************************* */
 int AdvanceStep (Data *d, Riemann_Solver *Riemann, timeStep *Dts, Grid *grid)
 /*!
@@ -202,11 +313,13 @@ int AdvanceStep (Data *d, Riemann_Solver *Riemann, timeStep *Dts, Grid *grid)
   double *vars[8], *faces[3];
   pg_step_info info;
   const char *env;
-  long up_every = 0, sync_every = 1;
+  long up_every = 0, sync_every = 0;
 
   if ((env = getenv("PLUTO_GPU_UPLOAD_EVERY")) != NULL) up_every = atol(env);
   if ((env = getenv("PLUTO_GPU_SYNC_EVERY")) != NULL)   sync_every = atol(env);
-  if (sync_every < 1) sync_every = 1;
+  if (sync_every < 0) sync_every = 0;
+  /* a re-upload pushes the host copy: keep it current for host-side edits */
+  if (up_every > 0 && sync_every == 0) sync_every = up_every;
 
   gpu_host_arrays(d, vars, faces);
   s_data = d;
@@ -216,6 +329,7 @@ int AdvanceStep (Data *d, Riemann_Solver *Riemann, timeStep *Dts, Grid *grid)
     int dd, ud = 0;
     gpu_config(&cfg, Riemann, grid);
     gpu_check(pg_create(&cfg, &s_gpu), "pg_create");
+    atexit(gpu_atexit);
     for (dd = 0; dd < DIMENSIONS; dd++)
       ud |= grid->lbound[dd] == USERDEF || grid->rbound[dd] == USERDEF;
   #if INTERNAL_BOUNDARY == YES
@@ -240,8 +354,7 @@ int AdvanceStep (Data *d, Riemann_Solver *Riemann, timeStep *Dts, Grid *grid)
   Dts->invDt_hyp = MAX(Dts->invDt_hyp, info.inv_dt_hyp);
   g_maxMach      = MAX(g_maxMach, info.max_mach);
 
-  if (s_calls % sync_every == 0) {
-    gpu_check(pg_download(s_gpu, vars, faces, PG_LAYOUT_PLUTO), "pg_download");
-  }
+  s_host_stale = 1;
+  if (sync_every > 0 && s_calls % sync_every == 0) gpu_sync_host(d);
   return 0;
 }

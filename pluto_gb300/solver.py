@@ -63,6 +63,10 @@ def make_config(spec: dict, precision: str = "fp64", compute_mach: bool = False)
     return c
 
 
+# SetDefaultVarNames (Src/var_names.c) names of the 8 slots
+OUTPUT_NAMES = ["rho", "vx1", "vx2", "vx3", "Bx1", "Bx2", "Bx3", "prs"]
+
+
 def _ptrs(arrs, n):
     P = C.POINTER(C.c_double)
     out = (P * n)()
@@ -182,6 +186,81 @@ class Solver:
         preallocated arrays instead (e.g. pinned host memory, which the
         device writes in place)."""
         return self._get("pg_download", out)
+
+    # -- output files (WriteData's .dbl / .flt / .vtk) --
+    def output_vars(self, fmt: str, vtk_vector: bool = False):
+        """[(var id, name, dump)] in the order SetOutput lists them: the
+        primitives (PLUTO's NVAR order), then Bx1s.. under CT (dumped in .dbl
+        only); VTK_VECTOR_DUMP makes vx1 and Bx1 vector entries."""
+        comps = self.cfg.components
+        slots = [0, 1, 2] + ([3] if comps == 3 else []) + [4, 5] + ([6] if comps == 3 else []) + [7]
+        out = [[q, OUTPUT_NAMES[q], 1] for q in slots]
+        if self.ct:
+            out += [[8 + d, f"Bx{d + 1}s", 1 if fmt == "dbl" else 0] for d in range(self.dims)]
+        if fmt == "vtk" and vtk_vector:
+            for first in (1, 4):
+                for e in out:
+                    if first <= e[0] < first + self.dims:
+                        e[2] = L.PG_OUT_VECTOR if e[0] == first else 0
+        return [tuple(e) for e in out]
+
+    def _output_spec(self, directory, fmt, nfile, single_file, vars, units, xbeg, xend, time, dt, step,
+                     write_record, vtk_vector):
+        o = L.PgOutput()
+        o.format = {"dbl": L.PG_OUT_DBL, "flt": L.PG_OUT_FLT, "vtk": L.PG_OUT_VTK}[fmt]
+        o.single_file = int(bool(single_file))
+        o.nfile = int(nfile)
+        vars = list(vars if vars is not None else self.output_vars(fmt, vtk_vector))
+        if len(vars) > L.PG_OUT_MAX_VARS:
+            raise ValueError("too many output variables")
+        o.nvar = len(vars)
+        units = units or {}
+        keep = []
+        for m, (vid, name, dump) in enumerate(vars):
+            o.var[m] = int(vid)
+            o.dump[m] = int(dump)
+            keep.append(name.encode())
+            o.name[m] = keep[-1]
+            o.unit[m] = float(units.get(name, 1.0))
+        keep.append(str(directory).encode())
+        o.dir = keep[-1]
+        if fmt == "vtk":
+            xbeg = xbeg if xbeg is not None else (0.0, 0.0, 0.0)
+            xend = xend if xend is not None else tuple(xbeg[d] + self.cfg.nx[d] * self.cfg.dx[d] for d in range(3))
+            for d in range(3):
+                n = self.cfg.nx[d] if d < self.dims else 1
+                dx = (xend[d] - xbeg[d]) / float(n)
+                x = np.array([xbeg[d] + float(i) * dx for i in range(n)] + [0.0])
+                x[n] = x[n - 1] + dx  # Src/set_grid.c:395-403, :60-64
+                keep.append(x)
+                o.xnode[d] = x.ctypes.data_as(C.POINTER(C.c_double))
+        o.time, o.dt, o.step = float(time), float(dt), int(step)
+        o.write_record = int(bool(write_record))
+        return o, keep
+
+    def write_output(self, directory, fmt: str = "dbl", nfile: int = 0, *, single_file: bool = True,
+                     vars=None, units=None, xbeg=None, xend=None, time: float = 0.0, dt: float = 0.0,
+                     step: int = 0, write_record: bool = True, vtk_vector: bool = False):
+        """Write the current state as PLUTO's WriteData would (files
+        data.NNNN.<fmt> or <var>.NNNN.<fmt> and the <fmt>.out record) from the
+        device, asynchronously: returns once the state is packed on the
+        device; output_wait() blocks until the files are written.  VTK needs
+        the domain extents xbeg/xend (pluto.ini X*-grid) for the node
+        coordinates; inactive axes take the reference's 0..1."""
+        o, keep = self._output_spec(directory, fmt, nfile, single_file, vars, units, xbeg, xend, time, dt,
+                                    step, write_record, vtk_vector)
+        L.check(L.lib().pg_write_output(self.h, C.byref(o)), "pg_write_output")
+        del keep
+
+    def output_wait(self):
+        L.check(L.lib().pg_output_wait(self.h), "pg_output_wait")
+
+    def read_output(self, directory, nfile: int, *, single_file: bool = True, vars=None):
+        """Restart: upload the state of a .dbl written as above."""
+        o, keep = self._output_spec(directory, "dbl", nfile, single_file, vars, None, None, None, 0.0, 0.0, 0,
+                                    False, False)
+        L.check(L.lib().pg_read_output(self.h, C.byref(o)), "pg_read_output")
+        del keep
 
     # -- differentiation (frozen dt) --
     def tangent_upload(self, dvc: np.ndarray, dbs=(None, None, None)):

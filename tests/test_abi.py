@@ -89,8 +89,9 @@ def test_char_tracing_validation(lib, extra, ok):
         lib.pg_destroy(h)
 
 
-def test_config_layout_matches_header(tmp_path):
-    """The ctypes pg_config matches the C header field by field (offsets and
+@pytest.mark.parametrize("struct,cname", [("PgConfig", "pg_config"), ("PgOutput", "pg_output")])
+def test_config_layout_matches_header(tmp_path, struct, cname):
+    """The ctypes structures match the C header field by field (offsets and
     size, from a program compiled against include/pluto_gb300.h)."""
     import shutil
     import subprocess
@@ -98,15 +99,16 @@ def test_config_layout_matches_header(tmp_path):
     cc = shutil.which("gcc") or shutil.which("cc")
     if not cc:
         pytest.skip("no C compiler")
-    names = [f[0] for f in L.PgConfig._fields_]
+    S = getattr(L, struct)
+    names = [f[0] for f in S._fields_]
     src = tmp_path / "layout.c"
     src.write_text("#include <stdio.h>\n#include <stddef.h>\n#include \"pluto_gb300.h\"\nint main(void){\n"
-                   + "".join(f'printf("%zu\\n", offsetof(pg_config, {n}));\n' for n in names)
-                   + 'printf("%zu\\n", sizeof(pg_config)); return 0; }\n')
+                   + "".join(f'printf("%zu\\n", offsetof({cname}, {n}));\n' for n in names)
+                   + f'printf("%zu\\n", sizeof({cname})); return 0; }}\n')
     exe = tmp_path / "layout"
     subprocess.run([cc, "-I", str(ROOT / "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
-    want = [getattr(L.PgConfig, n).offset for n in names] + [C.sizeof(L.PgConfig)]
+    want = [getattr(S, n).offset for n in names] + [C.sizeof(S)]
     assert got == want, dict(zip(names + ["sizeof"], zip(got, want)))
 
 

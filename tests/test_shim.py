@@ -22,8 +22,16 @@ def _link(setup_fn, tmp_path):
     lib = pb.build()
     s = setup_fn()
     run = br.build(s)  # reference objects for this scheme
-    objs = [p for p in (run / "obj").glob("*.o") if p.stem not in ("rk_step", "update_stage")]
+    objs = [p for p in (run / "obj").glob("*.o")
+            if p.stem not in ("rk_step", "update_stage", "ctu_step", "write_data", "init")]
     inc = ["-I", str(run)] + sum((["-I", str(REF / d)] for d in br.INC_DIRS), []) + ["-I", str(ROOT / "include")]
+    # the two objects Makefile.gpu compiles with renamed definitions (wrapped by the shim)
+    for src, define in ((REF / "Src" / "write_data.c", "-DWriteData=pg_host_WriteData"),
+                        (run / "init.c", "-DAnalysis=pg_user_Analysis")):
+        o = tmp_path / (src.stem + ".o")
+        subprocess.run(["gcc", "-c", "-O2", "-w", define, *inc, str(src), "-o", str(o)],
+                       check=True, capture_output=True, text=True)
+        objs.append(o)
     shim_o = tmp_path / "gpu_step.o"
     subprocess.run(["gcc", "-c", "-O2", "-Wall", "-Wno-unused-variable", *inc,
                     str(ROOT / "pluto_gb300" / "shim" / "gpu_step.c"), "-o", str(shim_o)],
@@ -67,8 +75,11 @@ def test_enable_script_edits_the_template_makefile(tmp_path):
     assert once.index("Additional_object_files_here") < once.index(en.BEGIN) < once.index("PLUTO target rule")
     en.main([str(mk)])
     assert mk.read_text() == once
+    (tmp_path / "write_data.o").write_bytes(b"stale")
+    (tmp_path / "init.o").write_bytes(b"stale")
     en.main([str(mk), "--disable"])
     assert mk.read_text() == orig
+    assert not (tmp_path / "write_data.o").exists() and not (tmp_path / "init.o").exists()
 
 
 def test_shim_links_internal_boundary(tmp_path):
