@@ -27,7 +27,7 @@
 extern "C" {
 #endif
 
-#define PG_ABI_VERSION 2  /* 2: pg_config gained bc_hi / bc_sides */
+#define PG_ABI_VERSION 3  /* 2: pg_config gained bc_hi / bc_sides; 3: char_limiting */
 
 /* status codes */
 enum {
@@ -86,6 +86,9 @@ typedef struct {
   int bc_hi[3];         /* type of the end side (X*_END) when bc_sides is 1 */
   int bc_sides;         /* 0: bc[d] on both sides; 1: bc[d] / bc_hi[d] per side
                            (PERIODIC must then be on both sides of an axis) */
+  int char_limiting;    /* CHAR_LIMITING YES: PLM slopes limited in characteristic
+                           variables (Src/States/plm_states.c:446-705); LINEAR
+                           reconstruction, PG_FP64 solvers (RK and CTU) */
 } pg_config;
 
 typedef struct {

@@ -83,6 +83,7 @@ class Setup:
     dbl_mode: str = "single_file"    # [Static Grid Output] dbl mode
     out_modes: tuple = ()            # extra outputs written at the dbl cadence: ((fmt, mode), ...)
     vtk_vector: bool = False         # VTK_VECTOR_DUMP YES
+    char_limiting: bool = False      # CHAR_LIMITING YES
 
 
 def _fmt(x: float) -> str:
@@ -112,6 +113,8 @@ def definitions_h(s: Setup) -> str:
         out.append(f"#define  {key:<30} {idx}")
     out.append("/* [Beg] user-defined constants (do not change this line) */")
     out.append(f"#define  LIMITER                        {s.limiter}")
+    if s.char_limiting:
+        out.append("#define  CHAR_LIMITING                  YES")
     if s.ct:
         out.append(f"#define  CT_EMF_AVERAGE                 {s.emf}")
         out.append(f"#define  ASSIGN_VECTOR_POTENTIAL        {'YES' if s.vecpot else 'NO'}")

@@ -914,6 +914,9 @@ static void pencil_free(Pencil *w) {
   free(w->rhs); free(w->bn); free(w->ifc);
 }
 
+static void plm_char_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV], int beg, int end, int lim,
+                            double gamma, const Rot *r, int c3, int dims);
+
 static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1d,
                   double *mach_out) {
   const int dims = p->c.dims;
@@ -957,7 +960,9 @@ static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1
       /* States, update_stage.c:193 with beg = nbeg-1, end = nend+1 */
       {
         int beg = nbeg - 1, end = nend + 1;
-        if (p->c.recon == OC_LINEAR) plm_states(w.v, w.vp, w.vm, beg, end, p->c.limiter);
+        if (p->c.recon == OC_LINEAR && p->c.char_limiting)
+          plm_char_states(w.v, w.vp, w.vm, beg, end, p->c.limiter, p->c.gamma, &r, p->c.components == 3, dims);
+        else if (p->c.recon == OC_LINEAR) plm_states(w.v, w.vp, w.vm, beg, end, p->c.limiter);
         else ppm_states(w.v, w.vp, w.vm, beg, end);
         if (p->c.ct) { /* plm_states.c:271-275 */
           for (i = beg - 1; i <= end; i++) {
@@ -1489,6 +1494,56 @@ static void char_tracing(const double *vc, double *vp, double *vm, double gamma,
   }
 }
 
+
+/* States with CHAR_LIMITING YES, Src/States/plm_states.c:446-705 (uniform
+   Cartesian grid: cp = cm = 2, dp = dm = 0.5): per cell the undivided
+   differences projected on the left eigenvectors of PrimEigenvectors, limited
+   per characteristic family (LIMITER DEFAULT: the generalised minmod with
+   steepness kstp 1 for fast and slow waves, 2 otherwise), projected back on
+   the right eigenvectors and clipped by MINMOD against twice the primitive
+   differences. */
+static void plm_char_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV], int beg, int end, int lim,
+                            double gamma, const Rot *r, int c3, int dims) {
+  const int nflx = c3 ? 8 : 6;
+  int i, k, nv;
+  for (i = beg; i <= end; i++) {
+    double L[8][8], R[8][8], lambda[8], dvp[NV], dvm[NV], dwp[8], dwm[8], dwl[8];
+    const double a2 = gamma * v[i][PRS] / v[i][RHO]; /* SoundSpeed2 */
+    prim_eigen(v[i], a2, r, c3, dims, L, R, lambda);
+    for (nv = 0; nv < NV; nv++) {
+      dvp[nv] = v[i + 1][nv] - v[i][nv];
+      dvm[nv] = v[i][nv] - v[i - 1][nv];
+    }
+    prim_to_char(L, dvm, r, c3, dwm);
+    prim_to_char(L, dvp, r, c3, dwp);
+    for (k = nflx; k--;) {
+      if (lim == OC_DEFAULT_LIM) { /* SET_GM_LIMITER, plm_coeffs.h:96-100 */
+        const double ck = (k == WFM || k == WFP || k == WSM || k == WSP) ? 1.0 : 2.0;
+        if (dwp[k] * dwm[k] > 0.0) {
+          double qc = 0.5 * (dwm[k] + dwp[k]), scrh = ABS_MIN(dwp[k] * ck, dwm[k] * ck);
+          dwl[k] = ABS_MIN(qc, scrh);
+        } else dwl[k] = 0.0;
+      } else {
+        dwl[k] = limit(lim, -1, dwp[k], dwm[k]);
+      }
+    }
+    for (nv = NV; nv--;) {
+      double dc = 0.0, dvl;
+      if (!c3 && (nv == VX3 || nv == BX3)) {
+        vp[i][nv] = vm[i][nv] = v[i][nv];
+        continue;
+      }
+      for (k = 0; k < nflx; k++) dc += dwl[k] * R[nv][k];
+      if (dvp[nv] * dvm[nv] > 0.0) {
+        double d2v = ABS_MIN(2.0 * dvp[nv], 2.0 * dvm[nv]);
+        dvl = MINMOD(d2v, dc);
+      } else dvl = 0.0;
+      vp[i][nv] = v[i][nv] + dvl * 0.5;
+      vm[i][nv] = v[i][nv] - dvl * 0.5;
+    }
+  }
+}
+
 /* face-EMF slot of (dir, component): ezi, ezj, eyi, eyk, exj, exk */
 enum { EZI = 0, EZJ, EYI, EYK, EXJ, EXK };
 
@@ -1545,7 +1600,10 @@ static void ctu_sweep(oc_problem *p, int dir, double dt, int stage, double *inv_
         if (ct) w.bn[i] = p->bs[dir][FI(p, dir, ijk[2], ijk[1], ijk[0])];
       }
       if (stage == 1) {
-        plm_states(w.v, w.vp, w.vm, nbeg - 1, nend + 1, p->c.limiter);
+        if (p->c.char_limiting)
+          plm_char_states(w.v, w.vp, w.vm, nbeg - 1, nend + 1, p->c.limiter, p->c.gamma, &r, c3, dims);
+        else
+          plm_states(w.v, w.vp, w.vm, nbeg - 1, nend + 1, p->c.limiter);
         if (ct)
           for (i = nbeg - 2; i <= nend + 1; i++) {
             w.vp[i][r.bn] = w.bn[i];
@@ -2051,6 +2109,7 @@ oc_problem *oc_create(const oc_config *cfg) {
     if (cfg->bc_hi[d] < OC_PERIODIC || cfg->bc_hi[d] > OC_USERDEF) { free(p); return NULL; }
     if ((cfg->bc[d] == OC_PERIODIC) != (cfg->bc_hi[d] == OC_PERIODIC)) { free(p); return NULL; }
   }
+  if (cfg->char_limiting && cfg->recon != OC_LINEAR) { free(p); return NULL; } /* PPM form not restated */
   p->ng = cfg->recon == OC_PARABOLIC ? 3 : 2; /* Src/get_nghost.c:28-104 */
   if (IS_CTU(cfg->stepping)) {
     if (cfg->recon != OC_LINEAR) { free(p); return NULL; } /* hancock.c:64-67 */

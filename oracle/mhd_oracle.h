@@ -50,6 +50,7 @@ typedef struct {
   int nthreads;        /* OpenMP threads (0: runtime default) */
   int emf;             /* CT_EMF_AVERAGE (0 = UCT_HLL) */
   int bc_hi[3];        /* end side (X*-end) */
+  int char_limiting;   /* CHAR_LIMITING YES (LINEAR reconstruction) */
 } oc_config;
 
 typedef struct oc_problem oc_problem;

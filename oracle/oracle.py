@@ -30,7 +30,7 @@ class OcConfig(C.Structure):
                 ("dx", C.c_double * 3), ("gamma", C.c_double), ("recon", C.c_int),
                 ("limiter", C.c_int), ("solver", C.c_int), ("stepping", C.c_int),
                 ("ct", C.c_int), ("bc", C.c_int * 3), ("nthreads", C.c_int), ("emf", C.c_int),
-                ("bc_hi", C.c_int * 3)]
+                ("bc_hi", C.c_int * 3), ("char_limiting", C.c_int)]
 
 
 _lib = None
@@ -111,6 +111,7 @@ class Oracle:
         c.ct = int(bool(spec["ct"]))
         c.nthreads = nthreads
         c.emf = EMF[spec.get("emf", "UCT_HLL")]
+        c.char_limiting = int(bool(spec.get("char_limiting", False)))
         self.h = lib().oc_create(C.byref(c))
         if not self.h:
             raise ValueError("oracle rejected the configuration")

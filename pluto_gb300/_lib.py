@@ -37,7 +37,7 @@ EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", 
            "pg_adjoint_step", "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load",
            "pg_selftest_conversions", "pg_set_userdef", "pg_set_internal_boundary",
            "pg_write_output", "pg_output_wait", "pg_read_output"]
-PG_ABI_VERSION = 2  # the pg_config layout these bindings describe
+PG_ABI_VERSION = 3  # the pg_config layout these bindings describe
 # pg_userdef_fn: (user, side 0..5, vpos 0 cells / 1..3 faces, stage)
 USERDEF_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int)
 PG_STATIC_MAX_ZONES = 32768
@@ -51,7 +51,7 @@ class PgConfig(C.Structure):
                 ("time_stepping", C.c_int), ("divb", C.c_int), ("emf_average", C.c_int),
                 ("bc", C.c_int * 3), ("precision", C.c_int), ("compute_mach", C.c_int),
                 ("small_density", C.c_double), ("small_pressure", C.c_double),
-                ("bc_hi", C.c_int * 3), ("bc_sides", C.c_int)]
+                ("bc_hi", C.c_int * 3), ("bc_sides", C.c_int), ("char_limiting", C.c_int)]
 
 
 PG_OUT_DBL, PG_OUT_FLT, PG_OUT_VTK = 0, 1, 2

@@ -182,6 +182,7 @@ extern "C" int pg_batch_create(const pg_config* cfg, int ntubes, const int* nx, 
     return bfail(PG_ERR_INVALID, "pg_batch_create: batches take RK2 or RK3 time stepping");
   if (c.bc[0] == PG_USERDEF || (c.bc_sides && c.bc_hi[0] == PG_USERDEF))
     return bfail(PG_ERR_INVALID, "pg_batch_create: user-defined boundaries are not batched");
+  if (c.char_limiting) return bfail(PG_ERR_INVALID, "pg_batch_create: CHAR_LIMITING is not batched");
   int rs;
   if (c.reconstruction == PG_PARABOLIC) rs = 4;
   else if (c.limiter == PG_MINMOD_LIM) rs = 1;

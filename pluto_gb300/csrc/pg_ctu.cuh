@@ -40,219 +40,6 @@ __device__ __forceinline__ void prim_rhs(const T* v, const T* dv, double gamma, 
   Adv[PRS] = gamma * v[PRS] * dv[vn] + v[vn] * dv[PRS];
 }
 
-// PrimEigenvectors (Src/MHD/eigenv.c:190-688, ideal EOS, no 8-wave / GLM):
-// eigenvalues and left/right primitive eigenvectors along DIR in the wave
-// order fast-, fast+, entropy, div-B, slow-, slow+, Alfven-, Alfven+
-// (Src/MHD/mod_defs.h:54-71).  L[wave][var], R[var][wave] start at zero;
-// the zero entries take part in the tracing sums below like in the
-// reference's dense loops.
-enum : int { WFM = 0, WFP, WEN, WDB, WSM, WSP, WAM, WAP };
-template <int DIR>
-__device__ __forceinline__ void prim_eigen(const double* q, double a2, bool c3, int dims, double L[8][8],
-                                           double R[8][8], double* lambda) {
-  using Rt = Rot<DIR>;
-  constexpr int vn = Rt::vn, vt = Rt::vt, vb = Rt::vb, bn = Rt::bn, bt = Rt::bt, bb = Rt::bb;
-  const double sqrt_1_2 = 0.70710678118654752440;
-#pragma unroll
-  for (int a = 0; a < 8; a++) {
-    lambda[a] = 0.0;
-#pragma unroll
-    for (int b = 0; b < 8; b++) L[a][b] = R[a][b] = 0.0;
-  }
-  const double u = q[vn], tau = 1.0 / q[RHO], sqrt_rho = ::sqrt(q[RHO]);
-  double scrh0, scrh1, scrh2, scrh3, scrh4;
-  scrh2 = q[bn] * q[bn];
-  scrh3 = c3 ? 0.0 + q[bt] * q[bt] + q[bb] * q[bb] : 0.0 + q[bt] * q[bt];
-  const double b2 = scrh2 + scrh3, ca2 = scrh2 * tau, A2 = b2 * tau, At2 = scrh3 * tau;
-  scrh1 = a2 - A2;
-  scrh0 = ::sqrt(scrh1 * scrh1 + 4.0 * a2 * At2);
-  const double cf2 = 0.5 * (a2 + A2 + scrh0), cs2 = a2 * ca2 / cf2;
-  const double cf = ::sqrt(cf2), cs = ::sqrt(cs2), ca = ::sqrt(ca2), a = ::sqrt(a2);
-  double alpha_f, alpha_s;
-  if (cf == cs) {
-    alpha_f = 1.0;
-    alpha_s = 0.0;
-  } else {
-    scrh0 = 1.0 / scrh0;
-    alpha_f = ::sqrt(pmax(0.0, (a2 - cs2) * scrh0));
-    alpha_s = ::sqrt(pmax(0.0, (cf2 - a2) * scrh0));
-  }
-  double beta_y, beta_z = 0.0;
-  scrh0 = ::sqrt(scrh3);
-  if (scrh0 > 1.e-9) {
-    if (c3) {
-      beta_y = q[bt] / scrh0;
-      beta_z = q[bb] / scrh0;
-    } else {
-      beta_y = q[bt] >= 0.0 ? 1.0 : -1.0;
-    }
-  } else {
-    beta_y = c3 ? sqrt_1_2 : 1.0;
-    if (c3) beta_z = sqrt_1_2;
-  }
-  const double S = q[bn] >= 0.0 ? 1.0 : -1.0;
-  // fast waves
-  lambda[WFM] = u - cf;
-  scrh0 = alpha_s * cs * S;
-  scrh1 = alpha_s * sqrt_rho * a;
-  scrh2 = 0.5 / a2;
-  scrh3 = scrh2 * tau;
-  R[RHO][WFM] = q[RHO] * alpha_f;
-  R[vn][WFM] = -cf * alpha_f;
-  R[vt][WFM] = scrh0 * beta_y;
-  R[bt][WFM] = scrh1 * beta_y;
-  if (c3) {
-    R[vb][WFM] = scrh0 * beta_z;
-    R[bb][WFM] = scrh1 * beta_z;
-  }
-  R[PRS][WFM] = alpha_f * a2 * q[RHO];
-  L[WFM][vn] = R[vn][WFM] * scrh2;
-  L[WFM][vt] = R[vt][WFM] * scrh2;
-  L[WFM][bt] = R[bt][WFM] * scrh3;
-  if (c3) {
-    L[WFM][vb] = R[vb][WFM] * scrh2;
-    L[WFM][bb] = R[bb][WFM] * scrh3;
-  }
-  L[WFM][PRS] = alpha_f * scrh3;
-  lambda[WFP] = u + cf;
-#pragma unroll
-  for (int v = 0; v < 8; v++) {
-    const bool odd = v == vn || v == vt || v == vb;  // velocities flip sign
-    R[v][WFP] = odd ? -R[v][WFM] : R[v][WFM];
-    L[WFP][v] = odd ? -L[WFM][v] : L[WFM][v];
-  }
-  // entropy and div-B waves
-  lambda[WEN] = u;
-  R[RHO][WEN] = 1.0;
-  L[WEN][RHO] = 1.0;
-  L[WEN][PRS] = -1.0 / a2;
-  lambda[WDB] = 0.0;
-  // slow waves
-  lambda[WSM] = u - cs;
-  scrh0 = alpha_f * cf * S;
-  scrh1 = alpha_f * sqrt_rho * a;
-  R[RHO][WSM] = q[RHO] * alpha_s;
-  R[vn][WSM] = -cs * alpha_s;
-  R[vt][WSM] = -scrh0 * beta_y;
-  R[bt][WSM] = -scrh1 * beta_y;
-  if (c3) {
-    R[vb][WSM] = -scrh0 * beta_z;
-    R[bb][WSM] = -scrh1 * beta_z;
-  }
-  scrh4 = alpha_s * a2 * q[RHO];
-  R[PRS][WSM] = scrh4;
-  L[WSM][vn] = R[vn][WSM] * scrh2;
-  L[WSM][vt] = R[vt][WSM] * scrh2;
-  L[WSM][bt] = R[bt][WSM] * scrh3;
-  if (c3) {
-    L[WSM][vb] = R[vb][WSM] * scrh2;
-    L[WSM][bb] = R[bb][WSM] * scrh3;
-  }
-  L[WSM][PRS] = alpha_s * scrh3;
-  lambda[WSP] = u + cs;
-#pragma unroll
-  for (int v = 0; v < 8; v++) {
-    const bool odd = v == vn || v == vt || v == vb;
-    R[v][WSP] = odd ? -R[v][WSM] : R[v][WSM];
-    L[WSP][v] = odd ? -L[WSM][v] : L[WSM][v];
-  }
-  // Alfven waves (three components)
-  if (c3) {
-    lambda[WAM] = u - ca;
-    scrh2 = beta_y * sqrt_1_2;
-    scrh3 = beta_z * sqrt_1_2;
-    R[vt][WAM] = -scrh3;
-    R[vb][WAM] = scrh2;
-    R[bt][WAM] = -scrh3 * sqrt_rho * S;
-    R[bb][WAM] = scrh2 * sqrt_rho * S;
-    L[WAM][vt] = R[vt][WAM];
-    L[WAM][vb] = R[vb][WAM];
-    L[WAM][bt] = R[bt][WAM] * tau;
-    L[WAM][bb] = R[bb][WAM] * tau;
-    lambda[WAP] = u + ca;
-    R[vt][WAP] = R[vt][WAM];
-    R[vb][WAP] = R[vb][WAM];
-    R[bt][WAP] = -R[bt][WAM];
-    R[bb][WAP] = -R[bb][WAM];
-    L[WAP][vt] = L[WAM][vt];
-    L[WAP][vb] = L[WAM][vb];
-    L[WAP][bt] = -L[WAM][bt];
-    L[WAP][bb] = -L[WAM][bb];
-    if (dims <= 2 && q[bn] == 0 && q[bt] == 0.0)  // eigenv.c:528-531
-#pragma unroll
-      for (int k = 0; k < 8; k++) R[bt][k] = 0.0;
-  }
-}
-
-// CharTracingStep (Src/States/char_tracing.c:280-573; LINEAR, reference
-// state 3, uniform Cartesian grid, no passive scalars): the PLM states vp, vm
-// of the zone with centre value vc are replaced by their characteristic
-// traces over dt/2.  PrimSource is zero here (Src/MHD/prim_eqn.c:120-210
-// without geometry, gravity or div-B terms) and is added as +0.  With two
-// components the third velocity and field slots are left alone.
-template <int DIR>
-__device__ __forceinline__ void char_tracing(const double* vc, double* vp, double* vm, double gamma, double dtdx,
-                                             double dt, bool c3, int dims) {
-  using Rt = Rot<DIR>;
-  constexpr int vn = Rt::vn, vt = Rt::vt, vb = Rt::vb, bt = Rt::bt, bb = Rt::bb;
-  double L[8][8], R[8][8], lambda[8];
-  const double a2 = gamma * vc[PRS] / vc[RHO];  // SoundSpeed2, Src/EOS/Ideal/eos.c:33
-  prim_eigen<DIR>(vc, a2, c3, dims, L, R, lambda);
-  const int nflx = c3 ? 8 : 6;
-  double nu[8], dv[8], dw[8];
-#pragma unroll
-  for (int k = 0; k < 8; k++) nu[k] = dtdx * lambda[k];
-  const double nu_max = pmax(nu[1], 0.0), nu_min = pmin(nu[0], 0.0);
-#pragma unroll
-  for (int v = 0; v < 8; v++) dv[v] = vp[v] - vm[v];
-  {  // PrimToChar, Src/MHD/eigenv.c:1310-1380
-    double wv, wB;
-    wv = c3 ? L[WFM][vn] * dv[vn] + L[WFM][vt] * dv[vt] + L[WFM][vb] * dv[vb]
-            : L[WFM][vn] * dv[vn] + L[WFM][vt] * dv[vt];
-    wB = c3 ? L[WFM][PRS] * dv[PRS] + L[WFM][bt] * dv[bt] + L[WFM][bb] * dv[bb]
-            : L[WFM][PRS] * dv[PRS] + L[WFM][bt] * dv[bt];
-    dw[WFM] = wv + wB;
-    dw[WFP] = -wv + wB;
-    dw[WEN] = L[WEN][RHO] * dv[RHO] + L[WEN][PRS] * dv[PRS];
-    dw[WDB] = 0.0;
-    wv = c3 ? L[WSM][vn] * dv[vn] + L[WSM][vt] * dv[vt] + L[WSM][vb] * dv[vb]
-            : L[WSM][vn] * dv[vn] + L[WSM][vt] * dv[vt];
-    wB = c3 ? L[WSM][PRS] * dv[PRS] + L[WSM][bt] * dv[bt] + L[WSM][bb] * dv[bb]
-            : L[WSM][PRS] * dv[PRS] + L[WSM][bt] * dv[bt];
-    dw[WSM] = wv + wB;
-    dw[WSP] = -wv + wB;
-    wv = L[WAM][vt] * dv[vt] + L[WAM][vb] * dv[vb];
-    wB = L[WAM][bt] * dv[bt] + L[WAM][bb] * dv[bb];
-    dw[WAM] = wv + wB;
-    dw[WAP] = wv - wB;
-  }
-#pragma unroll
-  for (int v = 0; v < 8; v++) {
-    if (!c3 && (v == VX3 || v == BX3)) continue;
-    vp[v] = vc[v] + 0.5 * dv[v] * (1.0 - nu_max);
-    vm[v] = vc[v] - 0.5 * dv[v] * (1.0 + nu_min);
-  }
-#pragma unroll
-  for (int k = 0; k < 8; k++) {
-    if (k >= nflx) break;
-    const bool right = nu[k] >= 0.0;
-    const double w = dw[k] * (right ? 0.5 * (nu_max - nu[k]) : 0.5 * (nu_min - nu[k]));
-#pragma unroll
-    for (int v = 0; v < 8; v++) {
-      if (!c3 && (v == VX3 || v == BX3)) continue;
-      if (right) vp[v] += w * R[v][k];
-      else vm[v] += w * R[v][k];
-    }
-  }
-  const double src = 0.0;
-#pragma unroll
-  for (int v = 0; v < 8; v++) {
-    if (!c3 && (v == VX3 || v == BX3)) continue;
-    vp[v] += 0.5 * dt * src;
-    vm[v] += 0.5 * dt * src;
-  }
-}
-
 template <class T>
 __global__ void k_ctu_begin(F64A<T> a) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -286,15 +73,31 @@ __global__ void k_ctu_states(F64A<T> a, Box box) {
   const double dt2 = 0.5 * a.sc->dt;
   const double inv_dl = g.inv_dx[DIR];
   T v0[NV], vp[NV], vm[NV];
+  bool limited = false;
+  if constexpr (std::is_same<T, double>::value) {
+    if (a.char_lim) {  // CHAR_LIMITING YES, plm_states.c:446-705
+      double vl[NV], vr[NV];
 #pragma unroll
-  for (int nv = 0; nv < NV; nv++) {
-    const T* V = a.V[nv];
-    v0[nv] = V[c];
-    T dvp = V[c + s] - v0[nv];
-    T dvm = v0[nv] - V[c - s];
-    T dv = limit(a.limiter, nv, dvp, dvm);
-    vp[nv] = v0[nv] + dv * 0.5;
-    vm[nv] = v0[nv] - dv * 0.5;
+      for (int nv = 0; nv < NV; nv++) {
+        vl[nv] = a.V[nv][c - s];
+        v0[nv] = a.V[nv][c];
+        vr[nv] = a.V[nv][c + s];
+      }
+      plm_char<DIR>(vl, v0, vr, a.gamma, a.limiter, a.c3 != 0, g.dims, vp, vm);
+      limited = true;
+    }
+  }
+  if (!limited) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) {
+      const T* V = a.V[nv];
+      v0[nv] = V[c];
+      T dvp = V[c + s] - v0[nv];
+      T dvm = v0[nv] - V[c - s];
+      T dv = limit(a.limiter, nv, dvp, dvm);
+      vp[nv] = v0[nv] + dv * 0.5;
+      vm[nv] = v0[nv] - dv * 0.5;
+    }
   }
   if (a.ct) {  // plm_states.c:271-275
     vp[R::bn] = a.Bs[DIR][c];

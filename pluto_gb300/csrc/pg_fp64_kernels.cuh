@@ -10,6 +10,7 @@
 #include "pg_physics.cuh"
 #include "pg_dual.cuh"
 #include "pg_bound_ct.cuh"
+#include "pg_char.cuh"
 
 namespace pg {
 
@@ -49,6 +50,7 @@ struct F64A {
   int div_dims;     // RK: invDt_hyp /= DIMENSIONS (update_stage.c:311); CTU: no
   int emf_avg, c3;
   int chtr;         // CTU predictor: characteristic tracing (else primitive Hancock)
+  int char_lim;     // CHAR_LIMITING YES: PLM limited in characteristic variables
 };
 
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
@@ -176,7 +178,22 @@ __global__ void k_recon(F64A<T> a, Box box) {
   const Geom& g = a.g;
   const long long c = cidx(g, k, j, i), s = g.s[DIR];
   T vp[NV], vm[NV];
-  if (a.recon == PG_LINEAR) {
+  bool done = false;
+  if constexpr (std::is_same<T, double>::value) {
+    if (a.char_lim) {  // CHAR_LIMITING YES, plm_states.c:446-705
+      double vl[NV], v0[NV], vr[NV];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        vl[nv] = a.V[nv][c - s];
+        v0[nv] = a.V[nv][c];
+        vr[nv] = a.V[nv][c + s];
+      }
+      plm_char<DIR>(vl, v0, vr, a.gamma, a.limiter, a.c3 != 0, g.dims, vp, vm);
+      done = true;
+    }
+  }
+  if (done) {
+  } else if (a.recon == PG_LINEAR) {
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
       const T* V = a.V[nv];
@@ -515,6 +532,7 @@ static F64A<T> make_args(Solver* S) {
   for (int d = 0; d < 3; d++) a.SV[d] = S->SV[d];
   a.div_dims = !is_ctu(S->cfg.time_stepping);
   a.chtr = S->cfg.time_stepping == PG_CHAR_TRACING;
+  a.char_lim = S->cfg.char_limiting;
   a.emf_avg = S->cfg.emf_average;
   a.c3 = S->cfg.components == 3;
   a.intb = S->ud_internal ? 1 : 0;

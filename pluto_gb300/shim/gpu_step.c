@@ -105,6 +105,9 @@ static void gpu_config(pg_config *c, Riemann_Solver *Riemann, Grid *grid)
   c->limiter = PG_DEFAULT_LIM;
 #endif
   c->riemann = gpu_riemann(Riemann);
+#if CHAR_LIMITING == YES
+  c->char_limiting = 1;
+#endif
 #if TIME_STEPPING == RK3
   c->time_stepping = PG_RK3;
 #elif TIME_STEPPING == EULER

@@ -56,6 +56,7 @@ def make_config(spec: dict, precision: str = "fp64", compute_mach: bool = False)
     c.time_stepping = STEPPING[spec.get("stepping", "RK2")]
     c.divb = L.PG_CONSTRAINED_TRANSPORT if spec.get("ct", True) else L.PG_DIVB_NONE
     c.emf_average = EMF[spec.get("emf", "UCT_HLL")]
+    c.char_limiting = int(bool(spec.get("char_limiting", False)))
     c.precision = PRECISION[precision]
     c.compute_mach = int(bool(compute_mach))
     c.small_density = 1e-12

@@ -51,6 +51,7 @@ def spec_of(s: br.Setup) -> dict:
                 limiter=s.limiter, solver=s.solver, stepping=s.stepping, ct=s.ct, emf=s.emf,
                 bc=s.bc, cfl=s.cfl, first_dt=s.first_dt, steps=s.steps,
                 internal_boundary=s.internal_boundary,
+                char_limiting=s.char_limiting,
                 params=s.params)
 
 
@@ -202,6 +203,16 @@ def setups():
                 bc="outflow", name="blast_chtr_outflow_16"),
         replace(br.blast_setup(16, 12), stepping="CHARACTERISTIC_TRACING", ct=False, name="blast_chtr_noct_16"),
         replace(br.blast_setup(16, 12), stepping="HANCOCK", ct=False, name="blast_ctu_noct_16"),
+        # CHAR_LIMITING YES (limiting in characteristic variables, plm_states.c:446-705)
+        replace(br.ot_setup("hlld", 32, 30), char_limiting=True, name="ot_charlim_32"),
+        replace(br.blast_setup(16, 12), char_limiting=True, limiter="DEFAULT", name="blast_charlim_default_16"),
+        replace(br.tube_setup(1, 200, 120), char_limiting=True, limiter="MINMOD_LIM", name="tube_charlim_1_200"),
+        replace(br.cpa_setup(32, 20), char_limiting=True, limiter="VANLEER_LIM", stepping="RK3",
+                name="cpa_charlim_rk3_32"),
+        replace(br.ot_setup("hlld", 32, 30), char_limiting=True, stepping="CHARACTERISTIC_TRACING",
+                emf="UCT_CONTACT", name="ot_chtr_charlim_32"),
+        replace(br.blast_setup(16, 12), char_limiting=True, stepping="HANCOCK", emf="ARITHMETIC",
+                name="blast_ctu_charlim_16"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

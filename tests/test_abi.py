@@ -40,7 +40,7 @@ def test_every_declared_symbol_is_exported(lib):
 
 def test_abi_version(lib):
     from pluto_gb300 import _lib as L
-    assert lib.pg_abi_version() == L.PG_ABI_VERSION == 2
+    assert lib.pg_abi_version() == L.PG_ABI_VERSION == 3
 
 
 @pytest.mark.parametrize("field,value", [("dims", 4), ("components", 1), ("gamma", 1.0),
@@ -84,6 +84,25 @@ def test_char_tracing_validation(lib, extra, ok):
     spec.update(extra)
     h = C.c_void_p()
     rc = lib.pg_create(C.byref(make_config(spec, precision)), C.byref(h))
+    assert (rc != 1) == ok, lib.pg_last_error()
+    if rc == 0:
+        lib.pg_destroy(h)
+
+
+@pytest.mark.parametrize("extra,precision,ok", [({}, "fp64", True), ({"recon": "PARABOLIC"}, "fp64", False),
+                                                 ({}, "mixed", False), ({}, "fp64_tangent", False),
+                                                 ({"stepping": "HANCOCK"}, "fp64", True),
+                                                 ({"char_limiting": 2}, "fp64", False)])
+def test_char_limiting_validation(lib, extra, precision, ok):
+    """CHAR_LIMITING YES: linear reconstruction on the plain FP64 path."""
+    spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1), gamma=5 / 3, ct=False,
+                char_limiting=True)
+    spec.update(extra)
+    c = make_config(spec, precision)
+    if extra.get("char_limiting") == 2:
+        c.char_limiting = 2
+    h = C.c_void_p()
+    rc = lib.pg_create(C.byref(c), C.byref(h))
     assert (rc != 1) == ok, lib.pg_last_error()
     if rc == 0:
         lib.pg_destroy(h)

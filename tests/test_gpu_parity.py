@@ -56,7 +56,9 @@ def test_fp64_matches_reference_goldens(name):
                                   "ot_euler_32", "tube_euler_0_256", "ot_internal_32",
                                   "ot_chtr_uctc_32", "ot_chtr_arith_roe_32", "cpa_chtr_32", "turb_chtr_12",
                                   "tube_chtr_1_200", "blast_chtr_outflow_16", "blast_chtr_noct_16",
-                                  "blast_ctu_noct_16"])
+                                  "blast_ctu_noct_16", "ot_charlim_32", "blast_charlim_default_16",
+                                  "tube_charlim_1_200", "cpa_charlim_rk3_32", "ot_chtr_charlim_32",
+                                  "blast_ctu_charlim_16"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
@@ -252,6 +254,30 @@ def test_char_tracing_vs_oracle_random_3d(emf, solver, bc):
     assert np.array_equal(a, b), _errors(a, ab, b, bb)
     for d in range(3):
         assert np.array_equal(ab[d], bb[d])
+
+
+@pytest.mark.parametrize("limiter,stepping,extra", [("MC_LIM", "RK2", {}), ("DEFAULT", "RK3", {}),
+                                                    ("MINMOD_LIM", "RK2", {"ct": False}),
+                                                    ("VANLEER_LIM", "CHARACTERISTIC_TRACING",
+                                                     {"emf": "UCT_CONTACT", "bc": "outflow"}),
+                                                    ("DEFAULT", "HANCOCK", {"emf": "ARITHMETIC"})])
+def test_char_limiting_vs_oracle_random_3d(limiter, stepping, extra):
+    """CHAR_LIMITING YES on a random 3D state against the oracle, bit for bit."""
+    from oracle.oracle import Oracle
+    spec, vc, bs = _random_blast(16, seed=21)
+    spec.update(char_limiting=True, limiter=limiter, stepping=stepping, **extra)
+    s = _solver(spec)
+    o = Oracle(spec, nthreads=4)
+    s.upload(vc, bs)
+    o.set_state(vc, bs)
+    s.run(4, 1e-3, 0.3)
+    o.run(4, 1e-3, 0.3)
+    a, ab = s.download()
+    b, bb = o.get_state()
+    assert np.array_equal(a, b), _errors(a, ab, b, bb)
+    if spec.get("ct", True):
+        for d in range(3):
+            assert np.array_equal(ab[d], bb[d])
 
 
 def test_char_tracing_without_ct_vs_oracle_3d():
