@@ -1544,6 +1544,57 @@ static void plm_char_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV],
   }
 }
 
+
+/* CharTracingStep for parabolic states, Src/States/char_tracing.c:46-279
+   (CHTR_REF_STATE 3 without CHAR_LIMITING, uniform Cartesian grid, no passive
+   scalars): the PPM reference state of the fastest wave towards each
+   interface, then each family's parabola integrated over its domain of
+   dependence added on the side it reaches; PrimSource zero (+0). */
+static void char_tracing_ppm(const double *vc, double *vp, double *vm, double gamma, double dtdx, double dt,
+                             const Rot *r, int c3, int dims) {
+  double L[8][8], R[8][8], lambda[8], nu[8], dvp[NV], dvm[NV], dwp[8], dwm[8], nup, num, dwh, d2w;
+  const int nflx = c3 ? 8 : 6;
+  const double a2 = gamma * vc[PRS] / vc[RHO];
+  const double src = 0.0;
+  int k, nv;
+  prim_eigen(vc, a2, r, c3, dims, L, R, lambda);
+  for (k = 0; k < nflx; k++) nu[k] = dtdx * lambda[k];
+  for (nv = NV; nv--;) {
+    dvp[nv] = vp[nv] - vc[nv];
+    dvm[nv] = vm[nv] - vc[nv];
+  }
+  prim_to_char(L, dvp, r, c3, dwp);
+  prim_to_char(L, dvm, r, c3, dwm);
+  nup = MAX(nu[1], 0.0);
+  num = MIN(nu[0], 0.0);
+  for (nv = NV; nv--;) {
+    if (!c3 && (nv == VX3 || nv == BX3)) continue;
+    dwh = vp[nv] - vm[nv];
+    d2w = vp[nv] + vm[nv] - 2.0 * vc[nv];
+    vp[nv] -= 0.5 * nup * (dwh + d2w * (3.0 - 2.0 * nup));
+    vm[nv] -= 0.5 * num * (dwh - d2w * (3.0 + 2.0 * num));
+  }
+  for (k = 0; k < nflx; k++) {
+    dwh = dwp[k] - dwm[k];
+    d2w = dwp[k] + dwm[k];
+    if (nu[k] >= 0.0) {
+      double Spp = -0.5 * (nu[k] - nup) * (dwh + 3.0 * d2w) + (nu[k] * nu[k] - nup * nup) * d2w;
+      for (nv = NV; nv--;)
+        if (c3 || (nv != VX3 && nv != BX3)) vp[nv] += Spp * R[nv][k];
+    } else {
+      double Smm = -0.5 * (nu[k] - num) * (dwh - 3.0 * d2w) + (nu[k] * nu[k] - num * num) * d2w;
+      for (nv = NV; nv--;)
+        if (c3 || (nv != VX3 && nv != BX3)) vm[nv] += Smm * R[nv][k];
+    }
+  }
+  for (nv = NV; nv--;) {
+    if (!c3 && (nv == VX3 || nv == BX3)) continue;
+    dwh = 0.5 * dt * src;
+    vp[nv] += dwh;
+    vm[nv] += dwh;
+  }
+}
+
 /* face-EMF slot of (dir, component): ezi, ezj, eyi, eyk, exj, exk */
 enum { EZI = 0, EZJ, EYI, EYK, EXJ, EXK };
 
@@ -1600,7 +1651,9 @@ static void ctu_sweep(oc_problem *p, int dir, double dt, int stage, double *inv_
         if (ct) w.bn[i] = p->bs[dir][FI(p, dir, ijk[2], ijk[1], ijk[0])];
       }
       if (stage == 1) {
-        if (p->c.char_limiting)
+        if (p->c.recon == OC_PARABOLIC)
+          ppm_states(w.v, w.vp, w.vm, nbeg - 1, nend + 1);
+        else if (p->c.char_limiting)
           plm_char_states(w.v, w.vp, w.vm, nbeg - 1, nend + 1, p->c.limiter, p->c.gamma, &r, c3, dims);
         else
           plm_states(w.v, w.vp, w.vm, nbeg - 1, nend + 1, p->c.limiter);
@@ -1611,7 +1664,10 @@ static void ctu_sweep(oc_problem *p, int dir, double dt, int stage, double *inv_
           }
         if (p->c.stepping == OC_CHARTR) { /* CharTracingStep, then its face field */
           for (i = nbeg - 1; i <= nend + 1; i++)
-            char_tracing(w.v[i], w.vp[i], w.vm[i], p->c.gamma, dt / dxd, dt, &r, c3, dims);
+            if (p->c.recon == OC_PARABOLIC)
+              char_tracing_ppm(w.v[i], w.vp[i], w.vm[i], p->c.gamma, dt / dxd, dt, &r, c3, dims);
+            else
+              char_tracing(w.v[i], w.vp[i], w.vm[i], p->c.gamma, dt / dxd, dt, &r, c3, dims);
           if (ct)
             for (i = nbeg - 2; i <= nend + 1; i++) {
               w.vp[i][r.bn] = w.bn[i];
@@ -2112,7 +2168,8 @@ oc_problem *oc_create(const oc_config *cfg) {
   if (cfg->char_limiting && cfg->recon != OC_LINEAR) { free(p); return NULL; } /* PPM form not restated */
   p->ng = cfg->recon == OC_PARABOLIC ? 3 : 2; /* Src/get_nghost.c:28-104 */
   if (IS_CTU(cfg->stepping)) {
-    if (cfg->recon != OC_LINEAR) { free(p); return NULL; } /* hancock.c:64-67 */
+    /* hancock.c:64-67; characteristic tracing takes parabolic states too */
+    if (cfg->recon != OC_LINEAR && cfg->stepping != OC_CHARTR) { free(p); return NULL; }
     if (cfg->ct && cfg->emf != OC_ARITHMETIC && cfg->emf != OC_UCT_CONTACT) { free(p); return NULL; }
     if (cfg->ct) p->ng++;                                    /* get_nghost.c:84-90 */
   }

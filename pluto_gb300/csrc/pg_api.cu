@@ -68,10 +68,10 @@ int validate_config(const pg_config* c) {
       !is_ctu(c->time_stepping))
     return fail(PG_ERR_INVALID, "unsupported time stepping");
   if (is_ctu(c->time_stepping)) {
-    // Src/States/hancock.c:64-67; char_tracing.c traces linear states only
-    // (the PARABOLIC form is not restated)
-    if (c->reconstruction != PG_LINEAR)
-      return fail(PG_ERR_INVALID, "the CTU predictors need linear reconstruction");
+    // Src/States/hancock.c:64-67: the Hancock predictor takes linear states;
+    // characteristic tracing takes linear or parabolic ones
+    if (c->reconstruction != PG_LINEAR && c->time_stepping != PG_CHAR_TRACING)
+      return fail(PG_ERR_INVALID, "the MUSCL-Hancock predictor needs linear reconstruction");
     if (c->precision != PG_FP64 && c->precision != PG_FP64_TANGENT)
       return fail(PG_ERR_INVALID, "CTU runs on the FP64 path");
     if (c->time_stepping == PG_CHAR_TRACING && c->precision != PG_FP64)

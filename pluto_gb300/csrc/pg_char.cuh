@@ -282,4 +282,58 @@ __device__ __forceinline__ void char_tracing(const double* vc, double* vp, doubl
   }
 }
 
+
+// CharTracingStep for parabolic states (Src/States/char_tracing.c:46-279;
+// CHTR_REF_STATE 3 without CHAR_LIMITING, uniform Cartesian grid): the PPM
+// reference state of the fastest wave towards each interface, then each
+// family's parabola averaged over its domain of dependence added on the side
+// it reaches; PrimSource is zero (+0).
+template <int DIR>
+__device__ __forceinline__ void char_tracing_ppm(const double* vc, double* vp, double* vm, double gamma,
+                                                 double dtdx, double dt, bool c3, int dims) {
+  double L[8][8], R[8][8], lambda[8], nu[8], dvp[8], dvm[8], dwp[8], dwm[8];
+  const double a2 = gamma * vc[PRS] / vc[RHO];  // SoundSpeed2, Src/EOS/Ideal/eos.c:33
+  prim_eigen<DIR>(vc, a2, c3, dims, L, R, lambda);
+  const int nflx = c3 ? 8 : 6;
+#pragma unroll
+  for (int k = 0; k < 8; k++) nu[k] = dtdx * lambda[k];
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    dvp[v] = vp[v] - vc[v];
+    dvm[v] = vm[v] - vc[v];
+  }
+  prim_to_char<DIR>(L, dvp, c3, dwp);
+  prim_to_char<DIR>(L, dvm, c3, dwm);
+  const double nup = pmax(nu[1], 0.0), num = pmin(nu[0], 0.0);
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    if (!c3 && (v == VX3 || v == BX3)) continue;
+    const double dwh = vp[v] - vm[v], d2w = vp[v] + vm[v] - 2.0 * vc[v];
+    vp[v] -= 0.5 * nup * (dwh + d2w * (3.0 - 2.0 * nup));
+    vm[v] -= 0.5 * num * (dwh - d2w * (3.0 + 2.0 * num));
+  }
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    if (k >= nflx) break;
+    const double dwh = dwp[k] - dwm[k], d2w = dwp[k] + dwm[k];
+    const bool right = nu[k] >= 0.0;
+    const double S = right ? -0.5 * (nu[k] - nup) * (dwh + 3.0 * d2w) + (nu[k] * nu[k] - nup * nup) * d2w
+                           : -0.5 * (nu[k] - num) * (dwh - 3.0 * d2w) + (nu[k] * nu[k] - num * num) * d2w;
+#pragma unroll
+    for (int v = 0; v < 8; v++) {
+      if (!c3 && (v == VX3 || v == BX3)) continue;
+      if (right) vp[v] += S * R[v][k];
+      else vm[v] += S * R[v][k];
+    }
+  }
+  const double src = 0.0;
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    if (!c3 && (v == VX3 || v == BX3)) continue;
+    const double dwh = 0.5 * dt * src;
+    vp[v] += dwh;
+    vm[v] += dwh;
+  }
+}
+
 }  // namespace pg

@@ -87,7 +87,19 @@ __global__ void k_ctu_states(F64A<T> a, Box box) {
       limited = true;
     }
   }
-  if (!limited) {
+  if (!limited && a.recon == PG_PARABOLIC) {  // PPM states (ppm_states.c:68-253), then CharTracingStep
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) {
+      const T* V = a.V[nv];
+      const T w2 = V[c - 2 * s], w1 = V[c - s], e1 = V[c + s], e2 = V[c + 2 * s];
+      v0[nv] = V[c];
+      T p = ppm_iface(w1, v0[nv], e1, e2);  // interface c+1/2
+      T m = ppm_iface(w2, w1, v0[nv], e1);  // interface c-1/2
+      ppm_limit(v0[nv], p, m);
+      vp[nv] = p;
+      vm[nv] = m;
+    }
+  } else if (!limited) {
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
       const T* V = a.V[nv];
@@ -106,7 +118,10 @@ __global__ void k_ctu_states(F64A<T> a, Box box) {
   bool traced = false;
   if constexpr (std::is_same<T, double>::value) {
     if (a.chtr) {  // characteristic tracing, then the face field again (char_tracing.c:536-540)
-      char_tracing<DIR>(v0, vp, vm, a.gamma, a.sc->dt / g.dx[DIR], a.sc->dt, a.c3 != 0, g.dims);
+      if (a.recon == PG_PARABOLIC)
+        char_tracing_ppm<DIR>(v0, vp, vm, a.gamma, a.sc->dt / g.dx[DIR], a.sc->dt, a.c3 != 0, g.dims);
+      else
+        char_tracing<DIR>(v0, vp, vm, a.gamma, a.sc->dt / g.dx[DIR], a.sc->dt, a.c3 != 0, g.dims);
       if (a.ct) {
         vp[R::bn] = a.Bs[DIR][c];
         vm[R::bn] = a.Bs[DIR][c - s];

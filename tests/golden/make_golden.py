@@ -213,6 +213,17 @@ def setups():
                 emf="UCT_CONTACT", name="ot_chtr_charlim_32"),
         replace(br.blast_setup(16, 12), char_limiting=True, stepping="HANCOCK", emf="ARITHMETIC",
                 name="blast_ctu_charlim_16"),
+        # PARABOLIC + CHARACTERISTIC_TRACING (CTU-PPM, char_tracing.c:46-279)
+        replace(br.ot_setup("hlld", 32, 30), recon="PARABOLIC", stepping="CHARACTERISTIC_TRACING",
+                emf="UCT_CONTACT", name="ot_ppm_chtr_32"),
+        replace(br.turb_setup(12, 10), stepping="CHARACTERISTIC_TRACING", emf="UCT_CONTACT",
+                name="turb_ppm_chtr_12"),
+        replace(br.tube_setup(1, 200, 120), recon="PARABOLIC", stepping="CHARACTERISTIC_TRACING",
+                name="tube_ppm_chtr_1_200"),
+        replace(br.cpa_setup(32, 20), recon="PARABOLIC", stepping="CHARACTERISTIC_TRACING", emf="ARITHMETIC",
+                solver="roe", bc="outflow", name="cpa_ppm_chtr_roe_32"),
+        replace(br.blast_setup(16, 12), recon="PARABOLIC", stepping="CHARACTERISTIC_TRACING", ct=False,
+                name="blast_ppm_chtr_noct_16"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

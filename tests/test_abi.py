@@ -69,14 +69,16 @@ def test_ct_requires_2d_and_accepts_outflow(lib):
         lib.pg_destroy(h)
 
 
-@pytest.mark.parametrize("extra,ok", [({}, True), ({"recon": "PARABOLIC"}, False),
+@pytest.mark.parametrize("extra,ok", [({}, True), ({"recon": "PARABOLIC"}, True),
+                                      ({"recon": "PARABOLIC", "stepping": "HANCOCK"}, False),
                                       ({"precision": "mixed"}, False), ({"precision": "fp64_tangent"}, False),
                                       ({"ct": True, "emf": "UCT_HLL"}, False),
                                       ({"ct": True, "emf": "UCT_CONTACT"}, True),
                                       ({"ct": True, "emf": "ARITHMETIC"}, True)])
 def test_char_tracing_validation(lib, extra, ok):
-    """TIME_STEPPING CHARACTERISTIC_TRACING: linear reconstruction, the plain
-    FP64 path, and under CT the ARITHMETIC or UCT_CONTACT emf average."""
+    """TIME_STEPPING CHARACTERISTIC_TRACING: linear or parabolic states (the
+    Hancock predictor: linear only), the plain FP64 path, and under CT the
+    ARITHMETIC or UCT_CONTACT emf average."""
     extra = dict(extra)
     precision = extra.pop("precision", "fp64")
     spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1), gamma=5 / 3, ct=False,

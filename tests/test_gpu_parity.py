@@ -58,7 +58,8 @@ def test_fp64_matches_reference_goldens(name):
                                   "tube_chtr_1_200", "blast_chtr_outflow_16", "blast_chtr_noct_16",
                                   "blast_ctu_noct_16", "ot_charlim_32", "blast_charlim_default_16",
                                   "tube_charlim_1_200", "cpa_charlim_rk3_32", "ot_chtr_charlim_32",
-                                  "blast_ctu_charlim_16"])
+                                  "blast_ctu_charlim_16", "ot_ppm_chtr_32", "turb_ppm_chtr_12",
+                                  "tube_ppm_chtr_1_200", "cpa_ppm_chtr_roe_32", "blast_ppm_chtr_noct_16"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
@@ -278,6 +279,28 @@ def test_char_limiting_vs_oracle_random_3d(limiter, stepping, extra):
     if spec.get("ct", True):
         for d in range(3):
             assert np.array_equal(ab[d], bb[d])
+
+
+@pytest.mark.parametrize("emf,solver,bc", [("UCT_CONTACT", "hlld", "periodic"), ("ARITHMETIC", "hll", "outflow"),
+                                           ("UCT_CONTACT", "roe", [("reflective", "outflow"), "periodic",
+                                                                   ("eqtsymmetric", "outflow")])])
+def test_ppm_char_tracing_vs_oracle_random_3d(emf, solver, bc):
+    """CTU with parabolic states and characteristic tracing on a random 3D
+    state against the oracle, bit for bit."""
+    from oracle.oracle import Oracle
+    spec, vc, bs = _random_blast(16, seed=31)
+    spec.update(recon="PARABOLIC", stepping="CHARACTERISTIC_TRACING", emf=emf, solver=solver, bc=bc)
+    s = _solver(spec)
+    o = Oracle(spec, nthreads=4)
+    s.upload(vc, bs)
+    o.set_state(vc, bs)
+    s.run(4, 1e-3, 0.3)
+    o.run(4, 1e-3, 0.3)
+    a, ab = s.download()
+    b, bb = o.get_state()
+    assert np.array_equal(a, b), _errors(a, ab, b, bb)
+    for d in range(3):
+        assert np.array_equal(ab[d], bb[d])
 
 
 def test_char_tracing_without_ct_vs_oracle_3d():
