@@ -86,9 +86,9 @@ typedef struct {
   int bc_hi[3];         /* type of the end side (X*_END) when bc_sides is 1 */
   int bc_sides;         /* 0: bc[d] on both sides; 1: bc[d] / bc_hi[d] per side
                            (PERIODIC must then be on both sides of an axis) */
-  int char_limiting;    /* CHAR_LIMITING YES: PLM slopes limited in characteristic
-                           variables (Src/States/plm_states.c:446-705); LINEAR
-                           reconstruction, PG_FP64 solvers (RK and CTU) */
+  int char_limiting;    /* CHAR_LIMITING YES: states limited in characteristic
+                           variables (Src/States/plm_states.c:446-705,
+                           ppm_states.c:258-560); PG_FP64 solvers (RK and CTU) */
 } pg_config;
 
 typedef struct {

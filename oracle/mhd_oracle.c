@@ -916,6 +916,8 @@ static void pencil_free(Pencil *w) {
 
 static void plm_char_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV], int beg, int end, int lim,
                             double gamma, const Rot *r, int c3, int dims);
+static void ppm_char_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV], int beg, int end, double gamma,
+                            const Rot *r, int c3, int dims);
 
 static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1d,
                   double *mach_out) {
@@ -962,6 +964,8 @@ static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1
         int beg = nbeg - 1, end = nend + 1;
         if (p->c.recon == OC_LINEAR && p->c.char_limiting)
           plm_char_states(w.v, w.vp, w.vm, beg, end, p->c.limiter, p->c.gamma, &r, p->c.components == 3, dims);
+        else if (p->c.char_limiting)
+          ppm_char_states(w.v, w.vp, w.vm, beg, end, p->c.gamma, &r, p->c.components == 3, dims);
         else if (p->c.recon == OC_LINEAR) plm_states(w.v, w.vp, w.vm, beg, end, p->c.limiter);
         else ppm_states(w.v, w.vp, w.vm, beg, end);
         if (p->c.ct) { /* plm_states.c:271-275 */
@@ -1551,7 +1555,7 @@ static void plm_char_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV],
    interface, then each family's parabola integrated over its domain of
    dependence added on the side it reaches; PrimSource zero (+0). */
 static void char_tracing_ppm(const double *vc, double *vp, double *vm, double gamma, double dtdx, double dt,
-                             const Rot *r, int c3, int dims) {
+                             const Rot *r, int c3, int dims, int ref_state) {
   double L[8][8], R[8][8], lambda[8], nu[8], dvp[NV], dvm[NV], dwp[8], dwm[8], nup, num, dwh, d2w;
   const int nflx = c3 ? 8 : 6;
   const double a2 = gamma * vc[PRS] / vc[RHO];
@@ -1568,7 +1572,7 @@ static void char_tracing_ppm(const double *vc, double *vp, double *vm, double ga
   nup = MAX(nu[1], 0.0);
   num = MIN(nu[0], 0.0);
   for (nv = NV; nv--;) {
-    if (!c3 && (nv == VX3 || nv == BX3)) continue;
+    if (ref_state != 3 || (!c3 && (nv == VX3 || nv == BX3))) continue;
     dwh = vp[nv] - vm[nv];
     d2w = vp[nv] + vm[nv] - 2.0 * vc[nv];
     vp[nv] -= 0.5 * nup * (dwh + d2w * (3.0 - 2.0 * nup));
@@ -1578,11 +1582,13 @@ static void char_tracing_ppm(const double *vc, double *vp, double *vm, double ga
     dwh = dwp[k] - dwm[k];
     d2w = dwp[k] + dwm[k];
     if (nu[k] >= 0.0) {
-      double Spp = -0.5 * (nu[k] - nup) * (dwh + 3.0 * d2w) + (nu[k] * nu[k] - nup * nup) * d2w;
+      double Spp = ref_state == 3 ? -0.5 * (nu[k] - nup) * (dwh + 3.0 * d2w) + (nu[k] * nu[k] - nup * nup) * d2w
+                                  : -0.5 * nu[k] * (dwh + d2w * (3.0 - 2.0 * nu[k]));
       for (nv = NV; nv--;)
         if (c3 || (nv != VX3 && nv != BX3)) vp[nv] += Spp * R[nv][k];
     } else {
-      double Smm = -0.5 * (nu[k] - num) * (dwh - 3.0 * d2w) + (nu[k] * nu[k] - num * num) * d2w;
+      double Smm = ref_state == 3 ? -0.5 * (nu[k] - num) * (dwh - 3.0 * d2w) + (nu[k] * nu[k] - num * num) * d2w
+                                  : -0.5 * nu[k] * (dwh - d2w * (3.0 + 2.0 * nu[k]));
       for (nv = NV; nv--;)
         if (c3 || (nv != VX3 && nv != BX3)) vm[nv] += Smm * R[nv][k];
     }
@@ -1592,6 +1598,74 @@ static void char_tracing_ppm(const double *vc, double *vp, double *vm, double ga
     dwh = 0.5 * dt * src;
     vp[nv] += dwh;
     vm[nv] += dwh;
+  }
+}
+
+
+/* States with RECONSTRUCTION PARABOLIC and CHAR_LIMITING YES,
+   Src/States/ppm_states.c:258-560 (PPM_ORDER 4, PARABOLIC_LIM 1, uniform
+   Cartesian coefficients: hp = hm = 3, so cp = cm = 2): the unlimited
+   fourth-order interface values projected on the left eigenvectors and
+   clipped by MINMOD against the projected neighbour differences, summed back
+   over the right eigenvectors, the parabolic limiter on the primitive
+   increments, and linear density / pressure where a state came out negative. */
+static void ppm_char_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV], int beg, int end, double gamma,
+                            const Rot *r, int c3, int dims) {
+  const double w_1 = -1.0 / 12.0, w0 = 7.0 / 12.0, w1 = 7.0 / 12.0, w2 = -1.0 / 12.0;
+  const double hp = 3.0, hm = 3.0;
+  const int nflx = c3 ? 8 : 6;
+  int i, k, nv;
+  for (i = beg; i <= end; i++) {
+    double L[8][8], R[8][8], lambda[8], dvp[NV], dvm[NV], dvF0[NV], dvF1[NV];
+    double dwp[8], dwm[8], dwp1[8], dwm1[8], cp, cm;
+    const double a2 = gamma * v[i][PRS] / v[i][RHO]; /* SoundSpeed2 */
+    prim_eigen(v[i], a2, r, c3, dims, L, R, lambda);
+    for (nv = 0; nv < NV; nv++) {
+      double ip = w_1 * v[i - 1][nv] + w0 * v[i][nv] + w1 * v[i + 1][nv] + w2 * v[i + 2][nv];
+      double im = w_1 * v[i - 2][nv] + w0 * v[i - 1][nv] + w1 * v[i][nv] + w2 * v[i + 1][nv];
+      dvp[nv] = ip - v[i][nv];
+      dvm[nv] = im - v[i][nv];
+      dvF1[nv] = v[i + 1][nv] - v[i][nv];
+      dvF0[nv] = v[i][nv] - v[i - 1][nv];
+    }
+    prim_to_char(L, dvp, r, c3, dwp);
+    prim_to_char(L, dvm, r, c3, dwm);
+    prim_to_char(L, dvF0, r, c3, dwm1);
+    prim_to_char(L, dvF1, r, c3, dwp1);
+    for (k = 0; k < nflx; k++) {
+      dwp[k] = MINMOD(dwp[k], dwp1[k]);
+      dwm[k] = MINMOD(dwm[k], -dwm1[k]);
+    }
+    cm = (hm + 1.0) / (hp - 1.0);
+    cp = (hp + 1.0) / (hm - 1.0);
+    for (nv = 0; nv < NV; nv++) {
+      double dp = 0.0, dm = 0.0;
+      if (!c3 && (nv == VX3 || nv == BX3)) {
+        vp[i][nv] = vm[i][nv] = v[i][nv];
+        continue;
+      }
+      for (k = 0; k < nflx; k++) {
+        dp += dwp[k] * R[nv][k];
+        dm += dwm[k] * R[nv][k];
+      }
+      if (dp * dm >= 0.0) dp = dm = 0.0;
+      else {
+        if (fabs(dp) >= cm * fabs(dm)) dp = -cm * dm;
+        else if (fabs(dm) >= cp * fabs(dp)) dm = -cp * dp;
+      }
+      vp[i][nv] = v[i][nv] + dp;
+      vm[i][nv] = v[i][nv] + dm;
+    }
+    if (vp[i][RHO] < 0.0 || vm[i][RHO] < 0.0) {
+      double d = 0.5 * (MINMOD(dvF1[RHO], dvF0[RHO]));
+      vp[i][RHO] = v[i][RHO] + d;
+      vm[i][RHO] = v[i][RHO] + (-d);
+    }
+    if (vp[i][PRS] < 0.0 || vm[i][PRS] < 0.0) {
+      double d = 0.5 * (MINMOD(dvF1[PRS], dvF0[PRS]));
+      vp[i][PRS] = v[i][PRS] + d;
+      vm[i][PRS] = v[i][PRS] + (-d);
+    }
   }
 }
 
@@ -1651,7 +1725,9 @@ static void ctu_sweep(oc_problem *p, int dir, double dt, int stage, double *inv_
         if (ct) w.bn[i] = p->bs[dir][FI(p, dir, ijk[2], ijk[1], ijk[0])];
       }
       if (stage == 1) {
-        if (p->c.recon == OC_PARABOLIC)
+        if (p->c.recon == OC_PARABOLIC && p->c.char_limiting)
+          ppm_char_states(w.v, w.vp, w.vm, nbeg - 1, nend + 1, p->c.gamma, &r, c3, dims);
+        else if (p->c.recon == OC_PARABOLIC)
           ppm_states(w.v, w.vp, w.vm, nbeg - 1, nend + 1);
         else if (p->c.char_limiting)
           plm_char_states(w.v, w.vp, w.vm, nbeg - 1, nend + 1, p->c.limiter, p->c.gamma, &r, c3, dims);
@@ -1665,7 +1741,8 @@ static void ctu_sweep(oc_problem *p, int dir, double dt, int stage, double *inv_
         if (p->c.stepping == OC_CHARTR) { /* CharTracingStep, then its face field */
           for (i = nbeg - 1; i <= nend + 1; i++)
             if (p->c.recon == OC_PARABOLIC)
-              char_tracing_ppm(w.v[i], w.vp[i], w.vm[i], p->c.gamma, dt / dxd, dt, &r, c3, dims);
+              char_tracing_ppm(w.v[i], w.vp[i], w.vm[i], p->c.gamma, dt / dxd, dt, &r, c3, dims,
+                               p->c.char_limiting ? 2 : 3); /* char_tracing.c:35-43 */
             else
               char_tracing(w.v[i], w.vp[i], w.vm[i], p->c.gamma, dt / dxd, dt, &r, c3, dims);
           if (ct)
@@ -2165,7 +2242,6 @@ oc_problem *oc_create(const oc_config *cfg) {
     if (cfg->bc_hi[d] < OC_PERIODIC || cfg->bc_hi[d] > OC_USERDEF) { free(p); return NULL; }
     if ((cfg->bc[d] == OC_PERIODIC) != (cfg->bc_hi[d] == OC_PERIODIC)) { free(p); return NULL; }
   }
-  if (cfg->char_limiting && cfg->recon != OC_LINEAR) { free(p); return NULL; } /* PPM form not restated */
   p->ng = cfg->recon == OC_PARABOLIC ? 3 : 2; /* Src/get_nghost.c:28-104 */
   if (IS_CTU(cfg->stepping)) {
     /* hancock.c:64-67; characteristic tracing takes parabolic states too */

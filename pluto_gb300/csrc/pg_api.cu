@@ -94,8 +94,6 @@ int validate_config(const pg_config* c) {
     return fail(PG_ERR_INVALID, "unsupported precision");
   if (c->char_limiting != 0 && c->char_limiting != 1) return fail(PG_ERR_INVALID, "char_limiting is 0 or 1");
   if (c->char_limiting) {
-    if (c->reconstruction != PG_LINEAR)
-      return fail(PG_ERR_INVALID, "CHAR_LIMITING is implemented for linear reconstruction");
     if (c->precision != PG_FP64)
       return fail(PG_ERR_INVALID, "CHAR_LIMITING runs on the plain FP64 path (no mixed or tangent-linear form)");
   }

@@ -283,14 +283,15 @@ __device__ __forceinline__ void char_tracing(const double* vc, double* vp, doubl
 }
 
 
-// CharTracingStep for parabolic states (Src/States/char_tracing.c:46-279;
-// CHTR_REF_STATE 3 without CHAR_LIMITING, uniform Cartesian grid): the PPM
-// reference state of the fastest wave towards each interface, then each
-// family's parabola averaged over its domain of dependence added on the side
-// it reaches; PrimSource is zero (+0).
+// CharTracingStep for parabolic states (Src/States/char_tracing.c:46-279,
+// uniform Cartesian grid): with reference state 3 (no CHAR_LIMITING) the
+// states first move to the PPM reference state of the fastest wave towards
+// each interface; then (states 3 and 2) each family's parabola averaged over
+// its domain of dependence is added on the side it reaches; PrimSource is
+// zero (+0).
 template <int DIR>
 __device__ __forceinline__ void char_tracing_ppm(const double* vc, double* vp, double* vm, double gamma,
-                                                 double dtdx, double dt, bool c3, int dims) {
+                                                 double dtdx, double dt, bool c3, int dims, int ref_state) {
   double L[8][8], R[8][8], lambda[8], nu[8], dvp[8], dvm[8], dwp[8], dwm[8];
   const double a2 = gamma * vc[PRS] / vc[RHO];  // SoundSpeed2, Src/EOS/Ideal/eos.c:33
   prim_eigen<DIR>(vc, a2, c3, dims, L, R, lambda);
@@ -307,7 +308,7 @@ __device__ __forceinline__ void char_tracing_ppm(const double* vc, double* vp, d
   const double nup = pmax(nu[1], 0.0), num = pmin(nu[0], 0.0);
 #pragma unroll
   for (int v = 0; v < 8; v++) {
-    if (!c3 && (v == VX3 || v == BX3)) continue;
+    if (ref_state != 3 || (!c3 && (v == VX3 || v == BX3))) continue;
     const double dwh = vp[v] - vm[v], d2w = vp[v] + vm[v] - 2.0 * vc[v];
     vp[v] -= 0.5 * nup * (dwh + d2w * (3.0 - 2.0 * nup));
     vm[v] -= 0.5 * num * (dwh - d2w * (3.0 + 2.0 * num));
@@ -317,8 +318,12 @@ __device__ __forceinline__ void char_tracing_ppm(const double* vc, double* vp, d
     if (k >= nflx) break;
     const double dwh = dwp[k] - dwm[k], d2w = dwp[k] + dwm[k];
     const bool right = nu[k] >= 0.0;
-    const double S = right ? -0.5 * (nu[k] - nup) * (dwh + 3.0 * d2w) + (nu[k] * nu[k] - nup * nup) * d2w
-                           : -0.5 * (nu[k] - num) * (dwh - 3.0 * d2w) + (nu[k] * nu[k] - num * num) * d2w;
+    double S;
+    if (ref_state == 3)
+      S = right ? -0.5 * (nu[k] - nup) * (dwh + 3.0 * d2w) + (nu[k] * nu[k] - nup * nup) * d2w
+                : -0.5 * (nu[k] - num) * (dwh - 3.0 * d2w) + (nu[k] * nu[k] - num * num) * d2w;
+    else  // reference state 2 (with CHAR_LIMITING, char_tracing.c:35-43)
+      S = right ? -0.5 * nu[k] * (dwh + d2w * (3.0 - 2.0 * nu[k])) : -0.5 * nu[k] * (dwh - d2w * (3.0 + 2.0 * nu[k]));
 #pragma unroll
     for (int v = 0; v < 8; v++) {
       if (!c3 && (v == VX3 || v == BX3)) continue;
@@ -333,6 +338,76 @@ __device__ __forceinline__ void char_tracing_ppm(const double* vc, double* vp, d
     const double dwh = 0.5 * dt * src;
     vp[v] += dwh;
     vm[v] += dwh;
+  }
+}
+
+
+// States with RECONSTRUCTION PARABOLIC and CHAR_LIMITING YES
+// (Src/States/ppm_states.c:258-560; PPM_ORDER 4, PARABOLIC_LIM 1, uniform
+// Cartesian: hp = hm = 3, cp = cm = 2) for the zone v0 with neighbours
+// w2 w1 | e1 e2 along DIR: the unlimited interface values projected on the
+// left eigenvectors and clipped by MINMOD against the projected neighbour
+// differences, summed back over the right eigenvectors in wave order, the
+// parabolic limiter on the primitive increments, and linear density /
+// pressure where a state came out negative.
+template <int DIR>
+__device__ __forceinline__ void ppm_char(const double* w2, const double* w1, const double* v0, const double* e1,
+                                         const double* e2, double gamma, bool c3, int dims, double* vp, double* vm) {
+  const double q_1 = -1.0 / 12.0, q0 = 7.0 / 12.0, q1 = 7.0 / 12.0, q2 = -1.0 / 12.0;
+  double L[8][8], R[8][8], lambda[8], dvp[8], dvm[8], dvF0[8], dvF1[8], dwp[8], dwm[8], dwp1[8], dwm1[8];
+  const double a2 = gamma * v0[PRS] / v0[RHO];  // SoundSpeed2
+  prim_eigen<DIR>(v0, a2, c3, dims, L, R, lambda);
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    const double ip = q_1 * w1[v] + q0 * v0[v] + q1 * e1[v] + q2 * e2[v];
+    const double im = q_1 * w2[v] + q0 * w1[v] + q1 * v0[v] + q2 * e1[v];
+    dvp[v] = ip - v0[v];
+    dvm[v] = im - v0[v];
+    dvF1[v] = e1[v] - v0[v];
+    dvF0[v] = v0[v] - w1[v];
+  }
+  prim_to_char<DIR>(L, dvp, c3, dwp);
+  prim_to_char<DIR>(L, dvm, c3, dwm);
+  prim_to_char<DIR>(L, dvF0, c3, dwm1);
+  prim_to_char<DIR>(L, dvF1, c3, dwp1);
+  const int nflx = c3 ? 8 : 6;
+#pragma unroll
+  for (int k = 0; k < 8; k++) {
+    dwp[k] = minmod(dwp[k], dwp1[k]);
+    dwm[k] = minmod(dwm[k], -dwm1[k]);
+  }
+  const double cm = (3.0 + 1.0) / (3.0 - 1.0), cp = (3.0 + 1.0) / (3.0 - 1.0);
+#pragma unroll
+  for (int v = 0; v < 8; v++) {
+    if (!c3 && (v == VX3 || v == BX3)) {
+      vp[v] = vm[v] = v0[v];
+      continue;
+    }
+    double dp = 0.0, dm = 0.0;
+#pragma unroll
+    for (int k = 0; k < 8; k++)
+      if (k < nflx) {
+        dp += dwp[k] * R[v][k];
+        dm += dwm[k] * R[v][k];
+      }
+    if (dp * dm >= 0.0) {
+      dp = dm = 0.0;
+    } else {
+      if (::fabs(dp) >= cm * ::fabs(dm)) dp = -cm * dm;
+      else if (::fabs(dm) >= cp * ::fabs(dp)) dm = -cp * dp;
+    }
+    vp[v] = v0[v] + dp;
+    vm[v] = v0[v] + dm;
+  }
+  if (vp[RHO] < 0.0 || vm[RHO] < 0.0) {
+    const double d = 0.5 * (minmod(dvF1[RHO], dvF0[RHO]));
+    vp[RHO] = v0[RHO] + d;
+    vm[RHO] = v0[RHO] + (-d);
+  }
+  if (vp[PRS] < 0.0 || vm[PRS] < 0.0) {
+    const double d = 0.5 * (minmod(dvF1[PRS], dvF0[PRS]));
+    vp[PRS] = v0[PRS] + d;
+    vm[PRS] = v0[PRS] + (-d);
   }
 }
 

@@ -75,7 +75,19 @@ __global__ void k_ctu_states(F64A<T> a, Box box) {
   T v0[NV], vp[NV], vm[NV];
   bool limited = false;
   if constexpr (std::is_same<T, double>::value) {
-    if (a.char_lim) {  // CHAR_LIMITING YES, plm_states.c:446-705
+    if (a.char_lim && a.recon == PG_PARABOLIC) {  // CHAR_LIMITING YES, ppm_states.c:258-560
+      double w2[NV], w1[NV], e1[NV], e2[NV];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        w2[nv] = a.V[nv][c - 2 * s];
+        w1[nv] = a.V[nv][c - s];
+        v0[nv] = a.V[nv][c];
+        e1[nv] = a.V[nv][c + s];
+        e2[nv] = a.V[nv][c + 2 * s];
+      }
+      ppm_char<DIR>(w2, w1, v0, e1, e2, a.gamma, a.c3 != 0, g.dims, vp, vm);
+      limited = true;
+    } else if (a.char_lim) {  // CHAR_LIMITING YES, plm_states.c:446-705
       double vl[NV], vr[NV];
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) {
@@ -119,7 +131,8 @@ __global__ void k_ctu_states(F64A<T> a, Box box) {
   if constexpr (std::is_same<T, double>::value) {
     if (a.chtr) {  // characteristic tracing, then the face field again (char_tracing.c:536-540)
       if (a.recon == PG_PARABOLIC)
-        char_tracing_ppm<DIR>(v0, vp, vm, a.gamma, a.sc->dt / g.dx[DIR], a.sc->dt, a.c3 != 0, g.dims);
+        char_tracing_ppm<DIR>(v0, vp, vm, a.gamma, a.sc->dt / g.dx[DIR], a.sc->dt, a.c3 != 0, g.dims,
+                              a.char_lim ? 2 : 3);
       else
         char_tracing<DIR>(v0, vp, vm, a.gamma, a.sc->dt / g.dx[DIR], a.sc->dt, a.c3 != 0, g.dims);
       if (a.ct) {

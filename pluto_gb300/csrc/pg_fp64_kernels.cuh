@@ -180,7 +180,19 @@ __global__ void k_recon(F64A<T> a, Box box) {
   T vp[NV], vm[NV];
   bool done = false;
   if constexpr (std::is_same<T, double>::value) {
-    if (a.char_lim) {  // CHAR_LIMITING YES, plm_states.c:446-705
+    if (a.char_lim && a.recon == PG_PARABOLIC) {  // CHAR_LIMITING YES, ppm_states.c:258-560
+      double w2[NV], w1[NV], v0[NV], e1[NV], e2[NV];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        w2[nv] = a.V[nv][c - 2 * s];
+        w1[nv] = a.V[nv][c - s];
+        v0[nv] = a.V[nv][c];
+        e1[nv] = a.V[nv][c + s];
+        e2[nv] = a.V[nv][c + 2 * s];
+      }
+      ppm_char<DIR>(w2, w1, v0, e1, e2, a.gamma, a.c3 != 0, g.dims, vp, vm);
+      done = true;
+    } else if (a.char_lim) {  // CHAR_LIMITING YES, plm_states.c:446-705
       double vl[NV], v0[NV], vr[NV];
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) {

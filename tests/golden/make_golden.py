@@ -224,6 +224,14 @@ def setups():
                 solver="roe", bc="outflow", name="cpa_ppm_chtr_roe_32"),
         replace(br.blast_setup(16, 12), recon="PARABOLIC", stepping="CHARACTERISTIC_TRACING", ct=False,
                 name="blast_ppm_chtr_noct_16"),
+        # PARABOLIC + CHAR_LIMITING (ppm_states.c:258-560), RK and CTU (reference state 2)
+        replace(br.ot_setup("hlld", 32, 30), recon="PARABOLIC", char_limiting=True, name="ot_ppm_charlim_32"),
+        replace(br.turb_setup(12, 10), char_limiting=True, name="turb_ppm_charlim_12"),
+        replace(br.tube_setup(1, 200, 120), recon="PARABOLIC", char_limiting=True, name="tube_ppm_charlim_1_200"),
+        replace(br.ot_setup("hlld", 32, 30), recon="PARABOLIC", char_limiting=True,
+                stepping="CHARACTERISTIC_TRACING", emf="UCT_CONTACT", name="ot_ppm_chtr_charlim_32"),
+        replace(br.blast_setup(16, 12), recon="PARABOLIC", char_limiting=True, stepping="CHARACTERISTIC_TRACING",
+                emf="ARITHMETIC", bc="outflow", name="blast_ppm_chtr_charlim_16"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

@@ -91,12 +91,12 @@ def test_char_tracing_validation(lib, extra, ok):
         lib.pg_destroy(h)
 
 
-@pytest.mark.parametrize("extra,precision,ok", [({}, "fp64", True), ({"recon": "PARABOLIC"}, "fp64", False),
+@pytest.mark.parametrize("extra,precision,ok", [({}, "fp64", True), ({"recon": "PARABOLIC"}, "fp64", True),
                                                  ({}, "mixed", False), ({}, "fp64_tangent", False),
                                                  ({"stepping": "HANCOCK"}, "fp64", True),
                                                  ({"char_limiting": 2}, "fp64", False)])
 def test_char_limiting_validation(lib, extra, precision, ok):
-    """CHAR_LIMITING YES: linear reconstruction on the plain FP64 path."""
+    """CHAR_LIMITING YES: linear or parabolic states on the plain FP64 path."""
     spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1), gamma=5 / 3, ct=False,
                 char_limiting=True)
     spec.update(extra)

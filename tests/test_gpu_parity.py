@@ -59,7 +59,9 @@ def test_fp64_matches_reference_goldens(name):
                                   "blast_ctu_noct_16", "ot_charlim_32", "blast_charlim_default_16",
                                   "tube_charlim_1_200", "cpa_charlim_rk3_32", "ot_chtr_charlim_32",
                                   "blast_ctu_charlim_16", "ot_ppm_chtr_32", "turb_ppm_chtr_12",
-                                  "tube_ppm_chtr_1_200", "cpa_ppm_chtr_roe_32", "blast_ppm_chtr_noct_16"])
+                                  "tube_ppm_chtr_1_200", "cpa_ppm_chtr_roe_32", "blast_ppm_chtr_noct_16",
+                                  "ot_ppm_charlim_32", "turb_ppm_charlim_12", "tube_ppm_charlim_1_200",
+                                  "ot_ppm_chtr_charlim_32", "blast_ppm_chtr_charlim_16"])
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
@@ -261,7 +263,10 @@ def test_char_tracing_vs_oracle_random_3d(emf, solver, bc):
                                                     ("MINMOD_LIM", "RK2", {"ct": False}),
                                                     ("VANLEER_LIM", "CHARACTERISTIC_TRACING",
                                                      {"emf": "UCT_CONTACT", "bc": "outflow"}),
-                                                    ("DEFAULT", "HANCOCK", {"emf": "ARITHMETIC"})])
+                                                    ("DEFAULT", "HANCOCK", {"emf": "ARITHMETIC"}),
+                                                    ("MC_LIM", "RK3", {"recon": "PARABOLIC"}),
+                                                    ("MC_LIM", "CHARACTERISTIC_TRACING",
+                                                     {"recon": "PARABOLIC", "emf": "UCT_CONTACT"})])
 def test_char_limiting_vs_oracle_random_3d(limiter, stepping, extra):
     """CHAR_LIMITING YES on a random 3D state against the oracle, bit for bit."""
     from oracle.oracle import Oracle
