@@ -519,9 +519,10 @@ def main():
         l1["max"] = l1["mixed"]["max"]
         del ra, rb
 
-    # ---- e2e through the C ABI with host buffers, as the AdvanceStep shim runs by default:
-    # ---- pg_upload once, then every step pg_advance (host dt in, invDt out) and a
-    # ---- pg_download of the whole state into the host arrays (PLUTO_GPU_SYNC_EVERY=1)
+    # ---- e2e through the C ABI with host buffers: pg_upload once, then every step
+    # ---- pg_advance (host dt in, invDt out) and a pg_download of the whole state into
+    # ---- the host arrays (the AdvanceStep shim with PLUTO_GPU_SYNC_EVERY=1; its default
+    # ---- downloads only for host readers, see the "output" leg)
     e2e = None
     if args.e2e_steps > 0:
         import torch
