@@ -400,7 +400,7 @@ def main():
     ap.add_argument("--fp64-steps", type=int, default=3)
     ap.add_argument("--l1-steps", type=int, default=100)
     ap.add_argument("--l1-n", type=int, default=512)
-    ap.add_argument("--e2e-steps", type=int, default=10)
+    ap.add_argument("--e2e-steps", type=int, default=30)
     ap.add_argument("--ref-n", type=int, default=96)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tubes", type=int, default=4096)
@@ -548,6 +548,7 @@ def main():
         tb = time.perf_counter()
         e.download(out=(out_vc, out_f))
         tc = time.perf_counter()
+        # synchronous form: each download completes before the next step starts
         barrier(ws)
         t0 = time.perf_counter()
         e.upload(host_vc, host_f)
@@ -556,15 +557,33 @@ def main():
             inv, _, _ = e.advance(dt)
             e.download(out=(out_vc, out_f))
             dt = min((1.0 / inv) * cfl, 1.1 * dt)
-        el = time.perf_counter() - t0
-        el = allmax(el, ws)
+        el_sync = allmax(time.perf_counter() - t0, ws)
+        # pipelined form (headline): step n's state is snapshotted on the device and
+        # copied to the host on a second stream while step n+1 runs; every copy has
+        # landed in host memory before the clock stops
+        e.download_async((out_vc, out_f))
+        e.download_wait()
+        barrier(ws)
+        t0 = time.perf_counter()
+        e.upload(host_vc, host_f)
+        dt = first_dt
+        for _ in range(args.e2e_steps):
+            inv, _, _ = e.advance(dt)
+            e.download_async((out_vc, out_f))
+            dt = min((1.0 / inv) * cfl, 1.1 * dt)
+        e.download_wait()
+        el = allmax(time.perf_counter() - t0, ws)
         del e
         state_bytes = 8 * (8 * cells + sum(f.size for f in faces))
         e2e = {"value": ws * cells * args.e2e_steps / el, "unit": "zone-updates/s",
                "h2d_bytes_per_step": int(state_bytes / args.e2e_steps + 8),
                "d2h_bytes_per_step": int(state_bytes + 48),
                "path": "pg_upload once (pinned host FP64) + per step pg_advance (host dt in, invDt out, "
-                       "synchronous) + pg_download of the whole FP64 state into pinned host arrays",
+                       "synchronous) + pg_download_async of the whole FP64 state into pinned host arrays "
+                       "(device snapshot, copy on a second stream overlapping the next step; all copies "
+                       "complete inside the timed region)",
+               "sync_value": ws * cells * args.e2e_steps / el_sync,
+               "sync_path": "the same with a synchronous pg_download after every step",
                "steps": args.e2e_steps,
                "upload_gbs": state_bytes / (tb - ta) / 1e9, "download_gbs": state_bytes / (tc - tb) / 1e9}
 

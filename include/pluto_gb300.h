@@ -291,6 +291,17 @@ typedef struct {
 } pg_output;
 int pg_write_output(pg_solver *s, const pg_output *out);
 int pg_output_wait(pg_solver *s);
+/* Asynchronous download (interior layout, as pg_download with
+   PG_LAYOUT_INTERIOR): enqueues a device-side snapshot of the state and its
+   copy into the caller's host arrays on a second stream, and returns; steps
+   enqueued afterwards run while the copy proceeds (pinned host arrays make it
+   asynchronous).  pg_download_wait blocks until the arrays hold the
+   snapshot; a further pg_download_async first waits for the previous copy.
+   The host arrays must not be touched until then.  FP64 and mixed
+   precisions. */
+int pg_download_async(pg_solver *s, double *const vars[8], double *const faces[3]);
+int pg_download_wait(pg_solver *s);
+
 /* Restart from a .dbl written as above (RestartFromFile's data part,
    Src/restart.c:17-150): reads the files named by out (format PG_OUT_DBL;
    dump, var, single_file, nfile, dir; native little-endian doubles) and

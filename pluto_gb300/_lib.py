@@ -36,7 +36,7 @@ EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", 
            "pg_batch_set_schedule", "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set",
            "pg_adjoint_step", "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load",
            "pg_selftest_conversions", "pg_set_userdef", "pg_set_internal_boundary",
-           "pg_write_output", "pg_output_wait", "pg_read_output"]
+           "pg_write_output", "pg_output_wait", "pg_read_output", "pg_download_async", "pg_download_wait"]
 PG_ABI_VERSION = 3  # the pg_config layout these bindings describe
 # pg_userdef_fn: (user, side 0..5, vpos 0 cells / 1..3 faces, stage)
 USERDEF_FN = C.CFUNCTYPE(None, C.c_void_p, C.c_int, C.c_int, C.c_int)
@@ -132,6 +132,8 @@ def lib():
     L.pg_write_output.argtypes = [vp, C.POINTER(PgOutput)]
     L.pg_output_wait.argtypes = [vp]
     L.pg_read_output.argtypes = [vp, C.POINTER(PgOutput)]
+    L.pg_download_async.argtypes = [vp, C.POINTER(dp), C.POINTER(dp)]
+    L.pg_download_wait.argtypes = [vp]
     L.pg_last_error.restype = C.c_char_p
     for fn in ("pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", "pg_run",
                "pg_run_async", "pg_sync", "pg_run_timed", "pg_profile_kernels", "pg_get_stream",
@@ -141,7 +143,7 @@ def lib():
                "pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set", "pg_adjoint_step",
                "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load", "pg_selftest_conversions",
                "pg_set_userdef", "pg_set_internal_boundary", "pg_write_output", "pg_output_wait",
-               "pg_read_output"):
+               "pg_read_output", "pg_download_async", "pg_download_wait"):
         getattr(L, fn).restype = C.c_int
     if L.pg_abi_version() != PG_ABI_VERSION:
         raise OSError(f"libpluto_gb300 has ABI version {L.pg_abi_version()}, these bindings expect "

@@ -26,6 +26,7 @@
 #include <condition_variable>
 #include <cstdio>
 #include <cstring>
+#include <algorithm>
 #include <deque>
 #include <mutex>
 #include <string>
@@ -52,30 +53,33 @@ struct PackSeg {
 
 __device__ __forceinline__ unsigned bswap32(unsigned x) { return __byte_perm(x, 0u, 0x0123); }
 
-// one output variable of the interior box into the staging buffer
+// one output variable of the interior box into the staging buffer: warps
+// along i within a (j, k) row, block rows and a resident-size grid striding
+// over the rows, so the index arithmetic is one 32-bit division per row
+constexpr int kPackX = 32, kPackY = 8;
 template <class T>
-__global__ void k_pack(PackSeg s, Geom g) {
-  const long long total = (long long)s.n[0] * s.n[1] * s.n[2];
-  for (long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x; q < total;
-       q += (long long)gridDim.x * blockDim.x) {
-    const int i = s.lo[0] + (int)(q % s.n[0]);
-    const long long r = q / s.n[0];
-    const int j = s.lo[1] + (int)(r % s.n[1]), k = s.lo[2] + (int)(r / s.n[1]);
-    const long long c = cidx(g, k, j, i);
-    if (s.kind == K_F64) {
-      ((double*)s.dst)[q] = (double)((const T*)s.src[0])[c];
-    } else if (s.kind == K_VEC3BE) {
-      unsigned* o = (unsigned*)s.dst + 3 * q;
+__global__ void __launch_bounds__(kPackX * kPackY) k_pack(PackSeg s, Geom g) {
+  const int rows = s.n[1] * s.n[2];
+  for (int row = blockIdx.y * blockDim.y + threadIdx.y; row < rows; row += gridDim.y * blockDim.y) {
+    const int j = s.lo[1] + row % s.n[1], k = s.lo[2] + row / s.n[1];
+    const long long c0 = cidx(g, k, j, s.lo[0]), q0 = (long long)row * s.n[0];
+    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n[0]; i += gridDim.x * blockDim.x) {
+      const long long c = c0 + i, q = q0 + i;
+      if (s.kind == K_F64) {
+        ((double*)s.dst)[q] = (double)((const T*)s.src[0])[c];
+      } else if (s.kind == K_VEC3BE) {
+        unsigned* o = (unsigned*)s.dst + 3 * q;
 #pragma unroll
-      for (int m = 0; m < 3; m++) {
-        const double v = m < s.ncomp ? (double)((const T*)s.src[m])[c] : 0.0;
-        const float f = (float)((double)(float)v * s.unit);
-        o[m] = bswap32(__float_as_uint(f));
+        for (int m = 0; m < 3; m++) {
+          const double v = m < s.ncomp ? (double)((const T*)s.src[m])[c] : 0.0;
+          const float f = (float)((double)(float)v * s.unit);
+          o[m] = bswap32(__float_as_uint(f));
+        }
+      } else {
+        const float f = (float)((double)((const T*)s.src[0])[c] * s.unit);
+        const unsigned b = __float_as_uint(f);
+        ((unsigned*)s.dst)[q] = s.kind == K_F32BE ? bswap32(b) : b;
       }
-    } else {
-      const float f = (float)((double)((const T*)s.src[0])[c] * s.unit);
-      const unsigned b = __float_as_uint(f);
-      ((unsigned*)s.dst)[q] = s.kind == K_F32BE ? bswap32(b) : b;
     }
   }
 }
@@ -113,6 +117,9 @@ struct OutputState {
   cudaStream_t copy = nullptr;
   int device = 0;
   Slot slots[2];
+  Slot dl;                           // staging of pg_download_async
+  cudaEvent_t dl_packed = nullptr, dl_done = nullptr;
+  bool dl_pending = false;
   std::thread worker;
   std::mutex m;
   std::condition_variable cv;
@@ -158,6 +165,7 @@ static int build_plan(const Solver* S, const pg_output* o, Plan& P, std::string&
   if (o->format < PG_OUT_DBL || o->format > PG_OUT_VTK) return err = "unknown output format", PG_ERR_INVALID;
   if (o->nvar < 0 || o->nvar > PG_OUT_MAX_VARS) return err = "nvar out of range", PG_ERR_INVALID;
   if (!o->dir) return err = "null output directory", PG_ERR_INVALID;
+  if ((long long)(g.nx[1] + 1) * (g.nx[2] + 1) >= (1LL << 31)) return err = "too many grid rows", PG_ERR_TOO_LARGE;
   const char* ext = ext_of(o->format);
   const long long ncell = (long long)g.nx[0] * (g.dims >= 2 ? g.nx[1] : 1) * (g.dims == 3 ? g.nx[2] : 1);
   std::string header;
@@ -369,6 +377,24 @@ static int wait_all(OutputState* O, std::string& msg) {
 
 using namespace pg;
 
+// about eight resident blocks per SM, the rest of the rows by striding
+static void launch_pack(const PackSeg& s, const Geom& g, bool is_float, cudaStream_t st) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaGetDevice(&dev);
+    cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (nsm <= 0) nsm = 1;
+  }
+  const long long rows = (long long)s.n[1] * s.n[2];
+  const unsigned gx = (unsigned)((s.n[0] + kPackX - 1) / kPackX);
+  const long long want = (rows + kPackY - 1) / kPackY, cap = std::max<long long>(1, 8LL * nsm / gx);
+  const dim3 grid(gx, (unsigned)std::min(std::min(want, cap), 65535LL));
+  const dim3 block(kPackX, kPackY);
+  if (is_float) k_pack<float><<<grid, block, 0, st>>>(s, g);
+  else k_pack<double><<<grid, block, 0, st>>>(s, g);
+}
+
 void pg::output_free(Solver* S) {
   OutputState* O = (OutputState*)S->out;
   if (!O) return;
@@ -380,10 +406,14 @@ void pg::output_free(Solver* S) {
   }
   O->cv.notify_all();
   if (O->worker.joinable()) O->worker.join();
+  if (O->dl_pending) cudaEventSynchronize(O->dl_done);
   for (Slot& s : O->slots) {
     if (s.dev) cudaFree(s.dev);
     if (s.host) cudaFreeHost(s.host);
   }
+  if (O->dl.dev) cudaFree(O->dl.dev);
+  if (O->dl_packed) cudaEventDestroy(O->dl_packed);
+  if (O->dl_done) cudaEventDestroy(O->dl_done);
   if (O->copy) cudaStreamDestroy(O->copy);
   delete O;
   S->out = nullptr;
@@ -459,17 +489,11 @@ extern "C" int pg_write_output(pg_solver* h, const pg_output* o) {
     }
     sl.cap = P.bytes;
   }
-  int nsm = 0;
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, O->device);
   for (PackSeg& s : P.segs) {
     bool is_float = false;
     if (bind_sources(S, s, is_float)) return release(PG_ERR_INVALID, "pg_write_output: state array missing");
     s.dst = sl.dev + (uintptr_t)s.dst;
-    const long long total = (long long)s.n[0] * s.n[1] * s.n[2];
-    const long long want = (total + kThreads - 1) / kThreads;
-    const unsigned blocks = (unsigned)(want < 8LL * nsm ? (want > 0 ? want : 1) : 8LL * nsm);
-    if (is_float) k_pack<float><<<blocks, kThreads, 0, S->stream>>>(s, S->g);
-    else k_pack<double><<<blocks, kThreads, 0, S->stream>>>(s, S->g);
+    launch_pack(s, S->g, is_float, S->stream);
   }
   cudaEvent_t packed = nullptr, copied = nullptr;
   if (cudaGetLastError() != cudaSuccess || cudaEventCreateWithFlags(&packed, cudaEventDisableTiming) != cudaSuccess ||
@@ -566,4 +590,117 @@ extern "C" int pg_read_output(pg_solver* h, const pg_output* o) {
   }
   if (host) cudaFreeHost(host);
   return rc;
+}
+
+// Asynchronous download of the state (interior layout): pack kernels on the
+// solver's stream write the FP64 interior of every requested array into a
+// device staging buffer, then the copy stream moves each array to the
+// caller's host memory while the next steps run.
+extern "C" int pg_download_async(pg_solver* h, double* const vars[8], double* const faces[3]) {
+  if (!h || !vars) {
+    set_last_error("pg_download_async: null argument");
+    return PG_ERR_INVALID;
+  }
+  Solver* S = &h->S;
+  if (S->cfg.precision == PG_FP64_TANGENT) {
+    set_last_error("pg_download_async: FP64 and mixed precisions only");
+    return PG_ERR_INVALID;
+  }
+  OutputState* O = output_state(S);
+  if (!O) {
+    set_last_error("pg_download_async: cannot create the copy stream");
+    return PG_ERR_CUDA;
+  }
+  const Geom& g = S->g;
+  const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
+  if ((long long)(g.nx[1] + 1) * (g.nx[2] + 1) >= (1LL << 31)) {
+    set_last_error("pg_download_async: too many grid rows");
+    return PG_ERR_TOO_LARGE;
+  }
+  std::vector<PackSeg> segs;
+  std::vector<double*> dst;
+  size_t bytes = 0;
+  for (int id = 0; id < 11; id++) {
+    double* host = id < 8 ? vars[id] : (faces && ct && id - 8 < g.dims ? faces[id - 8] : nullptr);
+    if (!host) continue;
+    PackSeg s;
+    memset(&s, 0, sizeof s);
+    const int fd = id >= 8 ? id - 8 : -1;
+    for (int ax = 0; ax < 3; ax++) {
+      const bool stag = ax == fd && ax < g.dims;
+      s.lo[ax] = g.beg[ax] - (stag ? 1 : 0);
+      s.n[ax] = g.nx[ax] + (stag ? 1 : 0);
+    }
+    s.kind = K_F64;
+    s.ncomp = 1;
+    s.unit = 1.0;
+    s.src[0] = (const void*)(intptr_t)id;
+    s.src[1] = s.src[2] = (const void*)(intptr_t)-1;
+    bytes = (bytes + 15) & ~(size_t)15;
+    s.dst = (unsigned char*)(uintptr_t)bytes;
+    bytes += (size_t)s.n[0] * s.n[1] * s.n[2] * sizeof(double);
+    segs.push_back(s);
+    dst.push_back(host);
+  }
+  if (O->dl_pending) {  // the staging buffer is still being copied out
+    if (cudaEventSynchronize(O->dl_done) != cudaSuccess) {
+      set_last_error("pg_download_async: previous copy failed");
+      return PG_ERR_CUDA;
+    }
+    O->dl_pending = false;
+  }
+  if (O->dl.cap < bytes) {
+    if (O->dl.dev) cudaFree(O->dl.dev);
+    O->dl.dev = nullptr;
+    O->dl.cap = 0;
+    if (cudaMalloc(&O->dl.dev, bytes) != cudaSuccess) {
+      set_last_error("pg_download_async: staging buffer");
+      return PG_ERR_NOMEM;
+    }
+    O->dl.cap = bytes;
+  }
+  if (!O->dl_packed && (cudaEventCreateWithFlags(&O->dl_packed, cudaEventDisableTiming) != cudaSuccess ||
+                        cudaEventCreateWithFlags(&O->dl_done, cudaEventDisableTiming) != cudaSuccess)) {
+    set_last_error("pg_download_async: events");
+    return PG_ERR_CUDA;
+  }
+  std::vector<size_t> off;
+  for (PackSeg& s : segs) {
+    bool is_float = false;
+    off.push_back((uintptr_t)s.dst);
+    if (bind_sources(S, s, is_float)) {
+      set_last_error("pg_download_async: state array missing");
+      return PG_ERR_INVALID;
+    }
+    s.dst = O->dl.dev + (uintptr_t)s.dst;
+    launch_pack(s, S->g, is_float, S->stream);
+  }
+  cudaEventRecord(O->dl_packed, S->stream);
+  cudaStreamWaitEvent(O->copy, O->dl_packed, 0);
+  for (size_t m = 0; m < segs.size(); m++) {
+    const size_t len = (size_t)segs[m].n[0] * segs[m].n[1] * segs[m].n[2] * sizeof(double);
+    cudaMemcpyAsync(dst[m], O->dl.dev + off[m], len, cudaMemcpyDeviceToHost, O->copy);
+  }
+  cudaEventRecord(O->dl_done, O->copy);
+  if (cudaGetLastError() != cudaSuccess) {
+    set_last_error("pg_download_async: launch or copy");
+    return PG_ERR_CUDA;
+  }
+  O->dl_pending = true;
+  return PG_OK;
+}
+
+extern "C" int pg_download_wait(pg_solver* h) {
+  if (!h) {
+    set_last_error("pg_download_wait: null argument");
+    return PG_ERR_INVALID;
+  }
+  OutputState* O = (OutputState*)h->S.out;
+  if (!O || !O->dl_pending) return PG_OK;
+  O->dl_pending = false;
+  if (cudaEventSynchronize(O->dl_done) != cudaSuccess) {
+    set_last_error("pg_download_wait: copy failed");
+    return PG_ERR_CUDA;
+  }
+  return PG_OK;
 }

@@ -123,20 +123,26 @@ class Solver:
             faces = [np.zeros(self.face_shape(d)) if (self.ct and d < self.dims) else None
                      for d in range(3)]
         else:
-            vc, faces = out[0], list(out[1]) + [None] * (3 - len(out[1]))
-            if vc.shape != (NVAR, nz, ny, nx) or vc.dtype != np.float64 or not vc.flags.c_contiguous:
-                raise ValueError("out[0] must be a C-contiguous float64 array of shape %s" % ((NVAR, nz, ny, nx),))
-            for d in range(3):
-                want = self.ct and d < self.dims
-                f = faces[d]
-                if want and (f is None or f.shape != self.face_shape(d) or f.dtype != np.float64
-                             or not f.flags.c_contiguous):
-                    raise ValueError("out[1][%d] must be a C-contiguous float64 array of shape %s"
-                                     % (d, self.face_shape(d)))
-                if not want:
-                    faces[d] = None
+            vc, faces = self._check_out(out)
         views = [vc[q] for q in range(NVAR)]
         L.check(getattr(L.lib(), fn)(self.h, _ptrs(views, 8), _ptrs(faces, 3), L.PG_LAYOUT_INTERIOR), fn)
+        return vc, faces
+
+    def _check_out(self, out):
+        """(vc, faces) of caller-provided arrays, shapes and layout checked."""
+        nx, ny, nz = self.nx
+        vc, faces = out[0], list(out[1]) + [None] * (3 - len(out[1]))
+        if vc.shape != (NVAR, nz, ny, nx) or vc.dtype != np.float64 or not vc.flags.c_contiguous:
+            raise ValueError("out[0] must be a C-contiguous float64 array of shape %s" % ((NVAR, nz, ny, nx),))
+        for d in range(3):
+            want = self.ct and d < self.dims
+            f = faces[d]
+            if want and (f is None or f.shape != self.face_shape(d) or f.dtype != np.float64
+                         or not f.flags.c_contiguous):
+                raise ValueError("out[1][%d] must be a C-contiguous float64 array of shape %s"
+                                 % (d, self.face_shape(d)))
+            if not want:
+                faces[d] = None
         return vc, faces
 
     def ghost_shape(self):
@@ -187,6 +193,20 @@ class Solver:
         preallocated arrays instead (e.g. pinned host memory, which the
         device writes in place)."""
         return self._get("pg_download", out)
+
+    def download_async(self, out):
+        """Enqueue a snapshot of the state into out=(vc, faces) (pinned
+        host arrays as for download(out=...)) and return; the copy runs on a
+        second stream while later steps proceed.  download_wait() blocks
+        until out holds the snapshot."""
+        vc, faces = self._check_out(out)
+        views = [vc[q] for q in range(NVAR)]
+        self._async_keep = (vc, faces)
+        L.check(L.lib().pg_download_async(self.h, _ptrs(views, 8), _ptrs(faces, 3)), "pg_download_async")
+
+    def download_wait(self):
+        L.check(L.lib().pg_download_wait(self.h), "pg_download_wait")
+        self._async_keep = None
 
     # -- output files (WriteData's .dbl / .flt / .vtk) --
     def output_vars(self, fmt: str, vtk_vector: bool = False):

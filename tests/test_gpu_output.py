@@ -115,3 +115,32 @@ def test_output_errors(tmp_path):
     s.write_output(tmp_path, "dbl", 0)
     s.output_wait()
     assert (tmp_path / "data.0000.dbl").stat().st_size == 8 * (32 * 32 * 6 + 2 * 33 * 32)
+
+
+@pytest.mark.parametrize("precision", ["fp64", "mixed"])
+def test_download_async_snapshots_each_step(precision):
+    """pg_download_async copies the state at the call while the next steps
+    run: each snapshot equals a synchronous download of the same state."""
+    import torch
+    from pluto_gb300 import Solver
+    meta, vc0, bs0, _, _ = load_golden("blast_16")
+    a, b = Solver(meta, precision=precision), Solver(meta, precision=precision)
+    a.upload(vc0, bs0)
+    b.upload(vc0, bs0)
+
+    def pinned(shape):
+        return torch.empty(shape, dtype=torch.float64, pin_memory=True).numpy()
+
+    bufs = [(pinned(vc0.shape), [pinned(f.shape) for f in bs0]) for _ in range(3)]
+    want = []
+    for n in range(3):
+        a.advance(1e-3)
+        b.advance(1e-3)
+        a.download_async(bufs[n])  # waits for the previous copy, not for later steps
+        want.append(b.download())
+    a.advance(1e-3)
+    a.download_wait()
+    for (vc, bs), (wv, wb) in zip(bufs, want):
+        assert np.array_equal(vc, wv)
+        for d in range(3):
+            assert np.array_equal(bs[d], wb[d])
