@@ -34,6 +34,7 @@
 #include <vector>
 
 #include "pg_internal.h"
+#include "pg_dw.cuh"
 
 float* mixed_cell_array(pg::Solver* S, int nv);
 float* mixed_face_array(pg::Solver* S, int d);
@@ -53,35 +54,55 @@ struct PackSeg {
 
 __device__ __forceinline__ unsigned bswap32(unsigned x) { return __byte_perm(x, 0u, 0x0123); }
 
-// one output variable of the interior box into the staging buffer: warps
-// along i within a (j, k) row, block rows and a resident-size grid striding
-// over the rows, so the index arithmetic is one 32-bit division per row
-constexpr int kPackX = 32, kPackY = 8;
+// float <-> double in integer arithmetic (pg_dw.cuh: exact widening,
+// round-to-nearest-even narrowing, checked against the IEEE conversions by
+// pg_selftest_conversions): the hardware conversions issue on the FP64 pipe
+__device__ __forceinline__ double to_f64(float v) { return widen(v); }
+__device__ __forceinline__ double to_f64(double v) { return v; }
+__device__ __forceinline__ float to_f32(float v, double unit) { return unit == 1.0 ? v : narrow(widen(v) * unit); }
+__device__ __forceinline__ float to_f32(double v, double unit) { return narrow(unit == 1.0 ? v : v * unit); }
+
+// one output variable of the interior box into the staging buffer: threads
+// along i, blockIdx.y over j, blockIdx.z striding over k, four k planes per
+// pass with every load issued before the stores (no integer division
+// anywhere: it issues on the FP64 pipe on this GPU)
+constexpr int kPackPlanes = 4;
 template <class T>
-__global__ void __launch_bounds__(kPackX * kPackY) k_pack(PackSeg s, Geom g) {
-  const int rows = s.n[1] * s.n[2];
-  for (int row = blockIdx.y * blockDim.y + threadIdx.y; row < rows; row += gridDim.y * blockDim.y) {
-    const int j = s.lo[1] + row % s.n[1], k = s.lo[2] + row / s.n[1];
-    const long long c0 = cidx(g, k, j, s.lo[0]), q0 = (long long)row * s.n[0];
-    for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < s.n[0]; i += gridDim.x * blockDim.x) {
-      const long long c = c0 + i, q = q0 + i;
-      if (s.kind == K_F64) {
-        ((double*)s.dst)[q] = (double)((const T*)s.src[0])[c];
-      } else if (s.kind == K_VEC3BE) {
-        unsigned* o = (unsigned*)s.dst + 3 * q;
+__global__ void k_pack(PackSeg s, Geom g) {
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= s.n[0]) return;
+  const int nc = s.kind == K_VEC3BE ? s.ncomp : 1;
+  for (int j = blockIdx.y; j < s.n[1]; j += gridDim.y)
+    for (int k0 = blockIdx.z; k0 < s.n[2]; k0 += kPackPlanes * gridDim.z) {
+      T v[kPackPlanes][3];
 #pragma unroll
-        for (int m = 0; m < 3; m++) {
-          const double v = m < s.ncomp ? (double)((const T*)s.src[m])[c] : 0.0;
-          const float f = (float)((double)(float)v * s.unit);
-          o[m] = bswap32(__float_as_uint(f));
+      for (int u = 0; u < kPackPlanes; u++) {
+        const int k = k0 + u * gridDim.z;
+        const long long c = cidx(g, s.lo[2] + k, s.lo[1] + j, s.lo[0] + i);
+#pragma unroll
+        for (int m = 0; m < 3; m++)
+          if (k < s.n[2] && m < nc) v[u][m] = ((const T*)s.src[m])[c];
+      }
+#pragma unroll
+      for (int u = 0; u < kPackPlanes; u++) {
+        const int k = k0 + u * gridDim.z;
+        if (k >= s.n[2]) break;
+        const long long q = ((long long)k * s.n[1] + j) * s.n[0] + i;
+        if (s.kind == K_F64) {
+          ((double*)s.dst)[q] = to_f64(v[u][0]);
+        } else if (s.kind == K_VEC3BE) {  // (float)v * unit, stored as float (write_vtk.c)
+          unsigned* o = (unsigned*)s.dst + 3 * q;
+#pragma unroll
+          for (int m = 0; m < 3; m++) {
+            const float f = m < nc ? to_f32(to_f32(v[u][m], 1.0), s.unit) : 0.0f;
+            o[m] = bswap32(__float_as_uint(f));
+          }
+        } else {
+          const unsigned b = __float_as_uint(to_f32(v[u][0], s.unit));
+          ((unsigned*)s.dst)[q] = s.kind == K_F32BE ? bswap32(b) : b;
         }
-      } else {
-        const float f = (float)((double)((const T*)s.src[0])[c] * s.unit);
-        const unsigned b = __float_as_uint(f);
-        ((unsigned*)s.dst)[q] = s.kind == K_F32BE ? bswap32(b) : b;
       }
     }
-  }
 }
 
 // a file: literal byte pieces and spans of the packed buffer, in order
@@ -165,7 +186,8 @@ static int build_plan(const Solver* S, const pg_output* o, Plan& P, std::string&
   if (o->format < PG_OUT_DBL || o->format > PG_OUT_VTK) return err = "unknown output format", PG_ERR_INVALID;
   if (o->nvar < 0 || o->nvar > PG_OUT_MAX_VARS) return err = "nvar out of range", PG_ERR_INVALID;
   if (!o->dir) return err = "null output directory", PG_ERR_INVALID;
-  if ((long long)(g.nx[1] + 1) * (g.nx[2] + 1) >= (1LL << 31)) return err = "too many grid rows", PG_ERR_TOO_LARGE;
+  if ((long long)(g.nx[0] + 1) * (g.nx[1] + 1) * (g.nx[2] + 1) >= (1LL << 31))
+    return err = "a variable of more than 2^31 elements", PG_ERR_TOO_LARGE;
   const char* ext = ext_of(o->format);
   const long long ncell = (long long)g.nx[0] * (g.dims >= 2 ? g.nx[1] : 1) * (g.dims == 3 ? g.nx[2] : 1);
   std::string header;
@@ -377,7 +399,8 @@ static int wait_all(OutputState* O, std::string& msg) {
 
 using namespace pg;
 
-// about eight resident blocks per SM, the rest of the rows by striding
+// rows of 128 threads; j over gridDim.y, k strided over gridDim.z so that
+// about sixteen blocks per SM are resident
 static void launch_pack(const PackSeg& s, const Geom& g, bool is_float, cudaStream_t st) {
   static int nsm = 0;
   if (!nsm) {
@@ -386,13 +409,16 @@ static void launch_pack(const PackSeg& s, const Geom& g, bool is_float, cudaStre
     cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
     if (nsm <= 0) nsm = 1;
   }
-  const long long rows = (long long)s.n[1] * s.n[2];
-  const unsigned gx = (unsigned)((s.n[0] + kPackX - 1) / kPackX);
-  const long long want = (rows + kPackY - 1) / kPackY, cap = std::max<long long>(1, 8LL * nsm / gx);
-  const dim3 grid(gx, (unsigned)std::min(std::min(want, cap), 65535LL));
-  const dim3 block(kPackX, kPackY);
-  if (is_float) k_pack<float><<<grid, block, 0, st>>>(s, g);
-  else k_pack<double><<<grid, block, 0, st>>>(s, g);
+  constexpr int kPackThreads = 128;
+  const unsigned gx = (unsigned)((s.n[0] + kPackThreads - 1) / kPackThreads);
+  const unsigned gy = (unsigned)std::min(s.n[1], 65535);
+  const long long per_z = (long long)gx * gy;
+  const unsigned gz = (unsigned)std::max<long long>(
+      1, std::min<long long>({((long long)s.n[2] + kPackPlanes - 1) / kPackPlanes,
+                              (16LL * nsm + per_z - 1) / per_z, 65535LL}));
+  const dim3 grid(gx, gy, gz);
+  if (is_float) k_pack<float><<<grid, kPackThreads, 0, st>>>(s, g);
+  else k_pack<double><<<grid, kPackThreads, 0, st>>>(s, g);
 }
 
 void pg::output_free(Solver* S) {
@@ -613,8 +639,8 @@ extern "C" int pg_download_async(pg_solver* h, double* const vars[8], double* co
   }
   const Geom& g = S->g;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
-  if ((long long)(g.nx[1] + 1) * (g.nx[2] + 1) >= (1LL << 31)) {
-    set_last_error("pg_download_async: too many grid rows");
+  if ((long long)(g.nx[0] + 1) * (g.nx[1] + 1) * (g.nx[2] + 1) >= (1LL << 31)) {
+    set_last_error("pg_download_async: a variable of more than 2^31 elements");
     return PG_ERR_TOO_LARGE;
   }
   std::vector<PackSeg> segs;
