@@ -137,7 +137,8 @@ class Clocks:
 
 # ---------------------------------------------------------------------------
 # algorithmic bytes of the mixed kernels (FP32 storage), per cell of the box
-# a launch covers; see DESIGN.md "Roofline accounting"
+# a launch covers: each compulsory state array read or written once at its
+# stored width (FP32 primitives and face fields, FP64 resident accumulators)
 # ---------------------------------------------------------------------------
 def kernel_bytes(name, n, stage_mix=True):
     """Compulsory HBM bytes of one launch of kernel family ``name`` on an n^3
@@ -192,9 +193,10 @@ def cpu_rate(n=96, budget_s=12.0, threads=None):
 
 def reference_arm(args, rank, ws):
     """--impl reference: the reference algorithm on the host cores.  The
-    reference C binary cannot be built on the GPU machine (its source tree is not
-    there), so the oracle port -- bit-identical to it on the golden problems --
-    is timed, with all host threads, one bounded sample per step."""
+    reference C binary cannot be built on the benchmark machine (an Arm host
+    without the reference source tree), so the oracle port -- bit-identical
+    to it on the golden problems -- is timed, with all host threads, one
+    bounded sample per step."""
     if rank != 0:
         return
     from oracle.oracle import Oracle, build as obuild

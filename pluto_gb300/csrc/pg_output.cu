@@ -189,7 +189,6 @@ static int build_plan(const Solver* S, const pg_output* o, Plan& P, std::string&
   if ((long long)(g.nx[0] + 1) * (g.nx[1] + 1) * (g.nx[2] + 1) >= (1LL << 31))
     return err = "a variable of more than 2^31 elements", PG_ERR_TOO_LARGE;
   const char* ext = ext_of(o->format);
-  const long long ncell = (long long)g.nx[0] * (g.dims >= 2 ? g.nx[1] : 1) * (g.dims == 3 ? g.nx[2] : 1);
   std::string header;
   if (o->format == PG_OUT_VTK) {
     for (int d = 0; d < 3; d++)
@@ -291,7 +290,6 @@ static int build_plan(const Solver* S, const pg_output* o, Plan& P, std::string&
       }
     }
   if (o->single_file) P.files.insert(P.files.begin(), single);
-  (void)ncell;
   // the ".out" record (Src/write_data.c:360-385)
   P.write_record = o->write_record != 0;
   P.nfile = o->nfile;
