@@ -45,23 +45,7 @@ def test_fp64_matches_reference_goldens(name):
     assert abs(t - meta["t_final"]) <= 1e-6 * meta["t_final"]
 
 
-@pytest.mark.parametrize("name", ["ot_hlld_32", "blast_16", "tube_0_256", "turb_12", "blast_floor_16",
-                                  "ot_roe_32", "cpa_roe_32", "blast_roe_16", "tube_roe_0_256",
-                                  "ot_outflow_32", "turb_outflow_12", "ot_ctu_uctc_32",
-                                  "ot_ctu_arith_roe_32", "turb_ctu_uctc_12", "tube_ctu_1_200",
-                                  "cpa_ctu_outflow_32", "blast_reflective_16", "ot_reflective_32",
-                                  "cpa_eqtsym_32", "tube_reflective_0_256", "ot_ctu_reflective_32",
-                                  "blast_sides_16", "ot_sides_32", "ot_ctu_sides_32", "tube_sides_0_256",
-                                  "ot_userdef_32", "blast_userdef_16", "blast_userdef_ct_16",
-                                  "ot_euler_32", "tube_euler_0_256", "ot_internal_32",
-                                  "ot_chtr_uctc_32", "ot_chtr_arith_roe_32", "cpa_chtr_32", "turb_chtr_12",
-                                  "tube_chtr_1_200", "blast_chtr_outflow_16", "blast_chtr_noct_16",
-                                  "blast_ctu_noct_16", "ot_charlim_32", "blast_charlim_default_16",
-                                  "tube_charlim_1_200", "cpa_charlim_rk3_32", "ot_chtr_charlim_32",
-                                  "blast_ctu_charlim_16", "ot_ppm_chtr_32", "turb_ppm_chtr_12",
-                                  "tube_ppm_chtr_1_200", "cpa_ppm_chtr_roe_32", "blast_ppm_chtr_noct_16",
-                                  "ot_ppm_charlim_32", "turb_ppm_charlim_12", "tube_ppm_charlim_1_200",
-                                  "ot_ppm_chtr_charlim_32", "blast_ppm_chtr_charlim_16"])
+@pytest.mark.parametrize("name", GOLDEN_NAMES)
 def test_fp64_bitwise_on_goldens(name):
     meta, vc0, bs0, vc1, bs1 = load_golden(name)
     s = _solver(meta)
