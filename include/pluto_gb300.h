@@ -53,7 +53,7 @@ enum { PG_EULER = 1, PG_RK2 = 2, PG_RK3 = 3,                      /* TIME_STEPPI
    CHARACTERISTIC_TRACING, CTU with the characteristic tracing predictor
    (char_tracing.c, linear reconstruction) */
 enum { PG_DIVB_NONE = 0, PG_CONSTRAINED_TRANSPORT = 1 };          /* DIVB_CONTROL */
-enum { PG_ARITHMETIC = 1, PG_UCT_CONTACT = 3, PG_UCT_HLL = 4 };   /* CT_EMF_AVERAGE */
+enum { PG_ARITHMETIC = 1, PG_UCT0 = 2, PG_UCT_CONTACT = 3, PG_UCT_HLL = 4 }; /* CT_EMF_AVERAGE */
 enum { PG_PERIODIC = 0, PG_OUTFLOW = 1, PG_REFLECTIVE = 2,
        PG_EQTSYMMETRIC = 3, PG_USERDEF = 4 };                     /* [Boundary] */
 /* arithmetic: PG_FP64 bit-compatible with the reference C path;

@@ -919,6 +919,9 @@ static void plm_char_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV],
 static void ppm_char_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV], int beg, int end, double gamma,
                             const Rot *r, int c3, int dims);
 
+/* face-EMF slots of eface[] */
+enum { EZI = 0, EZJ, EYI, EYK, EXJ, EXK };
+
 static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1d,
                   double *mach_out) {
   const int dims = p->c.dims;
@@ -1000,6 +1003,20 @@ static void sweep(oc_problem *p, int dir, double dt, int stage, double *inv_dt_1
           c = CI(p, ijk[2], ijk[1], ijk[0]);
           p->sl[dir][c] = MAX(0.0, -w.ifc[i].SL);
           p->sr[dir][c] = MAX(0.0, w.ifc[i].SR);
+          if (p->c.emf != OC_UCT_HLL) { /* the other averages: face EMFs and mass-flux signs */
+            const double *F = w.ifc[i].f;
+            if (dir == 0) {
+              p->eface[EZI][c] = -F[BX2];
+              if (dims == 3) p->eface[EYI][c] = F[BX3];
+            } else if (dir == 1) {
+              p->eface[EZJ][c] = F[BX1];
+              if (dims == 3) p->eface[EXJ][c] = -F[BX3];
+            } else {
+              p->eface[EYK][c] = -F[BX1];
+              p->eface[EXK][c] = F[BX2];
+            }
+            p->sv[dir][c] = F[RHO] > 1.e-6 ? 1 : (F[RHO] < -1.e-6 ? -1 : 0);
+          }
         }
         for (i = nbeg - 1; i <= nend + 1; i++) {
           size_t c;
@@ -1220,6 +1237,8 @@ static void cons_to_prim_3d(oc_problem *p) {
   p->nfail += nf;
 }
 
+static void ctu_compute_emf(oc_problem *p, int stage);
+
 /* UpdateStage, update_stage.c:37-314 */
 static void update_stage(oc_problem *p, double dt, int stage, double *inv_dt,
                          double *inv_dt_1d) {
@@ -1227,7 +1246,16 @@ static void update_stage(oc_problem *p, double dt, int stage, double *inv_dt,
   if (p->c.dims > 1 && stage == 1) memset(p->cdt, 0, p->ncell * sizeof(double));
   for (dir = 0; dir < p->c.dims; dir++) sweep(p, dir, dt, stage, inv_dt_1d, &p->max_mach);
   if (p->c.ct) {
-    compute_emf(p);
+    if (p->c.emf == OC_UCT_HLL) {
+      compute_emf(p);
+    } else { /* edges over i in [IBEG-1, IEND] etc. (ct_emf.c:130-131) */
+      int d;
+      for (d = 0; d < 3; d++) {
+        p->emf_lo[d] = d < p->c.dims ? p->beg[d] - 1 : 0;
+        p->emf_hi[d] = d < p->c.dims ? p->end[d] : 0;
+      }
+      ctu_compute_emf(p, 2);
+    }
     ct_update(p, dt);
   }
   if (p->c.dims > 1 && stage == 1) { /* :308-312 */
@@ -1670,7 +1698,6 @@ static void ppm_char_states(double (*v)[NV], double (*vp)[NV], double (*vm)[NV],
 }
 
 /* face-EMF slot of (dir, component): ezi, ezj, eyi, eyk, exj, exk */
-enum { EZI = 0, EZJ, EYI, EYK, EXJ, EXK };
 
 /* One CTU sweep.  stage 1: normal predictors (PLM + primitive Hancock,
    hancock.c:36-172, CheckPrimStates check_states.c:18-70), Riemann
@@ -1888,10 +1915,12 @@ static void ctu_sweep(oc_problem *p, int dir, double dt, int stage, double *inv_
   *inv_dt = invdt;
 }
 
-/* CT_ComputeEMF for ARITHMETIC and UCT_CONTACT (ct_emf.c:210-291,
-   ct_emf_average.c:13-164); CT_ComputeCenterEMF (ct_emf.c:348-388). */
+/* CT_ComputeEMF for ARITHMETIC, UCT0 and UCT_CONTACT (ct_emf.c:210-291,
+   ct_emf_average.c:13-164); CT_ComputeCenterEMF (ct_emf.c:348-388).
+   stage 1 = CTU predictor (no corner integration, ct_emf_average.c:89-91);
+   the RK stages and the CTU corrector pass 2. */
 static void ctu_compute_emf(oc_problem *p, int stage) {
-  const int dims = p->c.dims, uct = p->c.emf == OC_UCT_CONTACT;
+  const int dims = p->c.dims, uct = p->c.emf == OC_UCT_CONTACT, uct0 = p->c.emf == OC_UCT0;
   const double w = uct ? 1.0 : 0.25;
   const int ib = p->emf_lo[0], ie = p->emf_hi[0], jb = p->emf_lo[1], je = p->emf_hi[1];
   const int kb = dims == 3 ? p->emf_lo[2] : 0, ke = dims == 3 ? p->emf_hi[2] : 0;
@@ -1900,7 +1929,7 @@ static void ctu_compute_emf(oc_problem *p, int stage) {
   double *exj = p->eface[EXJ], *exk = p->eface[EXK];
   double *Ex1 = p->ecc[0], *Ex2 = p->ecc[1], *Ex3 = p->ecc[2];
   int i, j, k;
-  if (uct) {
+  if (uct || uct0) {
     size_t c;
     for (c = 0; c < p->ncell; c++) {
       double vx1 = p->vc[VX1][c], vx2 = p->vc[VX2][c], vx3 = p->vc[VX3][c];
@@ -1911,6 +1940,25 @@ static void ctu_compute_emf(oc_problem *p, int stage) {
     }
   }
 #define E3(a, kk, jj, ii) (a[CI(p, kk, jj, ii)])
+  if (uct0) /* face EMFs minus the centred ones, in place (ct_emf.c:261-282) */
+    for (k = kb; k <= ke + KO; k++)
+      for (j = jb; j <= je + 1; j++)
+        for (i = ib; i <= ie + 1; i++) {
+          if (dims == 3) {
+            E3(exj, k, j, i) *= 2.0;
+            E3(exk, k, j, i) *= 2.0;
+            E3(eyi, k, j, i) *= 2.0;
+            E3(eyk, k, j, i) *= 2.0;
+            E3(exj, k, j, i) -= 0.5 * (E3(Ex1, k, j, i) + E3(Ex1, k, j + 1, i));
+            E3(exk, k, j, i) -= 0.5 * (E3(Ex1, k, j, i) + E3(Ex1, k + 1, j, i));
+            E3(eyi, k, j, i) -= 0.5 * (E3(Ex2, k, j, i) + E3(Ex2, k, j, i + 1));
+            E3(eyk, k, j, i) -= 0.5 * (E3(Ex2, k, j, i) + E3(Ex2, k + 1, j, i));
+          }
+          E3(ezi, k, j, i) *= 2.0;
+          E3(ezj, k, j, i) *= 2.0;
+          E3(ezi, k, j, i) -= 0.5 * (E3(Ex3, k, j, i) + E3(Ex3, k, j, i + 1));
+          E3(ezj, k, j, i) -= 0.5 * (E3(Ex3, k, j, i) + E3(Ex3, k, j + 1, i));
+        }
   for (k = kb; k <= ke; k++)
     for (j = jb; j <= je; j++)
       for (i = ib; i <= ie; i++) {
@@ -2246,7 +2294,11 @@ oc_problem *oc_create(const oc_config *cfg) {
   if (IS_CTU(cfg->stepping)) {
     /* hancock.c:64-67; characteristic tracing takes parabolic states too */
     if (cfg->recon != OC_LINEAR && cfg->stepping != OC_CHARTR) { free(p); return NULL; }
-    if (cfg->ct && cfg->emf != OC_ARITHMETIC && cfg->emf != OC_UCT_CONTACT) { free(p); return NULL; }
+    /* ct_emf.c:196-200: UCT_HLL needs the RK sweeps */
+    if (cfg->ct && cfg->emf != OC_ARITHMETIC && cfg->emf != OC_UCT0 && cfg->emf != OC_UCT_CONTACT) {
+      free(p);
+      return NULL;
+    }
     if (cfg->ct) p->ng++;                                    /* get_nghost.c:84-90 */
   }
   for (d = 0; d < 3; d++) {
@@ -2286,6 +2338,8 @@ oc_problem *oc_create(const oc_config *cfg) {
         p->rhs_s[d][nv] = calloc(p->ncell, sizeof(double));
       }
     for (nv = 0; nv < NV; nv++) p->uh[nv] = calloc(p->ncell, sizeof(double));
+  }
+  if (cfg->ct && (IS_CTU(cfg->stepping) || cfg->emf != OC_UCT_HLL)) {
     for (d = 0; d < 6; d++) p->eface[d] = calloc(p->ncell, sizeof(double));
     for (d = 0; d < 3; d++) {
       p->sv[d] = calloc(p->ncell, 1);

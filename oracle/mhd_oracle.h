@@ -30,7 +30,7 @@ enum { OC_EULER = 1, OC_RK2 = 2, OC_RK3 = 3, OC_HANCOCK = 4, OC_CHARTR = 5 };
 /* OC_CHARTR: CTU with CharTracingStep (TIME_STEPPING CHARACTERISTIC_TRACING,
    LINEAR reconstruction) */
 #define IS_CTU(s) ((s) == OC_HANCOCK || (s) == OC_CHARTR) /* HANCOCK: CTU with the primitive Hancock predictor */
-enum { OC_ARITHMETIC = 1, OC_UCT_CONTACT = 3, OC_UCT_HLL = 4 }; /* CT_EMF_AVERAGE */
+enum { OC_ARITHMETIC = 1, OC_UCT0 = 2, OC_UCT_CONTACT = 3, OC_UCT_HLL = 4 }; /* CT_EMF_AVERAGE, Src/MHD/CT/ct.h:17-21 */
 enum { OC_PERIODIC = 0, OC_OUTFLOW = 1, OC_REFLECTIVE = 2, OC_EQTSYMMETRIC = 3, OC_USERDEF = 4 };
 
 /* USERDEF sides: called in Boundary's order with side 0..5 (X1_BEG..X3_END),

@@ -22,7 +22,7 @@ SOLVER = {"hll": 0, "hlld": 1, "roe": 2}
 STEPPING = {"EULER": 1, "RK2": 2, "RK3": 3, "HANCOCK": 4, "CHARACTERISTIC_TRACING": 5}
 CTU_STEPPING = ("HANCOCK", "CHARACTERISTIC_TRACING")
 BC = {"periodic": 0, "outflow": 1, "reflective": 2, "eqtsymmetric": 3, "userdef": 4}
-EMF = {"ARITHMETIC": 1, "UCT_CONTACT": 3, "UCT_HLL": 4}
+EMF = {"ARITHMETIC": 1, "UCT0": 2, "UCT_CONTACT": 3, "UCT_HLL": 4}
 
 
 class OcConfig(C.Structure):

@@ -18,7 +18,7 @@ PG_FLAT_LIM, PG_MINMOD_LIM, PG_VANLEER_LIM, PG_MC_LIM, PG_DEFAULT_LIM = 0, 1, 2,
 PG_HLL, PG_HLLD, PG_ROE = 0, 1, 2
 PG_RK2, PG_RK3, PG_HANCOCK, PG_CHAR_TRACING = 2, 3, 4, 5
 PG_DIVB_NONE, PG_CONSTRAINED_TRANSPORT = 0, 1
-PG_ARITHMETIC, PG_UCT_CONTACT, PG_UCT_HLL = 1, 3, 4
+PG_ARITHMETIC, PG_UCT0, PG_UCT_CONTACT, PG_UCT_HLL = 1, 2, 3, 4
 PG_PERIODIC, PG_OUTFLOW, PG_REFLECTIVE, PG_EQTSYMMETRIC, PG_USERDEF = 0, 1, 2, 3, 4
 PG_EULER = 1
 PG_FP64, PG_MIXED, PG_MIXED_DW, PG_FP64_TANGENT = 0, 1, 2, 3

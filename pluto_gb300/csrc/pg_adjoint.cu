@@ -849,6 +849,10 @@ extern "C" int pg_adjoint_set(pg_solver* h, const double* const vars[8], const d
     set_last_error("pg_adjoint_set: no adjoint of the characteristic-limited states");
     return PG_ERR_INVALID;
   }
+  if (S->cfg.divb == PG_CONSTRAINED_TRANSPORT && S->cfg.emf_average != PG_UCT_HLL) {
+    set_last_error("pg_adjoint_set: the adjoint covers the UCT_HLL emf average");
+    return PG_ERR_INVALID;
+  }
   if (S->cfg.divb == PG_CONSTRAINED_TRANSPORT)
     for (int d = 0; d < S->g.dims; d++)
       if (S->cfg.bc[d] != PG_PERIODIC) {

@@ -79,12 +79,13 @@ int validate_config(const pg_config* c) {
   }
   if (c->divb == PG_CONSTRAINED_TRANSPORT) {
     if (c->dims < 2) return fail(PG_ERR_INVALID, "constrained transport needs dims >= 2");
-    if (is_ctu(c->time_stepping)) {  // Src/MHD/CT/ct_emf.c:196-199
-      if (c->emf_average != PG_ARITHMETIC && c->emf_average != PG_UCT_CONTACT)
-        return fail(PG_ERR_INVALID, "CTU takes the ARITHMETIC or UCT_CONTACT emf average");
-    } else if (c->emf_average != PG_UCT_HLL) {
-      return fail(PG_ERR_INVALID, "RK time stepping takes the UCT_HLL emf average");
-    }
+    if (c->emf_average < PG_ARITHMETIC || c->emf_average > PG_UCT_HLL)
+      return fail(PG_ERR_INVALID, "unsupported emf average");
+    if (is_ctu(c->time_stepping) && c->emf_average == PG_UCT_HLL)  // Src/MHD/CT/ct_emf.c:196-200
+      return fail(PG_ERR_INVALID, "CTU takes the ARITHMETIC, UCT0 or UCT_CONTACT emf average");
+    // the mixed sweeps fuse the UCT_HLL edge data into the sweep kernels
+    if (c->emf_average != PG_UCT_HLL && c->precision != PG_FP64 && c->precision != PG_FP64_TANGENT)
+      return fail(PG_ERR_INVALID, "the ARITHMETIC, UCT0 and UCT_CONTACT averages run on the FP64 path");
 
   } else if (c->divb != PG_DIVB_NONE) {
     return fail(PG_ERR_INVALID, "unsupported divergence control");

@@ -18,9 +18,6 @@
 
 namespace pg {
 
-// face-EMF slots of F64A::EF: ezi, ezj, eyi, eyk, exj, exk
-enum : int { EF_ZI = 0, EF_ZJ, EF_YI, EF_YK, EF_XJ, EF_XK };
-
 // PrimRHS (ideal EOS, no 8-wave / GLM terms): A(v) . dv along DIR
 template <int DIR, class T>
 __device__ __forceinline__ void prim_rhs(const T* v, const T* dv, double gamma, bool c3, T* Adv) {
@@ -266,20 +263,7 @@ __global__ void k_ctu_riemann(F64A<T> a, Box box, int nlo) {
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) a.F[nv][c] = o.f[nv];
     a.P[c] = o.press;
-    if (a.ct) {  // CT_StoreUpwindEMF
-      if (DIR == 0) {
-        a.EF[EF_ZI][c] = -o.f[BX2];
-        if (g.dims == 3) a.EF[EF_YI][c] = o.f[BX3];
-      } else if (DIR == 1) {
-        a.EF[EF_ZJ][c] = o.f[BX1];
-        if (g.dims == 3) a.EF[EF_XJ][c] = -o.f[BX3];
-      } else {
-        a.EF[EF_YK][c] = -o.f[BX1];
-        a.EF[EF_XK][c] = o.f[BX2];
-      }
-      const double fr = value_of(o.f[RHO]);
-      a.SV[DIR][c] = fr > 1.e-6 ? 1 : (fr < -1.e-6 ? -1 : 0);
-    }
+    if (a.ct) store_face_emf<T, DIR>(a, c, o.f);  // CT_StoreUpwindEMF
     const int x = DIR == 0 ? i : (DIR == 1 ? j : k);
     if (x >= nlo) invdt = value_of(o.cmax) * g.inv_dx[DIR];
   }
@@ -343,10 +327,15 @@ __device__ __forceinline__ int ctu_sv(const signed char* sv, const Geom& g, int 
   return sv[cidx(g, k, j, i)];
 }
 
-// Edge EMFs: ARITHMETIC, or UCT_CONTACT (arithmetic sum, then on the
-// corrector the upwind corner integration of Gardiner & Stone, then x 1/4).
-// Each edge adds its four corner-integration terms in the order the
-// reference's loop applies them (ct_emf_average.c:82-156).
+// Edge EMFs (CT_ComputeEMF, Src/MHD/CT/ct_emf.c:210-291): ARITHMETIC;
+// UCT0 (each face EMF replaced by twice itself minus the mean of the
+// centred EMFs of the two zones sharing the face, then the arithmetic
+// average); or UCT_CONTACT (arithmetic sum, then the upwind corner
+// integration of Gardiner & Stone, then x 1/4).  STAGE 1 is the CTU
+// predictor, which skips the corner integration (ct_emf_average.c:89-91);
+// the corrector and every RK stage pass 2.  Each edge adds its four
+// corner-integration terms in the order the reference's loop applies them
+// (ct_emf_average.c:82-156).
 template <class T, int STAGE>
 __global__ void k_ctu_emf(F64A<T> a, Box eb) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
@@ -354,17 +343,24 @@ __global__ void k_ctu_emf(F64A<T> a, Box eb) {
   int i, j, k;
   eb.coords(q, i, j, k);
   const Geom& g = a.g;
-  const bool uct = a.emf_avg == PG_UCT_CONTACT, d3 = g.dims == 3;
+  const bool uct = a.emf_avg == PG_UCT_CONTACT, uct0 = a.emf_avg == PG_UCT0, d3 = g.dims == 3;
   const double w = uct ? 1.0 : 0.25;
   const long long c = cidx(g, k, j, i);
-  T ez = w * (ctu_ef(a, EF_ZI, k, j, i) + ctu_ef(a, EF_ZI, k, j + 1, i) + ctu_ef(a, EF_ZJ, k, j, i) +
-              ctu_ef(a, EF_ZJ, k, j, i + 1));
+  // face EMF of a slot; under UCT0 2 e - (e_c + e_c')/2 (ct_emf.c:261-282)
+  auto fe = [&](int slot, int kk, int jj, int ii) -> T {
+    T f = ctu_ef(a, slot, kk, jj, ii);
+    if (!uct0) return f;
+    const int e = slot <= EF_ZJ ? 2 : (slot <= EF_YK ? 1 : 0);
+    const int di = slot == EF_ZI || slot == EF_YI, dj = slot == EF_ZJ || slot == EF_XJ,
+              dk = slot == EF_YK || slot == EF_XK;
+    f = f * 2.0;
+    return f - 0.5 * (ctu_ecc(a, e, kk, jj, ii) + ctu_ecc(a, e, kk + dk, jj + dj, ii + di));
+  };
+  T ez = w * (fe(EF_ZI, k, j, i) + fe(EF_ZI, k, j + 1, i) + fe(EF_ZJ, k, j, i) + fe(EF_ZJ, k, j, i + 1));
   T ex = T(0.0), ey = T(0.0);
   if (d3) {
-    ex = w * (ctu_ef(a, EF_XK, k, j, i) + ctu_ef(a, EF_XK, k, j + 1, i) + ctu_ef(a, EF_XJ, k, j, i) +
-              ctu_ef(a, EF_XJ, k + 1, j, i));
-    ey = w * (ctu_ef(a, EF_YI, k, j, i) + ctu_ef(a, EF_YI, k + 1, j, i) + ctu_ef(a, EF_YK, k, j, i) +
-              ctu_ef(a, EF_YK, k, j, i + 1));
+    ex = w * (fe(EF_XK, k, j, i) + fe(EF_XK, k, j + 1, i) + fe(EF_XJ, k, j, i) + fe(EF_XJ, k + 1, j, i));
+    ey = w * (fe(EF_YI, k, j, i) + fe(EF_YI, k + 1, j, i) + fe(EF_YK, k, j, i) + fe(EF_YK, k, j, i + 1));
   }
   if (uct && STAGE == 2) {
     // derivative terms (ct_emf_average.c:67-79)

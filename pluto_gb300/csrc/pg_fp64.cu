@@ -70,13 +70,14 @@ int fp64_alloc(Solver* S) {
         if (alloc(&S->Upd[d][nv]) || alloc(&S->Umd[d][nv]) || alloc(&S->Rhd[d][nv])) return PG_ERR_NOMEM;
     for (int nv = 0; nv < 8; nv++)
       if (alloc(&S->Uh[nv])) return PG_ERR_NOMEM;
-    if (ct) {
-      for (int q = 0; q < 6; q++)
-        if (alloc(&S->EF[q])) return PG_ERR_NOMEM;
-      for (int d = 0; d < S->g.dims; d++) {
-        if (cudaMalloc(&S->SV[d], n) != cudaSuccess) return PG_ERR_NOMEM;
-        cudaMemset(S->SV[d], 0, n);
-      }
+  }
+  // face EMFs and mass-flux signs: CTU, and RK with the ARITHMETIC/UCT0/UCT_CONTACT averages
+  if (ct && (is_ctu(S->cfg.time_stepping) || S->cfg.emf_average != PG_UCT_HLL)) {
+    for (int q = 0; q < 6; q++)
+      if (alloc(&S->EF[q])) return PG_ERR_NOMEM;
+    for (int d = 0; d < S->g.dims; d++) {
+      if (cudaMalloc(&S->SV[d], n) != cudaSuccess) return PG_ERR_NOMEM;
+      cudaMemset(S->SV[d], 0, n);
     }
   }
   if (cudaMalloc(&S->flag, n) != cudaSuccess) return PG_ERR_NOMEM;

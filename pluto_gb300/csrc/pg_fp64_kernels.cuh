@@ -53,6 +53,28 @@ struct F64A {
   int char_lim;     // CHAR_LIMITING YES: PLM limited in characteristic variables
 };
 
+// face-EMF slots of F64A::EF: ezi, ezj, eyi, eyk, exj, exk
+enum : int { EF_ZI = 0, EF_ZJ, EF_YI, EF_YK, EF_XJ, EF_XK };
+
+// CT_StoreUpwindEMF (Src/MHD/CT/ct_emf.c:104-190) for the ARITHMETIC, UCT0
+// and UCT_CONTACT averages: the EMF components of the face flux and the sign
+// of its mass flux (the UCT_CONTACT upwind direction, threshold 1e-6).
+template <class T, int DIR>
+__device__ __forceinline__ void store_face_emf(const F64A<T>& a, long long c, const T* f) {
+  if (DIR == 0) {
+    a.EF[EF_ZI][c] = -f[BX2];
+    if (a.g.dims == 3) a.EF[EF_YI][c] = f[BX3];
+  } else if (DIR == 1) {
+    a.EF[EF_ZJ][c] = f[BX1];
+    if (a.g.dims == 3) a.EF[EF_XJ][c] = -f[BX3];
+  } else {
+    a.EF[EF_YK][c] = -f[BX1];
+    a.EF[EF_XK][c] = f[BX2];
+  }
+  const double fr = value_of(f[RHO]);
+  a.SV[DIR][c] = fr > 1.e-6 ? 1 : (fr < -1.e-6 ? -1 : 0);
+}
+
 __device__ __forceinline__ void atomic_max_nonneg(unsigned long long* addr, double v) {
   // Non-negative doubles (and NaN) order like their bit patterns.
   atomicMax(addr, (unsigned long long)__double_as_longlong(v));
@@ -280,6 +302,7 @@ __global__ void k_riemann(F64A<T> a, Box box, int want_invdt_1d) {
     if (a.ct) {
       a.SL[DIR][c] = pmax(T(0.0), -o.SL);
       a.SR[DIR][c] = pmax(T(0.0), o.SR);
+      if (a.emf_avg != PG_UCT_HLL) store_face_emf<T, DIR>(a, c, o.f);
     }
     if (want_invdt_1d) invdt = value_of(o.cmax) * g.inv_dx[DIR];  // update_stage.c:237-241
   }
@@ -600,6 +623,10 @@ static void launch_sweep(Solver* S, const F64A<T>& a, int stage) {
   PG_LAUNCH(S, "fp64_update", (k_update<T, DIR><<<grid_for(ub.count()), kThreads, 0, st>>>(a, ub, cdt_mode)));
 }
 
+// edge EMFs from the stored face EMFs (pg_ctu.cuh)
+template <class T, int STAGE>
+__global__ void k_ctu_emf(F64A<T> a, Box eb);
+
 template <class T, int STAGE, int NSTAGE>
 static void launch_stage_tail(Solver* S, const F64A<T>& a, const Box& dom) {
   const Geom& g = S->g;
@@ -610,7 +637,10 @@ static void launch_stage_tail(Solver* S, const F64A<T>& a, const Box& dom) {
       if (ax < g.dims) { eb.lo[ax] = g.beg[ax] - 1; eb.hi[ax] = g.end[ax]; }
       else { eb.lo[ax] = eb.hi[ax] = 0; }
     }
-    PG_LAUNCH(S, "fp64_emf", (k_emf<T><<<grid_for(eb.count(), 128), 128, 0, st>>>(a, eb)));
+    if (a.emf_avg == PG_UCT_HLL)
+      PG_LAUNCH(S, "fp64_emf", (k_emf<T><<<grid_for(eb.count(), 128), 128, 0, st>>>(a, eb)));
+    else  // every RK stage integrates to the corner like the CTU corrector (no CTU guard)
+      PG_LAUNCH(S, "fp64_emf", (k_ctu_emf<T, 2><<<grid_for(eb.count(), 128), 128, 0, st>>>(a, eb)));
     PG_LAUNCH(S, "fp64_ct_update", (k_ct_update<T, STAGE, NSTAGE><<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb)));
   }
   int reduce = (STAGE == 1 && g.dims > 1);

@@ -125,6 +125,8 @@ static void gpu_config(pg_config *c, Riemann_Solver *Riemann, Grid *grid)
   c->emf_average = PG_ARITHMETIC;
   #elif CT_EMF_AVERAGE == UCT_CONTACT
   c->emf_average = PG_UCT_CONTACT;
+  #elif CT_EMF_AVERAGE == UCT0
+  c->emf_average = PG_UCT0;
   #else
   c->emf_average = PG_UCT_HLL;
   #endif

@@ -26,7 +26,8 @@ RIEMANN = {"hll": L.PG_HLL, "hlld": L.PG_HLLD, "roe": L.PG_ROE}
 STEPPING = {"EULER": L.PG_EULER, "RK2": L.PG_RK2, "RK3": L.PG_RK3, "HANCOCK": L.PG_HANCOCK,
             "CHARACTERISTIC_TRACING": L.PG_CHAR_TRACING}
 CTU_STEPPING = ("HANCOCK", "CHARACTERISTIC_TRACING")
-EMF = {"ARITHMETIC": L.PG_ARITHMETIC, "UCT_CONTACT": L.PG_UCT_CONTACT, "UCT_HLL": L.PG_UCT_HLL}
+EMF = {"ARITHMETIC": L.PG_ARITHMETIC, "UCT0": L.PG_UCT0, "UCT_CONTACT": L.PG_UCT_CONTACT,
+       "UCT_HLL": L.PG_UCT_HLL}
 BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW, "reflective": L.PG_REFLECTIVE,
       "eqtsymmetric": L.PG_EQTSYMMETRIC, "userdef": L.PG_USERDEF}
 PRECISION = {"fp64": L.PG_FP64, "mixed": L.PG_MIXED, "mixed_dw": L.PG_MIXED_DW,

@@ -232,6 +232,16 @@ def setups():
                 stepping="CHARACTERISTIC_TRACING", emf="UCT_CONTACT", name="ot_ppm_chtr_charlim_32"),
         replace(br.blast_setup(16, 12), recon="PARABOLIC", char_limiting=True, stepping="CHARACTERISTIC_TRACING",
                 emf="ARITHMETIC", bc="outflow", name="blast_ppm_chtr_charlim_16"),
+        # the other CT_EMF_AVERAGE choices: ARITHMETIC, UCT_CONTACT and UCT0 under RK; UCT0 under CTU
+        replace(br.ot_setup("hlld", 32, 30), emf="UCT_CONTACT", name="ot_uctc_32"),
+        replace(br.ot_setup("roe", 32, 30), emf="ARITHMETIC", name="ot_arith_roe_32"),
+        replace(br.ot_setup("hlld", 32, 30), emf="UCT0", name="ot_uct0_32"),
+        replace(br.blast_setup(16, 12), emf="UCT0", name="blast_uct0_16"),
+        replace(br.turb_setup(12, 10), emf="UCT_CONTACT", name="turb_uctc_12"),
+        replace(br.cpa_setup(32, 20), emf="ARITHMETIC", bc="outflow", name="cpa_arith_outflow_32"),
+        replace(br.ot_setup("hlld", 32, 30), stepping="HANCOCK", emf="UCT0", name="ot_ctu_uct0_32"),
+        replace(br.blast_setup(16, 12), stepping="CHARACTERISTIC_TRACING", emf="UCT0",
+                name="blast_chtr_uct0_16"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

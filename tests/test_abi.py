@@ -91,6 +91,25 @@ def test_char_tracing_validation(lib, extra, ok):
         lib.pg_destroy(h)
 
 
+@pytest.mark.parametrize("stepping,emf,precision,ok", [
+    ("RK2", "UCT_HLL", "fp64", True), ("RK2", "ARITHMETIC", "fp64", True), ("RK3", "UCT0", "fp64", True),
+    ("EULER", "UCT_CONTACT", "fp64", True), ("RK2", "UCT0", "fp64_tangent", True),
+    ("RK2", "UCT_HLL", "mixed", True), ("RK2", "UCT_CONTACT", "mixed", False), ("RK2", "UCT0", "mixed_dw", False),
+    ("HANCOCK", "UCT0", "fp64", True), ("HANCOCK", "UCT_HLL", "fp64", False),
+    ("CHARACTERISTIC_TRACING", "UCT0", "fp64", True)])
+def test_emf_average_validation(lib, stepping, emf, precision, ok):
+    """CT_EMF_AVERAGE: all four averages under RK (ARITHMETIC, UCT0 and
+    UCT_CONTACT on the FP64 and tangent-linear builds only), every one but
+    UCT_HLL under CTU (Src/MHD/CT/ct_emf.c:196-200)."""
+    spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1), gamma=5 / 3, ct=True,
+                stepping=stepping, emf=emf)
+    h = C.c_void_p()
+    rc = lib.pg_create(C.byref(make_config(spec, precision)), C.byref(h))
+    assert (rc != 1) == ok, lib.pg_last_error()
+    if rc == 0:
+        lib.pg_destroy(h)
+
+
 @pytest.mark.parametrize("extra,precision,ok", [({}, "fp64", True), ({"recon": "PARABOLIC"}, "fp64", True),
                                                  ({}, "mixed", False), ({}, "fp64_tangent", False),
                                                  ({"stepping": "HANCOCK"}, "fp64", True),

@@ -178,11 +178,16 @@ def test_adjoint_dot_product(name):
     assert abs(lhs - rhs) <= 1e-11 * max(abs(lhs), abs(rhs)), (lhs, rhs)
 
 
-@pytest.mark.parametrize("name", ["cpa2d_plm_hlld", "turb3d_ppm_hlld"])
-def test_tangent_matches_central_differences(name):
+@pytest.mark.parametrize("name,emf", [("cpa2d_plm_hlld", None), ("turb3d_ppm_hlld", None),
+                                     ("cpa2d_plm_hlld", "UCT0"), ("cpa2d_plm_hlld", "ARITHMETIC")])
+def test_tangent_matches_central_differences(name, emf):
+    """Tangent-linear step against central differences; also with the UCT0
+    and ARITHMETIC edge averages of the RK path (no branch of their own)."""
     from pluto_gb300 import Solver
     from pluto_gb300.adjoint import tangent_linear
     spec, vc, f, dts = _case(name)
+    if emf:
+        spec = dict(spec, emf=emf)
     f = _faces(spec, f)
     vc = _smooth(vc)
     rng = np.random.default_rng(5)

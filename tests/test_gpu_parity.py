@@ -144,6 +144,35 @@ def test_fp64_vs_oracle_outflow_ct_3d(bc):
         assert np.array_equal(ab[d], bb[d])
 
 
+@pytest.mark.parametrize("emf,solver,stepping,bc", [
+    ("ARITHMETIC", "hlld", "RK2", "periodic"),
+    ("UCT_CONTACT", "roe", "RK3", "periodic"),
+    ("UCT0", "hll", "RK2", "periodic"),
+    ("UCT_CONTACT", "hlld", "RK2", [("reflective", "outflow"), "periodic", ("outflow", "eqtsymmetric")]),
+    ("UCT0", "hlld", "EULER", ["outflow", "outflow", "periodic"]),
+    ("ARITHMETIC", "roe", "RK2", [("userdef", "outflow"), "periodic", ("reflective", "userdef")])])
+def test_rk_emf_averages_vs_oracle_random_3d(emf, solver, stepping, bc):
+    """RK time stepping with the ARITHMETIC, UCT0 and UCT_CONTACT edge
+    averages (face EMFs stored by the Riemann kernel, corner integration in
+    every stage) on a random 3D state against the oracle, bit for bit."""
+    from oracle.oracle import Oracle
+    spec, vc, bs = _random_blast(16, seed=21)
+    spec.update(emf=emf, solver=solver, stepping=stepping, bc=bc)
+    s = _solver(spec)
+    o = Oracle(spec, nthreads=4)
+    if userdef_cases.has_userdef(spec):
+        o.set_userdef(userdef_cases.make(spec))
+    s.upload(vc, bs)
+    o.set_state(vc, bs)
+    s.run(4, 1e-3, 0.3)
+    o.run(4, 1e-3, 0.3)
+    a, ab = s.download()
+    b, bb = o.get_state()
+    assert np.array_equal(a, b), _errors(a, ab, b, bb)
+    for d in range(3):
+        assert np.array_equal(ab[d], bb[d])
+
+
 def test_divergence_free_under_ct():
     spec, vc, bs = _random_blast(24, seed=3)
     s = _solver(spec)
@@ -195,7 +224,9 @@ def test_nan_state_reported_not_trapped():
                                            ("ARITHMETIC", "roe", [("outflow", "reflective"), "periodic",
                                                                   ("eqtsymmetric", "outflow")]),
                                            ("UCT_CONTACT", "hlld", [("userdef", "outflow"), "periodic",
-                                                                    ("outflow", "userdef")])])
+                                                                    ("outflow", "userdef")]),
+                                           ("UCT0", "hlld", "periodic"),
+                                           ("UCT0", "roe", [("outflow", "reflective"), "periodic", "outflow"])])
 def test_ctu_vs_oracle_random_3d(emf, solver, bc):
     """CTU (primitive Hancock predictor, corner-coupled corrector) with CT on a
     random 3D state against the oracle, bit for bit."""
@@ -308,11 +339,14 @@ def test_char_tracing_without_ct_vs_oracle_3d():
     assert np.array_equal(a, b)
 
 
-def test_ctu_tangent_value_part_is_the_fp64_step():
-    from pluto_gb300 import Solver
+@pytest.mark.parametrize("stepping,emf", [("HANCOCK", "UCT_CONTACT"), ("HANCOCK", "UCT0"), ("RK2", "UCT_CONTACT"),
+                                          ("RK3", "UCT0"), ("RK2", "ARITHMETIC")])
+def test_ctu_tangent_value_part_is_the_fp64_step(stepping, emf):
+    """The value part of the tangent-linear build (dual numbers) is the
+    plain FP64 step, for CTU and for RK with the non-UCT_HLL averages."""
     from pluto_gb300.adjoint import tangent_linear
     spec, vc, bs = _random_blast(12, seed=4)
-    spec.update(stepping="HANCOCK", emf="UCT_CONTACT")
+    spec.update(stepping=stepping, emf=emf)
     s = _solver(spec)
     s.upload(vc, bs)
     dts = [1e-3] * 3
