@@ -317,6 +317,99 @@ def adjoint_timing():
             "timing": "host clock around synchronous C-ABI calls (one pg_advance per step)"}
 
 
+def turbulence_leg(args):
+    """Decaying MHD turbulence (768^3 periodic on [0,1]^3, rho = p = 1,
+    random-phase solenoidal v and A with E(k) ~ k^-2 on shells 1..4, rms Mach
+    1, plasma beta 10; PPM + HLLD + RK3 + CT (UCT_HLL), CFL 0.3): the mixed
+    path at full size (zone-updates/s, algorithmic HBM GB/s), the plain FP64
+    path at full size when it fits in device memory (else at the L1 grid),
+    and the per-variable L1 error of both mixed forms against FP64 after
+    ``turb_l1_steps`` steps on a ``turb_l1_n``^3 copy of the same problem."""
+    import torch
+    from pluto_gb300 import Solver, problems
+    n = args.turb_n
+    # the initial state is built in host memory (~140 B per zone at its peak)
+    try:
+        avail = int(next(l for l in open("/proc/meminfo") if l.startswith("MemAvailable")).split()[1]) * 1024
+    except Exception:
+        avail = None
+    host_note = None
+    while avail is not None and avail < 160 * n ** 3 and n > 128:
+        n //= 2
+        host_note = f"grid reduced to {n}^3: {avail / 1e9:.0f} GB of host memory available"
+    spec, vc, faces = problems.turbulence3d(n)
+    cfl, first_dt = spec["cfl"], spec["first_dt"]
+    cells = n ** 3
+    mx = Solver(spec, precision="mixed")
+    mx.upload(vc, faces)
+    mx.run(args.warmup, first_dt, cfl)
+    launches = mx.launches_per_step()
+    with Clocks(int(os.environ.get("LOCAL_RANK", "0"))) as clk:
+        ms = mx.run_timed(args.steps, 0.0, cfl)
+    value = cells * args.steps / (ms / 1e3)
+    prof = mx.profile_kernels(1, 0.0, cfl)
+    info = mx.info()
+    del mx
+    torch.cuda.empty_cache()
+    # plain FP64 path: 75 doubles + 1 flag byte per zone of the ghosted grid
+    ng = 3
+    need = 601 * (n + 2 * ng) ** 3
+    free = torch.cuda.mem_get_info()[0]
+    n64 = n if free > 1.05 * need else args.turb_l1_n
+    if n64 != n:
+        spec64, vc64, faces64 = problems.turbulence3d(n64)
+    else:
+        spec64, vc64, faces64 = spec, vc, faces
+    f64 = Solver(spec64, precision="fp64")
+    f64.upload(vc64, faces64)
+    f64.run(1, first_dt, cfl)
+    ms64 = f64.run_timed(args.fp64_steps, 0.0, cfl)
+    value64 = n64 ** 3 * args.fp64_steps / (ms64 / 1e3)
+    del f64, vc64, faces64
+    del vc, faces
+    # L1 of mixed vs FP64 from the same initial state
+    nl = args.turb_l1_n
+    spec_l, vc_l, faces_l = problems.turbulence3d(nl)
+    a = Solver(spec_l, precision="fp64")
+    a.upload(vc_l, faces_l)
+    a.run(args.turb_l1_steps, first_dt, cfl)
+    ra, rb = a.download()
+    del a
+    names = ["rho", "vx1", "vx2", "vx3", "Bx1", "Bx2", "Bx3", "prs"]
+    l1 = {"steps": args.turb_l1_steps, "grid": nl, "bar": 1e-5}
+    for prec in ("mixed", "mixed_dw"):
+        b = Solver(spec_l, precision=prec)
+        b.upload(vc_l, faces_l)
+        b.run(args.turb_l1_steps, first_dt, cfl)
+        ma, mb = b.download()
+        del b
+        per = {names[q]: rel_l1(ma[q], ra[q]) for q in range(8)}
+        for d in range(3):
+            per[f"Bx{d+1}s"] = rel_l1(mb[d], rb[d])
+        l1[prec] = {"per_variable": per, "max": max(per.values())}
+    peak = PEAKS.get("hbm_gbs", 6782.1)
+    algo = 8 * 11 * 4  # RK3: 8W FP32 words per zone-update, W = NVAR + DIMENSIONS = 11
+    dom = max(prof, key=lambda k: prof[k][0])
+    return {
+        "metric": "MHD zone-updates/s on 1 GB300 (3D decaying turbulence)", "value": value,
+        "unit": "zone-updates/s", "n_gpus": 1, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": ms / args.steps, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+        "dtype": "f32 storage/fluxes + f64 accumulation",
+        "data": "synthetic (seeded random-phase spectrum generated in-process)",
+        "config": {"workload": f"3D decaying MHD turbulence {n}^3 periodic, PPM + HLLD + RK3 + CT(UCT_HLL), "
+                               "CFL 0.3", "grid": [n, n, n], "precision": "mixed",
+                   "l2": "inputs larger than L2, no flush needed", "host_note": host_note},
+        "hbm_algorithmic": {"bytes_per_zone_update": algo, "achieved_gbs": value * algo / 1e9,
+                            "frac": value * algo / 1e9 / peak, "peak_gbs": peak, "peak_source": PEAK_SRC},
+        "fp64": {"value": value64, "grid": n64, "steps": args.fp64_steps, "ms_per_step": ms64 / args.fp64_steps,
+                 "speedup_mixed_over_fp64": value / value64},
+        "l1_mixed_vs_fp64": l1,
+        "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()}, "dominant_kernel": dom,
+        "gpu_launches": launches * args.steps, "floors_in_run": info.get("nfail"),
+        "clocks": clk.summary(),
+    }
+
+
 def output_timing(n=256, outputs=4, steps_between=50):
     """The device output path (pg_write_output, .dbl single file) against
     download-then-write through the C ABI, on the mixed 3D blast at n^3:
@@ -412,6 +505,11 @@ def main():
     ap.add_argument("--no-batch", action="store_true")
     ap.add_argument("--no-adjoint", action="store_true")
     ap.add_argument("--no-output", action="store_true")
+    ap.add_argument("--turbulence", action="store_true",
+                    help="print the decaying-turbulence line (PPM/RK3, --turb-n^3) instead of the blast line")
+    ap.add_argument("--turb-n", type=int, default=768)
+    ap.add_argument("--turb-l1-n", type=int, default=256)
+    ap.add_argument("--turb-l1-steps", type=int, default=50)
     args = ap.parse_args()
     rank, ws = dist_init()
     if args.impl == "reference":
@@ -422,6 +520,10 @@ def main():
     from pluto_gb300 import Solver, problems
     from pluto_gb300 import build as pbuild
     pbuild.build()
+    if args.turbulence:
+        if rank == 0:
+            print(json.dumps(turbulence_leg(args)), flush=True)
+        return
 
     n = args.n
     spec, vc, faces = problems.blast3d(n)

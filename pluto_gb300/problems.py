@@ -144,9 +144,55 @@ def riemann_tube(n, seed, gamma=2.0):
     return spec, vc, [None, None, None]
 
 
-def turbulence3d(n=768, seed=0, kmin=1, kmax=4, mach=1.0, beta=10.0):
+def _modes_on_grid(modes, n, which, comp, shift):
+    """sum over the modes of amp * vec[comp] * cos(2 pi k.x + phase) at the
+    points x = j dx + shift (j = 0..n-1 per axis, array [z][y][x]), by one
+    inverse FFT of the mode coefficients (cuFFT on the device when there is
+    one, else numpy); equal to the direct sum up to round-off."""
+    dx = 1.0 / n
+    coef = {}
+    for kv, amp, a1, ph1, a2, ph2 in modes:
+        if which == "v":
+            c = amp * a1[comp] * np.exp(1j * ph1)
+        else:
+            c = amp * a2[comp] / np.linalg.norm(kv) * np.exp(1j * ph2)
+        c *= np.exp(2j * np.pi * float(kv @ np.asarray(shift)))
+        idx = (int(kv[2]) % n, int(kv[1]) % n, int(kv[0]) % n)
+        coef[idx] = coef.get(idx, 0.0) + c
+    try:
+        import torch
+        dev = "cuda" if torch.cuda.is_available() else None
+    except Exception:
+        dev = None
+    if dev:
+        F = torch.zeros((n, n, n), dtype=torch.complex128, device=dev)
+        ii = torch.tensor(list(coef.keys()), dtype=torch.long, device=dev)
+        F[ii[:, 0], ii[:, 1], ii[:, 2]] = torch.tensor(list(coef.values()), dtype=torch.complex128, device=dev)
+        out = torch.fft.ifftn(F, norm="forward").real.cpu().numpy()
+        del F, ii
+        torch.cuda.empty_cache()
+        return out
+    F = np.zeros((n, n, n), dtype=np.complex128)
+    for idx, c in coef.items():
+        F[idx] = c
+    return np.fft.ifftn(F, norm="forward").real
+
+
+def _wrap(a, axes):
+    """append the first layer along each periodic axis (face/edge grids of n+1 points)"""
+    for ax in axes:
+        a = np.concatenate([a, np.take(a, [0], axis=ax)], axis=ax)
+    return a
+
+
+def turbulence3d(n=768, seed=0, kmin=1, kmax=4, mach=1.0, beta=10.0, fft=None):
     """Decaying MHD turbulence: random-phase solenoidal v and vector potential
-    A with E(k) ~ k^-2 on shells kmin<=|k|<=kmax; B = curl A on the faces."""
+    A with E(k) ~ k^-2 on shells kmin<=|k|<=kmax; B = curl A on the faces.
+    fft (default: n >= 64) evaluates the mode sums by inverse FFT instead of
+    term by term (the same fields up to round-off; the term-by-term sum takes
+    hours at 768^3)."""
+    if fft is None:
+        fft = n >= 64
     rng = np.random.default_rng(seed)
     dx = 1.0 / n
     ks = [(kx, ky, kz) for kx in range(-kmax, kmax + 1) for ky in range(-kmax, kmax + 1)
@@ -176,32 +222,45 @@ def turbulence3d(n=768, seed=0, kmin=1, kmax=4, mach=1.0, beta=10.0):
                     np.cos(tp * (kv[0] * X + kv[1] * Y + kv[2] * Z) + ph2)
         return out
 
-    Zc, Yc, Xc = np.meshgrid(x, x, x, indexing="ij")
-    v = field((Xc, Yc, Zc), "v")
+    if fft:
+        h = 0.5 * dx
+        v = np.stack([_modes_on_grid(modes, n, "v", c, (h, h, h)) for c in range(3)])
+        ax = _wrap(_modes_on_grid(modes, n, "a", 0, (h, 0.0, 0.0)), (0, 1))
+        ay = _wrap(_modes_on_grid(modes, n, "a", 1, (0.0, h, 0.0)), (0, 2))
+        az = _wrap(_modes_on_grid(modes, n, "a", 2, (0.0, 0.0, h)), (1, 2))
+    else:
+        Zc, Yc, Xc = np.meshgrid(x, x, x, indexing="ij")
+        v = field((Xc, Yc, Zc), "v")
+        del Zc, Yc, Xc
     cs = math.sqrt(5.0 / 3.0)
     v *= mach * cs / math.sqrt((v ** 2).sum(0).mean())
     # edge-centred A components: Ax at (i, j+1/2, k+1/2), Ay at (i+1/2, j, k+1/2), Az at (i+1/2, j+1/2, k)
-    Z, Y, X = np.meshgrid(xe, xe, x, indexing="ij")
-    ax = field((X, Y, Z), "a")[0]
-    Z, Y, X = np.meshgrid(xe, x, xe, indexing="ij")
-    ay = field((X, Y, Z), "a")[1]
-    Z, Y, X = np.meshgrid(x, xe, xe, indexing="ij")
-    az = field((X, Y, Z), "a")[2]
+    if not fft:
+        Z, Y, X = np.meshgrid(xe, xe, x, indexing="ij")
+        ax = field((X, Y, Z), "a")[0]
+        Z, Y, X = np.meshgrid(xe, x, xe, indexing="ij")
+        ay = field((X, Y, Z), "a")[1]
+        Z, Y, X = np.meshgrid(x, xe, xe, indexing="ij")
+        az = field((X, Y, Z), "a")[2]
+        del Z, Y, X
     # faces: bx = dAz/dy - dAy/dz at (i+1/2, j, k) etc.
     bx = (az[:, 1:, :] - az[:, :-1, :]) / dx - (ay[1:, :, :] - ay[:-1, :, :]) / dx
     by = (ax[1:, :, :] - ax[:-1, :, :]) / dx - (az[:, :, 1:] - az[:, :, :-1]) / dx
     bz = (ay[:, :, 1:] - ay[:, :, :-1]) / dx - (ax[:, 1:, :] - ax[:, :-1, :]) / dx
+    del ax, ay, az
     faces = [bx, by, bz]
     cb = _cell_b(faces, 3)
     brms2 = float(sum((c ** 2).mean() for c in cb))
+    del cb
     scale = math.sqrt(2.0 * 1.0 / beta / brms2)
-    faces = [f * scale for f in faces]
+    for f in faces:
+        f *= scale
     vc = np.zeros((8, n, n, n))
     vc[0] = 1.0
     vc[7] = 1.0
     vc[1:4] = v
-    cb = _cell_b(faces, 3)
-    vc[4], vc[5], vc[6] = cb
+    del v
+    vc[4], vc[5], vc[6] = _cell_b(faces, 3)
     spec = dict(name=f"turb3d_{n}", dims=3, components=3, nx=(n, n, n), dx=(dx, dx, dx),
                 gamma=5.0 / 3.0, recon="PARABOLIC", limiter="MC_LIM", solver="hlld",
                 stepping="RK3", ct=True, bc="periodic", cfl=0.3, first_dt=1e-4)
