@@ -82,9 +82,16 @@ def test_tma_sweeps_match_plain_sweeps(case, prec, monkeypatch):
     assert max(errs.values()) <= 1e-6, errs
 
 
-# the CTU step (TIME_STEPPING HANCOCK) runs on the FP64 path only
-# CHAR_LIMITING runs on the plain FP64 path only
-RK_GOLDENS = [n for n in GOLDEN_NAMES if "_ctu" not in n and "_chtr" not in n and "charlim" not in n]
+def _mixed_scheme(name):
+    """the mixed solvers take RK time stepping without CHAR_LIMITING and, under
+    CT, the UCT_HLL edge average (CTU, characteristic limiting and the other
+    averages run on the FP64 path)"""
+    meta = load_golden(name)[0]
+    return (meta["stepping"] in ("EULER", "RK2", "RK3") and not meta.get("char_limiting")
+            and (not meta["ct"] or meta.get("emf", "UCT_HLL") == "UCT_HLL"))
+
+
+RK_GOLDENS = [n for n in GOLDEN_NAMES if _mixed_scheme(n)]
 
 
 @pytest.mark.parametrize("prec", MIXED)
