@@ -47,11 +47,13 @@ enum { PG_FLAT_LIM = 0, PG_MINMOD_LIM = 1, PG_VANLEER_LIM = 2,
        PG_MC_LIM = 3, PG_DEFAULT_LIM = 4 };                       /* LIMITER */
 enum { PG_HLL = 0, PG_HLLD = 1, PG_ROE = 2 };                     /* [Solver] */
 enum { PG_EULER = 1, PG_RK2 = 2, PG_RK3 = 3,                      /* TIME_STEPPING */
-       PG_HANCOCK = 4, PG_CHAR_TRACING = 5 };
+       PG_HANCOCK = 4, PG_CHAR_TRACING = 5, PG_HANCOCK_CONS = 6 };
 /* EULER: the RK predictor alone (rk_step.c); HANCOCK: CTU (ctu_step.c) with the
    primitive MUSCL-Hancock predictor; CHAR_TRACING: TIME_STEPPING
    CHARACTERISTIC_TRACING, CTU with the characteristic tracing predictor
-   (char_tracing.c, linear reconstruction) */
+   (char_tracing.c, linear reconstruction); HANCOCK_CONS: TIME_STEPPING
+   HANCOCK with PRIMITIVE_HANCOCK NO, CTU with the conservative MUSCL-Hancock
+   predictor (hancock.c:159-434) */
 enum { PG_DIVB_NONE = 0, PG_CONSTRAINED_TRANSPORT = 1 };          /* DIVB_CONTROL */
 enum { PG_ARITHMETIC = 1, PG_UCT0 = 2, PG_UCT_CONTACT = 3, PG_UCT_HLL = 4 }; /* CT_EMF_AVERAGE */
 enum { PG_PERIODIC = 0, PG_OUTFLOW = 1, PG_REFLECTIVE = 2,

@@ -64,7 +64,7 @@ class Setup:
     components: int
     recon: str = "LINEAR"          # LINEAR | PARABOLIC
     limiter: str = "MC_LIM"
-    stepping: str = "RK2"          # RK2 | RK3
+    stepping: str = "RK2"          # EULER | RK2 | RK3 | HANCOCK | CHARACTERISTIC_TRACING | HANCOCK_CONS
     ct: bool = True
     emf: str = "UCT_HLL"
     vecpot: bool = False
@@ -95,7 +95,8 @@ def definitions_h(s: Setup) -> str:
         ("PHYSICS", "MHD"), ("DIMENSIONS", s.dims), ("COMPONENTS", s.components),
         ("GEOMETRY", "CARTESIAN"), ("BODY_FORCE", "NO"), ("FORCED_TURB", "NO"),
         ("COOLING", "NO"), ("RECONSTRUCTION", s.recon),
-        ("TIME_STEPPING", s.stepping), ("DIMENSIONAL_SPLITTING", "NO"),
+        ("TIME_STEPPING", "HANCOCK" if s.stepping == "HANCOCK_CONS" else s.stepping),
+        ("DIMENSIONAL_SPLITTING", "NO"),
         ("NTRACER", 0), ("USER_DEF_PARAMETERS", len(s.params)),
         ("EOS", "IDEAL"), ("ENTROPY_SWITCH", "NO"),
         ("DIVB_CONTROL", "CONSTRAINED_TRANSPORT" if s.ct else "NO"),
@@ -115,6 +116,8 @@ def definitions_h(s: Setup) -> str:
     out.append(f"#define  LIMITER                        {s.limiter}")
     if s.char_limiting:
         out.append("#define  CHAR_LIMITING                  YES")
+    if s.stepping == "HANCOCK_CONS":  # the conservative MUSCL-Hancock predictor (pluto.h:484-495)
+        out.append("#define  PRIMITIVE_HANCOCK              NO")
     if s.ct:
         out.append(f"#define  CT_EMF_AVERAGE                 {s.emf}")
         out.append(f"#define  ASSIGN_VECTOR_POTENTIAL        {'YES' if s.vecpot else 'NO'}")
@@ -234,7 +237,7 @@ def build(s: Setup, jobs: int = 8) -> Path:
     names += ["plm_states"] if s.recon == "LINEAR" else ["ppm_states", "ppm_coeffs"]
     # time stepping: RK (rk_step + update_stage) or CTU (ctu_step + hancock,
     # or char_tracing for CHARACTERISTIC_TRACING)
-    if s.stepping == "HANCOCK":
+    if s.stepping in ("HANCOCK", "HANCOCK_CONS"):
         names += ["ctu_step", "hancock"]
     elif s.stepping == "CHARACTERISTIC_TRACING":
         names += ["ctu_step", "char_tracing"]

@@ -1777,6 +1777,44 @@ static void ctu_sweep(oc_problem *p, int dir, double dt, int stage, double *inv_
               w.vp[i][r.bn] = w.bn[i];
               w.vm[i + 1][r.bn] = w.bn[i];
             }
+        } else if (p->c.stepping == OC_HANCOCK_CONS) {
+          /* conservative Hancock step (PRIMITIVE_HANCOCK NO), hancock.c:159-434:
+             each zone's own interface states evolved by dt/2 with the
+             difference of their fluxes; where U^{n+1/2} fails ConsToPrim the
+             zone falls back to first order */
+          const double dtdx = dt2 / dxd;
+          for (i = nbeg - 1; i <= nend + 1; i++) {
+            double uc[NV], uL[NV], uR[NV], fp[NV], fm[NV], uh[NV], vh[NV], pp, pm;
+            unsigned char fl = 0;
+            prim_to_cons(w.v[i], uc, gmm1);
+            prim_to_cons(w.vp[i], uL, gmm1);
+            prim_to_cons(w.vm[i], uR, gmm1);
+            flux(w.vp[i], uL, fp, &pp, &r);
+            flux(w.vm[i], uR, fm, &pm, &r);
+            for (nv = 0; nv < NV; nv++) {
+              double rhs = -dtdx * (fp[nv] - fm[nv]);
+              if (nv == r.vn) rhs -= dtdx * (pp - pm);
+              uh[nv] = uc[nv] + rhs;
+            }
+            cons_to_prim(uh, vh, gmm1, &fl);
+            if (fl) {
+              for (nv = 0; nv < NV; nv++) vh[nv] = w.vp[i][nv] = w.vm[i][nv] = w.v[i][nv];
+              if (ct) { w.vp[i][r.bn] = w.bn[i]; w.vm[i][r.bn] = w.bn[i - 1]; }
+            }
+            for (nv = 0; nv < NV; nv++) {
+              double P1 = w.vp[i][nv] - w.vm[i][nv], dvp, dvm;
+              dvp = dvm = vh[nv] - w.v[i][nv];
+              dvp += 0.5 * P1;
+              dvm -= 0.5 * P1;
+              w.vp[i][nv] = w.v[i][nv] + dvp;
+              w.vm[i][nv] = w.v[i][nv] + dvm;
+            }
+          }
+          if (ct)
+            for (i = nbeg - 2; i <= nend + 1; i++) {
+              w.vp[i][r.bn] = w.bn[i];
+              w.vm[i + 1][r.bn] = w.bn[i];
+            }
         } else {
           for (i = nbeg - 1; i <= nend + 1; i++) { /* primitive Hancock step */
             double dv[NV], Adv[NV];
@@ -1865,7 +1903,7 @@ static void ctu_sweep(oc_problem *p, int dir, double dt, int stage, double *inv_
         w.rhs[i][r.vn] -= scrh * (w.ifc[i].press - w.ifc[i - 1].press);
       }
       if (stage == 1) {
-        if (ct) { /* CTU_CT_Source */
+        if (ct && p->c.stepping != OC_HANCOCK_CONS) { /* CTU_CT_Source (ctu_step.c:122-133) */
           const double dt2_dx = dt2 / dxd;
           for (i = nbeg - 1; i <= nend + 1; i++) {
             double db = dt2_dx * (w.up[i][r.bn] - w.um[i][r.bn]), scrh;

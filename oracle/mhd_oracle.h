@@ -26,10 +26,11 @@ enum { OC_RHO = 0, OC_VX1, OC_VX2, OC_VX3, OC_BX1, OC_BX2, OC_BX3, OC_PRS, OC_NV
 enum { OC_LINEAR = 0, OC_PARABOLIC = 1 };
 enum { OC_FLAT_LIM = 0, OC_MINMOD_LIM, OC_VANLEER_LIM, OC_MC_LIM, OC_DEFAULT_LIM };
 enum { OC_HLL = 0, OC_HLLD = 1, OC_ROE = 2 };
-enum { OC_EULER = 1, OC_RK2 = 2, OC_RK3 = 3, OC_HANCOCK = 4, OC_CHARTR = 5 };
+enum { OC_EULER = 1, OC_RK2 = 2, OC_RK3 = 3, OC_HANCOCK = 4, OC_CHARTR = 5, OC_HANCOCK_CONS = 6 };
+/* OC_HANCOCK_CONS: CTU with the conservative Hancock predictor (PRIMITIVE_HANCOCK NO) */
 /* OC_CHARTR: CTU with CharTracingStep (TIME_STEPPING CHARACTERISTIC_TRACING,
    LINEAR reconstruction) */
-#define IS_CTU(s) ((s) == OC_HANCOCK || (s) == OC_CHARTR) /* HANCOCK: CTU with the primitive Hancock predictor */
+#define IS_CTU(s) ((s) == OC_HANCOCK || (s) == OC_CHARTR || (s) == OC_HANCOCK_CONS) /* HANCOCK: CTU with the primitive Hancock predictor */
 enum { OC_ARITHMETIC = 1, OC_UCT0 = 2, OC_UCT_CONTACT = 3, OC_UCT_HLL = 4 }; /* CT_EMF_AVERAGE, Src/MHD/CT/ct.h:17-21 */
 enum { OC_PERIODIC = 0, OC_OUTFLOW = 1, OC_REFLECTIVE = 2, OC_EQTSYMMETRIC = 3, OC_USERDEF = 4 };
 

@@ -19,8 +19,8 @@ NVAR = 8
 RECON = {"LINEAR": 0, "PARABOLIC": 1}
 LIMITER = {"FLAT_LIM": 0, "MINMOD_LIM": 1, "VANLEER_LIM": 2, "MC_LIM": 3, "DEFAULT": 4}
 SOLVER = {"hll": 0, "hlld": 1, "roe": 2}
-STEPPING = {"EULER": 1, "RK2": 2, "RK3": 3, "HANCOCK": 4, "CHARACTERISTIC_TRACING": 5}
-CTU_STEPPING = ("HANCOCK", "CHARACTERISTIC_TRACING")
+STEPPING = {"EULER": 1, "RK2": 2, "RK3": 3, "HANCOCK": 4, "CHARACTERISTIC_TRACING": 5, "HANCOCK_CONS": 6}
+CTU_STEPPING = ("HANCOCK", "CHARACTERISTIC_TRACING", "HANCOCK_CONS")
 BC = {"periodic": 0, "outflow": 1, "reflective": 2, "eqtsymmetric": 3, "userdef": 4}
 EMF = {"ARITHMETIC": 1, "UCT0": 2, "UCT_CONTACT": 3, "UCT_HLL": 4}
 

@@ -16,7 +16,7 @@ PG_OK = 0
 PG_LINEAR, PG_PARABOLIC = 0, 1
 PG_FLAT_LIM, PG_MINMOD_LIM, PG_VANLEER_LIM, PG_MC_LIM, PG_DEFAULT_LIM = 0, 1, 2, 3, 4
 PG_HLL, PG_HLLD, PG_ROE = 0, 1, 2
-PG_RK2, PG_RK3, PG_HANCOCK, PG_CHAR_TRACING = 2, 3, 4, 5
+PG_RK2, PG_RK3, PG_HANCOCK, PG_CHAR_TRACING, PG_HANCOCK_CONS = 2, 3, 4, 5, 6
 PG_DIVB_NONE, PG_CONSTRAINED_TRANSPORT = 0, 1
 PG_ARITHMETIC, PG_UCT0, PG_UCT_CONTACT, PG_UCT_HLL = 1, 2, 3, 4
 PG_PERIODIC, PG_OUTFLOW, PG_REFLECTIVE, PG_EQTSYMMETRIC, PG_USERDEF = 0, 1, 2, 3, 4

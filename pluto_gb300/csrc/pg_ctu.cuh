@@ -139,7 +139,50 @@ __global__ void k_ctu_states(F64A<T> a, Box box) {
       traced = true;
     }
   }
-  if (!traced) {  // primitive Hancock step
+  if (!traced && a.cons_hancock) {
+    // conservative Hancock step (PRIMITIVE_HANCOCK NO, Src/States/hancock.c:159-434):
+    // the zone's own interface states evolved by dt/2 with the difference of
+    // their fluxes; where U^{n+1/2} fails ConsToPrim the zone falls back to
+    // first order (its centre value on both sides)
+    const T gm1 = T(a.gamma - 1.0);
+    const double dtdx = dt2 / g.dx[DIR];
+    T uc[NV], uL[NV], uR[NV], fp[NV], fm[NV], uh[NV], vh[NV], pp, pm;
+    prim_to_cons(v0, uc, gm1);
+    prim_to_cons(vp, uL, gm1);
+    prim_to_cons(vm, uR, gm1);
+    flux<DIR>(vp, uL, fp, pp);
+    flux<DIR>(vm, uR, fm, pm);
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) {
+      T rhs = -dtdx * (fp[nv] - fm[nv]);
+      if (nv == R::vn) rhs = rhs - dtdx * (pp - pm);
+      uh[nv] = uc[nv] + rhs;
+    }
+    unsigned char fl = 0;
+    cons_to_prim(uh, vh, gm1, T(a.small_rho), T(a.small_p), &fl);
+    if (fl) {
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) vh[nv] = vp[nv] = vm[nv] = v0[nv];
+      if (a.ct) {
+        vp[R::bn] = a.Bs[DIR][c];
+        vm[R::bn] = a.Bs[DIR][c - s];
+      }
+    }
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) {
+      const T P1 = vp[nv] - vm[nv];
+      T dvp = vh[nv] - v0[nv];
+      T dvm = dvp;
+      dvp = dvp + 0.5 * P1;
+      dvm = dvm - 0.5 * P1;
+      vp[nv] = v0[nv] + dvp;
+      vm[nv] = v0[nv] + dvm;
+    }
+    if (a.ct) {
+      vp[R::bn] = a.Bs[DIR][c];
+      vm[R::bn] = a.Bs[DIR][c - s];
+    }
+  } else if (!traced) {  // primitive Hancock step
     T dv[NV], Adv[NV];
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) dv[nv] = vp[nv] - vm[nv];
@@ -169,7 +212,7 @@ __global__ void k_ctu_states(F64A<T> a, Box box) {
     a.VP[nv][c] = vp[nv];
     a.VM[nv][c] = vm[nv];
   }
-  if (a.ct) {  // CTU_CT_Source
+  if (a.ct && !a.cons_hancock) {  // CTU_CT_Source (not with the conservative predictor, ctu_step.c:122-133)
     const bool c3 = a.c3 != 0;
     const T db = (dt2 / g.dx[DIR]) * (up[R::bn] - um[R::bn]);
     up[MX1] += v0[BX1] * db;

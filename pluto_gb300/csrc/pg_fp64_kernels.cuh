@@ -50,6 +50,7 @@ struct F64A {
   int div_dims;     // RK: invDt_hyp /= DIMENSIONS (update_stage.c:311); CTU: no
   int emf_avg, c3;
   int chtr;         // CTU predictor: characteristic tracing (else primitive Hancock)
+  int cons_hancock; // CTU predictor: conservative Hancock step (PRIMITIVE_HANCOCK NO)
   int char_lim;     // CHAR_LIMITING YES: PLM limited in characteristic variables
 };
 
@@ -567,6 +568,7 @@ static F64A<T> make_args(Solver* S) {
   for (int d = 0; d < 3; d++) a.SV[d] = S->SV[d];
   a.div_dims = !is_ctu(S->cfg.time_stepping);
   a.chtr = S->cfg.time_stepping == PG_CHAR_TRACING;
+  a.cons_hancock = S->cfg.time_stepping == PG_HANCOCK_CONS;
   a.char_lim = S->cfg.char_limiting;
   a.emf_avg = S->cfg.emf_average;
   a.c3 = S->cfg.components == 3;

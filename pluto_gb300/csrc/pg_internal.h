@@ -163,7 +163,9 @@ void output_free(Solver* S);  // waits for pending outputs, then releases their 
 
 constexpr int kThreads = 256;
 // TIME_STEPPING of the CTU family (ctu_step.c): HANCOCK or CHARACTERISTIC_TRACING
-inline bool is_ctu(int time_stepping) { return time_stepping == PG_HANCOCK || time_stepping == PG_CHAR_TRACING; }
+inline bool is_ctu(int time_stepping) {
+  return time_stepping == PG_HANCOCK || time_stepping == PG_CHAR_TRACING || time_stepping == PG_HANCOCK_CONS;
+}
 
 inline unsigned grid_for(long long n, int threads = kThreads) {
   long long b = (n + threads - 1) / threads;

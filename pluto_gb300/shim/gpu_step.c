@@ -112,6 +112,8 @@ static void gpu_config(pg_config *c, Riemann_Solver *Riemann, Grid *grid)
   c->time_stepping = PG_RK3;
 #elif TIME_STEPPING == EULER
   c->time_stepping = PG_EULER;
+#elif TIME_STEPPING == HANCOCK && PRIMITIVE_HANCOCK == NO
+  c->time_stepping = PG_HANCOCK_CONS;
 #elif TIME_STEPPING == HANCOCK
   c->time_stepping = PG_HANCOCK;
 #elif TIME_STEPPING == CHARACTERISTIC_TRACING

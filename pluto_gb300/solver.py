@@ -24,8 +24,8 @@ LIMITER = {"FLAT_LIM": L.PG_FLAT_LIM, "MINMOD_LIM": L.PG_MINMOD_LIM,
            "VANLEER_LIM": L.PG_VANLEER_LIM, "MC_LIM": L.PG_MC_LIM, "DEFAULT": L.PG_DEFAULT_LIM}
 RIEMANN = {"hll": L.PG_HLL, "hlld": L.PG_HLLD, "roe": L.PG_ROE}
 STEPPING = {"EULER": L.PG_EULER, "RK2": L.PG_RK2, "RK3": L.PG_RK3, "HANCOCK": L.PG_HANCOCK,
-            "CHARACTERISTIC_TRACING": L.PG_CHAR_TRACING}
-CTU_STEPPING = ("HANCOCK", "CHARACTERISTIC_TRACING")
+            "CHARACTERISTIC_TRACING": L.PG_CHAR_TRACING, "HANCOCK_CONS": L.PG_HANCOCK_CONS}
+CTU_STEPPING = ("HANCOCK", "CHARACTERISTIC_TRACING", "HANCOCK_CONS")
 EMF = {"ARITHMETIC": L.PG_ARITHMETIC, "UCT0": L.PG_UCT0, "UCT_CONTACT": L.PG_UCT_CONTACT,
        "UCT_HLL": L.PG_UCT_HLL}
 BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW, "reflective": L.PG_REFLECTIVE,

@@ -242,6 +242,13 @@ def setups():
         replace(br.ot_setup("hlld", 32, 30), stepping="HANCOCK", emf="UCT0", name="ot_ctu_uct0_32"),
         replace(br.blast_setup(16, 12), stepping="CHARACTERISTIC_TRACING", emf="UCT0",
                 name="blast_chtr_uct0_16"),
+        # TIME_STEPPING HANCOCK with PRIMITIVE_HANCOCK NO (conservative predictor, hancock.c:159-434)
+        replace(br.ot_setup("hlld", 32, 30), stepping="HANCOCK_CONS", emf="UCT_CONTACT", name="ot_ctu_cons_32"),
+        replace(br.blast_setup(16, 12), stepping="HANCOCK_CONS", emf="ARITHMETIC", name="blast_ctu_cons_16"),
+        replace(br.blast_setup(16, 12, pin=1000.0, bmag=30.0), stepping="HANCOCK_CONS", emf="UCT0",
+                name="blast_ctu_cons_floor_16"),
+        replace(br.tube_setup(1, 200, 120), stepping="HANCOCK_CONS", name="tube_ctu_cons_1_200"),
+        replace(br.cpa_setup(32, 20), stepping="HANCOCK_CONS", emf="UCT0", bc="outflow", name="cpa_ctu_cons_32"),
     ]
     for s in out:
         s.first_dt = 1e-3 if not s.name.startswith("tube") else 1e-4

@@ -44,7 +44,7 @@ def test_abi_version(lib):
 
 
 @pytest.mark.parametrize("field,value", [("dims", 4), ("components", 1), ("gamma", 1.0),
-                                         ("riemann", 7), ("time_stepping", 6), ("precision", 9)])
+                                         ("riemann", 7), ("time_stepping", 7), ("precision", 9)])
 def test_invalid_config_rejected_before_any_cuda_call(lib, field, value):
     spec = dict(dims=2, components=2, nx=(16, 16, 1), dx=(1 / 16, 1 / 16, 1.0), gamma=5 / 3)
     cfg = make_config(spec)
@@ -96,7 +96,9 @@ def test_char_tracing_validation(lib, extra, ok):
     ("EULER", "UCT_CONTACT", "fp64", True), ("RK2", "UCT0", "fp64_tangent", True),
     ("RK2", "UCT_HLL", "mixed", True), ("RK2", "UCT_CONTACT", "mixed", False), ("RK2", "UCT0", "mixed_dw", False),
     ("HANCOCK", "UCT0", "fp64", True), ("HANCOCK", "UCT_HLL", "fp64", False),
-    ("CHARACTERISTIC_TRACING", "UCT0", "fp64", True)])
+    ("CHARACTERISTIC_TRACING", "UCT0", "fp64", True),
+    ("HANCOCK_CONS", "UCT0", "fp64", True), ("HANCOCK_CONS", "ARITHMETIC", "fp64_tangent", True),
+    ("HANCOCK_CONS", "UCT_HLL", "fp64", False), ("HANCOCK_CONS", "UCT_CONTACT", "mixed", False)])
 def test_emf_average_validation(lib, stepping, emf, precision, ok):
     """CT_EMF_AVERAGE: all four averages under RK (ARITHMETIC, UCT0 and
     UCT_CONTACT on the FP64 and tangent-linear builds only), every one but

@@ -218,21 +218,23 @@ def test_nan_state_reported_not_trapped():
     assert e.value.code == 4
 
 
-@pytest.mark.parametrize("emf,solver,bc", [("UCT_CONTACT", "hlld", "periodic"), ("ARITHMETIC", "hll", "outflow"),
-                                           ("UCT_CONTACT", "roe", "outflow"),
-                                           ("UCT_CONTACT", "hlld", ["reflective", "periodic", "eqtsymmetric"]),
-                                           ("ARITHMETIC", "roe", [("outflow", "reflective"), "periodic",
-                                                                  ("eqtsymmetric", "outflow")]),
-                                           ("UCT_CONTACT", "hlld", [("userdef", "outflow"), "periodic",
-                                                                    ("outflow", "userdef")]),
-                                           ("UCT0", "hlld", "periodic"),
-                                           ("UCT0", "roe", [("outflow", "reflective"), "periodic", "outflow"])])
-def test_ctu_vs_oracle_random_3d(emf, solver, bc):
-    """CTU (primitive Hancock predictor, corner-coupled corrector) with CT on a
-    random 3D state against the oracle, bit for bit."""
+@pytest.mark.parametrize("emf,solver,bc,stepping", [
+    ("UCT_CONTACT", "hlld", "periodic", "HANCOCK"), ("ARITHMETIC", "hll", "outflow", "HANCOCK"),
+    ("UCT_CONTACT", "roe", "outflow", "HANCOCK"),
+    ("UCT_CONTACT", "hlld", ["reflective", "periodic", "eqtsymmetric"], "HANCOCK"),
+    ("ARITHMETIC", "roe", [("outflow", "reflective"), "periodic", ("eqtsymmetric", "outflow")], "HANCOCK"),
+    ("UCT_CONTACT", "hlld", [("userdef", "outflow"), "periodic", ("outflow", "userdef")], "HANCOCK"),
+    ("UCT0", "hlld", "periodic", "HANCOCK"),
+    ("UCT0", "roe", [("outflow", "reflective"), "periodic", "outflow"], "HANCOCK"),
+    ("UCT_CONTACT", "hlld", "periodic", "HANCOCK_CONS"),
+    ("ARITHMETIC", "roe", "outflow", "HANCOCK_CONS"),
+    ("UCT0", "hll", [("reflective", "outflow"), "periodic", ("eqtsymmetric", "userdef")], "HANCOCK_CONS")])
+def test_ctu_vs_oracle_random_3d(emf, solver, bc, stepping):
+    """CTU (primitive or conservative Hancock predictor, corner-coupled
+    corrector) with CT on a random 3D state against the oracle, bit for bit."""
     from oracle.oracle import Oracle
     spec, vc, bs = _random_blast(16, seed=9)
-    spec.update(stepping="HANCOCK", emf=emf, solver=solver, bc=bc, limiter="MC_LIM")
+    spec.update(stepping=stepping, emf=emf, solver=solver, bc=bc, limiter="MC_LIM")
     s = _solver(spec)
     o = Oracle(spec, nthreads=4)
     if userdef_cases.has_userdef(spec):
@@ -340,6 +342,7 @@ def test_char_tracing_without_ct_vs_oracle_3d():
 
 
 @pytest.mark.parametrize("stepping,emf", [("HANCOCK", "UCT_CONTACT"), ("HANCOCK", "UCT0"), ("RK2", "UCT_CONTACT"),
+                                          ("HANCOCK_CONS", "UCT_CONTACT"),
                                           ("RK3", "UCT0"), ("RK2", "ARITHMETIC")])
 def test_ctu_tangent_value_part_is_the_fp64_step(stepping, emf):
     """The value part of the tangent-linear build (dual numbers) is the

@@ -26,7 +26,7 @@ def has_userdef(spec) -> bool:
 
 def nghost(spec) -> int:
     ng = 3 if spec.get("recon", "LINEAR") == "PARABOLIC" else 2
-    if spec.get("stepping", "RK2") in ("HANCOCK", "CHARACTERISTIC_TRACING") and spec.get("ct", True):
+    if spec.get("stepping", "RK2") in ("HANCOCK", "CHARACTERISTIC_TRACING", "HANCOCK_CONS") and spec.get("ct", True):
         ng += 1
     return ng
 
