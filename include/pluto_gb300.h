@@ -78,7 +78,9 @@ typedef struct {
   int riemann;
   int time_stepping;
   int divb;
-  int emf_average;
+  int emf_average;      /* CT_EMF_AVERAGE under CT (Src/MHD/CT/ct_emf.c:210-291):
+                           RK takes all four, CTU all but UCT_HLL (ct_emf.c:196-200);
+                           ARITHMETIC/UCT0/UCT_CONTACT on PG_FP64 and PG_FP64_TANGENT */
   int bc[3];            /* boundary type per axis (the beginning side, X*_BEG,
                            and the end side too unless bc_sides is 1) */
   int precision;        /* PG_FP64: bit-compatible with the reference C path */
