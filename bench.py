@@ -48,16 +48,20 @@ METRIC = "MHD zone-updates/s on 1 GB300: mixed vs FP64 at L1 err <=1e-5; % of HB
 # distributed plumbing (replicas only)
 # ---------------------------------------------------------------------------
 def dist_init():
+    """One process per GPU (torchrun env); NCCL on GPUs, gloo on a host
+    without one (the replica plumbing is tested that way)."""
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
     if ws > 1:
         import torch
         import torch.distributed as dist
         os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
-        local = int(os.environ.get("LOCAL_RANK", "0"))
-        torch.cuda.set_device(local)
-        os.environ["CUDA_VISIBLE_DEVICES_LOCAL"] = str(local)
-        dist.init_process_group("nccl")
+        if torch.cuda.is_available():
+            local = int(os.environ.get("LOCAL_RANK", "0"))
+            torch.cuda.set_device(local)
+            dist.init_process_group("nccl")
+        else:
+            dist.init_process_group("gloo")
     return rank, ws
 
 
@@ -72,7 +76,8 @@ def allmax(x, ws):
         return x
     import torch
     import torch.distributed as dist
-    t = torch.tensor([x], dtype=torch.float64, device="cuda")
+    dev = "cuda" if dist.get_backend() == "nccl" else "cpu"
+    t = torch.tensor([x], dtype=torch.float64, device=dev)
     dist.all_reduce(t, op=dist.ReduceOp.MAX)
     return float(t.item())
 
