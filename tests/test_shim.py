@@ -89,3 +89,37 @@ def test_shim_links_internal_boundary(tmp_path):
     from oracle import build_ref as br
     s = replace(br.ot_setup("hlld", 32, 30), name="ot_shim_internal", internal_boundary=True)
     assert _link(lambda: s, tmp_path).exists()
+
+
+def _preprocessed_shim(s):
+    """gpu_step.c after the preprocessor, against the scheme's definitions.h"""
+    from oracle import build_ref as br
+    run = br.build(s)
+    inc = ["-I", str(run)] + sum((["-I", str(REF / d)] for d in br.INC_DIRS), []) + ["-I", str(ROOT / "include")]
+    r = subprocess.run(["gcc", "-E", "-P", *inc, str(ROOT / "pluto_gb300" / "shim" / "gpu_step.c")],
+                       check=True, capture_output=True, text=True)
+    return " ".join(r.stdout.split())
+
+
+@pytest.mark.parametrize("stepping,emf,want_ts,want_emf", [
+    ("HANCOCK_CONS", "UCT0", "PG_HANCOCK_CONS", "PG_UCT0"),
+    ("HANCOCK", "ARITHMETIC", "PG_HANCOCK", "PG_ARITHMETIC"),
+    ("RK2", "UCT_CONTACT", "PG_RK2", "PG_UCT_CONTACT"),
+    ("RK3", "UCT0", "PG_RK3", "PG_UCT0")])
+def test_shim_maps_time_stepping_and_emf_average(stepping, emf, want_ts, want_emf):
+    """definitions.h's TIME_STEPPING (with PRIMITIVE_HANCOCK NO for the
+    conservative predictor) and CT_EMF_AVERAGE select the matching pg_config
+    values in the shim."""
+    from dataclasses import replace
+    from oracle import build_ref as br
+    s = replace(br.ot_setup("hlld", 32, 30), stepping=stepping, emf=emf, name=f"ot_shim_{stepping}_{emf}")
+    text = _preprocessed_shim(s)
+    assert f"c->time_stepping = {want_ts};" in text and text.count("c->time_stepping =") == 1
+    assert f"c->emf_average = {want_emf};" in text and text.count("c->emf_average =") == 1
+
+
+def test_shim_links_conservative_hancock(tmp_path):
+    from dataclasses import replace
+    from oracle import build_ref as br
+    s = replace(br.ot_setup("hlld", 32, 30), stepping="HANCOCK_CONS", emf="UCT0", name="ot_shim_cons")
+    assert _link(lambda: s, tmp_path).exists()
