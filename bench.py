@@ -485,6 +485,28 @@ def output_timing(n=256, outputs=4, steps_between=50):
             "download_then_write": {"added_ms_per_output": (t_sync - base) / outputs * 1e3}}
 
 
+def profile_case(args):
+    """--profile-case PROBLEM: ``--steps`` eager steps of one problem on a
+    fresh solver at ``--n``^3 (``--precision``), no CUDA graph, so that every
+    kernel is a separate launch a profiler can select with -k/-s/-c.  Prints
+    one line; no timing is taken."""
+    from pluto_gb300 import Solver, problems
+    if args.profile_case == "blast":
+        spec, vc, faces = problems.blast3d(args.n)
+    elif args.profile_case == "turb":
+        spec, vc, faces = problems.turbulence3d(args.n)
+    else:
+        spec, vc, faces = problems.orszag_tang(args.n)
+    s = Solver(spec, precision=args.precision)
+    s.upload(vc, faces)
+    dt = spec["first_dt"]
+    for _ in range(args.steps):
+        inv, _, _ = s.advance(dt)
+        dt = min((1.0 / inv) * spec["cfl"], 1.1 * dt)
+    print(json.dumps({"profile_case": args.profile_case, "n": args.n, "precision": args.precision,
+                      "steps": args.steps, "next_dt": dt}), flush=True)
+
+
 def rel_l1(a, b):
     den = np.abs(b).sum()
     return float(np.abs(a - b).sum() / den) if den > 0 else float(np.abs(a - b).sum())
@@ -515,6 +537,10 @@ def main():
     ap.add_argument("--turb-n", type=int, default=768)
     ap.add_argument("--turb-l1-n", type=int, default=256)
     ap.add_argument("--turb-l1-steps", type=int, default=50)
+    ap.add_argument("--profile-case", choices=["blast", "turb", "ot"],
+                    help="run --steps eager steps of one problem at --n (for ncu to attach to) and exit")
+    ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed_dw", "fp64"],
+                    help="precision of --profile-case")
     args = ap.parse_args()
     rank, ws = dist_init()
     if args.impl == "reference":
@@ -525,6 +551,9 @@ def main():
     from pluto_gb300 import Solver, problems
     from pluto_gb300 import build as pbuild
     pbuild.build()
+    if args.profile_case:
+        profile_case(args)
+        return
     if args.turbulence:
         if rank == 0:
             print(json.dumps(turbulence_leg(args)), flush=True)

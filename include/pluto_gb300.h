@@ -216,17 +216,19 @@ int pg_batch_set_schedule(pg_batch *b, int threads, int blocks_per_sm, int large
 
 /* Allocation-free variant of one 1D AdvanceStep (no reference counterpart;
    an addition of this library).  For callers that may not allocate device
-   memory while they run -- code under CUDA stream capture, hosts whose own
-   pool allocator owns all device memory, real-time loops that cannot take
-   the implicit device synchronisation of cudaMalloc/cudaFree.  The step's
-   work arrays live in one file-scope device array of about 13.4 MB, held by
-   every GPU that loads the library, sized for PG_STATIC_MAX_ZONES zones;
-   larger problems return PG_ERR_TOO_LARGE.  cfg: dims 1, no constrained
-   transport, PG_FP64.  v_in / v_out: device pointers to the interior state
+   memory while they run -- hosts whose own pool allocator owns all device
+   memory, real-time loops that cannot take the implicit device
+   synchronisation of cudaMalloc/cudaFree.  The step's work arrays live in
+   one file-scope device array of about 13.4 MB, held by every GPU that
+   loads the library, sized for PG_STATIC_MAX_ZONES zones; larger problems
+   return PG_ERR_TOO_LARGE.  cfg: dims 1, no constrained transport, PG_FP64,
+   EULER/RK2/RK3 (CTU returns PG_ERR_INVALID), no PG_USERDEF side (returns
+   PG_ERR_INVALID).  v_in / v_out: device pointers to the interior state
    [8][nx] (RHO, VX1..3, BX1..3, PRS; may alias).  cuda_stream: cudaStream_t
-   or NULL.  Blocks until the step is done.  Calls share the array: calls
-   that overlap on the GPU race.  The first call on a device looks up the
-   array's address; make it before any stream capture starts. */
+   or NULL.  Blocks until the step is done (it reads the step's scalars back
+   and synchronises the stream).  Calls share the array: calls that overlap
+   on the GPU race.  The first call on a device looks up the array's device
+   address with that device current and keeps it for the process. */
 #define PG_STATIC_MAX_ZONES 32768
 int pg_tube_step_static(const pg_config *cfg, const double *v_in, double *v_out, double dt,
                         void *cuda_stream, pg_step_info *info);

@@ -24,6 +24,8 @@ PG_EULER = 1
 PG_FP64, PG_MIXED, PG_MIXED_DW, PG_FP64_TANGENT = 0, 1, 2, 3
 PG_LAYOUT_INTERIOR, PG_LAYOUT_PLUTO = 0, 1
 
+PG_ERR_INVALID, PG_ERR_CUDA, PG_ERR_NOMEM, PG_ERR_NAN = 1, 2, 3, 4
+PG_ERR_DT_TOO_SMALL, PG_ERR_TIMEOUT, PG_ERR_TOO_LARGE = 5, 6, 7
 ERRORS = {1: "PG_ERR_INVALID", 2: "PG_ERR_CUDA", 3: "PG_ERR_NOMEM", 4: "PG_ERR_NAN",
           5: "PG_ERR_DT_TOO_SMALL", 6: "PG_ERR_TIMEOUT", 7: "PG_ERR_TOO_LARGE"}
 

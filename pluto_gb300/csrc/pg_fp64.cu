@@ -24,6 +24,7 @@
 //   k_end_step     NextTimeStep (Src/main.c:459-532)
 #include <cstdio>
 #include <cstring>
+#include <mutex>
 
 #include "pg_fp64_kernels.cuh"
 
@@ -118,14 +119,17 @@ int fp64_enqueue_step(Solver* S) { return fp64_enqueue_step_t<double>(S); }
 // ===========================================================================
 // Allocation-free entry point: pg_tube_step_static
 //
-// For callers that cannot call cudaMalloc while they run: code executing
-// under CUDA stream capture (allocation is illegal inside a capture), a host
-// application that has handed all device memory to its own pool allocator,
-// or a real-time loop that must not hit the implicit device synchronisation
-// of cudaMalloc/cudaFree.  One plain-FP64 AdvanceStep of a 1D problem without
-// constrained transport (the Riemann-tube family: HLL/HLLD, PLM/PPM,
-// RK2/RK3, periodic or outflow) runs with every work array carved out of the
-// file-scope device array below, the same kernels as pg_advance.
+// For callers that cannot call cudaMalloc while they run: a host application
+// that has handed all device memory to its own pool allocator, or a real-time
+// loop that must not hit the implicit device synchronisation of
+// cudaMalloc/cudaFree.  One plain-FP64 AdvanceStep of a 1D problem without
+// constrained transport (the Riemann-tube family: HLL/HLLD/Roe, PLM/PPM,
+// EULER/RK2/RK3, periodic, outflow, reflective or equatorial-symmetric sides)
+// runs with every work array carved out of the file-scope device array
+// below, the same kernels as pg_advance.  CTU time stepping (its predictor
+// needs three more sets of arrays) and user-defined sides (they call back
+// into a host function registered on a solver) are rejected before anything
+// is launched.
 //
 // The array is sized for PG_STATIC_MAX_ZONES interior zones (plus ghosts):
 // 51 double arrays + flags + scalars, about 13.4 MB, held by every GPU that
@@ -135,8 +139,9 @@ int fp64_enqueue_step(Solver* S) { return fp64_enqueue_step_t<double>(S); }
 // the same step, and the scalars are cleared on entry.  Calls that overlap
 // on the GPU (two streams, two host threads) race on the array: serialise
 // them.  The first call on a device looks up the array's device address
-// (cudaGetSymbolAddress) and caches it; make that first call before any
-// stream capture begins.
+// (cudaGetSymbolAddress) with that device current and caches it for the
+// process; cudaDeviceReset invalidates the cache, so do not reset a device
+// between calls.
 // ===========================================================================
 namespace pg {
 
@@ -149,6 +154,7 @@ constexpr size_t kStaticBytes =
 static __device__ __align__(256) unsigned char g_pg_static_scratch[kStaticBytes];
 
 static void* s_static_base[64];  // device address of the array, per device
+static std::mutex s_static_mutex;  // guards the lookup of s_static_base
 
 __global__ void k_static_setup(DevScalars* sc, double dt) {
   sc->dt = dt;
@@ -189,6 +195,14 @@ extern "C" int pg_tube_step_static(const pg_config* cfg, const double* v_in, dou
     set_last_error("pg_tube_step_static: only 1D FP64 problems without constrained transport");
     return PG_ERR_INVALID;
   }
+  if (is_ctu(cfg->time_stepping)) {  // the CTU predictor's arrays are not in the static array
+    set_last_error("pg_tube_step_static: CTU time stepping is not supported (EULER, RK2 or RK3)");
+    return PG_ERR_INVALID;
+  }
+  if (cfg->bc[0] == PG_USERDEF || (cfg->bc_sides && cfg->bc_hi[0] == PG_USERDEF)) {
+    set_last_error("pg_tube_step_static: user-defined sides need a solver (pg_set_userdef)");
+    return PG_ERR_INVALID;
+  }
   if (cfg->nx[0] > PG_STATIC_MAX_ZONES) {
     set_last_error("pg_tube_step_static: nx exceeds PG_STATIC_MAX_ZONES (32768 zones)");
     return PG_ERR_TOO_LARGE;
@@ -202,14 +216,19 @@ extern "C" int pg_tube_step_static(const pg_config* cfg, const double* v_in, dou
     set_last_error("pg_tube_step_static: no current CUDA device");
     return PG_ERR_CUDA;
   }
-  if (!s_static_base[dev]) {  // once per device, with that device current
-    void* p = nullptr;
-    cudaError_t e = cudaGetSymbolAddress(&p, g_pg_static_scratch);
-    if (e != cudaSuccess || !p) {
-      set_last_error("pg_tube_step_static: cudaGetSymbolAddress failed");
-      return PG_ERR_CUDA;
+  void* base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(s_static_mutex);
+    if (!s_static_base[dev]) {  // once per device, with that device current
+      void* p = nullptr;
+      cudaError_t e = cudaGetSymbolAddress(&p, g_pg_static_scratch);
+      if (e != cudaSuccess || !p) {
+        set_last_error("pg_tube_step_static: cudaGetSymbolAddress failed");
+        return PG_ERR_CUDA;
+      }
+      s_static_base[dev] = p;
     }
-    s_static_base[dev] = p;
+    base = s_static_base[dev];
   }
   // A solver description on the host stack; every device pointer is a slice
   // of the static array.
@@ -220,7 +239,7 @@ extern "C" int pg_tube_step_static(const pg_config* cfg, const double* v_in, dou
   S.stream = (cudaStream_t)cuda_stream;
   S.device_dt = false;
   const long long n = S.g.ncell;  // <= kStaticZones
-  double* d = (double*)s_static_base[dev];
+  double* d = (double*)base;
   int a = 0;
   for (int nv = 0; nv < 8; nv++) {
     S.V[nv] = d + (size_t)(a++) * kStaticZones;
@@ -244,6 +263,7 @@ extern "C" int pg_tube_step_static(const pg_config* cfg, const double* v_in, dou
   k_static_copy<<<(8 * nx + 255) / 256, 256, 0, S.stream>>>(vt, v_in, nullptr, nx, beg, 1);
   rc = fp64_enqueue_step(&S);
   if (rc) {
+    cudaStreamSynchronize(S.stream);  // nothing queued may outlive this call
     set_last_error("pg_tube_step_static: kernel launch failed");
     return PG_ERR_CUDA;
   }

@@ -4,14 +4,13 @@ complete PLUTO executable with libpluto_gb300 in place of the RK objects.
 Needs the reference source tree (skipped where it is absent, e.g. on the GPU
 machine); no GPU is used: the binary is built, not run.
 """
-import os
 import subprocess
 from pathlib import Path
 
 import pytest
 
 ROOT = Path(__file__).resolve().parents[1]
-REF = Path(os.environ.get("PLUTO_REF", "/root/reference"))
+from oracle.build_ref import REF  # noqa: E402  (the reference tree, PLUTO_REF)
 
 pytestmark = pytest.mark.skipif(not (REF / "Src" / "main.c").exists(), reason="reference tree absent")
 

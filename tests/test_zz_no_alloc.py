@@ -1,12 +1,16 @@
 """Allocation-free 1D step (pg_tube_step_static) against the regular entry point.
 
 pg_tube_step_static serves callers that may not allocate device memory while
-they run (stream capture, an application whose pool owns the device memory,
-latency-critical loops): its work arrays are one file-scope device array.
-Here it must reproduce pg_create/pg_upload/pg_advance/pg_download on two
-consecutive calls, the second one fed with the first one's output, with the
-tolerance of the other FP64 tests (it runs the same kernels, so the results
-are in fact identical).  This file is collected last on purpose.
+they run (an application whose pool allocator owns the device memory, loops
+that cannot take the device synchronisation of cudaMalloc/cudaFree): its
+work arrays are one file-scope device array.  Here it must reproduce
+pg_create/pg_upload/pg_advance/pg_download on two consecutive calls, the
+second one fed with the first one's output, with the tolerance of the other
+FP64 tests (it runs the same kernels, so the results are in fact identical).
+Configurations it cannot run (CTU, user-defined sides, constrained
+transport, more than one dimension, sizes above the array) are rejected
+before any CUDA call, so those checks also run without a GPU.  This file is
+collected last on purpose.
 """
 import ctypes as C
 
@@ -14,8 +18,6 @@ import numpy as np
 import pytest
 
 from conftest import rel_l1
-
-pytestmark = pytest.mark.gpu
 
 TOL = 1e-10
 
@@ -29,13 +31,16 @@ def _static_step(lib, cfg, d_in, d_out, dt, stream):
     return info
 
 
-@pytest.mark.parametrize("n,seed,recon", [(3000, 3, "LINEAR"), (1500, 5, "PARABOLIC")])
-def test_static_step_matches_regular_entry_point_on_two_calls(n, seed, recon):
+@pytest.mark.gpu
+@pytest.mark.parametrize("n,seed,recon,bc", [(3000, 3, "LINEAR", "outflow"), (1500, 5, "PARABOLIC", "outflow"),
+                                             (2048, 7, "LINEAR", "periodic")])
+def test_static_step_matches_regular_entry_point_on_two_calls(n, seed, recon, bc):
     import torch
     from pluto_gb300 import Solver, problems
     from pluto_gb300 import _lib as L
     spec, vc, _ = problems.riemann_tube(n, seed)
     spec["recon"] = recon
+    spec["bc"] = bc
     lib = L.lib()
     ref = Solver(spec, precision="fp64")
     ref.upload(vc)
@@ -58,14 +63,37 @@ def test_static_step_matches_regular_entry_point_on_two_calls(n, seed, recon):
     assert i1.nfail == nf1 and i2.nfail == nf2
 
 
-def test_static_step_rejects_oversize():
+def _rejected(spec_changes, msg):
+    """Calls the entry point with a configuration it must refuse; the pointers
+    are never dereferenced because the refusal comes before any CUDA call."""
     from pluto_gb300 import _lib as L
     from pluto_gb300 import problems
     from pluto_gb300.solver import make_config
     spec, _, _ = problems.riemann_tube(64, 0)
-    spec["nx"] = (L.PG_STATIC_MAX_ZONES + 1, 1, 1)
+    spec.update(spec_changes)
     cfg = make_config(spec)
     lib = L.lib()
     info = L.PgStepInfo()
     rc = lib.pg_tube_step_static(C.byref(cfg), C.c_void_p(16), C.c_void_p(16), 1e-4, None, C.byref(info))
-    assert rc == 7 and b"PG_STATIC_MAX_ZONES" in lib.pg_last_error()
+    return rc, lib.pg_last_error()
+
+
+def test_static_step_rejects_oversize():
+    from pluto_gb300 import _lib as L
+    rc, err = _rejected({"nx": (L.PG_STATIC_MAX_ZONES + 1, 1, 1)}, "")
+    assert rc == L.PG_ERR_TOO_LARGE and b"PG_STATIC_MAX_ZONES" in err
+
+
+@pytest.mark.parametrize("changes,word", [
+    ({"stepping": "HANCOCK"}, b"CTU"),
+    ({"stepping": "CHARACTERISTIC_TRACING"}, b"CTU"),
+    ({"stepping": "HANCOCK_CONS"}, b"CTU"),
+    ({"bc": "userdef"}, b"user-defined"),
+    ({"bc": [("outflow", "userdef"), "periodic", "periodic"]}, b"user-defined"),
+    ({"dims": 2, "nx": (64, 64, 1), "dx": (1 / 64, 1 / 64, 1.0), "ct": True}, b"1D"),
+    ({"dims": 2, "nx": (64, 64, 1), "dx": (1 / 64, 1 / 64, 1.0)}, b"1D"),
+])
+def test_static_step_rejects_unsupported_configs(changes, word):
+    from pluto_gb300 import _lib as L
+    rc, err = _rejected(changes, word)
+    assert rc == L.PG_ERR_INVALID and word in err, err
