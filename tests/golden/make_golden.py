@@ -5,6 +5,7 @@ Run in a container that has the reference tree (``PLUTO_REF``, default
 ``/root/reference``) and gcc:
 
     python tests/golden/make_golden.py [name ...]
+    python tests/golden/make_golden.py --large [name ...]   # tests/golden/large/
 
 Each fixture ``<name>.npz`` holds the reference's own initial dump (step 0)
 and its dump after ``steps`` steps, as written by the reference (``.dbl``,
@@ -255,8 +256,94 @@ def setups():
     return out
 
 
+# ---------------------------------------------------------------------------
+# Fixtures at the benchmark configurations' own sizes (tests/golden/large/).
+# The final states are too large to commit; each fixture keeps the reference's
+# initial dump (it compresses well) and, of the dump after ``steps`` steps,
+# the SHA-256 of every variable's bytes (little-endian doubles in the dump's
+# order) and of the whole file, with per-variable sums for diagnosis.
+# ---------------------------------------------------------------------------
+LARGE = GOLDEN / "large"
+TUBE_FAMILY = (32, 400)  # the first 32 tubes of the batched family (seed 0), 400 steps each
+
+
+def large_setups():
+    return [
+        # 2D Orszag-Tang 256^2, PLM/MC + HLLD + RK2 + CT(UCT_HLL), CFL 0.4, 200 steps
+        replace(br.ot_setup("hlld", 256, 200), name="ot_hlld_256_200", first_dt=1e-4),
+        # the 3D blast scheme (PLM/MC + HLLD + RK2 + CT, CFL 0.3) at 64^3: the pressure
+        # floor fires from step ~16 on
+        replace(br.blast_setup(64, 21), name="blast_64_21", first_dt=1e-4),
+        # rotated circularly polarised Alfven wave 128^2, 256 steps (the adjoint problem's forward run)
+        replace(br.cpa_setup(128, 256), name="cpa_128_256", first_dt=1e-4),
+    ]
+
+
+def _digest(arrays):
+    import hashlib
+    h = hashlib.sha256()
+    for a in arrays:
+        h.update(np.ascontiguousarray(a, dtype="<f8").tobytes())
+    return h.hexdigest()
+
+
+def large_record(final: dict, names) -> dict:
+    import math as _m
+    return {"names": list(names), "sha256": _digest([final[nm] for nm in names]),
+            "sha256_per_variable": {nm: _digest([final[nm]]) for nm in names},
+            "sums": {nm: _m.fsum(final[nm].ravel().tolist()) for nm in names}}
+
+
+def dump_names(run_dir: Path, index: int = 1):
+    rec = [l.split() for l in (run_dir / "dbl.out").read_text().split("\n") if l.strip()]
+    return [r for r in rec if int(r[0]) == index][0][6:]
+
+
+def make_large(only=()):
+    import hashlib
+    LARGE.mkdir(exist_ok=True)
+    for s in large_setups():
+        if only and s.name not in only:
+            continue
+        a, b = br.run(s)
+        run_dir = br.OUT / s.name
+        names = dump_names(run_dir)
+        rec = large_record(b, names)
+        assert rec["sha256"] == hashlib.sha256((run_dir / "data.0001.dbl").read_bytes()).hexdigest()
+        vc0, bs0 = to_arrays(a, s)
+        arrs = {"vc0": vc0}
+        arrs.update({k + "_0": v for k, v in bs0.items()})
+        meta = spec_of(s)
+        meta.update(t_final=b["t"], dt_final=b["dt"], step_final=b["step"], final=rec)
+        np.savez_compressed(LARGE / f"{s.name}.npz", meta=json.dumps(meta), **arrs)
+        print(f"{s.name}: t={b['t']:.6e} dt={b['dt']:.6e} step={b['step']} sha={rec['sha256'][:16]}")
+    name = f"tubes_family0_{TUBE_FAMILY[0]}x{TUBE_FAMILY[1]}"
+    if only and name not in only:
+        return
+    from pluto_gb300.batch import tube_family
+    ntubes, steps = TUBE_FAMILY
+    _, ns, _, _ = tube_family(4096, 0, 128, 4096)
+    ns = ns[:ntubes]
+    tubes = [replace(br.tube_setup(t, int(ns[t]), steps), name=f"tubefam_{t}_{int(ns[t])}") for t in range(ntubes)]
+    import concurrent.futures as cf
+    with cf.ThreadPoolExecutor(8) as ex:
+        res = list(ex.map(br.run, tubes))
+    v0 = np.concatenate([to_arrays(a, s)[0].reshape(8, -1) for (a, _), s in zip(res, tubes)], axis=1)
+    v1 = np.concatenate([to_arrays(b, s)[0].reshape(8, -1) for (_, b), s in zip(res, tubes)], axis=1)
+    t1 = np.array([b["t"] for _, b in res])
+    dt1 = np.array([b["dt"] for _, b in res])
+    meta = spec_of(tubes[0])
+    meta.update(name=name, nx_tubes=[int(n) for n in ns], steps=steps, family_seed=0)
+    np.savez_compressed(LARGE / f"{name}.npz", meta=json.dumps(meta), v0=v0, v1=v1, t1=t1, dt1=dt1)
+    print(f"{name}: {ntubes} tubes, {int(ns.sum())} cells, t in [{t1.min():.4f}, {t1.max():.4f}]")
+
+
 def main():
-    only = set(sys.argv[1:])  # fixture names to (re)make; all when empty
+    args = sys.argv[1:]
+    if args and args[0] == "--large":
+        make_large(set(args[1:]))
+        return
+    only = set(args)  # fixture names to (re)make; all when empty
     for s in setups():
         if only and s.name not in only:
             continue
