@@ -207,11 +207,13 @@ int pg_batch_download(pg_batch *b, double *vars);
 int pg_batch_run(pg_batch *b, int nsteps, double first_dt, double cfl, double cfl_max_var,
                  double *elapsed_ms);
 int pg_batch_get(pg_batch *b, double *time, double *dt, int64_t *nfail);
-/* Schedule autotuner: times trial_steps for each (threads per CTA, CTAs per
-   SM, queue order) candidate from the same state, keeps the fastest and
-   restores the state. */
+/* Schedule autotuner: times trial_steps for each (threads per CTA = warps
+   sharing one tube, CTAs per SM) candidate from the same state, tubes queued
+   largest first, each candidate twice (the faster time counts); keeps the
+   fastest and restores the state.  *best_order is always 1. */
 int pg_batch_autotune(pg_batch *b, int trial_steps, double first_dt, double cfl, double cfl_max_var,
                       int *best_threads, int *best_blocks_per_sm, int *best_order, double *best_ms);
+/* threads: 32..256, a multiple of 32 (the warps of a CTA share one tube). */
 int pg_batch_set_schedule(pg_batch *b, int threads, int blocks_per_sm, int largest_first);
 
 /* Allocation-free variant of one 1D AdvanceStep (no reference counterpart;

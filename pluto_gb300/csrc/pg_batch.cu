@@ -16,13 +16,9 @@ namespace pg {
 template <class T, class A>
 static cudaError_t launch_batch_t(const BatchArgs<T>& b, int rs, int solver, int nstage, int nsteps, int grid,
                                   int threads, cudaStream_t st) {
-  const size_t smem = batch_smem_bytes<T>(threads);
 #define PG_BATCH_CASE(RS_, SOLV_, NST_)                                                                  \
   if (rs == RS_ && solver == SOLV_ && nstage == NST_) {                                                  \
-    auto k = k_batch<T, A, RS_, SOLV_, NST_>;                                                            \
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);    \
-    if (e != cudaSuccess) return e;                                                                      \
-    k<<<grid, threads, smem, st>>>(b, nsteps);                                                           \
+    k_batch<T, A, RS_, SOLV_, NST_><<<grid, threads, 0, st>>>(b, nsteps);                                \
     return cudaGetLastError();                                                                           \
   }
   PG_BATCH_CASE(1, PG_HLLD, 2)
@@ -53,6 +49,7 @@ cudaError_t launch_batch_f64(const BatchArgs<double>& b, int rs, int solver, int
 }
 cudaError_t launch_batch_mixed(const BatchArgs<float>& b, bool dw, int rs, int solver, int nstage, int nsteps,
                                int grid, int threads, cudaStream_t st);
+cudaError_t launch_batch_cons_init(const BatchArgs<float>& b, bool dw, cudaStream_t st);
 
 }  // namespace pg
 
@@ -74,10 +71,10 @@ struct pg_batch {
   unsigned long long* d_nfail = nullptr;
   unsigned int* d_counter = nullptr;
   void* V[2][8] = {};
-  void* U0[8] = {};
+  void* U0[8] = {};  // 8-byte elements (double, or FP32 pairs for PG_MIXED_DW)
   void* U1[8] = {};
   // schedule
-  int threads = 128, blocks_per_sm = 2, order_mode = 1;  // 1: largest tube first
+  int threads = 128, blocks_per_sm = 4, order_mode = 1;  // 1: largest tube first
   double cfl = 0.8, cfl_max_var = 1.1;
   int graph_nsteps = -1;
   cudaGraphExec_t graph = nullptr;
@@ -110,8 +107,8 @@ BatchArgs<T> bargs(pg_batch* B) {
   for (int s = 0; s < 2; s++)
     for (int nv = 0; nv < 8; nv++) a.V[s][nv] = (T*)B->V[s][nv];
   for (int nv = 0; nv < 8; nv++) {
-    a.U0[nv] = (T*)B->U0[nv];
-    a.U1[nv] = (T*)B->U1[nv];
+    a.U0[nv] = B->U0[nv];
+    a.U1[nv] = B->U1[nv];
   }
   a.dt = B->d_dt;
   a.time = B->d_time;
@@ -141,6 +138,16 @@ int enqueue_batch(pg_batch* B, int nsteps) {
   else
     e = launch_batch_mixed(bargs<float>(B), B->cfg.precision == PG_MIXED_DW, B->rs, B->cfg.riemann, nst, nsteps,
                            grid, B->threads, B->stream);
+  if (e != cudaSuccess) return bfail(PG_ERR_CUDA, cudaGetErrorString(e));
+  return PG_OK;
+}
+
+// Mixed path: the resident conserved state from the primitives (after an
+// upload or a restored snapshot).
+int init_conserved(pg_batch* B) {
+  if (B->f64) return PG_OK;
+  cudaError_t e = launch_batch_cons_init(bargs<float>(B), B->cfg.precision == PG_MIXED_DW, B->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(B->stream);
   if (e != cudaSuccess) return bfail(PG_ERR_CUDA, cudaGetErrorString(e));
   return PG_OK;
 }
@@ -222,7 +229,7 @@ extern "C" int pg_batch_create(const pg_config* cfg, int ntubes, const int* nx, 
        al((void**)&B->d_nfail, sizeof(unsigned long long) * ntubes) && al((void**)&B->d_counter, sizeof(unsigned));
   for (int s = 0; s < 2 && ok; s++)
     for (int nv = 0; nv < 8 && ok; nv++) ok = al(&B->V[s][nv], es * o);
-  for (int nv = 0; nv < 8 && ok; nv++) ok = al(&B->U0[nv], es * o) && al(&B->U1[nv], es * o);
+  for (int nv = 0; nv < 8 && ok; nv++) ok = al(&B->U0[nv], 8 * o) && al(&B->U1[nv], 8 * o);
   if (!ok) {
     free_batch(B);
     delete B;
@@ -279,7 +286,7 @@ extern "C" int pg_batch_upload(pg_batch* B, const double* vars) {
   }
   BCK(cudaMemcpy(B->d_cur, cur.data(), sizeof(int) * B->ntubes, cudaMemcpyHostToDevice));
   BCK(cudaMemset(B->d_nfail, 0, sizeof(unsigned long long) * B->ntubes));
-  return PG_OK;
+  return init_conserved(B);
 }
 
 extern "C" int pg_batch_download(pg_batch* B, double* vars) {
@@ -367,9 +374,12 @@ extern "C" int pg_batch_run(pg_batch* B, int nsteps, double first_dt, double cfl
 }
 
 // Autotuner: times trial_steps of the batch for every schedule candidate
-// (threads per CTA x CTAs per SM x queue order) from the same starting state,
-// keeps the fastest, restores the state.  Results: threads, CTAs/SM, order
-// (1 = largest tube first), best time (ms).
+// (threads per CTA, i.e. warps per tube team, x CTAs per SM), tubes queued
+// largest first, from the same starting state; each candidate runs twice and
+// keeps its faster time (the first trial also brings the clocks up), the
+// fastest candidate wins and the state is restored.  Every tube runs all
+// trial_steps steps, so the trial has the makespan structure of a full run.
+// Results: threads, CTAs/SM, order (1 = largest tube first), best time (ms).
 extern "C" int pg_batch_autotune(pg_batch* B, int trial_steps, double first_dt, double cfl, double cfl_max_var,
                                  int* best_threads, int* best_blocks_per_sm, int* best_order, double* best_ms) {
   if (!B || trial_steps < 1) return bfail(PG_ERR_INVALID, "pg_batch_autotune: bad argument");
@@ -400,39 +410,37 @@ extern "C" int pg_batch_autotune(pg_batch* B, int trial_steps, double first_dt, 
     BCK(cudaMemcpy(B->d_dt, dt0, sizeof(double) * B->ntubes, cudaMemcpyDeviceToDevice));
     BCK(cudaMemcpy(B->d_time, t0, sizeof(double) * B->ntubes, cudaMemcpyDeviceToDevice));
     BCK(cudaMemcpy(B->d_cur, cur0, sizeof(int) * B->ntubes, cudaMemcpyDeviceToDevice));
-    return PG_OK;
+    return init_conserved(B);
   };
-  const int cand_threads[] = {64, 128, 256, 512};
-  const int cand_bps[] = {1, 2, 4, 8};
+  const int cand_threads[] = {64, 128, 256};
+  const int cand_bps[] = {2, 4, 8, 16};
   double best = 1e300;
-  int bt = B->threads, bb = B->blocks_per_sm, bo = B->order_mode;
-  for (int order = 0; order <= 1; order++) {
-    B->order_mode = order;
-    if (set_order(B)) return PG_ERR_CUDA;
-    for (int th : cand_threads)
-      for (int bps : cand_bps) {
-        if (th * bps > 2048) continue;
-        B->threads = th;
-        B->blocks_per_sm = bps;
-        B->graph_nsteps = -1;
+  int bt = B->threads, bb = B->blocks_per_sm;
+  B->order_mode = 1;
+  if (set_order(B)) return PG_ERR_CUDA;
+  for (int th : cand_threads)
+    for (int bps : cand_bps) {
+      if (th * bps > 2048) continue;
+      B->threads = th;
+      B->blocks_per_sm = bps;
+      B->graph_nsteps = -1;
+      double t_best = 1e300;
+      for (int rep = 0; rep < 2; rep++) {
         if (restore()) return PG_ERR_CUDA;
         double ms = 0;
-        int rc = pg_batch_run(B, trial_steps, 0.0, cfl, cfl_max_var, &ms);
-        if (rc) continue;  // e.g. shared memory limits for this shape
-        if (ms < best) {
-          best = ms;
-          bt = th;
-          bb = bps;
-          bo = order;
-        }
+        if (pg_batch_run(B, trial_steps, 0.0, cfl, cfl_max_var, &ms)) break;  // e.g. resource limits
+        t_best = ms < t_best ? ms : t_best;
       }
-  }
+      if (t_best < best) {
+        best = t_best;
+        bt = th;
+        bb = bps;
+      }
+    }
   B->threads = bt;
   B->blocks_per_sm = bb;
-  B->order_mode = bo;
   B->graph_nsteps = -1;
-  int rc = set_order(B);
-  if (!rc) rc = restore();
+  int rc = restore();
   for (void* p : snap) cudaFree(p);
   cudaFree(dt0);
   cudaFree(t0);
@@ -440,14 +448,14 @@ extern "C" int pg_batch_autotune(pg_batch* B, int trial_steps, double first_dt, 
   cudaMemset(B->d_status, 0, sizeof(int));
   if (best_threads) *best_threads = bt;
   if (best_blocks_per_sm) *best_blocks_per_sm = bb;
-  if (best_order) *best_order = bo;
+  if (best_order) *best_order = 1;
   if (best_ms) *best_ms = best;
   return rc;
 }
 
 // Fix a schedule explicitly (threads per CTA, CTAs per SM, queue order).
 extern "C" int pg_batch_set_schedule(pg_batch* B, int threads, int blocks_per_sm, int order) {
-  if (!B || threads < 32 || threads % 32 || threads > 1024 || blocks_per_sm < 1)
+  if (!B || threads < 32 || threads % 32 || threads > 256 || blocks_per_sm < 1)
     return bfail(PG_ERR_INVALID, "pg_batch_set_schedule: bad argument");
   B->threads = threads;
   B->blocks_per_sm = blocks_per_sm;

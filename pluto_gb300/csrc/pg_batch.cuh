@@ -1,15 +1,14 @@
 // Batched 1D ideal-MHD problems (independent "tubes" of uneven sizes) in
-// one persistent launch.  Each CTA pulls a tube from a work queue (largest
-// first) and runs every step of it: per-tube dt (Src/main.c:389-575, the 1D
-// rule of Src/Time_Stepping/update_stage.c:237-241), ghost fill
-// (Src/boundary.c), RK2/RK3 stages (Src/Time_Stepping/rk_step.c) with the
-// same point physics as the other paths (pg_physics.cuh).
+// one persistent launch.  Each CTA -- a team of warps -- pulls a tube from a
+// work queue (largest first) and runs every step of it: per-tube dt
+// (Src/main.c:389-575, the 1D rule of Src/Time_Stepping/update_stage.c:
+// 237-241), ghost fill (Src/boundary.c), RK2/RK3 stages
+// (Src/Time_Stepping/rk_step.c) with the same point physics as the other
+// paths (pg_physics.cuh).
 //
-// Per stage the tube is processed in chunks of blockDim zones: every zone of
-// the chunk (plus one on each side) is reconstructed once into shared
-// memory, every interface of the chunk is solved once, then the zones are
-// updated.  Stage inputs and outputs live in separate buffers, so chunks
-// never see half-updated neighbours.
+// Per stage the warps of the team share the tube's 30-zone chunks; inside a
+// chunk neighbouring states and fluxes move between lanes by shuffles, so a
+// stage needs one block barrier (before the next stage reads neighbours).
 #pragma once
 #include "pg_internal.h"
 #include "pg_physics.cuh"
@@ -28,8 +27,13 @@ struct BatchArgs {
   const double* inv_dx;      // 1/dx per tube
   const double* dxv;         // dx per tube
   T* V[2][NV];               // stage ping-pong of primitives
-  T* U0[NV];                 // conserved state at the start of the step
-  T* U1[NV];                 // conserved result of the previous stage
+  // Conserved state at the start of the step (U0) and the result of the
+  // previous stage (U1), 8-byte elements: double on the FP64 path; on the
+  // mixed path the accumulator type A (double or an FP32 pair).  The mixed
+  // path keeps U0 resident across steps (written by the last stage); the
+  // FP64 path rebuilds it from the primitives every step, as the reference.
+  void* U0[NV];
+  void* U1[NV];
   double* dt;                // per-tube dt (in: current, out: next)
   double* time;              // per-tube time
   unsigned long long* nfail; // per-tube floor events
@@ -39,8 +43,6 @@ struct BatchArgs {
   double gamma, cfl, cfl_max_var, small_rho, small_p;
   int ng, bc, limiter, solver, ncomp;
 };
-
-template <class T> struct Batch;
 
 // Reconstruction of one zone from V[c-2..c+2] (PLM uses c-1..c+1).
 template <class T, int RS>
@@ -61,21 +63,6 @@ __device__ __forceinline__ void batch_recon(const T* V, long long c, int lim, in
   }
 }
 
-template <class T>
-__device__ __forceinline__ T block_max_T(T v, T* red) {
-  for (int o = 16; o > 0; o >>= 1) {
-    T w = __shfl_down_sync(0xffffffffu, v, o);
-    v = (w > v || w != w) ? w : v;
-  }
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  __syncthreads();
-  if (lane == 0) red[w] = v;
-  __syncthreads();
-  T r = red[0];
-  for (int q = 1; q < (int)(blockDim.x >> 5); q++) r = (red[q] > r || red[q] != red[q]) ? red[q] : r;
-  return r;
-}
-
 // Stage update of one zone: U_stage = base + rhs, RK combination, ConsToPrim.
 // FP64 instantiation follows the reference operation order exactly.
 template <int STAGE, int NSTAGE>
@@ -87,73 +74,61 @@ __device__ __forceinline__ int batch_update_f64(const BatchArgs<double>& b, long
     prim_to_cons(vin, u, gmm1);
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
-      b.U0[nv][c] = u[nv];
+      ((double*)b.U0[nv])[c] = u[nv];
       u[nv] += rhs[nv];
     }
   } else {
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++) u[nv] = b.U1[nv][c] + rhs[nv];
+    for (int nv = 0; nv < NV; nv++) u[nv] = ((const double*)b.U1[nv])[c] + rhs[nv];
     if (STAGE == 2) {
       const double w0 = NSTAGE == 3 ? 0.75 : 0.5, wc = NSTAGE == 3 ? 0.25 : 0.5;
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) u[nv] = w0 * b.U0[nv][c] + wc * u[nv];
+      for (int nv = 0; nv < NV; nv++) u[nv] = w0 * ((const double*)b.U0[nv])[c] + wc * u[nv];
     } else {
       const double one_third = 1.0 / 3.0;
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) u[nv] = one_third * (b.U0[nv][c] + 2.0 * u[nv]);
+      for (int nv = 0; nv < NV; nv++) u[nv] = one_third * (((const double*)b.U0[nv])[c] + 2.0 * u[nv]);
     }
   }
   unsigned char fl = 0;
   int fail = cons_to_prim(u, v, gmm1, b.small_rho, b.small_p, &fl);
   if (STAGE < NSTAGE) {
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++) b.U1[nv][c] = u[nv];
+    for (int nv = 0; nv < NV; nv++) ((double*)b.U1[nv])[c] = u[nv];
   }
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) vout[nv] = v[nv];
   return fail;
 }
 
-// Mixed: FP32 primitives and fluxes, conserved accumulation in A.
+// Mixed: FP32 primitives and fluxes; the conserved state stays resident in
+// the accumulator type A across stages and steps (U0 at the start of the
+// step, U1 the stage result), so the state is never re-rounded through FP32
+// primitives between stages.  ConsToPrim (Src/MHD/mappers.c:88-254) with the
+// pressure recovered in A and the reference's floors.
 template <int STAGE, int NSTAGE, class A>
 __device__ __forceinline__ int batch_update_mixed(const BatchArgs<float>& b, long long c, const float* rhs,
-                                                  const float* vin, float* vout) {
+                                                  float* vout) {
   using O = Acc<A>;
   using TT = typename O::T;
   const double inv_gmm1_d = 1.0 / (b.gamma - 1.0);
   const TT inv_gmm1 = O::konst(inv_gmm1_d, (float)inv_gmm1_d, (float)(inv_gmm1_d - (double)(float)inv_gmm1_d));
   TT u[NV];
   if (STAGE == 1) {
-    u[RHO] = O::from(vin[RHO]);
 #pragma unroll
-    for (int q = 0; q < 3; q++) {
-      u[VX1 + q] = O::prod(vin[RHO], vin[VX1 + q]);
-      u[BX1 + q] = O::from(vin[BX1 + q]);
-    }
-    TT kin = O::add(O::add(O::prod(vin[VX1], vin[VX1]), O::prod(vin[VX2], vin[VX2])), O::prod(vin[VX3], vin[VX3]));
-    TT b2 = O::add(O::add(O::prod(vin[BX1], vin[BX1]), O::prod(vin[BX2], vin[BX2])), O::prod(vin[BX3], vin[BX3]));
-    u[ENG] = O::add(O::mulf(O::add(O::mulf(kin, vin[RHO]), b2), 0.5f), O::mulf(inv_gmm1, vin[PRS]));
-    // U0 keeps the high part only when A is a double-word: store the value
-    // rounded to FP32 (storage is FP32 in the mixed path).
+    for (int nv = 0; nv < NV; nv++) u[nv] = O::addf(O::ld(b.U0[nv], c), rhs[nv]);
+  } else if (STAGE == 2 && NSTAGE == 2) {  // (U0 + U1 + rhs) / 2
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++) {
-      b.U0[nv][c] = O::tof(u[nv]);
-      u[nv] = O::addf(u[nv], rhs[nv]);
-    }
+    for (int nv = 0; nv < NV; nv++) u[nv] = O::half_sum3(O::ld(b.U0[nv], c), O::ld(b.U1[nv], c), rhs[nv]);
+  } else if (STAGE == 2) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++)
+      u[nv] = O::add(O::mulf(O::ld(b.U0[nv], c), 0.75f), O::mulf(O::addf(O::ld(b.U1[nv], c), rhs[nv]), 0.25f));
   } else {
+    const TT third = O::konst(1.0 / 3.0, (float)(1.0 / 3.0), (float)(1.0 / 3.0 - (double)(float)(1.0 / 3.0)));
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++) u[nv] = O::addf(O::from(b.U1[nv][c]), rhs[nv]);
-    if (STAGE == 2 && NSTAGE == 2) {
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) u[nv] = O::mulf(O::addf(u[nv], b.U0[nv][c]), 0.5f);
-    } else if (STAGE == 2) {
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) u[nv] = O::add(O::mulf(O::from(b.U0[nv][c]), 0.75f), O::mulf(u[nv], 0.25f));
-    } else {
-      const TT third = O::konst(1.0 / 3.0, (float)(1.0 / 3.0), (float)(1.0 / 3.0 - (double)(float)(1.0 / 3.0)));
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) u[nv] = O::mul(O::add(O::from(b.U0[nv][c]), O::mulf(u[nv], 2.0f)), third);
-    }
+    for (int nv = 0; nv < NV; nv++)
+      u[nv] = O::mul(O::add(O::ld(b.U0[nv], c), O::mulf(O::addf(O::ld(b.U1[nv], c), rhs[nv]), 2.0f)), third);
   }
   int fail = 0;
   if (O::neg(u[RHO])) {
@@ -170,15 +145,14 @@ __device__ __forceinline__ int batch_update_mixed(const BatchArgs<float>& b, lon
     fail = 1;
   }
   float p = O::tof(O::mulf(O::sub(u[ENG], kinb2), (float)(b.gamma - 1.0)));
-  if (p < 0.f) {
+  if (p < 0.f) {  // floor and recompute the energy (Src/MHD/mappers.c:190-200)
     p = (float)b.small_p;
     u[ENG] = O::add(O::mulf(inv_gmm1, p), kinb2);
     fail = 1;
   }
-  if (STAGE < NSTAGE) {
+  void* const* Uout = STAGE == NSTAGE ? b.U0 : b.U1;
 #pragma unroll
-    for (int nv = 0; nv < NV; nv++) b.U1[nv][c] = O::tof(u[nv]);
-  }
+  for (int nv = 0; nv < NV; nv++) O::st(Uout[nv], c, u[nv]);
   vout[RHO] = rho_f;
 #pragma unroll
   for (int q = 0; q < 3; q++) {
@@ -192,22 +166,32 @@ __device__ __forceinline__ int batch_update_mixed(const BatchArgs<float>& b, lon
 template <class T, class A, int STAGE, int NSTAGE>
 __device__ __forceinline__ int batch_update(const BatchArgs<T>& b, long long c, const T* rhs, const T* vin, T* vout) {
   if constexpr (sizeof(T) == 8) return batch_update_f64<STAGE, NSTAGE>(b, c, rhs, vin, vout);
-  else return batch_update_mixed<STAGE, NSTAGE, A>(b, c, rhs, vin, vout);
+  else return batch_update_mixed<STAGE, NSTAGE, A>(b, c, rhs, vout);
 }
 
-// One stage of one tube.  Returns this stage's max(cmax/dx) contribution.
+// One stage of one tube by the whole CTA.  The tube is cut into chunks of
+// 30 zones; warp w takes chunks w, w + NW, ...  Within a chunk lane l
+// reconstructs zone i = beg - 1 + 30 chunk + l, takes the right state of
+// interface i+1/2 from lane l+1 and the flux of interface i-1/2 from lane
+// l-1 (shuffles): 32 reconstructions, 31 interfaces, 30 updated zones, no
+// block barrier.  Stage input and output are separate buffers, so chunks
+// never see half-updated neighbours; the CTA synchronises once per stage.
+// cm_max collects max(cmax/dx) over the tube's interfaces
+// (Src/Time_Stepping/update_stage.c:237-241).
 template <class T, class A, int RS, int SOLVER, int STAGE, int NSTAGE>
-__device__ double batch_stage(const BatchArgs<T>& b, int tube, T* const* Vin, T* const* Vout, double dt, T* svp,
-                              T* svm, T* sf, T* red, unsigned long long& fails) {
+__device__ void batch_stage(const BatchArgs<T>& b, int tube, int in_buf, double dt, T& cm_max,
+                            unsigned long long& fails) {
+  T* const* Vin = b.V[in_buf];
+  T* const* Vout = b.V[1 - in_buf];
   const int n = b.nx[tube], ng = b.ng;
   const long long base = b.off[tube];
   const int beg = ng, end = ng + n - 1;
-  const int B = blockDim.x, tid = threadIdx.x;
+  const int tid = threadIdx.x, lane = tid & 31, w = tid >> 5, nw = blockDim.x >> 5;
   const T inv_dx = (T)b.inv_dx[tube];
   const T dtdx = (T)(dt / b.dxv[tube]);
   // ghost fill of the stage input (outflow: copy edge zone; periodic: wrap;
   // reflective / equatorial-symmetric: mirror with the FlipSign signs)
-  for (int q = tid; q < 2 * ng * NV; q += B) {
+  for (int q = tid; q < 2 * ng * NV; q += blockDim.x) {
     int nv = q / (2 * ng), gi = q % (2 * ng);
     int i = gi < ng ? gi : end + 1 + (gi - ng);
     int src = bc_src(i, beg, end, n, b.bc);
@@ -215,78 +199,87 @@ __device__ double batch_stage(const BatchArgs<T>& b, int tube, T* const* Vin, T*
     Vin[nv][base + i] = bc_flip(0, bc_side(b.bc, i > end), nv, b.ncomp) < 0 ? -v : v;
   }
   __syncthreads();
-  T cm_max = T(0);
   const double gam = b.gamma;
-  for (int lo = beg; lo <= end; lo += B) {
-    const int hi = min(lo + B - 1, end);
-    // states of zones lo-1 .. hi+1
-    for (int z = lo - 1 + tid; z <= hi + 1; z += B) {
-      const int s = z - (lo - 1);
+  const T gmm1 = (T)(gam - 1.0);
+  const int nch = (n + 29) / 30;
+  for (int ch = w; ch < nch; ch += nw) {
+    const int i = beg - 1 + 30 * ch + lane;
+    const bool cell_ok = i <= end + 1;          // zones beg-1 .. end+1
+    const bool face_ok = i <= end && lane < 31;  // interfaces beg-1+1/2 .. end+1/2
+    const long long c = base + i;
+    T vp[NV], vm[NV], v0[NV];
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) {
-        T vp, vm;
-        batch_recon<T, RS>(Vin[nv], base + z, b.limiter, nv, vp, vm);
-        svp[nv * (B + 2) + s] = vp;
-        svm[nv * (B + 2) + s] = vm;
+    for (int nv = 0; nv < NV; nv++) {
+      vp[nv] = vm[nv] = v0[nv] = T(0);
+      if (cell_ok) {
+        batch_recon<T, RS>(Vin[nv], c, b.limiter, nv, vp[nv], vm[nv]);
+        v0[nv] = Vin[nv][c];
       }
     }
-    __syncthreads();
-    // interfaces lo-1+1/2 .. hi+1/2
-    for (int z = lo - 1 + tid; z <= hi; z += B) {
-      const int s = z - (lo - 1);
-      T vL[NV], vR[NV], uL[NV], uR[NV], mach;
+    T vR[NV];
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) {
-        vL[nv] = svp[nv * (B + 2) + s];
-        vR[nv] = svm[nv * (B + 2) + s + 1];
-      }
-      const T gmm1 = (T)(gam - 1.0);
-      prim_to_cons(vL, uL, gmm1);
+    for (int nv = 0; nv < NV; nv++) vR[nv] = __shfl_down_sync(0xffffffffu, vm[nv], 1);
+    T fl[NV], pr = T(0);
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) fl[nv] = T(0);
+    if (face_ok) {
+      T uL[NV], uR[NV], mach;
+      prim_to_cons(vp, uL, gmm1);
       prim_to_cons(vR, uR, gmm1);
       Iface<T> o;
       if (SOLVER == PG_HLL) {
-        hll_solver<0, false>(vL, uL, vR, uR, (T)gam, o, mach);
+        hll_solver<0, false>(vp, uL, vR, uR, (T)gam, o, mach);
       } else if (SOLVER == PG_ROE) {
         int bad = 0;
-        roe_solver<0, false>(vL, uL, vR, uR, (T)gam, b.ncomp == 3, o, mach, bad);
+        roe_solver<0, false>(vp, uL, vR, uR, (T)gam, b.ncomp == 3, o, mach, bad);
         if (bad) atomicOr(b.status, 2);
       } else {
-        hlld_solver<0, false>(vL, uL, vR, uR, (T)gam, o, mach);
+        hlld_solver<0, false>(vp, uL, vR, uR, (T)gam, o, mach);
       }
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) sf[nv * (B + 1) + s] = o.f[nv];
-      sf[NV * (B + 1) + s] = o.press;
+      for (int nv = 0; nv < NV; nv++) fl[nv] = o.f[nv];
+      pr = o.press;
       T cmi = o.cmax * inv_dx;  // update_stage.c:239
       cm_max = (cmi > cm_max || cmi != cmi) ? cmi : cm_max;
     }
-    __syncthreads();
-    // zones lo .. hi
-    for (int z = lo + tid; z <= hi; z += B) {
-      const int s = z - (lo - 1);  // interface z+1/2 is slot s, z-1/2 is s-1
-      T rhs[NV], vin[NV], vout[NV];
+    T flm[NV];
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) {
-        rhs[nv] = -dtdx * (sf[nv * (B + 1) + s] - sf[nv * (B + 1) + s - 1]);
-        vin[nv] = Vin[nv][base + z];
-      }
-      rhs[VX1] -= dtdx * (sf[NV * (B + 1) + s] - sf[NV * (B + 1) + s - 1]);
-      fails += batch_update<T, A, STAGE, NSTAGE>(b, base + z, rhs, vin, vout);
+    for (int nv = 0; nv < NV; nv++) flm[nv] = __shfl_up_sync(0xffffffffu, fl[nv], 1);
+    const T prm = __shfl_up_sync(0xffffffffu, pr, 1);
+    if (lane >= 1 && lane <= 30 && i <= end) {
+      T rhs[NV], vout[NV];
 #pragma unroll
-      for (int nv = 0; nv < NV; nv++) Vout[nv][base + z] = vout[nv];
+      for (int nv = 0; nv < NV; nv++) rhs[nv] = -dtdx * (fl[nv] - flm[nv]);
+      rhs[VX1] -= dtdx * (pr - prm);
+      fails += batch_update<T, A, STAGE, NSTAGE>(b, c, rhs, v0, vout);
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) Vout[nv][c] = vout[nv];
     }
-    __syncthreads();
   }
-  return (double)block_max_T<T>(cm_max, red);
+  __syncthreads();  // the stage output is complete (the next stage reads neighbours)
 }
 
+template <class T>
+__device__ __forceinline__ T block_max_T(T v, T* red) {
+  for (int o = 16; o > 0; o >>= 1) {
+    T w = __shfl_down_sync(0xffffffffu, v, o);
+    v = (w > v || w != w) ? w : v;
+  }
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  if (lane == 0) red[w] = v;
+  __syncthreads();
+  T r = red[0];
+  for (int q = 1; q < (int)(blockDim.x >> 5); q++) r = (red[q] > r || red[q] != red[q]) ? red[q] : r;
+  __syncthreads();  // red is reused
+  return r;
+}
+
+// Persistent kernel: each CTA (a team of NW warps) pulls a tube from the
+// queue (largest first) and runs every step of it with its own dt
+// (NextTimeStep, Src/main.c:459-532; 1D: no division by DIMENSIONS).
 template <class T, class A, int RS, int SOLVER, int NSTAGE>
-__global__ void k_batch(BatchArgs<T> b, int nsteps) {
-  extern __shared__ __align__(16) unsigned char smem_raw[];
-  const int B = blockDim.x;
-  T* svp = (T*)smem_raw;
-  T* svm = svp + NV * (B + 2);
-  T* sf = svm + NV * (B + 2);
-  T* red = sf + (NV + 1) * (B + 1);
+__global__ void __launch_bounds__(256) k_batch(BatchArgs<T> b, int nsteps) {
+  __shared__ T red[8];
   __shared__ int s_t;
   for (;;) {
     if (threadIdx.x == 0) s_t = (int)atomicAdd(b.counter, 1u);
@@ -299,27 +292,14 @@ __global__ void k_batch(BatchArgs<T> b, int nsteps) {
     int cur = b.cur[tube];
     unsigned long long fails = 0;
     for (int step = 0; step < nsteps; step++) {
-      T* A0[NV];
-      T* A1[NV];
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) {
-        A0[nv] = b.V[cur][nv];
-        A1[nv] = b.V[1 - cur][nv];
-      }
-      double inv = 0.0, m;
-      m = batch_stage<T, A, RS, SOLVER, 1, NSTAGE>(b, tube, A0, A1, dt, svp, svm, sf, red, fails);
-      inv = m > inv ? m : inv;
-      if (NSTAGE == 2) {
-        m = batch_stage<T, A, RS, SOLVER, 2, NSTAGE>(b, tube, A1, A0, dt, svp, svm, sf, red, fails);
-        inv = m > inv ? m : inv;
-      } else {
-        m = batch_stage<T, A, RS, SOLVER, 2, NSTAGE>(b, tube, A1, A0, dt, svp, svm, sf, red, fails);
-        inv = m > inv ? m : inv;
-        m = batch_stage<T, A, RS, SOLVER, 3, NSTAGE>(b, tube, A0, A1, dt, svp, svm, sf, red, fails);
-        inv = m > inv ? m : inv;
+      T cm = T(0);
+      batch_stage<T, A, RS, SOLVER, 1, NSTAGE>(b, tube, cur, dt, cm, fails);
+      batch_stage<T, A, RS, SOLVER, 2, NSTAGE>(b, tube, 1 - cur, dt, cm, fails);
+      if (NSTAGE == 3) {
+        batch_stage<T, A, RS, SOLVER, 3, NSTAGE>(b, tube, cur, dt, cm, fails);
         cur = 1 - cur;  // the result of stage 3 is in the other buffer
       }
-      // NextTimeStep, Src/main.c:459-532 (1D: no division by DIMENSIONS);
+      const double inv = (double)block_max_T<T>(cm, red);
       // cfl <= 0 keeps dt fixed
       time += dt;
       if (b.cfl > 0.0) {
@@ -341,9 +321,38 @@ __global__ void k_batch(BatchArgs<T> b, int nsteps) {
   }
 }
 
-template <class T>
-inline size_t batch_smem_bytes(int B) {
-  return sizeof(T) * ((size_t)2 * NV * (B + 2) + (size_t)(NV + 1) * (B + 1) + 32);
+// Mixed path: the resident conserved state U0 of every tube from its
+// primitives (PrimToCons in A), after an upload or a restored snapshot.
+// One CTA per tube.
+template <class A>
+__global__ void k_batch_cons_init(BatchArgs<float> b) {
+  using O = Acc<A>;
+  const int tube = blockIdx.x;
+  if (tube >= b.ntubes) return;
+  const int n = b.nx[tube], ng = b.ng;
+  const long long base = b.off[tube];
+  const int cur = b.cur[tube];
+  const double inv_gmm1_d = 1.0 / (b.gamma - 1.0);
+  const typename O::T inv_gmm1 =
+      O::konst(inv_gmm1_d, (float)inv_gmm1_d, (float)(inv_gmm1_d - (double)(float)inv_gmm1_d));
+  for (int i = ng + threadIdx.x; i < ng + n; i += blockDim.x) {
+    const long long c = base + i;
+    float v[NV];
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) v[nv] = b.V[cur][nv][c];
+    typename O::T u[NV];
+    u[RHO] = O::from(v[RHO]);
+#pragma unroll
+    for (int q = 0; q < 3; q++) {
+      u[VX1 + q] = O::prod(v[RHO], v[VX1 + q]);
+      u[BX1 + q] = O::from(v[BX1 + q]);
+    }
+    typename O::T kin = O::add(O::add(O::prod(v[VX1], v[VX1]), O::prod(v[VX2], v[VX2])), O::prod(v[VX3], v[VX3]));
+    typename O::T b2 = O::add(O::add(O::prod(v[BX1], v[BX1]), O::prod(v[BX2], v[BX2])), O::prod(v[BX3], v[BX3]));
+    u[ENG] = O::add(O::mulf(O::add(O::mulf(kin, v[RHO]), b2), 0.5f), O::mulf(inv_gmm1, v[PRS]));
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) O::st(b.U0[nv], c, u[nv]);
+  }
 }
 
 }  // namespace pg

@@ -7,13 +7,9 @@ namespace pg {
 template <class A>
 static cudaError_t launch_mixed_a(const BatchArgs<float>& b, int rs, int solver, int nstage, int nsteps, int grid,
                                   int threads, cudaStream_t st) {
-  const size_t smem = batch_smem_bytes<float>(threads);
 #define PG_BATCH_CASE(RS_, SOLV_, NST_)                                                               \
   if (rs == RS_ && solver == SOLV_ && nstage == NST_) {                                               \
-    auto k = k_batch<float, A, RS_, SOLV_, NST_>;                                                     \
-    cudaError_t e = cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem); \
-    if (e != cudaSuccess) return e;                                                                   \
-    k<<<grid, threads, smem, st>>>(b, nsteps);                                                        \
+    k_batch<float, A, RS_, SOLV_, NST_><<<grid, threads, 0, st>>>(b, nsteps);                         \
     return cudaGetLastError();                                                                        \
   }
   PG_BATCH_CASE(1, PG_HLLD, 2)
@@ -36,6 +32,12 @@ static cudaError_t launch_mixed_a(const BatchArgs<float>& b, int rs, int solver,
   PG_BATCH_CASE(4, PG_ROE, 3)
 #undef PG_BATCH_CASE
   return cudaErrorInvalidValue;
+}
+
+cudaError_t launch_batch_cons_init(const BatchArgs<float>& b, bool use_dw, cudaStream_t st) {
+  if (use_dw) k_batch_cons_init<pg::dw><<<b.ntubes, 128, 0, st>>>(b);
+  else k_batch_cons_init<pg::f64hw><<<b.ntubes, 128, 0, st>>>(b);
+  return cudaGetLastError();
 }
 
 cudaError_t launch_batch_mixed(const BatchArgs<float>& b, bool use_dw, int rs, int solver, int nstage, int nsteps,

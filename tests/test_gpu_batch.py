@@ -65,8 +65,10 @@ def test_batch_fp64_matches_golden_tubes():
 @pytest.mark.parametrize("prec", ["mixed", "mixed_dw"])
 def test_batch_mixed_close_to_fp64(prec):
     """Mixed batch against the FP64 batch at equal times (fixed dt 1e-4, 200
-    steps): with the CFL dt each precision takes its own dt sequence, and on
-    shock tubes the time offset alone moves the discontinuities."""
+    steps), every tube and variable within relative L1 1e-5: the mixed batch
+    keeps each tube's conserved state resident in the accumulator type.  (With
+    the CFL dt each precision takes its own dt sequence, and on shock tubes
+    the time offset alone moves the discontinuities.)"""
     from pluto_gb300.batch import Batch
     spec, ns, dxs, states = _family(64, 3, 64, 600)
     out, meta = {}, {}
@@ -86,23 +88,42 @@ def test_batch_mixed_close_to_fp64(prec):
     print("worst tube |diff| profile max at", int(d.argmax()), "max", float(d.max()),
           "cells with |diff|>1e-4:", int((d > 1e-4).sum()))
     assert np.array_equal(meta["fp64"][0], meta[prec][0])  # same times
-    # shock tubes: FP32 storage rounding is amplified at the discontinuities
     assert errs[len(errs) // 2][0] <= 1e-6
-    assert errs[-1][0] <= 1e-4, errs[-1]
+    assert errs[-1][0] <= 1e-5, errs[-1]
 
 
-def test_batch_autotune_keeps_results():
+@pytest.mark.parametrize("prec", ["fp64", "mixed"])
+def test_batch_autotune_keeps_results(prec):
     from pluto_gb300.batch import Batch
     spec, ns, dxs, states = _family(40, 11, 32, 400)
-    b = Batch(spec, ns, dxs, "fp64")
+    b = Batch(spec, ns, dxs, prec)
     b.upload(states)
     tun = b.autotune(5, 1e-4, spec["cfl"])
-    assert tun["threads"] in (64, 128, 256, 512)
+    assert tun["threads"] in (64, 128, 256) and tun["largest_first"] == 1
     b.run(30, 1e-4, spec["cfl"])
     got = b.download()
-    ref = Batch(spec, ns, dxs, "fp64")
+    ref = Batch(spec, ns, dxs, prec)
     ref.upload(states)
     ref.run(30, 1e-4, spec["cfl"])
     want = ref.download()
     for t in range(len(ns)):
         assert np.array_equal(got[t], want[t])
+
+
+@pytest.mark.parametrize("prec", ["fp64", "mixed", "mixed_dw"])
+def test_batch_schedule_does_not_change_results(prec):
+    """Every zone's arithmetic is the same whichever warps of the team take
+    its chunk and however many teams share an SM."""
+    from pluto_gb300.batch import Batch
+    spec, ns, dxs, states = _family(50, 13, 16, 700)
+    outs = []
+    for threads, bps, order in ((32, 1, 0), (256, 8, 1), (96, 3, 1)):
+        b = Batch(spec, ns, dxs, prec)
+        b.set_schedule(threads, bps, order)
+        b.upload(states)
+        b.run(40, 1e-4, spec["cfl"])
+        outs.append((b.download(), b.get()))
+    for got, info in outs[1:]:
+        for t in range(len(ns)):
+            assert np.array_equal(got[t], outs[0][0][t])
+        assert np.array_equal(info[0], outs[0][1][0]) and np.array_equal(info[1], outs[0][1][1])
