@@ -1,6 +1,7 @@
 // C ABI of libpluto_gb300: solver lifetime, host<->device transfers, the
 // AdvanceStep-equivalent and the device-resident step loop.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -121,10 +122,17 @@ void init_geom(Solver* S) {
     g.dx[d] = act ? cfg->dx[d] : 1.0;
     g.inv_dx[d] = 1.0 / g.dx[d];  // Src/set_geometry.c:244
   }
+  // Row pitch: the mixed paths pad rows to a multiple of 4 floats so that the
+  // TMA-staged sweeps (16-byte global strides) run at every grid size, e.g.
+  // 768^3 with PPM's 3 ghosts (774-zone rows -> pitch 776).
+  long long pitch = g.nt[0];
+  const bool mixed = cfg->precision == PG_MIXED || cfg->precision == PG_MIXED_DW;
+  const char* tma = getenv("PLUTO_GB300_SWEEP_TMA");
+  if (mixed && g.dims >= 2 && !(tma && tma[0] == '0')) pitch = (pitch + 3) & ~3LL;
   g.s[0] = 1;
-  g.s[1] = g.nt[0];
-  g.s[2] = (long long)g.nt[0] * g.nt[1];
-  g.ncell = (long long)g.nt[0] * g.nt[1] * g.nt[2];
+  g.s[1] = pitch;
+  g.s[2] = pitch * g.nt[1];
+  g.ncell = pitch * g.nt[1] * g.nt[2];
 }
 
 void set_last_error(const char* msg) { g_last_error = msg; }
@@ -220,7 +228,7 @@ extern "C" int pg_set_userdef(pg_solver* h, pg_userdef_fn fn, void* user, double
     return (double*)d;
   };
   for (int nv = 0; nv < 8; nv++) {
-    S->ud_dev_v[nv] = reach(vars[nv], (size_t)g.ncell, nv);
+    S->ud_dev_v[nv] = reach(vars[nv], (size_t)host_cells(g), nv);
     if (vars[nv] && !S->ud_dev_v[nv]) return fail(PG_ERR_CUDA, "pg_set_userdef: host array not reachable");
   }
   for (int d = 0; d < 3; d++) {
@@ -260,7 +268,7 @@ extern "C" int pg_set_internal_boundary(pg_solver* h, unsigned char* flags) {
       d = flags;
     } else {
       cudaGetLastError();
-      if (cudaHostRegister(flags, (size_t)S->g.ncell, cudaHostRegisterMapped) != cudaSuccess ||
+      if (cudaHostRegister(flags, (size_t)host_cells(S->g), cudaHostRegisterMapped) != cudaSuccess ||
           cudaHostGetDevicePointer((void**)&d, flags, 0) != cudaSuccess) {
         cudaGetLastError();
         return fail(PG_ERR_CUDA, "pg_set_internal_boundary: flag array not reachable");
@@ -299,6 +307,8 @@ int xfer_f64(Solver* S, double* dev, double* host, int fd, int layout, bool to_d
   }
   const size_t e = sizeof(double);
   cudaMemcpyKind kind = to_dev ? cudaMemcpyHostToDevice : cudaMemcpyDeviceToHost;
+  // the FP64 arrays have unpadded rows (only the mixed paths pad them)
+  if (g.s[1] != g.nt[0]) return fail(PG_ERR_INVALID, "xfer_f64: padded rows");
   if (layout == PG_LAYOUT_PLUTO) {
     if (fd < 0) {
       size_t n = (size_t)g.ncell;

@@ -20,14 +20,20 @@ struct Geom {
   int beg[3];      // first interior index (0 on inactive axes)
   int end[3];      // last interior index
   int nx[3];       // interior cells
-  long long s[3];  // strides in elements: 1, nt0, nt0*nt1
-  long long ncell;
+  // strides in elements: 1, the row pitch P, P*nt1.  P = nt0, except on the
+  // mixed path where rows are padded to a multiple of 4 floats (16 bytes, the
+  // TMA stride rule); the padding zones are never read or written.
+  long long s[3];
+  long long ncell;  // elements of one device array: P*nt1*nt2 (host arrays: nt0*nt1*nt2)
   double dx[3], inv_dx[3];
 };
 
 __host__ __device__ inline long long cidx(const Geom& g, int k, int j, int i) {
-  return ((long long)k * g.nt[1] + j) * g.nt[0] + i;
+  return (long long)k * g.s[2] + (long long)j * g.s[1] + i;
 }
+
+// zones of one host array in PLUTO's ghosted layout (no row padding)
+inline long long host_cells(const Geom& g) { return (long long)g.nt[0] * g.nt[1] * g.nt[2]; }
 
 // Inclusive index box.
 struct Box {

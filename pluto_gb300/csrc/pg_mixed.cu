@@ -217,8 +217,7 @@ __global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_l
   const int i = g.beg[0] - 1 + 30 * wx + lane;
   const bool cell_ok = i <= g.end[0] + 1;          // cells beg-1 .. end+1
   const bool face_ok = i <= g.end[0] && lane < 31;  // interfaces beg-1+1/2 .. end+1/2
-  const int nt0 = g.nt[0];
-  const int c = (k * g.nt[1] + j) * nt0 + i;
+  const int c = (k * g.nt[1] + j) * (int)g.s[1] + i;
   // loaded up front so that their latency overlaps the reconstruction
   const float bn = (CT && face_ok) ? a.Bin[0][c] : 0.f;
   const float scrh = a.sc->dtdx[0];
@@ -301,7 +300,7 @@ __global__ void __launch_bounds__(32 * kXR, 2)
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const bool leader = threadIdx.x == 0;
   const float scrh = a.sc->dtdx[0];
-  const int nt0 = g.nt[0];
+  const int pitch = (int)g.s[1];
   const uint32_t tx_bytes = (uint32_t)((8 + (CT ? 1 : 0)) * kXR * kXW * 4);
   if (leader) {
     mbar_init(&bar[0], 1);
@@ -353,7 +352,7 @@ __global__ void __launch_bounds__(32 * kXR, 2)
       const int i = cs + 30 * q + lane;
       const bool cell_ok = row_ok && i <= g.end[0] + 1;
       const bool face_ok = row_ok && i <= g.end[0] && lane < 31;
-      const int c = (k * g.nt[1] + j) * nt0 + i;
+      const int c = (k * g.nt[1] + j) * pitch + i;
       const int x = i - xs;  // column in the staged rows
       float vp[NV], vm[NV];
 #pragma unroll
@@ -432,8 +431,8 @@ __global__ void __launch_bounds__(32 * kTY, 2) k_msweep_t(MixArgs a, int solver,
   const bool col_ok = ii < i_n && bo < o_n;
   const bool cell_ok = col_ok && m <= end + 1;               // cells beg-1 .. end+1
   const bool face_ok = col_ok && m <= end && ty < kTY - 1;   // interfaces beg-1+1/2 .. end+1/2
-  const int s = DIR == 1 ? g.nt[0] : g.nt[0] * g.nt[1];
-  const int c = (DIR == 1 ? (other * g.nt[1]) * g.nt[0] + i : other * g.nt[0] + i) + m * s;
+  const int s = (int)g.s[DIR];
+  const int c = (DIR == 1 ? other * (int)g.s[2] : other * (int)g.s[1]) + i + m * s;
   // the accumulated update of this zone, loaded now so that its latency
   // overlaps the reconstruction and the Riemann problem
   const bool upd = ty >= 1 && ty <= kTY - 2 && col_ok && m >= beg && m <= end;
@@ -531,7 +530,7 @@ __global__ void __launch_bounds__(32 * kTY, 2)
   const int tx = threadIdx.x, ty = threadIdx.y;
   const bool leader = tx == 0 && ty == 0;
   const int beg = g.beg[DIR], end = g.end[DIR];
-  const int s = DIR == 1 ? g.nt[0] : g.nt[0] * g.nt[1];
+  const int s = (int)g.s[DIR];
   const float scrh = a.sc->dtdx[DIR];
   const uint32_t tx_bytes = (uint32_t)((8 * R + 8 * NU + (stage1 ? NU : 0) + (CT ? NF : 0)) * 32 * 4);
   if (leader) {
@@ -587,7 +586,7 @@ __global__ void __launch_bounds__(32 * kTY, 2)
     const bool cell_ok = col_ok && m <= end + 1;
     const bool face_ok = col_ok && m <= end && ty < kTY - 1;
     const bool upd = ty >= 1 && ty <= kTY - 2 && col_ok && m >= beg && m <= end;
-    const int c = (DIR == 1 ? (other * g.nt[1]) * g.nt[0] + i : other * g.nt[0] + i) + m * s;
+    const int c = (DIR == 1 ? other * (int)g.s[2] : other * (int)g.s[1]) + i + m * s;
     const float* sV = smem + b * BUF;
     const float* sDU = sV + 8 * R * 32;
     const float* sCDT = sDU + 8 * NU * 32;
@@ -1051,7 +1050,9 @@ static bool mixed_prepare_tma_rs(Solver* S, MixedState* M) {
     return false;
   }
   const uint64_t d4[4] = {(uint64_t)g.nt[0], (uint64_t)g.nt[1], (uint64_t)g.nt[2], 8};
-  const uint64_t s4[3] = {(uint64_t)g.nt[0] * 4, (uint64_t)g.nt[0] * g.nt[1] * 4, (uint64_t)g.ncell * 4};
+  // global extents: the logical rows (loads past nt0 read the fill value);
+  // strides: the padded row pitch
+  const uint64_t s4[3] = {(uint64_t)g.s[1] * 4, (uint64_t)g.s[2] * 4, (uint64_t)g.ncell * 4};
   for (int sb = 0; sb < 2; sb++) {
     const uint32_t bv[4] = {kXW, kXR, 1, 8};
     const uint32_t bf[3] = {kXW, kXR, 1};
@@ -1083,7 +1084,7 @@ static bool mixed_prepare_tma(Solver* S, MixedState* M) {
   const char* env = getenv("PLUTO_GB300_SWEEP_TMA");
   if (env && env[0] == '0') return false;
   const Geom& g = S->g;
-  if (g.dims < 2 || (g.nt[0] % 4) != 0) return false;
+  if (g.dims < 2 || (g.s[1] % 4) != 0) return false;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
   int rs;
   if (S->cfg.reconstruction == PG_PARABOLIC) rs = RS_PPM;
@@ -1449,21 +1450,14 @@ int mixed_enqueue_step(Solver* S) {
 using namespace pg;
 
 // Host transfers for the mixed path: FP64 host arrays <-> FP32 device state.
-__global__ void k_f64_to_f32(const double* src, float* dst, long long n) {
-  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q < n) dst[q] = (float)src[q];
-}
-__global__ void k_f32_to_f64(const float* src, double* dst, long long n) {
-  long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q < n) dst[q] = (double)src[q];
-}
-
 static int mixed_xfer(Solver* S, const double* const vars[8], double* const outv[8], const double* const faces[3],
                       double* const outf[3], int layout, bool to_dev) {
   MixedState* M = (MixedState*)S->mixed;
   const Geom& g = S->g;
-  const long long n = g.ncell;
-  double* tmp = nullptr;  // FP64 staging array, only for host memory the device cannot reach
+  // pinned staging, only for host memory the device cannot reach: one array
+  // in the host layout (the device arrays may have padded rows)
+  double* pin = nullptr;
+  size_t pin_n = 0;
   int rc = PG_OK;
   const int cur = M->cur;
   auto one = [&](float* dev, const double* hin, double* hout, int fd) -> int {
@@ -1471,34 +1465,38 @@ static int mixed_xfer(Solver* S, const double* const vars[8], double* const outv
       launch_host_xfer<float>(S->stream, alias, dev, g, fd, layout, to_dev);
       return cudaGetLastError() == cudaSuccess ? PG_OK : PG_ERR_CUDA;
     }
-    if (!tmp && cudaMalloc(&tmp, n * sizeof(double)) != cudaSuccess) return PG_ERR_NOMEM;
-    if (to_dev) {
-      cudaMemsetAsync(tmp, 0, n * sizeof(double), S->stream);
-      int r = xfer_f64(S, tmp, (double*)hin, fd, layout, true);
-      if (r) return r;
-      k_f64_to_f32<<<grid_for(n), kThreads, 0, S->stream>>>(tmp, dev, n);
-      return PG_OK;
+    const HostBox hb = host_box(g, fd, layout);
+    const size_t n = (size_t)hb.hn[0] * hb.hn[1] * hb.hn[2];
+    if (n > pin_n) {
+      if (pin) cudaFreeHost(pin);
+      pin = nullptr;
+      pin_n = 0;
+      if (cudaHostAlloc((void**)&pin, n * sizeof(double), cudaHostAllocMapped) != cudaSuccess) return PG_ERR_NOMEM;
+      pin_n = n;
     }
-    k_f32_to_f64<<<grid_for(n), kThreads, 0, S->stream>>>(dev, tmp, n);
-    return xfer_f64(S, tmp, hout, fd, layout, false);
+    double* alias = host_alias(pin);
+    if (!alias) return PG_ERR_CUDA;
+    if (to_dev) memcpy(pin, hin, n * sizeof(double));
+    launch_host_xfer<float>(S->stream, alias, dev, g, fd, layout, to_dev);
+    if (cudaStreamSynchronize(S->stream) != cudaSuccess) return PG_ERR_CUDA;  // the staging array is reused
+    if (!to_dev) memcpy(hout, pin, n * sizeof(double));
+    return PG_OK;
   };
   for (int nv = 0; nv < 8 && !rc; nv++) {
     if (to_dev) {
       if (vars[nv]) rc = one(M->b.V[cur][nv], vars[nv], nullptr, -1);
-      else cudaMemsetAsync(M->b.V[cur][nv], 0, n * sizeof(float), S->stream);
+      else cudaMemsetAsync(M->b.V[cur][nv], 0, g.ncell * sizeof(float), S->stream);
     } else if (outv[nv]) {
       rc = one(M->b.V[cur][nv], nullptr, outv[nv], -1);
     }
-    if (tmp) cudaStreamSynchronize(S->stream);  // the staging array is reused
   }
   if (S->cfg.divb == PG_CONSTRAINED_TRANSPORT)
     for (int d = 0; d < g.dims && !rc; d++) {
       if (to_dev && faces && faces[d]) rc = one(M->b.Bs[cur][d], faces[d], nullptr, d);
       if (!to_dev && outf && outf[d]) rc = one(M->b.Bs[cur][d], nullptr, outf[d], d);
-      if (tmp) cudaStreamSynchronize(S->stream);
     }
   if (cudaStreamSynchronize(S->stream) != cudaSuccess && !rc) rc = PG_ERR_CUDA;
-  if (tmp) cudaFree(tmp);
+  if (pin) cudaFreeHost(pin);
   return rc;
 }
 

@@ -114,11 +114,15 @@ inline void CUDART_CB ud_host_call(void* p) {
   for (int fd = 0; fd < c->nbfield; fd++) S->ud_fn(S->ud_user, c->side, 1 + fd, c->stage);  // X*FACE
 }
 
-__global__ inline void k_flag_xfer(unsigned char* host, unsigned char* dev, long long n, int to_dev) {
+// zone flags: host array in PLUTO's layout, device array with the row pitch
+__global__ inline void k_flag_xfer(unsigned char* host, unsigned char* dev, Geom g, int to_dev) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= n) return;
-  if (to_dev) dev[q] = host[q];
-  else host[q] = dev[q];
+  if (q >= (long long)g.nt[0] * g.nt[1] * g.nt[2]) return;
+  const int i = (int)(q % g.nt[0]);
+  const long long r = q / g.nt[0];
+  const long long c = cidx(g, (int)(r / g.nt[1]), (int)(r % g.nt[1]), i);
+  if (to_dev) dev[c] = host[q];
+  else host[q] = dev[c];
 }
 
 // INTERNAL_BOUNDARY (Src/boundary.c:90-92): before the fill, the callback
@@ -155,7 +159,7 @@ inline void launch_internal_boundary(Solver* S, T* const V[8], T* const Bs[3], T
       fb.lo[fd] = -1;
       k_box_xfer<T><<<grid_for(fb.count()), kThreads, 0, st>>>(S->ud_dev_f[fd], Bs[fd], Bm1[fd], g, fd, fb, up);
     }
-    k_flag_xfer<<<grid_for(g.ncell), kThreads, 0, st>>>(S->ud_dev_flag, dflag, g.ncell, up);
+    k_flag_xfer<<<grid_for(host_cells(g)), kThreads, 0, st>>>(S->ud_dev_flag, dflag, g, up);
   }
 }
 

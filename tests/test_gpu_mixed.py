@@ -158,3 +158,54 @@ def test_mixed_rk3_ppm_turbulence_small(prec):
         out[p] = s.download()[0]
     errs = [rel_l1(out[prec][q], out["fp64"][q]) for q in range(8)]
     assert max(errs) <= 1e-5, errs
+
+
+def _padded_cases():
+    """Grids whose ghosted rows are not a multiple of 4 floats: the mixed
+    solvers pad the row pitch (TMA sweeps) unless the TMA sweeps are off."""
+    from pluto_gb300 import problems as P
+    out = {}
+    spec, vc, f = P.blast3d(30)                                  # rows 34 -> pitch 36
+    out["blast3d_30"] = (spec, vc, f)
+    spec, vc, f = P.turbulence3d(24)                             # PPM: rows 30 -> pitch 32
+    out["turb3d_24_ppm_rk3"] = (spec, vc, f)
+    meta = load_golden("ot_userdef_32")[0]                       # USERDEF side + CT, 2D
+    spec, vc, f = P.orszag_tang(30)
+    out["ot2d_30_userdef"] = (dict(meta, nx=spec["nx"], dx=spec["dx"]), vc, f)
+    meta = load_golden("ot_internal_32")[0]                      # INTERNAL_BOUNDARY, flags moved
+    out["ot2d_30_internal"] = (dict(meta, nx=spec["nx"], dx=spec["dx"]), vc, f)
+    meta = load_golden("blast_userdef_ct_16")[0]                 # 3D USERDEF sides + CT
+    spec, vc, f = P.blast3d(18)
+    out["blast3d_18_userdef_ct"] = (dict(meta, nx=spec["nx"], dx=spec["dx"]), vc, f)
+    return out
+
+
+@pytest.mark.parametrize("prec", MIXED)
+@pytest.mark.parametrize("case", ["blast3d_30", "turb3d_24_ppm_rk3", "ot2d_30_userdef", "ot2d_30_internal",
+                                  "blast3d_18_userdef_ct"])
+def test_padded_rows_match_unpadded(case, prec, monkeypatch):
+    """With padded rows the TMA sweeps run (and every transfer, boundary,
+    user callback and flag copy maps the pitch); the result equals the
+    unpadded direct-load solver to FP32 round-off, and stays within the
+    mixed bar of the FP64 path."""
+    spec, vc, f = _padded_cases()[case]
+    out, names = {}, {}
+    for tma in ("1", "0"):
+        monkeypatch.setenv("PLUTO_GB300_SWEEP_TMA", tma)
+        s = _s(spec, prec)
+        s.upload(vc, f)
+        names[tma] = set(s.profile_kernels(1, spec["first_dt"], spec["cfl"]))
+        s.upload(vc, f)
+        s.run(6, spec["first_dt"], spec["cfl"])
+        out[tma] = s.download()
+    assert "mixed_sweep_y_tma" in names["1"] and "mixed_sweep_y_tma" not in names["0"], names
+    ref = _s(spec, "fp64")
+    ref.upload(vc, f)
+    ref.run(6, spec["first_dt"], spec["cfl"])
+    want = ref.download()
+    for other, bar in ((out["0"], 1e-6), (want, 1e-5)):
+        errs = {q: rel_l1(out["1"][0][q], other[0][q]) for q in range(8) if np.abs(other[0][q]).sum() > 0}
+        for d in range(3):
+            if other[1][d] is not None:
+                errs[f"b{d}"] = rel_l1(out["1"][1][d], other[1][d])
+        assert max(errs.values()) <= bar, errs

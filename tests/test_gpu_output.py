@@ -144,3 +144,22 @@ def test_download_async_snapshots_each_step(precision):
         assert np.array_equal(vc, wv)
         for d in range(3):
             assert np.array_equal(bs[d], wb[d])
+
+
+def test_mixed_output_with_padded_rows(tmp_path):
+    """A mixed solver whose device rows are padded (30 + 4 ghosts -> pitch
+    36) writes the same files as the CPU writer fed with its download."""
+    from pluto_gb300 import Solver, problems
+    spec, vc0, f0 = problems.orszag_tang(30)
+    s = Solver(spec, precision="mixed")
+    s.upload(vc0, f0)
+    s.run(3, 1e-3, 0.4)
+    vc, bs = s.download()
+    (tmp_path / "gpu").mkdir()
+    for fmt in ("dbl", "flt", "vtk"):
+        s.write_output(tmp_path / "gpu", fmt, 2, xbeg=(0, 0, 0), xend=(1, 1, 1), time=0.5, dt=0.01, step=3)
+        ow.write(tmp_path / "cpu", fmt, 2, vc, bs, 2, 2, True,
+                 xnode=[ow.nodes(0.0, 1.0, 30), ow.nodes(0.0, 1.0, 30), ow.nodes(0.0, 1.0, 1)],
+                 time=0.5, dt=0.01, step=3)
+    s.output_wait()
+    assert _files(tmp_path / "gpu") == _files(tmp_path / "cpu")
