@@ -678,7 +678,7 @@ Box dir_box(const Geom& g, int dir, int lo_off, int hi_off, bool ct) {
       b.hi[ax] = g.end[ax] + e;
     }
   }
-  return b;
+  return b.prepare();
 }
 
 // Recompute the states and Riemann outputs along DIR from the solver's V/Bs.
@@ -764,6 +764,7 @@ void rev_stage(Solver* S, const AdjArgs& A, bool add_b0) {
         eb.lo[ax] = eb.hi[ax] = 0;
       }
     }
+    eb.prepare();
     k_adj_emf<<<grid_for(eb.count() * kEdgeIn * (g.dims == 3 ? 3 : 1), 64), 64, 0, st>>>(A, eb);
   }
   if (g.dims > 2) rev_dir<2>(S, A);
@@ -942,6 +943,7 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
     dom.lo[ax] = g.beg[ax];
     dom.hi[ax] = g.end[ax];
   }
+  dom.prepare();
   const F64A<double> f = make_args<double>(S);
   launch_bound<double>(S, f);
   k_begin_step<double><<<grid_for(n), kT, 0, st>>>(f, dom);

@@ -557,7 +557,7 @@ static Box ctu_box(const Geom& g, int dir, int nlo, int nhi, int ext) {
       b.hi[ax] = g.end[ax] + ext;
     }
   }
-  return b;
+  return b.prepare();
 }
 static Box ctu_cube(const Geom& g, int lo_off, int hi_off) {
   Box b;
@@ -568,7 +568,7 @@ static Box ctu_cube(const Geom& g, int lo_off, int hi_off) {
       b.hi[ax] = g.end[ax] + hi_off;
     }
   }
-  return b;
+  return b.prepare();
 }
 
 template <class T, int DIR, int STAGE>

@@ -256,8 +256,11 @@ __global__ void k_recon(F64A<T> a, Box box) {
     a.VP[nv][c] = vp[nv];
     a.VM[nv][c] = vm[nv];
   }
-  if (a.ct)
-    for (int comp = 0; comp < g.dims; comp++) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+  if (a.ct) {  // compile-time indices keep vp/vm in registers
+#pragma unroll
+    for (int comp = 0; comp < 3; comp++)
+      if (comp < g.dims) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+  }
 }
 
 // Riemann problem at interface c+1/2 along DIR.
@@ -470,8 +473,11 @@ __global__ void k_finalize(F64A<T> a, Box dom, int reduce_cdt) {
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) u[nv] = one_third * (a.U0[nv][c] + 2.0 * u[nv]);
     }
-    if (a.ct)
-      for (int d = 0; d < g.dims; d++) u[BX1 + d] = 0.5 * (a.Bs[d][c] + a.Bs[d][c - g.s[d]]);
+    if (a.ct) {
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+        if (d < g.dims) u[BX1 + d] = 0.5 * (a.Bs[d][c] + a.Bs[d][c - g.s[d]]);
+    }
     unsigned char fl = a.flag[c];
     fails = cons_to_prim(u, v, T(a.gamma - 1.0), T(a.small_rho), T(a.small_p), &fl);
     if (fails) a.flag[c] |= fl;  // flag[i] |= FLAG_CONS2PRIM_FAIL (mappers.c)
@@ -594,7 +600,7 @@ static Box sweep_box(const Geom& g, int dir, int along_lo_off, int along_hi_off,
       b.hi[ax] = g.end[ax] + ext;
     }
   }
-  return b;
+  return b.prepare();
 }
 
 template <class T, int DIR>
@@ -639,6 +645,7 @@ static void launch_stage_tail(Solver* S, const F64A<T>& a, const Box& dom) {
       if (ax < g.dims) { eb.lo[ax] = g.beg[ax] - 1; eb.hi[ax] = g.end[ax]; }
       else { eb.lo[ax] = eb.hi[ax] = 0; }
     }
+    eb.prepare();
     if (a.emf_avg == PG_UCT_HLL)
       PG_LAUNCH(S, "fp64_emf", (k_emf<T><<<grid_for(eb.count(), 128), 128, 0, st>>>(a, eb)));
     else  // every RK stage integrates to the corner like the CTU corrector (no CTU guard)
@@ -680,6 +687,7 @@ static void enqueue_rk(Solver* S, const F64A<T>& a) {
   const Geom& g = S->g;
   Box dom;
   for (int ax = 0; ax < 3; ax++) { dom.lo[ax] = g.beg[ax]; dom.hi[ax] = g.end[ax]; }
+  dom.prepare();
   cudaStream_t st = S->stream;
   // stage 1
   launch_bound(S, a);

@@ -35,14 +35,52 @@ __host__ __device__ inline long long cidx(const Geom& g, int k, int j, int i) {
 // zones of one host array in PLUTO's ghosted layout (no row padding)
 inline long long host_cells(const Geom& g) { return (long long)g.nt[0] * g.nt[1] * g.nt[2]; }
 
-// Inclusive index box.
+// Inclusive index box.  coords() decodes a linear thread index into (i,j,k);
+// after prepare() it divides by the box extents with the multiply-and-shift
+// method of Granlund and Montgomery ("Division by invariant integers using
+// multiplication", PLDI 1994, sec. 4) on 32-bit indices, so no integer
+// division runs on the device (64-bit division is a long instruction
+// sequence, and the conversions of the 32-bit one issue on the FP64 pipe).
 struct Box {
   int lo[3], hi[3];
+  unsigned mi = 0, mj = 0;                  // magic multipliers (0: not prepared)
+  unsigned char si1 = 0, si2 = 0, sj1 = 0, sj2 = 0;
   __host__ __device__ long long count() const {
     return (long long)(hi[0] - lo[0] + 1) * (hi[1] - lo[1] + 1) * (hi[2] - lo[2] + 1);
   }
+  // magic numbers for an unsigned 32-bit division by d >= 1:
+  // l = ceil(log2 d), m = floor(2^32 (2^l - d) / d) + 1, n / d =
+  // (t + ((n - t) >> min(l, 1))) >> max(l - 1, 0) with t = umulhi(n, m)
+  static void magic(unsigned d, unsigned& m, unsigned char& s1, unsigned char& s2) {
+    int l = 0;
+    while ((1ull << l) < d) l++;
+    m = (unsigned)((((1ull << l) - d) << 32) / d + 1);
+    s1 = (unsigned char)(l < 1 ? l : 1);
+    s2 = (unsigned char)(l > 1 ? l - 1 : 0);
+  }
+  __host__ Box& prepare() {
+    mi = mj = 0;
+    if (count() < (1ll << 32)) {
+      magic((unsigned)(hi[0] - lo[0] + 1), mi, si1, si2);
+      magic((unsigned)(hi[1] - lo[1] + 1), mj, sj1, sj2);
+    }
+    return *this;
+  }
+  __device__ static unsigned fdiv(unsigned n, unsigned m, unsigned s1, unsigned s2) {
+    const unsigned t = __umulhi(n, m);
+    return (t + ((n - t) >> s1)) >> s2;
+  }
   __device__ void coords(long long q, int& i, int& j, int& k) const {
     int ni = hi[0] - lo[0] + 1, nj = hi[1] - lo[1] + 1;
+    if (mi) {  // prepared: 32-bit multiply-and-shift division
+      const unsigned u = (unsigned)q;
+      const unsigned r = fdiv(u, mi, si1, si2);
+      const unsigned p = fdiv(r, mj, sj1, sj2);
+      i = lo[0] + (int)(u - r * (unsigned)ni);
+      j = lo[1] + (int)(r - p * (unsigned)nj);
+      k = lo[2] + (int)p;
+      return;
+    }
     i = lo[0] + (int)(q % ni);
     q /= ni;
     j = lo[1] + (int)(q % nj);

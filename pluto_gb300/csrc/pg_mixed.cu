@@ -232,8 +232,11 @@ __global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_l
       recon<RS>(a.limiter, nv, w2, __ldg(V + c - 1), __ldg(V + c), __ldg(V + c + 1), e2, vp[nv], vm[nv]);
     }
   }
-  if (CT && cell_ok)
-    for (int comp = 0; comp < g.dims; comp++) a.DV[0][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+  if (CT && cell_ok) {  // compile-time indices keep vp/vm in registers
+#pragma unroll
+    for (int comp = 0; comp < 3; comp++)
+      if (comp < g.dims) a.DV[0][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+  }
   float vR[NV];
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) vR[nv] = __shfl_down_sync(0xffffffffu, vm[nv], 1);
@@ -365,8 +368,11 @@ __global__ void __launch_bounds__(32 * kXR, 2)
           recon<RS>(a.limiter, nv, w2, p[-1], p[0], p[1], e2, vp[nv], vm[nv]);
         }
       }
-      if (CT && cell_ok)
-        for (int comp = 0; comp < g.dims; comp++) a.DV[0][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+      if (CT && cell_ok) {  // compile-time indices keep vp/vm in registers
+#pragma unroll
+        for (int comp = 0; comp < 3; comp++)
+          if (comp < g.dims) a.DV[0][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+      }
       float vR[NV];
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) vR[nv] = __shfl_down_sync(0xffffffffu, vm[nv], 1);
@@ -454,8 +460,11 @@ __global__ void __launch_bounds__(32 * kTY, 2) k_msweep_t(MixArgs a, int solver,
     }
     svm[nv][ty][tx] = vm[nv];
   }
-  if (CT && cell_ok)
-    for (int comp = 0; comp < g.dims; comp++) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+  if (CT && cell_ok) {  // compile-time indices keep vp/vm in registers
+#pragma unroll
+    for (int comp = 0; comp < 3; comp++)
+      if (comp < g.dims) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+  }
   __syncthreads();
   float fl[NV], pr = 0.f, cm = 0.f;
 #pragma unroll
@@ -603,8 +612,11 @@ __global__ void __launch_bounds__(32 * kTY, 2)
       }
       svm[(nv * kTY + ty) * 32 + tx] = vm[nv];
     }
-    if (CT && cell_ok)
-      for (int comp = 0; comp < g.dims; comp++) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+    if (CT && cell_ok) {  // compile-time indices keep vp/vm in registers
+#pragma unroll
+      for (int comp = 0; comp < 3; comp++)
+        if (comp < g.dims) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+    }
     __syncthreads();
     float fl[NV], pr = 0.f, cm = 0.f;
 #pragma unroll
@@ -853,9 +865,11 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
       }
     }
     // CT_AverageMagneticField: staggered components from the new faces
-    if (a.ct)
-      for (int d = 0; d < g.dims; d++)
-        u.b[d] = O::avg2(a.Bout[d][c], a.Bout[d][c - g.s[d]]);
+    if (a.ct) {  // compile-time indices keep the state in registers
+#pragma unroll
+      for (int d = 0; d < 3; d++)
+        if (d < g.dims) u.b[d] = O::avg2(a.Bout[d][c], a.Bout[d][c - g.s[d]]);
+    }
     // ConsToPrim (Src/MHD/mappers.c:88-254) with the pressure recovered in A
     unsigned char fl = 0;
     if (O::neg(u.rho)) {
@@ -1256,6 +1270,7 @@ static void mlaunch_bound(Solver* S, const MixArgs& a) {
         dom.lo[ax] = g.beg[ax];
         dom.hi[ax] = g.end[ax];
       }
+      dom.prepare();
       V8 prev;
       for (int nv = 0; nv < NV; nv++) prev.p[nv] = M->b.V[other][nv];
       if (S->cfg.precision == PG_MIXED_DW)
@@ -1385,6 +1400,7 @@ static void mlaunch_tail(Solver* S, const MixArgs& a, const Box& dom) {
       if (ax < g.dims) { eb.lo[ax] = g.beg[ax] - 1; eb.hi[ax] = g.end[ax]; }
       else { eb.lo[ax] = eb.hi[ax] = 0; }
     }
+    eb.prepare();
     PG_LAUNCH(S, "mixed_emf", (k_memf<<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb)));
     PG_LAUNCH(S, "mixed_face", (k_mface<STAGE, NSTAGE, A><<<grid_for(eb.count()), kThreads, 0, st>>>(a, eb)));
   }
@@ -1399,6 +1415,7 @@ static void menqueue(Solver* S) {
   const Geom& g = S->g;
   Box dom;
   for (int ax = 0; ax < 3; ax++) { dom.lo[ax] = g.beg[ax]; dom.hi[ax] = g.end[ax]; }
+  dom.prepare();
   const int bA = M->cur, bB = 1 - M->cur;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
   // stage 1: A -> B (EULER: in place, A -> A; the final kernel reads no
@@ -1510,6 +1527,7 @@ int mixed_upload_host(Solver* S, const double* const vars[8], const double* cons
     dom.lo[ax] = S->g.beg[ax];
     dom.hi[ax] = S->g.end[ax];
   }
+  dom.prepare();
   if (S->cfg.precision == PG_MIXED_DW)
     k_mcons_init<dw><<<grid_for(dom.count()), kThreads, 0, S->stream>>>(a, dom);
   else
