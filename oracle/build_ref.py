@@ -84,6 +84,8 @@ class Setup:
     out_modes: tuple = ()            # extra outputs written at the dbl cadence: ((fmt, mode), ...)
     vtk_vector: bool = False         # VTK_VECTOR_DUMP YES
     char_limiting: bool = False      # CHAR_LIMITING YES
+    analysis_body: str = ""          # body of Analysis (called every analysis_every steps)
+    analysis_every: int = -1
 
 
 def _fmt(x: float) -> str:
@@ -185,7 +187,7 @@ tab       -1.0  -1
 ppm       -1.0  -1
 png       -1.0  -1
 log        100000
-analysis  -1.0  -1
+analysis  -1.0  {s.analysis_every}
 
 [Chombo HDF5 output]
 
@@ -211,7 +213,10 @@ void Init (double *v, double x1, double x2, double x3)
 }
 
 void InitDomain (Data *d, Grid *grid) {}
-void Analysis (const Data *d, Grid *grid) {}
+void Analysis (const Data *d, Grid *grid)
+{
+%s
+}
 #if PHYSICS == MHD
 void BackgroundField (double x1, double x2, double x3, double *B0)
 { B0[0] = B0[1] = B0[2] = 0.0; }
@@ -232,7 +237,7 @@ def build(s: Setup, jobs: int = 8) -> Path:
     obj.mkdir(parents=True, exist_ok=True)
     (run / "definitions.h").write_text(definitions_h(s))
     (run / "pluto.ini").write_text(pluto_ini(s))
-    (run / "init.c").write_text(INIT_TEMPLATE % (s.init_body, s.userdef_body))
+    (run / "init.c").write_text(INIT_TEMPLATE % (s.init_body, s.analysis_body, s.userdef_body))
     names = list(BASE_SRC)
     names += ["plm_states"] if s.recon == "LINEAR" else ["ppm_states", "ppm_coeffs"]
     # time stepping: RK (rk_step + update_stage) or CTU (ctu_step + hancock,
