@@ -174,7 +174,7 @@ def kernel_bytes(name, n, stage_mix=True):
 # ---------------------------------------------------------------------------
 # CPU baseline: the oracle (plain-C restatement of the reference path)
 # ---------------------------------------------------------------------------
-def cpu_rate(n=96, budget_s=12.0, threads=None):
+def cpu_rate(n=192, budget_s=15.0, threads=None):
     from oracle.oracle import Oracle
     from pluto_gb300 import problems
     threads = threads or os.cpu_count() or 1
@@ -200,8 +200,10 @@ def reference_arm(args, rank, ws):
     """--impl reference: the reference algorithm on the host cores.  The
     reference C binary cannot be built on the benchmark machine (an Arm host
     without the reference source tree), so the oracle port -- bit-identical
-    to it on the golden problems -- is timed, with all host threads, one
-    bounded sample per step."""
+    to it on the golden problems and on the fixtures at the configurations'
+    sizes -- is timed, with all host threads, one step of the same blast
+    scheme at --ref-n^3 per bench step (a 512^3 step takes ~16 s on 16 Grace
+    cores, too long for the bench's step counts)."""
     if rank != 0:
         return
     from oracle.oracle import Oracle, build as obuild
@@ -538,7 +540,7 @@ def main():
     ap.add_argument("--l1-steps", type=int, default=100)
     ap.add_argument("--l1-n", type=int, default=512)
     ap.add_argument("--e2e-steps", type=int, default=30)
-    ap.add_argument("--ref-n", type=int, default=96)
+    ap.add_argument("--ref-n", type=int, default=192)
     ap.add_argument("--no-cpu", action="store_true")
     ap.add_argument("--tubes", type=int, default=4096)
     ap.add_argument("--tube-seed", type=int, default=0)

@@ -123,13 +123,20 @@ int pg_destroy(pg_solver *s);
    PG_LAYOUT_PLUTO: PLUTO's in-memory arrays including ghost zones,
      d->Vc[nv] = [NX3_TOT][NX2_TOT][NX1_TOT] and d->Vs[d] allocated as an
      ArrayBox with index origin -1 along d (Src/initialize.c:448-453); pass
-     the pointer to element [-1] (i.e. the start of the allocation). */
+     the pointer to element [-1] (i.e. the start of the allocation).
+   pg_upload also clears the sticky error state of earlier steps (a step that
+   returned PG_ERR_NAN or PG_ERR_TIMEOUT left invalid results; upload a valid
+   state to continue). */
 int pg_upload(pg_solver *s, const double *const vars[8], const double *const faces[3],
               int layout);
 int pg_download(pg_solver *s, double *const vars[8], double *const faces[3], int layout);
 
 /* One AdvanceStep with time step dt (host value of g_dt).  Blocks until the
-   step is complete and fills info (may be NULL). */
+   step is complete and fills info (may be NULL).  PG_ERR_TIMEOUT: a bounded
+   device-side wait ran out (the mixed paths' TMA tile waits; the environment
+   variable PLUTO_GB300_TILE_WAIT_TRIES, read when a step is enqueued, sets
+   their try limit -- 0 makes every such wait time out, for testing the
+   error path); the kernels return, the context stays usable. */
 int pg_advance(pg_solver *s, double dt, pg_step_info *info);
 
 /* The reference main loop for nsteps steps without host round trips:
@@ -168,6 +175,14 @@ int pg_profile_kernels(pg_solver *s, int nsteps, double first_dt, double cfl, do
 int pg_tangent_upload(pg_solver *s, const double *const vars[8], const double *const faces[3],
                       int layout);
 int pg_tangent_download(pg_solver *s, double *const vars[8], double *const faces[3], int layout);
+/* Kink margin of the tangent-linear step (PG_FP64_TANGENT, no reference
+   counterpart): enable = 1 starts recording, enable = 0 stops it and returns
+   in *margin the smallest |a - b| / |a' - b'| over every comparison the
+   steps made in between (limiter signs, MIN/MAX, Riemann-fan regions,
+   floors, |x|), a' the derivative along the uploaded tangent direction: the
+   perturbation size along that direction at which, to first order, some
+   branch of the computation would switch (+inf: none depends on it). */
+int pg_tangent_kink(pg_solver *s, int enable, double *margin);
 
 /* PG_FP64 solvers with RK2: adjoint of one step.  pg_adjoint_set loads the
    adjoint (gradient of a scalar with respect to the state after the step)

@@ -109,21 +109,27 @@ def rollout(runner: Rollout, vc: torch.Tensor, *faces: torch.Tensor):
     return _RolloutFn.apply(runner, vc, *faces)
 
 
-def tangent_linear(spec: dict, dts, vc, faces, dvc, dfaces):
-    """FP64 tangent-linear model: (final state, its derivative along (dvc, dfaces))."""
+def tangent_linear(spec: dict, dts, vc, faces, dvc, dfaces, kink: bool = False):
+    """FP64 tangent-linear model: (final state, its derivative along (dvc,
+    dfaces)); with kink=True also the kink margin of the run (the smallest
+    perturbation along the direction at which, to first order, some branch of
+    some step switches; see Solver.tangent_kink)."""
     s = Solver(spec, "fp64_tangent")
     try:
         fl = [faces[d] if (s.ct and d < s.dims) else None for d in range(3)]
         dl = [dfaces[d] if (s.ct and d < s.dims) else None for d in range(3)]
         s.upload(vc, fl)
         s.tangent_upload(dvc, dl)
+        if kink:
+            s.tangent_kink(True)
         for dt in dts:
             s.advance(float(dt))
+        margin = s.tangent_kink(False) if kink else None
         state = s.download()
         tangent = s.tangent_download()
     finally:
         s.close()
-    return state, tangent
+    return (state, tangent, margin) if kink else (state, tangent)
 
 
 def cfl_dt_sequence(spec: dict, vc, faces, nsteps: int, first_dt: float, cfl: float,

@@ -830,6 +830,34 @@ extern "C" int pg_tangent_download(pg_solver* h, double* const vars[8], double* 
   return tl_xfer(&h->S, vars, faces, layout, false, 1);
 }
 
+extern "C" int pg_tangent_kink(pg_solver* h, int enable, double* margin) {
+  if (!h) {
+    set_last_error("null argument");
+    return PG_ERR_INVALID;
+  }
+  Solver* S = &h->S;
+  if (S->cfg.precision != PG_FP64_TANGENT) {
+    set_last_error("pg_tangent_kink: needs a PG_FP64_TANGENT solver");
+    return PG_ERR_INVALID;
+  }
+  const double inf = __builtin_inf();
+  unsigned long long bits = 0;
+  memcpy(&bits, &inf, sizeof bits);
+  const int on = enable ? 1 : 0;
+  cudaError_t e = cudaStreamSynchronize(S->stream);
+  if (e == cudaSuccess && !enable && margin) {
+    e = cudaMemcpyFromSymbol(&bits, g_pg_kink_bits, sizeof bits);
+    memcpy(margin, &bits, sizeof bits);
+  }
+  if (e == cudaSuccess && enable) e = cudaMemcpyToSymbol(g_pg_kink_bits, &bits, sizeof bits);
+  if (e == cudaSuccess) e = cudaMemcpyToSymbol(g_pg_kink_on, &on, sizeof on);
+  if (e != cudaSuccess) {
+    set_last_error(cudaGetErrorString(e));
+    return PG_ERR_CUDA;
+  }
+  return PG_OK;
+}
+
 extern "C" int pg_adjoint_set(pg_solver* h, const double* const vars[8], const double* const faces[3], int layout) {
   int rc = check_fp64(h, "pg_adjoint_set", false);
   if (rc) return rc;

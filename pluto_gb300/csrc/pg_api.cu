@@ -367,6 +367,9 @@ extern "C" int pg_upload(pg_solver* h, const double* const vars[8], const double
   Solver* S = &h->S;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
   if (ct && !faces) return fail(PG_ERR_INVALID, "constrained transport needs staggered fields");
+  // a new state: the sticky error flags of earlier steps (NaN, timeout) no
+  // longer apply
+  CK(cudaMemsetAsync(&S->sc->status, 0, sizeof(int), S->stream));
   if (S->cfg.precision == PG_FP64_TANGENT) return tl_xfer(S, (double* const*)vars, (double* const*)faces, layout, true, 0);
   if (S->cfg.precision != PG_FP64) return mixed_upload_host(S, vars, faces, layout);
   for (int nv = 0; nv < 8; nv++) {

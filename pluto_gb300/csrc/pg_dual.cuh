@@ -94,17 +94,43 @@ template <int N> __host__ __device__ __forceinline__ Dual<N>& operator-=(Dual<N>
 template <int N> __host__ __device__ __forceinline__ Dual<N>& operator*=(Dual<N>& a, const Dual<N>& b) { return a = a * b; }
 template <int N> __host__ __device__ __forceinline__ Dual<N>& operator/=(Dual<N>& a, const Dual<N>& b) { return a = a / b; }
 
+// Distance to the nearest branch switch along the tangent direction.  With
+// recording on (pg_tangent_kink), every comparison of a Dual<1> (limiter
+// signs, MIN/MAX, Riemann-fan regions, floors, |x|) notes |a - b| / |a' - b'|,
+// the perturbation size at which, to first order, its outcome would flip;
+// the minimum over a run bounds the step h of central differences that cross
+// no kink.  Each translation unit has its own copy of these two variables.
+static __device__ int g_pg_kink_on;
+static __device__ unsigned long long g_pg_kink_bits;  // non-negative double bits: ordered as integers
+
+template <int N>
+__host__ __device__ __forceinline__ void kink_note(double dv, double dd) {
+#ifdef __CUDA_ARCH__
+  if (N != 1 || !g_pg_kink_on) return;
+  const double ad = ::fabs(dd);
+  if (!(ad > 0.0)) return;
+  const unsigned long long b = (unsigned long long)__double_as_longlong(::fabs(dv) / ad);
+  if (b < *(volatile unsigned long long*)&g_pg_kink_bits) atomicMin(&g_pg_kink_bits, b);
+#else
+  (void)dv;
+  (void)dd;
+#endif
+}
+
 #define PG_DUAL_CMP(OP)                                                                         \
   template <int N>                                                                              \
   __host__ __device__ __forceinline__ bool operator OP(const Dual<N>& a, const Dual<N>& b) {    \
+    kink_note<N>(a.v - b.v, a.d[0] - b.d[0]);                                                   \
     return a.v OP b.v;                                                                          \
   }                                                                                             \
   template <int N>                                                                              \
   __host__ __device__ __forceinline__ bool operator OP(const Dual<N>& a, double b) {            \
+    kink_note<N>(a.v - b, a.d[0]);                                                              \
     return a.v OP b;                                                                            \
   }                                                                                             \
   template <int N>                                                                              \
   __host__ __device__ __forceinline__ bool operator OP(double a, const Dual<N>& b) {            \
+    kink_note<N>(a - b.v, -b.d[0]);                                                             \
     return a OP b.v;                                                                            \
   }
 PG_DUAL_CMP(<)
@@ -117,6 +143,7 @@ PG_DUAL_CMP(!=)
 
 template <int N>
 __host__ __device__ __forceinline__ Dual<N> fabs(const Dual<N>& a) {
+  kink_note<N>(a.v, a.d[0]);
   return a.v < 0.0 ? -a : a;  // derivative of the branch taken (sign(+0) = +)
 }
 

@@ -20,6 +20,7 @@
 // Stage outputs are written to a second state buffer (the stage input is
 // still read by neighbours), so RK2/RK3 need two FP32 copies of the state.
 #include <cstdio>
+#include <cstdlib>
 #include <cstring>
 
 #include "pg_internal.h"
@@ -72,6 +73,9 @@ struct MixArgs {
   float third_hi, third_lo;        // 1/3 as a double-word pair
   int limiter, recon, ct, nbfield, accmask, device_dt, ncomp;
   int intb;  // INTERNAL_BOUNDARY: flagged zones are not updated
+  // try limit of a TMA sweep's wait for its tile (the waits that drain copies
+  // in flight after a timeout keep the default limit)
+  int tile_tries;
 };
 
 // ---------------------------------------------------------------------------
@@ -335,7 +339,7 @@ __global__ void __launch_bounds__(32 * kXR, 2)
       fence_proxy_async_smem();
       issue(tn, b ^ 1);
     }
-    const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1));
+    const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1), a.tile_tries);
     if (__syncthreads_or(!ok)) {
       if (leader) {
         atomicOr(&a.sc->status, 8);
@@ -575,7 +579,7 @@ __global__ void __launch_bounds__(32 * kTY, 2)
       fence_proxy_async_smem();  // buffer b^1 was read by the block in the previous iteration
       issue(tn, b ^ 1);
     }
-    const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1));
+    const bool ok = mbar_wait_bounded(&bar[b], (uint32_t)((it >> 1) & 1), a.tile_tries);
     if (__syncthreads_or(!ok)) {
       // a load did not complete in time: report, let the copies in flight
       // land (bounded), leave
@@ -1037,6 +1041,7 @@ __global__ void k_m1d_dt(MixArgs a, Box dom) {
 struct MixedState {
   MixBufs b;
   int cur = 0;  // buffer holding the state at the start of the next step
+  int tile_tries = 1 << 20;  // see MixArgs::tile_tries
   // TMA tensor maps of the y/z sweeps (tma: maps encoded, kernels configured)
   bool tma = false;
   SweepMaps ymaps[2], zmaps[2];  // per state buffer (V, face field); dU, CDT shared
@@ -1247,6 +1252,7 @@ static MixArgs margs(Solver* S, int in_buf, int out_buf, int v0_buf) {
     for (int d = 0; d < S->g.dims; d++) a.accmask &= ~(1 << (BX1 + d));
   a.device_dt = S->device_dt;
   a.intb = S->ud_internal ? 1 : 0;
+  a.tile_tries = M->tile_tries;
   return a;
 }
 
@@ -1449,6 +1455,15 @@ static void menqueue(Solver* S) {
 
 int mixed_enqueue_step(Solver* S) {
   const bool dwacc = S->cfg.precision == PG_MIXED_DW;
+  // PLUTO_GB300_TILE_WAIT_TRIES: the try limit of the sweeps' tile waits, read
+  // whenever a step is enqueued (a captured graph keeps the value it was
+  // captured with).  A fault-injection knob for tests: with 0 every tile wait
+  // times out at once, the step reports PG_ERR_TIMEOUT and its results are
+  // invalid; unset, the limit is 2^20 tries.
+  MixedState* M = (MixedState*)S->mixed;
+  const char* tries = getenv("PLUTO_GB300_TILE_WAIT_TRIES");
+  M->tile_tries = (tries && tries[0]) ? atoi(tries) : (1 << 20);
+  if (M->tile_tries < 0) M->tile_tries = 0;
   if (S->cfg.time_stepping == PG_RK3) {
     if (dwacc) menqueue<3, dw>(S);
     else menqueue<3, double>(S);

@@ -292,6 +292,14 @@ class Solver:
     def tangent_download(self):
         return self._get("pg_tangent_download")
 
+    def tangent_kink(self, enable: bool):
+        """Start (True) or stop (False) recording the kink margin of the
+        tangent-linear steps; stopping returns the smallest perturbation along
+        the tangent direction at which, to first order, a branch switches."""
+        m = C.c_double(0.0)
+        L.check(L.lib().pg_tangent_kink(self.h, 1 if enable else 0, C.byref(m)), "pg_tangent_kink")
+        return m.value
+
     def adjoint_set(self, lvc: np.ndarray, lbs=(None, None, None)):
         """Adjoint (gradient) on the state after the step to be reversed."""
         self._put("pg_adjoint_set", lvc, lbs)

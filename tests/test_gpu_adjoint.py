@@ -123,7 +123,7 @@ def _smooth_generic_2d(vc, f, rng, sigma, dx, dy, kmax=3):
         return out / kmax
 
     xc, yc = (np.arange(nx) + 0.5) / nx, (np.arange(ny) + 0.5) / ny
-    for q in (0, 1, 2, 3, 7):
+    for q in (0, 1, 2, 3, 6, 7):  # every cell variable that has no face (Bz too)
         v[q, 0] = v[q, 0] + sigma * field(xc, yc)
     az = sigma * min(dx, dy) * nx / (2 * np.pi) * field((np.arange(nx) + 1.0) / nx, (np.arange(ny) + 1.0) / ny)
     bx = f[0].copy()

@@ -209,3 +209,32 @@ def test_padded_rows_match_unpadded(case, prec, monkeypatch):
             if other[1][d] is not None:
                 errs[f"b{d}"] = rel_l1(out["1"][1][d], other[1][d])
         assert max(errs.values()) <= bar, errs
+
+
+@pytest.mark.parametrize("prec", MIXED)
+def test_tile_wait_timeout_is_reported_and_recoverable(prec, monkeypatch):
+    """A TMA tile wait that runs out (forced: a try limit of 0 through
+    PLUTO_GB300_TILE_WAIT_TRIES; the waits that drain copies in flight keep
+    their normal limit) makes the sweep kernels return, pg_advance report
+    PG_ERR_TIMEOUT, and leaves the solver usable: after a new upload the next
+    step equals a fresh solver's step bit for bit."""
+    from pluto_gb300 import Solver, problems
+    from pluto_gb300._lib import PG_ERR_TIMEOUT, PgError
+    spec, vc, f = problems.blast3d(32)
+    dt = spec["first_dt"]
+    s = _s(spec, prec)
+    s.upload(vc, f)
+    monkeypatch.setenv("PLUTO_GB300_TILE_WAIT_TRIES", "0")
+    with pytest.raises(PgError) as err:
+        s.advance(dt)
+    assert err.value.code == PG_ERR_TIMEOUT
+    monkeypatch.delenv("PLUTO_GB300_TILE_WAIT_TRIES")
+    s.upload(vc, f)
+    got = s.advance(dt), s.download()
+    ref = _s(spec, prec)
+    ref.upload(vc, f)
+    want = ref.advance(dt), ref.download()
+    assert got[0] == want[0]
+    assert np.array_equal(got[1][0], want[1][0])
+    for d in range(3):
+        assert np.array_equal(got[1][1][d], want[1][1][d])
