@@ -63,8 +63,14 @@ enum { PG_PERIODIC = 0, PG_OUTFLOW = 1, PG_REFLECTIVE = 2,
    face update / dt reduction; PG_MIXED_DW the same with the FP64 parts done
    as FP32 double-word pairs (48-bit significand) on the FP32 pipes.
    PG_FP64_TANGENT: the FP64 step together with its tangent-linear model
-   (each value carries one directional derivative; see pg_tangent_upload). */
-enum { PG_FP64 = 0, PG_MIXED = 1, PG_MIXED_DW = 2, PG_FP64_TANGENT = 3 };
+   (each value carries one directional derivative; see pg_tangent_upload).
+   PG_FP64_DD: the FP64 step in double-double arithmetic (about 106 bits;
+   no reference counterpart), for high-precision reference evaluations such
+   as central differences that check the adjoint: pg_upload / pg_download
+   move the high parts (the upload zeroes the low parts), pg_tangent_upload /
+   pg_tangent_download the low parts.  EULER/RK2/RK3, no user-defined sides,
+   no CHAR_LIMITING; no output files or batches. */
+enum { PG_FP64 = 0, PG_MIXED = 1, PG_MIXED_DW = 2, PG_FP64_TANGENT = 3, PG_FP64_DD = 4 };
 enum { PG_LAYOUT_INTERIOR = 0, PG_LAYOUT_PLUTO = 1 };             /* host array layout */
 
 typedef struct {

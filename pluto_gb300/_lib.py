@@ -21,7 +21,7 @@ PG_DIVB_NONE, PG_CONSTRAINED_TRANSPORT = 0, 1
 PG_ARITHMETIC, PG_UCT0, PG_UCT_CONTACT, PG_UCT_HLL = 1, 2, 3, 4
 PG_PERIODIC, PG_OUTFLOW, PG_REFLECTIVE, PG_EQTSYMMETRIC, PG_USERDEF = 0, 1, 2, 3, 4
 PG_EULER = 1
-PG_FP64, PG_MIXED, PG_MIXED_DW, PG_FP64_TANGENT = 0, 1, 2, 3
+PG_FP64, PG_MIXED, PG_MIXED_DW, PG_FP64_TANGENT, PG_FP64_DD = 0, 1, 2, 3, 4
 PG_LAYOUT_INTERIOR, PG_LAYOUT_PLUTO = 0, 1
 
 PG_ERR_INVALID, PG_ERR_CUDA, PG_ERR_NOMEM, PG_ERR_NAN = 1, 2, 3, 4

@@ -132,6 +132,37 @@ def tangent_linear(spec: dict, dts, vc, faces, dvc, dfaces, kink: bool = False):
     return (state, tangent, margin) if kink else (state, tangent)
 
 
+def _two_sum(a, b):
+    """a + b as an unevaluated pair (sum, error), exactly (Knuth's TwoSum)."""
+    t = a + b
+    bb = t - a
+    return t, (a - (t - bb)) + (b - bb)
+
+
+def dd_perturbed_run(spec: dict, dts, vc, faces, dvc, dfaces, h: float):
+    """The step in double-double arithmetic (precision "fp64_dd") over the
+    frozen dt sequence from x + h*delta, the start formed exactly as a pair
+    of doubles; returns the final cell state as (high parts, low parts).  For
+    central differences with h far below FP64 resolution."""
+    hv, lv = _two_sum(np.asarray(vc, dtype=np.float64), h * np.asarray(dvc, dtype=np.float64))
+    hf, lf = [None] * 3, [None] * 3
+    for d in range(3):
+        if faces[d] is not None:
+            hf[d], lf[d] = _two_sum(faces[d], h * dfaces[d])
+    s = Solver(spec, "fp64_dd")
+    try:
+        fl = [hf[d] if (s.ct and d < s.dims) else None for d in range(3)]
+        dl = [lf[d] if (s.ct and d < s.dims) else None for d in range(3)]
+        s.upload(hv, fl)
+        s.tangent_upload(lv, dl)
+        for dt in dts:
+            s.advance(float(dt))
+        (h1, _), (l1, _) = s.download(), s.tangent_download()
+    finally:
+        s.close()
+    return h1, l1
+
+
 def cfl_dt_sequence(spec: dict, vc, faces, nsteps: int, first_dt: float, cfl: float,
                     cfl_max_var: float = 1.1):
     """The dt sequence PLUTO's main loop takes from this state (NextTimeStep,

@@ -29,6 +29,7 @@ UNITS = {
     "pg_batch.cu": ["--fmad=false"],
     "pg_batch_mixed.cu": ["--use_fast_math"],
     "pg_adjoint.cu": ["--fmad=false"],
+    "pg_dd.cu": ["--fmad=false"],
     "pg_output.cu": [],
 }
 

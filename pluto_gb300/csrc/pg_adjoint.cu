@@ -811,8 +811,8 @@ extern "C" int pg_tangent_upload(pg_solver* h, const double* const vars[8], cons
     set_last_error("null argument");
     return PG_ERR_INVALID;
   }
-  if (h->S.cfg.precision != PG_FP64_TANGENT) {
-    set_last_error("pg_tangent_upload: needs a PG_FP64_TANGENT solver");
+  if (h->S.cfg.precision != PG_FP64_TANGENT && h->S.cfg.precision != PG_FP64_DD) {
+    set_last_error("pg_tangent_upload: needs a PG_FP64_TANGENT or PG_FP64_DD solver");
     return PG_ERR_INVALID;
   }
   return tl_xfer(&h->S, (double* const*)vars, (double* const*)faces, layout, true, 1);
@@ -823,8 +823,8 @@ extern "C" int pg_tangent_download(pg_solver* h, double* const vars[8], double* 
     set_last_error("null argument");
     return PG_ERR_INVALID;
   }
-  if (h->S.cfg.precision != PG_FP64_TANGENT) {
-    set_last_error("pg_tangent_download: needs a PG_FP64_TANGENT solver");
+  if (h->S.cfg.precision != PG_FP64_TANGENT && h->S.cfg.precision != PG_FP64_DD) {
+    set_last_error("pg_tangent_download: needs a PG_FP64_TANGENT or PG_FP64_DD solver");
     return PG_ERR_INVALID;
   }
   return tl_xfer(&h->S, vars, faces, layout, false, 1);

@@ -92,8 +92,15 @@ int validate_config(const pg_config* c) {
     return fail(PG_ERR_INVALID, "unsupported divergence control");
   }
   if (c->precision != PG_FP64 && c->precision != PG_MIXED && c->precision != PG_MIXED_DW &&
-      c->precision != PG_FP64_TANGENT)
+      c->precision != PG_FP64_TANGENT && c->precision != PG_FP64_DD)
     return fail(PG_ERR_INVALID, "unsupported precision");
+  if (c->precision == PG_FP64_DD) {
+    if (is_ctu(c->time_stepping)) return fail(PG_ERR_INVALID, "PG_FP64_DD takes EULER, RK2 or RK3 time stepping");
+    if (c->char_limiting) return fail(PG_ERR_INVALID, "PG_FP64_DD has no CHAR_LIMITING");
+    for (int d = 0; d < c->dims; d++)
+      if (c->bc[d] == PG_USERDEF || (c->bc_sides && c->bc_hi[d] == PG_USERDEF))
+        return fail(PG_ERR_INVALID, "PG_FP64_DD has no user-defined boundaries");
+  }
   if (c->char_limiting != 0 && c->char_limiting != 1) return fail(PG_ERR_INVALID, "char_limiting is 0 or 1");
   if (c->char_limiting) {
     if (c->precision != PG_FP64)
@@ -186,8 +193,9 @@ extern "C" int pg_create(const pg_config* cfg, pg_solver** out) {
   }
   cudaMemset(S->sc, 0, sizeof(DevScalars));
   memset(S->sc_host, 0, sizeof(DevScalars));
-  const bool f64 = cfg->precision == PG_FP64 || cfg->precision == PG_FP64_TANGENT;
-  if (cfg->precision == PG_FP64_TANGENT) S->elem_bytes = 2 * sizeof(double);  // value + tangent
+  const bool f64 = cfg->precision == PG_FP64 || cfg->precision == PG_FP64_TANGENT || cfg->precision == PG_FP64_DD;
+  if (cfg->precision == PG_FP64_TANGENT || cfg->precision == PG_FP64_DD)
+    S->elem_bytes = 2 * sizeof(double);  // value + tangent, or high + low part
   rc = f64 ? fp64_alloc(S) : mixed_alloc(S);
   if (rc) {
     free_all(S);
@@ -248,7 +256,7 @@ extern "C" int pg_set_internal_boundary(pg_solver* h, unsigned char* flags) {
   if (!h || !flags) return fail(PG_ERR_INVALID, "pg_set_internal_boundary: null argument");
   Solver* S = &h->S;
   if (!S->ud_fn) return fail(PG_ERR_INVALID, "pg_set_internal_boundary: call pg_set_userdef first");
-  if (S->cfg.precision == PG_FP64_TANGENT || is_ctu(S->cfg.time_stepping))
+  if (S->cfg.precision == PG_FP64_TANGENT || S->cfg.precision == PG_FP64_DD || is_ctu(S->cfg.time_stepping))
     return fail(PG_ERR_INVALID, "pg_set_internal_boundary: EULER/RK2/RK3 time stepping, FP64 or mixed");
   CK(cudaStreamSynchronize(S->stream));
   if (S->ud_pinned_flag) {
@@ -371,6 +379,12 @@ extern "C" int pg_upload(pg_solver* h, const double* const vars[8], const double
   // longer apply
   CK(cudaMemsetAsync(&S->sc->status, 0, sizeof(int), S->stream));
   if (S->cfg.precision == PG_FP64_TANGENT) return tl_xfer(S, (double* const*)vars, (double* const*)faces, layout, true, 0);
+  if (S->cfg.precision == PG_FP64_DD) {  // high parts; the low parts start at zero
+    for (int nv = 0; nv < 8; nv++) CK(cudaMemsetAsync(S->V[nv], 0, S->g.ncell * S->elem_bytes, S->stream));
+    if (ct)
+      for (int d = 0; d < S->g.dims; d++) CK(cudaMemsetAsync(S->Bs[d], 0, S->g.ncell * S->elem_bytes, S->stream));
+    return tl_xfer(S, (double* const*)vars, (double* const*)faces, layout, true, 0);
+  }
   if (S->cfg.precision != PG_FP64) return mixed_upload_host(S, vars, faces, layout);
   for (int nv = 0; nv < 8; nv++) {
     if (vars[nv]) {
@@ -395,7 +409,8 @@ extern "C" int pg_download(pg_solver* h, double* const vars[8], double* const fa
   if (layout != PG_LAYOUT_INTERIOR && layout != PG_LAYOUT_PLUTO) return fail(PG_ERR_INVALID, "bad layout");
   Solver* S = &h->S;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
-  if (S->cfg.precision == PG_FP64_TANGENT) return tl_xfer(S, vars, faces, layout, false, 0);
+  if (S->cfg.precision == PG_FP64_TANGENT || S->cfg.precision == PG_FP64_DD)
+    return tl_xfer(S, vars, faces, layout, false, 0);
   if (S->cfg.precision != PG_FP64) return mixed_download(S, vars, faces, layout);
   for (int nv = 0; nv < 8; nv++)
     if (vars[nv]) {
@@ -422,6 +437,7 @@ static int enqueue_step(Solver* S) {
   S->ud_stage = 0;
   if (S->cfg.precision == PG_FP64) return fp64_enqueue_step(S);
   if (S->cfg.precision == PG_FP64_TANGENT) return tl_enqueue_step(S);
+  if (S->cfg.precision == PG_FP64_DD) return dd_enqueue_step(S);
   return mixed_enqueue_step(S);
 }
 

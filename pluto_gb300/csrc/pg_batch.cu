@@ -185,6 +185,8 @@ extern "C" int pg_batch_create(const pg_config* cfg, int ntubes, const int* nx, 
   int rc = validate_config(&c);
   if (rc) return rc;
   if (c.dims != 1 || c.divb != PG_DIVB_NONE) return bfail(PG_ERR_INVALID, "pg_batch_create: 1D problems without CT");
+  if (c.precision != PG_FP64 && c.precision != PG_MIXED && c.precision != PG_MIXED_DW)
+    return bfail(PG_ERR_INVALID, "pg_batch_create: PG_FP64, PG_MIXED or PG_MIXED_DW");
   if (c.time_stepping != PG_RK2 && c.time_stepping != PG_RK3)
     return bfail(PG_ERR_INVALID, "pg_batch_create: batches take RK2 or RK3 time stepping");
   if (c.bc[0] == PG_USERDEF || (c.bc_sides && c.bc_hi[0] == PG_USERDEF))

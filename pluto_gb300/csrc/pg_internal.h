@@ -123,6 +123,7 @@ void fp64_free(Solver* S);
 int fp64_enqueue_step(Solver* S);  // all stages of one step on S->stream
 
 int tl_enqueue_step(Solver* S);  // PG_FP64_TANGENT: state and tangent
+int dd_enqueue_step(Solver* S);  // PG_FP64_DD: the step in double-double
 int tl_xfer(Solver* S, double* const vars[8], double* const faces[3], int layout, bool to_dev, int part);
 void adjoint_free(Solver* S);      // adjoint buffers, checkpoints, staging
 

@@ -465,7 +465,7 @@ extern "C" int pg_write_output(pg_solver* h, const pg_output* o) {
     return PG_ERR_INVALID;
   }
   Solver* S = &h->S;
-  if (S->cfg.precision == PG_FP64_TANGENT) {
+  if (S->cfg.precision == PG_FP64_TANGENT || S->cfg.precision == PG_FP64_DD) {
     set_last_error("pg_write_output: FP64 and mixed precisions only");
     return PG_ERR_INVALID;
   }
@@ -626,7 +626,7 @@ extern "C" int pg_download_async(pg_solver* h, double* const vars[8], double* co
     return PG_ERR_INVALID;
   }
   Solver* S = &h->S;
-  if (S->cfg.precision == PG_FP64_TANGENT) {
+  if (S->cfg.precision == PG_FP64_TANGENT || S->cfg.precision == PG_FP64_DD) {
     set_last_error("pg_download_async: FP64 and mixed precisions only");
     return PG_ERR_INVALID;
   }

@@ -32,11 +32,12 @@ __device__ __forceinline__ void ud_to_dev(double v, float* d) { *d = narrow(v); 
 __device__ __forceinline__ void ud_to_dev(double v, double* d) { *d = v; }
 __device__ __forceinline__ double ud_to_host(float v) { return widen(v); }
 __device__ __forceinline__ double ud_to_host(double v) { return v; }
-// dual numbers (tangent-linear solvers reject USERDEF sides; instantiated only)
+// dual and double-double numbers (their solvers reject USERDEF sides and
+// internal boundaries; instantiated only)
 template <class D>
 __device__ __forceinline__ void ud_to_dev(double v, D* d) { *d = D(v); }
 template <class D>
-__device__ __forceinline__ double ud_to_host(const D& v) { return v.v; }
+__device__ __forceinline__ double ud_to_host(const D& v) { return value_of(v); }
 
 // host: PLUTO-layout array (cells: nt0 x nt1 x nt2; face fd: one more along
 // fd with the -1 layer first); dev: the device cell/face array; bm1: the

@@ -31,7 +31,7 @@ EMF = {"ARITHMETIC": L.PG_ARITHMETIC, "UCT0": L.PG_UCT0, "UCT_CONTACT": L.PG_UCT
 BC = {"periodic": L.PG_PERIODIC, "outflow": L.PG_OUTFLOW, "reflective": L.PG_REFLECTIVE,
       "eqtsymmetric": L.PG_EQTSYMMETRIC, "userdef": L.PG_USERDEF}
 PRECISION = {"fp64": L.PG_FP64, "mixed": L.PG_MIXED, "mixed_dw": L.PG_MIXED_DW,
-             "fp64_tangent": L.PG_FP64_TANGENT}
+             "fp64_tangent": L.PG_FP64_TANGENT, "fp64_dd": L.PG_FP64_DD}
 NVAR = 8
 
 

@@ -7,13 +7,16 @@ Checks, all with a frozen dt sequence:
 - TL against central finite differences of the state;
 - the CP-Alfven objective (128^2, 256 steps, checkpoint every 16): the
   autograd gradient against the tangent-linear derivative (exact transpose)
-  and against central differences along 16 random unit directions (limited
-  by the kinks of the limiters and Riemann branches crossed inside [-h, h]).
+  and against central differences taken with the double-double step inside
+  the kink margin (the distance to the nearest branch switch), <= 1e-6;
+- at the CP-Alfven initial condition itself the kink margin is 0.
 """
 import math
 
 import numpy as np
 import pytest
+
+from conftest import load_golden, rel_l1
 
 pytestmark = pytest.mark.gpu
 
@@ -220,32 +223,41 @@ def test_tangent_matches_central_differences(name, emf):
     assert min(errs.values()) < 1e-6, errs
 
 
-def test_cp_alfven_gradient_against_tangent_and_finite_differences():
-    """Headline differentiation check on the 128^2 circularly polarised
-    Alfven wave (30 degrees), PLM/MC, HLLD, RK2, CT, 256 FP64 steps.  The
-    gradient is taken at a smooth generic point next to the initial condition
-    (see _smooth_generic_2d); the target is the forward result of the initial condition
-    with seeded Gaussian noise (sigma 1e-3) on density, velocity, pressure."""
-    import torch
+def _dd_central_difference(spec, dts, vc, f, dvc, df, h, tgt_vc):
+    """(J(x + h delta) - J(x - h delta)) / 2h of the CP-Alfven objective
+    J = 1/2 |rho - rho*|^2 + 1/2 |B - B*|^2, the two runs in double-double and
+    the difference of the objectives formed from the difference of the states
+    (J+ - J- = 1/2 sum (v+ - v-)(v+ + v- - 2 v*)), so that nothing cancels in
+    double precision."""
+    from pluto_gb300.adjoint import dd_perturbed_run
+    hp, lp = dd_perturbed_run(spec, dts, vc, f, dvc, df, h)
+    hm, lm = dd_perturbed_run(spec, dts, vc, f, dvc, df, -h)
+    diff = 0.0
+    for q in (0, 4, 5, 6):
+        dv = (hp[q] - hm[q]) + (lp[q] - lm[q])
+        diff += 0.5 * float((dv * (hp[q] + hm[q] - 2.0 * tgt_vc[q])).sum())
+    return diff / (2.0 * h)
+
+
+def _cp_alfven_setup(nsteps):
     from pluto_gb300 import problems as P
-    from pluto_gb300.adjoint import Rollout, cfl_dt_sequence, rollout, tangent_linear
+    from pluto_gb300.adjoint import Rollout, cfl_dt_sequence
     spec, vc, f = P.cp_alfven(128)
     f = _faces(spec, f)
-    nsteps = 256
     dts = cfl_dt_sequence(spec, vc, f, nsteps, spec["first_dt"], spec["cfl"])
     # target: the forward result from a seeded Gaussian perturbation (sigma 1e-3)
     rng = np.random.default_rng(2024)
     vt = vc.copy()
     for q in (0, 1, 2, 3, 7):
         vt[q] = vt[q] + 1e-3 * rng.normal(size=vt[q].shape)
+    tgt_vc, _ = Rollout(spec, dts, every=16).run(vt, f)
+    return spec, vc, f, dts, tgt_vc
+
+
+def _autograd_gradient(spec, dts, vc, f, tgt_vc):
+    import torch
+    from pluto_gb300.adjoint import Rollout, rollout
     r = Rollout(spec, dts, every=16)
-    tgt_vc, _ = r.run(vt, f)
-    vc, f = _smooth_generic_2d(vc, f, np.random.default_rng(99), 2e-2, spec["dx"][0], spec["dx"][1])
-
-    def objective(v_T):
-        return 0.5 * float(((v_T[0] - tgt_vc[0]) ** 2).sum() + ((v_T[4:7] - tgt_vc[4:7]) ** 2).sum())
-
-    # gradient through torch.autograd
     tv = torch.from_numpy(vc.copy()).requires_grad_(True)
     tfx = torch.from_numpy(f[0].copy()).requires_grad_(True)
     tfy = torch.from_numpy(f[1].copy()).requires_grad_(True)
@@ -253,40 +265,105 @@ def test_cp_alfven_gradient_against_tangent_and_finite_differences():
     tgt = torch.from_numpy(tgt_vc)
     J = 0.5 * (((out[0][0] - tgt[0]) ** 2).sum() + ((out[0][4:7] - tgt[4:7]) ** 2).sum())
     J.backward()
-    g_vc, g_f = tv.grad.numpy(), [tfx.grad.numpy(), tfy.grad.numpy(), None]
-    assert abs(float(J.detach()) - objective(r.run(vc, f)[0])) <= 1e-12 * float(J.detach())
+    return r, float(J.detach()), out[0].detach().numpy(), tv.grad.numpy(), [tfx.grad.numpy(), tfy.grad.numpy(), None]
+
+
+def test_cp_alfven_gradient_against_tangent_and_finite_differences():
+    """Headline differentiation check on the 128^2 circularly polarised
+    Alfven wave (30 degrees), PLM/MC, HLLD, RK2, CT, 256 FP64 steps with a
+    checkpoint every 16.  The gradient (torch.autograd over the hand-written
+    adjoint) is taken at a smooth generic point next to the initial condition
+    (_smooth_generic_2d); the target is the forward result of the initial
+    condition with seeded Gaussian noise (sigma 1e-3) on density, velocity,
+    pressure.
+
+    * against the FP64 tangent-linear model along 16 random directions: the
+      adjoint is its exact transpose (<= 1e-9);
+    * against central differences, <= 1e-6: the map is only piecewise smooth
+      -- the kink margin of the tangent-linear run shows a branch switch
+      (limiter, Riemann fan, MIN/MAX) within about 1e-10 of the point along
+      every direction, so FP64 differences (which need h >~ 1e-7 to beat
+      round-off) cross thousands of kinks.  The differences are therefore
+      taken with the double-double step (PG_FP64_DD) at h = 1e-12, at least
+      ten times inside the kink margin, where round-off is negligible."""
+    from pluto_gb300.adjoint import tangent_linear
+    spec, vc0, f0, dts, tgt_vc = _cp_alfven_setup(256)
+    vc, f = _smooth_generic_2d(vc0, f0, np.random.default_rng(99), 2e-2, spec["dx"][0], spec["dx"][1])
+    r, J, out_vc, g_vc, g_f = _autograd_gradient(spec, dts, vc, f, tgt_vc)
+
+    def objective(v_T):
+        return 0.5 * float(((v_T[0] - tgt_vc[0]) ** 2).sum() + ((v_T[4:7] - tgt_vc[4:7]) ** 2).sum())
+
+    assert abs(J - objective(r.run(vc, f)[0])) <= 1e-12 * J
     lam_vc = np.zeros_like(vc)
-    out_vc = out[0].detach().numpy()
     lam_vc[0] = out_vc[0] - tgt_vc[0]
     lam_vc[4:7] = out_vc[4:7] - tgt_vc[4:7]
 
-    worst_tl, fd_best = 0.0, []
+    h = 1e-12
+    worst_tl, worst_fd = 0.0, 0.0
     drng = np.random.default_rng(7)
-    for _ in range(16):
+    for n in range(16):
         dvc, df = _random_like(drng, vc, f)
         norm = math.sqrt(_inner(dvc, df, dvc, df))
         dvc = dvc / norm
         df = [x / norm if x is not None else None for x in df]
         adj = _inner(g_vc, g_f, dvc, df)
-        _, (tvc, _) = tangent_linear(spec, dts, vc, f, dvc, df)
+        _, (tvc, _), margin = tangent_linear(spec, dts, vc, f, dvc, df, kink=True)
         tl = float(np.dot(lam_vc.ravel(), tvc.ravel()))
         worst_tl = max(worst_tl, abs(adj - tl) / abs(tl))
-        errs = []
-        for h in (1e-5, 1e-6, 1e-7, 1e-8):
-            jp = objective(r.run(vc + h * dvc, [f[0] + h * df[0], f[1] + h * df[1], None])[0])
-            jm = objective(r.run(vc - h * dvc, [f[0] - h * df[0], f[1] - h * df[1], None])[0])
-            errs.append(abs((jp - jm) / (2 * h) - adj) / abs(adj))
-        print(f"direction: adjoint {adj:.6e}  TL {tl:.6e}  rel FD error for h=1e-5..1e-8: "
-              + ", ".join(f"{e:.2e}" for e in errs))
-        fd_best.append(min(errs))
-    fd_best.sort()
+        line = f"direction {n:2d}: adjoint {adj:.9e}  TL {tl:.9e}  kink margin {margin:.2e}"
+        if n < 8:  # double-double central differences (2 x 256 steps each)
+            assert margin >= 10 * h, margin
+            fd = _dd_central_difference(spec, dts, vc, f, dvc, df, h, tgt_vc)
+            worst_fd = max(worst_fd, abs(fd - adj) / abs(adj))
+            line += f"  DD central difference {fd:.9e}"
+        print(line)
     print(f"cp_alfven 128^2 x 256: max rel |adjoint - TL| = {worst_tl:.3e}, "
-          f"rel |adjoint - central FD| (best h per direction): median {fd_best[8]:.3e}, max {fd_best[-1]:.3e}")
-    # The adjoint is the exact transpose of the tangent-linear model.
+          f"max rel |adjoint - DD central difference (h=1e-12)| = {worst_fd:.3e}")
     assert worst_tl <= 1e-9
-    # Central differences of this piecewise-smooth map: error from limiter
-    # and Riemann-branch kinks crossed inside [-h, h] (proportional to h)
-    # plus round-off (proportional to 1/h); no h gets it under ~1e-6 for
-    # all 16 directions at 256 steps.
-    assert fd_best[8] <= 2e-5
-    assert fd_best[-1] <= 2e-4
+    assert worst_fd <= 1e-6
+
+
+@pytest.mark.parametrize("nsteps", [16, 64])
+def test_cp_alfven_initial_condition_sits_on_kinks(nsteps):
+    """At the CP-Alfven initial condition itself (uniform density and
+    pressure, a wave commensurate with the grid) limiters sit exactly on their
+    kinks: the kink margin along directions that perturb only the velocity and
+    the faces is exactly 0, so central differences there return a mean of
+    one-sided derivatives, not the derivative of the branch the step takes.
+    The adjoint is still the exact transpose of the tangent-linear model."""
+    from pluto_gb300.adjoint import tangent_linear
+    spec, vc, f, dts, tgt_vc = _cp_alfven_setup(nsteps)
+    _, _, out_vc, g_vc, g_f = _autograd_gradient(spec, dts, vc, f, tgt_vc)
+    lam_vc = np.zeros_like(vc)
+    lam_vc[0] = out_vc[0] - tgt_vc[0]
+    lam_vc[4:7] = out_vc[4:7] - tgt_vc[4:7]
+    drng = np.random.default_rng(11)
+    for _ in range(2):
+        dvc, df = _random_like(drng, vc, f)
+        dvc[[0, 4, 5, 6, 7]] = 0.0
+        norm = math.sqrt(_inner(dvc, df, dvc, df))
+        dvc = dvc / norm
+        df = [x / norm if x is not None else None for x in df]
+        adj = _inner(g_vc, g_f, dvc, df)
+        _, (tvc, _), margin = tangent_linear(spec, dts, vc, f, dvc, df, kink=True)
+        tl = float(np.dot(lam_vc.ravel(), tvc.ravel()))
+        assert abs(adj - tl) <= 1e-9 * abs(tl)
+        assert margin == 0.0
+
+
+def test_double_double_step_matches_reference():
+    """The double-double FP64 step (PG_FP64_DD) against the reference's dump:
+    equal to FP64 round-off (it is more accurate than the reference, not
+    identical), with non-zero low parts."""
+    from pluto_gb300 import Solver
+    meta, vc0, bs0, vc1, bs1 = load_golden("ot_hlld_32")
+    s = Solver(meta, "fp64_dd")
+    s.upload(vc0, bs0)
+    s.run(meta["steps"], meta["first_dt"], meta["cfl"])
+    hv, hb = s.download()
+    lv, _ = s.tangent_download()
+    errs = [rel_l1(hv[q], vc1[q]) for q in range(8) if np.abs(vc1[q]).sum() > 0]
+    assert max(errs) <= 1e-13, errs
+    assert np.abs(lv).max() > 0.0
+    assert np.all(np.abs(lv) <= 1e-15 * np.abs(hv) + 1e-300)
