@@ -182,7 +182,12 @@ template <> struct Acc<double> {
     return a * r;
   }
   static __device__ __forceinline__ float tof(T a) { return narrow(a); }
-  static __device__ __forceinline__ bool neg(T a) { return a < 0.0; }
+  // a < 0 from the bits (integer compare; a DSETP would take an FP64-pipe
+  // slot): sign set, not -0, not NaN
+  static __device__ __forceinline__ bool neg(T a) {
+    const long long b = __double_as_longlong(a);
+    return b < 0 && (b & 0x7fffffffffffffffll) != 0 && (b & 0x7fffffffffffffffll) <= 0x7ff0000000000000ll;
+  }
   static __device__ __forceinline__ T konst(double hi, float, float) { return hi; }
   // (x + y) / 2 of two floats: one FMA, the same value as 0.5 * (x + y)
   // (halving commutes with rounding)

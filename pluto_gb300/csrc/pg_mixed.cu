@@ -708,11 +708,17 @@ __global__ void k_memf(MixArgs a, Box box) {
   int i, j, k;
   box.coords(q, i, j, k);
   long long c = cidx(a.g, k, j, i);
-  a.E[2][c] = muct_edge<2>(a, c);
+  // the three edges first, then the stores: with no store in between the
+  // compiler shares the loads the edges have in common (S, velocities, slopes
+  // and faces of the zone and of its +x/+y/+z neighbours)
+  const float ez = muct_edge<2>(a, c);
   if (a.g.dims == 3) {
-    a.E[0][c] = muct_edge<0>(a, c);
-    a.E[1][c] = muct_edge<1>(a, c);
+    const float ex = muct_edge<0>(a, c);
+    const float ey = muct_edge<1>(a, c);
+    a.E[0][c] = ex;
+    a.E[1][c] = ey;
   }
+  a.E[2][c] = ez;
 }
 
 // CT face update: EMF differences in FP32, accumulation into the face field
@@ -731,13 +737,13 @@ __global__ void k_mface(MixArgs a, Box box) {
   const float* E2 = a.E[1];
   const float* E3 = a.E[2];
   const float f1 = a.sc->dtdx[0], f2 = a.sc->dtdx[1], f3 = a.sc->dtdx[2];
-  for (int fd = 0; fd < g.dims; fd++) {
-    bool in = true;
-    for (int ax = 0; ax < g.dims; ax++) {
-      int x = ax == 0 ? i : (ax == 1 ? j : k);
-      int lo = g.beg[ax] - (ax == fd ? 1 : 0), hi = g.end[ax];
-      in = in && x >= lo && x <= hi;
-    }
+  // the box spans beg-1..end on every active axis; face fd needs x >= beg on
+  // the other active axes
+  const bool in0 = i >= g.beg[0], in1 = g.dims < 2 || j >= g.beg[1], in2 = g.dims < 3 || k >= g.beg[2];
+#pragma unroll
+  for (int fd = 0; fd < 3; fd++) {
+    if (fd >= g.dims) break;
+    const bool in = (fd == 0 || in0) && (fd == 1 || in1) && (fd == 2 || in2);
     if (!in) continue;
     float rhs;
     if (fd == 0) {
