@@ -611,16 +611,23 @@ def main():
     avg_ms = dom_ms / dom_cnt
     alg = kernel_bytes(dom_name, n)
     achieved = alg / (avg_ms / 1e3) / 1e9 if alg else None
-    traffic = None
-    step_bytes_zone = None
-    tfile = ROOT / "profiles" / "traffic.json"
-    if tfile.exists():
+    # per-kernel ncu figures of one RK2 step of the same scheme at 192^3
+    # (DRAM bytes and warp instructions per interior zone, the binding unit);
+    # scaled to this grid by the zone count
+    traffic = traffic_note = limiter = None
+    step_bytes_zone = step_winst_zone = None
+    pfile = ROOT / "profiles" / "mixed_step_blast192.json"
+    if pfile.exists():
         try:
-            t = json.loads(tfile.read_text())
-            step_bytes_zone = t.get("step_bytes_per_zone")
-            if t.get("kernel") == dom_name:
-                traffic = t["bytes_per_unit"] * (n + 2) * (n + 2) * n if "sweep" in dom_name else \
-                    t["bytes_per_unit"] * cells
+            pj = json.loads(pfile.read_text())
+            step_bytes_zone = pj["step"]["dram_bytes_per_zone"]
+            step_winst_zone = pj["step"]["warp_inst_per_zone"]
+            kd = pj["kernels"].get(dom_name)
+            if kd:
+                traffic = kd["dram_bytes_per_zone_per_launch"] * cells
+                traffic_note = (f"ncu dram__bytes_read+write of {dom_name} per launch at {pj['grid']}^3 "
+                                f"({kd['dram_bytes_per_zone_per_launch']:.1f} B/zone), scaled by the zone count")
+                limiter = kd["bound"]
         except Exception:
             traffic = None
     mx_info = mx.info()
@@ -780,15 +787,28 @@ def main():
         "l1_mixed_vs_fp64": l1,
         "hbm_fraction_algorithmic": value * algo_bytes_zu / (peak * 1e9),
         # the whole step against HBM: DRAM bytes per zone of every launch of one
-        # step (ncu, blast 192^3, traffic grows with the zone count) over the step time
+        # step (ncu at 192^3, scaled by the zone count) over the step time
         "step_hbm": ({"bytes_per_zone_step": step_bytes_zone,
                       "achieved_gbs": step_bytes_zone * cells / (ms / args.steps / 1e3) / 1e9,
                       "frac": step_bytes_zone * cells / (ms / args.steps / 1e3) / 1e9 / peak,
-                      "peak_gbs": peak, "source": "profiles/mixed_kernels_blast192.md"}
+                      "peak_gbs": peak, "source": "profiles/mixed_step_blast192.json (ncu at 192^3, per zone)"}
                      if step_bytes_zone else None),
+        # the whole step against the instruction-issue ceiling: warp instructions
+        # per zone-update (ncu at 192^3) over one warp instruction per cycle per
+        # scheduler (152 SMs x 4) at the sampled SM clock
+        "compute_roofline": ({"warp_inst_per_zone_update": step_winst_zone,
+                              "issue_peak_warp_inst_per_s": 152 * 4 * (clocks.get("sm_mhz") or 2070.0) * 1e6,
+                              "floor_ms_per_step": step_winst_zone * cells
+                              / (152 * 4 * (clocks.get("sm_mhz") or 2070.0) * 1e6) * 1e3,
+                              "frac": step_winst_zone * cells / (152 * 4 * (clocks.get("sm_mhz") or 2070.0) * 1e6)
+                              / (ms / args.steps / 1e3),
+                              "source": "profiles/mixed_step_blast192.json (smsp__inst_executed.sum at 192^3)"}
+                             if step_winst_zone else None),
         "roofline": {"bound": "hbm", "kernel": dom_name, "achieved": achieved, "peak": peak,
                      "unit": "GB/s", "frac": (achieved / peak) if achieved else None,
-                     "traffic": traffic, "avg_launch_ms": avg_ms, "launches": dom_cnt,
+                     "limiter": limiter, "traffic": traffic, "traffic_note": traffic_note,
+                     "step_frac_algorithmic": value * algo_bytes_zu / (peak * 1e9),
+                     "avg_launch_ms": avg_ms, "launches": dom_cnt,
                      "share_of_step": dom_ms / tot if tot else None, "peak_source": PEAK_SRC,
                      "kernels": {k: {"ms": v[0], "launches": v[1]} for k, v in prof.items()}},
         "clocks": clocks,
