@@ -181,6 +181,14 @@ template <> struct Acc<double> {
     r = fma(r, fma(-b, r, 1.0), r);
     return a * r;
   }
+  // 1/b the same way (two FP64 operations)
+  static __device__ __forceinline__ T rcp(T b) {
+    const double r = widen(__frcp_rn(narrow(b)));
+    return fma(r, fma(-b, r, 1.0), r);
+  }
+  // a*b + c with one rounding, and e - k/2 with one rounding
+  static __device__ __forceinline__ T fmadd(T a, T b, T c) { return fma(a, b, c); }
+  static __device__ __forceinline__ T sub_half(T e, T k) { return fma(k, -0.5, e); }
   static __device__ __forceinline__ float tof(T a) { return narrow(a); }
   // a < 0 from the bits (integer compare; a DSETP would take an FP64-pipe
   // slot): sign set, not -0, not NaN
@@ -226,6 +234,9 @@ template <> struct Acc<dw> {
   static __device__ __forceinline__ T mulf(T a, float b) { return a * b; }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
   static __device__ __forceinline__ T div(T a, T b) { return dw_div(a, b); }
+  static __device__ __forceinline__ T rcp(T b) { return dw_div(dw{1.f, 0.f}, b); }
+  static __device__ __forceinline__ T fmadd(T a, T b, T c) { return a * b + c; }
+  static __device__ __forceinline__ T sub_half(T e, T k) { return e - k * 0.5f; }
   static __device__ __forceinline__ float tof(T a) { return dw_to_float(a); }
   static __device__ __forceinline__ bool neg(T a) { return a.hi < 0.f || (a.hi == 0.f && a.lo < 0.f); }
   static __device__ __forceinline__ T konst(double, float hi, float lo) { return {hi, lo}; }

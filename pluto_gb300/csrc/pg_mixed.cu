@@ -893,15 +893,17 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
     for (int d = 0; d < 3; d++) vel[d] = O::tof(u.m[d]) * tau;
     T m2 = O::add(O::add(O::mul(u.m[0], u.m[0]), O::mul(u.m[1], u.m[1])), O::mul(u.m[2], u.m[2]));
     T b2 = O::add(O::add(O::mul(u.b[0], u.b[0]), O::mul(u.b[1], u.b[1])), O::mul(u.b[2], u.b[2]));
-    T kinb2 = O::mulf(O::add(O::div(m2, u.rho), b2), 0.5f);
+    // twice the kinetic + magnetic energy density, m^2/rho + B^2, with the
+    // reciprocal's last multiply fused into the sum; p = (E - kin2/2)(g-1)
+    const T kin2 = O::fmadd(m2, O::rcp(u.rho), b2);
     if (O::neg(u.E)) {
-      u.E = O::add(O::mulf(inv_gmm1, (float)a.small_p), kinb2);
+      u.E = O::add(O::mulf(inv_gmm1, (float)a.small_p), O::mulf(kin2, 0.5f));
       fl = FLAG_CONS2PRIM_FAIL;
     }
-    float p = O::tof(O::mulf(O::sub(u.E, kinb2), a.gamma - 1.0f));
+    float p = O::tof(O::mulf(O::sub_half(u.E, kin2), a.gamma - 1.0f));
     if (p < 0.f) {  // floor and recompute the energy (Src/MHD/mappers.c:190-200)
       p = (float)a.small_p;
-      u.E = O::add(O::mulf(inv_gmm1, (float)a.small_p), kinb2);
+      u.E = O::add(O::mulf(inv_gmm1, (float)a.small_p), O::mulf(kin2, 0.5f));
       fl = FLAG_CONS2PRIM_FAIL;
     }
     // the accumulators of the next stage (the last stage: of the next step)
