@@ -39,20 +39,29 @@ def _cell_b(faces, dims):
     return out
 
 
-def blast3d(n=512, p_in=10.0, p_out=0.1, r0=0.1, bmag=10.0, dtype=np.float64):
-    """3D MHD blast wave on [-0.5,0.5]^3, periodic; taper over two zones."""
+def blast3d(n=512, p_in=10.0, p_out=0.1, r0=0.1, bmag=10.0, dtype=np.float64, nz=None):
+    """3D MHD blast wave on [-0.5,0.5]^3, periodic; taper over two zones.
+
+    ``nz`` < n keeps only the central nz layers in z (an n x n x nz periodic
+    slab with the n^3 grid's spacing; the cut is mirror-symmetric about z=0,
+    so the periodic wrap joins equal states)."""
     x, dx = _centres(n, -0.5, 0.5)
-    vc = np.zeros((8, n, n, n), dtype=dtype)
+    nz = n if nz is None else nz
+    if not 1 <= nz <= n:
+        raise ValueError(f"nz={nz} outside [1, {n}]")
+    z = x[(n - nz) // 2:(n - nz) // 2 + nz]
+    vc = np.zeros((8, nz, n, n), dtype=dtype)
     vc[0] = 1.0
-    r2 = (x[None, None, :] ** 2 + x[None, :, None] ** 2 + x[:, None, None] ** 2)
+    r2 = (x[None, None, :] ** 2 + x[None, :, None] ** 2 + z[:, None, None] ** 2)
     r = np.sqrt(r2)
     dr = 2 * dx
     p = np.where(r < r0, p_in, np.where(r < r0 + dr, p_in + (p_out - p_in) * (r - r0) / dr, p_out))
     vc[7] = p
     b = bmag / math.sqrt(3.0) / math.sqrt(4.0 * math.pi)
-    faces = [np.full((n, n, n + 1), b), np.full((n, n + 1, n), b), np.full((n + 1, n, n), b)]
+    faces = [np.full((nz, n, n + 1), b), np.full((nz, n + 1, n), b), np.full((nz + 1, n, n), b)]
     vc[4:7] = b
-    spec = dict(name=f"blast3d_{n}", dims=3, components=3, nx=(n, n, n), dx=(dx, dx, dx),
+    name = f"blast3d_{n}" if nz == n else f"blast3d_{n}_slab{nz}"
+    spec = dict(name=name, dims=3, components=3, nx=(n, n, nz), dx=(dx, dx, dx),
                 gamma=5.0 / 3.0, recon="LINEAR", limiter="MC_LIM", solver="hlld",
                 stepping="RK2", ct=True, bc="periodic", cfl=0.3, first_dt=1e-4)
     return spec, vc, faces
