@@ -20,16 +20,19 @@
 //   k_adj_recon    States (PLM / PPM) and CT_StoreVelSlopes
 //   k_adj_bound    Boundary (periodic / outflow copies), transposed
 //   k_adj_p2c      PrimToCons3D                (Src/mappers3D.c:74)
-// The local derivatives inside those kernels (limiter, reconstruction,
-// Riemann solver, edge EMF, prim<->cons maps) come from evaluating the same
+// The local derivatives inside those kernels belong to exactly the branch
+// the forward evaluation takes, floors included.  The HLL / HLLD Riemann
+// outputs and the edge EMF are transposed by hand-derived reverse-mode
+// point functions (pg_adjoint_pt.cuh), all inputs in one evaluation; the
+// limiter, reconstruction, Roe solver and prim<->cons maps evaluate the same
 // templated point functions as the forward kernels with Dual<1> inputs, one
-// seeded input at a time, so they belong to exactly the branch the forward
-// evaluation takes, floors included.
+// seeded input at a time.
 #include <cstring>
 #include <string>
 #include <utility>
 #include <vector>
 
+#include "pg_adjoint_pt.cuh"
 #include "pg_fp64_kernels.cuh"
 
 namespace pg {
@@ -113,86 +116,6 @@ int tl_xfer(Solver* S, double* const vars[8], double* const faces[3], int layout
     return PG_ERR_CUDA;
   }
   return PG_OK;
-}
-
-// ---------------------------------------------------------------------------
-// point functions evaluated by the adjoint kernels (the arithmetic of the
-// forward kernels, written over a small input vector)
-// ---------------------------------------------------------------------------
-
-// States of one zone from w[0..4] = v[c-2..c+2] (as k_recon).
-template <class T>
-__device__ __forceinline__ void recon_pt(int recon, int lim, int nv, const T* w, T& vp, T& vm) {
-  if (recon == PG_LINEAR) {
-    T v0 = w[2];
-    T dvp = w[3] - v0;
-    T dvm = v0 - w[1];
-    T dv = limit(lim, nv, dvp, dvm);
-    vp = v0 + dv * 0.5;
-    vm = v0 - dv * 0.5;
-  } else {
-    T v0 = w[2];
-    T p = ppm_iface(w[1], v0, w[3], w[4]);
-    T m = ppm_iface(w[0], w[1], v0, w[3]);
-    ppm_limit(v0, p, m);
-    vp = p;
-    vm = m;
-  }
-}
-
-// Riemann outputs at one interface (as k_riemann):
-// out[0..7] flux, out[8] total pressure, out[9] max(0,-SL), out[10] max(0,SR).
-template <class T, int DIR>
-__device__ __forceinline__ void riemann_pt(int solver, double gamma, bool c3, const T* vL, const T* vR, T* out) {
-  T uL[NV], uR[NV], mach = T(0.0);
-  const T gmm1 = T(gamma - 1.0);
-  prim_to_cons(vL, uL, gmm1);
-  prim_to_cons(vR, uR, gmm1);
-  Iface<T> o;
-  if (solver == PG_HLL) {
-    hll_solver<DIR, false>(vL, uL, vR, uR, T(gamma), o, mach);
-  } else if (solver == PG_ROE) {
-    int bad = 0;
-    roe_solver<DIR, false>(vL, uL, vR, uR, T(gamma), c3, o, mach, bad);
-  } else {
-    hlld_solver<DIR, false>(vL, uL, vR, uR, T(gamma), o, mach);
-  }
-#pragma unroll
-  for (int nv = 0; nv < NV; nv++) out[nv] = o.f[nv];
-  out[NV] = o.press;
-  out[NV + 1] = pmax(T(0.0), -o.SL);
-  out[NV + 2] = pmax(T(0.0), o.SR);
-}
-
-// Edge EMF from its 40 inputs (as uct_edge):
-//  in[0..7]   SR_x(c00) SR_x(c0y) SL_x(c00) SL_x(c0y) SR_y(c00) SR_y(cx0) SL_y(c00) SL_y(cx0)
-//  in[8..11]  x-face field at c00-sy, c00, c0y, c0y+sy
-//  in[12..15] y-face field at c00-sx, c00, cx0, cx0+sx
-//  in[16..39] per zone q of (c00, cx0, c0y, cxy): vy, vx, dvy_dx, dvy_dy, dvx_dx, dvx_dy
-constexpr int kEdgeIn = 40;
-template <class T>
-__device__ __forceinline__ T emf_pt(const T* in) {
-  T a_xp = pmax(in[0], in[1]);
-  T a_xm = pmax(in[2], in[3]);
-  T a_yp = pmax(in[4], in[5]);
-  T a_ym = pmax(in[6], in[7]);
-  T sbS = mc_lim2(in[10] - in[9], in[9] - in[8]);
-  T sbN = mc_lim2(in[11] - in[10], in[10] - in[9]);
-  T sbW = mc_lim2(in[14] - in[13], in[13] - in[12]);
-  T sbE = mc_lim2(in[15] - in[14], in[14] - in[13]);
-  T bS = in[9] + 0.5 * sbS;
-  T bW = in[13] + 0.5 * sbW;
-  T bN = in[10] - 0.5 * sbN;
-  T bE = in[14] - 0.5 * sbE;
-  const T* q0 = in + 16;  // c00
-  const T* q1 = in + 22;  // cx0
-  const T* q2 = in + 28;  // c0y
-  const T* q3 = in + 34;  // cxy
-  T eSW = (q0[0] + 0.5 * (q0[2] + q0[3])) * bS - (q0[1] + 0.5 * (q0[4] + q0[5])) * bW;
-  T eSE = (q1[0] - 0.5 * (q1[2] - q1[3])) * bS - (q1[1] - 0.5 * (q1[4] - q1[5])) * bE;
-  T eNE = (q3[0] - 0.5 * (q3[2] + q3[3])) * bN - (q3[1] - 0.5 * (q3[4] + q3[5])) * bE;
-  T eNW = (q2[0] + 0.5 * (q2[2] - q2[3])) * bN - (q2[1] + 0.5 * (q2[4] - q2[5])) * bW;
-  return uct_hll_combine(a_xp, a_xm, a_yp, a_ym, eSW, eSE, eNE, eNW, bS, bN, bW, bE);
 }
 
 // ---------------------------------------------------------------------------
@@ -384,11 +307,11 @@ __global__ void k_adj_ct(AdjArgs A, Tab8 lBc) {
   }
 }
 
-// One edge EMF component transposed for one seeded input kk: gathers the 40
-// inputs, evaluates the derivative of the edge value along input kk and
-// scatters it.
+// One edge EMF component transposed: gathers the 40 inputs, forms
+// lam * d(edge value)/d(input) for all of them in one reverse evaluation and
+// scatters the non-zero ones.
 template <int E>
-__device__ __forceinline__ void adj_edge(const AdjArgs& A, long long c, double lam, int kk) {
+__device__ __forceinline__ void adj_edge(const AdjArgs& A, long long c, double lam) {
   if (lam == 0.0) return;
   constexpr int AX = E == 2 ? 0 : (E == 0 ? 1 : 2);
   constexpr int AY = E == 2 ? 1 : (E == 0 ? 2 : 0);
@@ -410,12 +333,14 @@ __device__ __forceinline__ void adj_edge(const AdjArgs& A, long long c, double l
   in[7] = f.SL[AY][cx0]; dst[7] = &b.lS[AY][0][cx0];
   const long long bxi[4] = {c00 - sy, c00, c0y, c0y + sy};
   const long long byi[4] = {c00 - sx, c00, cx0, cx0 + sx};
+#pragma unroll
   for (int t = 0; t < 4; t++) {
     in[8 + t] = f.Bs[AX][bxi[t]];
     dst[8 + t] = &b.lBin[AX][bxi[t]];
     in[12 + t] = f.Bs[AY][byi[t]];
     dst[12 + t] = &b.lBin[AY][byi[t]];
   }
+#pragma unroll
   for (int q = 0; q < 4; q++) {
     const long long cc = cells[q];
     double** d6 = dst + 16 + 6 * q;
@@ -427,27 +352,24 @@ __device__ __forceinline__ void adj_edge(const AdjArgs& A, long long c, double l
     i6[4] = f.DV[AX][AX][cc];  d6[4] = &b.lDV[AX][AX][cc];
     i6[5] = f.DV[AY][AX][cc];  d6[5] = &b.lDV[AY][AX][cc];
   }
-  D1 x[kEdgeIn];
+  double gk[kEdgeIn];
+  emf_rev(in, lam, gk);
 #pragma unroll
-  for (int q = 0; q < kEdgeIn; q++) x[q] = D1(in[q]);
-  x[kk].d[0] = 1.0;
-  const double gk = lam * emf_pt(x).d[0];
-  if (gk != 0.0) atomicAdd(dst[kk], gk);
+  for (int q = 0; q < kEdgeIn; q++)
+    if (gk[q] != 0.0) atomicAdd(dst[q], gk[q]);
 }
 
 __global__ void k_adj_emf(AdjArgs A, Box box) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   const int ncomp = A.f.g.dims == 3 ? 3 : 1;
-  if (q >= box.count() * kEdgeIn * ncomp) return;
-  const int kk = (int)(q % kEdgeIn);
-  const long long r = q / kEdgeIn;
-  const int e = (int)(r % ncomp);
+  if (q >= box.count() * ncomp) return;
+  const int e = (int)(q % ncomp);
   int i, j, k;
-  box.coords(r / ncomp, i, j, k);
+  box.coords(q / ncomp, i, j, k);
   const long long c = cidx(A.f.g, k, j, i);
-  if (ncomp == 1 || e == 2) adj_edge<2>(A, c, A.b.lE[2][c], kk);
-  else if (e == 0) adj_edge<0>(A, c, A.b.lE[0][c], kk);
-  else adj_edge<1>(A, c, A.b.lE[1][c], kk);
+  if (ncomp == 1 || e == 2) adj_edge<2>(A, c, A.b.lE[2][c]);
+  else if (e == 0) adj_edge<0>(A, c, A.b.lE[0][c]);
+  else adj_edge<1>(A, c, A.b.lE[1][c]);
 }
 
 // U[c] += -dt/dx (F[c] - F[c-s]) (and the pressure term on the normal
@@ -468,10 +390,62 @@ __global__ void k_adj_flux(AdjArgs A, Box box) {
 
 // Riemann problem at interface c+1/2 transposed: adjoint on VP[c], VM[c+s]
 // (and on the face field that replaces their normal component under CT).
-// One thread per (interface, seeded input of the 16 states); lVP / lVM are
-// zero on entry.
+// HLL / HLLD: one thread per interface, all 16 inputs in one reverse
+// evaluation.  Roe: one thread per (interface, seeded input of the 16
+// states).  lVP / lVM are zero on entry.
 template <int DIR>
-__global__ void k_adj_riemann(AdjArgs A, Box box, int solver) {
+__device__ __forceinline__ bool adj_riemann_load(const AdjArgs& A, long long c, long long s, double* lam,
+                                                 double* vL, double* vR) {
+  const bool ct = A.f.ct;
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) lam[nv] = A.b.lF[nv][c];
+  lam[NV] = A.b.lP[c];
+  lam[NV + 1] = ct ? A.b.lS[DIR][0][c] : 0.0;
+  lam[NV + 2] = ct ? A.b.lS[DIR][1][c] : 0.0;
+  bool any = false;
+#pragma unroll
+  for (int o = 0; o < kRiemannOut; o++) any |= lam[o] != 0.0;
+  if (!any) return false;
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    vL[nv] = A.f.VP[nv][c];
+    vR[nv] = A.f.VM[nv][c + s];
+  }
+  if (ct) {
+    const double bn = A.f.Bs[DIR][c];
+    vL[Rot<DIR>::bn] = bn;
+    vR[Rot<DIR>::bn] = bn;
+  }
+  return true;
+}
+
+template <int DIR, int SOLVER>
+__global__ void k_adj_riemann(AdjArgs A, Box box) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= box.count()) return;
+  int i, j, k;
+  box.coords(q, i, j, k);
+  const Geom& g = A.f.g;
+  const long long c = cidx(g, k, j, i), s = g.s[DIR];
+  double lam[kRiemannOut], vL[NV], vR[NV], gL[NV], gR[NV];
+  if (!adj_riemann_load<DIR>(A, c, s, lam, vL, vR)) return;
+  if (SOLVER == PG_HLL) hll_rev<DIR>(vL, vR, A.f.gamma, lam, gL, gR);
+  else hlld_rev<DIR>(vL, vR, A.f.gamma, lam, gL, gR);
+  constexpr int BN = Rot<DIR>::bn;
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) {
+    if (A.f.ct && nv == BN) continue;
+    A.b.lVP[nv][c] = gL[nv];
+    A.b.lVM[nv][c + s] = gR[nv];
+  }
+  if (A.f.ct) {
+    const double gb = gL[BN] + gR[BN];
+    if (gb != 0.0) atomicAdd(&A.b.lBin[DIR][c], gb);
+  }
+}
+
+template <int DIR>
+__global__ void k_adj_riemann_dual(AdjArgs A, Box box, int solver) {
   const long long qq = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (qq >= box.count() * 2 * NV) return;
   const int kk = (int)(qq % (2 * NV));
@@ -480,30 +454,10 @@ __global__ void k_adj_riemann(AdjArgs A, Box box, int solver) {
   const Geom& g = A.f.g;
   const long long c = cidx(g, k, j, i), s = g.s[DIR];
   const bool ct = A.f.ct;
-  constexpr int NO = NV + 3;
-  double lam[NO];
-#pragma unroll
-  for (int nv = 0; nv < NV; nv++) lam[nv] = A.b.lF[nv][c];
-  lam[NV] = A.b.lP[c];
-  lam[NV + 1] = ct ? A.b.lS[DIR][0][c] : 0.0;
-  lam[NV + 2] = ct ? A.b.lS[DIR][1][c] : 0.0;
-  bool any = false;
-#pragma unroll
-  for (int o = 0; o < NO; o++) any |= lam[o] != 0.0;
+  double lam[kRiemannOut], vL[NV], vR[NV];
+  if (!adj_riemann_load<DIR>(A, c, s, lam, vL, vR)) return;
   constexpr int BN = Rot<DIR>::bn;
-  double vL[NV], vR[NV];
-#pragma unroll
-  for (int nv = 0; nv < NV; nv++) {
-    vL[nv] = A.f.VP[nv][c];
-    vR[nv] = A.f.VM[nv][c + s];
-  }
-  if (ct) {
-    const double bn = A.f.Bs[DIR][c];
-    vL[BN] = bn;
-    vR[BN] = bn;
-  }
-  if (!any) return;
-  D1 xL[NV], xR[NV], out[NO];
+  D1 xL[NV], xR[NV], out[kRiemannOut];
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
     xL[nv] = D1(vL[nv]);
@@ -514,7 +468,7 @@ __global__ void k_adj_riemann(AdjArgs A, Box box, int solver) {
   riemann_pt<D1, DIR>(solver, A.f.gamma, A.f.ncomp == 3, xL, xR, out);
   double gk = 0.0;
 #pragma unroll
-  for (int o = 0; o < NO; o++) gk += lam[o] * out[o].d[0];
+  for (int o = 0; o < kRiemannOut; o++) gk += lam[o] * out[o].d[0];
   const int nv = kk < NV ? kk : kk - NV;
   if (ct && nv == BN) {
     if (gk != 0.0) atomicAdd(&A.b.lBin[DIR][c], gk);
@@ -708,7 +662,12 @@ void rev_dir(Solver* S, const AdjArgs& A) {
     cudaMemsetAsync(A.b.lVM[nv], 0, n * sizeof(double), st);
   }
   k_adj_flux<DIR><<<grid_for(ib.count()), kT, 0, st>>>(A, ib);
-  k_adj_riemann<DIR><<<grid_for(ib.count() * 2 * NV, 64), 64, 0, st>>>(A, ib, S->cfg.riemann);
+  if (S->cfg.riemann == PG_HLLD)
+    k_adj_riemann<DIR, PG_HLLD><<<grid_for(ib.count(), 64), 64, 0, st>>>(A, ib);
+  else if (S->cfg.riemann == PG_HLL)
+    k_adj_riemann<DIR, PG_HLL><<<grid_for(ib.count(), 64), 64, 0, st>>>(A, ib);
+  else
+    k_adj_riemann_dual<DIR><<<grid_for(ib.count() * 2 * NV, 64), 64, 0, st>>>(A, ib, S->cfg.riemann);
   k_adj_recon<DIR><<<grid_for(rb.count() * NV, 128), 128, 0, st>>>(A, rb);
 }
 
@@ -765,7 +724,7 @@ void rev_stage(Solver* S, const AdjArgs& A, bool add_b0) {
       }
     }
     eb.prepare();
-    k_adj_emf<<<grid_for(eb.count() * kEdgeIn * (g.dims == 3 ? 3 : 1), 64), 64, 0, st>>>(A, eb);
+    k_adj_emf<<<grid_for(eb.count() * (g.dims == 3 ? 3 : 1), 64), 64, 0, st>>>(A, eb);
   }
   if (g.dims > 2) rev_dir<2>(S, A);
   if (g.dims > 1) rev_dir<1>(S, A);

@@ -1,4 +1,4 @@
-// Point-wise ideal-MHD physics on the device, templated on the arithmetic
+// Point-wise ideal-MHD physics (device code; also callable on the host), templated on the arithmetic
 // type.  Every expression keeps the operand order of PLUTO 4.3 so that the
 // FP64 instantiation, compiled without multiply-add contraction, reproduces
 // the reference C code bit for bit.  References are to files in the PLUTO
@@ -43,10 +43,10 @@ __host__ __device__ __forceinline__ int bc_src(int x, int beg, int end, int n, i
   return x;
 }
 
-template <class T> __device__ __forceinline__ T pmax(T a, T b) { return a >= b ? a : b; }  // macros.h MAX
-template <class T> __device__ __forceinline__ T pmin(T a, T b) { return a <= b ? a : b; }  // macros.h MIN
-template <class T> __device__ __forceinline__ T abs_min(T a, T b) { return fabs(a) < fabs(b) ? a : b; }
-template <class T> __device__ __forceinline__ T minmod(T a, T b) {
+template <class T> __host__ __device__ __forceinline__ T pmax(T a, T b) { return a >= b ? a : b; }  // macros.h MAX
+template <class T> __host__ __device__ __forceinline__ T pmin(T a, T b) { return a <= b ? a : b; }  // macros.h MIN
+template <class T> __host__ __device__ __forceinline__ T abs_min(T a, T b) { return fabs(a) < fabs(b) ? a : b; }
+template <class T> __host__ __device__ __forceinline__ T minmod(T a, T b) {
   return a * b > T(0) ? (fabs(a) < fabs(b) ? a : b) : T(0);
 }
 
@@ -58,7 +58,7 @@ template <> struct Rot<2> { static constexpr int vn = VX3, vt = VX1, vb = VX2, b
 
 // Src/MHD/mappers.c:25-86
 template <class T>
-__device__ __forceinline__ void prim_to_cons(const T* v, T* u, T gmm1) {
+__host__ __device__ __forceinline__ void prim_to_cons(const T* v, T* u, T gmm1) {
   T kinb2;
   u[RHO] = v[RHO];
   u[MX1] = v[RHO] * v[VX1];
@@ -75,7 +75,7 @@ __device__ __forceinline__ void prim_to_cons(const T* v, T* u, T gmm1) {
 
 // Src/MHD/mappers.c:88-254 (ideal EOS): floors modify u in place.
 template <class T>
-__device__ __forceinline__ int cons_to_prim(T* u, T* v, T gmm1, T small_rho, T small_p,
+__host__ __device__ __forceinline__ int cons_to_prim(T* u, T* v, T gmm1, T small_rho, T small_p,
                                             unsigned char* flag) {
   T tau, kinb2, m2, b2;
   int ifail = 0;
@@ -112,7 +112,7 @@ __device__ __forceinline__ int cons_to_prim(T* u, T* v, T gmm1, T small_rho, T s
 
 // Src/MHD/fluxes.c:110-249
 template <int DIR, class T>
-__device__ __forceinline__ void flux(const T* v, const T* u, T* fx, T& ptot) {
+__host__ __device__ __forceinline__ void flux(const T* v, const T* u, T* fx, T& ptot) {
   using R = Rot<DIR>;
   T Bmag2 = v[BX1] * v[BX1] + v[BX2] * v[BX2] + v[BX3] * v[BX3];
   ptot = v[PRS] + T(0.5) * Bmag2;
@@ -129,7 +129,7 @@ __device__ __forceinline__ void flux(const T* v, const T* u, T* fx, T& ptot) {
 
 // Src/MHD/eigenv.c:35-104 (ideal EOS)
 template <int DIR, class T>
-__device__ __forceinline__ void max_signal_speed(const T* v, T gamma, T& cmin, T& cmax) {
+__host__ __device__ __forceinline__ void max_signal_speed(const T* v, T gamma, T& cmin, T& cmax) {
   using R = Rot<DIR>;
   T gpr = gamma * v[PRS];
   T b1 = v[R::bn], b2 = v[R::bt], b3 = v[R::bb];
@@ -149,7 +149,7 @@ template <class T> struct Iface {
 
 // Src/MHD/hll_speed.c:23-108 (DAVIS_ESTIMATE); Mach estimate only on request.
 template <int DIR, bool MACH, class T>
-__device__ __forceinline__ void hll_speed(const T* vL, const T* vR, T gamma, T& SL, T& SR, T& mach) {
+__host__ __device__ __forceinline__ void hll_speed(const T* vL, const T* vR, T gamma, T& SL, T& SR, T& mach) {
   using R = Rot<DIR>;
   T slmin, slmax, srmin, srmax;
   max_signal_speed<DIR>(vL, gamma, slmin, slmax);
@@ -167,7 +167,7 @@ __device__ __forceinline__ void hll_speed(const T* vL, const T* vR, T gamma, T& 
 
 // Src/MHD/hll.c:30-166
 template <int DIR, bool MACH, class T>
-__device__ __forceinline__ void hll_solver(const T* vL, const T* uL, const T* vR, const T* uR, T gamma,
+__host__ __device__ __forceinline__ void hll_solver(const T* vL, const T* uL, const T* vR, const T* uR, T gamma,
                                            Iface<T>& o, T& mach) {
   T fL[NV], fR[NV], ptL, ptR, SL, SR, scrh;
   flux<DIR>(vL, uL, fL, ptL);
@@ -203,7 +203,7 @@ __device__ __forceinline__ void hll_solver(const T* vL, const T* uL, const T* vR
 // eigenvector entries (adding them changes no bit).  bad = 1 when the Roe
 // sound speed squared is negative (the reference stops the run there).
 template <int DIR, bool MACH, class T>
-__device__ __forceinline__ void roe_solver(const T* vL, const T* uL, const T* vR, const T* uR, T gamma, bool c3,
+__host__ __device__ __forceinline__ void roe_solver(const T* vL, const T* uL, const T* vR, const T* uR, T gamma, bool c3,
                                            Iface<T>& o, T& mach, int& bad) {
   using R = Rot<DIR>;
   constexpr int vn = R::vn, vt = R::vt, vb = R::vb, bn = R::bn, bt = R::bt, bb = R::bb;
@@ -373,7 +373,7 @@ __device__ __forceinline__ void roe_solver(const T* vL, const T* uL, const T* vR
 
 // Src/MHD/hlld.c:44-452 (ideal EOS, no background field)
 template <int DIR, bool MACH, class T>
-__device__ __forceinline__ void hlld_solver(const T* vL, const T* uL, const T* vR, const T* uR, T gamma,
+__host__ __device__ __forceinline__ void hlld_solver(const T* vL, const T* uL, const T* vR, const T* uR, T gamma,
                                             Iface<T>& o, T& mach) {
   using R = Rot<DIR>;
   constexpr int MXn = R::vn, MXt = R::vt, MXb = R::vb;
@@ -514,7 +514,7 @@ __device__ __forceinline__ void hlld_solver(const T* vL, const T* uL, const T* v
 enum : int { LIM_FLAT = 0, LIM_MINMOD = 1, LIM_VANLEER = 2, LIM_MC = 3, LIM_DEFAULT = 4 };
 
 template <class T>
-__device__ __forceinline__ T limit(int lim, int nv, T dvp, T dvm) {
+__host__ __device__ __forceinline__ T limit(int lim, int nv, T dvp, T dvm) {
   if (lim == LIM_DEFAULT) lim = (nv == RHO) ? LIM_MC : (nv == PRS ? LIM_MINMOD : LIM_VANLEER);
   switch (lim) {
     case LIM_FLAT: return T(0);
@@ -532,7 +532,7 @@ __device__ __forceinline__ T limit(int lim, int nv, T dvp, T dvm) {
 // PPM interface value with minmod clip, ppm_states.c:131-143 (PPM_ORDER 4,
 // Cartesian coefficients ppm_coeffs.c:478-520).
 template <class T>
-__device__ __forceinline__ T ppm_iface(T vm1, T v0, T vp1, T vp2) {
+__host__ __device__ __forceinline__ T ppm_iface(T vm1, T v0, T vp1, T vp2) {
   const T w_1 = T(-1.0 / 12.0), w0 = T(7.0 / 12.0), w1 = T(7.0 / 12.0), w2 = T(-1.0 / 12.0);
   T vp = w_1 * vm1 + w0 * v0 + w1 * vp1 + w2 * vp2;
   T dv = vp1 - v0;
@@ -542,7 +542,7 @@ __device__ __forceinline__ T ppm_iface(T vm1, T v0, T vp1, T vp2) {
 
 // Parabolic limiter, ppm_states.c:146-207 with hp = hm = 3 (cp = cm = 2).
 template <class T>
-__device__ __forceinline__ void ppm_limit(T v, T& vp, T& vm) {
+__host__ __device__ __forceinline__ void ppm_limit(T v, T& vp, T& vm) {
   const T cm = (T(3) + T(1)) / (T(3) - T(1));
   const T cp = (T(3) + T(1)) / (T(3) - T(1));
   T dvp = vp - v, dvm = vm - v;
@@ -557,7 +557,7 @@ __device__ __forceinline__ void ppm_limit(T v, T& vp, T& vm) {
 
 // Src/MHD/CT/ct_stag_slopes.c:92-105
 template <class T>
-__device__ __forceinline__ T mc_lim2(T dp, T dm) {
+__host__ __device__ __forceinline__ T mc_lim2(T dp, T dm) {
   if (dp * dm < T(0)) return T(0);
   T dc = T(0.5) * (dp + dm);
   T scrh = T(2) * (fabs(dp) < fabs(dm) ? dp : dm);
@@ -566,7 +566,7 @@ __device__ __forceinline__ T mc_lim2(T dp, T dm) {
 
 // Combination of the 2D HLL edge formula, ct_emf_average.c:262-289.
 template <class T>
-__device__ __forceinline__ T uct_hll_combine(T a_xp, T a_xm, T a_yp, T a_ym, T eSW, T eSE, T eNE, T eNW, T bS,
+__host__ __device__ __forceinline__ T uct_hll_combine(T a_xp, T a_xm, T a_yp, T a_ym, T eSW, T eSE, T eNE, T eNW, T bS,
                                              T bN, T bW, T bE) {
   T e = a_xp * a_yp * eSW + a_xm * a_yp * eSE + a_xm * a_ym * eNE + a_xp * a_ym * eNW;
   e /= (a_xp + a_xm) * (a_yp + a_ym);
