@@ -145,6 +145,11 @@ struct AdjBufs {
   double* B1[3];
   double* U1[8];
   double* U2[8];
+  // reconstructed states of directions 1 and 2 (direction 0 uses the
+  // solver's VP/VM): under CT the EMF needs every direction's wave speeds
+  // first, and the states of each direction stay for its reversal
+  double* VPd[2][8];
+  double* VMd[2][8];
 };
 
 struct AdjArgs {
@@ -500,6 +505,14 @@ __global__ void k_adj_recon(AdjArgs A, Box box) {
       lm -= ld;
     }
     if (lp == 0.0 && lm == 0.0) return;
+    if (recon == PG_LINEAR) {
+      double gw[3];
+      plm_rev(A.f.limiter, nv, A.f.V[nv][c - s], A.f.V[nv][c], A.f.V[nv][c + s], lp, lm, gw);
+#pragma unroll
+      for (int t = 0; t < 3; t++)
+        if (gw[t] != 0.0) atomicAdd(&A.b.lVin[nv][c + (t - 1) * s], gw[t]);
+      return;
+    }
     double w[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
     for (int t = t0; t <= t1; t++) w[t] = A.f.V[nv][c + (t - 2) * s];
     for (int t = t0; t <= t1; t++) {
@@ -574,6 +587,10 @@ static int adjoint_alloc(Solver* S, AdjBufs** out) {
   const size_t bytes = sizeof(double) * S->g.ncell;
   double** p = (double**)B;
   for (size_t q = 0; q < sizeof(AdjBufs) / sizeof(double*); q++) {
+    bool unused = false;  // the per-direction states of directions >= dims
+    for (int d = S->g.dims; d < 3; d++)
+      for (int nv = 0; nv < NV; nv++) unused |= &p[q] == &B->VPd[d - 1][nv] || &p[q] == &B->VMd[d - 1][nv];
+    if (unused) continue;
     if (cudaMalloc(&p[q], bytes) != cudaSuccess) {
       p[q] = nullptr;
       return PG_ERR_NOMEM;
@@ -650,13 +667,26 @@ void fwd_dir(Solver* S, const F64A<double>& f) {
     k_riemann<double, DIR, PG_HLLD, false><<<grid_for(ib.count(), 128), 128, 0, st>>>(f, ib, 0);
 }
 
+// The arguments with direction d's reconstructed states (see AdjBufs::VPd).
+AdjArgs with_dir_states(const AdjArgs& A, int d) {
+  AdjArgs r = A;
+  if (d > 0)
+    for (int nv = 0; nv < NV; nv++) {
+      r.f.VP[nv] = A.b.VPd[d - 1][nv];
+      r.f.VM[nv] = A.b.VMd[d - 1][nv];
+    }
+  return r;
+}
+
+// Direction DIR reversed; `recompute`: reconstruct its states and Riemann
+// outputs first (else they are in place from the CT pre-pass).
 template <int DIR>
-void rev_dir(Solver* S, const AdjArgs& A) {
+void rev_dir(Solver* S, const AdjArgs& A, bool recompute) {
   const Geom& g = S->g;
   cudaStream_t st = S->stream;
   const long long n = g.ncell;
   Box rb = dir_box(g, DIR, -1, 1, A.f.ct), ib = dir_box(g, DIR, -1, 0, A.f.ct);
-  fwd_dir<DIR>(S, A.f);  // states of this direction
+  if (recompute) fwd_dir<DIR>(S, A.f);  // states of this direction
   for (int nv = 0; nv < NV; nv++) {
     cudaMemsetAsync(A.b.lVP[nv], 0, n * sizeof(double), st);
     cudaMemsetAsync(A.b.lVM[nv], 0, n * sizeof(double), st);
@@ -708,11 +738,13 @@ void rev_stage(Solver* S, const AdjArgs& A, bool add_b0) {
     }
   }
   fwd_bound(S, A.f);
+  const AdjArgs A0 = with_dir_states(A, 0), A1 = with_dir_states(A, 1), A2 = with_dir_states(A, 2);
   if (ct) {
-    // wave speeds and velocity slopes of every direction, inputs of the EMF
-    fwd_dir<0>(S, A.f);
-    if (g.dims > 1) fwd_dir<1>(S, A.f);
-    if (g.dims > 2) fwd_dir<2>(S, A.f);
+    // states, wave speeds and velocity slopes of every direction (the EMF
+    // inputs), each direction's states kept for its reversal below
+    fwd_dir<0>(S, A0.f);
+    if (g.dims > 1) fwd_dir<1>(S, A1.f);
+    if (g.dims > 2) fwd_dir<2>(S, A2.f);
     k_adj_ct<<<grid_for(n), kT, 0, st>>>(A, tab(b.lB, 3));
     Box eb;
     for (int ax = 0; ax < 3; ax++) {
@@ -726,9 +758,9 @@ void rev_stage(Solver* S, const AdjArgs& A, bool add_b0) {
     eb.prepare();
     k_adj_emf<<<grid_for(eb.count() * (g.dims == 3 ? 3 : 1), 64), 64, 0, st>>>(A, eb);
   }
-  if (g.dims > 2) rev_dir<2>(S, A);
-  if (g.dims > 1) rev_dir<1>(S, A);
-  rev_dir<0>(S, A);
+  if (g.dims > 2) rev_dir<2>(S, A2, !ct);
+  if (g.dims > 1) rev_dir<1>(S, A1, !ct);
+  rev_dir<0>(S, A0, !ct);
   if (add_b0)
     for (int d = 0; d < g.dims; d++) k_add<<<grid_for(n), kT, 0, st>>>(b.lBin[d], b.lB0[d], n);
   BoundTab t;

@@ -738,6 +738,40 @@ __host__ __device__ __forceinline__ bool riemann_rev(int solver, double gamma, c
   return false;
 }
 
+// Partial derivatives (pp, pm) of limit(lim, nv, dvp, dvm) with respect to
+// dvp and dvm, on the branch limit takes (Src/States/plm_coeffs.h:72-175).
+__host__ __device__ __forceinline__ void limit_partials(int lim, int nv, double dvp, double dvm, double& pp,
+                                                        double& pm) {
+  pp = pm = 0.0;
+  if (lim == LIM_DEFAULT) lim = (nv == RHO) ? LIM_MC : (nv == PRS ? LIM_MINMOD : LIM_VANLEER);
+  if (lim == LIM_FLAT || !(dvp * dvm > 0.0)) return;
+  const bool pmin = ::fabs(dvp) < ::fabs(dvm);  // abs_min(dvp, dvm) selects dvp
+  if (lim == LIM_MINMOD) {
+    (pmin ? pp : pm) = 1.0;
+  } else if (lim == LIM_VANLEER) {  // 2 dvp dvm / (dvp + dvm)
+    const double s = dvp + dvm, r = 2.0 * dvp * dvm / s;
+    pp = (2.0 * dvm - r) / s;
+    pm = (2.0 * dvp - r) / s;
+  } else {  // MC: abs_min(0.5 (dvm + dvp), 2 abs_min(dvp, dvm))
+    const double qc = 0.5 * (dvm + dvp), scrh = 2.0 * (pmin ? dvp : dvm);
+    if (::fabs(qc) < ::fabs(scrh)) pp = pm = 0.5;
+    else (pmin ? pp : pm) = 2.0;
+  }
+}
+
+// PLM states of one zone transposed (recon_pt with PG_LINEAR): vp = v0 +
+// dv/2, vm = v0 - dv/2, dv = limit(w3 - v0, v0 - w1); g[0..2] = the adjoint
+// on w1, v0, w3 from the adjoints lp, lm on vp, vm.
+__host__ __device__ __forceinline__ void plm_rev(int lim, int nv, double w1, double v0, double w3, double lp,
+                                                 double lm, double* g) {
+  double pp, pm;
+  limit_partials(lim, nv, w3 - v0, v0 - w1, pp, pm);
+  const double adv = 0.5 * (lp - lm);
+  g[0] = -adv * pm;
+  g[1] = lp + lm + adv * (pm - pp);
+  g[2] = adv * pp;
+}
+
 // mc_lim2 (Src/MHD/CT/ct_stag_slopes.c:92-105) transposed: a_dp, a_dm
 __host__ __device__ __forceinline__ void mc_lim2_rev(double dp, double dm, double a, double& adp, double& adm) {
   adp = adm = 0.0;

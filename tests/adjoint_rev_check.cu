@@ -7,9 +7,9 @@
 // region: L / R flux, single-star L / R, double-star L / R, the HLLC
 // reversion) and random output adjoints lam, it forms J^T lam once by the
 // reverse function and once column by column from 16 seeded Dual<1>
-// evaluations of riemann_pt, likewise for the 40-input edge EMF, and prints
-// one line per (solver, direction) with the sample count, the branch counts
-// and the largest relative difference.
+// evaluations of riemann_pt, likewise for the 40-input edge EMF and the PLM
+// states, and prints one line per check with the sample count, the branch
+// counts and the largest relative difference.
 #include <cmath>
 #include <cstdint>
 #include <cstdio>
@@ -161,6 +161,35 @@ static double check_emf(int nsamp, long* branches) {
   return worst;
 }
 
+// PLM states (every limiter, the DEFAULT mix per variable) transposed
+static double check_plm(int nsamp, long* branches) {
+  double worst = 0.0;
+  for (int t = 0; t < nsamp; t++) {
+    double w[5];
+    for (int q = 0; q < 5; q++) w[q] = urange(-1.0, 1.0);
+    if (t % 3 == 0)  // monotone: the limiters' smooth branches
+      for (int q = 0; q < 5; q++) w[q] = 0.3 * q * q * (t % 2 ? 1.0 : -1.0) + urange(0.0, 0.1);
+    const int lim = t % 5, nv = (t / 5) % NV;
+    const double lp = urange(-1.0, 1.0), lm = urange(-1.0, 1.0);
+    double g[3];
+    plm_rev(lim, nv, w[1], w[2], w[3], lp, lm, g);
+    double diff = 0.0, scale = 0.0;
+    for (int kk = 1; kk <= 3; kk++) {
+      D1 x[5], vp, vm;
+      for (int q = 0; q < 5; q++) x[q] = D1(w[q]);
+      x[kk].d[0] = 1.0;
+      recon_pt(PG_LINEAR, lim, nv, x, vp, vm);
+      const double ref = lp * vp.d[0] + lm * vm.d[0];
+      scale = fmax(scale, fabs(ref));
+      diff = fmax(diff, fabs(g[kk - 1] - ref));
+    }
+    branches[(w[3] - w[2]) * (w[2] - w[1]) > 0.0 ? 1 : 0]++;
+    const double rel = scale > 0.0 ? diff / scale : diff;
+    if (!(rel <= worst)) worst = rel;
+  }
+  return worst;
+}
+
 int main(int argc, char** argv) {
   const int nsamp = argc > 1 ? atoi(argv[1]) : 20000;
   const double gamma = 5.0 / 3.0;
@@ -178,5 +207,8 @@ int main(int argc, char** argv) {
   long br[3] = {0, 0, 0};
   const double w = check_emf(nsamp, br);
   printf("emf samples %d branches %ld %ld %ld worst %.3e\n", nsamp, br[0], br[1], br[2], w);
+  long bp[2] = {0, 0};
+  const double wp = check_plm(nsamp, bp);
+  printf("plm samples %d branches %ld %ld worst %.3e\n", nsamp, bp[0], bp[1], wp);
   return 0;
 }
