@@ -158,6 +158,8 @@ def kernel_bytes(name, n, stage_mix=True):
         "mixed_sweep_x_tma": (ext, 32 + 4 + 20 + 2 + 8 + 12),
         "mixed_sweep_y_tma": (ext, 32 + 4 + 40 + 4 + 8 + 12),
         "mixed_sweep_z_tma": (ext, 32 + 4 + 40 + 4 + 8 + 12),
+        "mixed_sweep_y_march": (ext, 32 + 4 + 40 + 4 + 8 + 12),
+        "mixed_sweep_z_march": (ext, 32 + 4 + 40 + 4 + 8 + 12),
         "mixed_emf": (edges, 24 + 36 + 12 + 12 + 12),
         "mixed_face": (edges, 12 + 12 + 6 + 12),
         # resident FP64 accumulators: stage 1 reads U0 (5 x 8 B under CT), dU (5 x 4),

@@ -662,6 +662,136 @@ __global__ void __launch_bounds__(32 * kTY, 2)
 }
 
 // ---------------------------------------------------------------------------
+// y/z sweep marching along DIR: a thread walks one column segment of `seg`
+// cells, keeping the stencil planes, the left state of the interface above
+// and the flux of the interface below in registers.  No shared memory and no
+// halo rows: a segment reconstructs one extra cell and solves one extra
+// Riemann problem at its start.  A warp covers 32 consecutive x, so every
+// load and store is a whole 128-byte row; the next stencil plane is loaded
+// one cell ahead.  Same arithmetic, per cell, as k_msweep_t.
+// ---------------------------------------------------------------------------
+// resident blocks of k_msweep_m: PPM's five stencil planes need the
+// registers of 3 blocks per SM (170 per thread), PLM fits 4 (128)
+__host__ __device__ constexpr int march_min_blocks(int rs) { return rs == RS_PPM ? 3 : 4; }
+
+template <int RS, int DIR, bool CT>
+__global__ void __launch_bounds__(128, march_min_blocks(RS))
+    k_msweep_m(MixArgs a, int solver, int i_lo, int i_n, int o_lo, int o_n, int seg, int nseg, int stage1) {
+  constexpr int REACH = rs_ghost_reach(RS);
+  constexpr int NP = 2 * REACH + 1;  // stencil planes of one cell
+  const Geom& g = a.g;
+  const int lane = threadIdx.x & 31;
+  const long long wi = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int nbx = (i_n + 31) >> 5;
+  const int bx = (int)(wi % nbx);
+  const long long rest = wi / nbx;
+  const int o = (int)(rest % o_n), sg = (int)(rest / o_n);
+  const int i = i_lo + 32 * bx + lane;
+  if (sg >= nseg || i >= i_lo + i_n) return;  // no block-wide synchronisation below
+  const int other = o_lo + o;
+  const int beg = g.beg[DIR], end = g.end[DIR];
+  const int m0 = beg + sg * seg;
+  const int m1 = m0 + seg - 1 < end ? m0 + seg - 1 : end;
+  const long long s = g.s[DIR];
+  const long long cb = (DIR == 1 ? (long long)other * g.s[2] : (long long)other * g.s[1]) + i;
+  const float scrh = a.sc->dtdx[DIR];
+  const float idx = a.inv_dx_f[DIR];
+  constexpr int VN = Rot<DIR>::vn;
+  // planes pl[t] = V at m - REACH + t for the cell m being reconstructed next
+  float pl[NP][NV], nxt[NV];
+#pragma unroll
+  for (int t = 0; t < NP; t++)
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) pl[t][nv] = ldg(a.Vin[nv], cb + (m0 - 1 - REACH + t) * s);
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) nxt[nv] = ldg(a.Vin[nv], cb + (m0 + REACH) * s);
+  auto reconstruct = [&](float* vp, float* vm) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++)
+      recon<RS>(a.limiter, nv, RS == RS_PPM ? pl[0][nv] : 0.f, pl[REACH - 1][nv], pl[REACH][nv],
+                pl[REACH + 1][nv], RS == RS_PPM ? pl[NP - 1][nv] : 0.f, vp[nv], vm[nv]);
+  };
+  auto advance_planes = [&](int m_next) {  // planes of cell m_next from those of m_next - 1
+#pragma unroll
+    for (int t = 0; t + 1 < NP; t++)
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) pl[t][nv] = pl[t + 1][nv];
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) pl[NP - 1][nv] = nxt[nv];
+    // the plane after, for the following cell (inside the ghost layers)
+    if (m_next + REACH + 1 <= end + 1 + REACH) {
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) nxt[nv] = ldg(a.Vin[nv], cb + (m_next + REACH + 1) * s);
+    }
+  };
+  auto store_dv = [&](long long c, const float* vp, const float* vm) {
+#pragma unroll
+    for (int comp = 0; comp < 3; comp++)
+      if (comp < g.dims) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+  };
+  // The interface two segments share (m0-1/2) is solved by the loop body in
+  // both, the only inlined copy of the Riemann solver (two copies may
+  // contract multiply-adds differently), from the same inputs: its flux is
+  // bit-identical on either side and the update stays conservative.  The
+  // left state there, cell m0-1's, is reconstructed before the loop under
+  // PLM, whose only multiply-add (v0 +- dv/2) rounds the same contracted or
+  // not; PPM's weighted sums may not, so under PPM the loop starts one cell
+  // earlier: iteration m0-2 reconstructs cell m0-1 and its Riemann problem,
+  // which has no left state, is discarded.
+  constexpr bool kPre = RS != RS_PPM;
+  float vpC[NV], vmC[NV], fp[NV], pp = 0.f, cmp = 0.f;
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) vpC[nv] = vmC[nv] = fp[nv] = 0.f;
+  if (kPre) {
+    reconstruct(vpC, vmC);  // cell m0-1
+  } else {
+    vpC[RHO] = 1.f;  // a harmless left state for the discarded problem
+    vpC[PRS] = 1.f;
+  }
+  // cell m+1 reconstructed, interface m+1/2 solved, cell m updated
+  for (int m = kPre ? m0 - 1 : m0 - 2; m <= m1; m++) {
+    const long long c = cb + m * s;
+    const bool upd = m >= m0;
+    float du[NV], cdt = 0.f;
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) du[nv] = (upd && ((a.accmask >> nv) & 1)) ? a.dU[nv][c] : 0.f;
+    if (upd && stage1) cdt = a.CDT[c];
+    const bool first = !kPre && m < m0 - 1;  // the discarded problem
+    const bool side = upd || (!first && m0 == beg);  // cell m0-1 and its interface: the first segment's
+    const float bn = (CT && !first) ? a.Bin[DIR][c] : 0.f;
+    if (CT && side) store_dv(c, vpC, vmC);
+    float vpN[NV], vmN[NV];
+    if (!first) advance_planes(m + 1);  // the planes start at cell m0-1
+    reconstruct(vpN, vmN);
+    Iface<float> f;
+    solve_iface<DIR, CT>(a, solver, vpC, vmN, bn, f);
+    if (CT && side) {
+      a.S[DIR][0][c] = pmax(0.f, -f.SL);
+      a.S[DIR][1][c] = pmax(0.f, f.SR);
+    }
+    if (upd) {
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) {
+        if (!((a.accmask >> nv) & 1)) continue;
+        float rhs = -scrh * (f.f[nv] - fp[nv]);
+        if (nv == VN) rhs -= scrh * (f.press - pp);
+        a.dU[nv][c] = du[nv] + rhs;
+      }
+      if (stage1) a.CDT[c] = cdt + 0.5f * (cmp + f.cmax) * idx;
+    }
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) {
+      fp[nv] = f.f[nv];
+      vpC[nv] = vpN[nv];
+      vmC[nv] = vmN[nv];
+    }
+    pp = f.press;
+    cmp = f.cmax;
+  }
+  if (CT && m1 == end) store_dv(cb + (end + 1) * s, vpC, vmC);
+}
+
+// ---------------------------------------------------------------------------
 // edge EMFs (FP32)
 // ---------------------------------------------------------------------------
 template <int E>
@@ -1052,6 +1182,10 @@ struct MixedState {
   int tile_tries = 1 << 20;  // see MixArgs::tile_tries
   // TMA tensor maps of the y/z sweeps (tma: maps encoded, kernels configured)
   bool tma = false;
+  // y/z sweeps by k_msweep_m (marching columns) instead of the TMA tiles,
+  // with segments of march_seg cells (0: chosen per launch)
+  bool march = false;
+  int march_seg = 0;
   SweepMaps ymaps[2], zmaps[2];  // per state buffer (V, face field); dU, CDT shared
   XSweepMaps xmaps[2];
 };
@@ -1184,6 +1318,15 @@ int mixed_alloc(Solver* S) {
     cudaMemset(M->b.U[u], 0, 8 * n * 8);
   }
   M->tma = mixed_prepare_tma(S, M);
+  {
+    // y/z sweeps: marching columns unless PLUTO_GB300_SWEEP=tile (the
+    // TMA-staged tiles when the pitch allows them, else k_msweep_t)
+    const char* e = getenv("PLUTO_GB300_SWEEP");
+    M->march = S->g.dims > 1 && !(e && strcmp(e, "tile") == 0);
+    const char* sg = getenv("PLUTO_GB300_MARCH_SEG");
+    if (sg) M->march_seg = atoi(sg);
+    if (M->march_seg < 0 || M->march_seg > 4096) M->march_seg = 0;
+  }
   return PG_OK;
 }
 
@@ -1355,6 +1498,27 @@ static void mlaunch_sweeps_rs(Solver* S, const MixArgs& a, int stage) {
     int i_lo = g.beg[0] - ext, i_n = g.nx[0] + 2 * ext;
     int oax = dir == 1 ? 2 : 1;
     int o_lo = oax < g.dims ? g.beg[oax] - ext : 0, o_n = oax < g.dims ? g.nx[oax] + 2 * ext : 1;
+    if (M->march) {
+      // segment length: 64 cells, halved (down to 8) while the sweep has
+      // fewer than four waves of resident warps (16 per SM)
+      const long long wcols = (long long)((i_n + 31) / 32) * o_n;
+      int seg = M->march_seg;
+      if (seg <= 0) {
+        int nsm = 152, dv = 0;
+        if (cudaGetDevice(&dv) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dv);
+        seg = 64;
+        while (seg > 8 && wcols * ((g.nx[dir] + seg - 1) / seg) < 4LL * 16 * nsm) seg /= 2;
+      }
+      const int nseg = (g.nx[dir] + seg - 1) / seg;
+      const long long threads = 32LL * wcols * nseg;
+      if (dir == 1)
+        PG_LAUNCH(S, "mixed_sweep_y_march", (k_msweep_m<RS, 1, CT><<<grid_for(threads, 128), 128, 0, st>>>(
+                                                a, solver, i_lo, i_n, o_lo, o_n, seg, nseg, stage1)));
+      else
+        PG_LAUNCH(S, "mixed_sweep_z_march", (k_msweep_m<RS, 2, CT><<<grid_for(threads, 128), 128, 0, st>>>(
+                                                a, solver, i_lo, i_n, o_lo, o_n, seg, nseg, stage1)));
+      continue;
+    }
     if (M->tma) {
       using TL = SweepTile<RS>;
       const int sb = a.Vin[0] == M->b.V[0][0] ? 0 : 1;

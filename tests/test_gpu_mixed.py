@@ -63,6 +63,7 @@ def test_tma_sweeps_match_plain_sweeps(case, prec, monkeypatch):
     two kernels, so single ulps can differ and then spread)."""
     spec, vc, f = _tma_cases()[case]
     out, names = {}, {}
+    monkeypatch.setenv("PLUTO_GB300_SWEEP", "tile")  # y/z tiles, not the marching columns
     for tma in ("1", "1b", "0"):
         monkeypatch.setenv("PLUTO_GB300_SWEEP_TMA", tma[0])
         s = _s(spec, prec)
@@ -79,6 +80,36 @@ def test_tma_sweeps_match_plain_sweeps(case, prec, monkeypatch):
         if out["0"][1][d] is not None:
             assert np.array_equal(out["1"][1][d], out["1b"][1][d])
             errs[f"b{d}"] = rel_l1(out["1"][1][d], out["0"][1][d])
+    assert max(errs.values()) <= 1e-6, errs
+
+
+@pytest.mark.parametrize("prec", MIXED)
+@pytest.mark.parametrize("case", ["blast3d_plm_ct", "turb3d_ppm_rk3", "ot2d_roe_minmod",
+                                  "blast3d_noct_hll_outflow"])
+@pytest.mark.parametrize("seg", ["0", "5"])
+def test_marching_sweeps_match_tile_sweeps(case, prec, seg, monkeypatch):
+    """The y/z sweeps that march along columns (the default) compute what the
+    TMA tiles compute, to FP32 round-off, deterministically, for any segment
+    length (5: segments that do not divide the grid)."""
+    spec, vc, f = _tma_cases()[case]
+    out, names = {}, {}
+    monkeypatch.setenv("PLUTO_GB300_MARCH_SEG", seg)
+    for mode in ("march", "march_b", "tile"):
+        monkeypatch.setenv("PLUTO_GB300_SWEEP", mode.split("_")[0])
+        s = _s(spec, prec)
+        s.upload(vc, f)
+        names[mode] = set(s.profile_kernels(1, spec["first_dt"], spec["cfl"]))
+        s.upload(vc, f)
+        s.run(6, spec["first_dt"], spec["cfl"])
+        out[mode] = s.download()
+    assert "mixed_sweep_y_march" in names["march"] and "mixed_sweep_y_march" not in names["tile"], names
+    assert all(np.array_equal(out["march"][0][q], out["march_b"][0][q]) for q in range(8))
+    errs = {q: rel_l1(out["march"][0][q], out["tile"][0][q]) for q in range(8)
+            if np.abs(out["tile"][0][q]).sum() > 0}
+    for d in range(3):
+        if out["tile"][1][d] is not None:
+            assert np.array_equal(out["march"][1][d], out["march_b"][1][d])
+            errs[f"b{d}"] = rel_l1(out["march"][1][d], out["tile"][1][d])
     assert max(errs.values()) <= 1e-6, errs
 
 
@@ -190,6 +221,7 @@ def test_padded_rows_match_unpadded(case, prec, monkeypatch):
     mixed bar of the FP64 path."""
     spec, vc, f = _padded_cases()[case]
     out, names = {}, {}
+    monkeypatch.setenv("PLUTO_GB300_SWEEP", "tile")  # y/z tiles, not the marching columns
     for tma in ("1", "0"):
         monkeypatch.setenv("PLUTO_GB300_SWEEP_TMA", tma)
         s = _s(spec, prec)
