@@ -664,24 +664,30 @@ __global__ void __launch_bounds__(32 * kTY, 2)
 // ---------------------------------------------------------------------------
 // y/z sweep marching along DIR: a thread walks one column segment of `seg`
 // cells, keeping the stencil planes, the left state of the interface above
-// and the flux of the interface below in registers.  No shared memory and no
-// halo rows: a segment reconstructs one extra cell and solves one extra
-// Riemann problem at its start.  A warp covers 32 consecutive x, so every
-// load and store is a whole 128-byte row; the next stencil plane is loaded
-// one cell ahead.  Same arithmetic, per cell, as k_msweep_t.
+// and the flux of the interface below in registers.  No halo rows: a
+// segment reconstructs one extra cell and solves one extra Riemann problem
+// at its start.  A warp covers 32 consecutive x, so every load and store is
+// a whole 128-byte row.  What a cell needs from memory (the next stencil
+// plane, its accumulated update, C_dt and normal face field) is copied
+// asynchronously into a per-thread shared-memory slot one cell ahead, so no
+// registers wait on it.  Same arithmetic, per cell, as k_msweep_t.
 // ---------------------------------------------------------------------------
 // resident blocks of k_msweep_m: PPM's five stencil planes need the
 // registers of 3 blocks per SM (170 per thread), PLM fits 4 (128)
 __host__ __device__ constexpr int march_min_blocks(int rs) { return rs == RS_PPM ? 3 : 4; }
+constexpr int kMarchThreads = 128;
 
 template <int RS, int DIR, bool CT>
-__global__ void __launch_bounds__(128, march_min_blocks(RS))
+__global__ void __launch_bounds__(kMarchThreads, march_min_blocks(RS))
     k_msweep_m(MixArgs a, int solver, int i_lo, int i_n, int o_lo, int o_n, int seg, int nseg, int stage1) {
   constexpr int REACH = rs_ghost_reach(RS);
   constexpr int NP = 2 * REACH + 1;  // stencil planes of one cell
+  // staged per cell: the next plane (NV), dU (NV), C_dt, the face field
+  constexpr int NS = 2 * NV + 2, S_PL = 0, S_DU = NV, S_CDT = 2 * NV, S_BN = 2 * NV + 1;
+  __shared__ float sbuf[2][NS][kMarchThreads];
   const Geom& g = a.g;
-  const int lane = threadIdx.x & 31;
-  const long long wi = (blockIdx.x * (long long)blockDim.x + threadIdx.x) >> 5;
+  const int tid = threadIdx.x, lane = tid & 31;
+  const long long wi = (blockIdx.x * (long long)blockDim.x + tid) >> 5;
   const int nbx = (i_n + 31) >> 5;
   const int bx = (int)(wi % nbx);
   const long long rest = wi / nbx;
@@ -697,38 +703,6 @@ __global__ void __launch_bounds__(128, march_min_blocks(RS))
   const float scrh = a.sc->dtdx[DIR];
   const float idx = a.inv_dx_f[DIR];
   constexpr int VN = Rot<DIR>::vn;
-  // planes pl[t] = V at m - REACH + t for the cell m being reconstructed next
-  float pl[NP][NV], nxt[NV];
-#pragma unroll
-  for (int t = 0; t < NP; t++)
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) pl[t][nv] = ldg(a.Vin[nv], cb + (m0 - 1 - REACH + t) * s);
-#pragma unroll
-  for (int nv = 0; nv < NV; nv++) nxt[nv] = ldg(a.Vin[nv], cb + (m0 + REACH) * s);
-  auto reconstruct = [&](float* vp, float* vm) {
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++)
-      recon<RS>(a.limiter, nv, RS == RS_PPM ? pl[0][nv] : 0.f, pl[REACH - 1][nv], pl[REACH][nv],
-                pl[REACH + 1][nv], RS == RS_PPM ? pl[NP - 1][nv] : 0.f, vp[nv], vm[nv]);
-  };
-  auto advance_planes = [&](int m_next) {  // planes of cell m_next from those of m_next - 1
-#pragma unroll
-    for (int t = 0; t + 1 < NP; t++)
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) pl[t][nv] = pl[t + 1][nv];
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) pl[NP - 1][nv] = nxt[nv];
-    // the plane after, for the following cell (inside the ghost layers)
-    if (m_next + REACH + 1 <= end + 1 + REACH) {
-#pragma unroll
-      for (int nv = 0; nv < NV; nv++) nxt[nv] = ldg(a.Vin[nv], cb + (m_next + REACH + 1) * s);
-    }
-  };
-  auto store_dv = [&](long long c, const float* vp, const float* vm) {
-#pragma unroll
-    for (int comp = 0; comp < 3; comp++)
-      if (comp < g.dims) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
-  };
   // The interface two segments share (m0-1/2) is solved by the loop body in
   // both, the only inlined copy of the Riemann solver (two copies may
   // contract multiply-adds differently), from the same inputs: its flux is
@@ -739,6 +713,43 @@ __global__ void __launch_bounds__(128, march_min_blocks(RS))
   // earlier: iteration m0-2 reconstructs cell m0-1 and its Riemann problem,
   // which has no left state, is discarded.
   constexpr bool kPre = RS != RS_PPM;
+  const int mstart = kPre ? m0 - 1 : m0 - 2;
+  // planes pl[t] = V at m - REACH + t for the cell m being reconstructed next
+  float pl[NP][NV];
+#pragma unroll
+  for (int t = 0; t < NP; t++)
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) pl[t][nv] = ldg(a.Vin[nv], cb + (m0 - 1 - REACH + t) * s);
+  // the copies iteration m reads: the plane of cell m+1's stencil top (not
+  // in the discarded iteration, whose planes are already in place), dU and
+  // C_dt of cell m when it is updated, the face field of interface m+1/2
+  auto stage = [&](int b, int m) {
+    const long long c = cb + m * s;
+    const bool first = !kPre && m < m0 - 1, upd = m >= m0;
+    if (!first) {
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) cp_async4(&sbuf[b][S_PL + nv][tid], a.Vin[nv] + c + (1 + REACH) * s);
+      if (CT) cp_async4(&sbuf[b][S_BN][tid], a.Bin[DIR] + c);
+    }
+    if (upd) {
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++)
+        if ((a.accmask >> nv) & 1) cp_async4(&sbuf[b][S_DU + nv][tid], a.dU[nv] + c);
+      if (stage1) cp_async4(&sbuf[b][S_CDT][tid], a.CDT + c);
+    }
+    cp_async_commit();
+  };
+  auto reconstruct = [&](float* vp, float* vm) {
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++)
+      recon<RS>(a.limiter, nv, RS == RS_PPM ? pl[0][nv] : 0.f, pl[REACH - 1][nv], pl[REACH][nv],
+                pl[REACH + 1][nv], RS == RS_PPM ? pl[NP - 1][nv] : 0.f, vp[nv], vm[nv]);
+  };
+  auto store_dv = [&](long long c, const float* vp, const float* vm) {
+#pragma unroll
+    for (int comp = 0; comp < 3; comp++)
+      if (comp < g.dims) a.DV[DIR][comp][c] = vp[VX1 + comp] - vm[VX1 + comp];
+  };
   float vpC[NV], vmC[NV], fp[NV], pp = 0.f, cmp = 0.f;
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) vpC[nv] = vmC[nv] = fp[nv] = 0.f;
@@ -748,20 +759,28 @@ __global__ void __launch_bounds__(128, march_min_blocks(RS))
     vpC[RHO] = 1.f;  // a harmless left state for the discarded problem
     vpC[PRS] = 1.f;
   }
+  stage(0, mstart);
   // cell m+1 reconstructed, interface m+1/2 solved, cell m updated
-  for (int m = kPre ? m0 - 1 : m0 - 2; m <= m1; m++) {
+  for (int m = mstart, it = 0; m <= m1; m++, it++) {
+    const int b = it & 1;
+    if (m < m1) stage(b ^ 1, m + 1);  // buffer b^1 was read in the previous iteration
+    else cp_async_commit();           // (an empty group keeps the count)
+    cp_async_wait<1>();               // this iteration's copies have landed
     const long long c = cb + m * s;
     const bool upd = m >= m0;
-    float du[NV], cdt = 0.f;
-#pragma unroll
-    for (int nv = 0; nv < NV; nv++) du[nv] = (upd && ((a.accmask >> nv) & 1)) ? a.dU[nv][c] : 0.f;
-    if (upd && stage1) cdt = a.CDT[c];
-    const bool first = !kPre && m < m0 - 1;  // the discarded problem
+    const bool first = !kPre && m < m0 - 1;          // the discarded problem
     const bool side = upd || (!first && m0 == beg);  // cell m0-1 and its interface: the first segment's
-    const float bn = (CT && !first) ? a.Bin[DIR][c] : 0.f;
+    const float bn = (CT && !first) ? sbuf[b][S_BN][tid] : 0.f;
     if (CT && side) store_dv(c, vpC, vmC);
     float vpN[NV], vmN[NV];
-    if (!first) advance_planes(m + 1);  // the planes start at cell m0-1
+    if (!first) {  // the planes of cell m+1
+#pragma unroll
+      for (int t = 0; t + 1 < NP; t++)
+#pragma unroll
+        for (int nv = 0; nv < NV; nv++) pl[t][nv] = pl[t + 1][nv];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) pl[NP - 1][nv] = sbuf[b][S_PL + nv][tid];
+    }
     reconstruct(vpN, vmN);
     Iface<float> f;
     solve_iface<DIR, CT>(a, solver, vpC, vmN, bn, f);
@@ -775,9 +794,9 @@ __global__ void __launch_bounds__(128, march_min_blocks(RS))
         if (!((a.accmask >> nv) & 1)) continue;
         float rhs = -scrh * (f.f[nv] - fp[nv]);
         if (nv == VN) rhs -= scrh * (f.press - pp);
-        a.dU[nv][c] = du[nv] + rhs;
+        a.dU[nv][c] = sbuf[b][S_DU + nv][tid] + rhs;
       }
-      if (stage1) a.CDT[c] = cdt + 0.5f * (cmp + f.cmax) * idx;
+      if (stage1) a.CDT[c] = sbuf[b][S_CDT][tid] + 0.5f * (cmp + f.cmax) * idx;
     }
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) {
@@ -788,6 +807,7 @@ __global__ void __launch_bounds__(128, march_min_blocks(RS))
     pp = f.press;
     cmp = f.cmax;
   }
+  cp_async_wait<0>();  // nothing left in flight when the thread exits
   if (CT && m1 == end) store_dv(cb + (end + 1) * s, vpC, vmC);
 }
 
@@ -1512,10 +1532,10 @@ static void mlaunch_sweeps_rs(Solver* S, const MixArgs& a, int stage) {
       const int nseg = (g.nx[dir] + seg - 1) / seg;
       const long long threads = 32LL * wcols * nseg;
       if (dir == 1)
-        PG_LAUNCH(S, "mixed_sweep_y_march", (k_msweep_m<RS, 1, CT><<<grid_for(threads, 128), 128, 0, st>>>(
+        PG_LAUNCH(S, "mixed_sweep_y_march", (k_msweep_m<RS, 1, CT><<<grid_for(threads, kMarchThreads), kMarchThreads, 0, st>>>(
                                                 a, solver, i_lo, i_n, o_lo, o_n, seg, nseg, stage1)));
       else
-        PG_LAUNCH(S, "mixed_sweep_z_march", (k_msweep_m<RS, 2, CT><<<grid_for(threads, 128), 128, 0, st>>>(
+        PG_LAUNCH(S, "mixed_sweep_z_march", (k_msweep_m<RS, 2, CT><<<grid_for(threads, kMarchThreads), kMarchThreads, 0, st>>>(
                                                 a, solver, i_lo, i_n, o_lo, o_n, seg, nseg, stage1)));
       continue;
     }
