@@ -202,6 +202,11 @@ template <> struct Acc<double> {
   static __device__ __forceinline__ T avg2(float x, float y) { return fma(0.5, widen(x), widen_half(y)); }
   // RK2 corrector (u0 + u + d) / 2 with one FMA after the sum
   static __device__ __forceinline__ T half_sum3(T u0, T u, float d) { return fma(0.5, u0 + u, widen_half(d)); }
+  // u0 + (d0 + d1) / 2 with the two floats summed exactly (their exponents
+  // within 29 of each other; else one rounding) and one FMA
+  static __device__ __forceinline__ T add_half_sum(T u0, float d0, float d1) {
+    return fma(0.5, widen(d0) + widen(d1), u0);
+  }
   // element q of a resident accumulator array
   static __device__ __forceinline__ T ld(const void* p, long long q) { return ((const double*)p)[q]; }
   static __device__ __forceinline__ void st(void* p, long long q, T v) { ((double*)p)[q] = v; }
@@ -242,6 +247,9 @@ template <> struct Acc<dw> {
   static __device__ __forceinline__ T konst(double, float hi, float lo) { return {hi, lo}; }
   static __device__ __forceinline__ T avg2(float x, float y) { return (dw{x, 0.f} + y) * 0.5f; }
   static __device__ __forceinline__ T half_sum3(T u0, T u, float d) { return ((u + d) + u0) * 0.5f; }
+  static __device__ __forceinline__ T add_half_sum(T u0, float d0, float d1) {
+    return u0 + two_sum(d0, d1) * 0.5f;
+  }
   static __device__ __forceinline__ T ld(const void* p, long long q) {
     const float2 f = ((const float2*)p)[q];
     return {f.x, f.y};

@@ -36,6 +36,9 @@ struct MixBufs {
   float* V[2][8];
   float* Bs[2][3];
   float* dU[8];
+  // RK2: the stage-2 increments, so that the stage-1 ones stay for the
+  // corrector U0 + (dU0 + dU1)/2 (null for EULER and RK3)
+  float* dU1[8];
   float* S[3][2];
   float* DV[3][3];
   float* E[3];
@@ -57,6 +60,7 @@ struct MixArgs {
   const float* B0[3];
   float* Bout[3];
   float* dU[8];
+  const float* dUp[8];  // RK2 stage 2: the stage-1 increments
   float* S[3][2];
   float* DV[3][3];
   float* E[3];
@@ -517,6 +521,7 @@ __global__ void __launch_bounds__(32 * kTY, 2) k_msweep_t(MixArgs a, int solver,
 // ---------------------------------------------------------------------------
 struct SweepMaps {
   CUtensorMap V, dU, CDT, B;
+  CUtensorMap dU1;  // the RK2 stage-2 increments (a copy of dU without them)
 };
 
 template <int RS>
@@ -532,8 +537,9 @@ struct SweepTile {
 template <int RS, int DIR, bool CT>
 __global__ void __launch_bounds__(32 * kTY, 2)
     k_msweep_tma(const __grid_constant__ SweepMaps maps, MixArgs a, int solver, int xa, int i_lo, int i_n, int o_lo,
-                 int nbx, int ncols, int ntiles, int stage1) {
+                 int nbx, int ncols, int ntiles, int stage1, int dsel) {
   using TL = SweepTile<RS>;
+  const CUtensorMap* du_map = dsel ? &maps.dU1 : &maps.dU;  // the array a.dU points to
   constexpr int REACH = TL::REACH, R = TL::R, NU = TL::NU, NF = TL::NF, BUF = TL::BUF;
   extern __shared__ __align__(128) float smem[];
   float* svm = smem + 2 * BUF;        // [NV][kTY][32]
@@ -560,12 +566,12 @@ __global__ void __launch_bounds__(32 * kTY, 2)
     mbar_arrive_expect_tx(&bar[b], tx_bytes);
     if (DIR == 1) {
       tma_load_4d(base, &maps.V, x0, m0 - 1 - REACH, other, 0, &bar[b]);
-      tma_load_4d(base + 8 * R * 32, &maps.dU, x0, m0, other, 0, &bar[b]);
+      tma_load_4d(base + 8 * R * 32, du_map, x0, m0, other, 0, &bar[b]);
       if (stage1) tma_load_3d(base + (8 * R + 8 * NU) * 32, &maps.CDT, x0, m0, other, &bar[b]);
       if (CT) tma_load_3d(base + (8 * R + 9 * NU) * 32, &maps.B, x0, m0 - 1, other, &bar[b]);
     } else {
       tma_load_4d(base, &maps.V, x0, other, m0 - 1 - REACH, 0, &bar[b]);
-      tma_load_4d(base + 8 * R * 32, &maps.dU, x0, other, m0, 0, &bar[b]);
+      tma_load_4d(base + 8 * R * 32, du_map, x0, other, m0, 0, &bar[b]);
       if (stage1) tma_load_3d(base + (8 * R + 8 * NU) * 32, &maps.CDT, x0, other, m0, &bar[b]);
       if (CT) tma_load_3d(base + (8 * R + 9 * NU) * 32, &maps.B, x0, other, m0 - 1, &bar[b]);
     }
@@ -959,9 +965,16 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
     const T inv_gmm1 = O::konst(a.inv_gmm1_d, a.inv_gmm1_hi, a.inv_gmm1_lo);
     const long long n = g.ncell;
     const int msk = a.accmask;
-    // the resident accumulators: U of the previous stage (stage 1: of the
-    // step start); the cell field under CT comes from the faces below
-    const void* Uin = STAGE == 1 ? a.U0 : a.Us;
+    // RK2 corrector (U0 + U1 + dU1)/2 with U1 = U0 + dU0: U0 + (dU0 + dU1)/2,
+    // the FP32 increments summed before the one FP64 addition.  Where stage
+    // 1 hit a floor, U1 is not U0 + dU0: that zone's U1 was stored and the
+    // corrector takes it as written.
+    const bool rk2c = STAGE == 2 && NSTAGE == 2;
+    const bool floored1 = rk2c && (a.flag[c] & FLAG_CONS2PRIM_FAIL);
+    // the resident accumulators: U of the previous stage (stage 1 and the
+    // RK2 corrector: of the step start); the cell field under CT comes from
+    // the faces below
+    const void* Uin = (STAGE == 1 || (rk2c && !floored1)) ? a.U0 : a.Us;
     ConsA<A> u;
     u.rho = O::ld(Uin, RHO * n + c);
     u.E = O::ld(Uin, ENG * n + c);
@@ -975,10 +988,22 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
     float du[NV];
 #pragma unroll
     for (int nv = 0; nv < NV; nv++) du[nv] = (msk & (1 << nv)) ? a.dU[nv][c] : 0.f;
-    if (a.intb && (a.flag[c] & PG_FLAG_INTERNAL_BOUNDARY))  // Src/int_bound_reset.c:33-37
+    const bool frozen = a.intb && (a.flag[c] & PG_FLAG_INTERNAL_BOUNDARY);  // Src/int_bound_reset.c:33-37
+    if (frozen)
 #pragma unroll
       for (int nv = 0; nv < NV; nv++) du[nv] = 0.f;
-    if (STAGE == 2 && NSTAGE == 2) {  // (U0 + U1 + dU) / 2
+    if (rk2c && !floored1) {  // U0 + (dU0 + dU1)/2, the increments summed in A
+      float dp[NV];
+#pragma unroll
+      for (int nv = 0; nv < NV; nv++) dp[nv] = ((msk & (1 << nv)) && !frozen) ? a.dUp[nv][c] : 0.f;
+      if (msk & (1 << RHO)) u.rho = O::add_half_sum(u.rho, dp[RHO], du[RHO]);
+#pragma unroll
+      for (int d = 0; d < 3; d++) {
+        if (msk & (1 << (VX1 + d))) u.m[d] = O::add_half_sum(u.m[d], dp[VX1 + d], du[VX1 + d]);
+        if (msk & (1 << (BX1 + d))) u.b[d] = O::add_half_sum(u.b[d], dp[BX1 + d], du[BX1 + d]);
+      }
+      if (msk & (1 << ENG)) u.E = O::add_half_sum(u.E, dp[ENG], du[ENG]);
+    } else if (rk2c) {  // (U0 + U1 + dU1) / 2 with the stored U1
       const T u0rho = O::ld(a.U0, RHO * n + c), u0E = O::ld(a.U0, ENG * n + c);
       u.rho = O::half_sum3(u0rho, u.rho, du[RHO]);
       u.E = O::half_sum3(u0E, u.E, du[ENG]);
@@ -1056,14 +1081,18 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
       u.E = O::add(O::mulf(inv_gmm1, (float)a.small_p), O::mulf(kin2, 0.5f));
       fl = FLAG_CONS2PRIM_FAIL;
     }
-    // the accumulators of the next stage (the last stage: of the next step)
+    // the accumulators of the next stage (the last stage: of the next step);
+    // RK2's stage 1 stores its result only where a floor changed it (the
+    // corrector rebuilds the others from U0 and the increments)
     void* Uout = STAGE == NSTAGE ? a.U0 : a.Us;
-    O::st(Uout, RHO * n + c, u.rho);
-    O::st(Uout, ENG * n + c, u.E);
+    if (!(NSTAGE == 2 && STAGE == 1) || fl) {
+      O::st(Uout, RHO * n + c, u.rho);
+      O::st(Uout, ENG * n + c, u.E);
 #pragma unroll
-    for (int d = 0; d < 3; d++) {
-      O::st(Uout, (VX1 + d) * n + c, u.m[d]);
-      if (msk & (1 << (BX1 + d))) O::st(Uout, (BX1 + d) * n + c, u.b[d]);
+      for (int d = 0; d < 3; d++) {
+        O::st(Uout, (VX1 + d) * n + c, u.m[d]);
+        if (msk & (1 << (BX1 + d))) O::st(Uout, (BX1 + d) * n + c, u.b[d]);
+      }
     }
     float out[NV] = {rho_f, vel[0], vel[1], vel[2], O::tof(u.b[0]), O::tof(u.b[1]), O::tof(u.b[2]), p};
 #pragma unroll
@@ -1253,6 +1282,8 @@ static bool mixed_prepare_tma_rs(Solver* S, MixedState* M) {
       const uint32_t bf[3] = {32, box(TL::NF, 1), box(TL::NF, 2)};
       if (!encode_f32_map(&m.V, M->b.V[sb][0], 4, d4, s4, bv)) return false;
       if (!encode_f32_map(&m.dU, M->b.dU[0], 4, d4, s4, bu)) return false;
+      if (M->b.dU1[0] ? !encode_f32_map(&m.dU1, M->b.dU1[0], 4, d4, s4, bu) : false) return false;
+      if (!M->b.dU1[0]) m.dU1 = m.dU;
       if (!encode_f32_map(&m.CDT, M->b.CDT, 3, d4, s4, bc)) return false;
       if (CT && !encode_f32_map(&m.B, M->b.Bs[sb][dir], 3, d4, s4, bf)) return false;
       if (!CT) m.B = m.CDT;  // unused
@@ -1308,6 +1339,7 @@ int mixed_alloc(Solver* S) {
   for (int s = 0; s < 2; s++)
     if (al8(M->b.V[s])) return PG_ERR_NOMEM;
   if (al8(M->b.dU)) return PG_ERR_NOMEM;
+  if (S->cfg.time_stepping == PG_RK2 && al8(M->b.dU1)) return PG_ERR_NOMEM;
   if (al(&M->b.CDT)) return PG_ERR_NOMEM;
   if (ct) {
     for (int d = 0; d < S->g.dims; d++) {
@@ -1358,6 +1390,7 @@ void mixed_free(Solver* S) {
   };
   for (int s = 0; s < 2; s++) f(M->b.V[s][0]);  // blocks of 8 arrays
   f(M->b.dU[0]);
+  f(M->b.dU1[0]);
   f(M->b.CDT);
   f(M->b.flag);
   f(M->b.U[0]);
@@ -1551,12 +1584,13 @@ static void mlaunch_sweeps_rs(Solver* S, const MixArgs& a, int stage) {
       if (cudaGetDevice(&dv) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dv);
       const int grid = ntiles < 2 * nsm ? ntiles : 2 * nsm;
       dim3 block(32, kTY);
+      const int dsel = a.dU[0] == M->b.dU1[0] ? 1 : 0;
       if (dir == 1)
         PG_LAUNCH(S, "mixed_sweep_y_tma", (k_msweep_tma<RS, 1, CT><<<grid, block, TL::SMEM, st>>>(
-                                          maps, a, solver, xa, i_lo, i_n, o_lo, nbt, ncols, ntiles, stage1)));
+                                          maps, a, solver, xa, i_lo, i_n, o_lo, nbt, ncols, ntiles, stage1, dsel)));
       else
         PG_LAUNCH(S, "mixed_sweep_z_tma", (k_msweep_tma<RS, 2, CT><<<grid, block, TL::SMEM, st>>>(
-                                          maps, a, solver, xa, i_lo, i_n, o_lo, nbt, ncols, ntiles, stage1)));
+                                          maps, a, solver, xa, i_lo, i_n, o_lo, nbt, ncols, ntiles, stage1, dsel)));
       continue;
     }
     int nbx = (i_n + 31) / 32;
@@ -1626,8 +1660,13 @@ static void menqueue(Solver* S) {
   if (NSTAGE == 1) {
     PG_LAUNCH(S, "mixed_end_step", (k_mend_step<<<1, 1, 0, S->stream>>>(a1)));
   } else if (NSTAGE == 2) {
-    // stage 2: B (+A) -> A
+    // stage 2: B (+A) -> A; its increments go to the second buffer, the
+    // corrector reads both
     MixArgs a2 = margs(S, bB, bA, bA);
+    for (int nv = 0; nv < 8; nv++) {
+      a2.dUp[nv] = M->b.dU[nv];
+      a2.dU[nv] = M->b.dU1[nv];
+    }
     mlaunch_bound(S, a2);
     if (ct) mlaunch_sweeps<true>(S, a2, 2); else mlaunch_sweeps<false>(S, a2, 2);
     mlaunch_tail<2, NSTAGE, A>(S, a2, dom);
