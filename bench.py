@@ -163,9 +163,11 @@ def kernel_bytes(name, n, stage_mix=True):
         "mixed_emf": (edges, 24 + 36 + 12 + 12 + 12),
         "mixed_face": (edges, 12 + 12 + 6 + 12),
         # resident FP64 accumulators: stage 1 reads U0 (5 x 8 B under CT), dU (5 x 4),
-        # the faces (3 x 4), C_dt, writes V (8 x 4), U (5 x 8), the flag -> 149 B;
-        # stage 2 also reads the stage result (40 B) -> 189 B; mean of the two
-        "mixed_final": (cells, 169),
+        # the faces (3 x 4), C_dt, writes V (8 x 4) and the flag -> 109 B (its
+        # conserved result is stored only where a floor changed it); the RK2
+        # corrector reads U0, both increments (2 x 5 x 4), the faces and the flag,
+        # writes V, U0 (5 x 8) and the flag -> 166 B; mean of the two
+        "mixed_final": (cells, 138),
     }
     if name not in per:
         return None
