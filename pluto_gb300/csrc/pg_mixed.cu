@@ -291,7 +291,10 @@ __global__ void __launch_bounds__(128) k_msweep_x(MixArgs a, int solver, int t_l
 // wide, starting on a 16-byte boundary) and normal face field of the next
 // tile are loaded by TMA into the other half of a double buffer.
 // ---------------------------------------------------------------------------
-constexpr int kXR = 8, kXC = 4, kXW = 136;
+// kXW covers the chunks' cells, a PPM stencil reach of 2 each side and up to
+// 3 floats of alignment: 30 (kXC - 1) + 32 + 4 + 3 = 99, rounded to 16 bytes.
+// kXC = 3 keeps the double buffer at 58 KB, so 3 blocks fit on an SM.
+constexpr int kXR = 8, kXC = 3, kXW = 100, kXBLK = 3;
 
 struct XSweepMaps {
   CUtensorMap V, B;
@@ -301,7 +304,7 @@ constexpr int kXBUF = (8 + 1) * kXR * kXW;                  // floats per buffer
 constexpr int kXSMEM = 2 * kXBUF * 4 + 16;
 
 template <int RS, bool CT>
-__global__ void __launch_bounds__(32 * kXR, 2)
+__global__ void __launch_bounds__(32 * kXR, kXBLK)
     k_msweep_x_tma(const __grid_constant__ XSweepMaps maps, MixArgs a, int solver, int t_lo, int t_n, int b_lo,
                    int nxt, int njt, int ntiles, int stage1) {
   constexpr int REACH = rs_ghost_reach(RS);
@@ -1534,7 +1537,7 @@ static void mlaunch_sweeps_rs(Solver* S, const MixArgs& a, int stage) {
     const int ntiles = nxt * njt * b_n;
     int nsm = 152, dv = 0;
     if (cudaGetDevice(&dv) == cudaSuccess) cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dv);
-    const int grid = ntiles < 2 * nsm ? ntiles : 2 * nsm;
+    const int grid = ntiles < kXBLK * nsm ? ntiles : kXBLK * nsm;
     const int sb = a.Vin[0] == M->b.V[0][0] ? 0 : 1;
     PG_LAUNCH(S, "mixed_sweep_x_tma", (k_msweep_x_tma<RS, CT><<<grid, 32 * kXR, kXSMEM, st>>>(
                                           M->xmaps[sb], a, solver, t_lo, t_n, b_lo, nxt, njt, ntiles, stage1)));
