@@ -770,6 +770,9 @@ __global__ void __launch_bounds__(kMarchThreads, march_min_blocks(RS))
   }
   stage(0, mstart);
   // cell m+1 reconstructed, interface m+1/2 solved, cell m updated
+  // not unrolled: a second inlined copy of the solver could solve the
+  // shared interface differently in the two segments
+#pragma unroll 1
   for (int m = mstart, it = 0; m <= m1; m++, it++) {
     const int b = it & 1;
     if (m < m1) stage(b ^ 1, m + 1);  // buffer b^1 was read in the previous iteration
