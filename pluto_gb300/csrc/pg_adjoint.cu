@@ -22,11 +22,11 @@
 //   k_adj_p2c      PrimToCons3D                (Src/mappers3D.c:74)
 // The local derivatives inside those kernels belong to exactly the branch
 // the forward evaluation takes, floors included.  The HLL / HLLD Riemann
-// outputs and the edge EMF are transposed by hand-derived reverse-mode
-// point functions (pg_adjoint_pt.cuh), all inputs in one evaluation; the
-// limiter, reconstruction, Roe solver and prim<->cons maps evaluate the same
-// templated point functions as the forward kernels with Dual<1> inputs, one
-// seeded input at a time.
+// outputs, the edge EMF, the PLM / PPM states and the prim<->cons maps are
+// transposed by hand-derived reverse-mode point functions
+// (pg_adjoint_pt.cuh), all inputs in one evaluation; the Roe solver
+// evaluates the same templated point function as the forward kernels with
+// Dual<1> inputs, one seeded input at a time.
 #include <cstring>
 #include <string>
 #include <utility>
@@ -187,51 +187,39 @@ __device__ __forceinline__ bool ct_face(const Geom& g, int fd, int i, int j, int
   int i, j, k;                                                    \
   cell_ijk(g, c, i, j, k);
 
-// lU = J_C(U)^T lambda_V (+ lUx), zero off the domain.  One thread per
-// (zone, seeded conserved component).
+// lU = J_C(U)^T lambda_V (+ lUx), zero off the domain.  One thread per zone.
 __global__ void k_adj_c2p(AdjArgs A, Tab8 Ust, Tab8 L, int add_ux) {
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const Geom& g = A.f.g;
-  if (q >= g.ncell * NV) return;
-  const long long c = q / NV;
-  const int kk = (int)(q % NV);
-  int i, j, k;
-  cell_ijk(g, c, i, j, k);
+  ADJ_CELL_PROLOGUE
   if (!in_dom(g, i, j, k)) {
-    A.b.lU[kk][c] = 0.0;
+#pragma unroll
+    for (int nv = 0; nv < NV; nv++) A.b.lU[nv][c] = 0.0;
     return;
   }
-  D1 u[NV], v[NV];
+  double u[NV], lv[NV], lu[NV];
 #pragma unroll
-  for (int nv = 0; nv < NV; nv++) u[nv] = D1(Ust.p[nv][c]);
-  u[kk].d[0] = 1.0;
-  unsigned char fl = 0;
-  cons_to_prim(u, v, D1(A.f.gamma - 1.0), D1(A.f.small_rho), D1(A.f.small_p), &fl);
-  double s = 0.0;
+  for (int nv = 0; nv < NV; nv++) {
+    u[nv] = Ust.p[nv][c];
+    lv[nv] = L.p[nv][c];
+  }
+  c2p_rev(u, A.f.gamma - 1.0, A.f.small_rho, lv, lu);
 #pragma unroll
-  for (int nv = 0; nv < NV; nv++) s += L.p[nv][c] * v[nv].d[0];
-  A.b.lU[kk][c] = s + (add_ux ? A.b.lUx[kk][c] : 0.0);
+  for (int nv = 0; nv < NV; nv++) A.b.lU[nv][c] = lu[nv] + (add_ux ? A.b.lUx[nv][c] : 0.0);
 }
 
-// lVin[dom] += J_P(V^n)^T lU0.  One thread per (zone, seeded primitive).
+// lVin[dom] += J_P(V^n)^T lU0.  One thread per zone.
 __global__ void k_adj_p2c(AdjArgs A) {
-  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  const Geom& g = A.f.g;
-  if (q >= g.ncell * NV) return;
-  const long long c = q / NV;
-  const int kk = (int)(q % NV);
-  int i, j, k;
-  cell_ijk(g, c, i, j, k);
+  ADJ_CELL_PROLOGUE
   if (!in_dom(g, i, j, k)) return;
-  D1 v[NV], u[NV];
+  double v[NV], au[NV], av[NV];
 #pragma unroll
-  for (int nv = 0; nv < NV; nv++) v[nv] = D1(A.b.Vn[nv][c]);
-  v[kk].d[0] = 1.0;
-  prim_to_cons(v, u, D1(A.f.gamma - 1.0));
-  double s = 0.0;
+  for (int nv = 0; nv < NV; nv++) {
+    v[nv] = A.b.Vn[nv][c];
+    au[nv] = A.b.lU0[nv][c];
+    av[nv] = 0.0;
+  }
+  p2c_rev(v, A.f.gamma - 1.0, au, av);
 #pragma unroll
-  for (int nv = 0; nv < NV; nv++) s += A.b.lU0[nv][c] * u[nv].d[0];
-  A.b.lVin[kk][c] += s;
+  for (int nv = 0; nv < NV; nv++) A.b.lVin[nv][c] += av[nv];
 }
 
 // Face average U[BX] = (B[f] + B[f-s]) / 2 on the domain, transposed.
@@ -495,7 +483,6 @@ __global__ void k_adj_recon(AdjArgs A, Box box) {
   const Geom& g = A.f.g;
   const long long c = cidx(g, k, j, i), s = g.s[DIR];
   const int recon = A.f.recon;
-  const int t0 = recon == PG_LINEAR ? 1 : 0, t1 = recon == PG_LINEAR ? 3 : 4;
   {
     const int nv = (int)(qq % NV);
     double lp = A.b.lVP[nv][c], lm = A.b.lVM[nv][c];
@@ -513,16 +500,13 @@ __global__ void k_adj_recon(AdjArgs A, Box box) {
         if (gw[t] != 0.0) atomicAdd(&A.b.lVin[nv][c + (t - 1) * s], gw[t]);
       return;
     }
-    double w[5] = {0.0, 0.0, 0.0, 0.0, 0.0};
-    for (int t = t0; t <= t1; t++) w[t] = A.f.V[nv][c + (t - 2) * s];
-    for (int t = t0; t <= t1; t++) {
-      D1 x[5], vp, vm;
-      for (int u = 0; u < 5; u++) x[u] = D1(w[u]);
-      x[t].d[0] = 1.0;
-      recon_pt(recon, A.f.limiter, nv, x, vp, vm);
-      const double gk = lp * vp.d[0] + lm * vm.d[0];
-      if (gk != 0.0) atomicAdd(&A.b.lVin[nv][c + (t - 2) * s], gk);
-    }
+    double w[5], gw[5];
+#pragma unroll
+    for (int t = 0; t < 5; t++) w[t] = A.f.V[nv][c + (t - 2) * s];
+    ppm_rev(w, lp, lm, gw);
+#pragma unroll
+    for (int t = 0; t < 5; t++)
+      if (gw[t] != 0.0) atomicAdd(&A.b.lVin[nv][c + (t - 2) * s], gw[t]);
   }
 }
 
@@ -989,7 +973,7 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
   const double w0 = 0.5, wc = 0.5;  // RK2 weights
   // ---- stage 2 reversed ----
   A.b = *B;
-  k_adj_c2p<<<grid_for(n * NV), kT, 0, st>>>(A, tab(B->U2, 8), tab(B->lV, 8), 0);
+  k_adj_c2p<<<grid_for(n), kT, 0, st>>>(A, tab(B->U2, 8), tab(B->lV, 8), 0);
   if (ct) {
     k_adj_avg<<<grid_for(n), kT, 0, st>>>(A, tab(B->lB, 3));
     k_adj_zero_bx<<<grid_for(n), kT, 0, st>>>(A);
@@ -1004,7 +988,7 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
   for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
   // ---- stage 1 reversed ----
   A.b = *B;
-  k_adj_c2p<<<grid_for(n * NV), kT, 0, st>>>(A, tab(B->U1, 8), tab(B->lV, 8), 1);
+  k_adj_c2p<<<grid_for(n), kT, 0, st>>>(A, tab(B->U1, 8), tab(B->lV, 8), 1);
   if (ct) {
     k_adj_avg<<<grid_for(n), kT, 0, st>>>(A, tab(B->lB, 3));
     k_adj_zero_bx<<<grid_for(n), kT, 0, st>>>(A);
@@ -1013,7 +997,7 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
   for (int nv = 0; nv < NV; nv++) dcopy(S->V[nv], B->Vn[nv], n, st);
   for (int d = 0; d < nb; d++) dcopy(S->Bs[d], B->Bn[d], n, st);
   rev_stage(S, A, ct);
-  k_adj_p2c<<<grid_for(n * NV), kT, 0, st>>>(A);
+  k_adj_p2c<<<grid_for(n), kT, 0, st>>>(A);
   for (int nv = 0; nv < NV; nv++) std::swap(B->lV[nv], B->lVin[nv]);
   for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
   // the solver's state is the step's start again

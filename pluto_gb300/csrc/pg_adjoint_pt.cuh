@@ -117,6 +117,41 @@ __host__ __device__ __forceinline__ void p2c_rev(const double* v, double gmm1, c
   av[PRS] += e / gmm1;
 }
 
+// cons_to_prim (Src/MHD/mappers.c:88-254) transposed, floors included: lu
+// = (dv/du)^T lv on the branch the forward takes.  A floored density is the
+// constant small_rho (the velocities and kinetic energy still depend on the
+// momenta through tau = 1/small_rho); a floored energy gives the pressure
+// small_p's value, independent of u, and so does a floored pressure.
+__host__ __device__ __forceinline__ void c2p_rev(const double* u, double gmm1, double small_rho, const double* lv,
+                                                 double* lu) {
+  const double m2 = u[MX1] * u[MX1] + u[MX1 + 1] * u[MX1 + 1] + u[MX1 + 2] * u[MX1 + 2];
+  const double b2 = u[BX1] * u[BX1] + u[BX2] * u[BX2] + u[BX3] * u[BX3];
+  const bool rho_fl = u[RHO] < 0.0;
+  const double tau = 1.0 / (rho_fl ? small_rho : u[RHO]);
+  const double kinb2 = 0.5 * (m2 * tau + b2);
+  const bool p_dep = !(u[ENG] < 0.0) && !(gmm1 * (u[ENG] - kinb2) < 0.0);
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) lu[nv] = 0.0;
+  double atau = 0.0;
+#pragma unroll
+  for (int i = 0; i < 3; i++) {  // v = m tau, B = B
+    lu[MX1 + i] = lv[VX1 + i] * tau;
+    atau += lv[VX1 + i] * u[MX1 + i];
+    lu[BX1 + i] = lv[BX1 + i];
+  }
+  if (p_dep) {  // p = (g-1) (E - (m2 tau + b2)/2)
+    const double akin = -gmm1 * lv[PRS];
+    lu[ENG] = gmm1 * lv[PRS];
+    atau += 0.5 * m2 * akin;
+#pragma unroll
+    for (int i = 0; i < 3; i++) {
+      lu[MX1 + i] += u[MX1 + i] * tau * akin;
+      lu[BX1 + i] += u[BX1 + i] * akin;
+    }
+  }
+  if (!rho_fl) lu[RHO] = lv[RHO] - tau * tau * atau;
+}
+
 // flux (Src/MHD/fluxes.c:110-249): a_v, a_u += J^T (a_f, a_ptot)
 template <int DIR>
 __host__ __device__ __forceinline__ void flux_rev(const double* v, const double* u, const double* af, double apt,
@@ -770,6 +805,65 @@ __host__ __device__ __forceinline__ void plm_rev(int lim, int nv, double w1, dou
   g[0] = -adv * pm;
   g[1] = lp + lm + adv * (pm - pp);
   g[2] = adv * pp;
+}
+
+// ppm_iface transposed: out = v0 + minmod(S - v0, vp1 - v0) with S the
+// four-point interface value; adds a_out's share into g[0..3] (the
+// adjoints on vm1, v0, vp1, vp2).
+__host__ __device__ __forceinline__ void ppm_iface_rev(double vm1, double v0, double vp1, double vp2, double a,
+                                                       double* g) {
+  const double w_1 = -1.0 / 12.0, w0 = 7.0 / 12.0, w1 = 7.0 / 12.0, w2 = -1.0 / 12.0;
+  const double S = w_1 * vm1 + w0 * v0 + w1 * vp1 + w2 * vp2;  // as ppm_iface
+  const double dv = vp1 - v0, dvp = S - v0;
+  g[1] += a;
+  if (!(dvp * dv > 0.0)) return;  // minmod: 0
+  if (::fabs(dvp) < ::fabs(dv)) {  // the interface value's slope: a_S
+    g[0] += w_1 * a;
+    g[1] += w0 * a - a;
+    g[2] += w1 * a;
+    g[3] += w2 * a;
+  } else {  // the one-sided difference vp1 - v0
+    g[2] += a;
+    g[1] -= a;
+  }
+}
+
+// PPM states of one zone transposed (recon_pt with PG_PARABOLIC, the
+// parabolic limiter of ppm_states.c:146-207 with cp = cm = 2): g[0..4] =
+// the adjoint on w[0..4] = v[c-2..c+2] from lp, lm on vp, vm.
+__host__ __device__ __forceinline__ void ppm_rev(const double* w, double lp, double lm, double* g) {
+#pragma unroll
+  for (int t = 0; t < 5; t++) g[t] = 0.0;
+  const double v0 = w[2];
+  double p = ppm_iface(w[1], v0, w[3], w[4]);
+  double m = ppm_iface(w[0], w[1], v0, w[3]);
+  const double cm = (3.0 + 1.0) / (3.0 - 1.0), cp = cm;
+  const double dvp = p - v0, dvm = m - v0;
+  // vp = v0 + dvp', vm = v0 + dvm' with (dvp', dvm') of the branch taken
+  g[2] += lp + lm;
+  double adp = 0.0, adm = 0.0;  // adjoints on dvp, dvm
+  if (dvp * dvm >= 0.0) {
+    // dvp' = dvm' = 0
+  } else if (::fabs(dvp) >= cm * ::fabs(dvm)) {  // dvp' = -cm dvm
+    adm = lm - cm * lp;
+  } else if (::fabs(dvm) >= cp * ::fabs(dvp)) {  // dvm' = -cp dvp
+    adp = lp - cp * lm;
+  } else {
+    adp = lp;
+    adm = lm;
+  }
+  g[2] -= adp + adm;  // dvp = p - v0, dvm = m - v0
+  double gp[4] = {0.0, 0.0, 0.0, 0.0}, gm[4] = {0.0, 0.0, 0.0, 0.0};
+  ppm_iface_rev(w[1], v0, w[3], w[4], adp, gp);  // p from w1, v0, w3, w4
+  ppm_iface_rev(w[0], w[1], v0, w[3], adm, gm);  // m from w0, w1, v0, w3
+  g[1] += gp[0];
+  g[2] += gp[1];
+  g[3] += gp[2];
+  g[4] += gp[3];
+  g[0] += gm[0];
+  g[1] += gm[1];
+  g[2] += gm[2];
+  g[3] += gm[3];
 }
 
 // mc_lim2 (Src/MHD/CT/ct_stag_slopes.c:92-105) transposed: a_dp, a_dm

@@ -7,8 +7,8 @@
 // region: L / R flux, single-star L / R, double-star L / R, the HLLC
 // reversion) and random output adjoints lam, it forms J^T lam once by the
 // reverse function and once column by column from 16 seeded Dual<1>
-// evaluations of riemann_pt, likewise for the 40-input edge EMF and the PLM
-// states, and prints one line per check with the sample count, the branch
+// evaluations of riemann_pt, likewise for the 40-input edge EMF, the PLM
+// and PPM states and the prim/cons maps (floors included), and prints one line per check with the sample count, the branch
 // counts and the largest relative difference.
 #include <cmath>
 #include <cstdint>
@@ -190,6 +190,90 @@ static double check_plm(int nsamp, long* branches) {
   return worst;
 }
 
+// PPM states (interface values with the minmod clip, parabolic limiter)
+// transposed; branches counted: limiter case (none / flat / vp clipped / vm
+// clipped)
+static double check_ppm(int nsamp, long* branches) {
+  double worst = 0.0;
+  for (int t = 0; t < nsamp; t++) {
+    double w[5];
+    for (int q = 0; q < 5; q++) w[q] = urange(-1.0, 1.0);
+    if (t % 3 == 0)  // smooth profiles: the unclipped and one-sided branches
+      for (int q = 0; q < 5; q++) w[q] = 0.2 * q + 0.05 * q * q * (t % 2 ? 1.0 : -1.0) + urange(0.0, 0.02);
+    const double lp = urange(-1.0, 1.0), lm = urange(-1.0, 1.0);
+    double g[5];
+    ppm_rev(w, lp, lm, g);
+    double diff = 0.0, scale = 0.0;
+    for (int kk = 0; kk < 5; kk++) {
+      D1 x[5], vp, vm;
+      for (int q = 0; q < 5; q++) x[q] = D1(w[q]);
+      x[kk].d[0] = 1.0;
+      recon_pt(PG_PARABOLIC, 0, 0, x, vp, vm);
+      const double ref = lp * vp.d[0] + lm * vm.d[0];
+      scale = fmax(scale, fabs(ref));
+      diff = fmax(diff, fabs(g[kk] - ref));
+    }
+    const double p = ppm_iface(w[1], w[2], w[3], w[4]) - w[2], m = ppm_iface(w[0], w[1], w[2], w[3]) - w[2];
+    branches[p * m >= 0.0 ? 0 : (::fabs(p) >= 2.0 * ::fabs(m) ? 1 : (::fabs(m) >= 2.0 * ::fabs(p) ? 2 : 3))]++;
+    const double rel = scale > 0.0 ? diff / scale : diff;
+    if (!(rel <= worst)) worst = rel;
+  }
+  return worst;
+}
+
+// prim->cons and cons->prim (with the density, energy and pressure floors)
+// transposed; branches counted: no floor / density / energy / pressure
+static double check_maps(int nsamp, long* branches) {
+  double worst = 0.0;
+  const double gamma = 5.0 / 3.0, gmm1 = gamma - 1.0, small_rho = 1e-12, small_p = 1e-12;
+  for (int t = 0; t < nsamp; t++) {
+    double v[NV], u[NV], lam[NV], g[NV];
+    for (int nv = 0; nv < NV; nv++) v[nv] = urange(-2.0, 2.0);
+    v[RHO] = urange(0.2, 5.0);
+    v[PRS] = urange(0.05, 5.0);
+    for (int nv = 0; nv < NV; nv++) lam[nv] = urange(-1.0, 1.0);
+    // prim -> cons
+    for (int nv = 0; nv < NV; nv++) g[nv] = 0.0;
+    p2c_rev(v, gmm1, lam, g);
+    double diff = 0.0, scale = 0.0;
+    for (int kk = 0; kk < NV; kk++) {
+      D1 x[NV], y[NV];
+      for (int q = 0; q < NV; q++) x[q] = D1(v[q]);
+      x[kk].d[0] = 1.0;
+      prim_to_cons(x, y, D1(gmm1));
+      double ref = 0.0;
+      for (int q = 0; q < NV; q++) ref += lam[q] * y[q].d[0];
+      scale = fmax(scale, fabs(ref));
+      diff = fmax(diff, fabs(g[kk] - ref));
+    }
+    // cons -> prim from a state that may need a floor
+    prim_to_cons(v, u, gmm1);
+    const int kind = t % 4;
+    if (kind == 1) u[RHO] = -urange(0.01, 1.0);
+    if (kind == 2) u[ENG] = -urange(0.01, 1.0);
+    if (kind == 3) u[ENG] = 0.5 * (u[MX1] * u[MX1] + u[MX1 + 1] * u[MX1 + 1] + u[MX1 + 2] * u[MX1 + 2]) / u[RHO] +
+                            0.5 * (u[BX1] * u[BX1] + u[BX2] * u[BX2] + u[BX3] * u[BX3]) - urange(0.01, 1.0);
+    c2p_rev(u, gmm1, small_rho, lam, g);
+    int fl_kind = 0;
+    for (int kk = 0; kk < NV; kk++) {
+      D1 x[NV], y[NV];
+      for (int q = 0; q < NV; q++) x[q] = D1(u[q]);
+      x[kk].d[0] = 1.0;
+      unsigned char fl = 0;
+      cons_to_prim(x, y, D1(gmm1), D1(small_rho), D1(small_p), &fl);
+      double ref = 0.0;
+      for (int q = 0; q < NV; q++) ref += lam[q] * y[q].d[0];
+      scale = fmax(scale, fabs(ref));
+      diff = fmax(diff, fabs(g[kk] - ref));
+      if (fl) fl_kind = kind;
+    }
+    branches[fl_kind]++;
+    const double rel = scale > 0.0 ? diff / scale : diff;
+    if (!(rel <= worst)) worst = rel;
+  }
+  return worst;
+}
+
 int main(int argc, char** argv) {
   const int nsamp = argc > 1 ? atoi(argv[1]) : 20000;
   const double gamma = 5.0 / 3.0;
@@ -210,5 +294,11 @@ int main(int argc, char** argv) {
   long bp[2] = {0, 0};
   const double wp = check_plm(nsamp, bp);
   printf("plm samples %d branches %ld %ld worst %.3e\n", nsamp, bp[0], bp[1], wp);
+  long bq[4] = {0, 0, 0, 0};
+  const double wq = check_ppm(nsamp, bq);
+  printf("ppm samples %d branches %ld %ld %ld %ld worst %.3e\n", nsamp, bq[0], bq[1], bq[2], bq[3], wq);
+  long bm[4] = {0, 0, 0, 0};
+  const double wm = check_maps(nsamp, bm);
+  printf("maps samples %d branches %ld %ld %ld %ld worst %.3e\n", nsamp, bm[0], bm[1], bm[2], bm[3], wm);
   return 0;
 }

@@ -1,5 +1,5 @@
 """Hand-derived reverse-mode point functions of the adjoint (HLL / HLLD
-Riemann outputs, edge EMF, PLM states) against forward-mode Dual<1> derivatives of the
+Riemann outputs, edge EMF, PLM and PPM states, prim/cons maps) against forward-mode Dual<1> derivatives of the
 same point functions, on the host: tests/adjoint_rev_check.cu is compiled by
 nvcc as a host program and run on seeded random states that visit every HLLD
 region (L / R flux, single-star L / R, double-star L / R, HLLC reversion L / R)
@@ -55,6 +55,20 @@ def test_plm_reverse_matches_dual(report):
     assert float(ln.split("worst")[1]) < TOL, ln
     branches = [int(x) for x in ln.split("branches")[1].split("worst")[0].split()]
     assert all(n > 0 for n in branches), ln
+
+
+def test_ppm_reverse_matches_dual(report):
+    (ln,) = _lines(report, "ppm")
+    assert float(ln.split("worst")[1]) < TOL, ln
+    branches = [int(x) for x in ln.split("branches")[1].split("worst")[0].split()]
+    assert all(n > 0 for n in branches), ln
+
+
+def test_prim_cons_maps_reverse_matches_dual(report):
+    (ln,) = _lines(report, "maps")
+    assert float(ln.split("worst")[1]) < TOL, ln
+    branches = [int(x) for x in ln.split("branches")[1].split("worst")[0].split()]
+    assert all(n > 0 for n in branches), ln  # no floor, density, energy and pressure floors
 
 
 def test_emf_reverse_matches_dual(report):
