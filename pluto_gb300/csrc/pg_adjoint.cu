@@ -28,6 +28,7 @@
 // evaluates the same templated point function as the forward kernels with
 // Dual<1> inputs, one seeded input at a time.
 #include <cstring>
+#include <initializer_list>
 #include <string>
 #include <utility>
 #include <vector>
@@ -145,11 +146,15 @@ struct AdjBufs {
   double* B1[3];
   double* U1[8];
   double* U2[8];
-  // reconstructed states of directions 1 and 2 (direction 0 uses the
-  // solver's VP/VM): under CT the EMF needs every direction's wave speeds
-  // first, and the states of each direction stay for its reversal
-  double* VPd[2][8];
-  double* VMd[2][8];
+  // what the forward recomputation produced in each stage s: the
+  // reconstructed states of each direction d, the wave speeds and the
+  // velocity slopes (under CT).  The stage reversals read them instead of
+  // reconstructing and solving every direction again.
+  double* sVP[2][3][8];
+  double* sVM[2][3][8];
+  double* sSL[2][3];
+  double* sSR[2][3];
+  double* sDV[2][3][3];
 };
 
 struct AdjArgs {
@@ -559,38 +564,81 @@ struct Checkpoints {
   std::vector<std::vector<void*>> slots;  // per slot: 8 cell arrays + the face arrays
 };
 
+// The adjoint buffers and the one device block their arrays live in, back
+// to back in the order of AdjBufs (S->adj points here; AdjBufs first).
+struct AdjState {
+  AdjBufs b;
+  double* block = nullptr;
+};
+
 static int adjoint_alloc(Solver* S, AdjBufs** out) {
   if (S->adj) {
     *out = (AdjBufs*)S->adj;
     return PG_OK;
   }
-  AdjBufs* B = new AdjBufs();
+  AdjState* A = new AdjState();
+  AdjBufs* B = &A->b;
   memset(B, 0, sizeof *B);
-  S->adj = B;
+  S->adj = A;
   *out = B;
-  const size_t bytes = sizeof(double) * S->g.ncell;
+  const long long n = S->g.ncell;
   double** p = (double**)B;
-  for (size_t q = 0; q < sizeof(AdjBufs) / sizeof(double*); q++) {
-    bool unused = false;  // the per-direction states of directions >= dims
-    for (int d = S->g.dims; d < 3; d++)
-      for (int nv = 0; nv < NV; nv++) unused |= &p[q] == &B->VPd[d - 1][nv] || &p[q] == &B->VMd[d - 1][nv];
-    if (unused) continue;
-    if (cudaMalloc(&p[q], bytes) != cudaSuccess) {
-      p[q] = nullptr;
-      return PG_ERR_NOMEM;
-    }
-    if (cudaMemset(p[q], 0, bytes) != cudaSuccess) return PG_ERR_CUDA;
+  const size_t np = sizeof(AdjBufs) / sizeof(double*);
+  // the per-stage arrays of directions >= dims (and, without CT, the wave
+  // speeds and slopes) are not needed
+  const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
+  std::vector<char> used(np, 1);
+  for (size_t q = 0; q < np; q++) {
+    bool unused = false;
+    for (int st = 0; st < 2; st++)
+      for (int d = 0; d < 3; d++) {
+        const bool dir_off = d >= S->g.dims;
+        for (int nv = 0; nv < NV; nv++)
+          unused |= dir_off && (&p[q] == &B->sVP[st][d][nv] || &p[q] == &B->sVM[st][d][nv]);
+        unused |= (dir_off || !ct) && (&p[q] == &B->sSL[st][d] || &p[q] == &B->sSR[st][d]);
+        for (int c = 0; c < 3; c++) unused |= (dir_off || c >= S->g.dims || !ct) && &p[q] == &B->sDV[st][d][c];
+      }
+    used[q] = !unused;
   }
+  size_t count = 0;
+  for (size_t q = 0; q < np; q++) count += used[q];
+  const size_t bytes = sizeof(double) * (size_t)n * count;
+  if (cudaMalloc(&A->block, bytes) != cudaSuccess) {
+    A->block = nullptr;
+    return PG_ERR_NOMEM;
+  }
+  if (cudaMemset(A->block, 0, bytes) != cudaSuccess) return PG_ERR_CUDA;
+  size_t k = 0;
+  for (size_t q = 0; q < np; q++)
+    if (used[q]) p[q] = A->block + (k++) * n;
   return PG_OK;
+}
+
+// Zeroes p[0..count) with one cudaMemsetAsync per run of arrays that lie
+// back to back in the block (the adjoint's groups are contiguous, also after
+// the lV/lVin swaps, which exchange whole groups).
+static void zero_arrays(std::initializer_list<double* const*> groups, const int* counts, long long n,
+                        cudaStream_t st) {
+  std::vector<double*> p;
+  int g = 0;
+  for (double* const* grp : groups) {
+    for (int i = 0; i < counts[g]; i++) p.push_back(grp[i]);
+    g++;
+  }
+  size_t i = 0;
+  while (i < p.size()) {
+    size_t j = i + 1;
+    while (j < p.size() && p[j] == p[j - 1] + n) j++;
+    cudaMemsetAsync(p[i], 0, (j - i) * (size_t)n * sizeof(double), st);
+    i = j;
+  }
 }
 
 void adjoint_free(Solver* S) {
   if (S->adj) {
-    AdjBufs* B = (AdjBufs*)S->adj;
-    double** p = (double**)B;
-    for (size_t q = 0; q < sizeof(AdjBufs) / sizeof(double*); q++)
-      if (p[q]) cudaFree(p[q]);
-    delete B;
+    AdjState* A = (AdjState*)S->adj;
+    if (A->block) cudaFree(A->block);
+    delete A;
     S->adj = nullptr;
   }
   if (S->ckpt) {
@@ -615,8 +663,32 @@ namespace {
 
 constexpr int kT = kThreads;
 
-void dcopy(double* dst, const double* src, long long n, cudaStream_t st) {
-  cudaMemcpyAsync(dst, src, n * sizeof(double), cudaMemcpyDeviceToDevice, st);
+// Up to 16 device arrays of n doubles copied in one launch (blockIdx.y:
+// the array).
+struct CopyTab {
+  double* dst[16];
+  const double* src[16];
+};
+__global__ void k_copy_arrays(CopyTab t, long long n) {
+  const long long i = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (i < n) t.dst[blockIdx.y][i] = t.src[blockIdx.y][i];
+}
+
+// dstV[0..nv) = srcV[..], dstB[0..nb) = srcB[..] (cell arrays, then faces)
+void copy_state(double* const* dstV, const double* const* srcV, int nv, double* const* dstB,
+                const double* const* srcB, int nb, long long n, cudaStream_t st) {
+  CopyTab t;
+  int k = 0;
+  for (int q = 0; q < nv; q++, k++) {
+    t.dst[k] = dstV[q];
+    t.src[k] = srcV[q];
+  }
+  for (int q = 0; q < nb; q++, k++) {
+    t.dst[k] = dstB[q];
+    t.src[k] = srcB[q];
+  }
+  if (k == 0) return;
+  k_copy_arrays<<<dim3(grid_for(n), (unsigned)k), kT, 0, st>>>(t, n);
 }
 
 Box dir_box(const Geom& g, int dir, int lo_off, int hi_off, bool ct) {
@@ -636,44 +708,38 @@ Box dir_box(const Geom& g, int dir, int lo_off, int hi_off, bool ct) {
   return b.prepare();
 }
 
-// Recompute the states and Riemann outputs along DIR from the solver's V/Bs.
-template <int DIR>
-void fwd_dir(Solver* S, const F64A<double>& f) {
-  const Geom& g = S->g;
-  cudaStream_t st = S->stream;
-  Box rb = dir_box(g, DIR, -1, 1, f.ct), ib = dir_box(g, DIR, -1, 0, f.ct);
-  k_recon<double, DIR><<<grid_for(rb.count()), kT, 0, st>>>(f, rb);
-  if (S->cfg.riemann == PG_HLL)
-    k_riemann<double, DIR, PG_HLL, false><<<grid_for(ib.count(), 128), 128, 0, st>>>(f, ib, 0);
-  else if (S->cfg.riemann == PG_ROE)
-    k_riemann<double, DIR, PG_ROE, false><<<grid_for(ib.count(), 128), 128, 0, st>>>(f, ib, 0);
-  else
-    k_riemann<double, DIR, PG_HLLD, false><<<grid_for(ib.count(), 128), 128, 0, st>>>(f, ib, 0);
-}
-
-// The arguments with direction d's reconstructed states (see AdjBufs::VPd).
-AdjArgs with_dir_states(const AdjArgs& A, int d) {
-  AdjArgs r = A;
-  if (d > 0)
-    for (int nv = 0; nv < NV; nv++) {
-      r.f.VP[nv] = A.b.VPd[d - 1][nv];
-      r.f.VM[nv] = A.b.VMd[d - 1][nv];
+// The forward arrays with stage s's saved outputs: the states of direction
+// d, the wave speeds and slopes of every direction (see AdjBufs::sVP).
+F64A<double> stage_args(const F64A<double>& f, const AdjBufs& b, int s, int d) {
+  F64A<double> r = f;
+  for (int nv = 0; nv < NV; nv++) {
+    r.VP[nv] = b.sVP[s][d][nv];
+    r.VM[nv] = b.sVM[s][d][nv];
+  }
+  if (f.ct)
+    for (int e = 0; e < f.g.dims; e++) {
+      r.SL[e] = b.sSL[s][e];
+      r.SR[e] = b.sSR[s][e];
+      for (int c = 0; c < f.g.dims; c++) r.DV[e][c] = b.sDV[s][e][c];
     }
   return r;
 }
+AdjArgs stage_adj(const AdjArgs& A, int s, int d) {
+  AdjArgs r = A;
+  r.f = stage_args(A.f, A.b, s, d);
+  return r;
+}
 
-// Direction DIR reversed; `recompute`: reconstruct its states and Riemann
-// outputs first (else they are in place from the CT pre-pass).
+// Direction DIR reversed; A carries the stage's saved states of DIR.
 template <int DIR>
-void rev_dir(Solver* S, const AdjArgs& A, bool recompute) {
+void rev_dir(Solver* S, const AdjArgs& A) {
   const Geom& g = S->g;
   cudaStream_t st = S->stream;
   const long long n = g.ncell;
   Box rb = dir_box(g, DIR, -1, 1, A.f.ct), ib = dir_box(g, DIR, -1, 0, A.f.ct);
-  if (recompute) fwd_dir<DIR>(S, A.f);  // states of this direction
-  for (int nv = 0; nv < NV; nv++) {
-    cudaMemsetAsync(A.b.lVP[nv], 0, n * sizeof(double), st);
-    cudaMemsetAsync(A.b.lVM[nv], 0, n * sizeof(double), st);
+  {
+    const int cnt[2] = {NV, NV};
+    zero_arrays({A.b.lVP, A.b.lVM}, cnt, n, st);
   }
   k_adj_flux<DIR><<<grid_for(ib.count()), kT, 0, st>>>(A, ib);
   if (S->cfg.riemann == PG_HLLD)
@@ -705,31 +771,22 @@ Tab8 tab(double* const* p, int n) {
 // adjoint on the faces after CT_Update; the solver's V/Bs hold the stage
 // input.  On exit lVin/lBin hold the adjoint on the stage input before its
 // boundary fill.  add_b0: stage 1 of RK2, where Bs0 copies Bs after the fill.
-void rev_stage(Solver* S, const AdjArgs& A, bool add_b0) {
+// stage: 0 or 1, whose saved states, wave speeds and slopes are read.
+void rev_stage(Solver* S, const AdjArgs& A, bool add_b0, int stage) {
   const Geom& g = S->g;
   cudaStream_t st = S->stream;
   const long long n = g.ncell;
   const bool ct = A.f.ct;
   const AdjBufs& b = A.b;
-  for (int nv = 0; nv < NV; nv++) cudaMemsetAsync(b.lVin[nv], 0, n * sizeof(double), st);
-  for (int d = 0; d < 3; d++) {
-    cudaMemsetAsync(b.lBin[d], 0, n * sizeof(double), st);
-    if (ct) {
-      cudaMemsetAsync(b.lS[d][0], 0, n * sizeof(double), st);
-      cudaMemsetAsync(b.lS[d][1], 0, n * sizeof(double), st);
-      cudaMemsetAsync(b.lE[d], 0, n * sizeof(double), st);
-      for (int q = 0; q < 3; q++) cudaMemsetAsync(b.lDV[d][q], 0, n * sizeof(double), st);
-    }
+  {
+    const int cnt[5] = {NV, 3, 6, 9, 3};
+    if (ct) zero_arrays({b.lVin, b.lBin, &b.lS[0][0], &b.lDV[0][0], b.lE}, cnt, n, st);
+    else zero_arrays({b.lVin, b.lBin}, cnt, n, st);
   }
-  fwd_bound(S, A.f);
-  const AdjArgs A0 = with_dir_states(A, 0), A1 = with_dir_states(A, 1), A2 = with_dir_states(A, 2);
+  fwd_bound(S, A.f);  // the stage input's ghosts, read by the reversed reconstruction
+  const AdjArgs A0 = stage_adj(A, stage, 0);
   if (ct) {
-    // states, wave speeds and velocity slopes of every direction (the EMF
-    // inputs), each direction's states kept for its reversal below
-    fwd_dir<0>(S, A0.f);
-    if (g.dims > 1) fwd_dir<1>(S, A1.f);
-    if (g.dims > 2) fwd_dir<2>(S, A2.f);
-    k_adj_ct<<<grid_for(n), kT, 0, st>>>(A, tab(b.lB, 3));
+    k_adj_ct<<<grid_for(n), kT, 0, st>>>(A0, tab(b.lB, 3));
     Box eb;
     for (int ax = 0; ax < 3; ax++) {
       if (ax < g.dims) {
@@ -740,11 +797,11 @@ void rev_stage(Solver* S, const AdjArgs& A, bool add_b0) {
       }
     }
     eb.prepare();
-    k_adj_emf<<<grid_for(eb.count() * (g.dims == 3 ? 3 : 1), 64), 64, 0, st>>>(A, eb);
+    k_adj_emf<<<grid_for(eb.count() * (g.dims == 3 ? 3 : 1), 64), 64, 0, st>>>(A0, eb);
   }
-  if (g.dims > 2) rev_dir<2>(S, A2, !ct);
-  if (g.dims > 1) rev_dir<1>(S, A1, !ct);
-  rev_dir<0>(S, A0, !ct);
+  if (g.dims > 2) rev_dir<2>(S, stage_adj(A, stage, 2));
+  if (g.dims > 1) rev_dir<1>(S, stage_adj(A, stage, 1));
+  rev_dir<0>(S, A0);
   if (add_b0)
     for (int d = 0; d < g.dims; d++) k_add<<<grid_for(n), kT, 0, st>>>(b.lBin[d], b.lB0[d], n);
   BoundTab t;
@@ -939,32 +996,30 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
   // ---- forward recomputation of the step, saving what the reverse needs ----
   S->sc_host->dt = dt;
   cudaMemcpyAsync(&S->sc->dt, &S->sc_host->dt, sizeof(double), cudaMemcpyHostToDevice, st);
-  for (int nv = 0; nv < NV; nv++) dcopy(B->Vn[nv], S->V[nv], n, st);
-  for (int d = 0; d < nb; d++) dcopy(B->Bn[d], S->Bs[d], n, st);
+  copy_state(B->Vn, S->V, NV, B->Bn, S->Bs, nb, n, st);
   Box dom;
   for (int ax = 0; ax < 3; ax++) {
     dom.lo[ax] = g.beg[ax];
     dom.hi[ax] = g.end[ax];
   }
   dom.prepare();
+  // each stage's sweeps write their states, wave speeds and slopes into
+  // that stage's own arrays (stage_args), which the reversal reads
   const F64A<double> f = make_args<double>(S);
   launch_bound<double>(S, f);
   k_begin_step<double><<<grid_for(n), kT, 0, st>>>(f, dom);
-  launch_sweep<double, 0>(S, f, 1);
-  if (g.dims > 1) launch_sweep<double, 1>(S, f, 1);
-  if (g.dims > 2) launch_sweep<double, 2>(S, f, 1);
-  launch_stage_tail<double, 1, 2>(S, f, dom);
-  for (int nv = 0; nv < NV; nv++) {
-    dcopy(B->V1[nv], S->V[nv], n, st);
-    dcopy(B->U1[nv], S->U[nv], n, st);
-  }
-  for (int d = 0; d < nb; d++) dcopy(B->B1[d], S->Bs[d], n, st);
+  launch_sweep<double, 0>(S, stage_args(f, *B, 0, 0), 1);
+  if (g.dims > 1) launch_sweep<double, 1>(S, stage_args(f, *B, 0, 1), 1);
+  if (g.dims > 2) launch_sweep<double, 2>(S, stage_args(f, *B, 0, 2), 1);
+  launch_stage_tail<double, 1, 2>(S, stage_args(f, *B, 0, 0), dom);
+  copy_state(B->V1, S->V, NV, B->B1, S->Bs, nb, n, st);
+  copy_state(B->U1, S->U, NV, nullptr, nullptr, 0, n, st);
   launch_bound<double>(S, f);
-  launch_sweep<double, 0>(S, f, 2);
-  if (g.dims > 1) launch_sweep<double, 1>(S, f, 2);
-  if (g.dims > 2) launch_sweep<double, 2>(S, f, 2);
-  launch_stage_tail<double, 2, 2>(S, f, dom);
-  for (int nv = 0; nv < NV; nv++) dcopy(B->U2[nv], S->U[nv], n, st);
+  launch_sweep<double, 0>(S, stage_args(f, *B, 1, 0), 2);
+  if (g.dims > 1) launch_sweep<double, 1>(S, stage_args(f, *B, 1, 1), 2);
+  if (g.dims > 2) launch_sweep<double, 2>(S, stage_args(f, *B, 1, 2), 2);
+  launch_stage_tail<double, 2, 2>(S, stage_args(f, *B, 1, 0), dom);
+  copy_state(B->U2, S->U, NV, nullptr, nullptr, 0, n, st);
 
   AdjArgs A;
   memset(&A, 0, sizeof A);
@@ -980,9 +1035,8 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
     k_adj_rk_faces<<<grid_for(n), kT, 0, st>>>(A, w0, wc);
   }
   k_adj_rk_cells<<<grid_for(n), kT, 0, st>>>(A, w0, wc);
-  for (int nv = 0; nv < NV; nv++) dcopy(S->V[nv], B->V1[nv], n, st);
-  for (int d = 0; d < nb; d++) dcopy(S->Bs[d], B->B1[d], n, st);
-  rev_stage(S, A, false);
+  copy_state(S->V, B->V1, NV, S->Bs, B->B1, nb, n, st);
+  rev_stage(S, A, false, 1);
   // lVin / lBin hold the adjoint on V1 / B1: they become lV / lB
   for (int nv = 0; nv < NV; nv++) std::swap(B->lV[nv], B->lVin[nv]);
   for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
@@ -994,15 +1048,13 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
     k_adj_zero_bx<<<grid_for(n), kT, 0, st>>>(A);
   }
   k_adj_add_u0<<<grid_for(n), kT, 0, st>>>(A);
-  for (int nv = 0; nv < NV; nv++) dcopy(S->V[nv], B->Vn[nv], n, st);
-  for (int d = 0; d < nb; d++) dcopy(S->Bs[d], B->Bn[d], n, st);
-  rev_stage(S, A, ct);
+  copy_state(S->V, B->Vn, NV, S->Bs, B->Bn, nb, n, st);
+  rev_stage(S, A, ct, 0);
   k_adj_p2c<<<grid_for(n), kT, 0, st>>>(A);
   for (int nv = 0; nv < NV; nv++) std::swap(B->lV[nv], B->lVin[nv]);
   for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
   // the solver's state is the step's start again
-  for (int nv = 0; nv < NV; nv++) dcopy(S->V[nv], B->Vn[nv], n, st);
-  for (int d = 0; d < nb; d++) dcopy(S->Bs[d], B->Bn[d], n, st);
+  copy_state(S->V, B->Vn, NV, S->Bs, B->Bn, nb, n, st);
   return sync_status(S);
 }
 
