@@ -196,7 +196,10 @@ int pg_tangent_kink(pg_solver *s, int enable, double *margin);
    the gradient with respect to the state before a step of length dt taken
    from the solver's current state (which it leaves unchanged);
    pg_adjoint_get reads it back.  Adjoint values on ghost zones are ignored
-   on set and zero on get. */
+   on set and zero on get.  Covered: PLM/PPM (no characteristic limiting),
+   HLL/HLLD/Roe, constrained transport with the UCT_HLL average, periodic,
+   outflow, reflective and equatorial-symmetric sides; PG_ERR_INVALID for
+   user-defined sides and the other configurations. */
 int pg_adjoint_set(pg_solver *s, const double *const vars[8], const double *const faces[3],
                    int layout);
 int pg_adjoint_step(pg_solver *s, double dt);

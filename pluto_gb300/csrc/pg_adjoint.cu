@@ -139,6 +139,7 @@ struct AdjBufs {
   double* lS[3][2];  // on max(0,-SL) and max(0,SR) per direction
   double* lDV[3][3];
   double* lE[3];
+  double* lBm1[3];  // on the face field's -1 layers (non-periodic axes under CT)
   // forward states saved by the recomputation
   double* Vn[8];
   double* Bn[3];
@@ -546,6 +547,137 @@ __global__ void k_adj_bound(Geom g, BoundTab t, int narr, int bcx, int bcy, int 
   }
 }
 
+// ---------------------------------------------------------------------------
+// Boundary fill under CT with a non-periodic axis, transposed.  The forward
+// (launch_bound_ct, pg_bound_ct.cuh) goes axis by axis: ghost copies
+// (k_bound_axis), then on a non-periodic axis the normal face component
+// marched away from the boundary from div B = 0 and, on outflow sides, its
+// cell averages (k_fill_normal).  Undone in reverse order; every value the
+// forward overwrote gets the adjoint zero once its share has been passed on.
+// la: the adjoint arrays in the forward's layout (cells, faces, -1 layers).
+// ---------------------------------------------------------------------------
+template <int AX>
+__global__ void k_adj_bound_axis(BoundCT<double> la, int type, long long nghost) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= nghost) return;
+  const Geom& g = la.g;
+  constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
+  const int ng = g.beg[AX], n = g.nx[AX];
+  const int l = (int)(q % (2 * ng));
+  const long long t = q / (2 * ng);
+  int c[3], s[3];
+  c[B1] = (int)(t % g.nt[B1]);
+  c[B2] = (int)(t / g.nt[B1]);
+  const bool lo = l < ng;
+  c[AX] = lo ? l : g.end[AX] + 1 + (l - ng);
+  s[B1] = c[B1];
+  s[B2] = c[B2];
+  s[AX] = bc_src(c[AX], g.beg[AX], g.end[AX], n, type);
+  const int side = bc_side(type, !lo);
+  if (side == PG_USERDEF) return;  // no adjoint of user-defined sides
+  const long long dst = cidx(g, c[2], c[1], c[0]), src = cidx(g, s[2], s[1], s[0]);
+  auto pass = [](double* d, double* from, bool neg) {  // d += +-from, from = 0
+    const double w = *from;
+    *from = 0.0;
+    if (w != 0.0) atomicAdd(d, neg ? -w : w);
+  };
+#pragma unroll
+  for (int nv = 0; nv < NV; nv++) pass(&la.V[nv][src], &la.V[nv][dst], bc_flip(AX, side, nv, la.ncomp) < 0);
+  for (int fd = 0; fd < la.nbfield; fd++) {
+    if (fd != AX) {
+      const bool neg = bc_flip(AX, side, BX1 + fd, la.ncomp) < 0;
+      pass(&la.Bs[fd][src], &la.Bs[fd][dst], neg);
+      if (c[fd] == 0) {
+        int cm[3] = {c[0], c[1], c[2]}, sm[3] = {s[0], s[1], s[2]};
+        cm[fd] = -1;
+        sm[fd] = -1;
+        pass(bct_face(la, fd, sm[2], sm[1], sm[0]), bct_face(la, fd, cm[2], cm[1], cm[0]), neg);
+      }
+    } else if (type == PG_PERIODIC) {
+      if (lo || c[AX] != g.end[AX]) pass(&la.Bs[fd][src], &la.Bs[fd][dst], false);
+      if (lo && c[AX] == 0) {
+        int cm[3] = {c[0], c[1], c[2]}, sm[3] = {s[0], s[1], s[2]};
+        cm[AX] = -1;
+        sm[AX] = n - 1;
+        pass(bct_face(la, fd, sm[2], sm[1], sm[0]), bct_face(la, fd, cm[2], cm[1], cm[0]), false);
+      }
+    }
+  }
+}
+
+// k_fill_normal transposed: one thread per transverse line and side; its
+// normal-face and cell-average adjoints are its own, the transverse faces
+// the march read are shared with the neighbouring lines (atomic).
+template <int AX>
+__global__ void k_adj_fill_normal(BoundCT<double> la, long long ntrans, int type) {
+  const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+  if (q >= 2 * ntrans) return;
+  const Geom& g = la.g;
+  constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
+  const bool lo = (q & 1) == 0;
+  const int st = bc_side(type, !lo);
+  if (st == PG_PERIODIC) return;
+  const bool average = st == PG_OUTFLOW || st == PG_USERDEF;
+  const long long t = q >> 1;
+  int c[3];
+  c[B1] = (int)(t % g.nt[B1]);
+  c[B2] = (int)(t / g.nt[B1]);
+  const bool d3 = g.dims == 3;
+  const double An = la.area[AX];
+  auto lface = [&](int fd, const int* x) { return bct_face(la, fd, x[2], x[1], x[0]); };
+  // w * d(A_fd b_fd(+) - A_fd b_fd(-))/d(faces) for the transverse
+  // components the march read at cell c (x, y, z order; no z in 2D)
+  auto scatter_others = [&](double w) {
+    for (int fd = 0; fd < 3; fd++) {
+      if (fd == AX || (fd == 2 && !d3)) continue;
+      int m[3] = {c[0], c[1], c[2]};
+      m[fd] -= 1;
+      atomicAdd(lface(fd, c), w * la.area[fd]);
+      atomicAdd(lface(fd, m), -w * la.area[fd]);
+    }
+  };
+  // cell averages 0.5 (b(x) + b(x-1)) of the normal component, transposed
+  auto average_rev = [&](int x) {
+    c[AX] = x;
+    int m[3] = {c[0], c[1], c[2]};
+    m[AX] = x - 1;
+    double* pv = &la.V[BX1 + AX][cidx(g, c[2], c[1], c[0])];
+    const double a = *pv;
+    *pv = 0.0;
+    *lface(AX, c) += 0.5 * a;
+    *lface(AX, m) += 0.5 * a;
+  };
+  if (lo) {
+    if (average)
+      for (int x = 0; x < g.beg[AX]; x++) average_rev(x);
+    // forward, x = beg-1 .. 0: b(x-1) = (An b(x) + others(x)) / An
+    for (int x = 0; x <= g.beg[AX] - 1; x++) {
+      c[AX] = x;
+      int m[3] = {c[0], c[1], c[2]};
+      m[AX] = x - 1;
+      double* pr = lface(AX, m);
+      const double a = *pr;
+      *pr = 0.0;
+      *lface(AX, c) += a;
+      scatter_others(a / An);
+    }
+  } else {
+    if (average)
+      for (int x = g.end[AX] + 1; x < g.nt[AX]; x++) average_rev(x);
+    // forward, x = end+1 .. nt-1: b(x) = (An b(x-1) - others(x)) / An
+    for (int x = g.nt[AX] - 1; x >= g.end[AX] + 1; x--) {
+      c[AX] = x;
+      int m[3] = {c[0], c[1], c[2]};
+      m[AX] = x - 1;
+      double* pr = lface(AX, c);
+      const double a = *pr;
+      *pr = 0.0;
+      *lface(AX, m) += a;
+      scatter_others(-a / An);
+    }
+  }
+}
+
 // Adjoint input: the cell adjoint on ghosts and the face adjoint off the
 // faces the step writes are cleared (those values are refilled, not evolved).
 __global__ void k_adj_clean(AdjArgs A, int ct) {
@@ -598,6 +730,9 @@ static int adjoint_alloc(Solver* S, AdjBufs** out) {
         unused |= (dir_off || !ct) && (&p[q] == &B->sSL[st][d] || &p[q] == &B->sSR[st][d]);
         for (int c = 0; c < 3; c++) unused |= (dir_off || c >= S->g.dims || !ct) && &p[q] == &B->sDV[st][d][c];
       }
+    bool ct_outflow = false;
+    for (int d = 0; d < S->g.dims; d++) ct_outflow |= ct && S->cfg.bc[d] != PG_PERIODIC;
+    for (int d = 0; d < 3; d++) unused |= !ct_outflow && &p[q] == &B->lBm1[d];
     used[q] = !unused;
   }
   size_t count = 0;
@@ -751,8 +886,28 @@ void rev_dir(Solver* S, const AdjArgs& A) {
   k_adj_recon<DIR><<<grid_for(rb.count() * NV, 128), 128, 0, st>>>(A, rb);
 }
 
+BoundCT<double> bound_args(const Geom& g, double* const* V, double* const* Bs, double* const* Bm1, int nbfield,
+                           int ncomp) {
+  BoundCT<double> b;
+  b.g = g;
+  for (int nv = 0; nv < 8; nv++) b.V[nv] = V[nv];
+  for (int d = 0; d < 3; d++) {
+    b.Bs[d] = Bs[d];
+    b.Bm1[d] = Bm1[d];
+  }
+  b.nbfield = nbfield;
+  b.ncomp = ncomp;
+  face_areas(g, b.area);
+  return b;
+}
+
 void fwd_bound(Solver* S, const F64A<double>& f) {
   const Geom& g = S->g;
+  if (f.ct_outflow) {  // the axis-by-axis sequence with FillMagneticField
+    launch_bound_ct<double, double>(S, bound_args(g, f.V, f.Bs, f.Bm1, f.nbfield, f.ncomp), "fp64_bound",
+                                    "fp64_fill_normal");
+    return;
+  }
   const long long n0 = g.dims > 0 ? 2LL * g.beg[0] * g.nt[1] * g.nt[2] : 0;
   const long long n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
   const long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
@@ -764,6 +919,19 @@ Tab8 tab(double* const* p, int n) {
   Tab8 t;
   for (int q = 0; q < 8; q++) t.p[q] = q < n ? p[q] : nullptr;
   return t;
+}
+
+// Axis AX of the CT boundary fill reversed: the normal-face march and cell
+// averages first, then the ghost copies (the forward's order reversed).
+template <int AX>
+void rev_bound_axis(Solver* S, const BoundCT<double>& la) {
+  const Geom& g = la.g;
+  constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
+  const long long ntrans = (long long)g.nt[B1] * g.nt[B2];
+  const long long nghost = 2LL * g.beg[AX] * ntrans;
+  if (S->cfg.bc[AX] != PG_PERIODIC && la.nbfield > 0)
+    k_adj_fill_normal<AX><<<grid_for(2 * ntrans, 128), 128, 0, S->stream>>>(la, ntrans, S->cfg.bc[AX]);
+  k_adj_bound_axis<AX><<<grid_for(nghost), kT, 0, S->stream>>>(la, S->cfg.bc[AX], nghost);
 }
 
 // One stage reversed.  On entry lU holds the adjoint on the stage's
@@ -779,8 +947,9 @@ void rev_stage(Solver* S, const AdjArgs& A, bool add_b0, int stage) {
   const bool ct = A.f.ct;
   const AdjBufs& b = A.b;
   {
-    const int cnt[5] = {NV, 3, 6, 9, 3};
-    if (ct) zero_arrays({b.lVin, b.lBin, &b.lS[0][0], &b.lDV[0][0], b.lE}, cnt, n, st);
+    const int cnt[6] = {NV, 3, 6, 9, 3, 3};
+    if (A.f.ct_outflow) zero_arrays({b.lVin, b.lBin, &b.lS[0][0], &b.lDV[0][0], b.lE, b.lBm1}, cnt, n, st);
+    else if (ct) zero_arrays({b.lVin, b.lBin, &b.lS[0][0], &b.lDV[0][0], b.lE}, cnt, n, st);
     else zero_arrays({b.lVin, b.lBin}, cnt, n, st);
   }
   fwd_bound(S, A.f);  // the stage input's ghosts, read by the reversed reconstruction
@@ -804,6 +973,13 @@ void rev_stage(Solver* S, const AdjArgs& A, bool add_b0, int stage) {
   rev_dir<0>(S, A0);
   if (add_b0)
     for (int d = 0; d < g.dims; d++) k_add<<<grid_for(n), kT, 0, st>>>(b.lBin[d], b.lB0[d], n);
+  if (A.f.ct_outflow) {  // the axis-by-axis fill with FillMagneticField, reversed
+    const BoundCT<double> la = bound_args(g, b.lVin, b.lBin, b.lBm1, A.f.nbfield, A.f.ncomp);
+    if (g.dims > 2) rev_bound_axis<2>(S, la);
+    if (g.dims > 1) rev_bound_axis<1>(S, la);
+    rev_bound_axis<0>(S, la);
+    return;
+  }
   BoundTab t;
   int na = 0;
   for (int nv = 0; nv < NV; nv++) t.p[na++] = b.lVin[nv];
@@ -914,12 +1090,6 @@ extern "C" int pg_adjoint_set(pg_solver* h, const double* const vars[8], const d
     set_last_error("pg_adjoint_set: the adjoint covers the UCT_HLL emf average");
     return PG_ERR_INVALID;
   }
-  if (S->cfg.divb == PG_CONSTRAINED_TRANSPORT)
-    for (int d = 0; d < S->g.dims; d++)
-      if (S->cfg.bc[d] != PG_PERIODIC) {
-        set_last_error("pg_adjoint_set: non-periodic boundaries under constrained transport are not covered");
-        return PG_ERR_INVALID;
-      }
   for (int d = 0; d < S->g.dims; d++)
     if (bc_side(S->cfg.bc[d], false) == PG_USERDEF || bc_side(S->cfg.bc[d], true) == PG_USERDEF) {
       set_last_error("pg_adjoint_set: user-defined boundaries have no adjoint");

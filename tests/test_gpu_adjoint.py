@@ -3,7 +3,9 @@
 Checks, all with a frozen dt sequence:
 - the tangent-linear value part is the plain FP64 step bit for bit;
 - dot-product test <lambda, TL(delta)> == <adjoint(lambda), delta> for PLM
-  and PPM, HLL and HLLD, 1D outflow / 2D / 3D constrained transport;
+  and PPM, HLL and HLLD, 1D outflow / 2D / 3D constrained transport,
+  outflow / reflective / equatorial-symmetric sides under constrained
+  transport;
 - TL against central finite differences of the state;
 - the CP-Alfven objective (128^2, 256 steps, checkpoint every 16): the
   autograd gradient against the tangent-linear derivative (exact transpose)
@@ -65,12 +67,27 @@ def _case(name):
     if name == "ot2d_mirror_noct":
         spec, vc, f = P.orszag_tang(16)
         return dict(spec, ct=False, bc=["reflective", "eqtsymmetric", "periodic"]), vc, f, [1e-3] * 3
+    # non-periodic sides under CT: the axis-by-axis fill with the normal field
+    # from div B = 0 (and its cell averages on outflow sides), transposed
+    if name == "ot2d_outflow_ct":
+        spec, vc, f = P.orszag_tang(16)
+        return dict(spec, bc="outflow"), vc, f, [1e-3] * 4
+    if name == "cpa2d_mirror_ct":
+        spec, vc, f = P.cp_alfven(16)
+        return dict(spec, bc=["reflective", "eqtsymmetric", "periodic"]), vc, f, [2e-3] * 3
+    if name == "blast3d_outflow_ct":
+        spec, vc, f = P.blast3d(10)
+        return dict(spec, bc="outflow"), vc, f, [1e-3] * 3
+    if name == "turb3d_sides_ct":
+        spec, vc, f = P.turbulence3d(8, seed=5)
+        return (dict(spec, stepping="RK2", recon="LINEAR", bc=[("outflow", "reflective"), "periodic", "outflow"]),
+                vc, f, [1e-3] * 3)
     raise KeyError(name)
 
 
 CASES = ["cpa2d_plm_hlld", "ot2d_plm_hll", "turb3d_ppm_hlld", "turb3d_plm_minmod_hll",
          "tube1d_outflow", "tube1d_ppm_outflow", "cpa2d_plm_roe", "tube1d_reflective", "ot2d_mirror_noct",
-         "tube1d_sides"]
+         "tube1d_sides", "ot2d_outflow_ct", "cpa2d_mirror_ct", "blast3d_outflow_ct", "turb3d_sides_ct"]
 
 
 def _smooth(vc):
