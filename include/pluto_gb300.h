@@ -190,7 +190,7 @@ int pg_tangent_download(pg_solver *s, double *const vars[8], double *const faces
    branch of the computation would switch (+inf: none depends on it). */
 int pg_tangent_kink(pg_solver *s, int enable, double *margin);
 
-/* PG_FP64 solvers with RK2: adjoint of one step.  pg_adjoint_set loads the
+/* PG_FP64 solvers with EULER/RK2/RK3: adjoint of one step.  pg_adjoint_set loads the
    adjoint (gradient of a scalar with respect to the state after the step)
    into device buffers; pg_adjoint_step(dt) replaces it, on the device, with
    the gradient with respect to the state before a step of length dt taken

@@ -1,17 +1,17 @@
-// Differentiated FP64 path: tangent-linear model, adjoint of one RK2 step,
-// device-resident checkpoints.
+// Differentiated FP64 path: tangent-linear model, adjoint of one EULER /
+// RK2 / RK3 step, device-resident checkpoints.
 //
 // Tangent-linear: the FP64 step kernels of pg_fp64_kernels.cuh instantiated
 // with T = Dual<1>; value parts are the plain FP64 step, derivative parts its
 // directional derivative through the branches taken (precision
 // PG_FP64_TANGENT).
 //
-// Adjoint: pg_adjoint_step maps lambda(n+1) -> lambda(n) for one RK2 step of
+// Adjoint: pg_adjoint_step maps lambda(n+1) -> lambda(n) for one step of
 // a given (frozen) dt.  The step is recomputed from the solver's state, then
 // each forward operation is undone in reverse order by a hand-written kernel:
 //   k_adj_c2p      ConsToPrim                  (Src/MHD/mappers.c:88-254)
 //   k_adj_avg      CT_AverageMagneticField     (Src/MHD/CT/ct_field_average.c:13)
-//   k_adj_rk_*     RK2 combination             (Src/Time_Stepping/rk_step.c:93-160)
+//   k_adj_rk_*     RK combinations             (Src/Time_Stepping/rk_step.c:93-233)
 //   k_adj_ct       CT_Update                   (Src/MHD/CT/ct_update.c:29-220)
 //   k_adj_emf      CT_EMF_HLL_Solver           (Src/MHD/CT/ct_emf_average.c:179-352)
 //   k_adj_flux     RightHandSide, U += rhs     (Src/MHD/rhs.c:193-201)
@@ -143,19 +143,18 @@ struct AdjBufs {
   // forward states saved by the recomputation
   double* Vn[8];
   double* Bn[3];
-  double* V1[8];
-  double* B1[3];
-  double* U1[8];
-  double* U2[8];
+  double* Vst[2][8];  // stage inputs V1, V2 (the results of stages 1, 2)
+  double* Bst[2][3];  // and their faces
+  double* Ust[3][8];  // conserved result of each stage
   // what the forward recomputation produced in each stage s: the
   // reconstructed states of each direction d, the wave speeds and the
   // velocity slopes (under CT).  The stage reversals read them instead of
   // reconstructing and solving every direction again.
-  double* sVP[2][3][8];
-  double* sVM[2][3][8];
-  double* sSL[2][3];
-  double* sSR[2][3];
-  double* sDV[2][3][3];
+  double* sVP[3][3][8];
+  double* sVM[3][3][8];
+  double* sSL[3][3];
+  double* sSR[3][3];
+  double* sDV[3][3][3];
 };
 
 struct AdjArgs {
@@ -247,27 +246,28 @@ __global__ void k_adj_zero_bx(AdjArgs A) {
   for (int d = 0; d < A.f.g.dims; d++) A.b.lU[BX1 + d][c] = 0.0;
 }
 
-// Stage-2 RK2 combination transposed, cell part:
-// U2 = w0 U0 + wc U  =>  lU0 = w0 lU, lU <- wc lU, lUx = lU (adjoint on U1).
+// RK combination of stage s >= 2 transposed, cell part:
+// U_s = w0 U0 + wc U  =>  lU0 += w0 lU, lU <- wc lU, lUx = lU (adjoint on
+// U_{s-1}, the base of U).
 __global__ void k_adj_rk_cells(AdjArgs A, double w0, double wc) {
   long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (c >= A.f.g.ncell) return;
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
     const double l = A.b.lU[nv][c];
-    A.b.lU0[nv][c] = w0 * l;
+    A.b.lU0[nv][c] += w0 * l;
     A.b.lU[nv][c] = wc * l;
     A.b.lUx[nv][c] = wc * l;
   }
 }
-// Face part on the CT faces: B2 = w0 B0 + wc (B + dt curl E)
-// => lB0 = w0 lB, lB <- wc lB (the curl part is then taken from the scaled lB).
+// Face part on the CT faces: B_s = w0 B0 + wc (B + dt curl E)
+// => lB0 += w0 lB, lB <- wc lB (the curl part is then taken from the scaled lB).
 __global__ void k_adj_rk_faces(AdjArgs A, double w0, double wc) {
   ADJ_CELL_PROLOGUE
   for (int d = 0; d < g.dims; d++) {
     const double l = A.b.lB[d][c];
     const bool on = ct_face(g, d, i, j, k);
-    A.b.lB0[d][c] = on ? w0 * l : 0.0;
+    if (on) A.b.lB0[d][c] += w0 * l;
     A.b.lB[d][c] = on ? wc * l : l;
   }
 }
@@ -722,9 +722,18 @@ static int adjoint_alloc(Solver* S, AdjBufs** out) {
   std::vector<char> used(np, 1);
   for (size_t q = 0; q < np; q++) {
     bool unused = false;
-    for (int st = 0; st < 2; st++)
+    const int ns = S->cfg.time_stepping == PG_RK3 ? 3 : (S->cfg.time_stepping == PG_EULER ? 1 : 2);
+    for (int k = 0; k < 3; k++) {  // the saved states of stages the scheme does not have
+      for (int nv = 0; nv < NV; nv++) {
+        unused |= k >= ns - 1 && k < 2 && &p[q] == &B->Vst[k][nv];
+        unused |= k >= ns && &p[q] == &B->Ust[k][nv];
+      }
+      for (int d = 0; d < 3; d++) unused |= k < 2 && (k >= ns - 1 || !ct || d >= S->g.dims) && &p[q] == &B->Bst[k][d];
+    }
+    for (int st = 0; st < 3; st++)
       for (int d = 0; d < 3; d++) {
-        const bool dir_off = d >= S->g.dims;
+        const bool stage_off = st >= ns;
+        const bool dir_off = d >= S->g.dims || stage_off;
         for (int nv = 0; nv < NV; nv++)
           unused |= dir_off && (&p[q] == &B->sVP[st][d][nv] || &p[q] == &B->sVM[st][d][nv]);
         unused |= (dir_off || !ct) && (&p[q] == &B->sSL[st][d] || &p[q] == &B->sSR[st][d]);
@@ -1078,8 +1087,8 @@ extern "C" int pg_adjoint_set(pg_solver* h, const double* const vars[8], const d
     set_last_error("bad layout");
     return PG_ERR_INVALID;
   }
-  if (S->cfg.time_stepping != PG_RK2) {
-    set_last_error("pg_adjoint_set: the adjoint covers RK2 time stepping");
+  if (S->cfg.time_stepping != PG_RK2 && S->cfg.time_stepping != PG_RK3 && S->cfg.time_stepping != PG_EULER) {
+    set_last_error("pg_adjoint_set: the adjoint covers EULER, RK2 and RK3 time stepping");
     return PG_ERR_INVALID;
   }
   if (S->cfg.char_limiting) {
@@ -1176,53 +1185,63 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
   // each stage's sweeps write their states, wave speeds and slopes into
   // that stage's own arrays (stage_args), which the reversal reads
   const F64A<double> f = make_args<double>(S);
+  const int ns = S->cfg.time_stepping == PG_RK3 ? 3 : (S->cfg.time_stepping == PG_EULER ? 1 : 2);
   launch_bound<double>(S, f);
   k_begin_step<double><<<grid_for(n), kT, 0, st>>>(f, dom);
-  launch_sweep<double, 0>(S, stage_args(f, *B, 0, 0), 1);
-  if (g.dims > 1) launch_sweep<double, 1>(S, stage_args(f, *B, 0, 1), 1);
-  if (g.dims > 2) launch_sweep<double, 2>(S, stage_args(f, *B, 0, 2), 1);
-  launch_stage_tail<double, 1, 2>(S, stage_args(f, *B, 0, 0), dom);
-  copy_state(B->V1, S->V, NV, B->B1, S->Bs, nb, n, st);
-  copy_state(B->U1, S->U, NV, nullptr, nullptr, 0, n, st);
-  launch_bound<double>(S, f);
-  launch_sweep<double, 0>(S, stage_args(f, *B, 1, 0), 2);
-  if (g.dims > 1) launch_sweep<double, 1>(S, stage_args(f, *B, 1, 1), 2);
-  if (g.dims > 2) launch_sweep<double, 2>(S, stage_args(f, *B, 1, 2), 2);
-  launch_stage_tail<double, 2, 2>(S, stage_args(f, *B, 1, 0), dom);
-  copy_state(B->U2, S->U, NV, nullptr, nullptr, 0, n, st);
+  for (int s = 1; s <= ns; s++) {
+    if (s > 1) launch_bound<double>(S, f);
+    launch_sweep<double, 0>(S, stage_args(f, *B, s - 1, 0), s);
+    if (g.dims > 1) launch_sweep<double, 1>(S, stage_args(f, *B, s - 1, 1), s);
+    if (g.dims > 2) launch_sweep<double, 2>(S, stage_args(f, *B, s - 1, 2), s);
+    const F64A<double> fs = stage_args(f, *B, s - 1, 0);
+    if (ns == 1) launch_stage_tail<double, 1, 1>(S, fs, dom);
+    else if (ns == 2 && s == 1) launch_stage_tail<double, 1, 2>(S, fs, dom);
+    else if (ns == 2) launch_stage_tail<double, 2, 2>(S, fs, dom);
+    else if (s == 1) launch_stage_tail<double, 1, 3>(S, fs, dom);
+    else if (s == 2) launch_stage_tail<double, 2, 3>(S, fs, dom);
+    else launch_stage_tail<double, 3, 3>(S, fs, dom);
+    if (s < ns) copy_state(B->Vst[s - 1], S->V, NV, B->Bst[s - 1], S->Bs, nb, n, st);
+    copy_state(B->Ust[s - 1], S->U, NV, nullptr, nullptr, 0, n, st);
+  }
 
   AdjArgs A;
   memset(&A, 0, sizeof A);
   A.f = f;
   A.dt = dt;
-  const double w0 = 0.5, wc = 0.5;  // RK2 weights
-  // ---- stage 2 reversed ----
-  A.b = *B;
-  k_adj_c2p<<<grid_for(n), kT, 0, st>>>(A, tab(B->U2, 8), tab(B->lV, 8), 0);
-  if (ct) {
-    k_adj_avg<<<grid_for(n), kT, 0, st>>>(A, tab(B->lB, 3));
-    k_adj_zero_bx<<<grid_for(n), kT, 0, st>>>(A);
-    k_adj_rk_faces<<<grid_for(n), kT, 0, st>>>(A, w0, wc);
+  {
+    const int cnt[2] = {NV, 3};
+    zero_arrays({B->lU0, B->lB0}, cnt, n, st);  // accumulated over the stages
   }
-  k_adj_rk_cells<<<grid_for(n), kT, 0, st>>>(A, w0, wc);
-  copy_state(S->V, B->V1, NV, S->Bs, B->B1, nb, n, st);
-  rev_stage(S, A, false, 1);
-  // lVin / lBin hold the adjoint on V1 / B1: they become lV / lB
-  for (int nv = 0; nv < NV; nv++) std::swap(B->lV[nv], B->lVin[nv]);
-  for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
-  // ---- stage 1 reversed ----
-  A.b = *B;
-  k_adj_c2p<<<grid_for(n), kT, 0, st>>>(A, tab(B->U1, 8), tab(B->lV, 8), 1);
-  if (ct) {
-    k_adj_avg<<<grid_for(n), kT, 0, st>>>(A, tab(B->lB, 3));
-    k_adj_zero_bx<<<grid_for(n), kT, 0, st>>>(A);
+  // the weights of U_s = w0 U0 + wc (U_{s-1} + dt L) (rk_step.c:18-24)
+  auto weights = [&](int s, double& w0, double& wc) {
+    if (ns == 2) w0 = wc = 0.5;
+    else if (s == 2) { w0 = 0.75; wc = 0.25; }
+    else { w0 = 1.0 / 3.0; wc = 2.0 / 3.0; }
+  };
+  for (int s = ns; s >= 1; s--) {
+    A.b = *B;
+    // lU: adjoint on U_s from that on V_s (and on U_s as the next stage's base)
+    k_adj_c2p<<<grid_for(n), kT, 0, st>>>(A, tab(B->Ust[s - 1], 8), tab(B->lV, 8), s < ns ? 1 : 0);
+    if (ct) {
+      k_adj_avg<<<grid_for(n), kT, 0, st>>>(A, tab(B->lB, 3));
+      k_adj_zero_bx<<<grid_for(n), kT, 0, st>>>(A);
+    }
+    if (s >= 2) {
+      double w0, wc;
+      weights(s, w0, wc);
+      if (ct) k_adj_rk_faces<<<grid_for(n), kT, 0, st>>>(A, w0, wc);
+      k_adj_rk_cells<<<grid_for(n), kT, 0, st>>>(A, w0, wc);
+      copy_state(S->V, B->Vst[s - 2], NV, S->Bs, B->Bst[s - 2], nb, n, st);
+    } else {
+      k_adj_add_u0<<<grid_for(n), kT, 0, st>>>(A);  // stage 1's base is U0
+      copy_state(S->V, B->Vn, NV, S->Bs, B->Bn, nb, n, st);
+    }
+    rev_stage(S, A, s == 1 && ct, s - 1);
+    if (s == 1) k_adj_p2c<<<grid_for(n), kT, 0, st>>>(A);
+    // lVin / lBin hold the adjoint on the stage input: they become lV / lB
+    for (int nv = 0; nv < NV; nv++) std::swap(B->lV[nv], B->lVin[nv]);
+    for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
   }
-  k_adj_add_u0<<<grid_for(n), kT, 0, st>>>(A);
-  copy_state(S->V, B->Vn, NV, S->Bs, B->Bn, nb, n, st);
-  rev_stage(S, A, ct, 0);
-  k_adj_p2c<<<grid_for(n), kT, 0, st>>>(A);
-  for (int nv = 0; nv < NV; nv++) std::swap(B->lV[nv], B->lVin[nv]);
-  for (int d = 0; d < 3; d++) std::swap(B->lB[d], B->lBin[d]);
   // the solver's state is the step's start again
   copy_state(S->V, B->Vn, NV, S->Bs, B->Bn, nb, n, st);
   return sync_status(S);

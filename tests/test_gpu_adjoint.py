@@ -5,7 +5,7 @@ Checks, all with a frozen dt sequence:
 - dot-product test <lambda, TL(delta)> == <adjoint(lambda), delta> for PLM
   and PPM, HLL and HLLD, 1D outflow / 2D / 3D constrained transport,
   outflow / reflective / equatorial-symmetric sides under constrained
-  transport;
+  transport, RK2, RK3 and EULER stepping;
 - TL against central finite differences of the state;
 - the CP-Alfven objective (128^2, 256 steps, checkpoint every 16): the
   autograd gradient against the tangent-linear derivative (exact transpose)
@@ -82,12 +82,23 @@ def _case(name):
         spec, vc, f = P.turbulence3d(8, seed=5)
         return (dict(spec, stepping="RK2", recon="LINEAR", bc=[("outflow", "reflective"), "periodic", "outflow"]),
                 vc, f, [1e-3] * 3)
+    # RK3 (the turbulence configuration's stepping) and EULER
+    if name == "turb3d_ppm_rk3":
+        spec, vc, f = P.turbulence3d(8, seed=2)
+        return spec, vc, f, [1e-3] * 3
+    if name == "blast3d_outflow_rk3":
+        spec, vc, f = P.blast3d(8)
+        return dict(spec, stepping="RK3", bc="outflow"), vc, f, [1e-3] * 2
+    if name == "ot2d_euler":
+        spec, vc, f = P.orszag_tang(16)
+        return dict(spec, stepping="EULER"), vc, f, [5e-4] * 4
     raise KeyError(name)
 
 
 CASES = ["cpa2d_plm_hlld", "ot2d_plm_hll", "turb3d_ppm_hlld", "turb3d_plm_minmod_hll",
          "tube1d_outflow", "tube1d_ppm_outflow", "cpa2d_plm_roe", "tube1d_reflective", "ot2d_mirror_noct",
-         "tube1d_sides", "ot2d_outflow_ct", "cpa2d_mirror_ct", "blast3d_outflow_ct", "turb3d_sides_ct"]
+         "tube1d_sides", "ot2d_outflow_ct", "cpa2d_mirror_ct", "blast3d_outflow_ct", "turb3d_sides_ct",
+         "turb3d_ppm_rk3", "blast3d_outflow_rk3", "ot2d_euler"]
 
 
 def _smooth(vc):
