@@ -157,10 +157,32 @@ struct AdjBufs {
   double* sDV[3][3][3];
 };
 
+// linear zone index -> (i, j, k) with the row and plane divisors prepared on
+// the host (32-bit divisions while the arrays have fewer than 2^32 zones)
+struct CellMap {
+  Div32 nt0, nt1;
+  bool wide = false;
+  CellMap() = default;
+  __host__ explicit CellMap(const Geom& g) : nt0(g.nt[0]), nt1(g.nt[1]), wide(g.ncell >= (1LL << 32)) {}
+  __device__ void ijk(long long c, int& i, int& j, int& k) const {
+    if (!wide) {
+      const unsigned u = (unsigned)c, r = nt0.div(u), p = nt1.div(r);
+      i = (int)(u - r * nt0.d);
+      j = (int)(r - p * nt1.d);
+      k = (int)p;
+    } else {
+      i = (int)(c % nt0.d);
+      j = (int)((c / nt0.d) % nt1.d);
+      k = (int)(c / ((long long)nt0.d * nt1.d));
+    }
+  }
+};
+
 struct AdjArgs {
   F64A<double> f;  // forward arrays (the solver's own)
   AdjBufs b;
   double dt;
+  CellMap cm;
 };
 
 struct Tab8 {
@@ -169,11 +191,6 @@ struct Tab8 {
 
 __device__ __forceinline__ bool in_dom(const Geom& g, int i, int j, int k) {
   return i >= g.beg[0] && i <= g.end[0] && j >= g.beg[1] && j <= g.end[1] && k >= g.beg[2] && k <= g.end[2];
-}
-__device__ __forceinline__ void cell_ijk(const Geom& g, long long c, int& i, int& j, int& k) {
-  i = (int)(c % g.nt[0]);
-  j = (int)((c / g.nt[0]) % g.nt[1]);
-  k = (int)(c / ((long long)g.nt[0] * g.nt[1]));
 }
 // faces written by CT_Update for component fd (ct_update.c:79-81,132-134,188-190)
 __device__ __forceinline__ bool ct_face(const Geom& g, int fd, int i, int j, int k) {
@@ -190,7 +207,7 @@ __device__ __forceinline__ bool ct_face(const Geom& g, int fd, int i, int j, int
   const Geom& g = A.f.g;                                          \
   if (c >= g.ncell) return;                                       \
   int i, j, k;                                                    \
-  cell_ijk(g, c, i, j, k);
+  A.cm.ijk(c, i, j, k);
 
 // lU = J_C(U)^T lambda_V (+ lUx), zero off the domain.  One thread per zone.
 __global__ void k_adj_c2p(AdjArgs A, Tab8 Ust, Tab8 L, int add_ux) {
@@ -521,11 +538,11 @@ __global__ void k_adj_recon(AdjArgs A, Box box) {
 struct BoundTab {
   double* p[12];
 };
-__global__ void k_adj_bound(Geom g, BoundTab t, int narr, int bcx, int bcy, int bcz, int ncomp) {
+__global__ void k_adj_bound(Geom g, CellMap cm, BoundTab t, int narr, int bcx, int bcy, int bcz, int ncomp) {
   long long c = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (c >= g.ncell) return;
   int i, j, k;
-  cell_ijk(g, c, i, j, k);
+  cm.ijk(c, i, j, k);
   if (in_dom(g, i, j, k)) return;
   const int si = bmap(i, g.beg[0], g.end[0], g.nx[0], bcx);
   const int sj = g.dims > 1 ? bmap(j, g.beg[1], g.end[1], g.nx[1], bcy) : j;
@@ -557,17 +574,14 @@ __global__ void k_adj_bound(Geom g, BoundTab t, int narr, int bcx, int bcy, int 
 // la: the adjoint arrays in the forward's layout (cells, faces, -1 layers).
 // ---------------------------------------------------------------------------
 template <int AX>
-__global__ void k_adj_bound_axis(BoundCT<double> la, int type, long long nghost) {
+__global__ void k_adj_bound_axis(BoundCT<double> la, int type, AxisGhosts ag) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= nghost) return;
+  if (q >= ag.n) return;
   const Geom& g = la.g;
   constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
   const int ng = g.beg[AX], n = g.nx[AX];
-  const int l = (int)(q % (2 * ng));
-  const long long t = q / (2 * ng);
-  int c[3], s[3];
-  c[B1] = (int)(t % g.nt[B1]);
-  c[B2] = (int)(t / g.nt[B1]);
+  int l, c[3], s[3];
+  ag.coords(q, l, c[B1], c[B2]);
   const bool lo = l < ng;
   c[AX] = lo ? l : g.end[AX] + 1 + (l - ng);
   s[B1] = c[B1];
@@ -609,7 +623,7 @@ __global__ void k_adj_bound_axis(BoundCT<double> la, int type, long long nghost)
 // normal-face and cell-average adjoints are its own, the transverse faces
 // the march read are shared with the neighbouring lines (atomic).
 template <int AX>
-__global__ void k_adj_fill_normal(BoundCT<double> la, long long ntrans, int type) {
+__global__ void k_adj_fill_normal(BoundCT<double> la, long long ntrans, int type, AxisGhosts ag) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= 2 * ntrans) return;
   const Geom& g = la.g;
@@ -620,8 +634,7 @@ __global__ void k_adj_fill_normal(BoundCT<double> la, long long ntrans, int type
   const bool average = st == PG_OUTFLOW || st == PG_USERDEF;
   const long long t = q >> 1;
   int c[3];
-  c[B1] = (int)(t % g.nt[B1]);
-  c[B2] = (int)(t / g.nt[B1]);
+  ag.transverse(t, c[B1], c[B2]);
   const bool d3 = g.dims == 3;
   const double An = la.area[AX];
   auto lface = [&](int fd, const int* x) { return bct_face(la, fd, x[2], x[1], x[0]); };
@@ -917,11 +930,8 @@ void fwd_bound(Solver* S, const F64A<double>& f) {
                                     "fp64_fill_normal");
     return;
   }
-  const long long n0 = g.dims > 0 ? 2LL * g.beg[0] * g.nt[1] * g.nt[2] : 0;
-  const long long n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
-  const long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
-  k_bound<double><<<grid_for(n0 + n1 + n2), kT, 0, S->stream>>>(f, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0,
-                                                                n1, n2);
+  const GhostSlabs gs(g);
+  k_bound<double><<<grid_for(gs.count()), kT, 0, S->stream>>>(f, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], gs);
 }
 
 Tab8 tab(double* const* p, int n) {
@@ -937,10 +947,10 @@ void rev_bound_axis(Solver* S, const BoundCT<double>& la) {
   const Geom& g = la.g;
   constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
   const long long ntrans = (long long)g.nt[B1] * g.nt[B2];
-  const long long nghost = 2LL * g.beg[AX] * ntrans;
+  const AxisGhosts ag(g, AX);
   if (S->cfg.bc[AX] != PG_PERIODIC && la.nbfield > 0)
-    k_adj_fill_normal<AX><<<grid_for(2 * ntrans, 128), 128, 0, S->stream>>>(la, ntrans, S->cfg.bc[AX]);
-  k_adj_bound_axis<AX><<<grid_for(nghost), kT, 0, S->stream>>>(la, S->cfg.bc[AX], nghost);
+    k_adj_fill_normal<AX><<<grid_for(2 * ntrans, 128), 128, 0, S->stream>>>(la, ntrans, S->cfg.bc[AX], ag);
+  k_adj_bound_axis<AX><<<grid_for(ag.n), kT, 0, S->stream>>>(la, S->cfg.bc[AX], ag);
 }
 
 // One stage reversed.  On entry lU holds the adjoint on the stage's
@@ -994,7 +1004,7 @@ void rev_stage(Solver* S, const AdjArgs& A, bool add_b0, int stage) {
   for (int nv = 0; nv < NV; nv++) t.p[na++] = b.lVin[nv];
   if (ct)
     for (int d = 0; d < g.dims; d++) t.p[na++] = b.lBin[d];
-  k_adj_bound<<<grid_for(n), kT, 0, st>>>(g, t, na, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2],
+  k_adj_bound<<<grid_for(n), kT, 0, st>>>(g, CellMap(g), t, na, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2],
                                           S->cfg.components);
 }
 
@@ -1125,6 +1135,7 @@ extern "C" int pg_adjoint_set(pg_solver* h, const double* const vars[8], const d
   memset(&A, 0, sizeof A);
   A.f = make_args<double>(S);
   A.b = *B;
+  A.cm = CellMap(S->g);
   k_adj_clean<<<grid_for(n), kT, 0, st>>>(A, ct);
   return sync_status(S);
 }
@@ -1208,6 +1219,7 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
   memset(&A, 0, sizeof A);
   A.f = f;
   A.dt = dt;
+  A.cm = CellMap(f.g);
   {
     const int cnt[2] = {NV, 3};
     zero_arrays({B->lU0, B->lB0}, cnt, n, st);  // accumulated over the stages

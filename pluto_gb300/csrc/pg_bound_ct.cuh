@@ -59,17 +59,14 @@ __device__ __forceinline__ T* bct_face(const BoundCT<T>& a, int fd, int k, int j
 // reference's CENTER / X*FACE boxes).  Sources are interior along AX, so the
 // threads are independent.
 template <class T, int AX>
-__global__ void k_bound_axis(BoundCT<T> a, int type, long long nghost) {
+__global__ void k_bound_axis(BoundCT<T> a, int type, AxisGhosts ag) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= nghost) return;
+  if (q >= ag.n) return;
   const Geom& g = a.g;
   constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
   const int ng = g.beg[AX], n = g.nx[AX];
-  const int l = (int)(q % (2 * ng));
-  const long long t = q / (2 * ng);
-  int c[3], s[3];
-  c[B1] = (int)(t % g.nt[B1]);
-  c[B2] = (int)(t / g.nt[B1]);
+  int l, c[3], s[3];
+  ag.coords(q, l, c[B1], c[B2]);
   const bool lo = l < ng;
   c[AX] = lo ? l : g.end[AX] + 1 + (l - ng);
   s[B1] = c[B1];
@@ -114,7 +111,7 @@ __global__ void k_bound_axis(BoundCT<T> a, int type, long long nghost) {
 // away from the boundary face, then (outflow sides) its cell average.  type:
 // the axis's packed side types.
 template <class T, class C, int AX>
-__global__ void k_fill_normal(BoundCT<T> a, long long ntrans, int type) {
+__global__ void k_fill_normal(BoundCT<T> a, long long ntrans, int type, AxisGhosts ag) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= 2 * ntrans) return;
   const Geom& g = a.g;
@@ -124,8 +121,7 @@ __global__ void k_fill_normal(BoundCT<T> a, long long ntrans, int type) {
   const bool average = st == PG_OUTFLOW || st == PG_USERDEF;
   const long long t = q >> 1;
   int c[3];
-  c[B1] = (int)(t % g.nt[B1]);
-  c[B2] = (int)(t / g.nt[B1]);
+  ag.transverse(t, c[B1], c[B2]);
   const bool d3 = g.dims == 3;
   auto face = [&](int fd, int k, int j, int i) -> C { return C(*bct_face(a, fd, k, j, i)); };
   // A_d b_d(+) - A_d b_d(-) of component fd at cell c
@@ -181,17 +177,14 @@ __global__ void k_fill_normal(BoundCT<T> a, long long ntrans, int type) {
 // (0.5 (b + b(-1)) along the component's axis, its -1 layer from Bm1).  The
 // same thread layout as k_bound_axis.
 template <class T, class C, int AX>
-__global__ void k_avg_transverse(BoundCT<T> a, int type, long long nghost) {
+__global__ void k_avg_transverse(BoundCT<T> a, int type, AxisGhosts ag) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
-  if (q >= nghost) return;
+  if (q >= ag.n) return;
   const Geom& g = a.g;
   constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
   const int ng = g.beg[AX];
-  const int l = (int)(q % (2 * ng));
-  const long long t = q / (2 * ng);
-  int c[3];
-  c[B1] = (int)(t % g.nt[B1]);
-  c[B2] = (int)(t / g.nt[B1]);
+  int l, c[3];
+  ag.coords(q, l, c[B1], c[B2]);
   const bool lo = l < ng;
   if (bc_side(type, !lo) != PG_USERDEF) return;
   c[AX] = lo ? l : g.end[AX] + 1 + (l - ng);
@@ -209,9 +202,10 @@ static void launch_bound_ct_axis(Solver* S, const BoundCT<T>& b, const char* cop
   const Geom& g = b.g;
   constexpr int B1 = AX == 0 ? 1 : 0, B2 = AX == 2 ? 1 : 2;
   const long long ntrans = (long long)g.nt[B1] * g.nt[B2];
-  const long long nghost = 2LL * g.beg[AX] * ntrans;
+  const AxisGhosts ag(g, AX);
+  const long long nghost = ag.n;
   PG_LAUNCH(S, copy_name, (k_bound_axis<T, AX><<<grid_for(nghost), kThreads, 0, S->stream>>>(
-                              b, S->cfg.bc[AX], nghost)));
+                              b, S->cfg.bc[AX], ag)));
   if (bc_side(S->cfg.bc[AX], false) == PG_USERDEF || bc_side(S->cfg.bc[AX], true) == PG_USERDEF)
     launch_userdef_axis<T>(S, b.V, b.Bs, b.Bm1, b.nbfield, AX);
   // per side, outflow and user-defined: FillMagneticField +
@@ -219,13 +213,13 @@ static void launch_bound_ct_axis(Solver* S, const BoundCT<T>& b, const char* cop
   // FillMagneticField only (Src/boundary.c:188-206, 285-288)
   if (S->cfg.bc[AX] != PG_PERIODIC && b.nbfield > 0)
     PG_LAUNCH(S, fill_name, (k_fill_normal<T, C, AX><<<grid_for(2 * ntrans, 128), 128, 0, S->stream>>>(
-                                b, ntrans, S->cfg.bc[AX])));
+                                b, ntrans, S->cfg.bc[AX], ag)));
   // user-defined sides under CT: CT_AverageTransverseMagField too
   // (Src/boundary.c:287-289)
   if (b.nbfield > 0 &&
       (bc_side(S->cfg.bc[AX], false) == PG_USERDEF || bc_side(S->cfg.bc[AX], true) == PG_USERDEF))
     PG_LAUNCH(S, fill_name, (k_avg_transverse<T, C, AX><<<grid_for(nghost), kThreads, 0, S->stream>>>(
-                                b, S->cfg.bc[AX], nghost)));
+                                b, S->cfg.bc[AX], ag)));
 }
 
 template <class T, class C>

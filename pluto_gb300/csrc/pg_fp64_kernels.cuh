@@ -109,37 +109,11 @@ __device__ __forceinline__ int bmap(int x, int beg, int end, int n, int type) {
 }
 
 template <class T>
-__global__ void k_bound(F64A<T> a, int bcx, int bcy, int bcz, long long nslab0, long long nslab1,
-                        long long nslab2) {
+__global__ void k_bound(F64A<T> a, int bcx, int bcy, int bcz, GhostSlabs gs) {
   const Geom& g = a.g;
   long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   int i, j, k;
-  int gx = g.beg[0], gy = g.beg[1], gz = g.beg[2];
-  if (q < nslab0) {  // x ghost columns, all j,k
-    int ng2 = 2 * gx;
-    int ii = (int)(q % ng2);
-    long long r = q / ng2;
-    j = (int)(r % g.nt[1]);
-    k = (int)(r / g.nt[1]);
-    i = ii < gx ? ii : g.end[0] + 1 + (ii - gx);
-  } else if (q < nslab0 + nslab1) {  // y ghost rows, interior i, all k
-    q -= nslab0;
-    int ng2 = 2 * gy;
-    i = g.beg[0] + (int)(q % g.nx[0]);
-    long long r = q / g.nx[0];
-    int jj = (int)(r % ng2);
-    k = (int)(r / ng2);
-    j = jj < gy ? jj : g.end[1] + 1 + (jj - gy);
-  } else if (q < nslab0 + nslab1 + nslab2) {  // z ghost planes, interior i,j
-    q -= nslab0 + nslab1;
-    i = g.beg[0] + (int)(q % g.nx[0]);
-    long long r = q / g.nx[0];
-    j = g.beg[1] + (int)(r % g.nx[1]);
-    int kk = (int)(r / g.nx[1]);
-    k = kk < gz ? kk : g.end[2] + 1 + (kk - gz);
-  } else {
-    return;
-  }
+  if (!gs.coords(g, q, i, j, k)) return;
   int si = g.dims > 0 ? bmap(i, g.beg[0], g.end[0], g.nx[0], bcx) : i;
   int sj = g.dims > 1 ? bmap(j, g.beg[1], g.end[1], g.nx[1], bcy) : j;
   int sk = g.dims > 2 ? bmap(k, g.beg[2], g.end[2], g.nx[2], bcz) : k;
@@ -673,11 +647,9 @@ static void launch_bound(Solver* S, const F64A<T>& a) {
     face_areas(g, b.area);
     launch_bound_ct<T, T>(S, b, "fp64_bound", "fp64_fill_normal");
   } else {
-    long long n0 = g.dims > 0 ? 2LL * g.beg[0] * g.nt[1] * g.nt[2] : 0;
-    long long n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
-    long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
-    PG_LAUNCH(S, "fp64_bound", (k_bound<T><<<grid_for(n0 + n1 + n2), kThreads, 0, S->stream>>>(
-                                     a, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0, n1, n2)));
+    const GhostSlabs gs(g);
+    PG_LAUNCH(S, "fp64_bound", (k_bound<T><<<grid_for(gs.count()), kThreads, 0, S->stream>>>(
+                                     a, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], gs)));
   }
   S->ud_stage++;  // boundary fills so far in the step (the callbacks' stage index)
 }

@@ -88,6 +88,114 @@ struct Box {
   }
 };
 
+// Unsigned 32-bit division by a divisor fixed at launch, as multiply-and-shift
+// with Box::magic's numbers (no division instruction sequence in the kernel).
+struct Div32 {
+  unsigned d = 1, m = 1;
+  unsigned char s1 = 0, s2 = 0;
+  Div32() = default;
+  __host__ explicit Div32(unsigned dd) : d(dd) { Box::magic(dd, m, s1, s2); }
+  __device__ unsigned div(unsigned n) const { return Box::fdiv(n, m, s1, s2); }
+};
+
+// Thread index -> ghost zone of the single-pass boundary fill: first the x
+// ghost columns (2 beg0 per row, every j and k), then the y ghost rows
+// (interior i, 2 beg1 per column, every k), then the z ghost planes
+// (interior i and j).  32-bit divisions while the count is below 2^32.
+struct GhostSlabs {
+  long long n0 = 0, n1 = 0, n2 = 0;
+  Div32 x_ng2, x_nt1, y_nx0, y_ng2, z_nx0, z_nx1;
+  bool wide = false;
+  __host__ explicit GhostSlabs(const Geom& g) {
+    n0 = g.dims > 0 ? 2LL * g.beg[0] * g.nt[1] * g.nt[2] : 0;
+    n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
+    n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
+    wide = count() >= (1LL << 32);
+    if (g.dims > 0) { x_ng2 = Div32(2u * g.beg[0]); x_nt1 = Div32(g.nt[1]); }
+    if (g.dims > 1) { y_nx0 = Div32(g.nx[0]); y_ng2 = Div32(2u * g.beg[1]); }
+    if (g.dims > 2) { z_nx0 = Div32(g.nx[0]); z_nx1 = Div32(g.nx[1]); }
+  }
+  __host__ __device__ long long count() const { return n0 + n1 + n2; }
+  // false: q is past the last ghost zone
+  __device__ bool coords(const Geom& g, long long q, int& i, int& j, int& k) const {
+    int a, b, c;
+    const Div32 *da, *db;
+    int slab;
+    if (q < n0) { slab = 0; da = &x_ng2; db = &x_nt1; }
+    else if (q < n0 + n1) { q -= n0; slab = 1; da = &y_nx0; db = &y_ng2; }
+    else if (q < count()) { q -= n0 + n1; slab = 2; da = &z_nx0; db = &z_nx1; }
+    else return false;
+    if (!wide) {
+      const unsigned u = (unsigned)q, r = da->div(u), p = db->div(r);
+      a = (int)(u - r * da->d);
+      b = (int)(r - p * db->d);
+      c = (int)p;
+    } else {
+      a = (int)(q % da->d);
+      const long long r = q / da->d;
+      b = (int)(r % db->d);
+      c = (int)(r / db->d);
+    }
+    if (slab == 0) {  // a: ghost column, b = j, c = k
+      const int gx = g.beg[0];
+      i = a < gx ? a : g.end[0] + 1 + (a - gx);
+      j = b;
+      k = c;
+    } else if (slab == 1) {  // a: interior i, b: ghost row, c = k
+      const int gy = g.beg[1];
+      i = g.beg[0] + a;
+      j = b < gy ? b : g.end[1] + 1 + (b - gy);
+      k = c;
+    } else {  // a, b: interior i, j, c: ghost plane
+      const int gz = g.beg[2];
+      i = g.beg[0] + a;
+      j = g.beg[1] + b;
+      k = c < gz ? c : g.end[2] + 1 + (c - gz);
+    }
+    return true;
+  }
+};
+
+// Thread index -> ghost zone of axis AX's layers over the full extent of the
+// other axes B1 (faster) and B2: l in [0, 2 beg[AX]) (lower layers first),
+// then c1 = the B1 index, c2 = the B2 index.
+struct AxisGhosts {
+  long long n = 0;  // 2 beg[AX] nt[B1] nt[B2]
+  Div32 ng2, nt1;
+  bool wide = false;
+  __host__ AxisGhosts(const Geom& g, int ax) {
+    const int b1 = ax == 0 ? 1 : 0, b2 = ax == 2 ? 1 : 2;
+    n = 2LL * g.beg[ax] * g.nt[b1] * g.nt[b2];
+    wide = 2 * n >= (1LL << 32);  // k_fill_normal indexes 2 nt[B1] nt[B2] threads
+    ng2 = Div32(2u * (g.beg[ax] > 0 ? g.beg[ax] : 1));
+    nt1 = Div32(g.nt[b1]);
+  }
+  __device__ void coords(long long q, int& l, int& c1, int& c2) const {
+    if (!wide) {
+      const unsigned u = (unsigned)q, t = ng2.div(u), p = nt1.div(t);
+      l = (int)(u - t * ng2.d);
+      c1 = (int)(t - p * nt1.d);
+      c2 = (int)p;
+    } else {
+      l = (int)(q % ng2.d);
+      const long long t = q / ng2.d;
+      c1 = (int)(t % nt1.d);
+      c2 = (int)(t / nt1.d);
+    }
+  }
+  // the transverse zone t in [0, nt[B1] nt[B2])
+  __device__ void transverse(long long t, int& c1, int& c2) const {
+    if (!wide) {
+      const unsigned u = (unsigned)t, p = nt1.div(u);
+      c1 = (int)(u - p * nt1.d);
+      c2 = (int)p;
+    } else {
+      c1 = (int)(t % nt1.d);
+      c2 = (int)(t / nt1.d);
+    }
+  }
+};
+
 // Device scalars of one solver (one allocation).
 struct DevScalars {
   double dt;             // time step used by the kernels of the current step

@@ -157,36 +157,10 @@ struct BoundArrays {
   int n, ncomp;
 };
 
-__global__ void k_mbound(Geom g, BoundArrays arr, int bcx, int bcy, int bcz, long long n0, long long n1,
-                         long long n2) {
+__global__ void k_mbound(Geom g, BoundArrays arr, int bcx, int bcy, int bcz, GhostSlabs gs) {
   long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   int i, j, k;
-  int gx = g.beg[0], gy = g.beg[1], gz = g.beg[2];
-  if (q < n0) {
-    int ng2 = 2 * gx;
-    int ii = (int)(q % ng2);
-    long long r = q / ng2;
-    j = (int)(r % g.nt[1]);
-    k = (int)(r / g.nt[1]);
-    i = ii < gx ? ii : g.end[0] + 1 + (ii - gx);
-  } else if (q < n0 + n1) {
-    q -= n0;
-    int ng2 = 2 * gy;
-    i = g.beg[0] + (int)(q % g.nx[0]);
-    long long r = q / g.nx[0];
-    int jj = (int)(r % ng2);
-    k = (int)(r / ng2);
-    j = jj < gy ? jj : g.end[1] + 1 + (jj - gy);
-  } else if (q < n0 + n1 + n2) {
-    q -= n0 + n1;
-    i = g.beg[0] + (int)(q % g.nx[0]);
-    long long r = q / g.nx[0];
-    j = g.beg[1] + (int)(r % g.nx[1]);
-    int kk = (int)(r / g.nx[1]);
-    k = kk < gz ? kk : g.end[2] + 1 + (kk - gz);
-  } else {
-    return;
-  }
+  if (!gs.coords(g, q, i, j, k)) return;
   int si = mbmap(i, g.beg[0], g.end[0], g.nx[0], bcx);
   int sj = g.dims > 1 ? mbmap(j, g.beg[1], g.end[1], g.nx[1], bcy) : j;
   int sk = g.dims > 2 ? mbmap(k, g.beg[2], g.end[2], g.nx[2], bcz) : k;
@@ -1515,11 +1489,9 @@ static void mlaunch_bound(Solver* S, const MixArgs& a) {
   arr.ncomp = S->cfg.components;
   for (int nv = 0; nv < NV; nv++) arr.q[arr.n++] = (float*)a.Vin[nv];
   for (int d = 0; d < a.nbfield; d++) arr.q[arr.n++] = (float*)a.Bin[d];
-  long long n0 = 2LL * g.beg[0] * g.nt[1] * g.nt[2];
-  long long n1 = g.dims > 1 ? 2LL * g.beg[1] * g.nx[0] * g.nt[2] : 0;
-  long long n2 = g.dims > 2 ? 2LL * g.beg[2] * g.nx[0] * g.nx[1] : 0;
-  PG_LAUNCH(S, "mixed_bound", (k_mbound<<<grid_for(n0 + n1 + n2), kThreads, 0, S->stream>>>(
-                                    g, arr, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], n0, n1, n2)));
+  const GhostSlabs gs(g);
+  PG_LAUNCH(S, "mixed_bound", (k_mbound<<<grid_for(gs.count()), kThreads, 0, S->stream>>>(
+                                    g, arr, S->cfg.bc[0], S->cfg.bc[1], S->cfg.bc[2], gs)));
   S->ud_stage++;
 }
 
