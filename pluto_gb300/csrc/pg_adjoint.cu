@@ -760,11 +760,21 @@ static int adjoint_alloc(Solver* S, AdjBufs** out) {
   size_t count = 0;
   for (size_t q = 0; q < np; q++) count += used[q];
   const size_t bytes = sizeof(double) * (size_t)n * count;
+  // on failure nothing stays behind: the next call allocates again instead
+  // of handing out null arrays
+  auto drop = [&](int rc) {
+    if (A->block) cudaFree(A->block);
+    delete A;
+    S->adj = nullptr;
+    *out = nullptr;
+    return rc;
+  };
   if (cudaMalloc(&A->block, bytes) != cudaSuccess) {
     A->block = nullptr;
-    return PG_ERR_NOMEM;
+    cudaGetLastError();
+    return drop(PG_ERR_NOMEM);
   }
-  if (cudaMemset(A->block, 0, bytes) != cudaSuccess) return PG_ERR_CUDA;
+  if (cudaMemset(A->block, 0, bytes) != cudaSuccess) return drop(PG_ERR_CUDA);
   size_t k = 0;
   for (size_t q = 0; q < np; q++)
     if (used[q]) p[q] = A->block + (k++) * n;
@@ -779,7 +789,8 @@ static void zero_arrays(std::initializer_list<double* const*> groups, const int*
   std::vector<double*> p;
   int g = 0;
   for (double* const* grp : groups) {
-    for (int i = 0; i < counts[g]; i++) p.push_back(grp[i]);
+    for (int i = 0; i < counts[g]; i++)
+      if (grp[i]) p.push_back(grp[i]);  // arrays a scheme does not use are not allocated
     g++;
   }
   size_t i = 0;

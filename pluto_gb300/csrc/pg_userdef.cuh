@@ -116,7 +116,7 @@ inline void CUDART_CB ud_host_call(void* p) {
 }
 
 // zone flags: host array in PLUTO's layout, device array with the row pitch
-__global__ inline void k_flag_xfer(unsigned char* host, unsigned char* dev, Geom g, int to_dev) {
+static __global__ void k_flag_xfer(unsigned char* host, unsigned char* dev, Geom g, int to_dev) {
   const long long q = blockIdx.x * (long long)blockDim.x + threadIdx.x;
   if (q >= (long long)g.nt[0] * g.nt[1] * g.nt[2]) return;
   const int i = (int)(q % g.nt[0]);
