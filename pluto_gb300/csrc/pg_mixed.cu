@@ -1055,9 +1055,7 @@ __global__ void k_mfinal(MixArgs a, Box dom, int reduce_cdt) {
       u.E = O::add(O::mulf(inv_gmm1, (float)a.small_p), O::mulf(kin2, 0.5f));
       fl = FLAG_CONS2PRIM_FAIL;
     }
-    // the cancellation E - kin2/2 in A; the (g-1) scaling, which cancels
-    // nothing, after narrowing (one FP32 rounding more, no FP64 operation)
-    float p = O::tof(O::sub_half(u.E, kin2)) * (a.gamma - 1.0f);
+    float p = O::tof(O::mulf(O::sub_half(u.E, kin2), a.gamma - 1.0f));
     if (p < 0.f) {  // floor and recompute the energy (Src/MHD/mappers.c:190-200)
       p = (float)a.small_p;
       u.E = O::add(O::mulf(inv_gmm1, (float)a.small_p), O::mulf(kin2, 0.5f));
