@@ -123,10 +123,14 @@ __global__ void k_bound(F64A<T> a, int bcx, int bcy, int bcz, GhostSlabs gs) {
   const int bt[3] = {bcx, bcy, bcz};
   const int x[3] = {i, j, k};
   int flips = 0;  // bit nv set: variable nv changes sign
-  for (int d = 0; d < g.dims; d++)
+#pragma unroll
+  for (int d = 0; d < 3; d++) {  // compile-time axis indices keep x, bt in registers
+    if (d >= g.dims) break;
     if (x[d] < g.beg[d] || x[d] > g.end[d])
+#pragma unroll
       for (int nv = 0; nv < NV; nv++)
         if (bc_flip(d, bc_side(bt[d], x[d] > g.end[d]), nv, a.ncomp) < 0) flips ^= 1 << nv;
+  }
 #pragma unroll
   for (int nv = 0; nv < NV; nv++) {
     const T v = a.V[nv][src];

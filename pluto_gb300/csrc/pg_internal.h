@@ -119,22 +119,25 @@ struct GhostSlabs {
   // false: q is past the last ghost zone
   __device__ bool coords(const Geom& g, long long q, int& i, int& j, int& k) const {
     int a, b, c;
-    const Div32 *da, *db;
     int slab;
-    if (q < n0) { slab = 0; da = &x_ng2; db = &x_nt1; }
-    else if (q < n0 + n1) { q -= n0; slab = 1; da = &y_nx0; db = &y_ng2; }
-    else if (q < count()) { q -= n0 + n1; slab = 2; da = &z_nx0; db = &z_nx1; }
+    if (q < n0) slab = 0;
+    else if (q < n0 + n1) { q -= n0; slab = 1; }
+    else if (q < count()) { q -= n0 + n1; slab = 2; }
     else return false;
+    // divisors selected by value (a pointer to a parameter would force a
+    // local copy of the struct)
+    const Div32 da = slab == 0 ? x_ng2 : (slab == 1 ? y_nx0 : z_nx0);
+    const Div32 db = slab == 0 ? x_nt1 : (slab == 1 ? y_ng2 : z_nx1);
     if (!wide) {
-      const unsigned u = (unsigned)q, r = da->div(u), p = db->div(r);
-      a = (int)(u - r * da->d);
-      b = (int)(r - p * db->d);
+      const unsigned u = (unsigned)q, r = da.div(u), p = db.div(r);
+      a = (int)(u - r * da.d);
+      b = (int)(r - p * db.d);
       c = (int)p;
     } else {
-      a = (int)(q % da->d);
-      const long long r = q / da->d;
-      b = (int)(r % db->d);
-      c = (int)(r / db->d);
+      a = (int)(q % da.d);
+      const long long r = q / da.d;
+      b = (int)(r % db.d);
+      c = (int)(r / db.d);
     }
     if (slab == 0) {  // a: ghost column, b = j, c = k
       const int gx = g.beg[0];

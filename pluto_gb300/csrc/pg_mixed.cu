@@ -169,11 +169,17 @@ __global__ void k_mbound(Geom g, BoundArrays arr, int bcx, int bcy, int bcz, Gho
   const int bt[3] = {bcx, bcy, bcz};
   const int x[3] = {i, j, k};
   int flips = 0;
-  for (int d = 0; d < g.dims; d++)
+#pragma unroll
+  for (int d = 0; d < 3; d++) {  // compile-time axis indices keep x, bt in registers
+    if (d >= g.dims) break;
     if (x[d] < g.beg[d] || x[d] > g.end[d])
+#pragma unroll
       for (int nv = 0; nv < NV; nv++)
         if (bc_flip(d, bc_side(bt[d], x[d] > g.end[d]), nv, arr.ncomp) < 0) flips ^= 1 << nv;
-  for (int a = 0; a < arr.n; a++) {
+  }
+#pragma unroll
+  for (int a = 0; a < 11; a++) {  // compile-time indices: the pointer table stays a parameter
+    if (a >= arr.n) break;
     const float v = arr.q[a][src];
     arr.q[a][dst] = (a < NV && ((flips >> a) & 1)) ? -v : v;
   }
