@@ -80,7 +80,9 @@ __global__ void k_bound_axis(BoundCT<T> a, int type, AxisGhosts ag) {
     const T v = a.V[nv][src];
     a.V[nv][dst] = bc_flip(AX, side, nv, a.ncomp) < 0 ? -v : v;
   }
-  for (int fd = 0; fd < a.nbfield; fd++) {
+#pragma unroll
+  for (int fd = 0; fd < 3; fd++) {  // compile-time fd keeps c, s, cm, sm in registers
+    if (fd >= a.nbfield) break;
     if (fd != AX) {
       const bool neg = bc_flip(AX, side, BX1 + fd, a.ncomp) < 0;
       const T v = a.Bs[fd][src];
