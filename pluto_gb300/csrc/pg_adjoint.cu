@@ -157,27 +157,6 @@ struct AdjBufs {
   double* sDV[3][3][3];
 };
 
-// linear zone index -> (i, j, k) with the row and plane divisors prepared on
-// the host (32-bit divisions while the arrays have fewer than 2^32 zones)
-struct CellMap {
-  Div32 nt0, nt1;
-  bool wide = false;
-  CellMap() = default;
-  __host__ explicit CellMap(const Geom& g) : nt0(g.nt[0]), nt1(g.nt[1]), wide(g.ncell >= (1LL << 32)) {}
-  __device__ void ijk(long long c, int& i, int& j, int& k) const {
-    if (!wide) {
-      const unsigned u = (unsigned)c, r = nt0.div(u), p = nt1.div(r);
-      i = (int)(u - r * nt0.d);
-      j = (int)(r - p * nt1.d);
-      k = (int)p;
-    } else {
-      i = (int)(c % nt0.d);
-      j = (int)((c / nt0.d) % nt1.d);
-      k = (int)(c / ((long long)nt0.d * nt1.d));
-    }
-  }
-};
-
 struct AdjArgs {
   F64A<double> f;  // forward arrays (the solver's own)
   AdjBufs b;

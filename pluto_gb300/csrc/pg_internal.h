@@ -66,11 +66,15 @@ struct Box {
     }
     return *this;
   }
-  __device__ static unsigned fdiv(unsigned n, unsigned m, unsigned s1, unsigned s2) {
+  __host__ __device__ static unsigned fdiv(unsigned n, unsigned m, unsigned s1, unsigned s2) {
+#ifdef __CUDA_ARCH__
     const unsigned t = __umulhi(n, m);
+#else  // the same on the host (tests/index_decode_check.cu)
+    const unsigned t = (unsigned)(((unsigned long long)n * m) >> 32);
+#endif
     return (t + ((n - t) >> s1)) >> s2;
   }
-  __device__ void coords(long long q, int& i, int& j, int& k) const {
+  __host__ __device__ void coords(long long q, int& i, int& j, int& k) const {
     int ni = hi[0] - lo[0] + 1, nj = hi[1] - lo[1] + 1;
     if (mi) {  // prepared: 32-bit multiply-and-shift division
       const unsigned u = (unsigned)q;
@@ -95,7 +99,7 @@ struct Div32 {
   unsigned char s1 = 0, s2 = 0;
   Div32() = default;
   __host__ explicit Div32(unsigned dd) : d(dd) { Box::magic(dd, m, s1, s2); }
-  __device__ unsigned div(unsigned n) const { return Box::fdiv(n, m, s1, s2); }
+  __host__ __device__ unsigned div(unsigned n) const { return Box::fdiv(n, m, s1, s2); }
 };
 
 // Thread index -> ghost zone of the single-pass boundary fill: first the x
@@ -117,7 +121,7 @@ struct GhostSlabs {
   }
   __host__ __device__ long long count() const { return n0 + n1 + n2; }
   // false: q is past the last ghost zone
-  __device__ bool coords(const Geom& g, long long q, int& i, int& j, int& k) const {
+  __host__ __device__ bool coords(const Geom& g, long long q, int& i, int& j, int& k) const {
     int a, b, c;
     int slab;
     if (q < n0) slab = 0;
@@ -173,7 +177,7 @@ struct AxisGhosts {
     ng2 = Div32(2u * (g.beg[ax] > 0 ? g.beg[ax] : 1));
     nt1 = Div32(g.nt[b1]);
   }
-  __device__ void coords(long long q, int& l, int& c1, int& c2) const {
+  __host__ __device__ void coords(long long q, int& l, int& c1, int& c2) const {
     if (!wide) {
       const unsigned u = (unsigned)q, t = ng2.div(u), p = nt1.div(t);
       l = (int)(u - t * ng2.d);
@@ -187,7 +191,7 @@ struct AxisGhosts {
     }
   }
   // the transverse zone t in [0, nt[B1] nt[B2])
-  __device__ void transverse(long long t, int& c1, int& c2) const {
+  __host__ __device__ void transverse(long long t, int& c1, int& c2) const {
     if (!wide) {
       const unsigned u = (unsigned)t, p = nt1.div(u);
       c1 = (int)(u - p * nt1.d);
@@ -195,6 +199,28 @@ struct AxisGhosts {
     } else {
       c1 = (int)(t % nt1.d);
       c2 = (int)(t / nt1.d);
+    }
+  }
+};
+
+// linear zone index -> (i, j, k) of arrays whose row pitch is nt0 (the FP64
+// paths), with the row and plane divisors prepared on the host (32-bit
+// divisions while the arrays have fewer than 2^32 zones)
+struct CellMap {
+  Div32 nt0, nt1;
+  bool wide = false;
+  CellMap() = default;
+  __host__ explicit CellMap(const Geom& g) : nt0(g.nt[0]), nt1(g.nt[1]), wide(g.ncell >= (1LL << 32)) {}
+  __host__ __device__ void ijk(long long c, int& i, int& j, int& k) const {
+    if (!wide) {
+      const unsigned u = (unsigned)c, r = nt0.div(u), p = nt1.div(r);
+      i = (int)(u - r * nt0.d);
+      j = (int)(r - p * nt1.d);
+      k = (int)p;
+    } else {
+      i = (int)(c % nt0.d);
+      j = (int)((c / nt0.d) % nt1.d);
+      k = (int)(c / ((long long)nt0.d * nt1.d));
     }
   }
 };
