@@ -537,6 +537,18 @@ def profile_case(args):
     kernel is a separate launch a profiler can select with -k/-s/-c.  Prints
     one line; no timing is taken."""
     from pluto_gb300 import Solver, problems
+    if args.profile_case == "adjoint":  # the adjoint leg's workload at --n^2, --steps steps
+        from pluto_gb300.adjoint import Rollout, cfl_dt_sequence
+        spec, vc, f = problems.cp_alfven(args.n)
+        f = [f[0], f[1], None]
+        dts = cfl_dt_sequence(spec, vc, f, args.steps, spec["first_dt"], spec["cfl"])
+        r = Rollout(spec, dts, every=16)
+        r.run(vc, f, checkpoint=True)
+        lam = np.zeros_like(vc)
+        lam[0] = np.random.default_rng(0).normal(size=vc[0].shape)
+        r.gradient(lam, [np.zeros_like(f[0]), np.zeros_like(f[1]), None])
+        print(json.dumps({"profile_case": "adjoint", "n": args.n, "steps": args.steps}), flush=True)
+        return
     if args.profile_case == "blast":
         spec, vc, faces = problems.blast3d(args.n)
     elif args.profile_case == "turb":
@@ -584,8 +596,9 @@ def main():
     ap.add_argument("--turb-n", type=int, default=768)
     ap.add_argument("--turb-l1-n", type=int, default=256)
     ap.add_argument("--turb-l1-steps", type=int, default=50)
-    ap.add_argument("--profile-case", choices=["blast", "turb", "ot"],
-                    help="run --steps eager steps of one problem at --n (for ncu to attach to) and exit")
+    ap.add_argument("--profile-case", choices=["blast", "turb", "ot", "adjoint"],
+                    help="run --steps eager steps of one problem at --n (for ncu to attach to) and exit; "
+                         "adjoint: the CP-Alfven --n^2 forward with checkpoints and one gradient")
     ap.add_argument("--precision", default="mixed", choices=["mixed", "mixed_dw", "fp64"],
                     help="precision of --profile-case")
     args = ap.parse_args()
