@@ -205,6 +205,23 @@ int pg_adjoint_set(pg_solver *s, const double *const vars[8], const double *cons
 int pg_adjoint_step(pg_solver *s, double dt);
 int pg_adjoint_get(pg_solver *s, double *const vars[8], double *const faces[3], int layout);
 
+/* The same step split in two, for reversing a run of steps without
+   recomputing each one twice: pg_adjoint_slots(n) (after pg_adjoint_set)
+   allocates n slots, each holding what one step's forward recomputation
+   saves (its start state, stage inputs and results, reconstructed states,
+   wave speeds and slopes); PG_ERR_NOMEM, with nothing allocated, when they
+   would take more than half of the free device memory; n = 0 frees them.
+   pg_adjoint_forward(dt, slot) takes a step of length dt from the solver's
+   state, saving into slot, and leaves the solver at the step's end;
+   pg_adjoint_reverse(dt, slot) does what pg_adjoint_step does for the step
+   saved in slot (the same kernels; like any two runs of the reversal, whose
+   scatter adds are FP64 atomics, equal to round-off) and leaves the solver
+   at that step's start.  Forward steps q0..q1-1 into slots 0..q1-q0-1, then
+   reverse them in the opposite order. */
+int pg_adjoint_slots(pg_solver *s, int nslots);
+int pg_adjoint_forward(pg_solver *s, double dt, int slot);
+int pg_adjoint_reverse(pg_solver *s, double dt, int slot);
+
 /* Device-resident state checkpoints (PG_FP64 / PG_FP64_TANGENT): copy the
    whole state into slot (0..PG_MAX_CHECKPOINTS-1, allocated on first use)
    or back. */

@@ -36,8 +36,8 @@ EXPORTS = ["pg_create", "pg_destroy", "pg_upload", "pg_download", "pg_advance", 
            "pg_tube_step_static", "pg_batch_create", "pg_batch_destroy", "pg_batch_upload",
            "pg_batch_download", "pg_batch_run", "pg_batch_get", "pg_batch_autotune",
            "pg_batch_set_schedule", "pg_tangent_upload", "pg_tangent_download", "pg_tangent_kink", "pg_adjoint_set",
-           "pg_adjoint_step", "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load",
-           "pg_selftest_conversions", "pg_set_userdef", "pg_set_internal_boundary",
+           "pg_adjoint_step", "pg_adjoint_get", "pg_adjoint_slots", "pg_adjoint_forward",
+           "pg_adjoint_reverse", "pg_checkpoint_save", "pg_checkpoint_load", "pg_selftest_conversions", "pg_set_userdef", "pg_set_internal_boundary",
            "pg_write_output", "pg_output_wait", "pg_read_output", "pg_download_async", "pg_download_wait"]
 PG_ABI_VERSION = 3  # the pg_config layout these bindings describe
 # pg_userdef_fn: (user, side 0..5, vpos 0 cells / 1..3 faces, stage)
@@ -126,6 +126,9 @@ def lib():
     for fn in ("pg_tangent_upload", "pg_tangent_download", "pg_adjoint_set", "pg_adjoint_get"):
         getattr(L, fn).argtypes = [vp, C.POINTER(dp), C.POINTER(dp), ip]
     L.pg_adjoint_step.argtypes = [vp, C.c_double]
+    L.pg_adjoint_slots.argtypes = [vp, ip]
+    L.pg_adjoint_forward.argtypes = [vp, C.c_double, ip]
+    L.pg_adjoint_reverse.argtypes = [vp, C.c_double, ip]
     L.pg_tangent_kink.argtypes = [vp, ip, dp]
     L.pg_checkpoint_save.argtypes = [vp, ip]
     L.pg_checkpoint_load.argtypes = [vp, ip]
@@ -144,7 +147,8 @@ def lib():
                "pg_batch_create", "pg_batch_destroy", "pg_batch_upload", "pg_batch_download",
                "pg_batch_run", "pg_batch_get", "pg_batch_autotune", "pg_batch_set_schedule",
                "pg_tangent_upload", "pg_tangent_download", "pg_tangent_kink", "pg_adjoint_set", "pg_adjoint_step",
-               "pg_adjoint_get", "pg_checkpoint_save", "pg_checkpoint_load", "pg_selftest_conversions",
+               "pg_adjoint_get", "pg_adjoint_slots", "pg_adjoint_forward", "pg_adjoint_reverse",
+               "pg_checkpoint_save", "pg_checkpoint_load", "pg_selftest_conversions",
                "pg_set_userdef", "pg_set_internal_boundary", "pg_write_output", "pg_output_wait",
                "pg_read_output", "pg_download_async", "pg_download_wait"):
         getattr(L, fn).restype = C.c_int

@@ -56,16 +56,31 @@ class Rollout:
             s.advance(dt)
         return s.download()
 
-    def gradient(self, lvc, lfaces):
-        """Adjoint of the whole rollout (after ``run(..., checkpoint=True)``)."""
+    def gradient(self, lvc, lfaces, slots: bool = True):
+        """Adjoint of the whole rollout (after ``run(..., checkpoint=True)``).
+
+        Per segment, from its checkpoint: with ``slots`` (and room on the
+        device for one segment's steps) each step is recomputed once,
+        saving its stage outputs (adjoint_forward), and the steps are then
+        reversed from them (adjoint_reverse); otherwise the step states are
+        rebuilt first and every adjoint_step recomputes its own step again.
+        Both give the same gradient to round-off (the reversal's scatter adds
+        are FP64 atomics, so no two runs agree to the last bit)."""
         s = self.solver
         s.adjoint_set(lvc, self.face_list(lfaces))
         n, e = self.nsteps, self.every
         nseg = -(-n // e)
-        base = nseg  # slots of the states inside one segment
+        use_slots = slots and s.adjoint_slots(min(n, e))
+        base = nseg  # checkpoint slots of the states inside one segment
         for seg in range(nseg - 1, -1, -1):
             q0, q1 = seg * e, min(n, seg * e + e)
             s.checkpoint_load(seg)
+            if use_slots:
+                for q in range(q0, q1):
+                    s.adjoint_forward(self.dts[q], q - q0)
+                for q in range(q1 - 1, q0 - 1, -1):
+                    s.adjoint_reverse(self.dts[q], q - q0)
+                continue
             for q in range(q0, q1 - 1):  # states q0+1 .. q1-1 from the checkpoint
                 s.checkpoint_save(base + q - q0)
                 s.advance(self.dts[q])
@@ -73,6 +88,8 @@ class Rollout:
             for q in range(q1 - 1, q0 - 1, -1):
                 s.checkpoint_load(base + q - q0)
                 s.adjoint_step(self.dts[q])
+        if use_slots:
+            s.adjoint_slots(0)
         return s.adjoint_get()
 
 

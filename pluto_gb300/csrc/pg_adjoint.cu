@@ -27,6 +27,7 @@
 // (pg_adjoint_pt.cuh), all inputs in one evaluation; the Roe solver
 // evaluates the same templated point function as the forward kernels with
 // Dual<1> inputs, one seeded input at a time.
+#include <cstddef>
 #include <cstring>
 #include <initializer_list>
 #include <string>
@@ -693,7 +694,28 @@ struct Checkpoints {
 struct AdjState {
   AdjBufs b;
   double* block = nullptr;
+  // the block's own pointers of the saved forward states (AdjBufs from Vn
+  // to the end; null where the scheme does not use the array), and the
+  // per-step copies of them allocated by pg_adjoint_slots
+  std::vector<double*> home;
+  std::vector<double*> slots;
 };
+
+// index of AdjBufs::Vn among the struct's pointers: the saved forward
+// states are the members from there to the end
+static size_t saved_first() { return offsetof(AdjBufs, Vn) / sizeof(double*); }
+
+// point the saved-state members of A->b at slot's copies (slot < 0: at the
+// block's own arrays)
+static void bind_slot(AdjState* A, long long n, int slot) {
+  double** p = (double**)&A->b;
+  const size_t f0 = saved_first();
+  size_t k = 0;
+  for (size_t h = 0; h < A->home.size(); h++) {
+    if (!A->home[h]) continue;
+    p[f0 + h] = slot < 0 ? A->home[h] : A->slots[slot] + (k++) * n;
+  }
+}
 
 static int adjoint_alloc(Solver* S, AdjBufs** out) {
   if (S->adj) {
@@ -757,7 +779,13 @@ static int adjoint_alloc(Solver* S, AdjBufs** out) {
   size_t k = 0;
   for (size_t q = 0; q < np; q++)
     if (used[q]) p[q] = A->block + (k++) * n;
+  A->home.assign(p + saved_first(), p + np);
   return PG_OK;
+}
+
+static void free_slots(AdjState* A) {
+  for (double* q : A->slots) cudaFree(q);
+  A->slots.clear();
 }
 
 // Zeroes p[0..count) with one cudaMemsetAsync per run of arrays that lie
@@ -784,6 +812,7 @@ static void zero_arrays(std::initializer_list<double* const*> groups, const int*
 void adjoint_free(Solver* S) {
   if (S->adj) {
     AdjState* A = (AdjState*)S->adj;
+    free_slots(A);
     if (A->block) cudaFree(A->block);
     delete A;
     S->adj = nullptr;
@@ -1121,8 +1150,7 @@ extern "C" int pg_adjoint_set(pg_solver* h, const double* const vars[8], const d
   if (ct && faces)
     for (int d = 0; d < S->g.dims; d++)
       if (faces[d] && (rc = xfer_f64(S, B->lB[d], (double*)faces[d], d, layout, true))) return rc;
-  AdjArgs A;
-  memset(&A, 0, sizeof A);
+  AdjArgs A{};  // zero-initialized
   A.f = make_args<double>(S);
   A.b = *B;
   A.cm = CellMap(S->g);
@@ -1151,19 +1179,29 @@ extern "C" int pg_adjoint_get(pg_solver* h, double* const vars[8], double* const
   return sync_status(S);
 }
 
-extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
-  int rc = check_fp64(h, "pg_adjoint_step", false);
+// The checks every adjoint step entry makes; on success S and B are set.
+static int adj_step_checks(pg_solver* h, const char* name, double dt, Solver** Sout, AdjBufs** Bout) {
+  int rc = check_fp64(h, name, false);
   if (rc) return rc;
   Solver* S = &h->S;
   if (!S->adj) {
-    set_last_error("pg_adjoint_step: call pg_adjoint_set first");
+    set_last_error((std::string(name) + ": call pg_adjoint_set first").c_str());
     return PG_ERR_INVALID;
   }
   if (!(dt > 0)) {
-    set_last_error("pg_adjoint_step: dt must be positive");
+    set_last_error((std::string(name) + ": dt must be positive").c_str());
     return PG_ERR_INVALID;
   }
-  AdjBufs* B = (AdjBufs*)S->adj;
+  *Sout = S;
+  *Bout = (AdjBufs*)S->adj;
+  return PG_OK;
+}
+
+// Forward recomputation of one step from the solver's state: the saved
+// states (start state, stage inputs and results, each stage's reconstructed
+// states, wave speeds and slopes) go to B's saved-state arrays; the solver
+// is left at the step's end.
+static void adj_forward(Solver* S, AdjBufs* B, double dt) {
   const Geom& g = S->g;
   const long long n = g.ncell;
   const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
@@ -1173,7 +1211,6 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
     S->device_dt = false;
     S->graph_dirty = true;
   }
-  // ---- forward recomputation of the step, saving what the reverse needs ----
   S->sc_host->dt = dt;
   cudaMemcpyAsync(&S->sc->dt, &S->sc_host->dt, sizeof(double), cudaMemcpyHostToDevice, st);
   copy_state(B->Vn, S->V, NV, B->Bn, S->Bs, nb, n, st);
@@ -1204,9 +1241,20 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
     if (s < ns) copy_state(B->Vst[s - 1], S->V, NV, B->Bst[s - 1], S->Bs, nb, n, st);
     copy_state(B->Ust[s - 1], S->U, NV, nullptr, nullptr, 0, n, st);
   }
+}
 
-  AdjArgs A;
-  memset(&A, 0, sizeof A);
+// The step reversed from B's saved states: the adjoint on the step's end
+// becomes the adjoint on its start, and the solver is left at the step's
+// start.
+static void adj_reverse(Solver* S, AdjBufs* B, double dt) {
+  const Geom& g = S->g;
+  const long long n = g.ncell;
+  const bool ct = S->cfg.divb == PG_CONSTRAINED_TRANSPORT;
+  const int nb = ct ? g.dims : 0;
+  cudaStream_t st = S->stream;
+  const F64A<double> f = make_args<double>(S);
+  const int ns = S->cfg.time_stepping == PG_RK3 ? 3 : (S->cfg.time_stepping == PG_EULER ? 1 : 2);
+  AdjArgs A{};  // zero-initialized
   A.f = f;
   A.dt = dt;
   A.cm = CellMap(f.g);
@@ -1246,6 +1294,90 @@ extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
   }
   // the solver's state is the step's start again
   copy_state(S->V, B->Vn, NV, S->Bs, B->Bn, nb, n, st);
+}
+
+extern "C" int pg_adjoint_step(pg_solver* h, double dt) {
+  Solver* S;
+  AdjBufs* B;
+  int rc = adj_step_checks(h, "pg_adjoint_step", dt, &S, &B);
+  if (rc) return rc;
+  bind_slot((AdjState*)S->adj, S->g.ncell, -1);
+  adj_forward(S, B, dt);
+  adj_reverse(S, B, dt);
+  return sync_status(S);
+}
+
+extern "C" int pg_adjoint_slots(pg_solver* h, int nslots) {
+  int rc = check_fp64(h, "pg_adjoint_slots", false);
+  if (rc) return rc;
+  Solver* S = &h->S;
+  if (!S->adj) {
+    set_last_error("pg_adjoint_slots: call pg_adjoint_set first");
+    return PG_ERR_INVALID;
+  }
+  if (nslots < 0 || nslots > PG_MAX_CHECKPOINTS) {
+    set_last_error("pg_adjoint_slots: nslots outside 0..PG_MAX_CHECKPOINTS");
+    return PG_ERR_INVALID;
+  }
+  AdjState* A = (AdjState*)S->adj;
+  bind_slot(A, S->g.ncell, -1);
+  if ((int)A->slots.size() == nslots) return PG_OK;
+  free_slots(A);
+  if (nslots == 0) return PG_OK;
+  size_t count = 0;
+  for (double* q : A->home) count += q != nullptr;
+  const size_t bytes = sizeof(double) * (size_t)S->g.ncell * count;
+  size_t free_b = 0, total_b = 0;
+  if (cudaMemGetInfo(&free_b, &total_b) != cudaSuccess || bytes * (size_t)nslots > free_b / 2) {
+    cudaGetLastError();
+    set_last_error("pg_adjoint_slots: the slots would take more than half of the free device memory");
+    return PG_ERR_NOMEM;
+  }
+  for (int k = 0; k < nslots; k++) {
+    double* q = nullptr;
+    if (cudaMalloc(&q, bytes) != cudaSuccess) {
+      cudaGetLastError();
+      free_slots(A);
+      set_last_error("pg_adjoint_slots: allocation failed");
+      return PG_ERR_NOMEM;
+    }
+    A->slots.push_back(q);
+  }
+  return PG_OK;
+}
+
+static int slot_checks(pg_solver* h, const char* name, double dt, int slot, Solver** S, AdjBufs** B) {
+  int rc = adj_step_checks(h, name, dt, S, B);
+  if (rc) return rc;
+  AdjState* A = (AdjState*)(*S)->adj;
+  if (slot < 0 || slot >= (int)A->slots.size()) {
+    set_last_error((std::string(name) + ": slot outside the slots allocated by pg_adjoint_slots").c_str());
+    return PG_ERR_INVALID;
+  }
+  return PG_OK;
+}
+
+extern "C" int pg_adjoint_forward(pg_solver* h, double dt, int slot) {
+  Solver* S;
+  AdjBufs* B;
+  int rc = slot_checks(h, "pg_adjoint_forward", dt, slot, &S, &B);
+  if (rc) return rc;
+  AdjState* A = (AdjState*)S->adj;
+  bind_slot(A, S->g.ncell, slot);
+  adj_forward(S, B, dt);
+  bind_slot(A, S->g.ncell, -1);
+  return sync_status(S);
+}
+
+extern "C" int pg_adjoint_reverse(pg_solver* h, double dt, int slot) {
+  Solver* S;
+  AdjBufs* B;
+  int rc = slot_checks(h, "pg_adjoint_reverse", dt, slot, &S, &B);
+  if (rc) return rc;
+  AdjState* A = (AdjState*)S->adj;
+  bind_slot(A, S->g.ncell, slot);
+  adj_reverse(S, B, dt);
+  bind_slot(A, S->g.ncell, -1);
   return sync_status(S);
 }
 

@@ -305,11 +305,31 @@ class Solver:
         self._put("pg_adjoint_set", lvc, lbs)
 
     def adjoint_step(self, dt: float):
-        """Adjoint through one RK2 step of length dt from the current state."""
+        """Adjoint through one step of length dt from the current state."""
         L.check(L.lib().pg_adjoint_step(self.h, float(dt)), "pg_adjoint_step")
 
     def adjoint_get(self):
         return self._get("pg_adjoint_get")
+
+    def adjoint_slots(self, nslots: int) -> bool:
+        """Allocate nslots per-step slots for adjoint_forward/adjoint_reverse
+        (after adjoint_set); False, with nothing allocated, when they would
+        take more than half of the free device memory."""
+        rc = L.lib().pg_adjoint_slots(self.h, int(nslots))
+        if rc == L.PG_ERR_NOMEM:
+            return False
+        L.check(rc, "pg_adjoint_slots")
+        return True
+
+    def adjoint_forward(self, dt: float, slot: int):
+        """One step of length dt from the current state, saving what its
+        reversal needs into slot; the state advances."""
+        L.check(L.lib().pg_adjoint_forward(self.h, float(dt), int(slot)), "pg_adjoint_forward")
+
+    def adjoint_reverse(self, dt: float, slot: int):
+        """adjoint_step for the step saved in slot (the same kernels); the
+        state goes back to that step's start."""
+        L.check(L.lib().pg_adjoint_reverse(self.h, float(dt), int(slot)), "pg_adjoint_reverse")
 
     def checkpoint_save(self, slot: int):
         L.check(L.lib().pg_checkpoint_save(self.h, int(slot)), "pg_checkpoint_save")
