@@ -207,7 +207,7 @@ int pg_adjoint_get(pg_solver *s, double *const vars[8], double *const faces[3], 
 
 /* The same step split in two, for reversing a run of steps without
    recomputing each one twice: pg_adjoint_slots(n) (after pg_adjoint_set)
-   allocates n slots, each holding what one step's forward recomputation
+   allocates n slots (n in 0..PG_MAX_CHECKPOINTS), each holding what one step's forward recomputation
    saves (its start state, stage inputs and results, reconstructed states,
    wave speeds and slopes); PG_ERR_NOMEM, with nothing allocated, when they
    would take more than half of the free device memory; n = 0 frees them.
